@@ -1,0 +1,762 @@
+// Golden-vector harness for the CPU oracle: drives the reference's own host
+// stepping loop (Stepper<MemSpace::host>, src/celeritas/global/Stepper.cc:125-168)
+// on the synthetic physics file and the geometries that the GB300 path uses,
+// and prints per-step counters and per-volume energy deposition.
+//
+// Problem set-up follows celer-sim's Runner::build_core_params
+// (app/celer-sim/Runner.cc:281-446); the loop follows Transporter::operator()
+// (app/celer-sim/Transporter.cc:84-179).
+//
+// This file is test infrastructure: it links the reference library built by
+// the Makefile beside it and is never part of the shipped GB300 path.
+//
+// Usage:
+//   ref_harness run <physics.txt> <geometry> <primaries.txt> <num_slots>
+//               <seed> [--field Bx By Bz] [--msc] [--steps N] [--trace]
+//   ref_harness geo <physics.txt> <geometry>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "corecel/data/CollectionStateStore.hh"
+#include "corecel/io/Label.hh"
+#include "corecel/io/OutputRegistry.hh"
+#include "corecel/sys/ActionRegistry.hh"
+#include "geocel/GeoParamsOutput.hh"
+#include "orange/OrangeData.hh"
+#include "orange/OrangeInput.hh"
+#include "orange/OrangeParams.hh"
+#include "orange/OrangeTypes.hh"
+#include "orange/orangeinp/CsgObject.hh"
+#include "orange/orangeinp/InputBuilder.hh"
+#include "orange/orangeinp/IntersectRegion.hh"
+#include "orange/orangeinp/Shape.hh"
+#include "orange/orangeinp/Transformed.hh"
+#include "orange/orangeinp/UnitProto.hh"
+#include "orange/transform/VariantTransform.hh"
+#include "celeritas/Quantities.hh"
+#include "celeritas/Units.hh"
+#include "celeritas/em/params/UrbanMscParams.hh"
+#include "celeritas/field/FieldDriverOptions.hh"
+#include "celeritas/field/UniformFieldData.hh"
+#include "celeritas/geo/GeoMaterialParams.hh"
+#include "celeritas/geo/GeoParams.hh"
+#include "celeritas/global/ActionSequence.hh"
+#include "celeritas/global/CoreParams.hh"
+#include "celeritas/global/CoreState.hh"
+#include "celeritas/global/Stepper.hh"
+#include "celeritas/global/alongstep/AlongStepGeneralLinearAction.hh"
+#include "celeritas/global/alongstep/AlongStepUniformMscAction.hh"
+#include "celeritas/io/ImportData.hh"
+#include "celeritas/mat/MaterialParams.hh"
+#include "celeritas/phys/CutoffParams.hh"
+#include "celeritas/phys/ParticleParams.hh"
+#include "celeritas/phys/PhysicsParams.hh"
+#include "celeritas/phys/Primary.hh"
+#include "celeritas/phys/ProcessBuilder.hh"
+#include "celeritas/random/RngParams.hh"
+#include "celeritas/track/SimParams.hh"
+#include "celeritas/track/TrackInitParams.hh"
+#include "celeritas/user/SimpleCalo.hh"
+#include "celeritas/user/StepCollector.hh"
+
+using namespace celeritas;
+
+namespace
+{
+//---------------------------------------------------------------------------//
+// Key/value physics file ("key count v0 v1 ...")
+//---------------------------------------------------------------------------//
+struct KvFile
+{
+    std::map<std::string, std::vector<std::string>> records;
+
+    explicit KvFile(std::string const& path)
+    {
+        std::ifstream in(path);
+        if (!in)
+        {
+            throw std::runtime_error("cannot open " + path);
+        }
+        std::string line;
+        while (std::getline(in, line))
+        {
+            std::istringstream ss(line);
+            std::string key;
+            std::size_t n = 0;
+            if (!(ss >> key >> n))
+                continue;
+            std::vector<std::string> vals(n);
+            for (auto& v : vals)
+                ss >> v;
+            records[key] = std::move(vals);
+        }
+    }
+    bool has(std::string const& k) const { return records.count(k) > 0; }
+    std::vector<std::string> const& get(std::string const& k) const
+    {
+        auto it = records.find(k);
+        if (it == records.end())
+            throw std::runtime_error("missing key " + k);
+        return it->second;
+    }
+    std::vector<double> dbl(std::string const& k) const
+    {
+        std::vector<double> r;
+        for (auto const& s : get(k))
+            r.push_back(std::strtod(s.c_str(), nullptr));
+        return r;
+    }
+    double d(std::string const& k) const { return dbl(k).at(0); }
+    long i(std::string const& k) const { return std::stol(get(k).at(0)); }
+    std::string s(std::string const& k) const { return get(k).at(0); }
+};
+
+ImportPhysicsVector log_vector(KvFile const& kv, std::string const& key)
+{
+    ImportPhysicsVector v;
+    v.vector_type = ImportPhysicsVectorType::log;
+    v.x = kv.dbl(key + ".x");
+    v.y = kv.dbl(key + ".y");
+    return v;
+}
+
+//---------------------------------------------------------------------------//
+// Synthetic physics file -> ImportData
+//---------------------------------------------------------------------------//
+ImportData load_import(KvFile const& kv, bool with_msc)
+{
+    ImportData data;
+    data.units = "cgs";
+
+    long nel = kv.i("elements");
+    for (long i = 0; i < nel; ++i)
+    {
+        ImportElement el;
+        auto p = "element." + std::to_string(i);
+        el.name = kv.s(p + ".name");
+        el.atomic_number = kv.i(p + ".z");
+        el.atomic_mass = kv.d(p + ".a");
+        data.elements.push_back(el);
+    }
+    long nmat = kv.i("materials");
+    for (long i = 0; i < nmat; ++i)
+    {
+        auto p = "material." + std::to_string(i);
+        ImportGeoMaterial gm;
+        gm.name = kv.s(p + ".name");
+        auto st = kv.s(p + ".state");
+        gm.state = st == "solid"    ? ImportMaterialState::solid
+                   : st == "liquid" ? ImportMaterialState::liquid
+                                    : ImportMaterialState::gas;
+        gm.temperature = kv.d(p + ".temperature");
+        gm.number_density = kv.d(p + ".number_density");
+        auto els = kv.dbl(p + ".elements");
+        auto fr = kv.dbl(p + ".fractions");
+        for (std::size_t j = 0; j < els.size(); ++j)
+        {
+            gm.elements.push_back(
+                {static_cast<unsigned int>(els[j]), fr[j]});
+        }
+        data.geo_materials.push_back(gm);
+
+        ImportPhysMaterial pm;
+        pm.geo_material_id = i;
+        for (int pdg : {11, -11, 22})
+        {
+            auto c = kv.dbl(p + ".cut." + std::to_string(pdg));
+            pm.pdg_cutoffs[pdg] = ImportProductionCut{c[0], c[1]};
+        }
+        data.phys_materials.push_back(pm);
+    }
+
+    long npar = kv.i("particles");
+    for (long i = 0; i < npar; ++i)
+    {
+        auto const& v = kv.get("particle." + std::to_string(i));
+        ImportParticle ip;
+        ip.name = v[0];
+        ip.pdg = std::stoi(v[1]);
+        ip.mass = std::strtod(v[2].c_str(), nullptr);
+        ip.charge = std::strtod(v[3].c_str(), nullptr);
+        ip.spin = std::strtod(v[4].c_str(), nullptr);
+        ip.lifetime = -1;
+        ip.is_stable = true;
+        data.particles.push_back(ip);
+    }
+
+    auto make_table = [&](std::string const& prefix, ImportTableType tt) {
+        ImportPhysicsTable t;
+        t.table_type = tt;
+        t.x_units = ImportUnits::mev;
+        t.y_units = tt == ImportTableType::dedx    ? ImportUnits::mev_per_len
+                    : tt == ImportTableType::range ? ImportUnits::len
+                                                   : tt == ImportTableType::msc_xs ? ImportUnits::mev_sq_per_len : ImportUnits::len_inv;
+        for (long m = 0; m < nmat; ++m)
+        {
+            t.physics_vectors.push_back(
+                log_vector(kv, prefix + "." + std::to_string(m)));
+        }
+        return t;
+    };
+    auto make_model = [&](std::string const& prefix, ImportModelClass imc) {
+        ImportModel model;
+        model.model_class = imc;
+        for (long m = 0; m < nmat; ++m)
+        {
+            auto p = prefix + "." + std::to_string(m);
+            ImportModelMaterial imm;
+            if (kv.has(p + ".energy"))
+            {
+                imm.energy = kv.dbl(p + ".energy");
+                auto nel_mat
+                    = kv.dbl("material." + std::to_string(m) + ".elements")
+                          .size();
+                for (std::size_t e = 0; e < nel_mat; ++e)
+                {
+                    imm.micro_xs.push_back(
+                        kv.dbl(p + ".micro." + std::to_string(e)));
+                }
+            }
+            model.materials.push_back(imm);
+        }
+        return model;
+    };
+    auto empty_model = [&](ImportModelClass imc) {
+        ImportModel model;
+        model.model_class = imc;
+        model.materials.resize(nmat);
+        return model;
+    };
+
+    // Gamma processes
+    {
+        ImportProcess p;
+        p.particle_pdg = 22;
+        p.secondary_pdg = 11;
+        p.process_type = ImportProcessType::electromagnetic;
+        p.process_class = ImportProcessClass::compton;
+        p.models.push_back(empty_model(ImportModelClass::klein_nishina));
+        p.tables.push_back(
+            make_table("table.22.compton.lambda", ImportTableType::lambda));
+        data.processes.push_back(p);
+    }
+    {
+        ImportProcess p;
+        p.particle_pdg = 22;
+        p.secondary_pdg = 11;
+        p.process_type = ImportProcessType::electromagnetic;
+        p.process_class = ImportProcessClass::photoelectric;
+        p.models.push_back(
+            empty_model(ImportModelClass::livermore_photoelectric));
+        p.tables.push_back(make_table("table.22.photoelectric.lambda",
+                                      ImportTableType::lambda));
+        data.processes.push_back(p);
+    }
+    {
+        ImportProcess p;
+        p.particle_pdg = 22;
+        p.secondary_pdg = 11;
+        p.process_type = ImportProcessType::electromagnetic;
+        p.process_class = ImportProcessClass::conversion;
+        p.models.push_back(make_model("model.22.conversion.bethe_heitler",
+                                      ImportModelClass::bethe_heitler_lpm));
+        p.tables.push_back(
+            make_table("table.22.conversion.lambda", ImportTableType::lambda));
+        data.processes.push_back(p);
+    }
+    for (int pdg : {11, -11})
+    {
+        auto spdg = std::to_string(pdg);
+        {
+            ImportProcess p;
+            p.particle_pdg = pdg;
+            p.secondary_pdg = 11;
+            p.process_type = ImportProcessType::electromagnetic;
+            p.process_class = ImportProcessClass::e_ioni;
+            p.models.push_back(empty_model(ImportModelClass::moller_bhabha));
+            p.tables.push_back(make_table("table." + spdg + ".e_ioni.lambda",
+                                          ImportTableType::lambda));
+            p.tables.push_back(make_table("table." + spdg + ".e_ioni.dedx",
+                                          ImportTableType::dedx));
+            p.tables.push_back(make_table("table." + spdg + ".e_ioni.range",
+                                          ImportTableType::range));
+            data.processes.push_back(p);
+        }
+        {
+            ImportProcess p;
+            p.particle_pdg = pdg;
+            p.secondary_pdg = 22;
+            p.process_type = ImportProcessType::electromagnetic;
+            p.process_class = ImportProcessClass::e_brems;
+            p.models.push_back(
+                make_model("model." + spdg + ".e_brems.e_brems_sb",
+                           ImportModelClass::e_brems_sb));
+            p.models.push_back(
+                make_model("model." + spdg + ".e_brems.e_brems_lpm",
+                           ImportModelClass::e_brems_lpm));
+            p.tables.push_back(make_table("table." + spdg + ".e_brems.lambda",
+                                          ImportTableType::lambda));
+            data.processes.push_back(p);
+        }
+        if (pdg == -11)
+        {
+            ImportProcess p;
+            p.particle_pdg = pdg;
+            p.secondary_pdg = 22;
+            p.process_type = ImportProcessType::electromagnetic;
+            p.process_class = ImportProcessClass::annihilation;
+            p.models.push_back(empty_model(ImportModelClass::e_plus_to_gg));
+            data.processes.push_back(p);
+        }
+        if (with_msc)
+        {
+            ImportMscModel msc;
+            msc.particle_pdg = pdg;
+            msc.model_class = ImportModelClass::urban_msc;
+            msc.xs_table = make_table("msc." + spdg, ImportTableType::msc_xs);
+            data.msc_models.push_back(msc);
+        }
+    }
+
+    // Seltzer-Berger and Livermore data for each element
+    for (auto const& el : data.elements)
+    {
+        auto z = std::to_string(el.atomic_number);
+        ImportSBTable sb;
+        sb.x = kv.dbl("sb." + z + ".x");
+        sb.y = kv.dbl("sb." + z + ".y");
+        sb.value = kv.dbl("sb." + z + ".value");
+        data.sb_data[el.atomic_number] = sb;
+
+        ImportLivermorePE pe;
+        auto pz = "livermore." + z;
+        auto th = kv.dbl(pz + ".thresh");
+        pe.thresh_lo = th[0];
+        pe.thresh_hi = th[1];
+        pe.xs_hi.vector_type = ImportPhysicsVectorType::free;
+        pe.xs_hi.x = kv.dbl(pz + ".xs_hi.x");
+        pe.xs_hi.y = kv.dbl(pz + ".xs_hi.y");
+        if (kv.has(pz + ".xs_lo.x"))
+        {
+            pe.xs_lo.vector_type = ImportPhysicsVectorType::free;
+            pe.xs_lo.x = kv.dbl(pz + ".xs_lo.x");
+            pe.xs_lo.y = kv.dbl(pz + ".xs_lo.y");
+        }
+        long nsh = kv.i(pz + ".shells");
+        for (long s = 0; s < nsh; ++s)
+        {
+            auto ps = pz + ".shell." + std::to_string(s);
+            ImportLivermoreSubshell sh;
+            sh.binding_energy = kv.d(ps + ".binding");
+            sh.param_lo = kv.dbl(ps + ".param_lo");
+            sh.param_hi = kv.dbl(ps + ".param_hi");
+            sh.energy = kv.dbl(ps + ".energy");
+            sh.xs = kv.dbl(ps + ".xs");
+            pe.shells.push_back(sh);
+        }
+        data.livermore_pe_data[el.atomic_number] = pe;
+    }
+
+    // Parameters
+    data.em_params.energy_loss_fluct = kv.i("em.energy_loss_fluct");
+    data.em_params.lpm = kv.i("em.lpm");
+    data.em_params.integral_approach = kv.i("em.integral_approach");
+    data.em_params.linear_loss_limit = kv.d("em.linear_loss_limit");
+    data.em_params.lowest_electron_energy = kv.d("em.lowest_electron_energy");
+    data.em_params.msc_range_factor = kv.d("em.msc_range_factor");
+    data.em_params.msc_safety_factor = kv.d("em.msc_safety_factor");
+    data.em_params.msc_lambda_limit = kv.d("em.msc_lambda_limit");
+    {
+        auto lp = kv.dbl("trans.looping");
+        for (std::size_t j = 0; j + 2 < lp.size() + 0; j += 3)
+        {
+            ImportLoopingThreshold lt;
+            lt.threshold_trials = static_cast<int>(lp[j + 1]);
+            lt.important_energy = lp[j + 2];
+            data.trans_params.looping[static_cast<int>(lp[j])] = lt;
+        }
+        data.trans_params.max_substeps = kv.i("trans.max_substeps");
+    }
+    return data;
+}
+
+//---------------------------------------------------------------------------//
+// Geometry: ORANGE through orangeinp
+//---------------------------------------------------------------------------//
+using namespace celeritas::orangeinp;
+
+SPConstObject make_box(std::string label, Real3 const& lo, Real3 const& hi)
+{
+    Real3 half{(hi[0] - lo[0]) / 2, (hi[1] - lo[1]) / 2, (hi[2] - lo[2]) / 2};
+    Real3 center{(hi[0] + lo[0]) / 2, (hi[1] + lo[1]) / 2, (hi[2] + lo[2]) / 2};
+    SPConstObject result
+        = std::make_shared<BoxShape>(std::move(label), Box{half});
+    if (center[0] != 0 || center[1] != 0 || center[2] != 0)
+    {
+        result = std::make_shared<Transformed>(std::move(result),
+                                               Translation{center});
+    }
+    return result;
+}
+
+struct GeoSpec
+{
+    std::shared_ptr<OrangeParams> geo;
+    std::vector<std::string> vol_labels;  // tally volume labels
+    std::map<std::string, MaterialId> label_to_mat;
+};
+
+//! Sampling calorimeter: 50 x (2.3 mm Pb + 5.7 mm lAr), 40x40 cm, along +z,
+//! front face at z = 0, in a vacuum world box of half-width 30 cm in x/y and
+//! spanning z in [-10, 50].
+GeoSpec build_calo()
+{
+    constexpr int num_layers = 50;
+    constexpr double pb = 0.23, lar = 0.57, pitch = pb + lar;
+    constexpr double half_xy = 20.0;
+
+    UnitProto::Input inp;
+    inp.label = "calo";
+    inp.boundary.interior
+        = make_box("world", {-30, -30, -10}, {30, 30, 50});
+    inp.boundary.zorder = ZOrder::exterior;
+    inp.background.fill = GeoMaterialId{0};
+    inp.background.label = Label{"world"};
+
+    GeoSpec spec;
+    spec.label_to_mat["world"] = MaterialId{0};
+    for (int k = 0; k < num_layers; ++k)
+    {
+        double z0 = k * pitch;
+        double z1 = z0 + pb;
+        double z2 = (k + 1) * pitch;
+        auto pbl = "pb_" + std::to_string(k);
+        auto arl = "lar_" + std::to_string(k);
+        inp.materials.push_back({make_box(pbl, {-half_xy, -half_xy, z0},
+                                          {half_xy, half_xy, z1}),
+                                 GeoMaterialId{1},
+                                 Label{pbl}});
+        inp.materials.push_back({make_box(arl, {-half_xy, -half_xy, z1},
+                                          {half_xy, half_xy, z2}),
+                                 GeoMaterialId{2},
+                                 Label{arl}});
+        spec.label_to_mat[pbl] = MaterialId{1};
+        spec.label_to_mat[arl] = MaterialId{2};
+        spec.vol_labels.push_back(pbl);
+        spec.vol_labels.push_back(arl);
+    }
+
+    InputBuilder::Options opts;
+    opts.tol = Tolerance<>::from_default();
+    InputBuilder build(std::move(opts));
+    UnitProto global(std::move(inp));
+    spec.geo = std::make_shared<OrangeParams>(build(global));
+    return spec;
+}
+
+GeoSpec build_geometry(std::string const& name)
+{
+    if (name == "calo")
+        return build_calo();
+    throw std::runtime_error("unknown geometry " + name);
+}
+
+//---------------------------------------------------------------------------//
+// Problem construction (mirrors Runner::build_core_params)
+//---------------------------------------------------------------------------//
+struct Problem
+{
+    std::shared_ptr<CoreParams> core;
+    std::shared_ptr<SimpleCalo> calo;
+    std::shared_ptr<StepCollector> collector;
+    GeoSpec geo;
+};
+
+Problem build_problem(ImportData const& imported,
+                      std::string const& geo_name,
+                      unsigned int seed,
+                      Real3 field,
+                      bool msc)
+{
+    Problem prob;
+    prob.geo = build_geometry(geo_name);
+
+    CoreParams::Input params;
+    params.action_reg = std::make_shared<ActionRegistry>();
+    params.output_reg = std::make_shared<OutputRegistry>();
+    params.geometry = prob.geo.geo;
+    params.material = MaterialParams::from_import(imported);
+    {
+        GeoMaterialParams::Input gm;
+        gm.geometry = params.geometry;
+        gm.materials = params.material;
+        auto const& vols = params.geometry->volumes();
+        for (auto vid : range(VolumeId{vols.size()}))
+        {
+            auto const& lab = vols.at(vid);
+            auto it = prob.geo.label_to_mat.find(lab.name);
+            gm.volume_to_mat.push_back(
+                it == prob.geo.label_to_mat.end() ? MaterialId{} : it->second);
+        }
+        params.geomaterial
+            = std::make_shared<GeoMaterialParams>(std::move(gm));
+    }
+    params.particle = ParticleParams::from_import(imported);
+    params.cutoff = CutoffParams::from_import(
+        imported, params.particle, params.material);
+
+    params.physics = [&] {
+        PhysicsParams::Input input;
+        input.particles = params.particle;
+        input.materials = params.material;
+        input.action_registry = params.action_reg.get();
+        input.options.secondary_stack_factor = 3;
+        input.options.linear_loss_limit = imported.em_params.linear_loss_limit;
+        input.options.lowest_electron_energy = PhysicsParamsOptions::Energy(
+            imported.em_params.lowest_electron_energy);
+        ProcessBuilder::Options opts;
+        opts.brem_combined = false;
+        opts.brems_selection = BremsModelSelection::all;
+        ProcessBuilder build_process(
+            imported, params.particle, params.material, opts);
+        for (auto p :
+             ProcessBuilder::get_all_process_classes(imported.processes))
+        {
+            input.processes.push_back(build_process(p));
+        }
+        return std::make_shared<PhysicsParams>(std::move(input));
+    }();
+
+    bool eloss = imported.em_params.energy_loss_fluct;
+    auto urban = msc ? UrbanMscParams::from_import(
+                           *params.particle, *params.material, imported)
+                     : nullptr;
+    if (field[0] == 0 && field[1] == 0 && field[2] == 0)
+    {
+        auto along_step = AlongStepGeneralLinearAction::from_params(
+            params.action_reg->next_id(),
+            *params.material,
+            *params.particle,
+            urban,
+            eloss);
+        params.action_reg->insert(along_step);
+    }
+    else
+    {
+        UniformFieldParams field_params;
+        field_params.field = field;
+        for (real_type& v : field_params.field)
+        {
+            v = native_value_from(units::FieldTesla{v});
+        }
+        auto along_step = AlongStepUniformMscAction::from_params(
+            params.action_reg->next_id(),
+            *params.material,
+            *params.particle,
+            field_params,
+            urban,
+            eloss);
+        params.action_reg->insert(along_step);
+    }
+    params.rng = std::make_shared<RngParams>(seed);
+    params.sim = SimParams::from_import(
+        imported, params.particle, FieldDriverOptions{}.max_substeps);
+    params.max_streams = 1;
+    {
+        TrackInitParams::Input input;
+        input.capacity = 1u << 22;
+        input.max_events = 1u << 16;
+        input.track_order = TrackOrder::none;
+        params.init = std::make_shared<TrackInitParams>(input);
+    }
+
+    prob.core = std::make_shared<CoreParams>(std::move(params));
+
+    // Energy deposition tally over the listed volumes
+    {
+        std::vector<Label> labels;
+        for (auto const& l : prob.geo.vol_labels)
+            labels.push_back(Label{l});
+        prob.calo = std::make_shared<SimpleCalo>(
+            std::move(labels), *prob.core->geometry(), 1);
+        StepCollector::VecInterface ifaces{prob.calo};
+        prob.collector = std::make_shared<StepCollector>(
+            prob.core->geometry(),
+            std::move(ifaces),
+            prob.core->aux_reg().get(),
+            prob.core->action_reg().get());
+    }
+    return prob;
+}
+
+//---------------------------------------------------------------------------//
+// Primaries file: "pdg energy x y z dx dy dz time event" per line
+//---------------------------------------------------------------------------//
+std::vector<Primary>
+load_primaries(std::string const& path, ParticleParams const& particles)
+{
+    std::ifstream in(path);
+    if (!in)
+        throw std::runtime_error("cannot open " + path);
+    std::vector<Primary> result;
+    int pdg;
+    double e, x, y, z, dx, dy, dz, t;
+    long ev;
+    while (in >> pdg >> e >> x >> y >> z >> dx >> dy >> dz >> t >> ev)
+    {
+        Primary p;
+        p.particle_id = particles.find(PDGNumber{pdg});
+        p.energy = units::MevEnergy{e};
+        p.position = {x, y, z};
+        p.direction = {dx, dy, dz};
+        p.time = t;
+        p.event_id = EventId{static_cast<size_type>(ev)};
+        result.push_back(p);
+    }
+    return result;
+}
+
+int run(int argc, char** argv)
+{
+    if (argc < 7)
+    {
+        std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
+                     "<seed> [--field Bx By Bz] [--msc] [--steps N]\n";
+        return 2;
+    }
+    std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
+    size_type num_slots = std::stoul(argv[5]);
+    unsigned int seed = std::stoul(argv[6]);
+    Real3 field{0, 0, 0};
+    bool msc = false;
+    size_type max_steps = static_cast<size_type>(-1);
+    for (int i = 7; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--field")
+        {
+            field = {std::strtod(argv[i + 1], nullptr),
+                     std::strtod(argv[i + 2], nullptr),
+                     std::strtod(argv[i + 3], nullptr)};
+            i += 3;
+        }
+        else if (a == "--msc")
+            msc = true;
+        else if (a == "--steps")
+            max_steps = std::stoul(argv[++i]);
+    }
+
+    KvFile kv(phys_path);
+    ImportData imported = load_import(kv, msc);
+    Problem prob = build_problem(imported, geo_name, seed, field, msc);
+    auto primaries = load_primaries(prim_path, *prob.core->particle());
+
+    StepperInput sinp;
+    sinp.params = prob.core;
+    sinp.stream_id = StreamId{0};
+    sinp.num_track_slots = num_slots;
+    Stepper<MemSpace::host> step(std::move(sinp));
+
+    // Print action list (ordered) for the action-ID contract
+    {
+        auto const& reg = *prob.core->action_reg();
+        for (auto id : range(ActionId{reg.num_actions()}))
+        {
+            std::printf("action %u %s\n",
+                        id.unchecked_get(),
+                        std::string(reg.id_to_label(id)).c_str());
+        }
+    }
+
+    StepperResult counts = step(make_span(primaries));
+    size_type iter = 0;
+    unsigned long long track_steps = counts.active;
+    std::printf("step %u %u %u %u %u\n",
+                iter,
+                counts.generated,
+                counts.queued,
+                counts.active,
+                counts.alive);
+    while (counts && ++iter < max_steps)
+    {
+        counts = step();
+        track_steps += counts.active;
+        std::printf("step %u %u %u %u %u\n",
+                    iter,
+                    counts.generated,
+                    counts.queued,
+                    counts.active,
+                    counts.alive);
+    }
+    std::printf("total_steps %llu iterations %u\n", track_steps, iter + 1);
+    auto edep = prob.calo->calc_total_energy_deposition();
+    for (std::size_t i = 0; i < edep.size(); ++i)
+    {
+        std::printf("edep %s %.17g\n", prob.geo.vol_labels[i].c_str(), edep[i]);
+    }
+    return 0;
+}
+
+int dump_geo(int argc, char** argv)
+{
+    if (argc < 4)
+        return 2;
+    GeoSpec spec = build_geometry(argv[3]);
+    auto const& host = spec.geo->host_ref();
+    std::printf("volumes %zu\n", static_cast<std::size_t>(spec.geo->num_volumes()));
+    for (auto vid : range(VolumeId{spec.geo->num_volumes()}))
+    {
+        std::printf("volume %u %s\n",
+                    vid.unchecked_get(),
+                    spec.geo->volumes().at(vid).name.c_str());
+    }
+    std::printf("surfaces %zu\n", static_cast<std::size_t>(host.surface_types.size()));
+    for (auto i : range(host.surface_types.size()))
+    {
+        std::printf("surface %zu type %d\n",
+                    static_cast<std::size_t>(i),
+                    static_cast<int>(host.surface_types[ItemId<SurfaceType>(i)]));
+    }
+    std::printf("reals %zu\n", static_cast<std::size_t>(host.reals.size()));
+    for (auto i : range(host.reals.size()))
+    {
+        std::printf("real %zu %.17g\n",
+                    static_cast<std::size_t>(i),
+                    host.reals[ItemId<real_type>(i)]);
+    }
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc < 2)
+    {
+        std::cerr << "usage: ref_harness {run|geo} ...\n";
+        return 2;
+    }
+    std::string mode = argv[1];
+    try
+    {
+        if (mode == "run")
+            return run(argc, argv);
+        if (mode == "geo")
+            return dump_geo(argc, argv);
+    }
+    catch (std::exception const& e)
+    {
+        std::cerr << "error: " << e.what() << "\n";
+        return 1;
+    }
+    std::cerr << "unknown mode " << mode << "\n";
+    return 2;
+}
