@@ -1,0 +1,529 @@
+// Per-slot bodies of the step-loop actions. Each function advances one track
+// slot through one action; the CUDA kernels launch them one thread per slot
+// and the host test driver calls them in a loop over slots.
+//
+// Action semantics follow the reference's executors:
+//   pre-step          src/celeritas/phys/detail/PreStepExecutor.hh:46-115
+//   along-step        src/celeritas/global/alongstep/AlongStepGeneralLinearAction.cc
+//                     (PropagationApplier, TimeUpdater, ElossApplier with
+//                     FluctELoss/MeanELoss, TrackUpdater in detail/)
+//   discrete select   src/celeritas/phys/detail/DiscreteSelectExecutor.hh:38-63
+//   interactions      src/celeritas/phys/InteractionApplier.hh:105-171 with the
+//                     model executors in src/celeritas/em/executor/
+//   geo-boundary      src/celeritas/geo/detail/BoundaryExecutor.hh:33-80
+//   tracking-cut      src/celeritas/phys/detail/TrackingCutExecutor.hh
+//   step gather/calo  src/celeritas/user/detail/StepGatherExecutor.hh and
+//                     SimpleCaloExecutor.hh:48-67
+#pragma once
+
+#include "Geometry.hh"
+#include "Interactors.hh"
+
+namespace gbx
+{
+//---------------------------------------------------------------------------//
+// Small accessors
+//---------------------------------------------------------------------------//
+GBX_FORCEINLINE RVec3 load_dir(StateData const& s, size_type slot)
+{
+    return {real_type(s.dir[0][slot]),
+            real_type(s.dir[1][slot]),
+            real_type(s.dir[2][slot])};
+}
+
+GBX_FORCEINLINE real_type cutoff_energy(ParamsData const& p,
+                                        size_type material,
+                                        size_type particle)
+{
+    return p.cutoff_energy[material * p.num_particles + particle];
+}
+
+//! Mark a track as failed (CoreTrackView::apply_errored)
+GBX_FORCEINLINE void apply_errored(ParamsData const& p,
+                                   StateData const& s,
+                                   size_type slot)
+{
+    s.status[slot] = status_errored;
+    s.along_step_action[slot] = invalid_id;
+    s.post_step_action[slot] = p.action_tracking_cut;
+}
+
+//---------------------------------------------------------------------------//
+// pre-step
+//---------------------------------------------------------------------------//
+GBX_FUNCTION void pre_step(ParamsData const& p, StateData const& s, size_type slot)
+{
+    std::uint8_t status = s.status[slot];
+    if (status == status_inactive)
+    {
+        s.step_length[slot] = INFINITY;
+        s.post_step_action[slot] = invalid_id;
+        s.along_step_action[slot] = invalid_id;
+        return;
+    }
+    s.energy_deposition[slot] = 0;
+    s.secondaries_offset[slot] = 0;
+    s.secondaries_count[slot] = 0;
+    s.element[slot] = invalid_id;
+    if (status == status_errored)
+        return;
+    s.status[slot] = status_alive;
+
+    if (!(s.interaction_mfp[slot] > 0))
+    {
+        XorwowEngine rng(s.rng, slot);
+        s.interaction_mfp[slot] = sample_exponential<real_type>(rng);
+    }
+
+    size_type const pid = s.particle_id[slot];
+    size_type const mid = s.material[slot];
+    real_type const energy = s.energy[slot];
+    PhysicsTrack phys(p, pid, mid);
+
+    // calc_physics_step_limit
+    real_type total_macro_xs = 0;
+    for (size_type ppid = 0; ppid < phys.num_processes(); ++ppid)
+    {
+        real_type process_xs;
+        if (phys.group().use_integral[ppid])
+            process_xs = phys.calc_max_xs(ppid, energy);
+        else
+            process_xs = phys.calc_xs(ppid, energy);
+        total_macro_xs += process_xs;
+        s.per_process_xs[ppid][slot] = process_xs;
+    }
+    s.macro_xs[slot] = total_macro_xs;
+
+    double step;
+    size_type action = p.action_discrete;
+    if (energy == 0)
+    {
+        step = 0;
+    }
+    else
+    {
+        step = s.interaction_mfp[slot] / total_macro_xs;
+        size_type const eloss = phys.group().eloss_process;
+        if (eloss != invalid_id)
+        {
+            XsGrid const* g = phys.grid(vgt_range, eloss);
+            real_type range = calc_range(p, *g, energy);
+            s.dedx_range[slot] = range;
+            real_type eloss_step = phys.range_to_step(range);
+            if (eloss_step <= step)
+            {
+                step = eloss_step;
+                action = p.action_range;
+            }
+        }
+        else if (phys.num_processes() == 0)
+        {
+            action = invalid_id;
+        }
+    }
+    s.step_length[slot] = step;
+    s.post_step_action[slot] = action;
+    s.along_step_action[slot] = (p.particles[pid].charge == 0)
+                                    ? p.action_along_step_neutral
+                                    : p.action_along_step;
+}
+
+//---------------------------------------------------------------------------//
+// along-step (linear propagation, energy loss, track update)
+//---------------------------------------------------------------------------//
+//! Mean energy loss over a step (calc_mean_energy_loss)
+GBX_FORCEINLINE real_type calc_mean_eloss(ParamsData const& p,
+                                          StateData const& s,
+                                          PhysicsTrack const& phys,
+                                          size_type slot,
+                                          real_type pre_energy,
+                                          real_type step)
+{
+    size_type const ppid = phys.group().eloss_process;
+    XsGrid const* dedx = phys.grid(vgt_energy_loss, ppid);
+    real_type eloss = step * calc_grid_xs(p, *dedx, pre_energy);
+    if (eloss >= pre_energy * real_type(p.linear_loss_limit))
+    {
+        XsGrid const* rg = phys.grid(vgt_range, ppid);
+        real_type range = s.dedx_range[slot];
+        if (step == range)
+            return pre_energy;
+        eloss = pre_energy - calc_inverse_range(p, *rg, range - step);
+    }
+    return eloss;
+}
+
+//! Fluctuating (or mean) energy loss: FluctELoss::calc_eloss
+template<class G>
+GBX_FUNCTION real_type calc_eloss(ParamsData const& p,
+                                  StateData const& s,
+                                  PhysicsTrack const& phys,
+                                  size_type slot,
+                                  real_type step,
+                                  bool apply_cut,
+                                  G& rng)
+{
+    real_type const energy = s.energy[slot];
+    real_type const lowest = p.lowest_electron_energy;
+    if (apply_cut && energy < lowest)
+        return energy;
+    real_type eloss = calc_mean_eloss(p, s, phys, slot, energy, step);
+    if (p.enable_fluct && eloss < energy)
+    {
+        // EnergyLossHelper (src/celeritas/em/distribution/EnergyLossHelper.hh)
+        size_type const pid = s.particle_id[slot];
+        size_type const mid = s.material[slot];
+        real_type const mean_loss = eloss;
+        if (!(mean_loss < real_type(1e-5)))
+        {
+            real_type const mass = p.particles[pid].mass;
+            real_type const electron_mass = p.particles[p.electron_id].mass;
+            real_type const gamma = 1 + energy / mass;
+            real_type const bsq = beta_sq(mass, energy);
+            real_type const two_mebsgs = 2 * electron_mass * bsq * ipow<2>(gamma);
+            real_type max_energy_transfer;
+            if (pid == p.electron_id)
+            {
+                max_energy_transfer = real_type(0.5) * energy;
+            }
+            else
+            {
+                real_type mass_ratio = electron_mass / mass;
+                max_energy_transfer
+                    = two_mebsgs / (1 + mass_ratio * (2 * gamma + mass_ratio));
+            }
+            real_type const max_energy = min_of(
+                real_type(cutoff_energy(p, mid, p.electron_id)), max_energy_transfer);
+            if (max_energy > real_type(1e-5))
+            {
+                // e+/e- have mass ratio 1: always the Urban model
+                eloss = sample_urban_eloss(p.fluct[mid],
+                                           p.materials[mid],
+                                           mean_loss,
+                                           max_energy,
+                                           two_mebsgs,
+                                           bsq,
+                                           rng);
+            }
+        }
+        if (eloss >= energy)
+        {
+            eloss = apply_cut ? energy : mean_loss;
+        }
+    }
+    if (apply_cut && (energy - eloss <= lowest))
+        return energy;
+    return eloss;
+}
+
+GBX_FUNCTION void along_step(ParamsData const& p, StateData const& s, size_type slot)
+{
+    size_type const along = s.along_step_action[slot];
+    if (!is_track_valid(s.status[slot]))
+        return;
+    if (along != p.action_along_step && along != p.action_along_step_neutral)
+        return;
+    bool const charged = (along == p.action_along_step);
+
+    // PropagationApplier with the linear propagator
+    double const step_length = s.step_length[slot];
+    if (step_length != 0)
+    {
+        GeoTrackView geo(p.geo, s, slot);
+        Propagation prop = geo.find_next_step(step_length);
+        if (prop.boundary)
+            geo.move_to_boundary();
+        else
+            geo.move_internal(step_length);
+        if (prop.boundary)
+        {
+            s.step_length[slot] = prop.distance;
+            s.post_step_action[slot] = p.action_boundary;
+        }
+        else if (prop.distance < step_length)
+        {
+            s.step_length[slot] = prop.distance;
+            s.post_step_action[slot] = p.action_propagation_limit;
+        }
+    }
+
+    // TimeUpdater
+    if (s.status[slot] == status_errored)
+        return;
+    size_type const pid = s.particle_id[slot];
+    {
+        real_type const mass = p.particles[pid].mass;
+        real_type const speed
+            = std::sqrt(beta_sq(mass, s.energy[slot])) * real_type(constants::c_light);
+        if (speed > 0)
+        {
+            s.time[slot] += s.step_length[slot] / speed;
+        }
+    }
+
+    // ElossApplier
+    PhysicsTrack phys(p, pid, s.material[slot]);
+    if (charged && phys.group().eloss_process != invalid_id && s.energy[slot] != 0)
+    {
+        real_type const step = s.step_length[slot];
+        bool const apply_cut = (s.post_step_action[slot] != p.action_boundary);
+        real_type deposited;
+        {
+            XorwowEngine rng(s.rng, slot);
+            deposited = calc_eloss(p, s, phys, slot, step, apply_cut, rng);
+        }
+        if (deposited > 0)
+        {
+            s.energy_deposition[slot] += deposited;
+            s.energy[slot] -= deposited;
+        }
+        if (s.energy[slot] == 0)
+        {
+            if (!phys.group().has_at_rest)
+            {
+                s.status[slot] = status_killed;
+                s.post_step_action[slot] = p.action_range;
+            }
+            else
+            {
+                s.post_step_action[slot] = p.action_discrete;
+            }
+        }
+    }
+
+    // TrackUpdater
+    if (s.status[slot] == status_alive)
+    {
+        if (s.post_step_action[slot] != p.action_discrete)
+        {
+            real_type mfp = s.interaction_mfp[slot]
+                            - real_type(s.step_length[slot]) * s.macro_xs[slot];
+            s.interaction_mfp[slot] = mfp;
+        }
+    }
+    ++s.num_steps[slot];
+}
+
+//---------------------------------------------------------------------------//
+// discrete select
+//---------------------------------------------------------------------------//
+GBX_FUNCTION void discrete_select(ParamsData const& p,
+                                  StateData const& s,
+                                  size_type slot)
+{
+    if (s.post_step_action[slot] != p.action_discrete)
+        return;
+    s.interaction_mfp[slot] = 0;
+    size_type const pid = s.particle_id[slot];
+    size_type const mid = s.material[slot];
+    real_type const energy = s.energy[slot];
+    PhysicsTrack phys(p, pid, mid);
+    XorwowEngine rng(s.rng, slot);
+
+    // Select the process (Selector with total = macro xs)
+    size_type const nproc = phys.num_processes();
+    size_type ppid = nproc - 1;
+    {
+        real_type accum = -s.macro_xs[slot] * generate_canonical<real_type>(rng);
+        for (size_type i = 0; i + 1 < nproc; ++i)
+        {
+            accum += s.per_process_xs[i][slot];
+            if (accum > 0)
+            {
+                ppid = i;
+                break;
+            }
+        }
+    }
+    size_type action;
+    if (phys.group().use_integral[ppid])
+    {
+        real_type xs = phys.calc_xs(ppid, energy);
+        if (generate_canonical<real_type>(rng) * s.per_process_xs[ppid][slot] > xs)
+        {
+            s.post_step_action[slot] = p.action_integral_rejection;
+            return;
+        }
+    }
+    size_type const model = phys.find_model(ppid, energy);
+    MaterialRecord const& mat = p.materials[mid];
+    if (mat.num_elements == 1)
+    {
+        s.element[slot] = 0;
+    }
+    action = model + p.model_to_action;
+    s.post_step_action[slot] = action;
+}
+
+//---------------------------------------------------------------------------//
+// Interaction application (InteractionApplier)
+//---------------------------------------------------------------------------//
+GBX_FUNCTION void apply_interaction(ParamsData const& p,
+                                    StateData const& s,
+                                    size_type slot,
+                                    Interaction const& result)
+{
+    if (result.action == Interaction::failed)
+    {
+        // sim.step_limit({0, failure_action})
+        if (0 < s.step_length[slot])
+        {
+            s.step_length[slot] = 0;
+            s.post_step_action[slot] = p.action_failure;
+        }
+        return;
+    }
+    if (result.action == Interaction::unchanged)
+        return;
+    s.energy[slot] = result.energy;
+    if (result.action != Interaction::absorbed)
+    {
+        GeoTrackView geo(p.geo, s, slot);
+        geo.set_dir(Real3{double(result.direction.x),
+                          double(result.direction.y),
+                          double(result.direction.z)});
+    }
+    else
+    {
+        s.status[slot] = status_killed;
+    }
+    s.energy_deposition[slot] += result.energy_deposition;
+    s.secondaries_offset[slot] = result.secondaries
+                                     ? static_cast<size_type>(
+                                         result.secondaries - s.secondaries)
+                                     : 0;
+    s.secondaries_count[slot] = result.num_secondaries;
+}
+
+//! Run one model's interaction for a slot whose post-step action matches
+GBX_FUNCTION void interact(ParamsData const& p,
+                           StateData const& s,
+                           size_type slot,
+                           size_type action)
+{
+    if (s.post_step_action[slot] != action)
+        return;
+    size_type const pid = s.particle_id[slot];
+    size_type const mid = s.material[slot];
+    real_type const energy = s.energy[slot];
+    RVec3 const dir = load_dir(s, slot);
+    SecondaryAllocator allocate(s);
+    Interaction result;
+    {
+        XorwowEngine rng(s.rng, slot);
+        MaterialRecord const& mat = p.materials[mid];
+        size_type const elcomp = s.element[slot];
+        if (action == p.action_klein_nishina)
+        {
+            result = interact_klein_nishina(p, energy, dir, allocate, rng);
+        }
+        else if (action == p.action_livermore_pe)
+        {
+            result = interact_livermore_pe(
+                p, mat.element[elcomp], energy, dir, allocate, rng);
+        }
+        else if (action == p.action_bethe_heitler)
+        {
+            result = interact_bethe_heitler(
+                p, p.elements[mat.element[elcomp]], energy, dir, allocate, rng);
+        }
+        else if (action == p.action_seltzer_berger)
+        {
+            result = interact_seltzer_berger(p,
+                                             mat.element[elcomp],
+                                             mat,
+                                             pid == p.electron_id,
+                                             real_type(p.particles[pid].mass),
+                                             energy,
+                                             dir,
+                                             cutoff_energy(p, mid, p.gamma_id),
+                                             allocate,
+                                             rng);
+        }
+        else if (action == p.action_moller_bhabha)
+        {
+            result = interact_moller_bhabha(p,
+                                            pid == p.electron_id,
+                                            energy,
+                                            dir,
+                                            cutoff_energy(p, mid, p.electron_id),
+                                            allocate,
+                                            rng);
+        }
+        else if (action == p.action_eplusgg)
+        {
+            result = interact_eplusgg(p, energy, dir, allocate, rng);
+        }
+        else
+        {
+            return;
+        }
+    }
+    apply_interaction(p, s, slot, result);
+}
+
+//---------------------------------------------------------------------------//
+// geo-boundary and tracking-cut
+//---------------------------------------------------------------------------//
+GBX_FUNCTION void boundary_cross(ParamsData const& p,
+                                 StateData const& s,
+                                 size_type slot)
+{
+    if (s.post_step_action[slot] != p.action_boundary)
+        return;
+    GeoTrackView geo(p.geo, s, slot);
+    geo.cross_boundary();
+    if (geo.failed())
+    {
+        apply_errored(p, s, slot);
+        return;
+    }
+    if (!geo.is_outside())
+    {
+        size_type matid = p.geo.volume_material[geo.volume()];
+        if (matid == invalid_id)
+        {
+            apply_errored(p, s, slot);
+            return;
+        }
+        s.material[slot] = matid;
+    }
+    else
+    {
+        s.status[slot] = status_killed;
+    }
+}
+
+GBX_FUNCTION void tracking_cut(ParamsData const& p,
+                               StateData const& s,
+                               size_type slot)
+{
+    if (s.post_step_action[slot] != p.action_tracking_cut)
+        return;
+    size_type const pid = s.particle_id[slot];
+    real_type deposited = s.energy[slot];
+    if (p.particles[pid].is_antiparticle)
+    {
+        deposited += 2 * real_type(p.particles[pid].mass);
+    }
+    s.energy_deposition[slot] += deposited;
+    s.energy[slot] -= s.energy[slot];
+    s.status[slot] = status_killed;
+}
+
+//---------------------------------------------------------------------------//
+// Step gathering and calorimeter tally
+//---------------------------------------------------------------------------//
+//! Record the detector of the pre-step volume (StepGatherExecutor<pre>)
+GBX_FUNCTION void gather_pre(ParamsData const& p, StateData const& s, size_type slot)
+{
+    if (s.status[slot] == status_inactive)
+    {
+        s.detector[slot] = invalid_id;
+        return;
+    }
+    size_type vol = s.volume[slot];
+    s.detector[slot] = p.geo.volume_detector[vol];
+}
+
+}  // namespace gbx

@@ -1,0 +1,391 @@
+// Device-resident parameter tables and the track-state structure of arrays.
+//
+// Params (read-only, one contiguous device allocation) replace the
+// reference's CoreParamsData (src/celeritas/global/CoreTrackData.hh:36-110):
+// particles, materials, cutoffs, physics tables, model data and geometry are
+// flattened into index-addressed arrays. State replaces CoreStateData
+// (src/celeritas/global/CoreTrackData.hh:115-160) as a pure structure of
+// arrays: every per-slot field is its own array so that one warp touches one
+// contiguous 128-byte line per field.
+#pragma once
+
+#include "Random.hh"
+#include "Types.hh"
+
+namespace gbx
+{
+//---------------------------------------------------------------------------//
+// Enumerations (values match the reference's enums)
+//---------------------------------------------------------------------------//
+//! src/celeritas/Types.hh:113-122
+enum TrackStatus : std::uint8_t
+{
+    status_inactive = 0,
+    status_initializing = 1,
+    status_alive = 2,
+    status_errored = 3,
+    status_killed = 4,
+};
+
+GBX_FORCEINLINE bool is_track_valid(std::uint8_t s)
+{
+    return s != status_inactive && s != status_errored;
+}
+
+//! Value grid types (src/celeritas/phys/PhysicsData.hh ValueGridType)
+enum ValueGridType : int
+{
+    vgt_macro_xs = 0,
+    vgt_energy_loss = 1,
+    vgt_range = 2,
+    vgt_size = 3,
+};
+
+//! ORANGE-style boundary state (src/orange/OrangeTypes.hh BoundaryResult)
+enum BoundaryResult : std::uint8_t
+{
+    boundary_exiting = 0,
+    boundary_reentrant = 1,
+};
+
+constexpr int max_processes = 4;  //!< Max processes per particle
+constexpr int max_elements = 4;  //!< Max element components per material
+
+//---------------------------------------------------------------------------//
+// Tables
+//---------------------------------------------------------------------------//
+//! Log-uniform energy grid with values; grid energies precomputed on host
+struct XsGrid
+{
+    double log_front;  //!< log(E_min)
+    double log_back;  //!< log(E_max)
+    double log_delta;  //!< (log_back - log_front) / (size - 1)
+    size_type size;
+    size_type value;  //!< Offset of values in reals
+    size_type energy;  //!< Offset of exp(log_front + i * log_delta) in reals,
+                       //!< followed by exp(log_back)
+    size_type prime_index;  //!< Values at/after this index are scaled by E
+};
+
+//! Nonuniform grid: x and y offsets into reals
+struct GenericGrid
+{
+    size_type x;
+    size_type y;
+    size_type size;
+};
+
+struct ParticleRecord
+{
+    double mass;  //!< [MeV]
+    double charge;  //!< [e]
+    int pdg;
+    bool is_antiparticle;
+};
+
+struct ElementRecord
+{
+    int z;
+    double atomic_mass;  //!< [amu]
+    double cbrt_z;
+    double cbrt_zzp;
+    double log_z;
+    double coulomb_correction;
+    double mass_radiation_coeff;
+};
+
+struct MaterialRecord
+{
+    double number_density;
+    double electron_density;
+    double zeff;
+    double density;
+    double rad_length;
+    double log_mean_exc_energy;
+    double mean_exc_energy;
+    size_type num_elements;
+    size_type element[max_elements];
+    double fraction[max_elements];
+};
+
+//! Urban fluctuation parameters per material
+struct UrbanFluctRecord
+{
+    double binding_energy[2];
+    double log_binding_energy[2];
+    double oscillator_strength[2];
+};
+
+//! Per-particle physics process group
+struct ProcessGroup
+{
+    size_type num_processes;
+    size_type process[max_processes];  //!< Global process IDs
+    //! Models: energy grid (num_models+1 energies) and model IDs per process
+    size_type model_energy[max_processes];  //!< Offset in reals
+    size_type model_ids[max_processes];  //!< Offset in ints
+    size_type num_models[max_processes];
+    //! Value grids [vgt][process * num_materials + material] -> grid index
+    size_type grid_table[vgt_size];  //!< Offset in ints (invalid_id if none)
+    //! Integral approach: energy of max xs per material (offset, or invalid)
+    size_type energy_max_xs[max_processes];
+    bool use_integral[max_processes];
+    size_type eloss_process;  //!< Local process index with dedx/range or -1
+    bool has_at_rest;
+};
+
+//! Livermore photoelectric data per element
+struct LivermoreElement
+{
+    GenericGrid xs_lo;  //!< size 0 if absent
+    GenericGrid xs_hi;
+    double thresh_lo;
+    double thresh_hi;
+    size_type shells;  //!< Offset of first shell
+    size_type num_shells;
+};
+struct LivermoreShell
+{
+    double binding_energy;
+    double param[2][6];
+    GenericGrid xs;
+};
+
+//! Seltzer-Berger scaled DCS per element
+struct SBElementTable
+{
+    size_type x;  //!< Offset of log-energy grid
+    size_type nx;
+    size_type y;  //!< Offset of reduced photon energy grid
+    size_type ny;
+    size_type values;  //!< Offset of [nx][ny] values
+    size_type argmax;  //!< Offset (in ints) of per-x argmax over y
+};
+
+//---------------------------------------------------------------------------//
+// Geometry: axis-aligned box volumes in a background world (the ORANGE
+// simple-unit subset used by the sampling calorimeter)
+//---------------------------------------------------------------------------//
+//! Surface: an axis-aligned plane
+struct PlaneRecord
+{
+    int axis;
+    double position;
+};
+
+//! Volume bounded by faces; 'sense' gives the inside sense of each face
+struct BoxVolume
+{
+    size_type faces[6];  //!< Plane (surface) IDs
+    std::int8_t inside_sense[6];  //!< +1: inside is pos > plane, -1: below
+    size_type material;
+};
+
+struct GeoParams
+{
+    size_type num_surfaces;
+    PlaneRecord const* planes;
+    size_type num_volumes;  //!< Including exterior (0) and background
+    BoxVolume const* boxes;  //!< Indexed by volume id (exterior/background unused)
+    size_type exterior;  //!< Volume id of the exterior (0)
+    size_type background;  //!< Volume id of the implicit background
+    size_type world_faces[6];  //!< Boundary planes of the world box
+    std::int8_t world_sense[6];
+    //! Neighbors of each surface: volumes that own it as a face
+    size_type const* neighbor_offset;  //!< [num_surfaces + 1]
+    size_type const* neighbors;
+    //! Uniform search grid along the layering axis for point location
+    int stack_axis;
+    double tol_abs;
+    double tol_rel;
+    size_type const* volume_material;  //!< [num_volumes], invalid if none
+    size_type const* volume_detector;  //!< [num_volumes], invalid if none
+};
+
+//---------------------------------------------------------------------------//
+// All parameters
+//---------------------------------------------------------------------------//
+struct ParamsData
+{
+    // Storage
+    double const* reals;
+    size_type const* ints;
+
+    // Particles: 0 = e-, 1 = e+, 2 = gamma (same order as the input file)
+    size_type num_particles;
+    ParticleRecord const* particles;
+    size_type electron_id;
+    size_type positron_id;
+    size_type gamma_id;
+
+    // Materials
+    size_type num_materials;
+    MaterialRecord const* materials;
+    ElementRecord const* elements;
+    UrbanFluctRecord const* fluct;
+    double const* cutoff_energy;  //!< [material * num_particles + particle]
+
+    // Physics
+    ProcessGroup const* process_groups;  //!< [particle]
+    XsGrid const* grids;
+    size_type num_models;
+    size_type model_to_action;  //!< Action ID of model 0
+    // Scalars (src/celeritas/phys/PhysicsData.hh PhysicsParamsScalars)
+    double min_range;
+    double max_step_over_range;
+    double min_eprime_over_e;
+    double lowest_electron_energy;
+    double linear_loss_limit;
+    double secondary_stack_factor;
+    bool enable_fluct;
+    // Hardwired processes
+    size_type photoelectric_process;
+    size_type annihilation_process;
+    double photoelectric_table_thresh;
+    size_type livermore_model;
+    size_type eplusgg_model;
+
+    // Model data
+    LivermoreElement const* livermore_elements;
+    LivermoreShell const* livermore_shells;
+    SBElementTable const* sb_tables;
+    bool enable_lpm;
+
+    // Action IDs (the reference's registration order)
+    size_type action_pre_step;
+    size_type action_msc_range;
+    size_type action_range;
+    size_type action_discrete;
+    size_type action_integral_rejection;
+    size_type action_failure;
+    size_type action_along_step;
+    size_type action_along_step_neutral;
+    size_type action_propagation_limit;
+    size_type action_boundary;
+    size_type action_tracking_cut;
+    // Model actions in model order
+    size_type action_moller_bhabha;
+    size_type action_seltzer_berger;
+    size_type action_rel_brems;
+    size_type action_livermore_pe;
+    size_type action_klein_nishina;
+    size_type action_bethe_heitler;
+    size_type action_eplusgg;
+
+    GeoParams geo;
+
+    // Tally
+    size_type num_detectors;
+};
+
+//---------------------------------------------------------------------------//
+// State (structure of arrays)
+//---------------------------------------------------------------------------//
+struct Secondary
+{
+    size_type particle_id;  //!< invalid_id: cut/killed secondary
+    real_type energy;
+    Vec3<real_type> direction;
+};
+
+//! Track initializer (src/celeritas/track/TrackInitData.hh:67-78)
+struct TrackInitializer
+{
+    size_type track_id;
+    size_type parent_id;
+    size_type event_id;
+    double time;
+    Real3 pos;
+    Real3 dir;
+    size_type particle_id;
+    real_type energy;
+};
+
+//! Device-resident counters (src/celeritas/track/CoreStateCounters.hh:24-47)
+struct Counters
+{
+    size_type num_vacancies;
+    size_type num_initializers;
+    size_type num_secondaries;
+    size_type num_active;
+    size_type num_alive;
+    size_type num_generated;
+    size_type secondary_stack_size;  //!< Bump allocator top
+    size_type num_pending_primaries;
+    size_type error_flags;
+    size_type pad[7];
+};
+
+struct StateData
+{
+    size_type size;  //!< Number of track slots
+
+    // Sim
+    std::uint8_t* status;
+    size_type* track_id;
+    size_type* parent_id;
+    size_type* event_id;
+    size_type* num_steps;
+    double* time;
+    double* step_length;
+    size_type* post_step_action;
+    size_type* along_step_action;
+
+    // Particle
+    size_type* particle_id;
+    real_type* energy;
+
+    // Geometry
+    double* pos[3];
+    double* dir[3];
+    size_type* volume;
+    size_type* surface;  //!< Current surface or invalid
+    std::int8_t* surface_sense;  //!< Sense of the track relative to surface
+    std::uint8_t* boundary;
+    double* next_step;
+    size_type* next_surface;
+    std::int8_t* next_sense;
+    std::uint8_t* geo_failed;
+
+    // Material
+    size_type* material;
+
+    // Physics
+    real_type* interaction_mfp;
+    real_type* dedx_range;
+    real_type* macro_xs;
+    real_type* per_process_xs[max_processes];
+    real_type* energy_deposition;
+    size_type* secondaries_offset;
+    size_type* secondaries_count;
+    size_type* element;
+
+    // RNG
+    RngStateRef rng;
+
+    // Track initialization
+    size_type* vacancies;
+    size_type* secondary_counts;
+    size_type* parents;
+    TrackInitializer* initializers;
+    size_type initializer_capacity;
+    size_type* track_counters;  //!< Per-event next track ID
+    size_type max_events;
+
+    // Secondary stack
+    Secondary* secondaries;
+    size_type secondary_capacity;
+
+    // Step gather: detector ID at pre-step
+    size_type* detector;
+    // Tally: energy deposition per detector (FP64 accumulation)
+    double* calo_edep;
+
+    // Primaries staging
+    TrackInitializer* primaries;
+    size_type primary_capacity;
+
+    Counters* counters;
+};
+
+}  // namespace gbx

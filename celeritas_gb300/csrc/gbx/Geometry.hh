@@ -1,0 +1,533 @@
+// Navigation through axis-aligned box volumes inside an implicit background
+// volume and a world box (the sampling-calorimeter geometry class).
+//
+// Semantics follow ORANGE's single-level simple unit:
+// - sense of a point w.r.t. a plane is "outside" when pos - plane >= 0
+//   (src/orange/OrangeTypes.hh:412-424);
+// - a box volume's logic is the conjunction of its face senses
+//   (src/orange/univ/detail/LogicEvaluator.hh);
+// - distance to a plane is (plane - pos) / dir, kept if positive and not on
+//   the current surface (src/orange/surf/PlaneAligned.hh);
+// - box volumes take the first minimum over faces
+//   (src/orange/univ/SimpleUnitTracker.hh:271-330);
+// - the background volume scans crossings by increasing distance and accepts
+//   the first one whose bumped point lies inside a neighbor volume
+//   (SimpleUnitTracker::background_intersect);
+// - crossing a surface flips the sense and locates the new volume among the
+//   surface's neighbors with the crossed face's sense forced
+//   (SimpleUnitTracker::cross_boundary, OrangeTrackView.hh:662-787);
+// - moving uses axpy with fma (src/corecel/math/ArrayUtils.hh:78-85).
+//
+// The volume search used when a surface has many neighbors (the reference
+// uses a bounding-interval hierarchy) is a binary search over the layer
+// planes along the stacking axis followed by the same inside test, which
+// selects the same volume because box volumes do not overlap.
+#pragma once
+
+#include "Data.hh"
+
+namespace gbx
+{
+struct Propagation
+{
+    double distance;
+    bool boundary;
+    bool looping;
+};
+
+class GeoTrackView
+{
+  public:
+    GBX_FORCEINLINE GeoTrackView(GeoParams const& params,
+                                 StateData const& state,
+                                 size_type slot)
+        : p_(params), s_(state), slot_(slot)
+    {
+    }
+
+    //// ACCESSORS ////
+    GBX_FORCEINLINE Real3 pos() const
+    {
+        return {s_.pos[0][slot_], s_.pos[1][slot_], s_.pos[2][slot_]};
+    }
+    GBX_FORCEINLINE Real3 dir() const
+    {
+        return {s_.dir[0][slot_], s_.dir[1][slot_], s_.dir[2][slot_]};
+    }
+    GBX_FORCEINLINE size_type volume() const { return s_.volume[slot_]; }
+    GBX_FORCEINLINE bool is_outside() const
+    {
+        return s_.volume[slot_] == p_.exterior;
+    }
+    GBX_FORCEINLINE bool is_on_boundary() const
+    {
+        return s_.surface[slot_] != invalid_id;
+    }
+    GBX_FORCEINLINE bool failed() const { return s_.geo_failed[slot_] != 0; }
+
+    //// INITIALIZATION ////
+    //! Locate a new track from scratch (OrangeTrackView operator=(Initializer))
+    GBX_FUNCTION void initialize(Real3 const& pos, Real3 const& dir)
+    {
+        this->set_pos(pos);
+        this->set_dir_raw(dir);
+        bool on_surface = false;
+        size_type vol
+            = this->find_volume_at(pos, invalid_id, invalid_id, &on_surface);
+        std::uint8_t failed = 0;
+        if (on_surface)
+        {
+            failed = 1;
+            vol = p_.exterior;
+        }
+        s_.volume[slot_] = vol;
+        s_.geo_failed[slot_] = failed;
+        s_.boundary[slot_] = boundary_exiting;
+        s_.surface[slot_] = invalid_id;
+        s_.surface_sense[slot_] = 0;
+        s_.next_step[slot_] = 0;
+        s_.next_surface[slot_] = invalid_id;
+    }
+
+    //! Copy another track's geometry state with a new direction
+    //! (OrangeTrackView operator=(DetailedInitializer))
+    GBX_FUNCTION void copy_from(size_type other, Real3 const& dir)
+    {
+        if (other != slot_)
+        {
+            s_.volume[slot_] = s_.volume[other];
+            s_.surface[slot_] = s_.surface[other];
+            s_.surface_sense[slot_] = s_.surface_sense[other];
+            s_.boundary[slot_] = s_.boundary[other];
+            for (int i = 0; i < 3; ++i)
+            {
+                s_.pos[i][slot_] = s_.pos[i][other];
+            }
+        }
+        s_.geo_failed[slot_] = 0;
+        s_.next_step[slot_] = 0;
+        s_.next_surface[slot_] = invalid_id;
+        this->set_dir_raw(dir);
+    }
+
+    //// NAVIGATION ////
+    GBX_FUNCTION Propagation find_next_step(double max_step);
+    GBX_FUNCTION void move_to_boundary();
+    GBX_FUNCTION void move_internal(double dist);
+    GBX_FUNCTION void cross_boundary();
+    GBX_FUNCTION void set_dir(Real3 const& newdir);
+    GBX_FUNCTION double find_safety() const;
+
+  private:
+    GeoParams const& p_;
+    StateData const& s_;
+    size_type slot_;
+
+    GBX_FORCEINLINE void set_pos(Real3 const& v)
+    {
+        s_.pos[0][slot_] = v.x;
+        s_.pos[1][slot_] = v.y;
+        s_.pos[2][slot_] = v.z;
+    }
+    GBX_FORCEINLINE void set_dir_raw(Real3 const& v)
+    {
+        s_.dir[0][slot_] = v.x;
+        s_.dir[1][slot_] = v.y;
+        s_.dir[2][slot_] = v.z;
+    }
+
+    //! True if the point is on the "outside" (non-negative) side of a plane
+    static GBX_FORCEINLINE bool sense_outside(double q) { return !(q < 0); }
+
+    GBX_FORCEINLINE double plane_q(size_type surf, Real3 const& pos) const
+    {
+        PlaneRecord const& pl = p_.planes[surf];
+        return pos[pl.axis] - pl.position;
+    }
+
+    //! Evaluate the inside logic of a box volume at 'pos'. A face whose
+    //! surface equals 'forced' takes the given sense. Sets *on_surface if
+    //! any unforced face evaluates exactly on its plane.
+    GBX_FUNCTION bool box_inside(BoxVolume const& box,
+                                 Real3 const& pos,
+                                 size_type forced,
+                                 bool forced_outside,
+                                 bool* on_surface) const
+    {
+        bool inside = true;
+        for (int f = 0; f < 6; ++f)
+        {
+            bool s;
+            if (box.faces[f] == forced)
+            {
+                s = forced_outside;
+            }
+            else
+            {
+                double q = this->plane_q(box.faces[f], pos);
+                s = sense_outside(q);
+                if (q == 0 && on_surface)
+                {
+                    *on_surface = true;
+                }
+            }
+            inside = inside && (box.inside_sense[f] > 0 ? s : !s);
+        }
+        return inside;
+    }
+
+    //! Exterior volume logic: not inside the world box
+    GBX_FUNCTION bool exterior_inside(Real3 const& pos,
+                                      size_type forced,
+                                      bool forced_outside,
+                                      bool* on_surface) const
+    {
+        BoxVolume world;
+        for (int f = 0; f < 6; ++f)
+        {
+            world.faces[f] = p_.world_faces[f];
+            world.inside_sense[f] = p_.world_sense[f];
+        }
+        return !this->box_inside(world, pos, forced, forced_outside, on_surface);
+    }
+
+    GBX_FUNCTION bool volume_inside(size_type vol,
+                                    Real3 const& pos,
+                                    size_type forced,
+                                    bool forced_outside,
+                                    bool* on_surface) const
+    {
+        if (vol == p_.exterior)
+        {
+            return this->exterior_inside(pos, forced, forced_outside, on_surface);
+        }
+        return this->box_inside(
+            p_.boxes[vol], pos, forced, forced_outside, on_surface);
+    }
+
+    //! Locate the box volume containing a point among all volumes (the
+    //! reference's BIH search), skipping 'exclude'; background if none.
+    GBX_FUNCTION size_type find_volume_at(Real3 const& pos,
+                                          size_type exclude,
+                                          size_type forced,
+                                          bool* on_surface,
+                                          bool forced_outside = false) const;
+};
+
+//---------------------------------------------------------------------------//
+GBX_FUNCTION size_type GeoTrackView::find_volume_at(Real3 const& pos,
+                                                    size_type exclude,
+                                                    size_type forced,
+                                                    bool* on_surface,
+                                                    bool forced_outside) const
+{
+    // Exterior first: outside the world box
+    if (exclude != p_.exterior)
+    {
+        bool on = false;
+        if (this->exterior_inside(pos, forced, forced_outside, &on))
+        {
+            if (on_surface)
+                *on_surface = on;
+            return p_.exterior;
+        }
+    }
+    // Candidate box volumes: binary search along the stacking axis over the
+    // volumes' lower planes (boxes are sorted by increasing lower plane)
+    int const axis = p_.stack_axis;
+    double const x = pos[axis];
+    // Boxes occupy ids [1, background); find last box with lower <= x
+    size_type lo = 1, hi = p_.background;  // search in [lo, hi)
+    while (lo < hi)
+    {
+        size_type mid = lo + (hi - lo) / 2;
+        double lower = p_.planes[p_.boxes[mid].faces[4]].position;
+        if (lower <= x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    // lo - 1 is the last box whose lower plane is <= x; also test the one
+    // below in case the point sits exactly on a shared plane
+    for (int k = 0; k < 2; ++k)
+    {
+        if (lo < 2 + static_cast<size_type>(k))
+            break;
+        size_type cand = lo - 1 - k;
+        if (cand == exclude)
+            continue;
+        bool on = false;
+        if (this->box_inside(p_.boxes[cand], pos, forced, forced_outside, &on))
+        {
+            if (on_surface)
+                *on_surface = on;
+            return cand;
+        }
+    }
+    return p_.background;
+}
+
+//---------------------------------------------------------------------------//
+GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
+{
+    Propagation result{max_step, false, false};
+    if (s_.boundary[slot_] == boundary_reentrant)
+    {
+        s_.next_step[slot_] = 0;
+        s_.next_surface[slot_] = s_.surface[slot_];
+        s_.next_sense[slot_] = s_.surface_sense[slot_];
+        return {0, true, false};
+    }
+    Real3 const pos = this->pos();
+    Real3 const dir = this->dir();
+    size_type const vol = s_.volume[slot_];
+    size_type const cur_surf = s_.surface[slot_];
+
+    auto calc_dist = [&](size_type surf) -> double {
+        // Returns +inf if no valid crossing
+        if (surf == cur_surf)
+            return INFINITY;
+        PlaneRecord const& pl = p_.planes[surf];
+        double n_dir = dir[pl.axis];
+        if (n_dir != 0)
+        {
+            double d = (pl.position - pos[pl.axis]) / n_dir;
+            if (d > 0)
+                return d;
+        }
+        return INFINITY;
+    };
+
+    size_type hit_surf = invalid_id;
+    double hit_dist = max_step;
+    std::int8_t hit_sense = 0;
+
+    if (vol != p_.background)
+    {
+        // Simple (convex) box volume: first minimum over faces in order
+        BoxVolume const& box = p_.boxes[vol];
+        double best = INFINITY;
+        int best_face = -1;
+        for (int f = 0; f < 6; ++f)
+        {
+            double d = calc_dist(box.faces[f]);
+            if (d <= max_step && d < best)
+            {
+                best = d;
+                best_face = f;
+            }
+        }
+        if (best_face >= 0)
+        {
+            hit_surf = box.faces[best_face];
+            hit_dist = best;
+            if (hit_surf == cur_surf)
+            {
+                hit_sense = s_.surface_sense[slot_];
+            }
+            else
+            {
+                hit_sense = sense_outside(this->plane_q(hit_surf, pos)) ? 1 : -1;
+            }
+        }
+    }
+    else
+    {
+        // Implicit background: crossings by increasing distance; accept the
+        // first whose bumped point lies inside a neighboring volume
+        double bump = p_.tol_abs;
+        for (int i = 0; i < 3; ++i)
+        {
+            bump = max_of(bump, p_.tol_rel * std::fabs(pos[i]));
+        }
+        double prev = -INFINITY;
+        size_type prev_surf = invalid_id;
+        for (size_type iter = 0; iter < p_.num_surfaces; ++iter)
+        {
+            // Next candidate: smallest (distance, surface) after prev
+            double best = INFINITY;
+            size_type best_surf = invalid_id;
+            for (size_type s = 0; s < p_.num_surfaces; ++s)
+            {
+                double d = calc_dist(s);
+                if (!(d <= max_step))
+                    continue;
+                bool after = d > prev || (d == prev && s > prev_surf);
+                if (!after)
+                    continue;
+                if (d < best || (d == best && s < best_surf))
+                {
+                    best = d;
+                    best_surf = s;
+                }
+            }
+            if (best_surf == invalid_id)
+                break;
+            prev = best;
+            prev_surf = best_surf;
+
+            Real3 bumped = pos;
+            axpy(best + bump, dir, &bumped);
+            // Neighbors of this surface
+            size_type nbeg = p_.neighbor_offset[best_surf];
+            size_type nend = p_.neighbor_offset[best_surf + 1];
+            bool found = false;
+            bool found_outside = false;
+            if (nend - nbeg >= 3)
+            {
+                // Many neighbors: locate by position (non-overlapping boxes)
+                size_type v = this->find_volume_at(
+                    bumped, invalid_id, invalid_id, nullptr);
+                if (v != p_.background && v != p_.exterior)
+                {
+                    found = true;
+                    // Sense of the crossed surface evaluated at the bumped
+                    // point inside the new volume, flipped
+                    found_outside
+                        = !sense_outside(this->plane_q(best_surf, bumped));
+                }
+            }
+            else
+            {
+                for (size_type n = nbeg; n < nend; ++n)
+                {
+                    size_type v = p_.neighbors[n];
+                    if (this->volume_inside(v, bumped, invalid_id, false, nullptr))
+                    {
+                        found = true;
+                        found_outside
+                            = !sense_outside(this->plane_q(best_surf, bumped));
+                        break;
+                    }
+                }
+            }
+            if (found)
+            {
+                hit_surf = best_surf;
+                hit_dist = best;
+                hit_sense = found_outside ? 1 : -1;
+                break;
+            }
+        }
+    }
+
+    s_.next_step[slot_] = hit_dist;
+    s_.next_surface[slot_] = hit_surf;
+    s_.next_sense[slot_] = hit_sense;
+    result.distance = hit_dist;
+    result.boundary = (hit_surf != invalid_id);
+    return result;
+}
+
+GBX_FUNCTION void GeoTrackView::move_to_boundary()
+{
+    double const dist = s_.next_step[slot_];
+    Real3 pos = this->pos();
+    axpy(dist, this->dir(), &pos);
+    this->set_pos(pos);
+    s_.surface[slot_] = s_.next_surface[slot_];
+    s_.surface_sense[slot_] = s_.next_sense[slot_];
+    s_.next_step[slot_] = 0;
+    s_.next_surface[slot_] = invalid_id;
+}
+
+GBX_FUNCTION void GeoTrackView::move_internal(double dist)
+{
+    Real3 pos = this->pos();
+    axpy(dist, this->dir(), &pos);
+    this->set_pos(pos);
+    s_.next_step[slot_] = s_.next_step[slot_] - dist;
+    s_.surface[slot_] = invalid_id;
+}
+
+GBX_FUNCTION void GeoTrackView::cross_boundary()
+{
+    if (s_.boundary[slot_] == boundary_reentrant)
+    {
+        s_.boundary[slot_] = boundary_exiting;
+        return;
+    }
+    // Flip the sense on crossing
+    std::int8_t sense = -s_.surface_sense[slot_];
+    s_.surface_sense[slot_] = sense;
+    s_.boundary[slot_] = boundary_exiting;
+
+    size_type const surf = s_.surface[slot_];
+    size_type const cur_vol = s_.volume[slot_];
+    Real3 const pos = this->pos();
+    bool const forced_outside = sense > 0;
+
+    size_type nbeg = p_.neighbor_offset[surf];
+    size_type nend = p_.neighbor_offset[surf + 1];
+    size_type new_vol = invalid_id;
+    if (nend - nbeg < 3)
+    {
+        for (size_type n = nbeg; n < nend; ++n)
+        {
+            size_type v = p_.neighbors[n];
+            if (v == cur_vol)
+                continue;
+            if (this->volume_inside(v, pos, surf, forced_outside, nullptr))
+            {
+                new_vol = v;
+                break;
+            }
+        }
+    }
+    else
+    {
+        new_vol = this->find_volume_at(pos, cur_vol, surf, nullptr, forced_outside);
+        if (new_vol == p_.background)
+            new_vol = invalid_id;
+    }
+    if (new_vol == invalid_id)
+    {
+        new_vol = p_.background;
+    }
+    s_.volume[slot_] = new_vol;
+}
+
+GBX_FUNCTION void GeoTrackView::set_dir(Real3 const& newdir)
+{
+    size_type const surf = s_.surface[slot_];
+    if (surf != invalid_id)
+    {
+        // Normal of an axis-aligned plane is the unit axis vector
+        int axis = p_.planes[surf].axis;
+        Real3 const olddir = this->dir();
+        if ((newdir[axis] >= 0) != (olddir[axis] >= 0))
+        {
+            s_.boundary[slot_] = (s_.boundary[slot_] == boundary_exiting)
+                                     ? boundary_reentrant
+                                     : boundary_exiting;
+        }
+    }
+    this->set_dir_raw(newdir);
+    s_.next_step[slot_] = 0;
+    s_.next_surface[slot_] = invalid_id;
+}
+
+GBX_FUNCTION double GeoTrackView::find_safety() const
+{
+    Real3 const pos = this->pos();
+    size_type const vol = s_.volume[slot_];
+    double result = INFINITY;
+    if (vol != p_.background)
+    {
+        BoxVolume const& box = p_.boxes[vol];
+        for (int f = 0; f < 6; ++f)
+        {
+            result = min_of(result, std::fabs(this->plane_q(box.faces[f], pos)));
+        }
+    }
+    else
+    {
+        for (size_type s = 0; s < p_.num_surfaces; ++s)
+        {
+            result = min_of(result, std::fabs(this->plane_q(s, pos)));
+        }
+    }
+    return result;
+}
+
+}  // namespace gbx

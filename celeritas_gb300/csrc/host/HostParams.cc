@@ -1,0 +1,845 @@
+// Construction of the flattened parameter tables.
+//
+// The derived quantities are computed with the same expressions as the
+// reference's parameter classes so that device lookups reproduce the
+// reference's values:
+//   elements/materials  src/celeritas/mat/MaterialParams.cc (append_*_def),
+//                       src/celeritas/mat/detail/Utils.cc
+//   fluctuations        src/celeritas/em/params/FluctuationParams.cc
+//   physics tables      src/celeritas/phys/PhysicsParams.cc:280-636,
+//                       src/celeritas/grid/ValueGridBuilder.cc
+//   model data          src/celeritas/em/model/SeltzerBergerModel.cc (argmax),
+//                       src/celeritas/em/model/detail/LivermoreXsInserter.hh
+//   geometry            the ORANGE unit that orangeinp builds for the same
+//                       boxes (surface dedup, face order, connectivity)
+#include "HostParams.hh"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <stdexcept>
+
+#include "KvFile.hh"
+
+namespace gbx
+{
+namespace
+{
+//---------------------------------------------------------------------------//
+// Element data tables
+//---------------------------------------------------------------------------//
+//! Coulomb correction f(Z) = a^2 sum_n 1/(n (n^2 + a^2)), a = alpha Z,
+//! evaluated with the series in zeta(2k+1) - 1 (Davies-Bethe-Maximon).
+double calc_coulomb_correction(int z)
+{
+    // zeta(2k+1) - 1 for k = 1..16
+    static double const zeta[] = {2.0205690315959429e-01,
+                                  3.6927755143369927e-02,
+                                  8.3492773819228271e-03,
+                                  2.0083928260822143e-03,
+                                  4.9418860411946453e-04,
+                                  1.2271334757848915e-04,
+                                  3.0588236307020493e-05,
+                                  7.6371976378997626e-06,
+                                  1.9082127165539390e-06,
+                                  4.7693298678780645e-07,
+                                  1.1921992596531106e-07,
+                                  2.9803503514652279e-08,
+                                  7.4507117898354301e-09,
+                                  1.8626597235130491e-09,
+                                  4.6566290650337837e-10,
+                                  1.1641550172700519e-10};
+    double const alphazsq = ipow<2>(constants::alpha_fine_structure * z);
+    double fz = 1 / (1 + alphazsq);
+    double azpow = 1;
+    for (double zeta_i : zeta)
+    {
+        fz += azpow * zeta_i;
+        azpow *= -alphazsq;
+    }
+    return alphazsq * fz;
+}
+
+//! Mass radiation coefficient 1/(X0 rho) from Tsai's formula
+double calc_mass_rad_coeff(ElementRecord const& el)
+{
+    double const z_real = el.z;
+    double lrad, lrad_prime;
+    switch (el.z)
+    {
+        case 1:
+            lrad = 5.31;
+            lrad_prime = 6.144;
+            break;
+        case 2:
+            lrad = 4.79;
+            lrad_prime = 5.621;
+            break;
+        case 3:
+            lrad = 4.74;
+            lrad_prime = 5.805;
+            break;
+        case 4:
+            lrad = 4.71;
+            lrad_prime = 5.924;
+            break;
+        default:
+            lrad = std::log(184.15 * std::pow(z_real, double(-1) / 3));
+            lrad_prime = std::log(1194.0 * std::pow(z_real, double(-2) / 3));
+    }
+    constexpr double inv_x0_factor = 4 * constants::alpha_fine_structure
+                                     * ipow<2>(constants::r_electron);
+    return inv_x0_factor / (el.atomic_mass * constants::atomic_mass)
+           * (ipow<2>(z_real) * (lrad - el.coulomb_correction)
+              + z_real * lrad_prime);
+}
+
+//! Mean excitation energies [eV] by Z (ICRU Report 37 elemental values)
+double mean_excitation_energy(int z)
+{
+    static double const table[] = {
+        19.2,  41.8,  40.0,  63.7,  76.0,  81.0,  82.0,  95.0,  115.0, 137.0,
+        149.0, 156.0, 166.0, 173.0, 173.0, 180.0, 174.0, 188.0, 190.0, 191.0,
+        216.0, 233.0, 245.0, 257.0, 272.0, 286.0, 297.0, 311.0, 322.0, 330.0,
+        334.0, 350.0, 347.0, 348.0, 343.0, 352.0, 363.0, 366.0, 379.0, 393.0,
+        417.0, 424.0, 428.0, 441.0, 449.0, 470.0, 470.0, 469.0, 488.0, 488.0,
+        487.0, 485.0, 491.0, 482.0, 488.0, 491.0, 501.0, 523.0, 535.0, 546.0,
+        560.0, 574.0, 580.0, 591.0, 614.0, 628.0, 650.0, 658.0, 674.0, 684.0,
+        694.0, 705.0, 718.0, 727.0, 736.0, 746.0, 757.0, 790.0, 790.0, 800.0,
+        810.0, 823.0, 823.0, 830.0, 825.0, 794.0, 827.0, 826.0, 841.0, 847.0,
+        878.0, 890.0, 902.0, 921.0, 934.0, 939.0, 952.0, 966.0};
+    if (z < 1 || z > 98)
+        throw std::runtime_error("no mean excitation energy for Z");
+    return 1e-6 * table[z - 1];
+}
+
+bool soft_equal(double a, double b, double rel = 1e-12, double abs = 1e-14)
+{
+    double diff = std::fabs(a - b);
+    if (diff < abs)
+        return true;
+    return diff < rel * std::max(std::fabs(a), std::fabs(b));
+}
+
+//---------------------------------------------------------------------------//
+// Process/model catalog
+//---------------------------------------------------------------------------//
+// Process IDs follow the order of the reference's import process class enum
+// (e_ioni, e_brems, photoelectric, compton, conversion, annihilation)
+enum ProcessId : size_type
+{
+    proc_e_ioni = 0,
+    proc_e_brems,
+    proc_photoelectric,
+    proc_compton,
+    proc_conversion,
+    proc_annihilation,
+    proc_size
+};
+
+// Model IDs in the order the processes build them
+enum ModelId : size_type
+{
+    model_moller_bhabha = 0,
+    model_seltzer_berger,
+    model_rel_brems,
+    model_livermore_pe,
+    model_klein_nishina,
+    model_bethe_heitler,
+    model_eplusgg,
+    model_size
+};
+
+struct Applic
+{
+    size_type particle;
+    double lower;
+    double upper;
+};
+
+class Builder
+{
+  public:
+    Builder(KvFile const& kv, GeometrySpec const& geo, ParamsOptions const& opts)
+        : kv_(kv), geo_(geo), opts_(opts)
+    {
+    }
+
+    HostParams build();
+
+  private:
+    KvFile const& kv_;
+    GeometrySpec const& geo_;
+    ParamsOptions const& opts_;
+    HostParams hp_;
+
+    size_type add_reals(std::vector<double> const& v)
+    {
+        size_type off = hp_.reals.size();
+        hp_.reals.insert(hp_.reals.end(), v.begin(), v.end());
+        return off;
+    }
+    size_type add_ints(std::vector<size_type> const& v)
+    {
+        size_type off = hp_.ints.size();
+        hp_.ints.insert(hp_.ints.end(), v.begin(), v.end());
+        return off;
+    }
+    //! Insert a log-uniform grid from an imported (x, y) vector
+    size_type add_log_grid(std::vector<double> const& x,
+                           std::vector<double> const& y);
+    GenericGrid add_generic(std::vector<double> const& x,
+                            std::vector<double> const& y)
+    {
+        GenericGrid g;
+        g.x = this->add_reals(x);
+        g.y = this->add_reals(y);
+        g.size = static_cast<size_type>(x.size());
+        return g;
+    }
+
+    void build_actions();
+    void build_particles();
+    void build_materials();
+    void build_physics();
+    void build_models();
+    void build_geometry();
+};
+
+size_type Builder::add_log_grid(std::vector<double> const& x,
+                                std::vector<double> const& y)
+{
+    if (x.size() < 2 || x.size() != y.size() || !(x.front() > 0))
+        throw std::runtime_error("invalid log grid");
+    XsGrid g;
+    g.log_front = std::log(x.front());
+    g.log_back = std::log(x.back());
+    g.size = static_cast<size_type>(x.size());
+    g.log_delta = (g.log_back - g.log_front) / (g.size - 1);
+    g.prime_index = invalid_id;
+    g.value = this->add_reals(y);
+    std::vector<double> energies(g.size + 1);
+    for (size_type i = 0; i < g.size; ++i)
+    {
+        energies[i] = std::exp(g.log_front + g.log_delta * i);
+    }
+    energies[g.size] = std::exp(g.log_back);
+    g.energy = this->add_reals(energies);
+    size_type id = static_cast<size_type>(hp_.grids.size());
+    hp_.grids.push_back(g);
+    return id;
+}
+
+//---------------------------------------------------------------------------//
+void Builder::build_actions()
+{
+    // Registration order of CoreParams/PhysicsParams/Runner (action IDs)
+    hp_.action_labels = {"pre-step",
+                         "msc-range",
+                         "eloss-range",
+                         "physics-discrete-select",
+                         "physics-integral-rejected",
+                         "ioni-moller-bhabha",
+                         "brems-sb",
+                         "brems-rel",
+                         "photoel-livermore",
+                         "scat-klein-nishina",
+                         "conv-bethe-heitler",
+                         "annihil-2-gamma",
+                         "physics-failure",
+                         "along-step-general-linear",
+                         "extend-from-primaries",
+                         "initialize-tracks",
+                         "along-step-neutral",
+                         "geo-propagation-limit",
+                         "geo-boundary",
+                         "tracking-cut",
+                         "extend-from-secondaries",
+                         "step-gather-pre",
+                         "step-gather-post"};
+    ParamsData& s = hp_.scalars;
+    s.action_pre_step = 0;
+    s.action_msc_range = 1;
+    s.action_range = 2;
+    s.action_discrete = 3;
+    s.action_integral_rejection = 4;
+    s.model_to_action = 5;
+    s.action_moller_bhabha = 5 + model_moller_bhabha;
+    s.action_seltzer_berger = 5 + model_seltzer_berger;
+    s.action_rel_brems = 5 + model_rel_brems;
+    s.action_livermore_pe = 5 + model_livermore_pe;
+    s.action_klein_nishina = 5 + model_klein_nishina;
+    s.action_bethe_heitler = 5 + model_bethe_heitler;
+    s.action_eplusgg = 5 + model_eplusgg;
+    s.num_models = model_size;
+    s.action_failure = 12;
+    s.action_along_step = 13;
+    s.action_along_step_neutral = 16;
+    s.action_propagation_limit = 17;
+    s.action_boundary = 18;
+    s.action_tracking_cut = 19;
+}
+
+void Builder::build_particles()
+{
+    long npar = kv_.i("particles");
+    ParamsData& s = hp_.scalars;
+    s.electron_id = s.positron_id = s.gamma_id = invalid_id;
+    for (long i = 0; i < npar; ++i)
+    {
+        auto const& v = kv_.get("particle." + std::to_string(i));
+        ParticleRecord pr;
+        pr.pdg = std::stoi(v[1]);
+        pr.mass = std::strtod(v[2].c_str(), nullptr);
+        pr.charge = std::strtod(v[3].c_str(), nullptr);
+        pr.is_antiparticle = pr.pdg < 0;
+        if (pr.pdg == 11)
+            s.electron_id = i;
+        else if (pr.pdg == -11)
+            s.positron_id = i;
+        else if (pr.pdg == 22)
+            s.gamma_id = i;
+        hp_.particles.push_back(pr);
+    }
+    if (s.electron_id != 0 || s.positron_id != 1 || s.gamma_id != 2)
+        throw std::runtime_error("expected particles e-, e+, gamma in order");
+    s.num_particles = static_cast<size_type>(npar);
+}
+
+void Builder::build_materials()
+{
+    long nel = kv_.i("elements");
+    for (long i = 0; i < nel; ++i)
+    {
+        auto p = "element." + std::to_string(i);
+        ElementRecord el;
+        el.z = static_cast<int>(kv_.i(p + ".z"));
+        el.atomic_mass = kv_.d(p + ".a");
+        double const z_real = el.z;
+        el.cbrt_z = std::cbrt(z_real);
+        el.cbrt_zzp = std::cbrt(z_real * (z_real + 1));
+        el.log_z = std::log(z_real);
+        el.coulomb_correction = calc_coulomb_correction(el.z);
+        el.mass_radiation_coeff = calc_mass_rad_coeff(el);
+        hp_.elements.push_back(el);
+    }
+
+    long nmat = kv_.i("materials");
+    double const electron_mass = hp_.particles[hp_.scalars.electron_id].mass;
+    for (long i = 0; i < nmat; ++i)
+    {
+        auto p = "material." + std::to_string(i);
+        hp_.material_labels.push_back(kv_.s(p + ".name"));
+        MaterialRecord m{};
+        m.number_density = kv_.d(p + ".number_density");
+        auto els = kv_.dbl(p + ".elements");
+        auto fr = kv_.dbl(p + ".fractions");
+        if (els.size() > max_elements)
+            throw std::runtime_error("too many elements in material");
+        // Sort components by element ID; renormalize if they don't sum to 1
+        std::vector<std::pair<size_type, double>> comps;
+        double norm = 0;
+        for (std::size_t j = 0; j < els.size(); ++j)
+        {
+            comps.push_back({static_cast<size_type>(els[j]), fr[j]});
+            norm += fr[j];
+        }
+        if (!comps.empty() && !soft_equal(norm, 1.0))
+        {
+            norm = 1 / norm;
+            for (auto& c : comps)
+                c.second *= norm;
+        }
+        std::sort(comps.begin(), comps.end(), [](auto const& a, auto const& b) {
+            return a.first < b.first;
+        });
+        m.num_elements = static_cast<size_type>(comps.size());
+        double avg_amu_mass = 0;
+        double avg_z = 0;
+        double rad_coeff = 0;
+        double log_mean_exc_energy = 0;
+        for (std::size_t j = 0; j < comps.size(); ++j)
+        {
+            m.element[j] = comps[j].first;
+            m.fraction[j] = comps[j].second;
+            ElementRecord const& el = hp_.elements[comps[j].first];
+            double frac_z = comps[j].second * el.z;
+            avg_amu_mass += comps[j].second * el.atomic_mass;
+            avg_z += frac_z;
+            rad_coeff += comps[j].second * el.mass_radiation_coeff;
+            log_mean_exc_energy
+                += frac_z * std::log(mean_excitation_energy(el.z));
+        }
+        m.zeff = avg_z;
+        m.density = m.number_density * avg_amu_mass * constants::atomic_mass;
+        m.electron_density = m.number_density * avg_z;
+        m.rad_length = 1 / (rad_coeff * m.density);
+        log_mean_exc_energy = avg_z > 0 ? log_mean_exc_energy / avg_z
+                                        : -INFINITY;
+        m.log_mean_exc_energy = log_mean_exc_energy;
+        m.mean_exc_energy = std::exp(log_mean_exc_energy);
+        hp_.materials.push_back(m);
+
+        // Urban fluctuation parameters
+        UrbanFluctRecord f;
+        double const avg_zf = m.electron_density / m.number_density;
+        f.oscillator_strength[1] = avg_zf > 2 ? 2 / avg_zf : 0;
+        f.oscillator_strength[0] = 1 - f.oscillator_strength[1];
+        f.binding_energy[1] = 1e-5 * ipow<2>(avg_zf);
+        f.binding_energy[0]
+            = std::pow(m.mean_exc_energy
+                           / std::pow(f.binding_energy[1], f.oscillator_strength[1]),
+                       1 / f.oscillator_strength[0]);
+        f.log_binding_energy[1] = std::log(f.binding_energy[1]);
+        f.log_binding_energy[0] = std::log(f.binding_energy[0]);
+        hp_.fluct.push_back(f);
+
+        // Production cutoffs per particle
+        for (auto const& par : hp_.particles)
+        {
+            auto c = kv_.dbl(p + ".cut." + std::to_string(par.pdg));
+            hp_.cutoffs.push_back(c.at(0));
+        }
+    }
+    (void)electron_mass;
+    hp_.scalars.num_materials = static_cast<size_type>(nmat);
+}
+
+void Builder::build_physics()
+{
+    ParamsData& s = hp_.scalars;
+    // PhysicsParamsOptions defaults and imported EM parameters
+    s.min_range = 1 * constants::millimeter;
+    s.max_step_over_range = 0.2;
+    s.min_eprime_over_e = 0.8;
+    s.linear_loss_limit = kv_.d("em.linear_loss_limit");
+    s.lowest_electron_energy = kv_.d("em.lowest_electron_energy");
+    s.secondary_stack_factor = opts_.secondary_stack_factor;
+    s.enable_fluct = kv_.i("em.energy_loss_fluct") != 0;
+    s.enable_lpm = kv_.i("em.lpm") != 0;
+    bool const integral = kv_.i("em.integral_approach") != 0;
+    s.photoelectric_process = proc_photoelectric;
+    s.annihilation_process = proc_annihilation;
+    s.photoelectric_table_thresh = 0.2;
+    s.livermore_model = model_livermore_pe;
+    s.eplusgg_model = model_eplusgg;
+
+    double const electron_mass = hp_.particles[s.electron_id].mass;
+    double const max_e = INFINITY;
+    size_type const e = s.electron_id, ep = s.positron_id, g = s.gamma_id;
+
+    // Model applicability (hardcoded in the reference's model classes)
+    struct ModelDef
+    {
+        ModelId model;
+        ProcessId process;
+        std::vector<Applic> applic;
+    };
+    double const sb_upper = 1e3;  // seltzer_berger_upper_limit: 1 GeV
+    double const high_limit = 1e8;  // 100 TeV
+    std::vector<ModelDef> models = {
+        {model_moller_bhabha, proc_e_ioni, {{e, 0, 100e6}, {ep, 0, 100e6}}},
+        {model_seltzer_berger, proc_e_brems, {{e, 0, sb_upper}, {ep, 0, sb_upper}}},
+        {model_rel_brems,
+         proc_e_brems,
+         {{e, sb_upper, high_limit}, {ep, sb_upper, high_limit}}},
+        {model_livermore_pe, proc_photoelectric, {{g, 0, max_e}}},
+        {model_klein_nishina, proc_compton, {{g, 0, max_e}}},
+        {model_bethe_heitler, proc_conversion, {{g, 2 * electron_mass, 1e8}}},
+        {model_eplusgg, proc_annihilation, {{ep, 0, 1e8}}},
+    };
+
+    // particle -> process -> [(lower, upper, model)]
+    std::vector<std::map<size_type, std::vector<std::tuple<double, double, size_type>>>>
+        particle_models(hp_.particles.size());
+    for (auto const& md : models)
+    {
+        for (auto const& a : md.applic)
+        {
+            particle_models[a.particle][md.process].push_back(
+                {a.lower, a.upper, md.model});
+        }
+    }
+
+    // Which processes use the integral approach
+    auto uses_integral = [integral](size_type proc) {
+        return integral
+               && (proc == proc_e_ioni || proc == proc_e_brems
+                   || proc == proc_annihilation);
+    };
+    // Imported table names per process
+    auto process_name = [](size_type proc) -> std::string {
+        switch (proc)
+        {
+            case proc_e_ioni: return "e_ioni";
+            case proc_e_brems: return "e_brems";
+            case proc_photoelectric: return "photoelectric";
+            case proc_compton: return "compton";
+            case proc_conversion: return "conversion";
+            case proc_annihilation: return "annihilation";
+        }
+        return "";
+    };
+
+    size_type const nmat = s.num_materials;
+    for (size_type pid = 0; pid < hp_.particles.size(); ++pid)
+    {
+        ProcessGroup pg{};
+        pg.eloss_process = invalid_id;
+        for (int v = 0; v < vgt_size; ++v)
+            pg.grid_table[v] = invalid_id;
+        auto const& procs = particle_models[pid];
+        if (procs.size() > max_processes)
+            throw std::runtime_error("too many processes");
+        pg.num_processes = static_cast<size_type>(procs.size());
+        std::vector<std::vector<size_type>> tables(
+            vgt_size, std::vector<size_type>(procs.size() * nmat, invalid_id));
+        bool any_table[vgt_size] = {false, false, false};
+        size_type ppid = 0;
+        int pdg = hp_.particles[pid].pdg;
+        for (auto const& [proc, mlist_in] : procs)
+        {
+            auto mlist = mlist_in;
+            std::sort(mlist.begin(), mlist.end());
+            pg.process[ppid] = proc;
+            std::vector<double> egrid{std::get<0>(mlist.front())};
+            std::vector<size_type> mids;
+            for (auto const& m : mlist)
+            {
+                if (egrid.back() != std::get<0>(m))
+                    throw std::runtime_error("noncontiguous model energies");
+                egrid.push_back(std::get<1>(m));
+                mids.push_back(std::get<2>(m));
+            }
+            pg.model_energy[ppid] = this->add_reals(egrid);
+            pg.model_ids[ppid] = this->add_ints(mids);
+            pg.num_models[ppid] = static_cast<size_type>(mids.size());
+            pg.use_integral[ppid] = uses_integral(proc);
+
+            std::vector<double> energy_max_xs(nmat, 0);
+            std::string base = "table." + std::to_string(pdg) + "."
+                               + process_name(proc) + ".";
+            for (size_type mat = 0; mat < nmat; ++mat)
+            {
+                std::string ms = "." + std::to_string(mat);
+                size_type macro = invalid_id;
+                if (proc == proc_annihilation)
+                {
+                    pg.has_at_rest = true;
+                }
+                else if (kv_.has(base + "lambda" + ms + ".x"))
+                {
+                    macro = this->add_log_grid(kv_.dbl(base + "lambda" + ms + ".x"),
+                                               kv_.dbl(base + "lambda" + ms + ".y"));
+                    XsGrid const& xg = hp_.grids[macro];
+                    // Discrete interaction at rest if xs(E=0) > 0
+                    pg.has_at_rest |= hp_.reals[xg.value] > 0;
+                    if (pg.use_integral[ppid])
+                    {
+                        double xs_max = 0;
+                        double e_max = 0;
+                        for (size_type i = 0; i < xg.size; ++i)
+                        {
+                            double xs = hp_.reals[xg.value + i];
+                            if (xs > xs_max)
+                            {
+                                xs_max = xs;
+                                e_max = hp_.reals[xg.energy + i];
+                            }
+                        }
+                        energy_max_xs[mat] = e_max;
+                    }
+                }
+                tables[vgt_macro_xs][ppid * nmat + mat] = macro;
+                if (macro != invalid_id)
+                    any_table[vgt_macro_xs] = true;
+                if (kv_.has(base + "dedx" + ms + ".x")
+                    && kv_.has(base + "range" + ms + ".x"))
+                {
+                    tables[vgt_energy_loss][ppid * nmat + mat] = this->add_log_grid(
+                        kv_.dbl(base + "dedx" + ms + ".x"),
+                        kv_.dbl(base + "dedx" + ms + ".y"));
+                    tables[vgt_range][ppid * nmat + mat] = this->add_log_grid(
+                        kv_.dbl(base + "range" + ms + ".x"),
+                        kv_.dbl(base + "range" + ms + ".y"));
+                    any_table[vgt_energy_loss] = any_table[vgt_range] = true;
+                    pg.eloss_process = ppid;
+                }
+            }
+            pg.energy_max_xs[ppid]
+                = pg.use_integral[ppid] ? this->add_reals(energy_max_xs) : invalid_id;
+            ++ppid;
+        }
+        for (int v = 0; v < vgt_size; ++v)
+        {
+            if (any_table[v])
+                pg.grid_table[v] = this->add_ints(tables[v]);
+        }
+        hp_.groups.push_back(pg);
+    }
+}
+
+void Builder::build_models()
+{
+    // Seltzer-Berger tables per element, with the argmax over reduced energy
+    for (auto const& el : hp_.elements)
+    {
+        std::string z = std::to_string(el.z);
+        auto x = kv_.dbl("sb." + z + ".x");
+        auto y = kv_.dbl("sb." + z + ".y");
+        auto v = kv_.dbl("sb." + z + ".value");
+        if (v.size() != x.size() * y.size())
+            throw std::runtime_error("bad SB table size");
+        SBElementTable t;
+        t.x = this->add_reals(x);
+        t.nx = static_cast<size_type>(x.size());
+        t.y = this->add_reals(y);
+        t.ny = static_cast<size_type>(y.size());
+        t.values = this->add_reals(v);
+        std::vector<size_type> argmax(x.size());
+        for (std::size_t i = 0; i < x.size(); ++i)
+        {
+            auto first = v.begin() + i * y.size();
+            argmax[i] = static_cast<size_type>(
+                std::max_element(first, first + y.size()) - first);
+        }
+        t.argmax = this->add_ints(argmax);
+        hp_.sb_tables.push_back(t);
+    }
+
+    // Livermore photoelectric data per element
+    for (auto const& el : hp_.elements)
+    {
+        std::string pz = "livermore." + std::to_string(el.z);
+        LivermoreElement le{};
+        if (kv_.has(pz + ".xs_lo.x"))
+        {
+            le.xs_lo = this->add_generic(kv_.dbl(pz + ".xs_lo.x"),
+                                         kv_.dbl(pz + ".xs_lo.y"));
+        }
+        le.xs_hi = this->add_generic(kv_.dbl(pz + ".xs_hi.x"),
+                                     kv_.dbl(pz + ".xs_hi.y"));
+        auto th = kv_.dbl(pz + ".thresh");
+        le.thresh_lo = th[0];
+        le.thresh_hi = th[1];
+        le.shells = static_cast<size_type>(hp_.lv_shells.size());
+        long nsh = kv_.i(pz + ".shells");
+        le.num_shells = static_cast<size_type>(nsh);
+        for (long s = 0; s < nsh; ++s)
+        {
+            std::string ps = pz + ".shell." + std::to_string(s);
+            LivermoreShell sh{};
+            sh.binding_energy = kv_.d(ps + ".binding");
+            auto lo = kv_.dbl(ps + ".param_lo");
+            auto hi = kv_.dbl(ps + ".param_hi");
+            for (int i = 0; i < 6; ++i)
+            {
+                sh.param[0][i] = lo.at(i);
+                sh.param[1][i] = hi.at(i);
+            }
+            sh.xs = this->add_generic(kv_.dbl(ps + ".energy"), kv_.dbl(ps + ".xs"));
+            hp_.lv_shells.push_back(sh);
+        }
+        hp_.lv_elements.push_back(le);
+    }
+}
+
+void Builder::build_geometry()
+{
+    // Surfaces: world box faces, then each box's faces in insertion order,
+    // deduplicated against existing planes (first inserted wins). Each box
+    // face is placed at center +/- half-width, as a translated box.
+    auto add_plane = [this](int axis, double pos) -> size_type {
+        for (size_type i = 0; i < hp_.planes.size(); ++i)
+        {
+            auto const& pl = hp_.planes[i];
+            if (pl.axis == axis
+                && std::fabs(pl.position - pos)
+                       <= 1e-8 * std::max(1.0, std::fabs(pos)))
+            {
+                return i;
+            }
+        }
+        hp_.planes.push_back({axis, pos});
+        return static_cast<size_type>(hp_.planes.size() - 1);
+    };
+    auto box_faces = [&](double const* lo, double const* hi, size_type* faces) {
+        for (int ax = 0; ax < 3; ++ax)
+        {
+            double half = (hi[ax] - lo[ax]) / 2;
+            double center = (hi[ax] + lo[ax]) / 2;
+            faces[2 * ax] = add_plane(ax, -half + center);
+            faces[2 * ax + 1] = add_plane(ax, half + center);
+        }
+    };
+
+    GeoParams& g = hp_.scalars.geo;
+    size_type world[6];
+    box_faces(geo_.world_lo, geo_.world_hi, world);
+    for (int f = 0; f < 6; ++f)
+    {
+        g.world_faces[f] = world[f];
+        g.world_sense[f] = (f % 2 == 0) ? 1 : -1;
+    }
+
+    // Volumes: exterior (0), boxes (1..n), background (n+1)
+    size_type const nbox = static_cast<size_type>(geo_.boxes.size());
+    hp_.boxes.resize(nbox + 2);
+    hp_.volume_labels.push_back("[EXTERIOR]");
+    hp_.volume_material.push_back(invalid_id);
+    for (size_type b = 0; b < nbox; ++b)
+    {
+        BoxSpec const& spec = geo_.boxes[b];
+        size_type faces[6];
+        box_faces(spec.lo, spec.hi, faces);
+        // Faces sorted by surface ID, senses: lower planes need pos >= plane
+        std::vector<std::pair<size_type, std::int8_t>> fs;
+        for (int f = 0; f < 6; ++f)
+            fs.push_back({faces[f], static_cast<std::int8_t>(f % 2 == 0 ? 1 : -1)});
+        std::sort(fs.begin(), fs.end());
+        BoxVolume& bv = hp_.boxes[b + 1];
+        for (int f = 0; f < 6; ++f)
+        {
+            bv.faces[f] = fs[f].first;
+            bv.inside_sense[f] = fs[f].second;
+        }
+        bv.material = spec.material;
+        hp_.volume_labels.push_back(spec.label);
+        hp_.volume_material.push_back(spec.material);
+    }
+    hp_.volume_labels.push_back("world");
+    hp_.volume_material.push_back(geo_.background_material);
+
+    // Box lookup along the stack axis requires the lower face in slot 4
+    for (size_type b = 1; b <= nbox; ++b)
+    {
+        BoxVolume const& bv = hp_.boxes[b];
+        auto const& pl = hp_.planes[bv.faces[4]];
+        if (pl.axis != geo_.stack_axis || bv.inside_sense[4] != 1)
+            throw std::runtime_error("boxes must be layered along the stack axis");
+        if (b > 1
+            && !(hp_.planes[hp_.boxes[b - 1].faces[4]].position < pl.position))
+            throw std::runtime_error("boxes must be sorted along the stack axis");
+    }
+
+    // Connectivity: volumes owning each surface
+    size_type const nsurf = static_cast<size_type>(hp_.planes.size());
+    std::vector<std::vector<size_type>> conn(nsurf);
+    for (int f = 0; f < 6; ++f)
+        conn[world[f]].push_back(0);
+    for (size_type b = 1; b <= nbox; ++b)
+        for (int f = 0; f < 6; ++f)
+            conn[hp_.boxes[b].faces[f]].push_back(b);
+    hp_.neighbor_offset.push_back(0);
+    for (auto const& c : conn)
+    {
+        hp_.neighbors.insert(hp_.neighbors.end(), c.begin(), c.end());
+        hp_.neighbor_offset.push_back(static_cast<size_type>(hp_.neighbors.size()));
+    }
+
+    // Detectors: every box, in order
+    hp_.volume_detector.assign(nbox + 2, invalid_id);
+    for (size_type b = 1; b <= nbox; ++b)
+    {
+        hp_.volume_detector[b] = b - 1;
+        hp_.detector_labels.push_back(geo_.boxes[b - 1].label);
+    }
+
+    g.num_surfaces = nsurf;
+    g.num_volumes = nbox + 2;
+    g.exterior = 0;
+    g.background = nbox + 1;
+    g.stack_axis = geo_.stack_axis;
+    g.tol_rel = 1.5e-8;
+    g.tol_abs = 1.5e-8;
+    hp_.scalars.num_detectors = nbox;
+}
+
+HostParams Builder::build()
+{
+    if (kv_.s("format") != "gbx-physics-1")
+        throw std::runtime_error("unsupported physics file format");
+    this->build_actions();
+    this->build_particles();
+    this->build_materials();
+    this->build_physics();
+    this->build_models();
+    this->build_geometry();
+    for (auto const& b : geo_.boxes)
+    {
+        if (b.material >= hp_.materials.size())
+            throw std::runtime_error("box material out of range");
+    }
+    return std::move(hp_);
+}
+
+}  // namespace
+
+//---------------------------------------------------------------------------//
+GeometrySpec make_calorimeter_geometry(int num_layers,
+                                       double absorber,
+                                       double gap,
+                                       double half_xy)
+{
+    GeometrySpec g;
+    g.name = "calo";
+    double const pitch = absorber + gap;
+    g.world_lo[0] = g.world_lo[1] = -30;
+    g.world_hi[0] = g.world_hi[1] = 30;
+    g.world_lo[2] = -10;
+    g.world_hi[2] = 50;
+    g.background_material = 0;
+    g.stack_axis = 2;
+    for (int k = 0; k < num_layers; ++k)
+    {
+        double z0 = k * pitch;
+        double z1 = z0 + absorber;
+        double z2 = (k + 1) * pitch;
+        BoxSpec pb{"pb_" + std::to_string(k),
+                   {-half_xy, -half_xy, z0},
+                   {half_xy, half_xy, z1},
+                   1};
+        BoxSpec ar{"lar_" + std::to_string(k),
+                   {-half_xy, -half_xy, z1},
+                   {half_xy, half_xy, z2},
+                   2};
+        g.boxes.push_back(pb);
+        g.boxes.push_back(ar);
+    }
+    return g;
+}
+
+HostParams build_params(std::string const& physics_path,
+                        GeometrySpec const& geo,
+                        ParamsOptions const& opts)
+{
+    KvFile kv(physics_path);
+    Builder b(kv, geo, opts);
+    return b.build();
+}
+
+ParamsData make_host_view(HostParams const& hp)
+{
+    ParamsData p = hp.scalars;
+    p.reals = hp.reals.data();
+    p.ints = hp.ints.data();
+    p.particles = hp.particles.data();
+    p.materials = hp.materials.data();
+    p.elements = hp.elements.data();
+    p.fluct = hp.fluct.data();
+    p.cutoff_energy = hp.cutoffs.data();
+    p.process_groups = hp.groups.data();
+    p.grids = hp.grids.data();
+    p.livermore_elements = hp.lv_elements.data();
+    p.livermore_shells = hp.lv_shells.data();
+    p.sb_tables = hp.sb_tables.data();
+    p.geo.planes = hp.planes.data();
+    p.geo.boxes = hp.boxes.data();
+    p.geo.neighbor_offset = hp.neighbor_offset.data();
+    p.geo.neighbors = hp.neighbors.data();
+    p.geo.volume_material = hp.volume_material.data();
+    p.geo.volume_detector = hp.volume_detector.data();
+    return p;
+}
+
+}  // namespace gbx

@@ -1,0 +1,336 @@
+// CPU restatement of the reference's host stepping loop, used (1) to check
+// the per-slot action code of the GB300 path against the reference itself on
+// the CPU, and (2) as the timed CPU baseline on machines where the reference
+// cannot be built.
+//
+// The loop follows Stepper<MemSpace::host>::operator()
+// (src/celeritas/global/Stepper.cc:125-168) and ActionSequence::step
+// (src/celeritas/global/ActionSequence.cc:77-138): actions run in
+// (StepActionOrder, ActionId) order, each over all track slots in slot order.
+// The per-slot bodies are the GB300 path's host+device action functions
+// (celeritas_gb300/csrc/gbx/Actions.hh, TrackInit.hh) compiled for the host;
+// the global steps (vacancy compaction, secondary-count scan, initializer
+// bookkeeping) are restated here sequentially
+// (src/celeritas/track/detail/TrackInitAlgorithms.cc).
+//
+// This is test and baseline infrastructure, never the shipped GB300 path.
+//
+// Usage:
+//   port_stepper run <physics.txt> calo <primaries.txt> <slots> <seed>
+//                    [--steps N] [--quiet] [--threads T --events E]
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../celeritas_gb300/csrc/gbx/TrackInit.hh"
+#include "../../celeritas_gb300/csrc/host/HostParams.hh"
+#include "../../celeritas_gb300/csrc/host/HostState.hh"
+
+using namespace gbx;
+
+namespace
+{
+struct StepCounts
+{
+    size_type generated{0};
+    size_type queued{0};
+    size_type active{0};
+    size_type alive{0};
+    explicit operator bool() const { return queued > 0 || alive > 0; }
+};
+
+class PortStepper
+{
+  public:
+    PortStepper(HostParams const& hp,
+                size_type num_slots,
+                unsigned int seed,
+                size_type max_events)
+        : params_(make_host_view(hp))
+        , state_(num_slots,
+                 std::max<size_type>(1u << 20, 4 * num_slots),
+                 max_events,
+                 static_cast<size_type>(hp.scalars.secondary_stack_factor
+                                        * num_slots),
+                 hp.scalars.num_detectors,
+                 seed)
+        , action_labels_(hp.action_labels)
+    {
+    }
+
+    StepCounts operator()(std::vector<TrackInitializer> const& primaries)
+    {
+        state_.primaries = primaries;
+        return this->step(true);
+    }
+    StepCounts operator()() { return this->step(false); }
+
+    std::vector<double> const& edep() const { return state_.calo_edep; }
+
+    //! Print the state of every non-inactive slot
+    void trace(size_type iter) const
+    {
+        HostState const& s = state_;
+        for (size_type i = 0; i < s.size; ++i)
+        {
+            if (s.status[i] == status_inactive)
+                continue;
+            std::printf("trace %u %u st=%d pid=%u E=%.17g pos=(%.17g,%.17g,%.17g) "
+                        "dir=(%.17g,%.17g,%.17g) vol=%u act=%d len=%.17g mfp=%.17g "
+                        "edep=%.17g nsec=%u\n",
+                        iter,
+                        i,
+                        int(s.status[i]),
+                        s.particle_id[i],
+                        double(s.energy[i]),
+                        s.pos[0][i],
+                        s.pos[1][i],
+                        s.pos[2][i],
+                        s.dir[0][i],
+                        s.dir[1][i],
+                        s.dir[2][i],
+                        s.volume[i],
+                        int(s.post_step_action[i]),
+                        s.step_length[i],
+                        double(s.interaction_mfp[i]),
+                        double(s.energy_deposition[i]),
+                        s.secondaries_count[i]);
+        }
+    }
+
+  private:
+    ParamsData params_;
+    HostState state_;
+    std::vector<std::string> action_labels_;
+
+    StepCounts step(bool with_primaries)
+    {
+        ParamsData const& p = params_;
+        StateData s = state_.view();
+        Counters& c = state_.counters;
+        size_type const n = s.size;
+        c.num_generated = 0;
+
+        // extend-from-primaries (generate)
+        if (with_primaries)
+        {
+            size_type np = static_cast<size_type>(state_.primaries.size());
+            c.num_initializers += np;
+            if (c.num_initializers > s.initializer_capacity)
+                throw std::runtime_error("initializer capacity exceeded");
+            for (size_type i = 0; i < np; ++i)
+                process_primary(s, c.num_initializers, np, i);
+            c.num_generated += np;
+            std::fill(state_.parents.begin(), state_.parents.end(), invalid_id);
+        }
+        // initialize-tracks (start)
+        {
+            size_type num_new = std::min(c.num_vacancies, c.num_initializers);
+            for (size_type i = 0; i < num_new; ++i)
+                init_track(p, s, c, i);
+            c.num_initializers -= num_new;
+            c.num_vacancies -= num_new;
+            c.num_active = n - c.num_vacancies;
+        }
+        size_type const active = c.num_active;
+        // pre-step (pre): thread 0 clears the secondary stack
+        c.secondary_stack_size = 0;
+        for (size_type i = 0; i < n; ++i)
+            pre_step(p, s, i);
+        // step-gather-pre (user_pre)
+        for (size_type i = 0; i < n; ++i)
+            gather_pre(p, s, i);
+        // along-step-general-linear, along-step-neutral (along)
+        for (size_type i = 0; i < n; ++i)
+            along_step(p, s, i);
+        // physics-discrete-select (pre_post)
+        for (size_type i = 0; i < n; ++i)
+            discrete_select(p, s, i);
+        // models (post), in action-ID order
+        for (size_type a = p.model_to_action; a < p.model_to_action + p.num_models;
+             ++a)
+        {
+            for (size_type i = 0; i < n; ++i)
+                interact(p, s, i, a);
+        }
+        for (size_type i = 0; i < n; ++i)
+            boundary_cross(p, s, i);
+        for (size_type i = 0; i < n; ++i)
+            tracking_cut(p, s, i);
+        // step-gather-post -> calorimeter tally (user_post)
+        for (size_type i = 0; i < n; ++i)
+        {
+            if (s.status[i] == status_inactive)
+                continue;
+            size_type det = s.detector[i];
+            if (det != invalid_id)
+                s.calo_edep[det] += s.energy_deposition[i];
+        }
+        // extend-from-secondaries (end)
+        {
+            std::vector<char> vacant(n);
+            for (size_type i = 0; i < n; ++i)
+            {
+                bool v;
+                size_type cnt;
+                locate_alive(s, i, &v, &cnt);
+                vacant[i] = v;
+                s.secondary_counts[i] = cnt;
+            }
+            size_type nv = 0;
+            for (size_type i = 0; i < n; ++i)
+            {
+                if (vacant[i])
+                    s.vacancies[nv++] = i;
+            }
+            c.num_vacancies = nv;
+            size_type total = 0;
+            for (size_type i = 0; i < n; ++i)
+            {
+                size_type cnt = s.secondary_counts[i];
+                s.secondary_counts[i] = total;
+                total += cnt;
+            }
+            c.num_secondaries = total;
+            c.num_initializers += total;
+            if (c.num_initializers > s.initializer_capacity)
+                throw std::runtime_error("initializer capacity exceeded");
+            c.num_alive = n - c.num_vacancies;
+            for (size_type i = 0; i < n; ++i)
+                process_secondaries(p, s, c, i, s.secondary_counts[i]);
+        }
+        StepCounts r;
+        r.generated = c.num_generated;
+        r.active = active;
+        r.alive = c.num_alive;
+        r.queued = c.num_initializers;
+        return r;
+    }
+};
+
+std::vector<TrackInitializer> load_primaries(std::string const& path)
+{
+    std::ifstream in(path);
+    if (!in)
+        throw std::runtime_error("cannot open " + path);
+    std::vector<TrackInitializer> result;
+    int pdg;
+    double e, x, y, z, dx, dy, dz, t;
+    long ev;
+    while (in >> pdg >> e >> x >> y >> z >> dx >> dy >> dz >> t >> ev)
+    {
+        TrackInitializer ti{};
+        ti.particle_id = pdg == 11 ? 0 : (pdg == -11 ? 1 : 2);
+        ti.energy = e;
+        ti.pos = {x, y, z};
+        ti.dir = {dx, dy, dz};
+        ti.time = t;
+        ti.event_id = static_cast<size_type>(ev);
+        result.push_back(ti);
+    }
+    return result;
+}
+
+int run(int argc, char** argv)
+{
+    if (argc < 7)
+    {
+        std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
+                     "<seed> [--steps N] [--quiet]\n";
+        return 2;
+    }
+    std::string phys = argv[2], geo = argv[3], prim = argv[4];
+    size_type slots = std::stoul(argv[5]);
+    unsigned int seed = std::stoul(argv[6]);
+    size_type max_steps = static_cast<size_type>(-1);
+    bool quiet = false;
+    bool trace = false;
+    for (int i = 7; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--trace")
+            trace = true;
+        else if (a == "--steps")
+            max_steps = std::stoul(argv[++i]);
+        else if (a == "--quiet")
+            quiet = true;
+    }
+    if (geo != "calo")
+        throw std::runtime_error("unknown geometry " + geo);
+    HostParams hp
+        = build_params(phys, make_calorimeter_geometry(), ParamsOptions{});
+    auto primaries = load_primaries(prim);
+    size_type max_event = 0;
+    for (auto const& pr : primaries)
+        max_event = std::max(max_event, pr.event_id);
+
+    if (!quiet)
+    {
+        for (std::size_t i = 0; i < hp.action_labels.size(); ++i)
+            std::printf("action %zu %s\n", i, hp.action_labels[i].c_str());
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    PortStepper step(hp, slots, seed, max_event + 1);
+    StepCounts counts = step(primaries);
+    size_type iter = 0;
+    if (trace)
+        step.trace(iter);
+    unsigned long long track_steps = counts.active;
+    if (!quiet)
+        std::printf("step %u %u %u %u %u\n",
+                    iter,
+                    counts.generated,
+                    counts.queued,
+                    counts.active,
+                    counts.alive);
+    while (counts && ++iter < max_steps)
+    {
+        counts = step();
+        if (trace)
+            step.trace(iter);
+        track_steps += counts.active;
+        if (!quiet)
+            std::printf("step %u %u %u %u %u\n",
+                        iter,
+                        counts.generated,
+                        counts.queued,
+                        counts.active,
+                        counts.alive);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    std::printf("total_steps %llu iterations %u\n", track_steps, iter + 1);
+    std::printf("seconds %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+    auto const& edep = step.edep();
+    for (std::size_t i = 0; i < edep.size(); ++i)
+        std::printf("edep %s %.17g\n", hp.detector_labels[i].c_str(), edep[i]);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc < 2)
+    {
+        std::cerr << "usage: port_stepper run ...\n";
+        return 2;
+    }
+    try
+    {
+        std::string mode = argv[1];
+        if (mode == "run")
+            return run(argc, argv);
+    }
+    catch (std::exception const& e)
+    {
+        std::cerr << "error: " << e.what() << "\n";
+        return 1;
+    }
+    return 2;
+}

@@ -725,6 +725,51 @@ int dump_geo(int argc, char** argv)
                     static_cast<std::size_t>(i),
                     static_cast<int>(host.surface_types[ItemId<SurfaceType>(i)]));
     }
+    {
+        auto const& unit = host.simple_units[SimpleUnitId{0}];
+        std::printf("background %u\n", unit.background.unchecked_get());
+        for (auto i : range(unit.volumes.size()))
+        {
+            auto const& vr
+                = host.volume_records[unit.volumes[LocalVolumeId(i)]];
+            std::printf("volrec %zu flags %d maxisect %d faces",
+                        static_cast<std::size_t>(i),
+                        static_cast<int>(vr.flags),
+                        static_cast<int>(vr.max_intersections));
+            for (auto f : vr.faces)
+            {
+                std::printf(" %u", host.local_surface_ids[f].unchecked_get());
+            }
+            std::printf(" logic");
+            for (auto l : vr.logic)
+            {
+                std::printf(" %d", static_cast<int>(host.logic_ints[l]));
+            }
+            std::printf("\n");
+        }
+        for (auto s : range(unit.surfaces.types.size()))
+        {
+            auto const& surfs = unit.surfaces;
+            auto t = host.surface_types[surfs.types[s]];
+            auto off = host.real_ids[surfs.data_offsets[s]];
+            std::printf("surf %zu type %d data %.17g %.17g\n",
+                        static_cast<std::size_t>(s),
+                        static_cast<int>(t),
+                        host.reals[off],
+                        host.reals[off + 1]);
+        }
+        for (auto s : range(unit.connectivity.size()))
+        {
+            auto const& conn
+                = host.connectivity_records[unit.connectivity[s]];
+            std::printf("conn %zu", static_cast<std::size_t>(s));
+            for (auto v : conn.neighbors)
+            {
+                std::printf(" %u", host.local_volume_ids[v].unchecked_get());
+            }
+            std::printf("\n");
+        }
+    }
     std::printf("reals %zu\n", static_cast<std::size_t>(host.reals.size()));
     for (auto i : range(host.reals.size()))
     {
