@@ -1,0 +1,268 @@
+"""GB300-native electromagnetic-shower stepping loop.
+
+Python front end over the C ABI of ``include/celeritas_gb300.h``. The compute
+path is the in-tree CUDA library (``_build/libceleritas_gb300.so``, sm_103a);
+there is no CPU fallback: every call that needs the device raises if the
+library or a GPU is unavailable.
+
+The classes mirror the reference's host API for the stepping loop:
+``Params`` <-> ``celeritas::CoreParams`` (built as in celer-sim's
+``Runner::build_core_params``), ``Stepper`` <-> ``celeritas::Stepper`` with
+``step(primaries)``, ``step()``, ``run()``, ``kill_active()``, and
+``Primary``/``StepResult`` <-> ``celeritas::Primary``/``StepperResult``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .build import lib_path
+
+PACKAGE_DIR = os.path.dirname(os.path.abspath(__file__))
+DATA_DIR = os.path.join(PACKAGE_DIR, "data")
+
+
+class GbxError(RuntimeError):
+    """Error reported by the C ABI."""
+
+
+class _Primary(ctypes.Structure):
+    _fields_ = [
+        ("pdg", ctypes.c_int),
+        ("energy", ctypes.c_double),
+        ("pos", ctypes.c_double * 3),
+        ("dir", ctypes.c_double * 3),
+        ("time", ctypes.c_double),
+        ("event_id", ctypes.c_uint),
+    ]
+
+
+class _StepResult(ctypes.Structure):
+    _fields_ = [
+        ("generated", ctypes.c_uint),
+        ("queued", ctypes.c_uint),
+        ("active", ctypes.c_uint),
+        ("alive", ctypes.c_uint),
+    ]
+
+
+@dataclass(frozen=True)
+class StepResult:
+    generated: int
+    queued: int
+    active: int
+    alive: int
+
+    def __bool__(self):
+        return self.queued > 0 or self.alive > 0
+
+
+_lib = None
+
+# (name, restype, argtypes) for every entry point of include/celeritas_gb300.h
+_PROTOTYPES = [
+    ("gbx_last_error", ctypes.c_char_p, []),
+    ("gbx_params_create", ctypes.c_int,
+     [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbx_params_destroy", None, [ctypes.c_void_p]),
+    ("gbx_params_num_actions", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    ("gbx_params_action_label", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_uint, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gbx_params_num_detectors", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    ("gbx_params_detector_label", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_uint, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gbx_stepper_create", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbx_stepper_destroy", None, [ctypes.c_void_p]),
+    ("gbx_stepper_step", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(_Primary), ctypes.c_size_t, ctypes.POINTER(_StepResult)]),
+    ("gbx_stepper_run", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(_StepResult),
+      ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint)]),
+    ("gbx_stepper_launch_action", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint]),
+    ("gbx_stepper_insert_primaries", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(_Primary), ctypes.c_size_t]),
+    ("gbx_stepper_kill_active", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_synchronize", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_energy_deposition", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t]),
+    ("gbx_stepper_clear_energy_deposition", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_copy_state", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]),
+    ("gbx_stepper_state_info", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
+      ctypes.POINTER(ctypes.c_size_t)]),
+]
+
+EXPORTED_SYMBOLS = [name for name, _, _ in _PROTOTYPES]
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load the in-tree CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or lib_path()
+    if not os.path.exists(path):
+        raise GbxError(
+            f"GB300 library not built ({path}); run "
+            "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(path)
+    for name, restype, argtypes in _PROTOTYPES:
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = _lib.gbx_last_error().decode()
+        raise GbxError(msg or f"GB300 call failed with status {rc}")
+
+
+def physics_file(problem: str) -> str:
+    """Path of a committed synthetic physics input ("calo" or "cms")."""
+    return os.path.join(DATA_DIR, f"{problem}.physics.txt")
+
+
+class Params:
+    """Problem parameters on the device (celeritas::CoreParams)."""
+
+    def __init__(self, physics: str, geometry: str = "calo"):
+        lib = load_library()
+        handle = ctypes.c_void_p()
+        _check(lib.gbx_params_create(physics.encode(), geometry.encode(), ctypes.byref(handle)))
+        self._handle = handle
+        self.geometry = geometry
+
+    def __del__(self):
+        if getattr(self, "_handle", None) and _lib is not None:
+            _lib.gbx_params_destroy(self._handle)
+            self._handle = None
+
+    @property
+    def handle(self):
+        return self._handle
+
+    def action_labels(self) -> list[str]:
+        n = ctypes.c_uint()
+        _check(_lib.gbx_params_num_actions(self._handle, ctypes.byref(n)))
+        out = []
+        buf = ctypes.create_string_buffer(128)
+        for i in range(n.value):
+            _check(_lib.gbx_params_action_label(self._handle, i, buf, 128))
+            out.append(buf.value.decode())
+        return out
+
+    def detector_labels(self) -> list[str]:
+        n = ctypes.c_uint()
+        _check(_lib.gbx_params_num_detectors(self._handle, ctypes.byref(n)))
+        out = []
+        buf = ctypes.create_string_buffer(128)
+        for i in range(n.value):
+            _check(_lib.gbx_params_detector_label(self._handle, i, buf, 128))
+            out.append(buf.value.decode())
+        return out
+
+
+def make_primary_array(primaries: np.ndarray):
+    """Convert a structured primary array (see primaries.PRIMARY_DTYPE)."""
+    n = len(primaries)
+    arr = (_Primary * max(n, 1))()
+    for i in range(n):
+        p = primaries[i]
+        arr[i].pdg = int(p["pdg"])
+        arr[i].energy = float(p["energy"])
+        for k in range(3):
+            arr[i].pos[k] = float(p["pos"][k])
+            arr[i].dir[k] = float(p["dir"][k])
+        arr[i].time = float(p["time"])
+        arr[i].event_id = int(p["event"])
+    return arr, n
+
+
+class Stepper:
+    """Device track state and step loop (celeritas::Stepper<MemSpace::device>)."""
+
+    def __init__(self, params: Params, num_track_slots: int, seed: int = 0,
+                 use_graph: bool = True):
+        self.params = params
+        handle = ctypes.c_void_p()
+        _check(_lib.gbx_stepper_create(params.handle, num_track_slots, seed,
+                                       int(use_graph), ctypes.byref(handle)))
+        self._handle = handle
+        self.num_track_slots = num_track_slots
+
+    def __del__(self):
+        if getattr(self, "_handle", None) and _lib is not None:
+            _lib.gbx_stepper_destroy(self._handle)
+            self._handle = None
+
+    @staticmethod
+    def _result(r: _StepResult) -> StepResult:
+        return StepResult(r.generated, r.queued, r.active, r.alive)
+
+    def step(self, primaries: np.ndarray | None = None) -> StepResult:
+        res = _StepResult()
+        if primaries is not None and len(primaries):
+            arr, n = make_primary_array(primaries)
+            _check(_lib.gbx_stepper_step(self._handle, arr, n, ctypes.byref(res)))
+        else:
+            _check(_lib.gbx_stepper_step(self._handle, None, 0, ctypes.byref(res)))
+        return self._result(res)
+
+    def run(self, max_steps: int = 1_000_000, batch: int = 32) -> list[StepResult]:
+        """Step until empty; per-step results (host reads every 'batch' steps)."""
+        cap = max_steps
+        out = (_StepResult * cap)()
+        n = ctypes.c_uint()
+        _check(_lib.gbx_stepper_run(self._handle, max_steps, batch, out, cap, ctypes.byref(n)))
+        return [self._result(out[i]) for i in range(min(n.value, cap))]
+
+    def insert_primaries(self, primaries: np.ndarray):
+        arr, n = make_primary_array(primaries)
+        _check(_lib.gbx_stepper_insert_primaries(self._handle, arr, n))
+
+    def launch_action(self, action_id: int):
+        _check(_lib.gbx_stepper_launch_action(self._handle, action_id))
+
+    def synchronize(self):
+        _check(_lib.gbx_stepper_synchronize(self._handle))
+
+    def kill_active(self):
+        _check(_lib.gbx_stepper_kill_active(self._handle))
+
+    def energy_deposition(self) -> np.ndarray:
+        n = len(self.params.detector_labels())
+        out = np.zeros(n, dtype=np.float64)
+        _check(_lib.gbx_stepper_energy_deposition(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n))
+        return out
+
+    def clear_energy_deposition(self):
+        _check(_lib.gbx_stepper_clear_energy_deposition(self._handle))
+
+    def state_info(self, field: str) -> tuple[int, int]:
+        eb = ctypes.c_size_t()
+        cnt = ctypes.c_size_t()
+        _check(_lib.gbx_stepper_state_info(self._handle, field.encode(),
+                                           ctypes.byref(eb), ctypes.byref(cnt)))
+        return eb.value, cnt.value
+
+    def get_state(self, field: str, dtype) -> np.ndarray:
+        eb, cnt = self.state_info(field)
+        out = np.empty(eb * cnt, dtype=np.uint8)
+        _check(_lib.gbx_stepper_copy_state(self._handle, field.encode(),
+                                           out.ctypes.data_as(ctypes.c_void_p), out.nbytes, 0))
+        return out.view(dtype)
+
+    def set_state(self, field: str, data: np.ndarray):
+        data = np.ascontiguousarray(data)
+        _check(_lib.gbx_stepper_copy_state(self._handle, field.encode(),
+                                           data.ctypes.data_as(ctypes.c_void_p), data.nbytes, 1))

@@ -1,0 +1,394 @@
+// Implementation of the C ABI declared in include/celeritas_gb300.h.
+#include "../../include/celeritas_gb300.h"
+
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+
+#include "host/Core.hh"
+
+struct gbx_params_s
+{
+    std::shared_ptr<gbx::CoreParams const> params;
+};
+
+struct gbx_stepper_s
+{
+    std::unique_ptr<gbx::Stepper> stepper;
+};
+
+namespace
+{
+thread_local std::string g_last_error;
+
+template<class F>
+int guarded(F&& f)
+{
+    try
+    {
+        f();
+        g_last_error.clear();
+        return 0;
+    }
+    catch (std::exception const& e)
+    {
+        g_last_error = e.what();
+    }
+    catch (...)
+    {
+        g_last_error = "unknown error";
+    }
+    return 1;
+}
+
+int copy_label(std::string const& s, char* buf, size_t buf_size)
+{
+    if (!buf || buf_size == 0)
+        return 1;
+    std::size_t n = std::min(s.size(), buf_size - 1);
+    std::memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+    return 0;
+}
+
+std::vector<gbx::TrackInitializer>
+to_initializers(gbx::ParamsData const& p, gbx_primary const* prim, size_t n)
+{
+    std::vector<gbx::TrackInitializer> result(n);
+    for (size_t i = 0; i < n; ++i)
+    {
+        gbx::TrackInitializer& ti = result[i];
+        ti = {};
+        if (prim[i].pdg == 11)
+            ti.particle_id = p.electron_id;
+        else if (prim[i].pdg == -11)
+            ti.particle_id = p.positron_id;
+        else if (prim[i].pdg == 22)
+            ti.particle_id = p.gamma_id;
+        else
+            throw std::runtime_error("unsupported primary PDG "
+                                     + std::to_string(prim[i].pdg));
+        ti.energy = prim[i].energy;
+        ti.pos = {prim[i].pos[0], prim[i].pos[1], prim[i].pos[2]};
+        ti.dir = {prim[i].dir[0], prim[i].dir[1], prim[i].dir[2]};
+        ti.time = prim[i].time;
+        ti.event_id = prim[i].event_id;
+        ti.track_id = gbx::invalid_id;
+        ti.parent_id = gbx::invalid_id;
+    }
+    return result;
+}
+
+gbx_step_result to_c(gbx::StepperResult const& r)
+{
+    return {r.generated, r.queued, r.active, r.alive};
+}
+
+//! Address and size of a named state array
+struct FieldRef
+{
+    void* ptr{nullptr};
+    std::size_t elem{0};
+    std::size_t count{0};
+};
+
+FieldRef find_field(gbx::CoreState& st, std::string const& name)
+{
+    using namespace gbx;
+    StateData const& s = st.ref();
+    std::size_t n = s.size;
+    auto f = [n](auto* p) {
+        return FieldRef{
+            static_cast<void*>(p), sizeof(std::remove_pointer_t<decltype(p)>), n};
+    };
+    if (name == "status") return f(s.status);
+    if (name == "track_id") return f(s.track_id);
+    if (name == "parent_id") return f(s.parent_id);
+    if (name == "event_id") return f(s.event_id);
+    if (name == "num_steps") return f(s.num_steps);
+    if (name == "time") return f(s.time);
+    if (name == "step_length") return f(s.step_length);
+    if (name == "post_step_action") return f(s.post_step_action);
+    if (name == "along_step_action") return f(s.along_step_action);
+    if (name == "particle_id") return f(s.particle_id);
+    if (name == "energy") return f(s.energy);
+    if (name == "pos_x") return f(s.pos[0]);
+    if (name == "pos_y") return f(s.pos[1]);
+    if (name == "pos_z") return f(s.pos[2]);
+    if (name == "dir_x") return f(s.dir[0]);
+    if (name == "dir_y") return f(s.dir[1]);
+    if (name == "dir_z") return f(s.dir[2]);
+    if (name == "volume") return f(s.volume);
+    if (name == "surface") return f(s.surface);
+    if (name == "surface_sense") return f(s.surface_sense);
+    if (name == "boundary") return f(s.boundary);
+    if (name == "next_step") return f(s.next_step);
+    if (name == "next_surface") return f(s.next_surface);
+    if (name == "next_sense") return f(s.next_sense);
+    if (name == "geo_failed") return f(s.geo_failed);
+    if (name == "material") return f(s.material);
+    if (name == "interaction_mfp") return f(s.interaction_mfp);
+    if (name == "dedx_range") return f(s.dedx_range);
+    if (name == "macro_xs") return f(s.macro_xs);
+    for (int i = 0; i < max_processes; ++i)
+    {
+        if (name == "per_process_xs_" + std::to_string(i))
+            return f(s.per_process_xs[i]);
+    }
+    if (name == "energy_deposition") return f(s.energy_deposition);
+    if (name == "secondaries_offset") return f(s.secondaries_offset);
+    if (name == "secondaries_count") return f(s.secondaries_count);
+    if (name == "element") return f(s.element);
+    if (name == "detector") return f(s.detector);
+    if (name == "vacancies") return f(s.vacancies);
+    if (name == "parents") return f(s.parents);
+    if (name == "secondary_counts") return f(s.secondary_counts);
+    if (name == "rng")
+        return FieldRef{s.rng.s[0], sizeof(std::uint32_t), 6 * n};
+    if (name == "counters")
+        return FieldRef{s.counters, sizeof(Counters), 1};
+    if (name == "initializers")
+        return FieldRef{s.initializers, sizeof(TrackInitializer), s.initializer_capacity};
+    if (name == "secondaries")
+        return FieldRef{s.secondaries, sizeof(Secondary), s.secondary_capacity};
+    if (name == "track_counters")
+        return FieldRef{s.track_counters, sizeof(size_type), s.max_events};
+    throw std::runtime_error("unknown state field '" + name + "'");
+}
+
+gbx::GeometrySpec geometry_by_name(std::string const& name)
+{
+    if (name == "calo")
+        return gbx::make_calorimeter_geometry();
+    throw std::runtime_error("unknown geometry '" + name + "'");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbx_last_error(void)
+{
+    return g_last_error.c_str();
+}
+
+int gbx_params_create(const char* physics_file,
+                      const char* geometry,
+                      gbx_params** out)
+{
+    return guarded([&] {
+        if (!physics_file || !geometry || !out)
+            throw std::runtime_error("null argument");
+        gbx::CoreParams::Input inp;
+        inp.physics_file = physics_file;
+        inp.geometry = geometry_by_name(geometry);
+        auto p = std::make_unique<gbx_params_s>();
+        p->params = std::make_shared<gbx::CoreParams>(inp);
+        *out = p.release();
+    });
+}
+
+void gbx_params_destroy(gbx_params* params)
+{
+    delete params;
+}
+
+int gbx_params_num_actions(const gbx_params* params, unsigned int* num)
+{
+    return guarded([&] { *num = params->params->action_reg().num_actions(); });
+}
+
+int gbx_params_action_label(const gbx_params* params,
+                            unsigned int action_id,
+                            char* buf,
+                            size_t buf_size)
+{
+    return guarded([&] {
+        if (copy_label(params->params->action_reg().id_to_label(action_id),
+                       buf,
+                       buf_size))
+            throw std::runtime_error("invalid label buffer");
+    });
+}
+
+int gbx_params_num_detectors(const gbx_params* params, unsigned int* num)
+{
+    return guarded([&] { *num = params->params->host().scalars.num_detectors; });
+}
+
+int gbx_params_detector_label(const gbx_params* params,
+                              unsigned int detector,
+                              char* buf,
+                              size_t buf_size)
+{
+    return guarded([&] {
+        if (copy_label(params->params->host().detector_labels.at(detector),
+                       buf,
+                       buf_size))
+            throw std::runtime_error("invalid label buffer");
+    });
+}
+
+int gbx_stepper_create(gbx_params* params,
+                       unsigned int num_track_slots,
+                       unsigned int seed,
+                       int use_graph,
+                       gbx_stepper** out)
+{
+    return guarded([&] {
+        if (!params || !out)
+            throw std::runtime_error("null argument");
+        gbx::StepperInput inp;
+        inp.params = params->params;
+        inp.num_track_slots = num_track_slots;
+        inp.seed = seed;
+        inp.use_graph = use_graph != 0;
+        auto s = std::make_unique<gbx_stepper_s>();
+        s->stepper = std::make_unique<gbx::Stepper>(inp);
+        *out = s.release();
+    });
+}
+
+void gbx_stepper_destroy(gbx_stepper* stepper)
+{
+    delete stepper;
+}
+
+int gbx_stepper_step(gbx_stepper* stepper,
+                     const gbx_primary* primaries,
+                     size_t num_primaries,
+                     gbx_step_result* result)
+{
+    return guarded([&] {
+        auto& st = *stepper->stepper;
+        gbx::StepperResult r;
+        if (num_primaries > 0)
+        {
+            r = st(to_initializers(
+                st.params().host().scalars, primaries, num_primaries));
+        }
+        else
+        {
+            r = st();
+        }
+        if (result)
+            *result = to_c(r);
+    });
+}
+
+int gbx_stepper_run(gbx_stepper* stepper,
+                    unsigned int max_steps,
+                    unsigned int batch,
+                    gbx_step_result* results,
+                    size_t capacity,
+                    unsigned int* num_steps)
+{
+    return guarded([&] {
+        auto recs = stepper->stepper->run_until_empty(max_steps, batch);
+        for (size_t i = 0; i < recs.size() && i < capacity; ++i)
+            results[i] = to_c(recs[i]);
+        if (num_steps)
+            *num_steps = static_cast<unsigned int>(recs.size());
+    });
+}
+
+int gbx_stepper_launch_action(gbx_stepper* stepper, unsigned int action_id)
+{
+    return guarded([&] {
+        auto& st = *stepper->stepper;
+        auto const& reg = st.params().action_reg();
+        if (action_id >= reg.num_actions())
+            throw std::runtime_error("invalid action ID");
+        auto const* sa = dynamic_cast<gbx::CoreStepActionInterface const*>(
+            reg.action(action_id).get());
+        if (!sa)
+            throw std::runtime_error("action has no step");
+        sa->step(st.params(), st.state());
+        if (cudaError_t err = cudaGetLastError(); err != cudaSuccess)
+            throw std::runtime_error(cudaGetErrorString(err));
+    });
+}
+
+int gbx_stepper_insert_primaries(gbx_stepper* stepper,
+                                 const gbx_primary* primaries,
+                                 size_t num_primaries)
+{
+    return guarded([&] {
+        auto& st = *stepper->stepper;
+        auto inits = to_initializers(
+            st.params().host().scalars, primaries, num_primaries);
+        st.state().insert_primaries(inits.data(),
+                                    static_cast<gbx::size_type>(inits.size()));
+    });
+}
+
+int gbx_stepper_kill_active(gbx_stepper* stepper)
+{
+    return guarded([&] { stepper->stepper->kill_active(); });
+}
+
+int gbx_stepper_synchronize(gbx_stepper* stepper)
+{
+    return guarded([&] {
+        if (cudaError_t err = cudaStreamSynchronize(stepper->stepper->state().stream());
+            err != cudaSuccess)
+            throw std::runtime_error(cudaGetErrorString(err));
+    });
+}
+
+int gbx_stepper_energy_deposition(gbx_stepper* stepper,
+                                  double* out,
+                                  size_t num_detectors)
+{
+    return guarded([&] {
+        auto e = stepper->stepper->energy_deposition();
+        if (num_detectors < e.size())
+            throw std::runtime_error("output buffer too small");
+        std::memcpy(out, e.data(), e.size() * sizeof(double));
+    });
+}
+
+int gbx_stepper_clear_energy_deposition(gbx_stepper* stepper)
+{
+    return guarded([&] { stepper->stepper->clear_energy_deposition(); });
+}
+
+int gbx_stepper_copy_state(gbx_stepper* stepper,
+                           const char* field,
+                           void* host,
+                           size_t nbytes,
+                           int direction)
+{
+    return guarded([&] {
+        auto& st = stepper->stepper->state();
+        FieldRef f = find_field(st, field);
+        if (nbytes > f.elem * f.count)
+            throw std::runtime_error("copy exceeds state array size");
+        cudaError_t err;
+        if (direction > 0)
+            err = cudaMemcpyAsync(f.ptr, host, nbytes, cudaMemcpyHostToDevice, st.stream());
+        else
+            err = cudaMemcpyAsync(host, f.ptr, nbytes, cudaMemcpyDeviceToHost, st.stream());
+        if (err == cudaSuccess)
+            err = cudaStreamSynchronize(st.stream());
+        if (err != cudaSuccess)
+            throw std::runtime_error(cudaGetErrorString(err));
+    });
+}
+
+int gbx_stepper_state_info(gbx_stepper* stepper,
+                           const char* field,
+                           size_t* elem_bytes,
+                           size_t* count)
+{
+    return guarded([&] {
+        FieldRef f = find_field(stepper->stepper->state(), field);
+        *elem_bytes = f.elem;
+        *count = f.count;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,720 @@
+// Device-side implementation of the host API: parameter upload, state
+// allocation, the registered step actions and the graph-replayed stepper.
+#include "../host/Core.hh"
+
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+
+#include "../host/HostState.hh"
+
+namespace gbx
+{
+namespace
+{
+void check(cudaError_t err, char const* what)
+{
+    if (err != cudaSuccess)
+    {
+        throw std::runtime_error(std::string(what) + ": "
+                                 + cudaGetErrorString(err));
+    }
+}
+#define GBX_CUDA(call) ::gbx::check((call), #call)
+
+//! Packs host arrays into one aligned byte buffer
+class Packer
+{
+  public:
+    template<class T>
+    std::size_t add(std::vector<T> const& v)
+    {
+        return this->add_bytes(v.data(), v.size() * sizeof(T));
+    }
+    std::size_t add_bytes(void const* data, std::size_t nbytes)
+    {
+        std::size_t off = (bytes_.size() + 255) & ~std::size_t(255);
+        bytes_.resize(off + std::max<std::size_t>(nbytes, 1));
+        if (nbytes)
+            std::memcpy(bytes_.data() + off, data, nbytes);
+        return off;
+    }
+    std::vector<unsigned char> const& bytes() const { return bytes_; }
+
+  private:
+    std::vector<unsigned char> bytes_;
+};
+
+//! Computes aligned offsets for a device allocation
+class Layout
+{
+  public:
+    std::size_t reserve(std::size_t nbytes)
+    {
+        std::size_t off = (size_ + 255) & ~std::size_t(255);
+        size_ = off + std::max<std::size_t>(nbytes, 1);
+        return off;
+    }
+    std::size_t size() const { return size_; }
+
+  private:
+    std::size_t size_{0};
+};
+
+//---------------------------------------------------------------------------//
+// Actions
+//---------------------------------------------------------------------------//
+class KernelAction : public CoreStepActionInterface, public ConcreteAction
+{
+  public:
+    using Launch = void (*)(CoreParams const&, CoreState&, ActionId);
+    KernelAction(ActionId id,
+                 std::string label,
+                 std::string description,
+                 StepActionOrder order,
+                 Launch launch)
+        : ConcreteAction(id, std::move(label), std::move(description))
+        , order_(order)
+        , launch_(launch)
+    {
+    }
+    StepActionOrder order() const final { return order_; }
+    void step(CoreParams const& params, CoreState& state) const final
+    {
+        if (launch_)
+            launch_(params, state, this->action_id());
+    }
+
+  private:
+    StepActionOrder order_;
+    Launch launch_;
+};
+
+void step_primaries(CoreParams const&, CoreState& state, ActionId)
+{
+    if (size_type n = state.pending_primaries())
+    {
+        launch_process_primaries(state.context(), n, state.stream());
+        state.clear_pending_primaries();
+    }
+}
+void step_init(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_initialize_tracks(state.context(), state.stream());
+}
+void step_pre(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_pre_step(state.context(), state.stream());
+}
+void step_along(CoreParams const&, CoreState& state, ActionId id)
+{
+    launch_along_step(state.context(), id, state.stream());
+}
+void step_discrete(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_discrete_select(state.context(), state.stream());
+}
+void step_model(CoreParams const&, CoreState& state, ActionId id)
+{
+    launch_interact(state.context(), id, state.stream());
+}
+void step_boundary(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_boundary(state.context(), state.stream());
+}
+void step_cut(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_tracking_cut(state.context(), state.stream());
+}
+void step_calo(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_calo_tally(state.context(), state.stream());
+}
+void step_secondaries(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_extend_from_secondaries(state.context(), state.stream());
+}
+
+}  // namespace
+
+//---------------------------------------------------------------------------//
+// ActionRegistry and registration
+//---------------------------------------------------------------------------//
+void ActionRegistry::insert(SPConstAction action)
+{
+    if (!action || action->action_id() != this->next_id())
+        throw std::runtime_error("action IDs must be inserted sequentially");
+    labels_.emplace_back(action->label());
+    actions_.push_back(std::move(action));
+}
+
+ActionId ActionRegistry::find_action(std::string_view label) const
+{
+    for (size_type i = 0; i < labels_.size(); ++i)
+    {
+        if (labels_[i] == label)
+            return i;
+    }
+    return invalid_id;
+}
+
+void register_core_actions(ActionRegistry* reg)
+{
+    using O = StepActionOrder;
+    auto add = [reg](std::string label,
+                     std::string desc,
+                     O order,
+                     KernelAction::Launch launch) {
+        reg->insert(std::make_shared<KernelAction>(
+            reg->next_id(), std::move(label), std::move(desc), order, launch));
+    };
+    auto implicit = [reg](std::string label, std::string desc) {
+        reg->insert(std::make_shared<ImplicitAction>(
+            reg->next_id(), std::move(label), std::move(desc)));
+    };
+    // PhysicsParams actions
+    add("pre-step", "update beginning-of-step state", O::pre, step_pre);
+    implicit("msc-range", "limit range due to multiple scattering");
+    implicit("eloss-range", "limit range due to energy loss");
+    add("physics-discrete-select",
+        "select a discrete interaction",
+        O::pre_post,
+        step_discrete);
+    implicit("physics-integral-rejected", "reject by integral cross section");
+    // Models
+    add("ioni-moller-bhabha", "interact by Moller+Bhabha", O::post, step_model);
+    add("brems-sb", "interact by Seltzer-Berger bremsstrahlung", O::post, step_model);
+    add("brems-rel",
+        "interact by relativistic bremsstrahlung",
+        O::post,
+        step_model);
+    add("photoel-livermore",
+        "interact by Livermore photoelectric effect",
+        O::post,
+        step_model);
+    add("scat-klein-nishina",
+        "interact by Compton scattering (simple Klein-Nishina)",
+        O::post,
+        step_model);
+    add("conv-bethe-heitler",
+        "interact by Bethe-Heitler gamma conversion",
+        O::post,
+        step_model);
+    add("annihil-2-gamma",
+        "interact by positron annihilation yielding two gammas",
+        O::post,
+        step_model);
+    implicit("physics-failure",
+             "mark a track that failed to sample an interaction");
+    // Along-step action registered by the driver
+    add("along-step-general-linear",
+        "apply along-step for particles with no field",
+        O::along,
+        step_along);
+    // CoreParams actions
+    add("extend-from-primaries",
+        "create track initializers from primaries",
+        O::generate,
+        step_primaries);
+    add("initialize-tracks",
+        "initialize track states",
+        O::start,
+        step_init);
+    add("along-step-neutral",
+        "apply along-step for neutral particles",
+        O::along,
+        step_along);
+    implicit("geo-propagation-limit", "pause due to propagation misbehavior");
+    add("geo-boundary", "cross a geometry boundary", O::post, step_boundary);
+    add("tracking-cut", "kill a track and deposit its energy", O::post, step_cut);
+    add("extend-from-secondaries",
+        "create track initializers from secondaries",
+        O::end,
+        step_secondaries);
+    // Step gathering: the pre-step detector lookup is fused into the
+    // pre-step kernel; the post-step gather applies the calorimeter tally
+    add("step-gather-pre", "gather pre-step steps/hits", O::user_pre, nullptr);
+    add("step-gather-post", "gather post-step steps/hits", O::user_post, step_calo);
+}
+
+//---------------------------------------------------------------------------//
+// CoreParams
+//---------------------------------------------------------------------------//
+CoreParams::CoreParams(Input const& inp)
+    : host_(build_params(inp.physics_file, inp.geometry, inp.options))
+    , actions_(std::make_shared<ActionRegistry>())
+{
+    register_core_actions(actions_.get());
+    for (size_type i = 0; i < host_.action_labels.size(); ++i)
+    {
+        if (actions_->id_to_label(i) != host_.action_labels[i])
+            throw std::runtime_error("action registration order mismatch");
+    }
+
+    // Pack every table into one device allocation
+    Packer pk;
+    HostParams const& h = host_;
+    std::size_t o_reals = pk.add(h.reals);
+    std::size_t o_ints = pk.add(h.ints);
+    std::size_t o_part = pk.add(h.particles);
+    std::size_t o_el = pk.add(h.elements);
+    std::size_t o_mat = pk.add(h.materials);
+    std::size_t o_fl = pk.add(h.fluct);
+    std::size_t o_cut = pk.add(h.cutoffs);
+    std::size_t o_grp = pk.add(h.groups);
+    std::size_t o_grid = pk.add(h.grids);
+    std::size_t o_lve = pk.add(h.lv_elements);
+    std::size_t o_lvs = pk.add(h.lv_shells);
+    std::size_t o_sb = pk.add(h.sb_tables);
+    std::size_t o_pl = pk.add(h.planes);
+    std::size_t o_box = pk.add(h.boxes);
+    std::size_t o_no = pk.add(h.neighbor_offset);
+    std::size_t o_nb = pk.add(h.neighbors);
+    std::size_t o_vm = pk.add(h.volume_material);
+    std::size_t o_vd = pk.add(h.volume_detector);
+
+    auto const& bytes = pk.bytes();
+    GBX_CUDA(cudaMalloc(&device_storage_, bytes.size()));
+    GBX_CUDA(cudaMemcpy(
+        device_storage_, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+    auto* base = static_cast<unsigned char*>(device_storage_);
+    device_ = h.scalars;
+    device_.reals = reinterpret_cast<double const*>(base + o_reals);
+    device_.ints = reinterpret_cast<size_type const*>(base + o_ints);
+    device_.particles = reinterpret_cast<ParticleRecord const*>(base + o_part);
+    device_.elements = reinterpret_cast<ElementRecord const*>(base + o_el);
+    device_.materials = reinterpret_cast<MaterialRecord const*>(base + o_mat);
+    device_.fluct = reinterpret_cast<UrbanFluctRecord const*>(base + o_fl);
+    device_.cutoff_energy = reinterpret_cast<double const*>(base + o_cut);
+    device_.process_groups = reinterpret_cast<ProcessGroup const*>(base + o_grp);
+    device_.grids = reinterpret_cast<XsGrid const*>(base + o_grid);
+    device_.livermore_elements
+        = reinterpret_cast<LivermoreElement const*>(base + o_lve);
+    device_.livermore_shells = reinterpret_cast<LivermoreShell const*>(base + o_lvs);
+    device_.sb_tables = reinterpret_cast<SBElementTable const*>(base + o_sb);
+    device_.geo.planes = reinterpret_cast<PlaneRecord const*>(base + o_pl);
+    device_.geo.boxes = reinterpret_cast<BoxVolume const*>(base + o_box);
+    device_.geo.neighbor_offset = reinterpret_cast<size_type const*>(base + o_no);
+    device_.geo.neighbors = reinterpret_cast<size_type const*>(base + o_nb);
+    device_.geo.volume_material = reinterpret_cast<size_type const*>(base + o_vm);
+    device_.geo.volume_detector = reinterpret_cast<size_type const*>(base + o_vd);
+}
+
+CoreParams::~CoreParams()
+{
+    if (device_storage_)
+        cudaFree(device_storage_);
+}
+
+//---------------------------------------------------------------------------//
+// CoreState
+//---------------------------------------------------------------------------//
+CoreState::CoreState(CoreParams const& params,
+                     size_type num_track_slots,
+                     unsigned int seed,
+                     size_type initializer_capacity,
+                     size_type max_events,
+                     cudaStream_t stream)
+    : stream_(stream)
+{
+    if (num_track_slots == 0)
+        throw std::runtime_error("number of track slots must be positive");
+    size_type const n = num_track_slots;
+    size_type const sec_cap = static_cast<size_type>(
+        params.host().scalars.secondary_stack_factor * n);
+    size_type const init_cap
+        = initializer_capacity ? initializer_capacity : std::max(1u << 20, 4 * n);
+    size_type const ndet = params.host().scalars.num_detectors;
+    size_type const nblocks = (n + block_size - 1) / block_size;
+    size_type const log_cap = 4096;
+
+    Layout L;
+    auto arr = [&L, n](std::size_t elem) { return L.reserve(elem * n); };
+    std::size_t o_status = arr(1), o_track = arr(4), o_parent = arr(4),
+                o_event = arr(4), o_nsteps = arr(4), o_time = arr(8),
+                o_len = arr(8), o_post = arr(4), o_along = arr(4),
+                o_pid = arr(4), o_energy = arr(sizeof(real_type));
+    std::size_t o_pos[3], o_dir[3];
+    for (int i = 0; i < 3; ++i)
+        o_pos[i] = arr(8);
+    for (int i = 0; i < 3; ++i)
+        o_dir[i] = arr(8);
+    std::size_t o_vol = arr(4), o_surf = arr(4), o_sense = arr(1),
+                o_bound = arr(1), o_next = arr(8), o_nsurf = arr(4),
+                o_nsense = arr(1), o_failed = arr(1), o_mat = arr(4),
+                o_mfp = arr(sizeof(real_type)), o_range = arr(sizeof(real_type)),
+                o_macro = arr(sizeof(real_type));
+    std::size_t o_ppxs[max_processes];
+    for (auto& o : o_ppxs)
+        o = arr(sizeof(real_type));
+    std::size_t o_edep = arr(sizeof(real_type)), o_soff = arr(4),
+                o_scount = arr(4), o_elem = arr(4);
+    std::size_t o_rng = L.reserve(std::size_t(6) * 4 * n);
+    std::size_t o_vac = arr(4), o_cnts = arr(4), o_parents = arr(4);
+    std::size_t o_inits = L.reserve(sizeof(TrackInitializer) * std::size_t(init_cap));
+    std::size_t o_tcount = L.reserve(4 * std::size_t(max_events));
+    std::size_t o_secs = L.reserve(sizeof(Secondary) * std::size_t(sec_cap));
+    std::size_t o_det = arr(4);
+    std::size_t o_calo = L.reserve(8 * std::size_t(std::max<size_type>(ndet, 1)));
+    size_type const prim_cap = std::max<size_type>(n, 1u << 16);
+    std::size_t o_prims = L.reserve(sizeof(TrackInitializer) * std::size_t(prim_cap));
+    std::size_t o_counters = L.reserve(sizeof(Counters));
+    std::size_t o_bvac = L.reserve(4 * std::size_t(nblocks));
+    std::size_t o_bcnt = L.reserve(4 * std::size_t(nblocks));
+    std::size_t o_svac = arr(1);
+    std::size_t o_scnt = arr(4);
+    std::size_t o_log = L.reserve(sizeof(StepRecord) * log_cap);
+    std::size_t o_stepidx = L.reserve(sizeof(size_type));
+
+    GBX_CUDA(cudaMalloc(&storage_, L.size()));
+    GBX_CUDA(cudaMemsetAsync(storage_, 0, L.size(), stream_));
+    auto* b = static_cast<unsigned char*>(storage_);
+    auto at = [b](std::size_t off) { return static_cast<void*>(b + off); };
+
+    StateData& s = ref_;
+    s.size = n;
+    s.status = static_cast<std::uint8_t*>(at(o_status));
+    s.track_id = static_cast<size_type*>(at(o_track));
+    s.parent_id = static_cast<size_type*>(at(o_parent));
+    s.event_id = static_cast<size_type*>(at(o_event));
+    s.num_steps = static_cast<size_type*>(at(o_nsteps));
+    s.time = static_cast<double*>(at(o_time));
+    s.step_length = static_cast<double*>(at(o_len));
+    s.post_step_action = static_cast<size_type*>(at(o_post));
+    s.along_step_action = static_cast<size_type*>(at(o_along));
+    s.particle_id = static_cast<size_type*>(at(o_pid));
+    s.energy = static_cast<real_type*>(at(o_energy));
+    for (int i = 0; i < 3; ++i)
+    {
+        s.pos[i] = static_cast<double*>(at(o_pos[i]));
+        s.dir[i] = static_cast<double*>(at(o_dir[i]));
+    }
+    s.volume = static_cast<size_type*>(at(o_vol));
+    s.surface = static_cast<size_type*>(at(o_surf));
+    s.surface_sense = static_cast<std::int8_t*>(at(o_sense));
+    s.boundary = static_cast<std::uint8_t*>(at(o_bound));
+    s.next_step = static_cast<double*>(at(o_next));
+    s.next_surface = static_cast<size_type*>(at(o_nsurf));
+    s.next_sense = static_cast<std::int8_t*>(at(o_nsense));
+    s.geo_failed = static_cast<std::uint8_t*>(at(o_failed));
+    s.material = static_cast<size_type*>(at(o_mat));
+    s.interaction_mfp = static_cast<real_type*>(at(o_mfp));
+    s.dedx_range = static_cast<real_type*>(at(o_range));
+    s.macro_xs = static_cast<real_type*>(at(o_macro));
+    for (int i = 0; i < max_processes; ++i)
+        s.per_process_xs[i] = static_cast<real_type*>(at(o_ppxs[i]));
+    s.energy_deposition = static_cast<real_type*>(at(o_edep));
+    s.secondaries_offset = static_cast<size_type*>(at(o_soff));
+    s.secondaries_count = static_cast<size_type*>(at(o_scount));
+    s.element = static_cast<size_type*>(at(o_elem));
+    auto* rng = static_cast<std::uint32_t*>(at(o_rng));
+    for (int w = 0; w < 5; ++w)
+        s.rng.s[w] = rng + std::size_t(w) * n;
+    s.rng.weyl = rng + std::size_t(5) * n;
+    s.vacancies = static_cast<size_type*>(at(o_vac));
+    s.secondary_counts = static_cast<size_type*>(at(o_cnts));
+    s.parents = static_cast<size_type*>(at(o_parents));
+    s.initializers = static_cast<TrackInitializer*>(at(o_inits));
+    s.initializer_capacity = init_cap;
+    s.track_counters = static_cast<size_type*>(at(o_tcount));
+    s.max_events = max_events;
+    s.secondaries = static_cast<Secondary*>(at(o_secs));
+    s.secondary_capacity = sec_cap;
+    s.detector = static_cast<size_type*>(at(o_det));
+    s.calo_edep = static_cast<double*>(at(o_calo));
+    s.primaries = static_cast<TrackInitializer*>(at(o_prims));
+    s.primary_capacity = prim_cap;
+    s.counters = static_cast<Counters*>(at(o_counters));
+
+    // Initial values that are not zero: fill from host staging
+    {
+        std::vector<std::uint32_t> words;
+        initialize_xorwow(seed, n, &words);
+        GBX_CUDA(cudaMemcpyAsync(rng,
+                                 words.data(),
+                                 words.size() * 4,
+                                 cudaMemcpyHostToDevice,
+                                 stream_));
+        std::vector<size_type> seq(n);
+        for (size_type i = 0; i < n; ++i)
+            seq[i] = i;
+        GBX_CUDA(cudaMemcpyAsync(
+            s.vacancies, seq.data(), 4 * std::size_t(n), cudaMemcpyHostToDevice, stream_));
+        std::vector<size_type> inv(n, invalid_id);
+        for (size_type* dst : {s.track_id,
+                               s.parent_id,
+                               s.event_id,
+                               s.post_step_action,
+                               s.along_step_action,
+                               s.particle_id,
+                               s.volume,
+                               s.surface,
+                               s.next_surface,
+                               s.material,
+                               s.element,
+                               s.parents,
+                               s.detector})
+        {
+            GBX_CUDA(cudaMemcpyAsync(
+                dst, inv.data(), 4 * std::size_t(n), cudaMemcpyHostToDevice, stream_));
+        }
+        Counters c{};
+        c.num_vacancies = n;
+        GBX_CUDA(cudaMemcpyAsync(
+            s.counters, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+        GBX_CUDA(cudaStreamSynchronize(stream_));
+    }
+
+    ctx_.params = params.device_ref();
+    ctx_.state = s;
+    ctx_.scratch.block_vacant = static_cast<size_type*>(at(o_bvac));
+    ctx_.scratch.block_count = static_cast<size_type*>(at(o_bcnt));
+    ctx_.scratch.vacant = static_cast<std::uint8_t*>(at(o_svac));
+    ctx_.scratch.count = static_cast<size_type*>(at(o_scnt));
+    ctx_.scratch.num_blocks = nblocks;
+    ctx_.log = static_cast<StepRecord*>(at(o_log));
+    ctx_.log_capacity = log_cap;
+    ctx_.step_index = static_cast<size_type*>(at(o_stepidx));
+
+    pinned_capacity_ = prim_cap;
+    GBX_CUDA(cudaMallocHost(&pinned_primaries_,
+                            sizeof(TrackInitializer) * std::size_t(prim_cap)));
+}
+
+CoreState::~CoreState()
+{
+    if (storage_)
+        cudaFree(storage_);
+    if (pinned_primaries_)
+        cudaFreeHost(pinned_primaries_);
+}
+
+void CoreState::insert_primaries(TrackInitializer const* host_primaries, size_type n)
+{
+    if (pending_primaries_ != 0)
+        throw std::runtime_error("multiple consecutive primary insertions");
+    if (n > pinned_capacity_)
+        throw std::runtime_error("too many primaries for one insertion");
+    if (n == 0)
+        return;
+    // Stage through pinned memory so the copy is asynchronous
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    std::memcpy(pinned_primaries_, host_primaries, sizeof(TrackInitializer) * n);
+    GBX_CUDA(cudaMemcpyAsync(ref_.primaries,
+                             pinned_primaries_,
+                             sizeof(TrackInitializer) * n,
+                             cudaMemcpyHostToDevice,
+                             stream_));
+    pending_primaries_ = n;
+}
+
+Counters CoreState::counters() const
+{
+    Counters c;
+    GBX_CUDA(cudaMemcpyAsync(
+        &c, ref_.counters, sizeof(c), cudaMemcpyDeviceToHost, stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return c;
+}
+
+size_type CoreState::step_index() const
+{
+    size_type idx;
+    GBX_CUDA(cudaMemcpyAsync(
+        &idx, ctx_.step_index, sizeof(idx), cudaMemcpyDeviceToHost, stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return idx;
+}
+
+std::vector<StepRecord> CoreState::step_log(size_type first, size_type n) const
+{
+    std::vector<StepRecord> all(ctx_.log_capacity);
+    GBX_CUDA(cudaMemcpyAsync(all.data(),
+                             ctx_.log,
+                             sizeof(StepRecord) * all.size(),
+                             cudaMemcpyDeviceToHost,
+                             stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    std::vector<StepRecord> result(n);
+    for (size_type i = 0; i < n; ++i)
+        result[i] = all[(first + i) % ctx_.log_capacity];
+    return result;
+}
+
+//---------------------------------------------------------------------------//
+// ActionSequence
+//---------------------------------------------------------------------------//
+ActionSequence::ActionSequence(ActionRegistry const& reg)
+{
+    for (size_type i = 0; i < reg.num_actions(); ++i)
+    {
+        if (auto const* sa = dynamic_cast<CoreStepActionInterface const*>(
+                reg.action(i).get()))
+        {
+            actions_.push_back(sa);
+        }
+    }
+    // Sort by (order, ID)
+    std::stable_sort(actions_.begin(),
+                     actions_.end(),
+                     [](CoreStepActionInterface const* a,
+                        CoreStepActionInterface const* b) {
+                         if (a->order() != b->order())
+                             return a->order() < b->order();
+                         return a->action_id() < b->action_id();
+                     });
+}
+
+void ActionSequence::step(CoreParams const& params, CoreState& state) const
+{
+    for (auto const* a : actions_)
+    {
+        a->step(params, state);
+    }
+}
+
+//---------------------------------------------------------------------------//
+// Stepper
+//---------------------------------------------------------------------------//
+Stepper::Stepper(StepperInput const& input)
+    : params_(input.params), use_graph_(input.use_graph)
+{
+    if (!params_)
+        throw std::runtime_error("stepper requires params");
+    GBX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    state_ = std::make_unique<CoreState>(*params_,
+                                         input.num_track_slots,
+                                         input.seed,
+                                         input.initializer_capacity,
+                                         input.max_events,
+                                         stream_);
+    actions_ = std::make_unique<ActionSequence>(params_->action_reg());
+}
+
+Stepper::~Stepper()
+{
+    if (graph_exec_)
+        cudaGraphExecDestroy(graph_exec_);
+    if (graph_)
+        cudaGraphDestroy(graph_);
+    state_.reset();
+    if (stream_)
+        cudaStreamDestroy(stream_);
+}
+
+void Stepper::build_graph()
+{
+    GBX_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    actions_->step(*params_, *state_);
+    GBX_CUDA(cudaStreamEndCapture(stream_, &graph_));
+    GBX_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+}
+
+void Stepper::launch_steps(size_type count)
+{
+    for (size_type i = 0; i < count; ++i)
+    {
+        if (use_graph_ && state_->pending_primaries() == 0)
+        {
+            if (!graph_exec_)
+                this->build_graph();
+            GBX_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+        }
+        else
+        {
+            actions_->step(*params_, *state_);
+        }
+    }
+    GBX_CUDA(cudaGetLastError());
+}
+
+StepperResult Stepper::read_record(size_type index) const
+{
+    StepRecord r = state_->step_log(index, 1).front();
+    StepperResult out;
+    out.generated = r.generated;
+    out.queued = r.queued;
+    out.active = r.active;
+    out.alive = r.alive;
+    return out;
+}
+
+StepperResult Stepper::operator()(std::vector<TrackInitializer> const& primaries)
+{
+    state_->insert_primaries(primaries.data(),
+                             static_cast<size_type>(primaries.size()));
+    return (*this)();
+}
+
+StepperResult Stepper::operator()()
+{
+    size_type idx = state_->step_index();
+    this->launch_steps(1);
+    Counters c = state_->counters();
+    if (c.error_flags & error_initializer_overflow)
+        throw std::runtime_error("insufficient capacity for track initializers");
+    return this->read_record(idx);
+}
+
+std::vector<StepperResult> Stepper::run_until_empty(size_type max_steps,
+                                                    size_type batch)
+{
+    std::vector<StepperResult> results;
+    size_type first = state_->step_index();
+    batch = std::max<size_type>(1, std::min(batch, state_->log_capacity()));
+    size_type taken = 0;
+    bool done = false;
+    while (!done && taken < max_steps)
+    {
+        size_type n = std::min(batch, max_steps - taken);
+        this->launch_steps(n);
+        Counters c = state_->counters();
+        if (c.error_flags & error_initializer_overflow)
+            throw std::runtime_error("insufficient capacity for track initializers");
+        auto recs = state_->step_log(first + taken, n);
+        for (auto const& r : recs)
+        {
+            StepperResult out;
+            out.generated = r.generated;
+            out.queued = r.queued;
+            out.active = r.active;
+            out.alive = r.alive;
+            results.push_back(out);
+            if (!out)
+            {
+                done = true;
+                break;
+            }
+        }
+        taken += n;
+    }
+    return results;
+}
+
+void Stepper::kill_active()
+{
+    launch_kill_active(state_->context(), stream_);
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+}
+
+std::vector<double> Stepper::energy_deposition() const
+{
+    std::vector<double> result(params_->host().scalars.num_detectors);
+    GBX_CUDA(cudaMemcpyAsync(result.data(),
+                             state_->ref().calo_edep,
+                             sizeof(double) * result.size(),
+                             cudaMemcpyDeviceToHost,
+                             stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return result;
+}
+
+void Stepper::clear_energy_deposition()
+{
+    GBX_CUDA(cudaMemsetAsync(state_->ref().calo_edep,
+                             0,
+                             sizeof(double) * params_->host().scalars.num_detectors,
+                             stream_));
+}
+
+}  // namespace gbx

@@ -1,0 +1,516 @@
+// CUDA kernels of the GB300 stepping loop.
+//
+// Each action kernel runs one thread per track slot and calls the same
+// per-slot function as the reference's action executor (see gbx/Actions.hh
+// and gbx/TrackInit.hh). Counters stay on the device: the number of new
+// tracks, vacancies, secondaries and initializers are read and updated by
+// kernels, so a whole step is a fixed sequence of launches that a CUDA graph
+// can capture (the reference copies counters to the host several times per
+// step, src/celeritas/track/detail/TrackInitAlgorithms.cu:34-78).
+//
+// End-of-step bookkeeping (src/celeritas/track/ExtendFromSecondariesAction.cc)
+// is three kernels: per-slot vacancy flags and secondary counts with
+// per-block totals (warp ballot/popc and shuffle scans), one block scanning
+// the block totals and updating the counters, and a scatter that writes the
+// stably compacted vacancy list and processes each slot's secondaries at its
+// exclusive-scan offset.
+#include "Kernels.cuh"
+
+#include "../gbx/TrackInit.hh"
+
+namespace gbx
+{
+namespace
+{
+__device__ __forceinline__ size_type thread_slot()
+{
+    return blockIdx.x * blockDim.x + threadIdx.x;
+}
+
+inline unsigned int num_blocks_for(size_type n)
+{
+    return static_cast<unsigned int>((n + block_size - 1) / block_size);
+}
+
+//---------------------------------------------------------------------------//
+// Block-wide exclusive scan of one 32-bit value per thread (256 threads)
+//---------------------------------------------------------------------------//
+struct BlockScanStorage
+{
+    size_type warp_sums[block_size / 32];
+    size_type total;
+};
+
+__device__ __forceinline__ size_type block_exclusive_scan(size_type value,
+                                                          BlockScanStorage& tmp,
+                                                          size_type* total)
+{
+    int const lane = threadIdx.x & 31;
+    int const warp = threadIdx.x >> 5;
+    // Inclusive warp scan
+    size_type incl = value;
+#pragma unroll
+    for (int offset = 1; offset < 32; offset <<= 1)
+    {
+        size_type n = __shfl_up_sync(0xffffffffu, incl, offset);
+        if (lane >= offset)
+            incl += n;
+    }
+    if (lane == 31)
+        tmp.warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        constexpr int nwarps = block_size / 32;
+        size_type w = (lane < nwarps) ? tmp.warp_sums[lane] : 0;
+        size_type wincl = w;
+#pragma unroll
+        for (int offset = 1; offset < nwarps; offset <<= 1)
+        {
+            size_type n = __shfl_up_sync(0xffffffffu, wincl, offset);
+            if (lane >= offset)
+                wincl += n;
+        }
+        if (lane < nwarps)
+            tmp.warp_sums[lane] = wincl - w;  // exclusive warp offsets
+        if (lane == nwarps - 1)
+            tmp.total = wincl;
+    }
+    __syncthreads();
+    size_type result = tmp.warp_sums[warp] + incl - value;
+    *total = tmp.total;
+    __syncthreads();
+    return result;
+}
+
+//---------------------------------------------------------------------------//
+// Primaries and track initialization
+//---------------------------------------------------------------------------//
+__global__ void begin_primaries_kernel(StateData s, size_type num_primaries)
+{
+    Counters& c = *s.counters;
+    c.num_initializers += num_primaries;
+    c.num_generated = num_primaries;
+    if (c.num_initializers > s.initializer_capacity)
+    {
+        c.error_flags |= error_initializer_overflow;
+        c.num_initializers = s.initializer_capacity;
+    }
+    c.num_pending_primaries = num_primaries;
+}
+
+__global__ void process_primaries_kernel(StateData s, size_type num_primaries)
+{
+    size_type tid = thread_slot();
+    Counters const& c = *s.counters;
+    if (tid < num_primaries && !(c.error_flags & error_initializer_overflow))
+    {
+        process_primary(s, c.num_initializers, num_primaries, tid);
+    }
+    // Primaries have no parents: clear the parent list
+    for (size_type i = tid; i < s.size; i += gridDim.x * blockDim.x)
+    {
+        s.parents[i] = invalid_id;
+    }
+}
+
+__global__ __launch_bounds__(block_size) void initialize_tracks_kernel(
+    ParamsData p, StateData s)
+{
+    size_type tid = thread_slot();
+    Counters const c = *s.counters;
+    size_type num_new = min_of(c.num_vacancies, c.num_initializers);
+    if (tid < num_new)
+    {
+        init_track(p, s, c, tid);
+    }
+}
+
+__global__ void finish_initialize_kernel(StateData s,
+                                         StepRecord* log,
+                                         size_type log_capacity,
+                                         size_type* step_index)
+{
+    Counters& c = *s.counters;
+    size_type num_new = min_of(c.num_vacancies, c.num_initializers);
+    c.num_initializers -= num_new;
+    c.num_vacancies -= num_new;
+    c.num_active = s.size - c.num_vacancies;
+    // pre-step clears the secondary stack
+    c.secondary_stack_size = 0;
+    StepRecord& r = log[*step_index % log_capacity];
+    r.generated = c.num_generated;
+    r.active = c.num_active;
+    c.num_generated = 0;
+}
+
+//---------------------------------------------------------------------------//
+// Physics actions
+//---------------------------------------------------------------------------//
+__global__ __launch_bounds__(block_size) void pre_step_kernel(ParamsData p,
+                                                              StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        pre_step(p, s, slot);
+        gather_pre(p, s, slot);
+    }
+}
+
+__global__ __launch_bounds__(block_size) void along_step_kernel(ParamsData p,
+                                                                StateData s,
+                                                                size_type action)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size
+        && (action == invalid_id || s.along_step_action[slot] == action))
+    {
+        along_step(p, s, slot);
+    }
+}
+
+__global__ __launch_bounds__(block_size) void discrete_select_kernel(
+    ParamsData p, StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        discrete_select(p, s, slot);
+    }
+}
+
+__global__ __launch_bounds__(block_size) void interact_kernel(ParamsData p,
+                                                              StateData s,
+                                                              size_type action)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        interact(p, s, slot, action);
+    }
+}
+
+//! All model actions for the slots that selected one (the model actions are
+//! mutually exclusive per slot, so one launch applies each slot's model)
+__global__ __launch_bounds__(block_size) void interact_all_kernel(ParamsData p,
+                                                                  StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        size_type a = s.post_step_action[slot];
+        if (a >= p.model_to_action && a < p.model_to_action + p.num_models)
+        {
+            interact(p, s, slot, a);
+        }
+    }
+}
+
+__global__ __launch_bounds__(block_size) void boundary_kernel(ParamsData p,
+                                                              StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        boundary_cross(p, s, slot);
+    }
+}
+
+__global__ __launch_bounds__(block_size) void tracking_cut_kernel(ParamsData p,
+                                                                  StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        tracking_cut(p, s, slot);
+    }
+}
+
+//! Post-step boundary crossing, tracking cut and calorimeter tally fused
+__global__ __launch_bounds__(block_size) void post_kernel(ParamsData p,
+                                                          StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size)
+    {
+        boundary_cross(p, s, slot);
+        tracking_cut(p, s, slot);
+        if (s.status[slot] != status_inactive)
+        {
+            size_type det = s.detector[slot];
+            if (det != invalid_id)
+            {
+                atomicAdd(s.calo_edep + det, double(s.energy_deposition[slot]));
+            }
+        }
+    }
+}
+
+__global__ __launch_bounds__(block_size) void calo_kernel(ParamsData, StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size && s.status[slot] != status_inactive)
+    {
+        size_type det = s.detector[slot];
+        if (det != invalid_id)
+        {
+            atomicAdd(s.calo_edep + det, double(s.energy_deposition[slot]));
+        }
+    }
+}
+
+//---------------------------------------------------------------------------//
+// End of step: vacancies and secondaries
+//---------------------------------------------------------------------------//
+__global__ __launch_bounds__(block_size) void locate_alive_kernel(StateData s,
+                                                                  ScanScratch scr)
+{
+    __shared__ BlockScanStorage tmp;
+    size_type slot = thread_slot();
+    bool vacant = false;
+    size_type count = 0;
+    if (slot < s.size)
+    {
+        locate_alive(s, slot, &vacant, &count);
+        scr.vacant[slot] = vacant;
+        scr.count[slot] = count;
+    }
+    // Block totals: vacancies with ballot/popc, counts with a block scan
+    unsigned int ballot = __ballot_sync(0xffffffffu, vacant);
+    __shared__ size_type warp_vac[block_size / 32];
+    if ((threadIdx.x & 31) == 0)
+        warp_vac[threadIdx.x >> 5] = __popc(ballot);
+    size_type total_count;
+    block_exclusive_scan(count, tmp, &total_count);
+    if (threadIdx.x == 0)
+    {
+        size_type total_vac = 0;
+        for (int w = 0; w < block_size / 32; ++w)
+            total_vac += warp_vac[w];
+        scr.block_vacant[blockIdx.x] = total_vac;
+        scr.block_count[blockIdx.x] = total_count;
+    }
+}
+
+__global__ __launch_bounds__(1024) void scan_blocks_kernel(StateData s,
+                                                           ScanScratch scr,
+                                                           StepRecord* log,
+                                                           size_type log_capacity,
+                                                           size_type* step_index)
+{
+    // Exclusive scan of the per-block totals by one block of 1024 threads
+    __shared__ size_type sh_vac[1024];
+    __shared__ size_type sh_cnt[1024];
+    __shared__ size_type carry_vac, carry_cnt;
+    if (threadIdx.x == 0)
+    {
+        carry_vac = 0;
+        carry_cnt = 0;
+    }
+    __syncthreads();
+    for (size_type base = 0; base < scr.num_blocks; base += 1024)
+    {
+        size_type i = base + threadIdx.x;
+        size_type v = i < scr.num_blocks ? scr.block_vacant[i] : 0;
+        size_type c = i < scr.num_blocks ? scr.block_count[i] : 0;
+        sh_vac[threadIdx.x] = v;
+        sh_cnt[threadIdx.x] = c;
+        __syncthreads();
+        // Hillis-Steele inclusive scan
+        for (int off = 1; off < 1024; off <<= 1)
+        {
+            size_type av = threadIdx.x >= off ? sh_vac[threadIdx.x - off] : 0;
+            size_type ac = threadIdx.x >= off ? sh_cnt[threadIdx.x - off] : 0;
+            __syncthreads();
+            sh_vac[threadIdx.x] += av;
+            sh_cnt[threadIdx.x] += ac;
+            __syncthreads();
+        }
+        if (i < scr.num_blocks)
+        {
+            scr.block_vacant[i] = carry_vac + sh_vac[threadIdx.x] - v;
+            scr.block_count[i] = carry_cnt + sh_cnt[threadIdx.x] - c;
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023)
+        {
+            carry_vac += sh_vac[1023];
+            carry_cnt += sh_cnt[1023];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        Counters& c = *s.counters;
+        c.num_vacancies = carry_vac;
+        c.num_secondaries = carry_cnt;
+        c.num_initializers += carry_cnt;
+        if (c.num_initializers > s.initializer_capacity)
+        {
+            c.error_flags |= error_initializer_overflow;
+        }
+        c.num_alive = s.size - c.num_vacancies;
+        StepRecord& r = log[*step_index % log_capacity];
+        r.queued = c.num_initializers;
+        r.alive = c.num_alive;
+        *step_index += 1;
+    }
+}
+
+__global__ __launch_bounds__(block_size) void scatter_kernel(ParamsData p,
+                                                             StateData s,
+                                                             ScanScratch scr)
+{
+    __shared__ BlockScanStorage tmp;
+    __shared__ size_type warp_vac[block_size / 32];
+    size_type slot = thread_slot();
+    bool vacant = false;
+    size_type count = 0;
+    if (slot < s.size)
+    {
+        vacant = scr.vacant[slot];
+        count = scr.count[slot];
+    }
+    // Stable position among vacant slots: ballot prefix within the warp plus
+    // preceding warps in the block plus preceding blocks
+    unsigned int ballot = __ballot_sync(0xffffffffu, vacant);
+    int const lane = threadIdx.x & 31;
+    int const warp = threadIdx.x >> 5;
+    if (lane == 0)
+        warp_vac[warp] = __popc(ballot);
+    __syncthreads();
+    size_type vac_before = 0;
+    for (int w = 0; w < warp; ++w)
+        vac_before += warp_vac[w];
+    vac_before += __popc(ballot & ((1u << lane) - 1u));
+    size_type total_count;
+    size_type count_before = block_exclusive_scan(count, tmp, &total_count);
+
+    if (slot < s.size)
+    {
+        Counters const c = *s.counters;
+        if (vacant)
+        {
+            s.vacancies[scr.block_vacant[blockIdx.x] + vac_before] = slot;
+        }
+        if (!(c.error_flags & error_initializer_overflow))
+        {
+            process_secondaries(
+                p, s, c, slot, scr.block_count[blockIdx.x] + count_before);
+        }
+    }
+}
+
+__global__ void kill_active_kernel(ParamsData p, StateData s)
+{
+    size_type slot = thread_slot();
+    if (slot < s.size && is_track_valid(s.status[slot]))
+    {
+        apply_errored(p, s, slot);
+    }
+}
+
+}  // namespace
+
+//---------------------------------------------------------------------------//
+// Launchers
+//---------------------------------------------------------------------------//
+void launch_process_primaries(LaunchContext const& ctx,
+                              size_type num_primaries,
+                              cudaStream_t stream)
+{
+    begin_primaries_kernel<<<1, 1, 0, stream>>>(ctx.state, num_primaries);
+    size_type n = max_of(num_primaries, ctx.state.size);
+    process_primaries_kernel<<<num_blocks_for(n), block_size, 0, stream>>>(
+        ctx.state, num_primaries);
+}
+
+void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream)
+{
+    initialize_tracks_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+    finish_initialize_kernel<<<1, 1, 0, stream>>>(
+        ctx.state, ctx.log, ctx.log_capacity, ctx.step_index);
+}
+
+void launch_pre_step(LaunchContext const& ctx, cudaStream_t stream)
+{
+    pre_step_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+}
+
+void launch_along_step(LaunchContext const& ctx,
+                       size_type action,
+                       cudaStream_t stream)
+{
+    along_step_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state, action);
+}
+
+void launch_discrete_select(LaunchContext const& ctx, cudaStream_t stream)
+{
+    discrete_select_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+}
+
+void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t stream)
+{
+    if (action == invalid_id)
+    {
+        interact_all_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            ctx.params, ctx.state);
+    }
+    else
+    {
+        interact_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            ctx.params, ctx.state, action);
+    }
+}
+
+void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
+{
+    boundary_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+}
+
+void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
+{
+    tracking_cut_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+}
+
+void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream)
+{
+    calo_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+}
+
+void launch_extend_from_secondaries(LaunchContext const& ctx, cudaStream_t stream)
+{
+    unsigned int nb = num_blocks_for(ctx.state.size);
+    locate_alive_kernel<<<nb, block_size, 0, stream>>>(ctx.state, ctx.scratch);
+    scan_blocks_kernel<<<1, 1024, 0, stream>>>(
+        ctx.state, ctx.scratch, ctx.log, ctx.log_capacity, ctx.step_index);
+    scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, ctx.scratch);
+}
+
+void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream)
+{
+    kill_active_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+}
+
+void launch_step(LaunchContext const& ctx, cudaStream_t stream)
+{
+    launch_initialize_tracks(ctx, stream);
+    launch_pre_step(ctx, stream);
+    launch_along_step(ctx, invalid_id, stream);
+    launch_discrete_select(ctx, stream);
+    launch_interact(ctx, invalid_id, stream);
+    post_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state);
+    launch_extend_from_secondaries(ctx, stream);
+}
+
+}  // namespace gbx

@@ -1,0 +1,72 @@
+// Kernel declarations for the GB300 stepping loop.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../gbx/Data.hh"
+
+namespace gbx
+{
+//! Per-step counter record kept on the device (StepperResult)
+struct StepRecord
+{
+    size_type generated;
+    size_type queued;
+    size_type active;
+    size_type alive;
+};
+
+//! Scratch for the end-of-step compaction: per-block totals and offsets
+struct ScanScratch
+{
+    size_type* block_vacant;  //!< [num_blocks]
+    size_type* block_count;  //!< [num_blocks]
+    std::uint8_t* vacant;  //!< [num_slots]
+    size_type* count;  //!< [num_slots]
+    size_type num_blocks;
+};
+
+//! Error flags written by device code
+enum ErrorFlag : size_type
+{
+    error_initializer_overflow = 1u << 0,
+    error_primary_overflow = 1u << 1,
+};
+
+constexpr int block_size = 256;
+
+struct LaunchContext
+{
+    ParamsData params;
+    StateData state;
+    ScanScratch scratch;
+    StepRecord* log;  //!< Step log (ring buffer)
+    size_type log_capacity;
+    size_type* step_index;  //!< Device-resident step counter
+};
+
+// Individual action launchers (one thread per track slot)
+void launch_process_primaries(LaunchContext const& ctx,
+                              size_type num_primaries,
+                              cudaStream_t stream);
+void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream);
+void launch_pre_step(LaunchContext const& ctx, cudaStream_t stream);
+//! Along-step for tracks whose along-step action matches (all if invalid)
+void launch_along_step(LaunchContext const& ctx,
+                       size_type action,
+                       cudaStream_t stream);
+void launch_discrete_select(LaunchContext const& ctx, cudaStream_t stream);
+void launch_interact(LaunchContext const& ctx,
+                     size_type action,
+                     cudaStream_t stream);
+void launch_boundary(LaunchContext const& ctx, cudaStream_t stream);
+void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream);
+void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream);
+void launch_extend_from_secondaries(LaunchContext const& ctx,
+                                    cudaStream_t stream);
+void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
+
+//! One full step without primary insertion (graph-capturable)
+void launch_step(LaunchContext const& ctx, cudaStream_t stream);
+
+}  // namespace gbx

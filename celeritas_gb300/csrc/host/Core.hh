@@ -1,0 +1,267 @@
+// Host-side stepping-loop API with the reference's names and semantics:
+// StepActionOrder, ActionInterface / CoreStepActionInterface, ActionRegistry,
+// ActionSequence, CoreParams / CoreState and Stepper
+// (src/corecel/sys/ActionInterface.hh:29-186, ActionRegistry.hh:42-105,
+//  src/celeritas/global/ActionSequence.cc:37-138, CoreParams.hh:68-172,
+//  CoreState.hh:74-182, Stepper.hh:43-201).
+//
+// Each action's device step() launches one hand-written sm_103a kernel
+// through the C-ABI launch layer; state, counters and tables stay on the
+// device, and steps without primaries are replayed from a CUDA graph.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <string_view>
+#include <vector>
+
+#include "../device/Kernels.cuh"
+#include "HostParams.hh"
+
+namespace gbx
+{
+class CoreParams;
+class CoreState;
+
+//---------------------------------------------------------------------------//
+//! Ordering of step actions within a step (ActionInterface.hh:29-45)
+enum class StepActionOrder
+{
+    generate,
+    start,
+    user_start,
+    sort_start,
+    pre,
+    user_pre,
+    sort_pre,
+    along,
+    sort_along,
+    pre_post,
+    sort_pre_post,
+    post,
+    user_post,
+    end,
+    size_
+};
+
+using ActionId = size_type;
+
+//! Base class for all actions (ActionInterface.hh:78-96)
+class ActionInterface
+{
+  public:
+    virtual ~ActionInterface() = default;
+    virtual ActionId action_id() const = 0;
+    virtual std::string_view label() const = 0;
+    virtual std::string_view description() const = 0;
+};
+
+//! An action that acts on the core state every step (CoreStepActionInterface)
+class CoreStepActionInterface : public virtual ActionInterface
+{
+  public:
+    virtual StepActionOrder order() const = 0;
+    //! Launch the action's kernel(s) on the state's stream
+    virtual void step(CoreParams const& params, CoreState& state) const = 0;
+};
+
+//! Action with fixed ID, label and description (ConcreteAction)
+class ConcreteAction : public virtual ActionInterface
+{
+  public:
+    ConcreteAction(ActionId id, std::string label, std::string description)
+        : id_(id), label_(std::move(label)), description_(std::move(description))
+    {
+    }
+    ActionId action_id() const final { return id_; }
+    std::string_view label() const final { return label_; }
+    std::string_view description() const final { return description_; }
+
+  private:
+    ActionId id_;
+    std::string label_;
+    std::string description_;
+};
+
+//! Action with no step (implicit post-step limits such as "eloss-range")
+class ImplicitAction final : public ConcreteAction
+{
+  public:
+    using ConcreteAction::ConcreteAction;
+};
+
+//! Sequential registry of actions (ActionRegistry.hh:42-105)
+class ActionRegistry
+{
+  public:
+    using SPConstAction = std::shared_ptr<ActionInterface const>;
+
+    ActionId next_id() const { return static_cast<ActionId>(actions_.size()); }
+    void insert(SPConstAction action);
+    SPConstAction const& action(ActionId id) const { return actions_.at(id); }
+    std::string const& id_to_label(ActionId id) const { return labels_.at(id); }
+    ActionId find_action(std::string_view label) const;
+    ActionId num_actions() const { return static_cast<ActionId>(actions_.size()); }
+    bool empty() const { return actions_.empty(); }
+
+  private:
+    std::vector<SPConstAction> actions_;
+    std::vector<std::string> labels_;
+};
+
+//---------------------------------------------------------------------------//
+//! Immutable problem data on host and device (CoreParams)
+class CoreParams
+{
+  public:
+    struct Input
+    {
+        std::string physics_file;
+        GeometrySpec geometry;
+        ParamsOptions options;
+    };
+
+    explicit CoreParams(Input const& inp);
+    ~CoreParams();
+    CoreParams(CoreParams const&) = delete;
+    CoreParams& operator=(CoreParams const&) = delete;
+
+    HostParams const& host() const { return host_; }
+    ParamsData const& device_ref() const { return device_; }
+    ActionRegistry const& action_reg() const { return *actions_; }
+    ActionRegistry& action_reg() { return *actions_; }
+
+  private:
+    HostParams host_;
+    ParamsData device_{};
+    void* device_storage_{nullptr};
+    std::shared_ptr<ActionRegistry> actions_;
+};
+
+//---------------------------------------------------------------------------//
+//! Per-stream mutable track state on the device (CoreState)
+class CoreState
+{
+  public:
+    CoreState(CoreParams const& params,
+              size_type num_track_slots,
+              unsigned int seed,
+              size_type initializer_capacity,
+              size_type max_events,
+              cudaStream_t stream);
+    ~CoreState();
+    CoreState(CoreState const&) = delete;
+    CoreState& operator=(CoreState const&) = delete;
+
+    size_type size() const { return ref_.size; }
+    StateData const& ref() const { return ref_; }
+    LaunchContext const& context() const { return ctx_; }
+    cudaStream_t stream() const { return stream_; }
+
+    //! Stage primaries on the device for the next generate action
+    void insert_primaries(TrackInitializer const* host_primaries, size_type n);
+    size_type pending_primaries() const { return pending_primaries_; }
+    void clear_pending_primaries() { pending_primaries_ = 0; }
+
+    //! Copy the device counters to the host (synchronizes the stream)
+    Counters counters() const;
+    //! Number of completed steps recorded on the device
+    size_type step_index() const;
+    //! Read the step log entries [first, first + n)
+    std::vector<StepRecord> step_log(size_type first, size_type n) const;
+    size_type log_capacity() const { return ctx_.log_capacity; }
+
+  private:
+    StateData ref_{};
+    LaunchContext ctx_{};
+    void* storage_{nullptr};
+    TrackInitializer* pinned_primaries_{nullptr};
+    size_type pinned_capacity_{0};
+    size_type pending_primaries_{0};
+    cudaStream_t stream_{nullptr};
+};
+
+//---------------------------------------------------------------------------//
+//! Ordered list of step actions (ActionSequence)
+class ActionSequence
+{
+  public:
+    explicit ActionSequence(ActionRegistry const& reg);
+    void step(CoreParams const& params, CoreState& state) const;
+    std::vector<CoreStepActionInterface const*> const& actions() const
+    {
+        return actions_;
+    }
+
+  private:
+    std::vector<CoreStepActionInterface const*> actions_;
+};
+
+//! Stepper input (Stepper.hh:43-55)
+struct StepperInput
+{
+    std::shared_ptr<CoreParams const> params;
+    size_type stream_id{0};
+    size_type num_track_slots{0};
+    unsigned int seed{0};
+    size_type initializer_capacity{0};  //!< default 4 x slots (min 2^20)
+    size_type max_events{1u << 16};
+    bool use_graph{true};
+};
+
+//! Step counts (Stepper.hh:61-70)
+struct StepperResult
+{
+    size_type generated{0};
+    size_type queued{0};
+    size_type active{0};
+    size_type alive{0};
+    explicit operator bool() const { return queued > 0 || alive > 0; }
+};
+
+//! Step the track state, the reference's Stepper<MemSpace::device>
+class Stepper
+{
+  public:
+    explicit Stepper(StepperInput const& input);
+    ~Stepper();
+
+    //! Take one step with primaries
+    StepperResult operator()(std::vector<TrackInitializer> const& primaries);
+    //! Take one step
+    StepperResult operator()();
+    //! Take up to 'max_steps' steps until the state is empty; record counts
+    std::vector<StepperResult> run_until_empty(size_type max_steps,
+                                               size_type batch = 16);
+    //! Kill all tracks in flight
+    void kill_active();
+
+    CoreState& state() { return *state_; }
+    CoreParams const& params() const { return *params_; }
+    ActionSequence const& actions() const { return *actions_; }
+
+    //! Energy deposition per detector [MeV] (synchronizes)
+    std::vector<double> energy_deposition() const;
+    void clear_energy_deposition();
+
+  private:
+    std::shared_ptr<CoreParams const> params_;
+    std::unique_ptr<CoreState> state_;
+    std::unique_ptr<ActionSequence> actions_;
+    cudaStream_t stream_{nullptr};
+    cudaGraphExec_t graph_exec_{nullptr};
+    cudaGraph_t graph_{nullptr};
+    bool use_graph_{true};
+
+    void launch_steps(size_type count);
+    void build_graph();
+    StepperResult read_record(size_type index) const;
+};
+
+//! Register the stepping-loop actions in the reference's order and return
+//! the list (CoreParams::build_actions, PhysicsParams actions, models)
+void register_core_actions(ActionRegistry* reg);
+
+}  // namespace gbx

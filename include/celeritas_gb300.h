@@ -1,0 +1,157 @@
+/*
+ * C ABI of the GB300 electromagnetic-shower stepping loop.
+ *
+ * The boundary mirrors the reference's plugin API for the stepping loop:
+ *
+ *   - gbx_params_*   <-> celeritas::CoreParams (src/celeritas/global/CoreParams.hh:68-172)
+ *                        built as in celer-sim's Runner::build_core_params
+ *                        (app/celer-sim/Runner.cc:281-446)
+ *   - gbx_stepper_*  <-> celeritas::Stepper<MemSpace::device>
+ *                        (src/celeritas/global/Stepper.hh:43-201): operator(),
+ *                        operator()(Span<Primary const>), kill_active
+ *   - gbx_stepper_launch_action
+ *                    <-> CoreStepActionInterface::step(CoreParams const&,
+ *                        CoreStateDevice&) (src/corecel/sys/ActionInterface.hh:176-186),
+ *                        one call per registered action ID
+ *   - gbx_primary    <-> celeritas::Primary (src/celeritas/phys/Primary.hh:23-31)
+ *   - gbx_step_result <-> celeritas::StepperResult (src/celeritas/global/Stepper.hh:61-70)
+ *
+ * All functions return 0 on success and nonzero on failure; the message of
+ * the last failure on the calling thread is available from gbx_last_error().
+ * Plain pointers and sizes only: no C++ or framework types cross the ABI.
+ */
+#ifndef CELERITAS_GB300_H
+#define CELERITAS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbx_params_s gbx_params;
+typedef struct gbx_stepper_s gbx_stepper;
+
+/* A primary particle (celeritas::Primary): PDG code, kinetic energy [MeV],
+ * position [cm], unit direction, time [s], event index */
+typedef struct
+{
+    int pdg;
+    double energy;
+    double pos[3];
+    double dir[3];
+    double time;
+    unsigned int event_id;
+} gbx_primary;
+
+/* Track counts after a step (celeritas::StepperResult) */
+typedef struct
+{
+    unsigned int generated;
+    unsigned int queued;
+    unsigned int active;
+    unsigned int alive;
+} gbx_step_result;
+
+/* Message describing the last error on this thread ("" if none) */
+const char* gbx_last_error(void);
+
+/* Build problem parameters from a physics input file and a named geometry
+ * ("calo": 50-layer Pb/lAr sampling calorimeter). Replaces
+ * Runner::build_core_params (app/celer-sim/Runner.cc:281-446). */
+int gbx_params_create(const char* physics_file,
+                      const char* geometry,
+                      gbx_params** out);
+void gbx_params_destroy(gbx_params* params);
+/* Registered actions, in ID order (ActionRegistry::id_to_label,
+ * src/corecel/sys/ActionRegistry.hh:58-92) */
+int gbx_params_num_actions(const gbx_params* params, unsigned int* num);
+int gbx_params_action_label(const gbx_params* params,
+                            unsigned int action_id,
+                            char* buf,
+                            size_t buf_size);
+/* Energy-deposition detectors (SimpleCalo volume labels,
+ * src/celeritas/user/SimpleCalo.hh:40-86) */
+int gbx_params_num_detectors(const gbx_params* params, unsigned int* num);
+int gbx_params_detector_label(const gbx_params* params,
+                              unsigned int detector,
+                              char* buf,
+                              size_t buf_size);
+
+/* Create a stepper with its own device state and CUDA stream
+ * (Stepper(StepperInput), src/celeritas/global/Stepper.cc:66-87).
+ * 'use_graph' replays steps without primaries from a captured CUDA graph. */
+int gbx_stepper_create(gbx_params* params,
+                       unsigned int num_track_slots,
+                       unsigned int seed,
+                       int use_graph,
+                       gbx_stepper** out);
+void gbx_stepper_destroy(gbx_stepper* stepper);
+
+/* Take one step, inserting 'num_primaries' primaries first if nonzero
+ * (Stepper::operator()(Span<Primary const>) / operator()()) */
+int gbx_stepper_step(gbx_stepper* stepper,
+                     const gbx_primary* primaries,
+                     size_t num_primaries,
+                     gbx_step_result* result);
+
+/* Step until no tracks are queued or alive, or 'max_steps' steps; writes up
+ * to 'capacity' per-step results and the number of steps taken. Host reads
+ * happen every 'batch' steps only. (celer-sim Transporter loop,
+ * app/celer-sim/Transporter.cc:139-162) */
+int gbx_stepper_run(gbx_stepper* stepper,
+                    unsigned int max_steps,
+                    unsigned int batch,
+                    gbx_step_result* results,
+                    size_t capacity,
+                    unsigned int* num_steps);
+
+/* Launch the kernel(s) of one registered step action on the stepper's
+ * stream (CoreStepActionInterface::step for MemSpace::device) */
+int gbx_stepper_launch_action(gbx_stepper* stepper, unsigned int action_id);
+
+/* Stage primaries for the next extend-from-primaries action
+ * (ExtendFromPrimariesAction::insert, src/celeritas/track/ExtendFromPrimariesAction.cc:103-190) */
+int gbx_stepper_insert_primaries(gbx_stepper* stepper,
+                                 const gbx_primary* primaries,
+                                 size_t num_primaries);
+
+/* Kill all active tracks (Stepper::kill_active) */
+int gbx_stepper_kill_active(gbx_stepper* stepper);
+
+/* Wait for all work on the stepper's stream */
+int gbx_stepper_synchronize(gbx_stepper* stepper);
+
+/* Accumulated energy deposition per detector [MeV] (SimpleCalo
+ * calc_total_energy_deposition) and its reset */
+int gbx_stepper_energy_deposition(gbx_stepper* stepper,
+                                  double* out,
+                                  size_t num_detectors);
+int gbx_stepper_clear_energy_deposition(gbx_stepper* stepper);
+
+/* Copy one named state array between host and device (direction > 0:
+ * host -> device). Names: status, track_id, parent_id, event_id, num_steps,
+ * time, step_length, post_step_action, along_step_action, particle_id,
+ * energy, pos_x|y|z, dir_x|y|z, volume, surface, surface_sense, boundary,
+ * material, interaction_mfp, dedx_range, macro_xs, per_process_xs_0..3,
+ * energy_deposition, secondaries_offset, secondaries_count, element,
+ * rng (6 x slots words), vacancies, parents, counters, initializers,
+ * secondaries, detector. Used by tests to load a state snapshot, run one
+ * action and read the result. */
+int gbx_stepper_copy_state(gbx_stepper* stepper,
+                           const char* field,
+                           void* host,
+                           size_t nbytes,
+                           int direction);
+
+/* Bytes per element of a named state array and the number of elements */
+int gbx_stepper_state_info(gbx_stepper* stepper,
+                           const char* field,
+                           size_t* elem_bytes,
+                           size_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CELERITAS_GB300_H */
