@@ -326,6 +326,20 @@ int main(int argc, char** argv)
         std::string mode = argv[1];
         if (mode == "run")
             return run(argc, argv);
+        if (mode == "geo" && argc >= 4)
+        {
+            // Geometry tables built by the GB300 path's host code
+            HostParams hp = build_params(
+                argv[2], make_calorimeter_geometry(), ParamsOptions{});
+            for (std::size_t i = 0; i < hp.planes.size(); ++i)
+                std::printf("surf %zu axis %d position %.17g\n",
+                            i,
+                            hp.planes[i].axis,
+                            hp.planes[i].position);
+            for (std::size_t i = 0; i < hp.volume_labels.size(); ++i)
+                std::printf("volume %zu %s\n", i, hp.volume_labels[i].c_str());
+            return 0;
+        }
     }
     catch (std::exception const& e)
     {

@@ -1,0 +1,41 @@
+"""Shared test configuration: markers, golden fixtures and helpers."""
+
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(REPO, "tests", "golden")
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 GPU (sm_103a)")
+
+
+def load_golden(name: str) -> dict:
+    with open(os.path.join(GOLDEN, f"{name}.json")) as f:
+        return json.load(f)
+
+
+GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
+                "calo_ep500_n4", "calo_e1000_n100"]
+
+
+@pytest.fixture(scope="session")
+def built_port():
+    import oracle
+
+    return oracle.build_port()
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    from celeritas_gb300.build import build
+
+    return build()

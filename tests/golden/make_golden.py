@@ -1,0 +1,91 @@
+"""Generate the golden fixtures of the stepping loop from the reference.
+
+Runs the reference's own host stepping loop (oracle/ref, compiled from the
+reference sources) on the committed synthetic physics input and records,
+per case: the ordered action labels, the per-step StepperResult counters
+(generated, queued, active, alive), the total track-steps and the energy
+deposition per calorimeter volume. Also records the ORANGE surface data of
+the calorimeter geometry.
+
+Usage (where the reference sources are present):
+    python tests/golden/make_golden.py [--reference /path/to/reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+import oracle  # noqa: E402
+from celeritas_gb300 import physics_file  # noqa: E402
+from celeritas_gb300.primaries import pencil_beam, write_primaries_text  # noqa: E402
+
+# name: (pdg, energy [MeV], number of primaries, track slots, seed)
+CASES = {
+    "calo_e1000_n4": (11, 1000.0, 4, 65536, 0),
+    "calo_e1000_n4_slots512": (11, 1000.0, 4, 512, 0),
+    "calo_g100_n16": (22, 100.0, 16, 4096, 7),
+    "calo_ep500_n4": (-11, 500.0, 4, 4096, 3),
+    "calo_e1000_n100": (11, 1000.0, 100, 65536, 0),
+}
+
+
+def make_case(name: str) -> dict:
+    pdg, energy, num, slots, seed = CASES[name]
+    prim = pencil_beam(num, energy=energy, pdg=pdg)
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "primaries.txt")
+        write_primaries_text(ptxt, prim)
+        out = oracle.run_reference(physics_file("calo"), ptxt, slots, seed)
+    return {
+        "case": {"geometry": "calo", "pdg": pdg, "energy": energy,
+                 "num_primaries": num, "num_track_slots": slots, "seed": seed,
+                 "z0": -5.0},
+        "actions": [out["actions"][i] for i in sorted(out["actions"])],
+        "steps": out["steps"],
+        "total_steps": out["total_steps"],
+        "iterations": out["iterations"],
+        "edep": out["edep"],
+    }
+
+
+def geometry_dump() -> dict:
+    res = subprocess.run([oracle.REF_BIN, "geo", "x", "calo"], capture_output=True,
+                         text=True, check=True)
+    surfaces = []
+    volumes = []
+    for line in res.stdout.splitlines():
+        tok = line.split()
+        if tok and tok[0] == "surf":
+            surfaces.append({"type": int(tok[3]), "position": float(tok[5])})
+        elif tok and tok[0] == "volume":
+            volumes.append(tok[2])
+    return {"surfaces": surfaces, "volumes": volumes}
+
+
+def main():
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--reference", default=oracle.REFERENCE_DEFAULT)
+    parser.add_argument("--cases", nargs="*", default=list(CASES))
+    args = parser.parse_args()
+    if oracle.build_reference(args.reference) is None:
+        sys.exit("reference sources not found")
+    for name in args.cases:
+        data = make_case(name)
+        with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+            json.dump(data, f, indent=0)
+        print(name, data["iterations"], data["total_steps"])
+    with open(os.path.join(HERE, "calo_geometry.json"), "w") as f:
+        json.dump(geometry_dump(), f, indent=0)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,69 @@
+"""The CPU oracle against the reference's golden fixtures (no GPU).
+
+The golden fixtures were produced by the reference's own host stepping loop
+(tests/golden/make_golden.py). The CPU restatement must reproduce them bit
+for bit: every per-step counter, the number of iterations, the total
+track-steps and every per-volume energy deposition.
+"""
+
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden
+
+import oracle
+from celeritas_gb300 import physics_file
+from celeritas_gb300.primaries import pencil_beam, write_primaries_text
+
+
+def run_case(golden):
+    c = golden["case"]
+    prim = pencil_beam(c["num_primaries"], energy=c["energy"], pdg=c["pdg"], z0=c["z0"])
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "p.txt")
+        write_primaries_text(ptxt, prim)
+        return oracle.run_port(physics_file("calo"), ptxt, c["num_track_slots"], c["seed"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_port_matches_reference(built_port, name):
+    golden = load_golden(name)
+    out = run_case(golden)
+    assert [list(s) for s in out["steps"]] == golden["steps"]
+    assert out["total_steps"] == golden["total_steps"]
+    assert out["iterations"] == golden["iterations"]
+    assert out["edep"] == golden["edep"]  # bit-exact FP64
+
+
+def test_action_labels_match_reference(built_port):
+    golden = load_golden("calo_e1000_n4")
+    out = run_case(golden)
+    assert [out["actions"][i] for i in sorted(out["actions"])] == golden["actions"]
+
+
+def test_geometry_matches_orange(built_port):
+    """Surfaces and volumes built by the GB300 host code equal ORANGE's."""
+    golden = load_golden("calo_geometry")
+    res = subprocess.run([built_port, "geo", physics_file("calo"), "calo"],
+                         capture_output=True, text=True, check=True)
+    surfs, vols = [], []
+    for line in res.stdout.splitlines():
+        tok = line.split()
+        if tok[0] == "surf":
+            surfs.append((int(tok[3]), float(tok[5])))
+        elif tok[0] == "volume":
+            vols.append(tok[2])
+    assert [(s["type"], s["position"]) for s in golden["surfaces"]] == surfs
+    assert golden["volumes"] == vols
+
+
+def test_energy_conservation_bound(built_port):
+    """Deposited energy never exceeds the primaries' kinetic energy."""
+    golden = load_golden("calo_e1000_n4")
+    edep = np.array(list(golden["edep"].values()))
+    assert 0 < edep.sum() <= 4 * 1000.0
+    assert (edep >= 0).all()
