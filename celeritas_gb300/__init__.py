@@ -88,6 +88,12 @@ _PROTOTYPES = [
      [ctypes.c_void_p, ctypes.POINTER(_Primary), ctypes.c_size_t]),
     ("gbx_stepper_kill_active", ctypes.c_int, [ctypes.c_void_p]),
     ("gbx_stepper_synchronize", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_stream", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    ("gbx_stepper_step_kernels", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    ("gbx_stepper_set_action_times", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("gbx_stepper_action_times", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint),
+      ctypes.c_size_t]),
     ("gbx_stepper_energy_deposition", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t]),
     ("gbx_stepper_clear_energy_deposition", ctypes.c_int, [ctypes.c_void_p]),
@@ -237,6 +243,31 @@ class Stepper:
 
     def kill_active(self):
         _check(_lib.gbx_stepper_kill_active(self._handle))
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the stepper, as an integer (for event timing)."""
+        s = ctypes.c_void_p()
+        _check(_lib.gbx_stepper_stream(self._handle, ctypes.byref(s)))
+        return s.value or 0
+
+    def step_kernels(self) -> int:
+        """Kernel launches in one graph-replayed step."""
+        n = ctypes.c_uint()
+        _check(_lib.gbx_stepper_step_kernels(self._handle, ctypes.byref(n)))
+        return n.value
+
+    def set_action_times(self, enable: bool = True):
+        _check(_lib.gbx_stepper_set_action_times(self._handle, int(enable)))
+
+    def action_times(self) -> tuple[np.ndarray, np.ndarray]:
+        """Accumulated device ms and launch counts per action ID (then reset)."""
+        n = len(self.params.action_labels())
+        ms = np.zeros(n, dtype=np.float64)
+        nl = np.zeros(n, dtype=np.uint32)
+        _check(_lib.gbx_stepper_action_times(
+            self._handle, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            nl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), n))
+        return ms, nl
 
     def energy_deposition(self) -> np.ndarray:
         n = len(self.params.detector_labels())

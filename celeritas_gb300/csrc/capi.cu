@@ -339,6 +339,41 @@ int gbx_stepper_synchronize(gbx_stepper* stepper)
     });
 }
 
+int gbx_stepper_stream(gbx_stepper* stepper, void** stream)
+{
+    return guarded([&] { *stream = stepper->stepper->state().stream(); });
+}
+
+int gbx_stepper_step_kernels(gbx_stepper* stepper, unsigned int* num_kernels)
+{
+    return guarded([&] { *num_kernels = stepper->stepper->graph_kernel_count(); });
+}
+
+int gbx_stepper_set_action_times(gbx_stepper* stepper, int enable)
+{
+    return guarded([&] { stepper->stepper->set_action_times(enable != 0); });
+}
+
+int gbx_stepper_action_times(gbx_stepper* stepper,
+                             double* milliseconds,
+                             unsigned int* launches,
+                             size_t capacity)
+{
+    return guarded([&] {
+        auto& seq = stepper->stepper->action_sequence();
+        auto ms = seq.action_times();
+        auto nl = seq.action_launches();
+        for (size_t i = 0; i < ms.size() && i < capacity; ++i)
+        {
+            if (milliseconds)
+                milliseconds[i] = ms[i];
+            if (launches)
+                launches[i] = nl[i];
+        }
+        seq.reset_action_times();
+    });
+}
+
 int gbx_stepper_energy_deposition(gbx_stepper* stepper,
                                   double* out,
                                   size_t num_detectors)

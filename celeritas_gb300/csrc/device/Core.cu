@@ -563,13 +563,82 @@ ActionSequence::ActionSequence(ActionRegistry const& reg)
                              return a->order() < b->order();
                          return a->action_id() < b->action_id();
                      });
+    num_ids_ = reg.num_actions();
+    elapsed_.assign(num_ids_, 0.0);
+    launches_.assign(num_ids_, 0);
+    pending_.assign(num_ids_, false);
+}
+
+ActionSequence::~ActionSequence()
+{
+    for (auto e : start_)
+        cudaEventDestroy(e);
+    for (auto e : stop_)
+        cudaEventDestroy(e);
+}
+
+void ActionSequence::enable_action_times(bool enable)
+{
+    if (enable && start_.empty())
+    {
+        start_.resize(num_ids_);
+        stop_.resize(num_ids_);
+        for (size_type i = 0; i < num_ids_; ++i)
+        {
+            GBX_CUDA(cudaEventCreate(&start_[i]));
+            GBX_CUDA(cudaEventCreate(&stop_[i]));
+        }
+    }
+    timing_ = enable;
+}
+
+void ActionSequence::collect() const
+{
+    for (size_type i = 0; i < num_ids_; ++i)
+    {
+        if (pending_[i])
+        {
+            float ms = 0;
+            GBX_CUDA(cudaEventSynchronize(stop_[i]));
+            GBX_CUDA(cudaEventElapsedTime(&ms, start_[i], stop_[i]));
+            elapsed_[i] += ms;
+            pending_[i] = false;
+        }
+    }
+}
+
+std::vector<double> ActionSequence::action_times() const
+{
+    this->collect();
+    return elapsed_;
+}
+
+void ActionSequence::reset_action_times()
+{
+    this->collect();
+    elapsed_.assign(num_ids_, 0.0);
+    launches_.assign(num_ids_, 0);
 }
 
 void ActionSequence::step(CoreParams const& params, CoreState& state) const
 {
+    if (!timing_)
+    {
+        for (auto const* a : actions_)
+            a->step(params, state);
+        return;
+    }
+    // Events bracket each action on the state's stream; accumulate the
+    // previous step's timings before reusing the events
+    this->collect();
     for (auto const* a : actions_)
     {
+        ActionId id = a->action_id();
+        GBX_CUDA(cudaEventRecord(start_[id], state.stream()));
         a->step(params, state);
+        GBX_CUDA(cudaEventRecord(stop_[id], state.stream()));
+        pending_[id] = true;
+        ++launches_[id];
     }
 }
 
@@ -610,11 +679,31 @@ void Stepper::build_graph()
     GBX_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
 }
 
+size_type Stepper::graph_kernel_count()
+{
+    if (!graph_exec_)
+        this->build_graph();
+    std::size_t num_nodes = 0;
+    GBX_CUDA(cudaGraphGetNodes(graph_, nullptr, &num_nodes));
+    std::vector<cudaGraphNode_t> nodes(num_nodes);
+    GBX_CUDA(cudaGraphGetNodes(graph_, nodes.data(), &num_nodes));
+    size_type kernels = 0;
+    for (auto node : nodes)
+    {
+        cudaGraphNodeType type;
+        GBX_CUDA(cudaGraphNodeGetType(node, &type));
+        if (type == cudaGraphNodeTypeKernel)
+            ++kernels;
+    }
+    return kernels;
+}
+
 void Stepper::launch_steps(size_type count)
 {
     for (size_type i = 0; i < count; ++i)
     {
-        if (use_graph_ && state_->pending_primaries() == 0)
+        if (use_graph_ && state_->pending_primaries() == 0
+            && !actions_->action_times_enabled())
         {
             if (!graph_exec_)
                 this->build_graph();

@@ -189,14 +189,33 @@ class ActionSequence
 {
   public:
     explicit ActionSequence(ActionRegistry const& reg);
+    ~ActionSequence();
     void step(CoreParams const& params, CoreState& state) const;
     std::vector<CoreStepActionInterface const*> const& actions() const
     {
         return actions_;
     }
 
+    //! Record device time per action with CUDA events on the state's stream
+    //! (the reference's StepperInput::action_times; disables graph replay)
+    void enable_action_times(bool enable);
+    bool action_times_enabled() const { return timing_; }
+    //! Accumulated device milliseconds per action ID (synchronizes)
+    std::vector<double> action_times() const;
+    //! Number of timed launches per action ID
+    std::vector<size_type> action_launches() const { return launches_; }
+    void reset_action_times();
+
   private:
     std::vector<CoreStepActionInterface const*> actions_;
+    size_type num_ids_{0};
+    bool timing_{false};
+    mutable std::vector<cudaEvent_t> start_;
+    mutable std::vector<cudaEvent_t> stop_;
+    mutable std::vector<double> elapsed_;
+    mutable std::vector<size_type> launches_;
+    mutable std::vector<bool> pending_;
+    void collect() const;
 };
 
 //! Stepper input (Stepper.hh:43-55)
@@ -241,6 +260,13 @@ class Stepper
     CoreState& state() { return *state_; }
     CoreParams const& params() const { return *params_; }
     ActionSequence const& actions() const { return *actions_; }
+
+    //! Kernel nodes in the captured step graph (captures it if needed)
+    size_type graph_kernel_count();
+
+    //! Time each action's kernels with CUDA events (action_times)
+    void set_action_times(bool enable) { actions_->enable_action_times(enable); }
+    ActionSequence& action_sequence() { return *actions_; }
 
     //! Energy deposition per detector [MeV] (synchronizes)
     std::vector<double> energy_deposition() const;

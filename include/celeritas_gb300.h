@@ -122,6 +122,23 @@ int gbx_stepper_kill_active(gbx_stepper* stepper);
 /* Wait for all work on the stepper's stream */
 int gbx_stepper_synchronize(gbx_stepper* stepper);
 
+/* The stepper's CUDA stream (a cudaStream_t) for event timing by callers */
+int gbx_stepper_stream(gbx_stepper* stepper, void** stream);
+
+/* Number of kernel nodes in one graph-replayed step (builds the graph) */
+int gbx_stepper_step_kernels(gbx_stepper* stepper, unsigned int* num_kernels);
+
+/* Time every action's kernels with CUDA events on the stepper's stream
+ * (StepperInput::action_times, src/celeritas/global/Stepper.hh:43-55; steps
+ * are then launched eagerly instead of from the CUDA graph) */
+int gbx_stepper_set_action_times(gbx_stepper* stepper, int enable);
+/* Accumulated milliseconds and launch counts per action ID ('capacity'
+ * entries, indexed by action ID); the counters are then reset */
+int gbx_stepper_action_times(gbx_stepper* stepper,
+                             double* milliseconds,
+                             unsigned int* launches,
+                             size_t capacity);
+
 /* Accumulated energy deposition per detector [MeV] (SimpleCalo
  * calc_total_energy_deposition) and its reset */
 int gbx_stepper_energy_deposition(gbx_stepper* stepper,

@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <iostream>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -312,6 +313,79 @@ int run(int argc, char** argv)
     return 0;
 }
 
+//! Timed CPU baseline: events distributed over threads, one stepper per
+//! thread, each event transported to completion (celer-sim with
+//! CELERITAS_OPENMP=event, app/celer-sim/celer-sim.cc:126-138)
+int bench(int argc, char** argv)
+{
+    if (argc < 7)
+        return 2;
+    std::string phys = argv[2], geo = argv[3], prim = argv[4];
+    size_type slots = std::stoul(argv[5]);
+    unsigned int seed = std::stoul(argv[6]);
+    unsigned int threads = 1;
+    for (int i = 7; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--threads")
+            threads = std::stoul(argv[++i]);
+    }
+    if (geo != "calo")
+        throw std::runtime_error("unknown geometry " + geo);
+    HostParams hp
+        = build_params(phys, make_calorimeter_geometry(), ParamsOptions{});
+    auto primaries = load_primaries(prim);
+    // Group primaries by event
+    std::map<size_type, std::vector<TrackInitializer>> events;
+    for (auto const& p : primaries)
+        events[p.event_id].push_back(p);
+    std::vector<std::vector<TrackInitializer>> ev_list;
+    for (auto& kv : events)
+    {
+        for (auto& p : kv.second)
+            p.event_id = 0;
+        ev_list.push_back(std::move(kv.second));
+    }
+    std::vector<unsigned long long> steps(threads, 0);
+    std::vector<size_type> done(threads, 0);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (unsigned int t = 0; t < threads; ++t)
+    {
+        pool.emplace_back([&, t] {
+            PortStepper step(hp, slots, seed + t, 1);
+            for (std::size_t e = t; e < ev_list.size(); e += threads)
+            {
+                StepCounts c = step(ev_list[e]);
+                steps[t] += c.active;
+                while (c)
+                {
+                    c = step();
+                    steps[t] += c.active;
+                }
+                ++done[t];
+            }
+        });
+    }
+    for (auto& th : pool)
+        th.join();
+    auto t1 = std::chrono::steady_clock::now();
+    unsigned long long total = 0;
+    size_type nev = 0;
+    for (unsigned int t = 0; t < threads; ++t)
+    {
+        total += steps[t];
+        nev += done[t];
+    }
+    double sec = std::chrono::duration<double>(t1 - t0).count();
+    std::printf("bench threads %u events %u track_steps %llu seconds %.6f\n",
+                threads,
+                nev,
+                total,
+                sec);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv)
@@ -326,6 +400,8 @@ int main(int argc, char** argv)
         std::string mode = argv[1];
         if (mode == "run")
             return run(argc, argv);
+        if (mode == "bench")
+            return bench(argc, argv);
         if (mode == "geo" && argc >= 4)
         {
             // Geometry tables built by the GB300 path's host code
