@@ -36,11 +36,21 @@ import numpy as np  # noqa: E402
 
 WORKLOADS = {
     # configs[0]: 50-layer Pb/lAr calorimeter, 100 e- at 1 GeV, pencil beam,
-    # no field, no MSC, 2^16 slots, seed 0
+    # no field, no MSC, 2^16 slots, seed 0 (one event of 100 primaries)
     "c1": dict(geometry="calo", physics="calo", num_primaries=100, energy=1000.0,
-               pdg=11, slots=1 << 16, seed=0, events=1,
+               emax=None, sigma=0.0, pdg=11, slots=1 << 16, seed=0, events=1,
+               msc=False, field=(0.0, 0.0, 0.0),
                description="calorimeter 50x(2.3mm Pb+5.7mm lAr), 100 e- @ 1 GeV "
-                           "pencil beam, no field, no MSC, 2^16 track slots"),
+                           "pencil beam, no field, no MSC, 2^16 track slots, FP64"),
+    # configs[1]: same calorimeter with Urban MSC and a uniform 1 T field
+    # along x; 10^4 e-, log-uniform 100 MeV-10 GeV, Gaussian spread 1 cm,
+    # 2^20 slots; each primary is its own event, all events in flight
+    "c2": dict(geometry="calo", physics="calo", num_primaries=10000, energy=100.0,
+               emax=1e4, sigma=1.0, pdg=11, slots=1 << 20, seed=0, events=10000,
+               msc=True, field=(1.0, 0.0, 0.0),
+               description="calorimeter 50x(2.3mm Pb+5.7mm lAr), Urban MSC, 1 T "
+                           "uniform field along x, 10^4 e- log-uniform 0.1-10 GeV, "
+                           "sigma 1 cm, 2^20 track slots, FP64"),
 }
 
 
@@ -53,13 +63,28 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def make_primaries(wl, rank=0):
-    from celeritas_gb300.primaries import pencil_beam
+def make_primaries(wl, rank=0, num=None, seed_offset=0):
+    from celeritas_gb300.primaries import pencil_beam, spread_beam
 
-    p = pencil_beam(wl["num_primaries"], energy=wl["energy"], pdg=wl["pdg"],
-                    num_events=wl["events"])
+    num = wl["num_primaries"] if num is None else num
+    if wl["emax"] is None:
+        p = pencil_beam(num, energy=wl["energy"], pdg=wl["pdg"],
+                        num_events=min(wl["events"], num))
+    else:
+        p = spread_beam(num, emin=wl["energy"], emax=wl["emax"], sigma=wl["sigma"],
+                        pdg=wl["pdg"], seed=wl["seed"] + 1000 * rank + seed_offset,
+                        num_events=min(wl["events"], num))
     p["event"] += rank * wl["events"]
     return p
+
+
+def physics_args(wl):
+    args = []
+    if wl["msc"]:
+        args.append("--msc")
+    if any(wl["field"]):
+        args += ["--field"] + [repr(float(f)) for f in wl["field"]]
+    return args
 
 
 class ClockSampler:
@@ -121,21 +146,28 @@ def cpu_baseline(wl, threads, target_seconds=15.0, events=None):
     """Time the oracle's CPU restatement on the host cores (bounded sample)."""
     import oracle
     from celeritas_gb300 import physics_file
-    from celeritas_gb300.primaries import pencil_beam, write_primaries_text
+    from celeritas_gb300.primaries import write_primaries_text
 
     exe = oracle.build_port()
-    # One primary per event, events distributed over threads; each thread's
-    # stepper gets the workload's slots divided among streams (celer-sim)
-    slots = max(1024, wl["slots"] // threads)
+    # One primary per event, events distributed over threads (celer-sim with
+    # one stream per thread). A CPU stepper visits every slot each step, so
+    # each thread gets 4096 slots (enough for one shower of the workload):
+    # a CPU-favourable setting rather than the GPU's slot count per stream
+    slots = 4096
     if events is None:
-        # ~6.4k track-steps per GeV; CPU rate ~ 1e5-1e6 steps/s/thread
-        events = max(threads, 2 * threads)
-    prim = pencil_beam(events, energy=wl["energy"], pdg=wl["pdg"], num_events=events)
+        # Calibrate on a short sample, then size the sample to target_seconds
+        probe = cpu_baseline(wl, threads, events=2 * threads)
+        steps_per_event = probe["value"] / probe["events_per_s"]
+        events = int(target_seconds * probe["value"] / max(steps_per_event, 1.0))
+        events = max(2 * threads, min(events, 20000))
+    prim = make_primaries(wl, num=events)
+    prim["event"] = np.arange(events)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
         res = subprocess.run([exe, "bench", physics_file(wl["physics"]), wl["geometry"], ptxt,
-                              str(slots), str(wl["seed"]), "--threads", str(threads)],
+                              str(slots), str(wl["seed"]), "--threads", str(threads)]
+                             + physics_args(wl),
                              capture_output=True, text=True, check=True)
     tok = res.stdout.split()
     nev, steps, sec = int(tok[4]), int(tok[6]), float(tok[8])
@@ -145,8 +177,9 @@ def cpu_baseline(wl, threads, target_seconds=15.0, events=None):
         "events_per_s": nev / sec,
         "cores": threads,
         "kind": "port",
-        "sample": f"{nev} events of 1 x {wl['energy']:.0f} MeV e- ({steps} track-steps) "
-                  f"on {threads} threads, {slots} slots per thread stepper, {sec:.2f} s",
+        "sample": f"first {nev} events of the workload, 1 primary each ({steps} "
+                  f"track-steps) on {threads} threads, {slots} slots per thread "
+                  f"stepper, {sec:.2f} s",
     }
 
 
@@ -158,8 +191,13 @@ def run_reference(args, wl):
     threads = os.cpu_count() or 1
     vals, evs = [], []
     base = None
+    # Size each step's sample to ~8 s of CPU work from a short probe
+    probe = cpu_baseline(wl, threads, events=2 * threads)
+    steps_per_event = probe["value"] / probe["events_per_s"]
+    events = int(8.0 * probe["value"] / max(steps_per_event, 1.0))
+    events = max(2 * threads, min(events, 20000))
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(wl, threads, events=2 * threads)
+        r = cpu_baseline(wl, threads, events=events)
         if i >= args.warmup:
             vals.append(r["value"])
             evs.append(r["events_per_s"])
@@ -211,7 +249,8 @@ def run_gb300(args, wl):
         dist.barrier()
     gb.load_library()
 
-    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"])
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                       field_tesla=wl["field"], msc=wl["msc"])
     labels = params.action_labels()
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     stream = torch.cuda.ExternalStream(stepper.stream_handle())
@@ -350,7 +389,7 @@ def main():
     parser.add_argument("--steps", type=int, default=10)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    parser.add_argument("--workload", default="c1", choices=list(WORKLOADS))
+    parser.add_argument("--workload", default="c2", choices=list(WORKLOADS))
     parser.add_argument("--no-cpu-baseline", action="store_true")
     args = parser.parse_args()
     if args.warmup < 3:

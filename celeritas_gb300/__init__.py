@@ -41,6 +41,10 @@ class _Primary(ctypes.Structure):
     ]
 
 
+class _ParamsOptions(ctypes.Structure):
+    _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int)]
+
+
 class _StepResult(ctypes.Structure):
     _fields_ = [
         ("generated", ctypes.c_uint),
@@ -67,7 +71,8 @@ _lib = None
 _PROTOTYPES = [
     ("gbx_last_error", ctypes.c_char_p, []),
     ("gbx_params_create", ctypes.c_int,
-     [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+     [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_ParamsOptions),
+      ctypes.POINTER(ctypes.c_void_p)]),
     ("gbx_params_destroy", None, [ctypes.c_void_p]),
     ("gbx_params_num_actions", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
     ("gbx_params_action_label", ctypes.c_int,
@@ -140,12 +145,20 @@ def physics_file(problem: str) -> str:
 class Params:
     """Problem parameters on the device (celeritas::CoreParams)."""
 
-    def __init__(self, physics: str, geometry: str = "calo"):
+    def __init__(self, physics: str, geometry: str = "calo",
+                 field_tesla=(0.0, 0.0, 0.0), msc: bool = False):
         lib = load_library()
         handle = ctypes.c_void_p()
-        _check(lib.gbx_params_create(physics.encode(), geometry.encode(), ctypes.byref(handle)))
+        opts = _ParamsOptions()
+        for i in range(3):
+            opts.field_tesla[i] = float(field_tesla[i])
+        opts.msc = int(msc)
+        _check(lib.gbx_params_create(physics.encode(), geometry.encode(),
+                                     ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle
         self.geometry = geometry
+        self.field_tesla = tuple(field_tesla)
+        self.msc = msc
 
     def __del__(self):
         if getattr(self, "_handle", None) and _lib is not None:

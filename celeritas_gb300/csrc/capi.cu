@@ -177,6 +177,7 @@ const char* gbx_last_error(void)
 
 int gbx_params_create(const char* physics_file,
                       const char* geometry,
+                      const gbx_params_options* options,
                       gbx_params** out)
 {
     return guarded([&] {
@@ -185,6 +186,12 @@ int gbx_params_create(const char* physics_file,
         gbx::CoreParams::Input inp;
         inp.physics_file = physics_file;
         inp.geometry = geometry_by_name(geometry);
+        if (options)
+        {
+            inp.options.msc = options->msc != 0;
+            for (int i = 0; i < 3; ++i)
+                inp.options.field_tesla[i] = options->field_tesla[i];
+        }
         auto p = std::make_unique<gbx_params_s>();
         p->params = std::make_shared<gbx::CoreParams>(inp);
         *out = p.release();

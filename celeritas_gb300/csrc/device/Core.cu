@@ -158,7 +158,7 @@ ActionId ActionRegistry::find_action(std::string_view label) const
     return invalid_id;
 }
 
-void register_core_actions(ActionRegistry* reg)
+void register_core_actions(ActionRegistry* reg, bool uniform_field)
 {
     using O = StepActionOrder;
     auto add = [reg](std::string label,
@@ -207,8 +207,9 @@ void register_core_actions(ActionRegistry* reg)
     implicit("physics-failure",
              "mark a track that failed to sample an interaction");
     // Along-step action registered by the driver
-    add("along-step-general-linear",
-        "apply along-step for particles with no field",
+    add(uniform_field ? "along-step-uniform-msc" : "along-step-general-linear",
+        uniform_field ? "apply along-step in a uniform field"
+                      : "apply along-step for particles with no field",
         O::along,
         step_along);
     // CoreParams actions
@@ -244,7 +245,7 @@ CoreParams::CoreParams(Input const& inp)
     : host_(build_params(inp.physics_file, inp.geometry, inp.options))
     , actions_(std::make_shared<ActionRegistry>())
 {
-    register_core_actions(actions_.get());
+    register_core_actions(actions_.get(), host_.scalars.has_field);
     for (size_type i = 0; i < host_.action_labels.size(); ++i)
     {
         if (actions_->id_to_label(i) != host_.action_labels[i])
@@ -266,6 +267,10 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_lve = pk.add(h.lv_elements);
     std::size_t o_lvs = pk.add(h.lv_shells);
     std::size_t o_sb = pk.add(h.sb_tables);
+    std::size_t o_rb = pk.add(h.rb_elements);
+    std::size_t o_mscm = pk.add(h.msc_materials);
+    std::size_t o_mscp = pk.add(h.msc_par_mat);
+    std::size_t o_loop = pk.add(h.looping);
     std::size_t o_pl = pk.add(h.planes);
     std::size_t o_box = pk.add(h.boxes);
     std::size_t o_no = pk.add(h.neighbor_offset);
@@ -292,6 +297,10 @@ CoreParams::CoreParams(Input const& inp)
         = reinterpret_cast<LivermoreElement const*>(base + o_lve);
     device_.livermore_shells = reinterpret_cast<LivermoreShell const*>(base + o_lvs);
     device_.sb_tables = reinterpret_cast<SBElementTable const*>(base + o_sb);
+    device_.rb_elements = reinterpret_cast<RelBremElementRecord const*>(base + o_rb);
+    device_.msc.material = reinterpret_cast<UrbanMscMaterialRecord const*>(base + o_mscm);
+    device_.msc.par_mat = reinterpret_cast<UrbanMscParMatRecord const*>(base + o_mscp);
+    device_.looping = reinterpret_cast<LoopingRecord const*>(base + o_loop);
     device_.geo.planes = reinterpret_cast<PlaneRecord const*>(base + o_pl);
     device_.geo.boxes = reinterpret_cast<BoxVolume const*>(base + o_box);
     device_.geo.neighbor_offset = reinterpret_cast<size_type const*>(base + o_no);
@@ -349,6 +358,10 @@ CoreState::CoreState(CoreParams const& params,
         o = arr(sizeof(real_type));
     std::size_t o_edep = arr(sizeof(real_type)), o_soff = arr(4),
                 o_scount = arr(4), o_elem = arr(4);
+    std::size_t o_mdisp = arr(1), o_mtrue = arr(sizeof(real_type)),
+                o_mgeom = arr(sizeof(real_type)), o_malpha = arr(sizeof(real_type)),
+                o_mrinit = arr(sizeof(real_type)), o_mrfac = arr(sizeof(real_type)),
+                o_mlmin = arr(sizeof(real_type)), o_nloop = arr(4);
     std::size_t o_rng = L.reserve(std::size_t(6) * 4 * n);
     std::size_t o_vac = arr(4), o_cnts = arr(4), o_parents = arr(4);
     std::size_t o_inits = L.reserve(sizeof(TrackInitializer) * std::size_t(init_cap));
@@ -407,6 +420,14 @@ CoreState::CoreState(CoreParams const& params,
     s.secondaries_offset = static_cast<size_type*>(at(o_soff));
     s.secondaries_count = static_cast<size_type*>(at(o_scount));
     s.element = static_cast<size_type*>(at(o_elem));
+    s.msc_displaced = static_cast<std::uint8_t*>(at(o_mdisp));
+    s.msc_true_path = static_cast<real_type*>(at(o_mtrue));
+    s.msc_geom_path = static_cast<real_type*>(at(o_mgeom));
+    s.msc_alpha = static_cast<real_type*>(at(o_malpha));
+    s.msc_range_init = static_cast<real_type*>(at(o_mrinit));
+    s.msc_range_factor = static_cast<real_type*>(at(o_mrfac));
+    s.msc_limit_min = static_cast<real_type*>(at(o_mlmin));
+    s.num_looping_steps = static_cast<size_type*>(at(o_nloop));
     auto* rng = static_cast<std::uint32_t*>(at(o_rng));
     for (int w = 0; w < 5; ++w)
         s.rng.s[w] = rng + std::size_t(w) * n;

@@ -16,8 +16,10 @@
 //                     SimpleCaloExecutor.hh:48-67
 #pragma once
 
+#include "Field.hh"
 #include "Geometry.hh"
 #include "Interactors.hh"
+#include "Msc.hh"
 
 namespace gbx
 {
@@ -225,26 +227,83 @@ GBX_FUNCTION void along_step(ParamsData const& p, StateData const& s, size_type 
         return;
     bool const charged = (along == p.action_along_step);
 
-    // PropagationApplier with the linear propagator
+    // MscStepLimitApplier
+    if (charged && p.msc.enabled)
+    {
+        XorwowEngine rng(s.rng, slot);
+        msc_limit_step(p, s, slot, rng);
+    }
+
+    // PropagationApplier: straight line, or the uniform-field integrator for
+    // charged tracks (which can loop)
     double const step_length = s.step_length[slot];
     if (step_length != 0)
     {
         GeoTrackView geo(p.geo, s, slot);
-        Propagation prop = geo.find_next_step(step_length);
-        if (prop.boundary)
-            geo.move_to_boundary();
+        if (charged && p.has_field)
+        {
+            size_type const pid = s.particle_id[slot];
+            real_type const mass = p.particles[pid].mass;
+            real_type const energy = s.energy[slot];
+            double const momentum = std::sqrt(double(momentum_sq(mass, energy)));
+            UniformFieldEquation rhs;
+            rhs.field = {p.field[0], p.field[1], p.field[2]};
+            rhs.coeffi = (p.particles[pid].charge * detail::e_electron)
+                         / (1 * (detail::mev_value / constants::c_light));
+            FieldOptions const opt;
+            Propagation prop = propagate_in_field(opt, rhs, momentum, geo, step_length);
+            // update_looping
+            if (prop.looping)
+                ++s.num_looping_steps[slot];
+            else
+                s.num_looping_steps[slot] = 0;
+            if (prop.looping)
+            {
+                s.step_length[slot] = prop.distance;
+                LoopingRecord const& lr = p.looping[pid];
+                size_type const max_steps = (energy < real_type(lr.threshold_energy))
+                                                ? lr.max_subthreshold_steps
+                                                : lr.max_steps;
+                s.post_step_action[slot] = (s.num_looping_steps[slot] >= max_steps)
+                                               ? p.action_tracking_cut
+                                               : p.action_propagation_limit;
+            }
+            else if (prop.boundary)
+            {
+                s.step_length[slot] = prop.distance;
+                s.post_step_action[slot] = p.action_boundary;
+            }
+            else if (prop.distance < step_length)
+            {
+                s.step_length[slot] = prop.distance;
+                s.post_step_action[slot] = p.action_propagation_limit;
+            }
+        }
         else
-            geo.move_internal(step_length);
-        if (prop.boundary)
         {
-            s.step_length[slot] = prop.distance;
-            s.post_step_action[slot] = p.action_boundary;
+            Propagation prop = geo.find_next_step(step_length);
+            if (prop.boundary)
+                geo.move_to_boundary();
+            else
+                geo.move_internal(step_length);
+            if (prop.boundary)
+            {
+                s.step_length[slot] = prop.distance;
+                s.post_step_action[slot] = p.action_boundary;
+            }
+            else if (prop.distance < step_length)
+            {
+                s.step_length[slot] = prop.distance;
+                s.post_step_action[slot] = p.action_propagation_limit;
+            }
         }
-        else if (prop.distance < step_length)
-        {
-            s.step_length[slot] = prop.distance;
-            s.post_step_action[slot] = p.action_propagation_limit;
-        }
+    }
+
+    // MscApplier
+    if (charged && p.msc.enabled)
+    {
+        XorwowEngine rng(s.rng, slot);
+        msc_apply_step(p, s, slot, rng);
     }
 
     // TimeUpdater
@@ -439,6 +498,18 @@ GBX_FUNCTION void interact(ParamsData const& p,
                                              cutoff_energy(p, mid, p.gamma_id),
                                              allocate,
                                              rng);
+        }
+        else if (action == p.action_rel_brems)
+        {
+            result = interact_relativistic_brems(p,
+                                                 mat.element[elcomp],
+                                                 mat,
+                                                 real_type(p.particles[pid].mass),
+                                                 energy,
+                                                 dir,
+                                                 cutoff_energy(p, mid, p.gamma_id),
+                                                 allocate,
+                                                 rng);
         }
         else if (action == p.action_moller_bhabha)
         {

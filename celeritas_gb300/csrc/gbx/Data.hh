@@ -151,6 +151,16 @@ struct LivermoreShell
     GenericGrid xs;
 };
 
+//! Relativistic bremsstrahlung per-element factors
+struct RelBremElementRecord
+{
+    double fz;  //!< log(Z)/3 + Coulomb correction
+    double factor1;  //!< (F_el - f_c) + F_inel / Z
+    double factor2;  //!< (1 + 1/Z) / 12
+    double gamma_factor;  //!< 100 m_e / Z^(1/3)
+    double epsilon_factor;  //!< 100 m_e / Z^(2/3)
+};
+
 //! Seltzer-Berger scaled DCS per element
 struct SBElementTable
 {
@@ -160,6 +170,44 @@ struct SBElementTable
     size_type ny;
     size_type values;  //!< Offset of [nx][ny] values
     size_type argmax;  //!< Offset (in ints) of per-x argmax over y
+};
+
+//! Urban multiple scattering per-material coefficients
+struct UrbanMscMaterialRecord
+{
+    double stepmin_coeff[2];
+    double theta_coeff[2];
+    double tail_coeff[3];
+    double tail_corr;
+};
+
+//! Urban multiple scattering per-(material, e-/e+) data
+struct UrbanMscParMatRecord
+{
+    double scaled_zeff;
+    double d_over_r;
+};
+
+//! Urban multiple scattering parameters
+struct UrbanMscParams
+{
+    bool enabled;
+    double low_energy_limit;
+    double high_energy_limit;
+    double lambda_limit;  //!< PhysicsParamsOptions::lambda_limit
+    double range_factor;
+    double safety_factor;
+    UrbanMscMaterialRecord const* material;  //!< [material]
+    UrbanMscParMatRecord const* par_mat;  //!< [material * 2 + (e+ ? 1 : 0)]
+    size_type xs_grids;  //!< Offset in ints: grid index per (material, e-/e+)
+};
+
+//! Looping thresholds for charged particles in a field (SimParams)
+struct LoopingRecord
+{
+    size_type max_subthreshold_steps;
+    size_type max_steps;
+    double threshold_energy;
 };
 
 //---------------------------------------------------------------------------//
@@ -249,7 +297,14 @@ struct ParamsData
     LivermoreElement const* livermore_elements;
     LivermoreShell const* livermore_shells;
     SBElementTable const* sb_tables;
+    RelBremElementRecord const* rb_elements;
     bool enable_lpm;
+
+    // Multiple scattering and field
+    UrbanMscParams msc;
+    bool has_field;
+    double field[3];  //!< Uniform field [native units: gauss]
+    LoopingRecord const* looping;  //!< [particle]
 
     // Action IDs (the reference's registration order)
     size_type action_pre_step;
@@ -359,6 +414,16 @@ struct StateData
     size_type* secondaries_offset;
     size_type* secondaries_count;
     size_type* element;
+    // Multiple scattering step (MscStep) and persistent range (MscRange)
+    std::uint8_t* msc_displaced;
+    real_type* msc_true_path;
+    real_type* msc_geom_path;
+    real_type* msc_alpha;
+    real_type* msc_range_init;
+    real_type* msc_range_factor;
+    real_type* msc_limit_min;
+    // Field looping counter
+    size_type* num_looping_steps;
 
     // RNG
     RngStateRef rng;

@@ -1,0 +1,491 @@
+// Charged-particle propagation in a uniform magnetic field: Dormand-Prince
+// RK5(4) integration with an adaptive driver and a chord-based boundary
+// search through the geometry.
+//
+// Follows src/celeritas/field/FieldPropagator.hh:150-333,
+// FieldDriver.hh:182-429, DormandPrinceStepper.hh:102-222,
+// MagFieldEquation.hh, detail/FieldUtils.hh and the defaults of
+// FieldDriverOptions.hh:26-77. The integration runs in FP64 in every build
+// (positions, momenta and the error control).
+#pragma once
+
+#include "Geometry.hh"
+
+namespace gbx
+{
+//! Field-driver tuning parameters (FieldDriverOptions defaults)
+struct FieldOptions
+{
+    double minimum_step = 1.0e-5 * constants::millimeter;
+    double delta_chord = 0.25 * constants::millimeter;
+    double delta_intersection = 1.0e-4 * constants::millimeter;
+    double epsilon_step = 1.0e-5;
+    double epsilon_rel_max = 1.0e-3;
+    double errcon = 1.0e-4;
+    double pgrow = -0.20;
+    double pshrink = -0.25;
+    double safety = 0.9;
+    double max_stepping_increase = 5;
+    double max_stepping_decrease = 0.1;
+    short max_nsteps = 100;
+    short max_substeps = 10;
+    static constexpr double initial_step_tol = 1e-6;
+    static constexpr double dchord_tol = 1e-5 * constants::millimeter;
+    static constexpr double min_chord_shrink = 0.5;
+};
+
+struct OdeState
+{
+    Real3 pos;
+    Real3 mom;
+};
+
+GBX_FORCEINLINE void axpy(double a, OdeState const& x, OdeState* y)
+{
+    axpy(a, x.pos, &y->pos);
+    axpy(a, x.mom, &y->mom);
+}
+
+GBX_FORCEINLINE Real3 cross_product(Real3 const& x, Real3 const& y)
+{
+    return {x.y * y.z - x.z * y.y, x.z * y.x - x.x * y.z, x.x * y.y - x.y * y.x};
+}
+
+GBX_FORCEINLINE double fastpow(double a, double b)
+{
+    return std::exp(b * std::log(a));
+}
+
+//! Equation of motion in a uniform field: d(pos)/ds = p/|p|,
+//! d(mom)/ds = (q/|p|) p x B
+struct UniformFieldEquation
+{
+    Real3 field;
+    double coeffi;
+
+    GBX_FORCEINLINE OdeState operator()(OdeState const& y) const
+    {
+        double momentum_inv = 1.0 / std::sqrt(dot_product(y.mom, y.mom));
+        OdeState result;
+        result.pos = {momentum_inv * y.mom.x,
+                      momentum_inv * y.mom.y,
+                      momentum_inv * y.mom.z};
+        double const scale = coeffi * momentum_inv;
+        Real3 c = cross_product(y.mom, field);
+        result.mom = {scale * c.x, scale * c.y, scale * c.z};
+        return result;
+    }
+};
+
+struct FieldStepperResult
+{
+    OdeState mid_state;
+    OdeState end_state;
+    OdeState err_state;
+};
+
+//! Dormand-Prince 5(4) step with Shampine's midpoint interpolation
+GBX_FUNCTION FieldStepperResult dormand_prince_step(UniformFieldEquation const& rhs,
+                                                    double step,
+                                                    OdeState const& beg_state)
+{
+    using R = double;
+    constexpr R a11 = 0.2;
+    constexpr R a21 = 0.075;
+    constexpr R a22 = 0.225;
+    constexpr R a31 = 44 / R(45);
+    constexpr R a32 = -56 / R(15);
+    constexpr R a33 = 32 / R(9);
+    constexpr R a41 = 19372 / R(6561);
+    constexpr R a42 = -25360 / R(2187);
+    constexpr R a43 = 64448 / R(6561);
+    constexpr R a44 = -212 / R(729);
+    constexpr R a51 = 9017 / R(3168);
+    constexpr R a52 = -355 / R(33);
+    constexpr R a53 = 46732 / R(5247);
+    constexpr R a54 = 49 / R(176);
+    constexpr R a55 = -5103 / R(18656);
+    constexpr R a61 = 35 / R(384);
+    constexpr R a63 = 500 / R(1113);
+    constexpr R a64 = 125 / R(192);
+    constexpr R a65 = -2187 / R(6784);
+    constexpr R a66 = 11 / R(84);
+    constexpr R d71 = a61 - 5179 / R(57600);
+    constexpr R d73 = a63 - 7571 / R(16695);
+    constexpr R d74 = a64 - 393 / R(640);
+    constexpr R d75 = a65 + 92097 / R(339200);
+    constexpr R d76 = a66 - 187 / R(2100);
+    constexpr R d77 = -1 / R(40);
+    constexpr R c71 = R(6025192743.) / R(30085553152.);
+    constexpr R c73 = R(51252292925.) / R(65400821598.);
+    constexpr R c74 = R(-2691868925.) / R(45128329728.);
+    constexpr R c75 = R(187940372067.) / R(1594534317056.);
+    constexpr R c76 = R(-1776094331.) / R(19743644256.);
+    constexpr R c77 = R(11237099.) / R(235043384.);
+
+    FieldStepperResult result;
+    OdeState k1 = rhs(beg_state);
+    OdeState state = beg_state;
+    axpy(a11 * step, k1, &state);
+    OdeState k2 = rhs(state);
+    state = beg_state;
+    axpy(a21 * step, k1, &state);
+    axpy(a22 * step, k2, &state);
+    OdeState k3 = rhs(state);
+    state = beg_state;
+    axpy(a31 * step, k1, &state);
+    axpy(a32 * step, k2, &state);
+    axpy(a33 * step, k3, &state);
+    OdeState k4 = rhs(state);
+    state = beg_state;
+    axpy(a41 * step, k1, &state);
+    axpy(a42 * step, k2, &state);
+    axpy(a43 * step, k3, &state);
+    axpy(a44 * step, k4, &state);
+    OdeState k5 = rhs(state);
+    state = beg_state;
+    axpy(a51 * step, k1, &state);
+    axpy(a52 * step, k2, &state);
+    axpy(a53 * step, k3, &state);
+    axpy(a54 * step, k4, &state);
+    axpy(a55 * step, k5, &state);
+    OdeState k6 = rhs(state);
+    result.end_state = beg_state;
+    axpy(a61 * step, k1, &result.end_state);
+    axpy(a63 * step, k3, &result.end_state);
+    axpy(a64 * step, k4, &result.end_state);
+    axpy(a65 * step, k5, &result.end_state);
+    axpy(a66 * step, k6, &result.end_state);
+    OdeState k7 = rhs(result.end_state);
+    result.err_state = {{0, 0, 0}, {0, 0, 0}};
+    axpy(d71 * step, k1, &result.err_state);
+    axpy(d73 * step, k3, &result.err_state);
+    axpy(d74 * step, k4, &result.err_state);
+    axpy(d75 * step, k5, &result.err_state);
+    axpy(d76 * step, k6, &result.err_state);
+    axpy(d77 * step, k7, &result.err_state);
+    double half_step = step / double(2);
+    result.mid_state = beg_state;
+    axpy(c71 * half_step, k1, &result.mid_state);
+    axpy(c73 * half_step, k3, &result.mid_state);
+    axpy(c74 * half_step, k4, &result.mid_state);
+    axpy(c75 * half_step, k5, &result.mid_state);
+    axpy(c76 * half_step, k6, &result.mid_state);
+    axpy(c77 * half_step, k7, &result.mid_state);
+    return result;
+}
+
+//---------------------------------------------------------------------------//
+// Field driver
+//---------------------------------------------------------------------------//
+struct DriverResult
+{
+    OdeState state;
+    double step;
+};
+
+class FieldDriver
+{
+  public:
+    GBX_FORCEINLINE FieldDriver(FieldOptions const& options,
+                                UniformFieldEquation const& rhs)
+        : opt_(options), rhs_(rhs)
+    {
+    }
+
+    GBX_FUNCTION DriverResult advance(double step, OdeState const& state)
+    {
+        if (step <= opt_.minimum_step)
+        {
+            DriverResult result;
+            result.state = dormand_prince_step(rhs_, step, state).end_state;
+            result.step = step;
+            return result;
+        }
+        ChordSearch output = this->find_next_chord(min_of(step, max_chord_), state);
+        if (output.end.step < step)
+        {
+            max_chord_ = output.end.step * (1 / FieldOptions::min_chord_shrink);
+        }
+        if (output.err_sq > 1)
+        {
+            double next_step = step * this->new_step_scale(output.err_sq);
+            output.end = this->accurate_advance(output.end.step, state, next_step);
+        }
+        return output.end;
+    }
+
+    GBX_FORCEINLINE double minimum_step() const { return opt_.minimum_step; }
+    GBX_FORCEINLINE double delta_intersection() const
+    {
+        return opt_.delta_intersection;
+    }
+    GBX_FORCEINLINE short max_substeps() const { return opt_.max_substeps; }
+
+  private:
+    struct ChordSearch
+    {
+        DriverResult end;
+        double err_sq;
+    };
+    struct Integration
+    {
+        DriverResult end;
+        double proposed_step;
+    };
+
+    FieldOptions const& opt_;
+    UniformFieldEquation rhs_;
+    double max_chord_{INFINITY};
+
+    static GBX_FORCEINLINE double rel_err_sq(OdeState const& err_state,
+                                             double step,
+                                             Real3 const& mom)
+    {
+        double errpos2 = dot_product(err_state.pos, err_state.pos);
+        double errvel2 = dot_product(err_state.mom, err_state.mom);
+        errpos2 /= ipow<2>(step);
+        errvel2 /= dot_product(mom, mom);
+        return max_of(errpos2, errvel2);
+    }
+
+    static GBX_FORCEINLINE double distance_chord(Real3 const& beg_pos,
+                                                 Real3 const& mid_pos,
+                                                 Real3 const& end_pos)
+    {
+        Real3 beg_mid{mid_pos.x - beg_pos.x, mid_pos.y - beg_pos.y, mid_pos.z - beg_pos.z};
+        Real3 beg_end{end_pos.x - beg_pos.x, end_pos.y - beg_pos.y, end_pos.z - beg_pos.z};
+        Real3 cross = cross_product(beg_end, beg_mid);
+        return std::sqrt(dot_product(cross, cross) / dot_product(beg_end, beg_end));
+    }
+
+    GBX_FORCEINLINE double new_step_scale(double err_sq) const
+    {
+        return opt_.safety
+               * fastpow(err_sq, 0.5 * (err_sq > 1 ? opt_.pshrink : opt_.pgrow));
+    }
+
+    GBX_FUNCTION ChordSearch find_next_chord(double step, OdeState const& state) const
+    {
+        ChordSearch output;
+        bool succeeded = false;
+        auto remaining_steps = opt_.max_nsteps;
+        FieldStepperResult result;
+        do
+        {
+            result = dormand_prince_step(rhs_, step, state);
+            double dchord = distance_chord(
+                state.pos, result.mid_state.pos, result.end_state.pos);
+            if (dchord > opt_.delta_chord + FieldOptions::dchord_tol)
+            {
+                double scale_step = max_of(std::sqrt(opt_.delta_chord / dchord),
+                                           FieldOptions::min_chord_shrink);
+                step *= scale_step;
+            }
+            else
+            {
+                succeeded = true;
+            }
+        } while (!succeeded && --remaining_steps > 0);
+        output.end.step = step;
+        output.end.state = result.end_state;
+        output.err_sq = rel_err_sq(result.err_state, step, state.mom)
+                        / ipow<2>(opt_.epsilon_rel_max);
+        return output;
+    }
+
+    GBX_FUNCTION Integration one_good_step(double step, OdeState const& state) const
+    {
+        Integration output;
+        bool succeeded = false;
+        size_type remaining_steps = opt_.max_nsteps;
+        double err_sq;
+        FieldStepperResult result;
+        do
+        {
+            result = dormand_prince_step(rhs_, step, state);
+            err_sq = rel_err_sq(result.err_state, step, state.mom)
+                     / ipow<2>(opt_.epsilon_rel_max);
+            if (err_sq > 1)
+            {
+                step *= max_of(this->new_step_scale(err_sq),
+                               opt_.max_stepping_decrease);
+            }
+            else
+            {
+                succeeded = true;
+            }
+        } while (!succeeded && --remaining_steps > 0);
+        output.end.state = result.end_state;
+        output.end.step = step;
+        output.proposed_step
+            = step * min_of(this->new_step_scale(err_sq), opt_.max_stepping_increase);
+        return output;
+    }
+
+    GBX_FUNCTION Integration integrate_step(double step, OdeState const& state) const
+    {
+        Integration output;
+        if (step > opt_.minimum_step)
+        {
+            output = this->one_good_step(step, state);
+        }
+        else
+        {
+            FieldStepperResult result = dormand_prince_step(rhs_, step, state);
+            output.end.state = result.end_state;
+            output.end.step = step;
+            double err_sq = rel_err_sq(result.err_state, step, state.mom)
+                            / ipow<2>(opt_.epsilon_rel_max);
+            output.proposed_step = step * this->new_step_scale(err_sq);
+        }
+        return output;
+    }
+
+    GBX_FUNCTION DriverResult accurate_advance(double step,
+                                               OdeState const& state,
+                                               double hinitial) const
+    {
+        double end_curve_length = step;
+        double h = ((hinitial > FieldOptions::initial_step_tol * step)
+                    && (hinitial < step))
+                       ? hinitial
+                       : step;
+        double h_threshold = opt_.epsilon_step * step;
+        Integration output;
+        output.end.state = state;
+        bool succeeded = false;
+        double curve_length = 0;
+        auto remaining_steps = opt_.max_nsteps;
+        do
+        {
+            output = this->integrate_step(h, output.end.state);
+            curve_length += output.end.step;
+            if (h < h_threshold || curve_length >= end_curve_length)
+            {
+                succeeded = true;
+            }
+            else
+            {
+                h = min_of(max_of(output.proposed_step, opt_.minimum_step),
+                           end_curve_length - curve_length);
+            }
+        } while (!succeeded && --remaining_steps > 0);
+        output.end.step = min_of(curve_length, step);
+        return output.end;
+    }
+};
+
+//---------------------------------------------------------------------------//
+// Field propagator
+//---------------------------------------------------------------------------//
+//! Propagate a charged track up to 'step' along its curved trajectory,
+//! stopping at the first boundary crossing (FieldPropagator::operator())
+GBX_FUNCTION Propagation propagate_in_field(FieldOptions const& opt,
+                                            UniformFieldEquation const& rhs,
+                                            double momentum,
+                                            GeoTrackView& geo,
+                                            double step)
+{
+    FieldDriver driver(opt, rhs);
+    OdeState state;
+    state.pos = geo.pos();
+    Real3 const dir0 = geo.dir();
+    state.mom = {momentum * dir0.x, momentum * dir0.y, momentum * dir0.z};
+
+    double const delta_intersection = driver.delta_intersection();
+    double const minimum_substep = driver.minimum_step();
+    double const bump_distance = delta_intersection * double(0.1);
+
+    Propagation result{0, geo.is_on_boundary(), false};
+    double remaining = step;
+    auto remaining_substeps = driver.max_substeps();
+    do
+    {
+        DriverResult substep = driver.advance(remaining, state);
+        // Chord from the current position to the substep end
+        Real3 cdir{substep.state.pos.x - state.pos.x,
+                   substep.state.pos.y - state.pos.y,
+                   substep.state.pos.z - state.pos.z};
+        double const clen = norm(cdir);
+        cdir.x /= clen;
+        cdir.y /= clen;
+        cdir.z /= clen;
+        if (clen >= minimum_substep)
+        {
+            geo.set_dir(cdir);
+        }
+        Propagation linear_step = geo.find_next_step(clen + delta_intersection);
+        double const update_length = substep.step * linear_step.distance / clen;
+        auto is_intercept_close = [&]() {
+            double delta_sq = 0;
+            for (int i = 0; i < 3; ++i)
+            {
+                delta_sq += ipow<2>(state.pos[i] - substep.state.pos[i]
+                                    + linear_step.distance * cdir[i]);
+            }
+            return delta_sq <= ipow<2>(delta_intersection);
+        };
+        if (!linear_step.boundary)
+        {
+            state = substep.state;
+            result.boundary = false;
+            result.distance += substep.step;
+            remaining = step - result.distance;
+            geo.move_internal_to(state.pos);
+            --remaining_substeps;
+        }
+        else if (result.boundary && (linear_step.distance) < bump_distance)
+        {
+            remaining = substep.step / 2;
+        }
+        else if (update_length <= minimum_substep || is_intercept_close()
+                 || clen == 0)
+        {
+            result.boundary = (linear_step.distance <= clen
+                               || result.distance + update_length <= step
+                               || clen == 0);
+            if (!result.boundary)
+            {
+                state.pos = substep.state.pos;
+                geo.move_internal_to(substep.state.pos);
+            }
+            result.distance += min_of(update_length, substep.step);
+            state.mom = substep.state.mom;
+            remaining = 0;
+        }
+        else
+        {
+            remaining = update_length;
+        }
+    } while (remaining > minimum_substep && remaining_substeps > 0);
+
+    if (remaining_substeps == 0 && result.distance < step)
+    {
+        result.looping = true;
+    }
+    else if (result.distance > 0)
+    {
+        if (result.boundary)
+        {
+            geo.move_to_boundary();
+            state.pos = geo.pos();
+        }
+        else if (result.distance < step)
+        {
+            result.distance = step;
+        }
+    }
+    Real3 dir = make_unit_vector(state.mom);
+    geo.set_dir(dir);
+    if (result.distance == 0)
+    {
+        result.distance = min_of(bump_distance, step);
+        result.boundary = false;
+        axpy(result.distance, dir, &state.pos);
+        geo.move_internal_to(state.pos);
+    }
+    return result;
+}
+
+}  // namespace gbx

@@ -114,6 +114,14 @@ class GeoTrackView
     GBX_FUNCTION Propagation find_next_step(double max_step);
     GBX_FUNCTION void move_to_boundary();
     GBX_FUNCTION void move_internal(double dist);
+    //! Move within the current volume to a nearby point
+    GBX_FORCEINLINE void move_internal_to(Real3 const& pos)
+    {
+        this->set_pos(pos);
+        s_.surface[slot_] = invalid_id;
+        s_.next_step[slot_] = 0;
+        s_.next_surface[slot_] = invalid_id;
+    }
     GBX_FUNCTION void cross_boundary();
     GBX_FUNCTION void set_dir(Real3 const& newdir);
     GBX_FUNCTION double find_safety() const;

@@ -495,6 +495,244 @@ GBX_FUNCTION Interaction interact_seltzer_berger(ParamsData const& p,
 }
 
 //---------------------------------------------------------------------------//
+// Relativistic bremsstrahlung with LPM suppression
+// (src/celeritas/em/interactor/RelativisticBremInteractor.hh,
+//  interactor/detail/RBEnergySampler.hh, xs/RBDiffXsCalculator.hh,
+//  xs/LPMCalculator.hh)
+//---------------------------------------------------------------------------//
+namespace detail
+{
+// CGS unit system constants in the reference's definition order
+constexpr double unit_kilogram = 1000 * constants::gram;
+constexpr double unit_newton
+    = unit_kilogram * constants::meter / (constants::second * constants::second);
+constexpr double unit_joule = unit_newton * constants::meter;
+constexpr double unit_coulomb = unit_kilogram / (constants::tesla * constants::second);
+constexpr double unit_volt = unit_joule / unit_coulomb;
+constexpr double e_electron = 1.602176634e-19 * unit_coulomb;
+constexpr double mev_value = double(1e6) * e_electron * unit_volt;
+constexpr double h_planck = 6.62607015e-34 * unit_joule * constants::second;
+constexpr double electron_mass_g = 9.1093837015e-28 * constants::gram;
+
+//! LPM constant [MeV/cm]: alpha (m c^2)^2 / (2 h c)
+constexpr double lpm_constant()
+{
+    constexpr double electron_mass_csq
+        = electron_mass_g * ipow<2>(constants::c_light);
+    return constants::alpha_fine_structure * ipow<2>(electron_mass_csq)
+           / (2 * h_planck * constants::c_light) / mev_value;
+}
+
+constexpr double migdal_constant()
+{
+    return 4 * constants::pi * constants::r_electron
+           * ipow<2>(constants::lambdabar_electron);
+}
+
+struct LPMFunctions
+{
+    real_type xi;
+    real_type g;
+    real_type phi;
+};
+
+//! LPM suppression functions (Stanev / Klein parameterizations)
+GBX_FUNCTION LPMFunctions calc_lpm(MaterialRecord const& mat,
+                                   ElementRecord const& el,
+                                   real_type gamma_energy,
+                                   real_type epsilon)
+{
+    constexpr real_type sqrt_two = 1.41421356237309504880;
+    real_type const lpm_energy = real_type(mat.rad_length) * real_type(lpm_constant());
+    real_type const s_prime = std::sqrt(
+        lpm_energy / (8 * epsilon * gamma_energy * std::fabs(epsilon - 1)));
+    real_type const s1 = ipow<2>(real_type(el.cbrt_z) / real_type(184.15));
+    real_type xi = 2;
+    if (s_prime > 1)
+    {
+        xi = 1;
+    }
+    else if (s_prime > sqrt_two * s1)
+    {
+        real_type const log_s1 = std::log(sqrt_two * s1);
+        real_type const h = std::log(s_prime) / log_s1;
+        xi = 1 + h - real_type(0.08) * (1 - h) * h * (2 - h) / log_s1;
+    }
+    real_type s = s_prime / std::sqrt(xi);
+    // Dielectric suppression is always on for relativistic bremsstrahlung
+    {
+        real_type const k_p_sq = real_type(mat.electron_density)
+                                 * real_type(migdal_constant())
+                                 * ipow<2>(epsilon * gamma_energy);
+        s *= (1 + k_p_sq / ipow<2>(gamma_energy));
+        xi = 2;
+        if (s > 1)
+        {
+            xi = 1;
+        }
+        else if (s > s1)
+        {
+            xi = 1 + std::log(s) / std::log(s1);
+        }
+    }
+    real_type phi;
+    if (s < real_type(0.01))
+    {
+        real_type const c[2] = {6, real_type(-6 * constants::pi)};
+        phi = s * poly_eval<1>(c, s);
+    }
+    else if (s < real_type(1.55))
+    {
+        real_type const ca[3] = {real_type(0.623), real_type(0.796), real_type(0.658)};
+        real_type a = poly_eval<2>(ca, s);
+        real_type const cb[3]
+            = {real_type(-6), real_type(-6 * (3 - constants::pi)), 1 / a};
+        real_type b = poly_eval<2>(cb, s);
+        phi = 1 - std::exp(s * b);
+    }
+    else
+    {
+        phi = 1 - real_type(0.01190476) / ipow<4>(s);
+    }
+    if (xi * phi > 1 || s > real_type(0.57))
+    {
+        xi = 1 / phi;
+    }
+    real_type g;
+    if (s < real_type(0.01))
+    {
+        real_type const c[2] = {-2 * phi, 12};
+        g = poly_eval<1>(c, s);
+    }
+    else if (s < real_type(0.415827))
+    {
+        real_type const ca[5] = {real_type(1),
+                                 real_type(3.936),
+                                 real_type(4.97),
+                                 real_type(-0.05),
+                                 real_type(7.5)};
+        real_type a = poly_eval<4>(ca, s);
+        real_type const cb[2] = {real_type(-4), -8 / a};
+        real_type b = poly_eval<1>(cb, s);
+        real_type psi = 1 - std::exp(s * b);
+        g = 3 * psi - 2 * phi;
+    }
+    else if (s < real_type(1.9156))
+    {
+        real_type const c[5] = {real_type(-0.160723),
+                                real_type(3.755030),
+                                real_type(-1.798138),
+                                real_type(0.672827),
+                                real_type(-0.120772)};
+        g = std::tanh(poly_eval<4>(c, s));
+    }
+    else
+    {
+        g = 1 - real_type(0.0230655) / ipow<4>(s);
+    }
+    return {xi, g, phi};
+}
+}  // namespace detail
+
+template<class G>
+GBX_FUNCTION Interaction interact_relativistic_brems(ParamsData const& p,
+                                                     size_type element_id,
+                                                     MaterialRecord const& mat,
+                                                     real_type inc_mass,
+                                                     real_type inc_energy,
+                                                     RVec3 const& inc_dir,
+                                                     real_type gamma_cutoff,
+                                                     SecondaryAllocator& allocate,
+                                                     G& rng)
+{
+    Secondary* photon = allocate(1);
+    if (photon == nullptr)
+        return Interaction::from_failure();
+    using R = real_type;
+    RelBremElementRecord const& ed = p.rb_elements[element_id];
+    ElementRecord const& el = p.elements[element_id];
+    real_type const inc_momentum = std::sqrt(momentum_sq(inc_mass, inc_energy));
+    real_type const total_energy = inc_energy + inc_mass;
+    real_type const density_factor
+        = R(mat.electron_density) * R(detail::migdal_constant());
+    real_type const density_corr = density_factor * ipow<2>(total_energy);
+    real_type const lpm_energy = R(mat.rad_length) * R(detail::lpm_constant());
+    real_type const lpm_threshold = lpm_energy * std::sqrt(density_factor);
+    bool const enable_lpm = p.enable_lpm && (total_energy > lpm_threshold);
+
+    auto dxsec_per_atom = [&](real_type gamma_energy) -> real_type {
+        real_type dxsec{0};
+        real_type y = gamma_energy / total_energy;
+        real_type onemy = 1 - y;
+        real_type term0 = onemy + R(0.75) * ipow<2>(y);
+        if (el.z < 5)
+        {
+            dxsec = term0 * R(ed.factor1) + onemy * R(ed.factor2);
+        }
+        else
+        {
+            real_type invz = 1 / static_cast<real_type>(el.z);
+            real_type term1 = y / (total_energy - gamma_energy);
+            real_type gam = term1 * R(ed.gamma_factor);
+            real_type eps = term1 * R(ed.epsilon_factor);
+            real_type gam2 = ipow<2>(gam);
+            real_type eps2 = ipow<2>(eps);
+            real_type phi1 = R(16.863) - 2 * std::log(1 + R(0.311877) * gam2)
+                             + R(2.4) * std::exp(R(-0.9) * gam)
+                             + R(1.6) * std::exp(R(-1.5) * gam);
+            real_type phi2 = 2 / (3 + R(19.5) * gam + 18 * gam2);
+            real_type psi1 = R(24.34) - 2 * std::log(1 + R(13.111641) * eps2)
+                             + R(2.8) * std::exp(R(-8) * eps)
+                             + R(1.2) * std::exp(R(-29.2) * eps);
+            real_type psi2 = 2 / (3 + 120 * eps + 1200 * eps2);
+            dxsec = term0
+                        * ((R(0.25) * phi1 - R(ed.fz))
+                           + (R(0.25) * psi1 - 2 * R(el.log_z) / 3) * invz)
+                    + R(0.125) * onemy * (phi2 + psi2 * invz);
+        }
+        return max_of(dxsec, R(0));
+    };
+    auto dxsec_per_atom_lpm = [&](real_type gamma_energy) -> real_type {
+        real_type epsilon = total_energy / gamma_energy;
+        detail::LPMFunctions lpm = detail::calc_lpm(mat, el, gamma_energy, epsilon);
+        real_type y = gamma_energy / total_energy;
+        real_type onemy = 1 - y;
+        real_type y2 = R(0.25) * ipow<2>(y);
+        real_type term = lpm.xi * (y2 * lpm.g + (onemy + 2 * y2) * lpm.phi);
+        real_type dxsec = term * R(ed.factor1) + onemy * R(ed.factor2);
+        return max_of(dxsec, R(0));
+    };
+
+    // RBEnergySampler
+    real_type const tmin_sq = ipow<2>(min_of(gamma_cutoff, inc_energy));
+    real_type const tmax_sq = ipow<2>(min_of(R(1e8), inc_energy));
+    ReciprocalDistribution<real_type> sample_exit_esq(tmin_sq + density_corr,
+                                                      tmax_sq + density_corr);
+    real_type const max_value = R(ed.factor1) + R(ed.factor2);
+    real_type gamma_energy{0};
+    real_type dsigma{0};
+    do
+    {
+        gamma_energy = std::sqrt(sample_exit_esq(rng) - density_corr);
+        dsigma = enable_lpm ? dxsec_per_atom_lpm(gamma_energy)
+                            : dxsec_per_atom(gamma_energy);
+    } while (reject_sample<real_type>(dsigma, max_value, rng));
+
+    real_type const costheta = sample_tsai_urban(inc_energy, inc_mass, rng);
+
+    photon->direction = sample_exiting_direction<real_type>(costheta, inc_dir, rng);
+    photon->particle_id = p.gamma_id;
+    photon->energy = gamma_energy;
+    Interaction result;
+    result.energy = inc_energy - gamma_energy;
+    result.direction = calc_exiting_direction<real_type>(
+        inc_momentum, inc_dir, gamma_energy, photon->direction);
+    result.secondaries = photon;
+    result.num_secondaries = 1;
+    return result;
+}
+
+//---------------------------------------------------------------------------//
 // Moller-Bhabha ionization
 //---------------------------------------------------------------------------//
 template<class G>

@@ -27,6 +27,17 @@ GBX_FORCEINLINE size_type make_track_id(StateData const& s, size_type event)
 #endif
 }
 
+//! Reset per-track physics and looping state for a new track
+//! (PhysicsTrackView::operator=(Initializer_t), SimTrackView init)
+GBX_FORCEINLINE void reset_physics_state(StateData const& s, size_type slot)
+{
+    s.interaction_mfp[slot] = 0;
+    s.msc_range_init[slot] = 0;
+    s.msc_range_factor[slot] = 0;
+    s.msc_limit_min[slot] = 0;
+    s.num_looping_steps[slot] = 0;
+}
+
 //! Copy primary 'tid' into the initializer list (ProcessPrimariesExecutor)
 GBX_FUNCTION void process_primary(StateData const& s,
                                   size_type num_initializers,
@@ -92,7 +103,7 @@ GBX_FUNCTION void init_track(ParamsData const& p,
     }
     s.material[slot] = matid;
     // Physics state reset
-    s.interaction_mfp[slot] = 0;
+    reset_physics_state(s, slot);
 }
 
 //! Flag the slot as vacant or occupied and count secondaries that need a
@@ -178,7 +189,7 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
             geo.copy_from(slot, ti.dir);
             s.particle_id[slot] = ti.particle_id;
             s.energy[slot] = ti.energy;
-            s.interaction_mfp[slot] = 0;
+            reset_physics_state(s, slot);
             initialized = true;
             status = status_initializing;
         }

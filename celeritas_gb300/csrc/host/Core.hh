@@ -288,6 +288,6 @@ class Stepper
 
 //! Register the stepping-loop actions in the reference's order and return
 //! the list (CoreParams::build_actions, PhysicsParams actions, models)
-void register_core_actions(ActionRegistry* reg);
+void register_core_actions(ActionRegistry* reg, bool uniform_field);
 
 }  // namespace gbx

@@ -199,6 +199,7 @@ class Builder
     }
 
     void build_actions();
+    void build_msc_field();
     void build_particles();
     void build_materials();
     void build_physics();
@@ -607,6 +608,40 @@ void Builder::build_models()
         hp_.sb_tables.push_back(t);
     }
 
+    // Relativistic bremsstrahlung element factors (form factors of Tsai for
+    // Z < 5, Thomas-Fermi radiation logarithms above)
+    {
+        double const electron_mass = hp_.particles[hp_.scalars.electron_id].mass;
+        static double const form_factor[4][2] = {
+            {5.3104, 5.9173}, {4.7935, 5.6125}, {4.7402, 5.5377}, {4.7112, 5.4728}};
+        for (auto const& el : hp_.elements)
+        {
+            int const z = std::min(el.z, 120);
+            double ff_el, ff_inel;
+            if (z < 5)
+            {
+                ff_el = form_factor[z - 1][0];
+                ff_inel = form_factor[z - 1][1];
+            }
+            else
+            {
+                ff_el = double(std::log(184.15)) - el.log_z / 3;
+                ff_inel = double(std::log(1194.0)) - 2 * el.log_z / 3;
+            }
+            double const fc = el.coulomb_correction;
+            double const invz = double(1) / z;
+            double const z13 = el.cbrt_z;
+            double const z23 = ipow<2>(z13);
+            RelBremElementRecord r;
+            r.fz = el.log_z / 3 + fc;
+            r.factor1 = (ff_el - fc) + ff_inel * invz;
+            r.factor2 = (1 + invz) / 12;
+            r.gamma_factor = 100 * electron_mass / z13;
+            r.epsilon_factor = 100 * electron_mass / z23;
+            hp_.rb_elements.push_back(r);
+        }
+    }
+
     // Livermore photoelectric data per element
     for (auto const& el : hp_.elements)
     {
@@ -642,6 +677,93 @@ void Builder::build_models()
         }
         hp_.lv_elements.push_back(le);
     }
+}
+
+void Builder::build_msc_field()
+{
+    ParamsData& s = hp_.scalars;
+    // Field (UniformFieldParams: input in tesla, stored in native units)
+    s.has_field = false;
+    for (int i = 0; i < 3; ++i)
+    {
+        s.field[i] = opts_.field_tesla[i] * constants::tesla;
+        if (s.field[i] != 0)
+            s.has_field = true;
+    }
+    if (s.has_field)
+        hp_.action_labels[s.action_along_step] = "along-step-uniform-msc";
+
+    // Looping thresholds (SimParams::from_import with 10 field substeps)
+    {
+        auto lp = kv_.dbl("trans.looping");
+        long const max_substeps = kv_.i("trans.max_substeps");
+        size_type const field_substeps = 10;
+        size_type const max_subthreshold
+            = (static_cast<size_type>(max_substeps) + field_substeps - 1)
+              / field_substeps;
+        hp_.looping.assign(hp_.particles.size(), LoopingRecord{});
+        for (std::size_t j = 0; j + 2 < lp.size() + 0; j += 3)
+        {
+            int pdg = static_cast<int>(lp[j]);
+            for (std::size_t pid = 0; pid < hp_.particles.size(); ++pid)
+            {
+                if (hp_.particles[pid].pdg != pdg)
+                    continue;
+                LoopingRecord& r = hp_.looping[pid];
+                r.max_subthreshold_steps = max_subthreshold;
+                r.max_steps = static_cast<size_type>(lp[j + 1]) * max_subthreshold;
+                r.threshold_energy = lp[j + 2];
+            }
+        }
+    }
+
+    // Urban multiple scattering (UrbanMscParams)
+    UrbanMscParams& m = s.msc;
+    m.enabled = opts_.msc;
+    m.lambda_limit = 1 * constants::millimeter;
+    m.range_factor = 0.04;
+    m.safety_factor = 0.6;
+    m.xs_grids = invalid_id;
+    if (!opts_.msc)
+        return;
+    auto poly2 = [](double c0, double c1, double c2, double x) {
+        double const c[3] = {c0, c1, c2};
+        return poly_eval<2>(c, x);
+    };
+    std::vector<size_type> grids;
+    static double const a_coeff[2] = {0.87, 0.70};
+    static double const b_coeff[2] = {2.0 / 3, 1.0 / 2};
+    for (size_type mid = 0; mid < hp_.materials.size(); ++mid)
+    {
+        double const zeff = hp_.materials[mid].zeff;
+        UrbanMscMaterialRecord md;
+        md.stepmin_coeff[0] = 1e3 * 27.725 / (1 + 0.203 * zeff);
+        md.stepmin_coeff[1] = 1e3 * 6.152 / (1 + 0.111 * zeff);
+        double const z16 = std::exp(1.0 / 6.0 * std::log(zeff));
+        double fz = poly2(0.990395, -0.168386, 0.093286, z16);
+        md.theta_coeff[0] = fz * (1 - 8.7780e-2 / zeff);
+        md.theta_coeff[1] = fz * (4.0780e-2 + 1.7315e-4 * zeff);
+        double z13 = ipow<2>(z16);
+        md.tail_coeff[0] = poly2(2.3785, -4.1981e-1, 6.3100e-2, z13);
+        md.tail_coeff[1] = poly2(4.7526e-1, 1.7694, -3.3885e-1, z13);
+        md.tail_coeff[2] = poly2(2.3683e-1, -1.8111, 3.2774e-1, z13);
+        md.tail_corr = poly2(1.7888e-2, 1.9659e-2, -2.6664e-3, z13);
+        hp_.msc_materials.push_back(md);
+        for (int pi = 0; pi < 2; ++pi)
+        {
+            UrbanMscParMatRecord pm;
+            pm.scaled_zeff = a_coeff[pi] * std::exp(b_coeff[pi] * std::log(zeff));
+            pm.d_over_r = 9.6280e-1 - 8.4848e-2 * std::sqrt(zeff) + 4.3769e-3 * zeff;
+            hp_.msc_par_mat.push_back(pm);
+            int pdg = (pi == 0) ? 11 : -11;
+            std::string key = "msc." + std::to_string(pdg) + "." + std::to_string(mid);
+            grids.push_back(this->add_log_grid(kv_.dbl(key + ".x"), kv_.dbl(key + ".y")));
+        }
+    }
+    m.xs_grids = this->add_ints(grids);
+    auto x = kv_.dbl("msc.11.0.x");
+    m.low_energy_limit = x.front();
+    m.high_energy_limit = x.back();
 }
 
 void Builder::build_geometry()
@@ -764,6 +886,7 @@ HostParams Builder::build()
     this->build_materials();
     this->build_physics();
     this->build_models();
+    this->build_msc_field();
     this->build_geometry();
     for (auto const& b : geo_.boxes)
     {
@@ -833,6 +956,10 @@ ParamsData make_host_view(HostParams const& hp)
     p.livermore_elements = hp.lv_elements.data();
     p.livermore_shells = hp.lv_shells.data();
     p.sb_tables = hp.sb_tables.data();
+    p.rb_elements = hp.rb_elements.data();
+    p.msc.material = hp.msc_materials.data();
+    p.msc.par_mat = hp.msc_par_mat.data();
+    p.looping = hp.looping.data();
     p.geo.planes = hp.planes.data();
     p.geo.boxes = hp.boxes.data();
     p.geo.neighbor_offset = hp.neighbor_offset.data();

@@ -40,6 +40,10 @@ struct ParamsOptions
 {
     double secondary_stack_factor{3};
     bool brem_combined{false};
+    //! Urban multiple scattering for e-/e+
+    bool msc{false};
+    //! Uniform magnetic field [tesla]; zero for straight-line transport
+    double field_tesla[3]{0, 0, 0};
 };
 
 //! All parameter tables in host memory
@@ -57,6 +61,10 @@ struct HostParams
     std::vector<LivermoreElement> lv_elements;
     std::vector<LivermoreShell> lv_shells;
     std::vector<SBElementTable> sb_tables;
+    std::vector<RelBremElementRecord> rb_elements;
+    std::vector<UrbanMscMaterialRecord> msc_materials;
+    std::vector<UrbanMscParMatRecord> msc_par_mat;
+    std::vector<LoopingRecord> looping;
     // Geometry
     std::vector<PlaneRecord> planes;
     std::vector<BoxVolume> boxes;

@@ -55,6 +55,10 @@ struct HostState
     std::vector<real_type> per_process_xs[max_processes];
     std::vector<real_type> energy_deposition;
     std::vector<size_type> secondaries_offset, secondaries_count, element;
+    std::vector<std::uint8_t> msc_displaced;
+    std::vector<real_type> msc_true_path, msc_geom_path, msc_alpha;
+    std::vector<real_type> msc_range_init, msc_range_factor, msc_limit_min;
+    std::vector<size_type> num_looping_steps;
     std::vector<std::uint32_t> rng_words;
     std::vector<size_type> vacancies, secondary_counts, parents;
     std::vector<TrackInitializer> initializers;
@@ -108,6 +112,14 @@ struct HostState
         secondaries_offset.assign(n, 0);
         secondaries_count.assign(n, 0);
         element.assign(n, invalid_id);
+        msc_displaced.assign(n, 0);
+        msc_true_path.assign(n, 0);
+        msc_geom_path.assign(n, 0);
+        msc_alpha.assign(n, 0);
+        msc_range_init.assign(n, 0);
+        msc_range_factor.assign(n, 0);
+        msc_limit_min.assign(n, 0);
+        num_looping_steps.assign(n, 0);
         initialize_xorwow(seed, num_slots, &rng_words);
         // All slots start vacant, in increasing order
         vacancies.resize(n);
@@ -161,6 +173,14 @@ struct HostState
         s.secondaries_offset = secondaries_offset.data();
         s.secondaries_count = secondaries_count.data();
         s.element = element.data();
+        s.msc_displaced = msc_displaced.data();
+        s.msc_true_path = msc_true_path.data();
+        s.msc_geom_path = msc_geom_path.data();
+        s.msc_alpha = msc_alpha.data();
+        s.msc_range_init = msc_range_init.data();
+        s.msc_range_factor = msc_range_factor.data();
+        s.msc_limit_min = msc_limit_min.data();
+        s.num_looping_steps = num_looping_steps.data();
         for (int w = 0; w < 5; ++w)
             s.rng.s[w] = rng_words.data() + std::size_t(w) * size;
         s.rng.weyl = rng_words.data() + std::size_t(5) * size;

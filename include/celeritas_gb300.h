@@ -56,11 +56,23 @@ typedef struct
 /* Message describing the last error on this thread ("" if none) */
 const char* gbx_last_error(void);
 
+/* Physics options (the RunnerInput field / physics_options knobs,
+ * app/celer-sim/RunnerInput.hh:41-141): a uniform magnetic field in tesla
+ * (all zero: straight-line transport, along-step-general-linear; otherwise
+ * along-step-uniform-msc) and Urban multiple scattering for e-/e+ */
+typedef struct
+{
+    double field_tesla[3];
+    int msc;
+} gbx_params_options;
+
 /* Build problem parameters from a physics input file and a named geometry
- * ("calo": 50-layer Pb/lAr sampling calorimeter). Replaces
- * Runner::build_core_params (app/celer-sim/Runner.cc:281-446). */
+ * ("calo": 50-layer Pb/lAr sampling calorimeter); 'options' may be NULL
+ * (no field, no MSC). Replaces Runner::build_core_params
+ * (app/celer-sim/Runner.cc:281-446). */
 int gbx_params_create(const char* physics_file,
                       const char* geometry,
+                      const gbx_params_options* options,
                       gbx_params** out);
 void gbx_params_destroy(gbx_params* params);
 /* Registered actions, in ID order (ActionRegistry::id_to_label,

@@ -215,6 +215,24 @@ class PortStepper
     }
 };
 
+//! Physics options from the command line: --msc, --field Bx By Bz [tesla]
+ParamsOptions physics_options(int argc, char** argv)
+{
+    ParamsOptions opts;
+    for (int i = 1; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--msc")
+            opts.msc = true;
+        else if (a == "--field" && i + 3 < argc)
+        {
+            for (int k = 0; k < 3; ++k)
+                opts.field_tesla[k] = std::strtod(argv[i + 1 + k], nullptr);
+        }
+    }
+    return opts;
+}
+
 std::vector<TrackInitializer> load_primaries(std::string const& path)
 {
     std::ifstream in(path);
@@ -265,7 +283,7 @@ int run(int argc, char** argv)
     if (geo != "calo")
         throw std::runtime_error("unknown geometry " + geo);
     HostParams hp
-        = build_params(phys, make_calorimeter_geometry(), ParamsOptions{});
+        = build_params(phys, make_calorimeter_geometry(), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
     size_type max_event = 0;
     for (auto const& pr : primaries)
@@ -333,7 +351,7 @@ int bench(int argc, char** argv)
     if (geo != "calo")
         throw std::runtime_error("unknown geometry " + geo);
     HostParams hp
-        = build_params(phys, make_calorimeter_geometry(), ParamsOptions{});
+        = build_params(phys, make_calorimeter_geometry(), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
     // Group primaries by event
     std::map<size_type, std::vector<TrackInitializer>> events;

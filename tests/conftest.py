@@ -24,7 +24,20 @@ def load_golden(name: str) -> dict:
 
 
 GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
-                "calo_ep500_n4", "calo_e1000_n100"]
+                "calo_ep500_n4", "calo_e1000_n100", "calo_e10000_n2",
+                "calo_msc_e1000_n4", "calo_field_e1000_n4", "calo_msc_field_e5000_n2",
+                "calo_msc_field_ep2000_n2"]
+
+
+def case_options(case: dict) -> list[str]:
+    """Oracle command-line physics options for a golden case."""
+    opts = []
+    if case.get("msc"):
+        opts.append("--msc")
+    field = case.get("field") or [0, 0, 0]
+    if any(field):
+        opts += ["--field"] + [repr(float(f)) for f in field]
+    return opts
 
 
 @pytest.fixture(scope="session")

@@ -28,27 +28,48 @@ import oracle  # noqa: E402
 from celeritas_gb300 import physics_file  # noqa: E402
 from celeritas_gb300.primaries import pencil_beam, write_primaries_text  # noqa: E402
 
-# name: (pdg, energy [MeV], number of primaries, track slots, seed)
+# name: primaries (pdg, energy [MeV], count), track slots, seed, msc, field [T]
 CASES = {
-    "calo_e1000_n4": (11, 1000.0, 4, 65536, 0),
-    "calo_e1000_n4_slots512": (11, 1000.0, 4, 512, 0),
-    "calo_g100_n16": (22, 100.0, 16, 4096, 7),
-    "calo_ep500_n4": (-11, 500.0, 4, 4096, 3),
-    "calo_e1000_n100": (11, 1000.0, 100, 65536, 0),
+    "calo_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=65536, seed=0),
+    "calo_e1000_n4_slots512": dict(pdg=11, energy=1000.0, num=4, slots=512, seed=0),
+    "calo_g100_n16": dict(pdg=22, energy=100.0, num=16, slots=4096, seed=7),
+    "calo_ep500_n4": dict(pdg=-11, energy=500.0, num=4, slots=4096, seed=3),
+    "calo_e1000_n100": dict(pdg=11, energy=1000.0, num=100, slots=65536, seed=0),
+    "calo_e10000_n2": dict(pdg=11, energy=10000.0, num=2, slots=65536, seed=0),
+    "calo_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=65536, seed=0, msc=True),
+    "calo_field_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=65536, seed=0,
+                                field=[1.0, 0.0, 0.0]),
+    "calo_msc_field_e5000_n2": dict(pdg=11, energy=5000.0, num=2, slots=65536, seed=11,
+                                    msc=True, field=[1.0, 0.0, 0.0]),
+    "calo_msc_field_ep2000_n2": dict(pdg=-11, energy=2000.0, num=2, slots=8192, seed=5,
+                                     msc=True, field=[1.0, 0.0, 0.0]),
 }
 
 
+def case_options(c: dict) -> list[str]:
+    """Command-line physics options of the oracle programs for a case."""
+    opts = []
+    if c.get("msc"):
+        opts.append("--msc")
+    field = c.get("field")
+    if field and any(field):
+        opts += ["--field"] + [repr(float(f)) for f in field]
+    return opts
+
+
 def make_case(name: str) -> dict:
-    pdg, energy, num, slots, seed = CASES[name]
-    prim = pencil_beam(num, energy=energy, pdg=pdg)
+    c = CASES[name]
+    prim = pencil_beam(c["num"], energy=c["energy"], pdg=c["pdg"])
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "primaries.txt")
         write_primaries_text(ptxt, prim)
-        out = oracle.run_reference(physics_file("calo"), ptxt, slots, seed)
+        out = oracle.run_reference(physics_file("calo"), ptxt, c["slots"], c["seed"],
+                                   extra=case_options(c))
     return {
-        "case": {"geometry": "calo", "pdg": pdg, "energy": energy,
-                 "num_primaries": num, "num_track_slots": slots, "seed": seed,
-                 "z0": -5.0},
+        "case": {"geometry": "calo", "pdg": c["pdg"], "energy": c["energy"],
+                 "num_primaries": c["num"], "num_track_slots": c["slots"],
+                 "seed": c["seed"], "z0": -5.0, "msc": bool(c.get("msc", False)),
+                 "field": list(c.get("field", [0.0, 0.0, 0.0]))},
         "actions": [out["actions"][i] for i in sorted(out["actions"])],
         "steps": out["steps"],
         "total_steps": out["total_steps"],

@@ -31,6 +31,18 @@ def calo_params(gb):
     return gb.Params(gb.physics_file("calo"), "calo")
 
 
+_PARAMS = {}
+
+
+def params_for(gb, case):
+    """Params with the case's field and MSC options (cached per options)."""
+    key = (tuple(case.get("field", [0, 0, 0])), bool(case.get("msc")))
+    if key not in _PARAMS:
+        _PARAMS[key] = gb.Params(gb.physics_file("calo"), "calo",
+                                 field_tesla=key[0], msc=key[1])
+    return _PARAMS[key]
+
+
 def transport(gb, params, case, use_graph=True, batch=32):
     from celeritas_gb300.primaries import pencil_beam
 
@@ -42,14 +54,16 @@ def transport(gb, params, case, use_graph=True, batch=32):
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_matches_reference(gb, calo_params, name):
+def test_matches_reference(gb, name):
     golden = load_golden(name)
-    st, res = transport(gb, calo_params, golden["case"])
+    params = params_for(gb, golden["case"])
+    st, res = transport(gb, params, golden["case"])
     steps = [[r.generated, r.queued, r.active, r.alive] for r in res]
     assert steps == golden["steps"]
     assert len(res) == golden["iterations"]
     assert sum(r.active for r in res) == golden["total_steps"]
-    labels = calo_params.detector_labels()
+    assert params.action_labels() == golden["actions"]
+    labels = params.detector_labels()
     edep = st.energy_deposition()
     ref = np.array([golden["edep"][k] for k in labels])
     np.testing.assert_allclose(edep, ref, rtol=EDEP_RTOL, atol=1e-9)

@@ -13,7 +13,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden
+from conftest import GOLDEN_CASES, case_options, load_golden
 
 import oracle
 from celeritas_gb300 import physics_file
@@ -26,7 +26,8 @@ def run_case(golden):
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
-        return oracle.run_port(physics_file("calo"), ptxt, c["num_track_slots"], c["seed"])
+        return oracle.run_port(physics_file("calo"), ptxt, c["num_track_slots"], c["seed"],
+                               extra=case_options(c))
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
