@@ -403,13 +403,22 @@ def generate(problem: str) -> str:
         ecut, gcut = cuts[mi][11], cuts[mi][22]
         for pdg in (11, -11):
             pos = pdg < 0
-            per_e = bhabha_per_electron(egrid, ecut) if pos else moller_per_electron(egrid, ecut)
-            table(f"table.{pdg}.e_ioni.lambda.{mi}", egrid, m.n_e * per_e)
+            # Discrete-process tables start at their production threshold
+            # (cross section exactly zero there), so interpolation never gives
+            # a cross section below the threshold
+            ioni_grid = log_grid(ecut if pos else 2 * ecut, E_MAX)
+            per_e = (bhabha_per_electron(ioni_grid, ecut) if pos
+                     else moller_per_electron(ioni_grid, ecut))
+            per_e[0] = 0.0
+            table(f"table.{pdg}.e_ioni.lambda.{mi}", ioni_grid, m.n_e * per_e)
             dedx = coll_dedx(m, egrid, ecut, pos) + rad_dedx(m, egrid, gcut)
             dedx = np.maximum(dedx, 1e-300 if m.density < 1e-10 else 0)
             table(f"table.{pdg}.e_ioni.dedx.{mi}", egrid, dedx)
             table(f"table.{pdg}.e_ioni.range.{mi}", egrid, csda_range(egrid, dedx))
-            table(f"table.{pdg}.e_brems.lambda.{mi}", egrid, m.inv_x0 * brems_shape(egrid, gcut))
+            brems_grid = log_grid(gcut, E_MAX)
+            brems_xs = m.inv_x0 * brems_shape(brems_grid, gcut)
+            brems_xs[0] = 0.0
+            table(f"table.{pdg}.e_brems.lambda.{mi}", brems_grid, brems_xs)
             for model in ("e_brems_sb", "e_brems_lpm"):
                 w.put(f"model.{pdg}.e_brems.{model}.{mi}.energy", egrid)
                 for ei, z in enumerate(m.z):
