@@ -34,24 +34,10 @@ sys.path.insert(0, REPO)
 
 import numpy as np  # noqa: E402
 
-WORKLOADS = {
-    # configs[0]: 50-layer Pb/lAr calorimeter, 100 e- at 1 GeV, pencil beam,
-    # no field, no MSC, 2^16 slots, seed 0 (one event of 100 primaries)
-    "c1": dict(geometry="calo", physics="calo", num_primaries=100, energy=1000.0,
-               emax=None, sigma=0.0, pdg=11, slots=1 << 16, seed=0, events=1,
-               msc=False, field=(0.0, 0.0, 0.0),
-               description="calorimeter 50x(2.3mm Pb+5.7mm lAr), 100 e- @ 1 GeV "
-                           "pencil beam, no field, no MSC, 2^16 track slots, FP64"),
-    # configs[1]: same calorimeter with Urban MSC and a uniform 1 T field
-    # along x; 10^4 e-, log-uniform 100 MeV-10 GeV, Gaussian spread 1 cm,
-    # 2^20 slots; each primary is its own event, all events in flight
-    "c2": dict(geometry="calo", physics="calo", num_primaries=10000, energy=100.0,
-               emax=1e4, sigma=1.0, pdg=11, slots=1 << 20, seed=0, events=10000,
-               msc=True, field=(1.0, 0.0, 0.0),
-               description="calorimeter 50x(2.3mm Pb+5.7mm lAr), Urban MSC, 1 T "
-                           "uniform field along x, 10^4 e- log-uniform 0.1-10 GeV, "
-                           "sigma 1 cm, 2^20 track slots, FP64"),
-}
+from celeritas_gb300.workloads import WORKLOADS, make_primaries, physics_args  # noqa: E402
+
+
+MAX_STEPS = 20000
 
 
 def load_peaks():
@@ -61,30 +47,6 @@ def load_peaks():
             d = json.load(f)
         return d.get("hbm_gbs", 6800.0), "measured"
     return 6800.0, "fallback"
-
-
-def make_primaries(wl, rank=0, num=None, seed_offset=0):
-    from celeritas_gb300.primaries import pencil_beam, spread_beam
-
-    num = wl["num_primaries"] if num is None else num
-    if wl["emax"] is None:
-        p = pencil_beam(num, energy=wl["energy"], pdg=wl["pdg"],
-                        num_events=min(wl["events"], num))
-    else:
-        p = spread_beam(num, emin=wl["energy"], emax=wl["emax"], sigma=wl["sigma"],
-                        pdg=wl["pdg"], seed=wl["seed"] + 1000 * rank + seed_offset,
-                        num_events=min(wl["events"], num))
-    p["event"] += rank * wl["events"]
-    return p
-
-
-def physics_args(wl):
-    args = []
-    if wl["msc"]:
-        args.append("--msc")
-    if any(wl["field"]):
-        args += ["--field"] + [repr(float(f)) for f in wl["field"]]
-    return args
 
 
 class ClockSampler:
@@ -258,9 +220,15 @@ def run_gb300(args, wl):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     def transport():
-        first = stepper.step(prim)
-        rest = stepper.run(max_steps=1_000_000, batch=64)
-        return [first] + rest
+        return finish([stepper.step(prim)])
+
+    def finish(res):
+        # A shower of this workload ends in a few hundred steps; a run that
+        # hits the cap has a track that never terminates
+        res += stepper.run(max_steps=MAX_STEPS, batch=64)
+        if res[-1].alive or res[-1].queued:
+            raise RuntimeError(f"transport did not finish in {MAX_STEPS} steps")
+        return res
 
     for _ in range(args.warmup):
         transport()
@@ -279,7 +247,7 @@ def run_gb300(args, wl):
             start = torch.cuda.Event(enable_timing=True)
             stop = torch.cuda.Event(enable_timing=True)
             start.record(stream)
-            res = [stepper.step()] + stepper.run(max_steps=1_000_000, batch=64)
+            res = finish([stepper.step()])
             stop.record(stream)
             edep = stepper.energy_deposition()  # device -> host tally
             torch.cuda.synchronize()
@@ -321,7 +289,7 @@ def run_gb300(args, wl):
     dom_bytes = bytes_per_action[dom] / max(launches[dom_id], 1)
     peak, peak_kind = load_peaks()
     achieved = dom_bytes / (dom_launch_ms / 1e3) / 1e9
-    traffic = read_traffic(dom)
+    traffic = read_traffic(dom, float(np.mean(active)))
 
     kernels_per_step = stepper.step_kernels()
     launches_timed = int(sum(it * kernels_per_step + 2 for it in iterations))
@@ -370,16 +338,21 @@ def run_gb300(args, wl):
         dist.destroy_process_group()
 
 
-def read_traffic(kernel_label):
-    """DRAM bytes per launch of a kernel from the committed ncu summary."""
+def read_traffic(kernel_label, mean_active):
+    """DRAM bytes per launch of a kernel, from the committed ncu capture.
+
+    The capture holds one launch's DRAM bytes and that launch's active track
+    slots; the figure is scaled to the mean active slots per launch of this
+    run (the traffic of a step action grows with the tracks it processes).
+    """
     path = os.path.join(REPO, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for line in f:
             tok = line.split()
-            if len(tok) >= 2 and tok[0] == kernel_label:
-                return float(tok[1])
+            if len(tok) >= 3 and tok[0] == kernel_label:
+                return float(tok[1]) * mean_active / float(tok[2])
     return None
 
 

@@ -1,0 +1,52 @@
+"""Run one transport of a benchmark workload for a profiler.
+
+    python -m celeritas_gb300.profile_run --workload c2 [--primaries N]
+        [--max-iterations K] [--steps-log FILE] [--graph]
+
+Inserts the workload's primaries, then steps (eagerly by default, so that
+every kernel is its own launch) until the state empties or K iterations have
+run, and prints one line per iteration with the step counters. Meant to be
+wrapped by ncu: the launch order is fixed (one launch per step action and
+iteration), so '-k <kernel> -s <n>' selects a known iteration.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+from . import Params, Stepper, load_library, physics_file
+from .workloads import WORKLOADS, make_primaries
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="c2", choices=list(WORKLOADS))
+    ap.add_argument("--primaries", type=int, default=None)
+    ap.add_argument("--max-iterations", type=int, default=20000)
+    ap.add_argument("--steps-log", default=None)
+    ap.add_argument("--graph", action="store_true")
+    args = ap.parse_args(argv)
+
+    wl = WORKLOADS[args.workload]
+    load_library()
+    params = Params(physics_file(wl["physics"]), wl["geometry"],
+                    field_tesla=wl["field"], msc=wl["msc"])
+    stepper = Stepper(params, wl["slots"], seed=wl["seed"], use_graph=args.graph)
+    prim = make_primaries(wl, num=args.primaries)
+    res = [stepper.step(prim)]
+    while len(res) < args.max_iterations and (res[-1].alive or res[-1].queued):
+        res.append(stepper.step())
+    stepper.synchronize()
+    rows = [[r.generated, r.queued, r.active, r.alive] for r in res]
+    if args.steps_log:
+        with open(args.steps_log, "w") as f:
+            json.dump({"workload": args.workload, "primaries": len(prim),
+                       "steps": rows}, f)
+    print(f"iterations {len(res)} track-steps {sum(r[2] for r in rows)}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -28,6 +28,10 @@ ACTION_BYTES = {
     # mfp, num steps (91)
     "along-step-general-linear": (292, 5),
     "along-step-neutral": (292, 5),
+    # as above, plus the multiple-scattering step-limit state (range at
+    # the volume entry, range factor, minimum limit: 24 B read + written)
+    # and the looping-step counter (4 + 4)
+    "along-step-uniform-msc": (348, 5),
     # reads post action, particle, material, energy, macro + per-process xs
     # (52); rng (48); writes mfp, post action, element (16)
     "physics-discrete-select": (116, 4),

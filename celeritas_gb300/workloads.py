@@ -1,0 +1,57 @@
+"""Benchmark workloads of the EM-shower stepping loop and their primaries.
+
+Two workloads, both on the 50-layer Pb/lAr sampling calorimeter that the
+reference's benchmark problems use (world box 60 x 60 x 60 cm of vacuum;
+layers of 2.3 mm Pb + 5.7 mm lAr, 40 x 40 cm, starting at z = 0):
+
+* ``c1`` -- 100 e- at 1 GeV in one event, pencil beam along +z, no field, no
+  multiple scattering, 2^16 track slots, seed 0. Small enough for the CPU.
+* ``c2`` -- Urban multiple scattering and a uniform 1 T field along x;
+  10^4 e-, energies log-uniform in 0.1-10 GeV, Gaussian transverse spread of
+  1 cm, one primary per event with all events in flight, 2^20 track slots.
+
+Primaries are synthetic (seeded numpy), standing in for the reference's
+PrimaryGenerator (src/celeritas/phys/PrimaryGenerator.cc).
+"""
+
+from __future__ import annotations
+
+from .primaries import pencil_beam, spread_beam
+
+WORKLOADS = {
+    "c1": dict(geometry="calo", physics="calo", num_primaries=100, energy=1000.0,
+               emax=None, sigma=0.0, pdg=11, slots=1 << 16, seed=0, events=1,
+               msc=False, field=(0.0, 0.0, 0.0),
+               description="calorimeter 50x(2.3mm Pb+5.7mm lAr), 100 e- @ 1 GeV "
+                           "pencil beam, no field, no MSC, 2^16 track slots, FP64"),
+    "c2": dict(geometry="calo", physics="calo", num_primaries=10000, energy=100.0,
+               emax=1e4, sigma=1.0, pdg=11, slots=1 << 20, seed=0, events=10000,
+               msc=True, field=(1.0, 0.0, 0.0),
+               description="calorimeter 50x(2.3mm Pb+5.7mm lAr), Urban MSC, 1 T "
+                           "uniform field along x, 10^4 e- log-uniform 0.1-10 GeV, "
+                           "sigma 1 cm, 2^20 track slots, FP64"),
+}
+
+
+def make_primaries(wl: dict, rank: int = 0, num: int | None = None, seed_offset: int = 0):
+    """Primaries of a workload; 'rank' offsets the event IDs and the seed."""
+    num = wl["num_primaries"] if num is None else num
+    if wl["emax"] is None:
+        p = pencil_beam(num, energy=wl["energy"], pdg=wl["pdg"],
+                        num_events=min(wl["events"], num))
+    else:
+        p = spread_beam(num, emin=wl["energy"], emax=wl["emax"], sigma=wl["sigma"],
+                        pdg=wl["pdg"], seed=wl["seed"] + 1000 * rank + seed_offset,
+                        num_events=min(wl["events"], num))
+    p["event"] += rank * wl["events"]
+    return p
+
+
+def physics_args(wl: dict) -> list[str]:
+    """Command-line physics options of the CPU oracle programs."""
+    args = []
+    if wl["msc"]:
+        args.append("--msc")
+    if any(wl["field"]):
+        args += ["--field"] + [repr(float(f)) for f in wl["field"]]
+    return args
