@@ -107,9 +107,13 @@ _PROTOTYPES = [
     ("gbx_stepper_state_info", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
       ctypes.POINTER(ctypes.c_size_t)]),
+    ("gbx_stepper_extend_from_secondaries_static", ctypes.c_int, [ctypes.c_void_p]),
 ]
 
 EXPORTED_SYMBOLS = [name for name, _, _ in _PROTOTYPES]
+
+#: GBX_STATIC_SCRATCH_MAX_SLOTS of the C header
+STATIC_SCRATCH_MAX_SLOTS = 131072
 
 
 def load_library(path: str | None = None) -> ctypes.CDLL:
@@ -256,6 +260,15 @@ class Stepper:
 
     def kill_active(self):
         _check(_lib.gbx_stepper_kill_active(self._handle))
+
+    def extend_from_secondaries_static(self):
+        """Extend-from-secondaries with the library's static scratch array.
+
+        Allocates no device memory; the stepper may have at most
+        STATIC_SCRATCH_MAX_SLOTS track slots. Calls that overlap on the GPU
+        share the array and race.
+        """
+        _check(_lib.gbx_stepper_extend_from_secondaries_static(self._handle))
 
     def stream_handle(self) -> int:
         """cudaStream_t of the stepper, as an integer (for event timing)."""

@@ -332,6 +332,19 @@ int gbx_stepper_insert_primaries(gbx_stepper* stepper,
     });
 }
 
+static_assert(GBX_STATIC_SCRATCH_MAX_SLOTS == gbx::static_scratch_max_slots,
+              "public and internal static scratch limits differ");
+
+int gbx_stepper_extend_from_secondaries_static(gbx_stepper* stepper)
+{
+    return guarded([&] {
+        auto& state = stepper->stepper->state();
+        gbx::launch_extend_from_secondaries_static(state.context(), state.stream());
+        if (cudaError_t err = cudaGetLastError(); err != cudaSuccess)
+            throw std::runtime_error(cudaGetErrorString(err));
+    });
+}
+
 int gbx_stepper_kill_active(gbx_stepper* stepper)
 {
     return guarded([&] { stepper->stepper->kill_active(); });

@@ -16,6 +16,10 @@
 // exclusive-scan offset.
 #include "Kernels.cuh"
 
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
 #include "../gbx/TrackInit.hh"
 
 namespace gbx
@@ -511,6 +515,103 @@ void launch_step(LaunchContext const& ctx, cudaStream_t stream)
     post_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
         ctx.params, ctx.state);
     launch_extend_from_secondaries(ctx, stream);
+}
+
+//---------------------------------------------------------------------------//
+// Extend-from-secondaries with library-owned scratch
+//---------------------------------------------------------------------------//
+// The three extend-from-secondaries kernels need 5 bytes of scratch per
+// track slot plus 8 bytes per block. This variant takes that scratch from
+// one array compiled into the library instead of the stepper's allocation,
+// for callers that may not allocate device memory at all. Layout for n
+// slots and b = ceil(n / block_size) blocks, each part 256-byte aligned:
+//   block_vacant[b] | block_count[b] | count[n] | vacant[n]
+namespace
+{
+constexpr std::size_t align_256(std::size_t bytes)
+{
+    return (bytes + 255) & ~std::size_t(255);
+}
+
+constexpr std::size_t static_scratch_bytes(std::size_t n)
+{
+    std::size_t const b = (n + block_size - 1) / block_size;
+    return 2 * align_256(b * sizeof(size_type))
+           + align_256(n * sizeof(size_type)) + align_256(n);
+}
+
+// 659,456 bytes for 131,072 track slots
+constexpr std::size_t static_scratch_capacity
+    = static_scratch_bytes(static_scratch_max_slots);
+
+__device__ __align__(256) unsigned char static_scan_scratch[static_scratch_capacity];
+
+// Device address of static_scan_scratch, looked up once per device
+constexpr int static_scratch_max_devices = 64;
+std::mutex static_scratch_mutex;
+void* static_scratch_address[static_scratch_max_devices] = {};
+
+unsigned char* static_scratch_for_current_device()
+{
+    int device = -1;
+    if (cudaError_t err = cudaGetDevice(&device); err != cudaSuccess)
+    {
+        throw std::runtime_error(std::string("cudaGetDevice failed: ")
+                                 + cudaGetErrorString(err));
+    }
+    if (device < 0 || device >= static_scratch_max_devices)
+    {
+        throw std::runtime_error("static scratch supports device ordinals below "
+                                 + std::to_string(static_scratch_max_devices));
+    }
+    std::lock_guard<std::mutex> lock(static_scratch_mutex);
+    if (!static_scratch_address[device])
+    {
+        void* ptr = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&ptr, static_scan_scratch);
+        if (err != cudaSuccess || !ptr)
+        {
+            throw std::runtime_error(
+                std::string("cudaGetSymbolAddress of the static scratch failed: ")
+                + cudaGetErrorString(err));
+        }
+        static_scratch_address[device] = ptr;
+    }
+    return static_cast<unsigned char*>(static_scratch_address[device]);
+}
+}  // namespace
+
+void launch_extend_from_secondaries_static(LaunchContext const& ctx,
+                                           cudaStream_t stream)
+{
+    size_type const n = ctx.state.size;
+    if (n > static_scratch_max_slots)
+    {
+        throw std::runtime_error(
+            "the stepper has " + std::to_string(n)
+            + " track slots but the static scratch of extend-from-secondaries "
+              "holds at most "
+            + std::to_string(static_scratch_max_slots));
+    }
+    unsigned char* base = static_scratch_for_current_device();
+    unsigned int const nb = num_blocks_for(n);
+    std::size_t const block_part = align_256(std::size_t(nb) * sizeof(size_type));
+    std::size_t const count_part = align_256(std::size_t(n) * sizeof(size_type));
+
+    // Nothing is cleared: locate_alive_kernel writes vacant/count for every
+    // slot and both totals for every block before the scan and scatter
+    // kernels read them, so the previous call's contents are never used
+    ScanScratch scr;
+    scr.block_vacant = reinterpret_cast<size_type*>(base);
+    scr.block_count = reinterpret_cast<size_type*>(base + block_part);
+    scr.count = reinterpret_cast<size_type*>(base + 2 * block_part);
+    scr.vacant = base + 2 * block_part + count_part;
+    scr.num_blocks = nb;
+
+    locate_alive_kernel<<<nb, block_size, 0, stream>>>(ctx.state, scr);
+    scan_blocks_kernel<<<1, 1024, 0, stream>>>(
+        ctx.state, scr, ctx.log, ctx.log_capacity, ctx.step_index);
+    scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, scr);
 }
 
 }  // namespace gbx

@@ -66,6 +66,14 @@ void launch_extend_from_secondaries(LaunchContext const& ctx,
                                     cudaStream_t stream);
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
 
+//! Largest state that the library-owned extend-from-secondaries scratch fits
+constexpr size_type static_scratch_max_slots = 131072;
+//! Extend-from-secondaries with its scratch in a static device array of the
+//! library (no allocation; throws if the state has too many slots). The
+//! first call on a device looks up the array's address on that device.
+void launch_extend_from_secondaries_static(LaunchContext const& ctx,
+                                           cudaStream_t stream);
+
 //! One full step without primary insertion (graph-capturable)
 void launch_step(LaunchContext const& ctx, cudaStream_t stream);
 

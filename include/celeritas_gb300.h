@@ -179,6 +179,35 @@ int gbx_stepper_state_info(gbx_stepper* stepper,
                            size_t* elem_bytes,
                            size_t* count);
 
+/* Largest stepper (track slots) accepted by
+ * gbx_stepper_extend_from_secondaries_static */
+#define GBX_STATIC_SCRATCH_MAX_SLOTS 131072
+
+/* The extend-from-secondaries step action (what gbx_stepper_launch_action
+ * runs for that action ID) with its scan scratch taken from a fixed array
+ * compiled into this library, so that the call allocates no device memory.
+ * This entry point has no counterpart in the reference.
+ *
+ * It is for callers that launch the end-of-step compaction from code that
+ * may not allocate device memory: a host framework that owns all device
+ * memory through its own fixed pool and forbids cudaMalloc after start-up
+ * (an allocation there would bypass the pool's accounting, may synchronise
+ * the device, and can fail once the pool has claimed the memory).
+ *
+ * - The scratch is 659,456 bytes and fits steppers of at most
+ *   GBX_STATIC_SCRATCH_MAX_SLOTS track slots; larger ones are rejected with
+ *   an error and nothing is launched.
+ * - The first call on a device, with that device current, looks up the
+ *   array's device address (cudaGetSymbolAddress); make that first call
+ *   before any stream capture. The stepper's device must be current.
+ * - Every call on a device shares the one array and leaves its contents
+ *   behind. Each call writes every scratch element before reading it, so
+ *   nothing needs clearing; but calls that overlap on the GPU (two steppers
+ *   on different streams) race on the array and corrupt each other.
+ * - Kernels are launched on the stepper's stream; the call does not wait
+ *   for them. */
+int gbx_stepper_extend_from_secondaries_static(gbx_stepper* stepper);
+
 #ifdef __cplusplus
 }
 #endif
