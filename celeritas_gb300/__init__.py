@@ -42,7 +42,8 @@ class _Primary(ctypes.Structure):
 
 
 class _ParamsOptions(ctypes.Structure):
-    _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int)]
+    _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int),
+                ("track_order", ctypes.c_uint)]
 
 
 class _StepResult(ctypes.Structure):
@@ -112,6 +113,10 @@ _PROTOTYPES = [
 
 EXPORTED_SYMBOLS = [name for name, _, _ in _PROTOTYPES]
 
+#: Supported TrackOrder policies (the reference's enumerator values)
+TRACK_ORDERS = {"none": 0, "reindex_along_step_action": 5,
+                "reindex_step_limit_action": 6, "reindex_both_action": 7}
+
 #: GBX_STATIC_SCRATCH_MAX_SLOTS of the C header
 STATIC_SCRATCH_MAX_SLOTS = 131072
 
@@ -150,19 +155,24 @@ class Params:
     """Problem parameters on the device (celeritas::CoreParams)."""
 
     def __init__(self, physics: str, geometry: str = "calo",
-                 field_tesla=(0.0, 0.0, 0.0), msc: bool = False):
+                 field_tesla=(0.0, 0.0, 0.0), msc: bool = False,
+                 track_order: int | str = "none"):
         lib = load_library()
         handle = ctypes.c_void_p()
         opts = _ParamsOptions()
         for i in range(3):
             opts.field_tesla[i] = float(field_tesla[i])
         opts.msc = int(msc)
+        if isinstance(track_order, str):
+            track_order = TRACK_ORDERS[track_order]
+        opts.track_order = int(track_order)
         _check(lib.gbx_params_create(physics.encode(), geometry.encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle
         self.geometry = geometry
         self.field_tesla = tuple(field_tesla)
         self.msc = msc
+        self.track_order = int(track_order)
 
     def __del__(self):
         if getattr(self, "_handle", None) and _lib is not None:

@@ -148,6 +148,7 @@ FieldRef find_field(gbx::CoreState& st, std::string const& name)
     if (name == "secondary_counts") return f(s.secondary_counts);
     if (name == "rng")
         return FieldRef{s.rng.s[0], sizeof(std::uint32_t), 6 * n};
+    if (name == "track_slots") return f(s.track_slots);
     if (name == "counters")
         return FieldRef{s.counters, sizeof(Counters), 1};
     if (name == "initializers")
@@ -189,6 +190,7 @@ int gbx_params_create(const char* physics_file,
         if (options)
         {
             inp.options.msc = options->msc != 0;
+            inp.options.track_order = options->track_order;
             for (int i = 0; i < 3; ++i)
                 inp.options.field_tesla[i] = options->field_tesla[i];
         }

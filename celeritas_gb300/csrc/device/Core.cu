@@ -134,6 +134,14 @@ void step_secondaries(CoreParams const&, CoreState& state, ActionId)
 {
     launch_extend_from_secondaries(state.context(), state.stream());
 }
+void step_sort_along(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_sort_tracks(state.context(), SortKey::along_step, state.stream());
+}
+void step_sort_post(CoreParams const&, CoreState& state, ActionId)
+{
+    launch_sort_tracks(state.context(), SortKey::step_limit, state.stream());
+}
 
 }  // namespace
 
@@ -158,7 +166,9 @@ ActionId ActionRegistry::find_action(std::string_view label) const
     return invalid_id;
 }
 
-void register_core_actions(ActionRegistry* reg, bool uniform_field)
+void register_core_actions(ActionRegistry* reg,
+                           bool uniform_field,
+                           unsigned int track_order)
 {
     using O = StepActionOrder;
     auto add = [reg](std::string label,
@@ -232,6 +242,21 @@ void register_core_actions(ActionRegistry* reg, bool uniform_field)
         "create track initializers from secondaries",
         O::end,
         step_secondaries);
+    // Optional sorting actions (SortTracksAction): step-limit sort first
+    if (sorts_step_limit(track_order))
+    {
+        add("sort-tracks-post-step",
+            "sort tracks states",
+            O::sort_pre_post,
+            step_sort_post);
+    }
+    if (sorts_along_step(track_order))
+    {
+        add("sort-tracks-along-step",
+            "sort tracks states",
+            O::sort_pre,
+            step_sort_along);
+    }
     // Step gathering: the pre-step detector lookup is fused into the
     // pre-step kernel; the post-step gather applies the calorimeter tally
     add("step-gather-pre", "gather pre-step steps/hits", O::user_pre, nullptr);
@@ -245,7 +270,8 @@ CoreParams::CoreParams(Input const& inp)
     : host_(build_params(inp.physics_file, inp.geometry, inp.options))
     , actions_(std::make_shared<ActionRegistry>())
 {
-    register_core_actions(actions_.get(), host_.scalars.has_field);
+    register_core_actions(
+        actions_.get(), host_.scalars.has_field, host_.scalars.track_order);
     for (size_type i = 0; i < host_.action_labels.size(); ++i)
     {
         if (actions_->id_to_label(i) != host_.action_labels[i])
@@ -376,6 +402,12 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_bcnt = L.reserve(4 * std::size_t(nblocks));
     std::size_t o_svac = arr(1);
     std::size_t o_scnt = arr(4);
+    // Action sort: thread -> slot indirection, bin offsets, block counts
+    size_type const num_bins = params.host().scalars.num_actions + 1;
+    size_type const sort_blocks = (n + sort_block_size - 1) / sort_block_size;
+    std::size_t o_tslots = arr(4);
+    std::size_t o_aoff = L.reserve(4 * std::size_t(num_bins + 1));
+    std::size_t o_shist = L.reserve(4 * std::size_t(num_bins) * sort_blocks);
     std::size_t o_log = L.reserve(sizeof(StepRecord) * log_cap);
     std::size_t o_stepidx = L.reserve(sizeof(size_type));
 
@@ -446,6 +478,8 @@ CoreState::CoreState(CoreParams const& params,
     s.primaries = static_cast<TrackInitializer*>(at(o_prims));
     s.primary_capacity = prim_cap;
     s.counters = static_cast<Counters*>(at(o_counters));
+    s.track_slots = static_cast<size_type*>(at(o_tslots));
+    s.action_offsets = static_cast<size_type*>(at(o_aoff));
 
     // Initial values that are not zero: fill from host staging
     {
@@ -493,6 +527,9 @@ CoreState::CoreState(CoreParams const& params,
     ctx_.scratch.vacant = static_cast<std::uint8_t*>(at(o_svac));
     ctx_.scratch.count = static_cast<size_type*>(at(o_scnt));
     ctx_.scratch.num_blocks = nblocks;
+    ctx_.sort.block_hist = static_cast<size_type*>(at(o_shist));
+    ctx_.sort.num_bins = num_bins;
+    ctx_.sort.num_blocks = sort_blocks;
     ctx_.log = static_cast<StepRecord*>(at(o_log));
     ctx_.log_capacity = log_cap;
     ctx_.step_index = static_cast<size_type*>(at(o_stepidx));

@@ -415,6 +415,182 @@ __global__ void kill_active_kernel(ParamsData p, StateData s)
     }
 }
 
+//---------------------------------------------------------------------------//
+// Action sort (SortTracksAction): stable counting sort of the track slots by
+// action ID in three kernels. Blocks of sort_block_size slots count their
+// keys with warp-aggregated shared-memory atomics (match_any + popc); one
+// block scans the bin-major [bin][block] counts; the scatter ranks each slot
+// among equal keys of its warp (match_any) and of the preceding warps, so
+// slots of one action stay in increasing order.
+//---------------------------------------------------------------------------//
+__device__ __forceinline__ size_type sort_key(StateData const& s,
+                                              SortKey key,
+                                              size_type slot,
+                                              size_type invalid_bin)
+{
+    size_type a = (key == SortKey::along_step) ? s.along_step_action[slot]
+                                               : s.post_step_action[slot];
+    return a < invalid_bin ? a : invalid_bin;
+}
+
+__global__ __launch_bounds__(sort_block_size) void sort_count_kernel(
+    StateData s, SortScratch srt, SortKey key)
+{
+    extern __shared__ size_type hist[];  // [num_bins]
+    for (size_type i = threadIdx.x; i < srt.num_bins; i += blockDim.x)
+        hist[i] = 0;
+    __syncthreads();
+    size_type const slot = blockIdx.x * sort_block_size + threadIdx.x;
+    bool const valid = slot < s.size;
+    size_type const k = valid ? sort_key(s, key, slot, srt.num_bins - 1)
+                              : srt.num_bins;
+    unsigned int const peers = __match_any_sync(0xffffffffu, k);
+    unsigned int const lane = threadIdx.x & 31u;
+    if (valid && (peers & ((1u << lane) - 1u)) == 0)
+        atomicAdd(hist + k, static_cast<size_type>(__popc(peers)));
+    __syncthreads();
+    for (size_type i = threadIdx.x; i < srt.num_bins; i += blockDim.x)
+        srt.block_hist[i * srt.num_blocks + blockIdx.x] = hist[i];
+}
+
+__global__ __launch_bounds__(1024) void sort_scan_kernel(StateData s, SortScratch srt)
+{
+    __shared__ size_type warp_sums[32];
+    size_type const total = srt.num_bins * srt.num_blocks;
+    size_type const per = (total + 1023) / 1024;
+    size_type const begin = min_of(total, threadIdx.x * per);
+    size_type const end = min_of(total, begin + per);
+    size_type sum = 0;
+    for (size_type i = begin; i < end; ++i)
+        sum += srt.block_hist[i];
+    // Block-wide exclusive scan of the per-thread sums
+    unsigned int const lane = threadIdx.x & 31u;
+    unsigned int const warp = threadIdx.x >> 5;
+    size_type incl = sum;
+    for (unsigned int off = 1; off < 32; off <<= 1)
+    {
+        size_type v = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off)
+            incl += v;
+    }
+    if (lane == 31)
+        warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        size_type const w = warp_sums[lane];
+        size_type wi = w;
+        for (unsigned int off = 1; off < 32; off <<= 1)
+        {
+            size_type v = __shfl_up_sync(0xffffffffu, wi, off);
+            if (lane >= off)
+                wi += v;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    size_type run = warp_sums[warp] + incl - sum;
+    for (size_type i = begin; i < end; ++i)
+    {
+        size_type const c = srt.block_hist[i];
+        srt.block_hist[i] = run;
+        run += c;
+    }
+    __syncthreads();
+    for (size_type b = threadIdx.x; b < srt.num_bins; b += blockDim.x)
+        s.action_offsets[b] = srt.block_hist[b * srt.num_blocks];
+    if (threadIdx.x == 0)
+        s.action_offsets[srt.num_bins] = s.size;
+}
+
+__global__ __launch_bounds__(sort_block_size) void sort_scatter_kernel(
+    StateData s, SortScratch srt, SortKey key)
+{
+    constexpr unsigned int num_warps = sort_block_size / 32;
+    extern __shared__ size_type warp_hist[];  // [num_warps][num_bins]
+    size_type const nb = srt.num_bins;
+    for (size_type i = threadIdx.x; i < num_warps * nb; i += blockDim.x)
+        warp_hist[i] = 0;
+    __syncthreads();
+    size_type const slot = blockIdx.x * sort_block_size + threadIdx.x;
+    bool const valid = slot < s.size;
+    size_type const k = valid ? sort_key(s, key, slot, nb - 1) : nb;
+    unsigned int const peers = __match_any_sync(0xffffffffu, k);
+    unsigned int const lane = threadIdx.x & 31u;
+    unsigned int const warp = threadIdx.x >> 5;
+    unsigned int const lower = peers & ((1u << lane) - 1u);
+    if (valid && lower == 0)
+        warp_hist[warp * nb + k] = __popc(peers);
+    __syncthreads();
+    for (size_type b = threadIdx.x; b < nb; b += blockDim.x)
+    {
+        size_type acc = 0;
+        for (unsigned int w = 0; w < num_warps; ++w)
+        {
+            size_type const c = warp_hist[w * nb + b];
+            warp_hist[w * nb + b] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    if (valid)
+    {
+        size_type const pos = srt.block_hist[k * srt.num_blocks + blockIdx.x]
+                              + warp_hist[warp * nb + k] + __popc(lower);
+        s.track_slots[pos] = slot;
+    }
+}
+
+//! Slot of this thread within the sorted bins [first_bin, end_bin)
+__device__ __forceinline__ bool sorted_slot(StateData const& s,
+                                            size_type first_bin,
+                                            size_type end_bin,
+                                            size_type* slot)
+{
+    size_type const t = s.action_offsets[first_bin] + blockIdx.x * blockDim.x
+                        + threadIdx.x;
+    if (t >= s.action_offsets[end_bin])
+        return false;
+    *slot = s.track_slots[t];
+    return true;
+}
+
+__global__ __launch_bounds__(block_size) void along_step_sorted_kernel(
+    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+{
+    size_type slot;
+    if (sorted_slot(s, first_bin, end_bin, &slot))
+        along_step(p, s, slot);
+}
+
+__global__ __launch_bounds__(block_size) void interact_sorted_kernel(
+    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+{
+    size_type slot;
+    if (sorted_slot(s, first_bin, end_bin, &slot))
+    {
+        size_type a = s.post_step_action[slot];
+        if (a >= p.model_to_action && a < p.model_to_action + p.num_models)
+            interact(p, s, slot, a);
+    }
+}
+
+__global__ __launch_bounds__(block_size) void boundary_sorted_kernel(
+    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+{
+    size_type slot;
+    if (sorted_slot(s, first_bin, end_bin, &slot))
+        boundary_cross(p, s, slot);
+}
+
+__global__ __launch_bounds__(block_size) void tracking_cut_sorted_kernel(
+    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+{
+    size_type slot;
+    if (sorted_slot(s, first_bin, end_bin, &slot))
+        tracking_cut(p, s, slot);
+}
+
 }  // namespace
 
 //---------------------------------------------------------------------------//
@@ -448,6 +624,21 @@ void launch_along_step(LaunchContext const& ctx,
                        size_type action,
                        cudaStream_t stream)
 {
+    ParamsData const& p = ctx.params;
+    if (sorts_along_step(p.track_order))
+    {
+        // Launch over the action's sorted range (all along-step bins if
+        // invalid); the grid covers the largest possible range
+        size_type first = action, end = action + 1;
+        if (action == invalid_id)
+        {
+            first = min_of(p.action_along_step, p.action_along_step_neutral);
+            end = max_of(p.action_along_step, p.action_along_step_neutral) + 1;
+        }
+        along_step_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            p, ctx.state, first, end);
+        return;
+    }
     along_step_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
         ctx.params, ctx.state, action);
 }
@@ -460,6 +651,19 @@ void launch_discrete_select(LaunchContext const& ctx, cudaStream_t stream)
 
 void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t stream)
 {
+    ParamsData const& p = ctx.params;
+    if (sorts_step_limit(p.track_order))
+    {
+        size_type first = action, end = action + 1;
+        if (action == invalid_id)
+        {
+            first = p.model_to_action;
+            end = p.model_to_action + p.num_models;
+        }
+        interact_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            p, ctx.state, first, end);
+        return;
+    }
     if (action == invalid_id)
     {
         interact_all_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
@@ -474,12 +678,26 @@ void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t st
 
 void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
 {
+    ParamsData const& p = ctx.params;
+    if (sorts_step_limit(p.track_order))
+    {
+        boundary_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            p, ctx.state, p.action_boundary, p.action_boundary + 1);
+        return;
+    }
     boundary_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
         ctx.params, ctx.state);
 }
 
 void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
 {
+    ParamsData const& p = ctx.params;
+    if (sorts_step_limit(p.track_order))
+    {
+        tracking_cut_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            p, ctx.state, p.action_tracking_cut, p.action_tracking_cut + 1);
+        return;
+    }
     tracking_cut_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
         ctx.params, ctx.state);
 }
@@ -505,12 +723,30 @@ void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream)
         ctx.params, ctx.state);
 }
 
+void launch_sort_tracks(LaunchContext const& ctx, SortKey key, cudaStream_t stream)
+{
+    SortScratch const& srt = ctx.sort;
+    sort_count_kernel<<<srt.num_blocks,
+                        sort_block_size,
+                        srt.num_bins * sizeof(size_type),
+                        stream>>>(ctx.state, srt, key);
+    sort_scan_kernel<<<1, 1024, 0, stream>>>(ctx.state, srt);
+    sort_scatter_kernel<<<srt.num_blocks,
+                          sort_block_size,
+                          (sort_block_size / 32) * srt.num_bins * sizeof(size_type),
+                          stream>>>(ctx.state, srt, key);
+}
+
 void launch_step(LaunchContext const& ctx, cudaStream_t stream)
 {
     launch_initialize_tracks(ctx, stream);
     launch_pre_step(ctx, stream);
+    if (sorts_along_step(ctx.params.track_order))
+        launch_sort_tracks(ctx, SortKey::along_step, stream);
     launch_along_step(ctx, invalid_id, stream);
     launch_discrete_select(ctx, stream);
+    if (sorts_step_limit(ctx.params.track_order))
+        launch_sort_tracks(ctx, SortKey::step_limit, stream);
     launch_interact(ctx, invalid_id, stream);
     post_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
         ctx.params, ctx.state);

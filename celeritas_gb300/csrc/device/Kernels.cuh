@@ -26,6 +26,22 @@ struct ScanScratch
     size_type num_blocks;
 };
 
+//! Scratch of the action sort: per-block bin counts, bin-major
+//! ([bin][block]), for blocks of sort_block_size slots
+struct SortScratch
+{
+    size_type* block_hist;  //!< [num_bins * num_blocks]
+    size_type num_bins;  //!< num_actions + 1 (last: invalid action)
+    size_type num_blocks;
+};
+
+//! Which action a sort orders tracks by
+enum class SortKey
+{
+    along_step,  //!< along_step_action (reindex_along_step_action)
+    step_limit,  //!< post_step_action (reindex_step_limit_action)
+};
+
 //! Error flags written by device code
 enum ErrorFlag : size_type
 {
@@ -34,12 +50,14 @@ enum ErrorFlag : size_type
 };
 
 constexpr int block_size = 256;
+constexpr int sort_block_size = 1024;
 
 struct LaunchContext
 {
     ParamsData params;
     StateData state;
     ScanScratch scratch;
+    SortScratch sort;
     StepRecord* log;  //!< Step log (ring buffer)
     size_type log_capacity;
     size_type* step_index;  //!< Device-resident step counter
@@ -65,6 +83,9 @@ void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream);
 void launch_extend_from_secondaries(LaunchContext const& ctx,
                                     cudaStream_t stream);
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
+//! Stable counting sort of the track slots by action (SortTracksAction):
+//! fills state.track_slots and state.action_offsets
+void launch_sort_tracks(LaunchContext const& ctx, SortKey key, cudaStream_t stream);
 
 //! Largest state that the library-owned extend-from-secondaries scratch fits
 constexpr size_type static_scratch_max_slots = 131072;

@@ -32,6 +32,29 @@ GBX_FORCEINLINE bool is_track_valid(std::uint8_t s)
     return s != status_inactive && s != status_errored;
 }
 
+//! Track ordering policies (src/celeritas/Types.hh:151-171); the values
+//! are the reference's enumerators. Only 'none' and the action sorts are
+//! built.
+enum TrackOrder : unsigned int
+{
+    track_order_none = 0,
+    track_order_reindex_along_step_action = 5,
+    track_order_reindex_step_limit_action = 6,
+    track_order_reindex_both_action = 7,
+};
+
+GBX_FORCEINLINE bool sorts_along_step(unsigned int order)
+{
+    return order == track_order_reindex_along_step_action
+           || order == track_order_reindex_both_action;
+}
+
+GBX_FORCEINLINE bool sorts_step_limit(unsigned int order)
+{
+    return order == track_order_reindex_step_limit_action
+           || order == track_order_reindex_both_action;
+}
+
 //! Value grid types (src/celeritas/phys/PhysicsData.hh ValueGridType)
 enum ValueGridType : int
 {
@@ -326,6 +349,11 @@ struct ParamsData
     size_type action_klein_nishina;
     size_type action_bethe_heitler;
     size_type action_eplusgg;
+    // Track sorting: policy, sort actions (invalid if absent), action count
+    unsigned int track_order;
+    size_type action_sort_along;
+    size_type action_sort_post;
+    size_type num_actions;
 
     GeoParams geo;
 
@@ -449,6 +477,12 @@ struct StateData
     // Primaries staging
     TrackInitializer* primaries;
     size_type primary_capacity;
+
+    // Action-sorted thread -> slot indirection (CoreStateData::track_slots)
+    // and the first thread of each action bin; the last bin holds slots
+    // whose action is invalid (num_actions + 2 offsets)
+    size_type* track_slots;
+    size_type* action_offsets;
 
     Counters* counters;
 };

@@ -288,6 +288,8 @@ class Stepper
 
 //! Register the stepping-loop actions in the reference's order and return
 //! the list (CoreParams::build_actions, PhysicsParams actions, models)
-void register_core_actions(ActionRegistry* reg, bool uniform_field);
+void register_core_actions(ActionRegistry* reg,
+                           bool uniform_field,
+                           unsigned int track_order);
 
 }  // namespace gbx

@@ -255,10 +255,37 @@ void Builder::build_actions()
                          "geo-propagation-limit",
                          "geo-boundary",
                          "tracking-cut",
-                         "extend-from-secondaries",
-                         "step-gather-pre",
-                         "step-gather-post"};
+                         "extend-from-secondaries"};
     ParamsData& s = hp_.scalars;
+    // Optional track-sorting actions (CoreParams.cc:258-283): the step-limit
+    // sort is registered before the along-step sort
+    s.track_order = opts_.track_order;
+    s.action_sort_along = s.action_sort_post = invalid_id;
+    switch (opts_.track_order)
+    {
+        case track_order_none:
+            break;
+        case track_order_reindex_along_step_action:
+            s.action_sort_along = hp_.action_labels.size();
+            hp_.action_labels.push_back("sort-tracks-along-step");
+            break;
+        case track_order_reindex_step_limit_action:
+            s.action_sort_post = hp_.action_labels.size();
+            hp_.action_labels.push_back("sort-tracks-post-step");
+            break;
+        case track_order_reindex_both_action:
+            s.action_sort_post = hp_.action_labels.size();
+            hp_.action_labels.push_back("sort-tracks-post-step");
+            s.action_sort_along = hp_.action_labels.size();
+            hp_.action_labels.push_back("sort-tracks-along-step");
+            break;
+        default:
+            throw std::runtime_error("track order " + std::to_string(opts_.track_order)
+                                     + " is not supported (0, 5, 6 or 7)");
+    }
+    hp_.action_labels.push_back("step-gather-pre");
+    hp_.action_labels.push_back("step-gather-post");
+    s.num_actions = hp_.action_labels.size();
     s.action_pre_step = 0;
     s.action_msc_range = 1;
     s.action_range = 2;

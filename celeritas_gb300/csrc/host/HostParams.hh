@@ -44,6 +44,8 @@ struct ParamsOptions
     bool msc{false};
     //! Uniform magnetic field [tesla]; zero for straight-line transport
     double field_tesla[3]{0, 0, 0};
+    //! TrackOrder policy (none or one of the action sorts)
+    unsigned int track_order{0};
 };
 
 //! All parameter tables in host memory

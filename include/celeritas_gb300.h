@@ -56,14 +56,29 @@ typedef struct
 /* Message describing the last error on this thread ("" if none) */
 const char* gbx_last_error(void);
 
-/* Physics options (the RunnerInput field / physics_options knobs,
- * app/celer-sim/RunnerInput.hh:41-141): a uniform magnetic field in tesla
- * (all zero: straight-line transport, along-step-general-linear; otherwise
- * along-step-uniform-msc) and Urban multiple scattering for e-/e+ */
+/* Track ordering policies (celeritas::TrackOrder, src/celeritas/Types.hh:151-171,
+ * with the reference's enumerator values); only these are supported */
+enum
+{
+    GBX_TRACK_ORDER_NONE = 0,
+    GBX_TRACK_ORDER_REINDEX_ALONG_STEP_ACTION = 5,
+    GBX_TRACK_ORDER_REINDEX_STEP_LIMIT_ACTION = 6,
+    GBX_TRACK_ORDER_REINDEX_BOTH_ACTION = 7
+};
+
+/* Physics options (the RunnerInput field / physics_options / track_order
+ * knobs, app/celer-sim/RunnerInput.hh:41-141): a uniform magnetic field in
+ * tesla (all zero: straight-line transport, along-step-general-linear;
+ * otherwise along-step-uniform-msc), Urban multiple scattering for e-/e+,
+ * and the track order. An action-sorting order registers the reference's
+ * sort-tracks-post-step and/or sort-tracks-along-step actions (after
+ * extend-from-secondaries, CoreParams.cc:258-283) and launches the sorted
+ * actions over their ranges of action-sorted track slots. */
 typedef struct
 {
     double field_tesla[3];
     int msc;
+    unsigned int track_order;
 } gbx_params_options;
 
 /* Build problem parameters from a physics input file and a named geometry

@@ -215,7 +215,9 @@ class PortStepper
     }
 };
 
-//! Physics options from the command line: --msc, --field Bx By Bz [tesla]
+//! Physics options from the command line: --msc, --field Bx By Bz [tesla],
+//! --track-order N (changes the registered actions only: the host loop's
+//! results do not depend on the thread order)
 ParamsOptions physics_options(int argc, char** argv)
 {
     ParamsOptions opts;
@@ -228,6 +230,10 @@ ParamsOptions physics_options(int argc, char** argv)
         {
             for (int k = 0; k < 3; ++k)
                 opts.field_tesla[k] = std::strtod(argv[i + 1 + k], nullptr);
+        }
+        else if (a == "--track-order" && i + 1 < argc)
+        {
+            opts.track_order = std::stoul(argv[i + 1]);
         }
     }
     return opts;

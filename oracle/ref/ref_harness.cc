@@ -12,7 +12,7 @@
 //
 // Usage:
 //   ref_harness run <physics.txt> <geometry> <primaries.txt> <num_slots>
-//               <seed> [--field Bx By Bz] [--msc] [--steps N] [--trace]
+//               <seed> [--field Bx By Bz] [--msc] [--steps N] [--track-order N] [--trace]
 //   ref_harness geo <physics.txt> <geometry>
 #include <cmath>
 #include <cstdio>
@@ -484,7 +484,8 @@ Problem build_problem(ImportData const& imported,
                       std::string const& geo_name,
                       unsigned int seed,
                       Real3 field,
-                      bool msc)
+                      bool msc,
+                      TrackOrder track_order)
 {
     Problem prob;
     prob.geo = build_geometry(geo_name);
@@ -574,7 +575,7 @@ Problem build_problem(ImportData const& imported,
         TrackInitParams::Input input;
         input.capacity = 1u << 22;
         input.max_events = 1u << 16;
-        input.track_order = TrackOrder::none;
+        input.track_order = track_order;
         params.init = std::make_shared<TrackInitParams>(input);
     }
 
@@ -629,7 +630,8 @@ int run(int argc, char** argv)
     if (argc < 7)
     {
         std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
-                     "<seed> [--field Bx By Bz] [--msc] [--steps N]\n";
+                     "<seed> [--field Bx By Bz] [--msc] [--steps N] "
+                     "[--track-order N]\n";
         return 2;
     }
     std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
@@ -638,6 +640,7 @@ int run(int argc, char** argv)
     Real3 field{0, 0, 0};
     bool msc = false;
     size_type max_steps = static_cast<size_type>(-1);
+    TrackOrder track_order = TrackOrder::none;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -652,11 +655,14 @@ int run(int argc, char** argv)
             msc = true;
         else if (a == "--steps")
             max_steps = std::stoul(argv[++i]);
+        else if (a == "--track-order")
+            track_order = static_cast<TrackOrder>(std::stoi(argv[++i]));
     }
 
     KvFile kv(phys_path);
     ImportData imported = load_import(kv, msc);
-    Problem prob = build_problem(imported, geo_name, seed, field, msc);
+    Problem prob
+        = build_problem(imported, geo_name, seed, field, msc, track_order);
     auto primaries = load_primaries(prim_path, *prob.core->particle());
 
     StepperInput sinp;

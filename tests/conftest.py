@@ -26,7 +26,8 @@ def load_golden(name: str) -> dict:
 GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
                 "calo_ep500_n4", "calo_e1000_n100", "calo_e10000_n2",
                 "calo_msc_e1000_n4", "calo_field_e1000_n4", "calo_msc_field_e5000_n2",
-                "calo_msc_field_ep2000_n2"]
+                "calo_msc_field_ep2000_n2", "calo_sorted_both_e1000_n4",
+                "calo_sorted_post_g100_n16", "calo_msc_field_sorted_along_e2000_n2"]
 
 
 def case_options(case: dict) -> list[str]:
@@ -37,6 +38,8 @@ def case_options(case: dict) -> list[str]:
     field = case.get("field") or [0, 0, 0]
     if any(field):
         opts += ["--field"] + [repr(float(f)) for f in field]
+    if case.get("track_order"):
+        opts += ["--track-order", str(int(case["track_order"]))]
     return opts
 
 

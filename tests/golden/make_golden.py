@@ -43,6 +43,14 @@ CASES = {
                                     msc=True, field=[1.0, 0.0, 0.0]),
     "calo_msc_field_ep2000_n2": dict(pdg=-11, energy=2000.0, num=2, slots=8192, seed=5,
                                      msc=True, field=[1.0, 0.0, 0.0]),
+    # Action-sorted track orders (TrackOrder 5, 6, 7)
+    "calo_sorted_both_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=65536, seed=0,
+                                      track_order=7),
+    "calo_sorted_post_g100_n16": dict(pdg=22, energy=100.0, num=16, slots=4096, seed=7,
+                                      track_order=6),
+    "calo_msc_field_sorted_along_e2000_n2": dict(pdg=11, energy=2000.0, num=2, slots=65536,
+                                                 seed=3, msc=True, field=[1.0, 0.0, 0.0],
+                                                 track_order=5),
 }
 
 
@@ -54,6 +62,8 @@ def case_options(c: dict) -> list[str]:
     field = c.get("field")
     if field and any(field):
         opts += ["--field"] + [repr(float(f)) for f in field]
+    if c.get("track_order"):
+        opts += ["--track-order", str(int(c["track_order"]))]
     return opts
 
 
@@ -69,7 +79,8 @@ def make_case(name: str) -> dict:
         "case": {"geometry": "calo", "pdg": c["pdg"], "energy": c["energy"],
                  "num_primaries": c["num"], "num_track_slots": c["slots"],
                  "seed": c["seed"], "z0": -5.0, "msc": bool(c.get("msc", False)),
-                 "field": list(c.get("field", [0.0, 0.0, 0.0]))},
+                 "field": list(c.get("field", [0.0, 0.0, 0.0])),
+                 "track_order": int(c.get("track_order", 0))},
         "actions": [out["actions"][i] for i in sorted(out["actions"])],
         "steps": out["steps"],
         "total_steps": out["total_steps"],

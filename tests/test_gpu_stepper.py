@@ -40,10 +40,11 @@ _PARAMS = {}
 
 def params_for(gb, case):
     """Params with the case's field and MSC options (cached per options)."""
-    key = (tuple(case.get("field", [0, 0, 0])), bool(case.get("msc")))
+    key = (tuple(case.get("field", [0, 0, 0])), bool(case.get("msc")),
+           int(case.get("track_order", 0)))
     if key not in _PARAMS:
         _PARAMS[key] = gb.Params(gb.physics_file("calo"), "calo",
-                                 field_tesla=key[0], msc=key[1])
+                                 field_tesla=key[0], msc=key[1], track_order=key[2])
     return _PARAMS[key]
 
 
