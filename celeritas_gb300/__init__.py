@@ -67,6 +67,7 @@ class StepResult:
 
 
 _lib = None
+_libs: dict[str, ctypes.CDLL] = {}
 
 # (name, restype, argtypes) for every entry point of include/celeritas_gb300.h
 _PROTOTYPES = [
@@ -121,12 +122,17 @@ TRACK_ORDERS = {"none": 0, "reindex_along_step_action": 5,
 STATIC_SCRATCH_MAX_SLOTS = 131072
 
 
-def load_library(path: str | None = None) -> ctypes.CDLL:
-    """Load the in-tree CUDA library; raise if it has not been built."""
+def load_library(path: str | None = None, precision: str = "double") -> ctypes.CDLL:
+    """Load an in-tree CUDA library; raise if it has not been built.
+
+    ``precision`` is "double" (FP64 throughout, bit-exact with the
+    reference's FP64 build) or "mixed" (FP32 physics, FP64 positions,
+    geometry, field integration, time and tally).
+    """
     global _lib
-    if _lib is not None:
-        return _lib
-    path = path or lib_path()
+    if precision in _libs:
+        return _libs[precision]
+    path = path or lib_path(precision)
     if not os.path.exists(path):
         raise GbxError(
             f"GB300 library not built ({path}); run "
@@ -136,13 +142,15 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = restype
         fn.argtypes = argtypes
-    _lib = lib
+    _libs[precision] = lib
+    if precision == "double":
+        _lib = lib
     return lib
 
 
-def _check(rc: int):
+def _check(lib: ctypes.CDLL, rc: int):
     if rc != 0:
-        msg = _lib.gbx_last_error().decode()
+        msg = lib.gbx_last_error().decode()
         raise GbxError(msg or f"GB300 call failed with status {rc}")
 
 
@@ -156,8 +164,10 @@ class Params:
 
     def __init__(self, physics: str, geometry: str = "calo",
                  field_tesla=(0.0, 0.0, 0.0), msc: bool = False,
-                 track_order: int | str = "none"):
-        lib = load_library()
+                 track_order: int | str = "none", precision: str = "double"):
+        lib = load_library(precision=precision)
+        self._lib = lib
+        self.precision = precision
         handle = ctypes.c_void_p()
         opts = _ParamsOptions()
         for i in range(3):
@@ -166,7 +176,7 @@ class Params:
         if isinstance(track_order, str):
             track_order = TRACK_ORDERS[track_order]
         opts.track_order = int(track_order)
-        _check(lib.gbx_params_create(physics.encode(), geometry.encode(),
+        _check(lib, lib.gbx_params_create(physics.encode(), geometry.encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle
         self.geometry = geometry
@@ -175,8 +185,8 @@ class Params:
         self.track_order = int(track_order)
 
     def __del__(self):
-        if getattr(self, "_handle", None) and _lib is not None:
-            _lib.gbx_params_destroy(self._handle)
+        if getattr(self, "_handle", None):
+            self._lib.gbx_params_destroy(self._handle)
             self._handle = None
 
     @property
@@ -185,21 +195,21 @@ class Params:
 
     def action_labels(self) -> list[str]:
         n = ctypes.c_uint()
-        _check(_lib.gbx_params_num_actions(self._handle, ctypes.byref(n)))
+        _check(self._lib, self._lib.gbx_params_num_actions(self._handle, ctypes.byref(n)))
         out = []
         buf = ctypes.create_string_buffer(128)
         for i in range(n.value):
-            _check(_lib.gbx_params_action_label(self._handle, i, buf, 128))
+            _check(self._lib, self._lib.gbx_params_action_label(self._handle, i, buf, 128))
             out.append(buf.value.decode())
         return out
 
     def detector_labels(self) -> list[str]:
         n = ctypes.c_uint()
-        _check(_lib.gbx_params_num_detectors(self._handle, ctypes.byref(n)))
+        _check(self._lib, self._lib.gbx_params_num_detectors(self._handle, ctypes.byref(n)))
         out = []
         buf = ctypes.create_string_buffer(128)
         for i in range(n.value):
-            _check(_lib.gbx_params_detector_label(self._handle, i, buf, 128))
+            _check(self._lib, self._lib.gbx_params_detector_label(self._handle, i, buf, 128))
             out.append(buf.value.decode())
         return out
 
@@ -226,15 +236,16 @@ class Stepper:
     def __init__(self, params: Params, num_track_slots: int, seed: int = 0,
                  use_graph: bool = True):
         self.params = params
+        self._lib = params._lib
         handle = ctypes.c_void_p()
-        _check(_lib.gbx_stepper_create(params.handle, num_track_slots, seed,
+        _check(self._lib, self._lib.gbx_stepper_create(params.handle, num_track_slots, seed,
                                        int(use_graph), ctypes.byref(handle)))
         self._handle = handle
         self.num_track_slots = num_track_slots
 
     def __del__(self):
-        if getattr(self, "_handle", None) and _lib is not None:
-            _lib.gbx_stepper_destroy(self._handle)
+        if getattr(self, "_handle", None):
+            self._lib.gbx_stepper_destroy(self._handle)
             self._handle = None
 
     @staticmethod
@@ -245,9 +256,9 @@ class Stepper:
         res = _StepResult()
         if primaries is not None and len(primaries):
             arr, n = make_primary_array(primaries)
-            _check(_lib.gbx_stepper_step(self._handle, arr, n, ctypes.byref(res)))
+            _check(self._lib, self._lib.gbx_stepper_step(self._handle, arr, n, ctypes.byref(res)))
         else:
-            _check(_lib.gbx_stepper_step(self._handle, None, 0, ctypes.byref(res)))
+            _check(self._lib, self._lib.gbx_stepper_step(self._handle, None, 0, ctypes.byref(res)))
         return self._result(res)
 
     def run(self, max_steps: int = 1_000_000, batch: int = 32) -> list[StepResult]:
@@ -255,21 +266,21 @@ class Stepper:
         cap = max_steps
         out = (_StepResult * cap)()
         n = ctypes.c_uint()
-        _check(_lib.gbx_stepper_run(self._handle, max_steps, batch, out, cap, ctypes.byref(n)))
+        _check(self._lib, self._lib.gbx_stepper_run(self._handle, max_steps, batch, out, cap, ctypes.byref(n)))
         return [self._result(out[i]) for i in range(min(n.value, cap))]
 
     def insert_primaries(self, primaries: np.ndarray):
         arr, n = make_primary_array(primaries)
-        _check(_lib.gbx_stepper_insert_primaries(self._handle, arr, n))
+        _check(self._lib, self._lib.gbx_stepper_insert_primaries(self._handle, arr, n))
 
     def launch_action(self, action_id: int):
-        _check(_lib.gbx_stepper_launch_action(self._handle, action_id))
+        _check(self._lib, self._lib.gbx_stepper_launch_action(self._handle, action_id))
 
     def synchronize(self):
-        _check(_lib.gbx_stepper_synchronize(self._handle))
+        _check(self._lib, self._lib.gbx_stepper_synchronize(self._handle))
 
     def kill_active(self):
-        _check(_lib.gbx_stepper_kill_active(self._handle))
+        _check(self._lib, self._lib.gbx_stepper_kill_active(self._handle))
 
     def extend_from_secondaries_static(self):
         """Extend-from-secondaries with the library's static scratch array.
@@ -278,29 +289,29 @@ class Stepper:
         STATIC_SCRATCH_MAX_SLOTS track slots. Calls that overlap on the GPU
         share the array and race.
         """
-        _check(_lib.gbx_stepper_extend_from_secondaries_static(self._handle))
+        _check(self._lib, self._lib.gbx_stepper_extend_from_secondaries_static(self._handle))
 
     def stream_handle(self) -> int:
         """cudaStream_t of the stepper, as an integer (for event timing)."""
         s = ctypes.c_void_p()
-        _check(_lib.gbx_stepper_stream(self._handle, ctypes.byref(s)))
+        _check(self._lib, self._lib.gbx_stepper_stream(self._handle, ctypes.byref(s)))
         return s.value or 0
 
     def step_kernels(self) -> int:
         """Kernel launches in one graph-replayed step."""
         n = ctypes.c_uint()
-        _check(_lib.gbx_stepper_step_kernels(self._handle, ctypes.byref(n)))
+        _check(self._lib, self._lib.gbx_stepper_step_kernels(self._handle, ctypes.byref(n)))
         return n.value
 
     def set_action_times(self, enable: bool = True):
-        _check(_lib.gbx_stepper_set_action_times(self._handle, int(enable)))
+        _check(self._lib, self._lib.gbx_stepper_set_action_times(self._handle, int(enable)))
 
     def action_times(self) -> tuple[np.ndarray, np.ndarray]:
         """Accumulated device ms and launch counts per action ID (then reset)."""
         n = len(self.params.action_labels())
         ms = np.zeros(n, dtype=np.float64)
         nl = np.zeros(n, dtype=np.uint32)
-        _check(_lib.gbx_stepper_action_times(
+        _check(self._lib, self._lib.gbx_stepper_action_times(
             self._handle, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
             nl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), n))
         return ms, nl
@@ -308,28 +319,28 @@ class Stepper:
     def energy_deposition(self) -> np.ndarray:
         n = len(self.params.detector_labels())
         out = np.zeros(n, dtype=np.float64)
-        _check(_lib.gbx_stepper_energy_deposition(
+        _check(self._lib, self._lib.gbx_stepper_energy_deposition(
             self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n))
         return out
 
     def clear_energy_deposition(self):
-        _check(_lib.gbx_stepper_clear_energy_deposition(self._handle))
+        _check(self._lib, self._lib.gbx_stepper_clear_energy_deposition(self._handle))
 
     def state_info(self, field: str) -> tuple[int, int]:
         eb = ctypes.c_size_t()
         cnt = ctypes.c_size_t()
-        _check(_lib.gbx_stepper_state_info(self._handle, field.encode(),
+        _check(self._lib, self._lib.gbx_stepper_state_info(self._handle, field.encode(),
                                            ctypes.byref(eb), ctypes.byref(cnt)))
         return eb.value, cnt.value
 
     def get_state(self, field: str, dtype) -> np.ndarray:
         eb, cnt = self.state_info(field)
         out = np.empty(eb * cnt, dtype=np.uint8)
-        _check(_lib.gbx_stepper_copy_state(self._handle, field.encode(),
+        _check(self._lib, self._lib.gbx_stepper_copy_state(self._handle, field.encode(),
                                            out.ctypes.data_as(ctypes.c_void_p), out.nbytes, 0))
         return out.view(dtype)
 
     def set_state(self, field: str, data: np.ndarray):
         data = np.ascontiguousarray(data)
-        _check(_lib.gbx_stepper_copy_state(self._handle, field.encode(),
+        _check(self._lib, self._lib.gbx_stepper_copy_state(self._handle, field.encode(),
                                            data.ctypes.data_as(ctypes.c_void_p), data.nbytes, 1))

@@ -7,6 +7,12 @@ arch=compute_103a,code=sm_103a`` is generated: the library targets GB300.
 The FP64 build compiles device code with ``-fmad=false`` so that no multiply
 and add are contracted into an fma that the reference's expressions do not
 spell out; explicit fma calls (interpolation, axpy, dot products) remain.
+
+The mixed-precision build (``libceleritas_gb300_mixed.so``) compiles the
+same sources with ``-DGBX_PHYS_REAL=float``: energies, cross sections, step
+limits, multiple scattering, energy loss and the interactors compute in FP32,
+while positions, directions, geometry distances, time, the field integrator
+and the energy-deposition tally stay FP64. It may contract multiply-adds.
 """
 
 from __future__ import annotations
@@ -18,7 +24,8 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
-LIB_NAME = "libceleritas_gb300.so"
+LIB_NAMES = {"double": "libceleritas_gb300.so", "mixed": "libceleritas_gb300_mixed.so"}
+PRECISIONS = tuple(LIB_NAMES)
 
 SOURCES = [
     "csrc/device/Kernels.cu",
@@ -37,22 +44,26 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def common_flags() -> list[str]:
-    return ARCH_FLAGS + [
+def common_flags(precision: str = "double") -> list[str]:
+    flags = ARCH_FLAGS + [
         "-O3",
         "-lineinfo",
         "-std=c++17",
         "-Xcompiler",
         "-fPIC",
-        "-fmad=false",
         "--expt-relaxed-constexpr",
         "-Xptxas",
         "-v" if os.environ.get("GBX_PTXAS_VERBOSE") else "-O3",
     ]
+    if precision == "double":
+        flags.append("-fmad=false")
+    else:
+        flags += ["-fmad=true", "-DGBX_PHYS_REAL=float"]
+    return flags
 
 
-def lib_path() -> str:
-    return os.path.join(BUILD_DIR, LIB_NAME)
+def lib_path(precision: str = "double") -> str:
+    return os.path.join(BUILD_DIR, LIB_NAMES[precision])
 
 
 def _newest_mtime(paths):
@@ -70,17 +81,18 @@ def _deps():
     return deps
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile and link the library if any source changed; return its path."""
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    out = lib_path()
+def build(force: bool = False, verbose: bool = False, precision: str = "double") -> str:
+    """Compile and link one library if any source changed; return its path."""
+    obj_dir = os.path.join(BUILD_DIR, precision)
+    os.makedirs(obj_dir, exist_ok=True)
+    out = lib_path(precision)
     if not force and os.path.exists(out) and os.path.getmtime(out) >= _newest_mtime(_deps()):
         return out
     nvcc = nvcc_path()
-    flags = common_flags()
+    flags = common_flags(precision)
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         cmd = [nvcc] + flags + ["-x", "cu", "-c", os.path.join(HERE, src), "-o", obj]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
@@ -100,5 +112,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return out
 
 
+def build_all(force: bool = False) -> dict[str, str]:
+    """Build the FP64 and the mixed-precision libraries concurrently."""
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(PRECISIONS)) as pool:
+        futs = {p: pool.submit(build, force, False, p) for p in PRECISIONS}
+        return {p: f.result() for p, f in futs.items()}
+
+
 if __name__ == "__main__":
-    print(build(force=True, verbose=True))
+    print(build_all(force=True))

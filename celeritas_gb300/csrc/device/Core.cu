@@ -310,13 +310,13 @@ CoreParams::CoreParams(Input const& inp)
         device_storage_, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
     auto* base = static_cast<unsigned char*>(device_storage_);
     device_ = h.scalars;
-    device_.reals = reinterpret_cast<double const*>(base + o_reals);
+    device_.reals = reinterpret_cast<real_type const*>(base + o_reals);
     device_.ints = reinterpret_cast<size_type const*>(base + o_ints);
     device_.particles = reinterpret_cast<ParticleRecord const*>(base + o_part);
     device_.elements = reinterpret_cast<ElementRecord const*>(base + o_el);
     device_.materials = reinterpret_cast<MaterialRecord const*>(base + o_mat);
     device_.fluct = reinterpret_cast<UrbanFluctRecord const*>(base + o_fl);
-    device_.cutoff_energy = reinterpret_cast<double const*>(base + o_cut);
+    device_.cutoff_energy = reinterpret_cast<real_type const*>(base + o_cut);
     device_.process_groups = reinterpret_cast<ProcessGroup const*>(base + o_grp);
     device_.grids = reinterpret_cast<XsGrid const*>(base + o_grid);
     device_.livermore_elements

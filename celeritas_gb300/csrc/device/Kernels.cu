@@ -555,12 +555,21 @@ __device__ __forceinline__ bool sorted_slot(StateData const& s,
     return true;
 }
 
-__global__ __launch_bounds__(block_size) void along_step_sorted_kernel(
+// Minimum resident blocks per SM requested for the charged along-step kernel
+// (1: the compiler may use up to 255 registers per thread)
+#ifndef GBX_ALONG_MIN_BLOCKS
+#    define GBX_ALONG_MIN_BLOCKS 1
+#endif
+
+template<AlongKind K>
+__global__ __launch_bounds__(block_size,
+                             K == AlongKind::charged ? GBX_ALONG_MIN_BLOCKS : 1) void
+along_step_sorted_kernel(
     ParamsData p, StateData s, size_type first_bin, size_type end_bin)
 {
     size_type slot;
     if (sorted_slot(s, first_bin, end_bin, &slot))
-        along_step(p, s, slot);
+        along_step_impl<K>(p, s, slot);
 }
 
 __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
@@ -627,16 +636,19 @@ void launch_along_step(LaunchContext const& ctx,
     ParamsData const& p = ctx.params;
     if (sorts_along_step(p.track_order))
     {
-        // Launch over the action's sorted range (all along-step bins if
-        // invalid); the grid covers the largest possible range
-        size_type first = action, end = action + 1;
-        if (action == invalid_id)
+        // Launch each along-step action over its sorted range with a kernel
+        // compiled for that action only; the grid covers the largest range
+        unsigned int const nb = num_blocks_for(ctx.state.size);
+        if (action == invalid_id || action == p.action_along_step)
         {
-            first = min_of(p.action_along_step, p.action_along_step_neutral);
-            end = max_of(p.action_along_step, p.action_along_step_neutral) + 1;
+            along_step_sorted_kernel<AlongKind::charged><<<nb, block_size, 0, stream>>>(
+                p, ctx.state, p.action_along_step, p.action_along_step + 1);
         }
-        along_step_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p, ctx.state, first, end);
+        if (action == invalid_id || action == p.action_along_step_neutral)
+        {
+            along_step_sorted_kernel<AlongKind::neutral><<<nb, block_size, 0, stream>>>(
+                p, ctx.state, p.action_along_step_neutral, p.action_along_step_neutral + 1);
+        }
         return;
     }
     along_step_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(

@@ -96,7 +96,7 @@ GBX_FUNCTION void pre_step(ParamsData const& p, StateData const& s, size_type sl
     }
     s.macro_xs[slot] = total_macro_xs;
 
-    double step;
+    real_type step;
     size_type action = p.action_discrete;
     if (energy == 0)
     {
@@ -218,14 +218,34 @@ GBX_FUNCTION real_type calc_eloss(ParamsData const& p,
     return eloss;
 }
 
-GBX_FUNCTION void along_step(ParamsData const& p, StateData const& s, size_type slot)
+//! Which along-step actions a compiled along-step function handles: both
+//! (selected per slot), or only one, so that the neutral instance carries
+//! none of the charged-particle code and its registers
+enum class AlongKind
+{
+    any,
+    charged,
+    neutral,
+};
+
+template<AlongKind K>
+GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_type slot)
 {
     size_type const along = s.along_step_action[slot];
     if (!is_track_valid(s.status[slot]))
         return;
-    if (along != p.action_along_step && along != p.action_along_step_neutral)
+    if (K != AlongKind::neutral && along == p.action_along_step)
+    {
+    }
+    else if (K != AlongKind::charged && along == p.action_along_step_neutral)
+    {
+    }
+    else
+    {
         return;
-    bool const charged = (along == p.action_along_step);
+    }
+    bool const charged = (K == AlongKind::charged)
+                         || (K == AlongKind::any && along == p.action_along_step);
 
     // MscStepLimitApplier
     if (charged && p.msc.enabled)
@@ -316,7 +336,8 @@ GBX_FUNCTION void along_step(ParamsData const& p, StateData const& s, size_type 
             = std::sqrt(beta_sq(mass, s.energy[slot])) * real_type(constants::c_light);
         if (speed > 0)
         {
-            s.time[slot] += s.step_length[slot] / speed;
+            // Time accumulates in FP64; the increment is a physics quantity
+            s.time[slot] += double(real_type(s.step_length[slot]) / speed);
         }
     }
 
@@ -361,6 +382,11 @@ GBX_FUNCTION void along_step(ParamsData const& p, StateData const& s, size_type 
         }
     }
     ++s.num_steps[slot];
+}
+
+GBX_FORCEINLINE void along_step(ParamsData const& p, StateData const& s, size_type slot)
+{
+    along_step_impl<AlongKind::any>(p, s, slot);
 }
 
 //---------------------------------------------------------------------------//
@@ -434,7 +460,27 @@ GBX_FUNCTION void apply_interaction(ParamsData const& p,
     }
     if (result.action == Interaction::unchanged)
         return;
-    s.energy[slot] = result.energy;
+    // In FP32 the difference of two energies can round to just below zero
+    // (FP64 never reaches this branch on the reference's inputs): such a
+    // particle is at rest, and one without an at-rest process ends here
+    real_type energy = result.energy;
+    if (energy < 0)
+    {
+        energy = 0;
+        if (!p.process_groups[s.particle_id[slot]].has_at_rest)
+            s.status[slot] = status_killed;
+    }
+    for (size_type i = 0; i < result.num_secondaries; ++i)
+    {
+        Secondary& sec = result.secondaries[i];
+        if (sec.energy < 0 && sec.particle_id != invalid_id)
+        {
+            sec.energy = 0;
+            if (!p.process_groups[sec.particle_id].has_at_rest)
+                sec.particle_id = invalid_id;
+        }
+    }
+    s.energy[slot] = energy;
     if (result.action != Interaction::absorbed)
     {
         GeoTrackView geo(p.geo, s, slot);

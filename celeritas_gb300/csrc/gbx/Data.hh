@@ -80,9 +80,9 @@ constexpr int max_elements = 4;  //!< Max element components per material
 //! Log-uniform energy grid with values; grid energies precomputed on host
 struct XsGrid
 {
-    double log_front;  //!< log(E_min)
-    double log_back;  //!< log(E_max)
-    double log_delta;  //!< (log_back - log_front) / (size - 1)
+    real_type log_front;  //!< log(E_min)
+    real_type log_back;  //!< log(E_max)
+    real_type log_delta;  //!< (log_back - log_front) / (size - 1)
     size_type size;
     size_type value;  //!< Offset of values in reals
     size_type energy;  //!< Offset of exp(log_front + i * log_delta) in reals,
@@ -100,8 +100,8 @@ struct GenericGrid
 
 struct ParticleRecord
 {
-    double mass;  //!< [MeV]
-    double charge;  //!< [e]
+    real_type mass;  //!< [MeV]
+    real_type charge;  //!< [e]
     int pdg;
     bool is_antiparticle;
 };
@@ -109,34 +109,34 @@ struct ParticleRecord
 struct ElementRecord
 {
     int z;
-    double atomic_mass;  //!< [amu]
-    double cbrt_z;
-    double cbrt_zzp;
-    double log_z;
-    double coulomb_correction;
-    double mass_radiation_coeff;
+    real_type atomic_mass;  //!< [amu]
+    real_type cbrt_z;
+    real_type cbrt_zzp;
+    real_type log_z;
+    real_type coulomb_correction;
+    real_type mass_radiation_coeff;
 };
 
 struct MaterialRecord
 {
-    double number_density;
-    double electron_density;
-    double zeff;
-    double density;
-    double rad_length;
-    double log_mean_exc_energy;
-    double mean_exc_energy;
+    real_type number_density;
+    real_type electron_density;
+    real_type zeff;
+    real_type density;
+    real_type rad_length;
+    real_type log_mean_exc_energy;
+    real_type mean_exc_energy;
     size_type num_elements;
     size_type element[max_elements];
-    double fraction[max_elements];
+    real_type fraction[max_elements];
 };
 
 //! Urban fluctuation parameters per material
 struct UrbanFluctRecord
 {
-    double binding_energy[2];
-    double log_binding_energy[2];
-    double oscillator_strength[2];
+    real_type binding_energy[2];
+    real_type log_binding_energy[2];
+    real_type oscillator_strength[2];
 };
 
 //! Per-particle physics process group
@@ -162,26 +162,26 @@ struct LivermoreElement
 {
     GenericGrid xs_lo;  //!< size 0 if absent
     GenericGrid xs_hi;
-    double thresh_lo;
-    double thresh_hi;
+    real_type thresh_lo;
+    real_type thresh_hi;
     size_type shells;  //!< Offset of first shell
     size_type num_shells;
 };
 struct LivermoreShell
 {
-    double binding_energy;
-    double param[2][6];
+    real_type binding_energy;
+    real_type param[2][6];
     GenericGrid xs;
 };
 
 //! Relativistic bremsstrahlung per-element factors
 struct RelBremElementRecord
 {
-    double fz;  //!< log(Z)/3 + Coulomb correction
-    double factor1;  //!< (F_el - f_c) + F_inel / Z
-    double factor2;  //!< (1 + 1/Z) / 12
-    double gamma_factor;  //!< 100 m_e / Z^(1/3)
-    double epsilon_factor;  //!< 100 m_e / Z^(2/3)
+    real_type fz;  //!< log(Z)/3 + Coulomb correction
+    real_type factor1;  //!< (F_el - f_c) + F_inel / Z
+    real_type factor2;  //!< (1 + 1/Z) / 12
+    real_type gamma_factor;  //!< 100 m_e / Z^(1/3)
+    real_type epsilon_factor;  //!< 100 m_e / Z^(2/3)
 };
 
 //! Seltzer-Berger scaled DCS per element
@@ -198,28 +198,28 @@ struct SBElementTable
 //! Urban multiple scattering per-material coefficients
 struct UrbanMscMaterialRecord
 {
-    double stepmin_coeff[2];
-    double theta_coeff[2];
-    double tail_coeff[3];
-    double tail_corr;
+    real_type stepmin_coeff[2];
+    real_type theta_coeff[2];
+    real_type tail_coeff[3];
+    real_type tail_corr;
 };
 
 //! Urban multiple scattering per-(material, e-/e+) data
 struct UrbanMscParMatRecord
 {
-    double scaled_zeff;
-    double d_over_r;
+    real_type scaled_zeff;
+    real_type d_over_r;
 };
 
 //! Urban multiple scattering parameters
 struct UrbanMscParams
 {
     bool enabled;
-    double low_energy_limit;
-    double high_energy_limit;
-    double lambda_limit;  //!< PhysicsParamsOptions::lambda_limit
-    double range_factor;
-    double safety_factor;
+    real_type low_energy_limit;
+    real_type high_energy_limit;
+    real_type lambda_limit;  //!< PhysicsParamsOptions::lambda_limit
+    real_type range_factor;
+    real_type safety_factor;
     UrbanMscMaterialRecord const* material;  //!< [material]
     UrbanMscParMatRecord const* par_mat;  //!< [material * 2 + (e+ ? 1 : 0)]
     size_type xs_grids;  //!< Offset in ints: grid index per (material, e-/e+)
@@ -230,7 +230,7 @@ struct LoopingRecord
 {
     size_type max_subthreshold_steps;
     size_type max_steps;
-    double threshold_energy;
+    real_type threshold_energy;
 };
 
 //---------------------------------------------------------------------------//
@@ -278,8 +278,8 @@ struct GeoParams
 //---------------------------------------------------------------------------//
 struct ParamsData
 {
-    // Storage
-    double const* reals;
+    // Storage: physics tables (FP32 in the mixed-precision build)
+    real_type const* reals;
     size_type const* ints;
 
     // Particles: 0 = e-, 1 = e+, 2 = gamma (same order as the input file)
@@ -294,7 +294,7 @@ struct ParamsData
     MaterialRecord const* materials;
     ElementRecord const* elements;
     UrbanFluctRecord const* fluct;
-    double const* cutoff_energy;  //!< [material * num_particles + particle]
+    real_type const* cutoff_energy;  //!< [material * num_particles + particle]
 
     // Physics
     ProcessGroup const* process_groups;  //!< [particle]
@@ -302,17 +302,17 @@ struct ParamsData
     size_type num_models;
     size_type model_to_action;  //!< Action ID of model 0
     // Scalars (src/celeritas/phys/PhysicsData.hh PhysicsParamsScalars)
-    double min_range;
-    double max_step_over_range;
-    double min_eprime_over_e;
-    double lowest_electron_energy;
-    double linear_loss_limit;
+    real_type min_range;
+    real_type max_step_over_range;
+    real_type min_eprime_over_e;
+    real_type lowest_electron_energy;
+    real_type linear_loss_limit;
     double secondary_stack_factor;
     bool enable_fluct;
     // Hardwired processes
     size_type photoelectric_process;
     size_type annihilation_process;
-    double photoelectric_table_thresh;
+    real_type photoelectric_table_thresh;
     size_type livermore_model;
     size_type eplusgg_model;
 

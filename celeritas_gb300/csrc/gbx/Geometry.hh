@@ -341,44 +341,33 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
     }
     else
     {
-        // Implicit background: crossings by increasing distance; accept the
-        // first whose bumped point lies inside a neighboring volume
+        // Implicit background: the reference visits crossings by increasing
+        // (distance, surface ID) and accepts the first whose bumped point lies
+        // inside a neighboring volume. Acceptance depends on that crossing
+        // alone, so the first accepted crossing is the (distance, surface)
+        // minimum over accepted crossings: one pass over the surfaces, testing
+        // only candidates that would improve the current best, gives the same
+        // hit with one distance per surface instead of one scan per crossing.
         double bump = p_.tol_abs;
         for (int i = 0; i < 3; ++i)
         {
             bump = max_of(bump, p_.tol_rel * std::fabs(pos[i]));
         }
-        double prev = -INFINITY;
-        size_type prev_surf = invalid_id;
-        for (size_type iter = 0; iter < p_.num_surfaces; ++iter)
+        for (size_type surf = 0; surf < p_.num_surfaces; ++surf)
         {
-            // Next candidate: smallest (distance, surface) after prev
-            double best = INFINITY;
-            size_type best_surf = invalid_id;
-            for (size_type s = 0; s < p_.num_surfaces; ++s)
+            double const d = calc_dist(surf);
+            if (!(d <= max_step))
+                continue;
+            if (hit_surf != invalid_id
+                && !(d < hit_dist || (d == hit_dist && surf < hit_surf)))
             {
-                double d = calc_dist(s);
-                if (!(d <= max_step))
-                    continue;
-                bool after = d > prev || (d == prev && s > prev_surf);
-                if (!after)
-                    continue;
-                if (d < best || (d == best && s < best_surf))
-                {
-                    best = d;
-                    best_surf = s;
-                }
+                continue;
             }
-            if (best_surf == invalid_id)
-                break;
-            prev = best;
-            prev_surf = best_surf;
-
             Real3 bumped = pos;
-            axpy(best + bump, dir, &bumped);
+            axpy(d + bump, dir, &bumped);
             // Neighbors of this surface
-            size_type nbeg = p_.neighbor_offset[best_surf];
-            size_type nend = p_.neighbor_offset[best_surf + 1];
+            size_type nbeg = p_.neighbor_offset[surf];
+            size_type nend = p_.neighbor_offset[surf + 1];
             bool found = false;
             bool found_outside = false;
             if (nend - nbeg >= 3)
@@ -391,8 +380,7 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
                     found = true;
                     // Sense of the crossed surface evaluated at the bumped
                     // point inside the new volume, flipped
-                    found_outside
-                        = !sense_outside(this->plane_q(best_surf, bumped));
+                    found_outside = !sense_outside(this->plane_q(surf, bumped));
                 }
             }
             else
@@ -403,18 +391,16 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
                     if (this->volume_inside(v, bumped, invalid_id, false, nullptr))
                     {
                         found = true;
-                        found_outside
-                            = !sense_outside(this->plane_q(best_surf, bumped));
+                        found_outside = !sense_outside(this->plane_q(surf, bumped));
                         break;
                     }
                 }
             }
             if (found)
             {
-                hit_surf = best_surf;
-                hit_dist = best;
+                hit_surf = surf;
+                hit_dist = d;
                 hit_sense = found_outside ? 1 : -1;
-                break;
             }
         }
     }

@@ -396,7 +396,7 @@ struct SBXsCalc
 
     GBX_FORCEINLINE real_type operator()(real_type y) const
     {
-        double const* ygrid = p.reals + t.y;
+        real_type const* ygrid = p.reals + t.y;
         size_type iy = find_nonuniform(ygrid, t.ny, y);
         real_type const lower = ygrid[iy];
         real_type const upper = ygrid[iy + 1];
@@ -434,7 +434,7 @@ GBX_FUNCTION Interaction interact_seltzer_berger(ParamsData const& p,
 
     // Table position in log energy
     SBElementTable const& t = p.sb_tables[element_id];
-    double const* xgrid = p.reals + t.x;
+    real_type const* xgrid = p.reals + t.x;
     real_type const loge = std::log(inc_energy);
     size_type ix = find_nonuniform(xgrid, t.nx, loge);
     real_type const xf = (loge - real_type(xgrid[ix]))

@@ -191,7 +191,7 @@ GBX_FORCEINLINE real_type msc_displacement(real_type geom_path, real_type true_p
 GBX_FORCEINLINE bool msc_is_applicable(ParamsData const& p,
                                        StateData const& s,
                                        size_type slot,
-                                       double step)
+                                       real_type step)
 {
     if (!p.msc.enabled)
         return false;

@@ -30,9 +30,8 @@ GBX_FORCEINLINE T interp_linear(T x0, T y0, T x1, T y1, T x)
 
 //! Index of the largest grid value <= v (lower_bound, then step back unless
 //! exact); clamped so that index + 1 is valid.
-GBX_FORCEINLINE size_type find_nonuniform(double const* grid,
-                                          size_type size,
-                                          double v)
+template<class T>
+GBX_FORCEINLINE size_type find_nonuniform(T const* grid, size_type size, T v)
 {
     size_type lo = 0, count = size;
     while (count > 0)
@@ -61,9 +60,9 @@ GBX_FORCEINLINE real_type calc_grid_xs(ParamsData const& p,
                                        XsGrid const& g,
                                        real_type energy)
 {
-    double const* values = p.reals + g.value;
-    double const* energies = p.reals + g.energy;
-    double const loge = std::log(static_cast<double>(energy));
+    real_type const* values = p.reals + g.value;
+    real_type const* energies = p.reals + g.energy;
+    real_type const loge = std::log(energy);
     auto extrapolated = [&](size_type idx) {
         real_type result = values[idx];
         if (idx >= g.prime_index)
@@ -92,9 +91,9 @@ GBX_FORCEINLINE real_type calc_range(ParamsData const& p,
                                      XsGrid const& g,
                                      real_type energy)
 {
-    double const* values = p.reals + g.value;
-    double const* energies = p.reals + g.energy;
-    double const loge = std::log(static_cast<double>(energy));
+    real_type const* values = p.reals + g.value;
+    real_type const* energies = p.reals + g.energy;
+    real_type const loge = std::log(energy);
     if (loge <= g.log_front)
     {
         real_type result = values[0];
@@ -114,8 +113,8 @@ GBX_FORCEINLINE real_type calc_inverse_range(ParamsData const& p,
                                              XsGrid const& g,
                                              real_type range)
 {
-    double const* values = p.reals + g.value;
-    double const* energies = p.reals + g.energy;
+    real_type const* values = p.reals + g.value;
+    real_type const* energies = p.reals + g.energy;
     if (range < values[0])
     {
         return energies[0] * ipow<2>(range / values[0]);
@@ -135,8 +134,8 @@ GBX_FORCEINLINE real_type calc_generic(ParamsData const& p,
                                        GenericGrid const& g,
                                        real_type x)
 {
-    double const* xs = p.reals + g.x;
-    double const* ys = p.reals + g.y;
+    real_type const* xs = p.reals + g.x;
+    real_type const* ys = p.reals + g.y;
     if (x <= xs[0])
         return ys[0];
     if (x >= xs[g.size - 1])
@@ -162,7 +161,7 @@ GBX_FORCEINLINE real_type livermore_pe_micro_xs(ParamsData const& p,
     real_type result = 0.;
     if (energy >= el.thresh_lo)
     {
-        double const* param
+        real_type const* param
             = shells[el.num_shells - 1].param[energy < el.thresh_hi ? 0 : 1];
         real_type c[6];
         for (int i = 0; i < 6; ++i)
@@ -256,7 +255,7 @@ class PhysicsTrack
     //! Model applicable at an energy for a process (GridIdFinder)
     GBX_FORCEINLINE size_type find_model(size_type ppid, real_type energy) const
     {
-        double const* grid = p_.reals + group_.model_energy[ppid];
+        real_type const* grid = p_.reals + group_.model_energy[ppid];
         size_type n = group_.num_models[ppid] + 1;
         // lower_bound
         size_type lo = 0, count = n;

@@ -51,13 +51,13 @@ struct ParamsOptions
 //! All parameter tables in host memory
 struct HostParams
 {
-    std::vector<double> reals;
+    std::vector<real_type> reals;  //!< Physics tables (FP32 in the mixed build)
     std::vector<size_type> ints;
     std::vector<ParticleRecord> particles;
     std::vector<ElementRecord> elements;
     std::vector<MaterialRecord> materials;
     std::vector<UrbanFluctRecord> fluct;
-    std::vector<double> cutoffs;
+    std::vector<real_type> cutoffs;
     std::vector<ProcessGroup> groups;
     std::vector<XsGrid> grids;
     std::vector<LivermoreElement> lv_elements;

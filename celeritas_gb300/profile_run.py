@@ -2,6 +2,7 @@
 
     python -m celeritas_gb300.profile_run --workload c2 [--primaries N]
         [--max-iterations K] [--steps-log FILE] [--graph]
+        [--precision double|mixed] [--track-order N]
 
 Inserts the workload's primaries, then steps (eagerly by default, so that
 every kernel is its own launch) until the state empties or K iterations have
@@ -27,12 +28,15 @@ def main(argv=None):
     ap.add_argument("--max-iterations", type=int, default=20000)
     ap.add_argument("--steps-log", default=None)
     ap.add_argument("--graph", action="store_true")
+    ap.add_argument("--precision", default="double", choices=["double", "mixed"])
+    ap.add_argument("--track-order", type=int, default=0)
     args = ap.parse_args(argv)
 
     wl = WORKLOADS[args.workload]
-    load_library()
+    load_library(precision=args.precision)
     params = Params(physics_file(wl["physics"]), wl["geometry"],
-                    field_tesla=wl["field"], msc=wl["msc"])
+                    field_tesla=wl["field"], msc=wl["msc"],
+                    track_order=args.track_order, precision=args.precision)
     stepper = Stepper(params, wl["slots"], seed=wl["seed"], use_graph=args.graph)
     prim = make_primaries(wl, num=args.primaries)
     res = [stepper.step(prim)]
