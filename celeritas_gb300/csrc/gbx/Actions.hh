@@ -123,6 +123,14 @@ GBX_FUNCTION void pre_step(ParamsData const& p, StateData const& s, size_type sl
             action = invalid_id;
         }
     }
+    if constexpr (sizeof(real_type) < sizeof(double))
+    {
+        // FP32: a near-vacuum gives physics steps of ~1e23 cm whose products
+        // overflow FP32 in the multiple-scattering and field-integration
+        // arithmetic; any step above 1e10 cm is limited by the geometry
+        // long before it ends, so the cap changes no step that is taken
+        step = min_of(step, real_type(1e10));
+    }
     s.step_length[slot] = step;
     s.post_step_action[slot] = action;
     s.along_step_action[slot] = (p.particles[pid].charge == 0)

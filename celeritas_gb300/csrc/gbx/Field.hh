@@ -5,8 +5,13 @@
 // Follows src/celeritas/field/FieldPropagator.hh:150-333,
 // FieldDriver.hh:182-429, DormandPrinceStepper.hh:102-222,
 // MagFieldEquation.hh, detail/FieldUtils.hh and the defaults of
-// FieldDriverOptions.hh:26-77. The integration runs in FP64 in every build
-// (positions, momenta and the error control).
+// FieldDriverOptions.hh:26-77.
+//
+// FP64 build: the whole integration is FP64, operation for operation as in
+// the reference. Mixed-precision build: the Runge-Kutta stages (field
+// evaluations and stage momenta) are FP32; the positions are accumulated in
+// FP64 from FP32 increments, and the error estimate, the acceptance test and
+// the chord test are FP64. Only the step-size scale factor err^(-1/5) is FP32.
 #pragma once
 
 #include "Geometry.hh"
@@ -85,9 +90,9 @@ struct FieldStepperResult
 };
 
 //! Dormand-Prince 5(4) step with Shampine's midpoint interpolation
-GBX_FUNCTION FieldStepperResult dormand_prince_step(UniformFieldEquation const& rhs,
-                                                    double step,
-                                                    OdeState const& beg_state)
+GBX_FUNCTION FieldStepperResult dormand_prince_step_fp64(UniformFieldEquation const& rhs,
+                                                         double step,
+                                                         OdeState const& beg_state)
 {
     using R = double;
     constexpr R a11 = 0.2;
@@ -173,6 +178,141 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step(UniformFieldEquation const& 
     axpy(c76 * half_step, k6, &result.mid_state);
     axpy(c77 * half_step, k7, &result.mid_state);
     return result;
+}
+
+
+//! Mixed-precision Dormand-Prince 5(4) step for a uniform field. The field
+//! equation depends on the momentum only, so the stages carry FP32 momenta
+//! and FP32 derivatives; positions are the FP64 start plus an FP32
+//! increment; the embedded error estimate is accumulated in FP64.
+GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation const& rhs,
+                                                          double step,
+                                                          OdeState const& beg_state)
+{
+    using F = float;
+    using F3 = Vec3<float>;
+    // Butcher tableau of the FP64 stepper, rounded to FP32
+    constexpr F a11 = 0.2f;
+    constexpr F a21 = 0.075f, a22 = 0.225f;
+    constexpr F a31 = F(44. / 45), a32 = F(-56. / 15), a33 = F(32. / 9);
+    constexpr F a41 = F(19372. / 6561), a42 = F(-25360. / 2187),
+                a43 = F(64448. / 6561), a44 = F(-212. / 729);
+    constexpr F a51 = F(9017. / 3168), a52 = F(-355. / 33), a53 = F(46732. / 5247),
+                a54 = F(49. / 176), a55 = F(-5103. / 18656);
+    constexpr double b1 = 35. / 384, b3 = 500. / 1113, b4 = 125. / 192,
+                     b5 = -2187. / 6784, b6 = 11. / 84;
+    constexpr double d1 = b1 - 5179. / 57600, d3 = b3 - 7571. / 16695,
+                     d4 = b4 - 393. / 640, d5 = b5 + 92097. / 339200,
+                     d6 = b6 - 187. / 2100, d7 = -1. / 40;
+    constexpr F c1 = F(6025192743. / 30085553152.), c3 = F(51252292925. / 65400821598.),
+                c4 = F(-2691868925. / 45128329728.),
+                c5 = F(187940372067. / 1594534317056.),
+                c6 = F(-1776094331. / 19743644256.), c7 = F(11237099. / 235043384.);
+
+    F3 const field{F(rhs.field.x), F(rhs.field.y), F(rhs.field.z)};
+    F const coeffi = F(rhs.coeffi);
+    // d(pos)/ds = p/|p|, d(mom)/ds = (q/|p|) p x B
+    auto eval = [&](F3 const& m, F3* kpos, F3* kmom) {
+        F const inv = F(1) / std::sqrt(m.x * m.x + m.y * m.y + m.z * m.z);
+        *kpos = {m.x * inv, m.y * inv, m.z * inv};
+        F const scale = coeffi * inv;
+        *kmom = {scale * (m.y * field.z - m.z * field.y),
+                 scale * (m.z * field.x - m.x * field.z),
+                 scale * (m.x * field.y - m.y * field.x)};
+    };
+    // Stage momentum m0 + h * sum_j a[j] k_mom[j]
+    auto stage = [](F3 const& m0, F h, F const* a, int n, F3 const* k) {
+        F3 r = m0;
+#pragma unroll
+        for (int j = 0; j < n; ++j)
+        {
+            r.x += h * a[j] * k[j].x;
+            r.y += h * a[j] * k[j].y;
+            r.z += h * a[j] * k[j].z;
+        }
+        return r;
+    };
+    F const A1[1] = {a11};
+    F const A2[2] = {a21, a22};
+    F const A3[3] = {a31, a32, a33};
+    F const A4[4] = {a41, a42, a43, a44};
+    F const A5[5] = {a51, a52, a53, a54, a55};
+
+    F const h = F(step);
+    F3 const m0{F(beg_state.mom.x), F(beg_state.mom.y), F(beg_state.mom.z)};
+    F3 kp[7], km[7];
+    eval(m0, &kp[0], &km[0]);
+    eval(stage(m0, h, A1, 1, km), &kp[1], &km[1]);
+    eval(stage(m0, h, A2, 2, km), &kp[2], &km[2]);
+    eval(stage(m0, h, A3, 3, km), &kp[3], &km[3]);
+    eval(stage(m0, h, A4, 4, km), &kp[4], &km[4]);
+    eval(stage(m0, h, A5, 5, km), &kp[5], &km[5]);
+    // Fifth-order solution: FP32 increments added to the FP64 start
+    F const bf[7] = {F(b1), 0, F(b3), F(b4), F(b5), F(b6), 0};
+    F3 dpos{0, 0, 0}, m_end = m0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+    {
+        dpos.x += bf[i] * kp[i].x;
+        dpos.y += bf[i] * kp[i].y;
+        dpos.z += bf[i] * kp[i].z;
+        m_end.x += h * bf[i] * km[i].x;
+        m_end.y += h * bf[i] * km[i].y;
+        m_end.z += h * bf[i] * km[i].z;
+    }
+    eval(m_end, &kp[6], &km[6]);
+
+    FieldStepperResult result;
+    result.end_state.pos = {beg_state.pos.x + double(h * dpos.x),
+                            beg_state.pos.y + double(h * dpos.y),
+                            beg_state.pos.z + double(h * dpos.z)};
+    result.end_state.mom = {double(m_end.x), double(m_end.y), double(m_end.z)};
+
+    // Embedded error estimate in FP64
+    double const dd[7] = {d1, 0, d3, d4, d5, d6, d7};
+    result.err_state = {{0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+    {
+        if (i == 1)
+            continue;
+        double const w = dd[i] * step;
+        axpy(w, Real3{double(kp[i].x), double(kp[i].y), double(kp[i].z)},
+             &result.err_state.pos);
+        axpy(w, Real3{double(km[i].x), double(km[i].y), double(km[i].z)},
+             &result.err_state.mom);
+    }
+
+    // Shampine midpoint for the chord test
+    F const cf[7] = {c1, 0, c3, c4, c5, c6, c7};
+    F3 mpos{0, 0, 0}, m_mid = m0;
+    F const half = F(0.5) * h;
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+    {
+        mpos.x += cf[i] * kp[i].x;
+        mpos.y += cf[i] * kp[i].y;
+        mpos.z += cf[i] * kp[i].z;
+        m_mid.x += half * cf[i] * km[i].x;
+        m_mid.y += half * cf[i] * km[i].y;
+        m_mid.z += half * cf[i] * km[i].z;
+    }
+    result.mid_state.pos = {beg_state.pos.x + double(half * mpos.x),
+                            beg_state.pos.y + double(half * mpos.y),
+                            beg_state.pos.z + double(half * mpos.z)};
+    result.mid_state.mom = {double(m_mid.x), double(m_mid.y), double(m_mid.z)};
+    return result;
+}
+
+//! Dormand-Prince step of this build's precision
+GBX_FORCEINLINE FieldStepperResult dormand_prince_step(UniformFieldEquation const& rhs,
+                                                       double step,
+                                                       OdeState const& beg_state)
+{
+    if constexpr (sizeof(real_type) == sizeof(double))
+        return dormand_prince_step_fp64(rhs, step, beg_state);
+    else
+        return dormand_prince_step_mixed(rhs, step, beg_state);
 }
 
 //---------------------------------------------------------------------------//
@@ -261,8 +401,18 @@ class FieldDriver
 
     GBX_FORCEINLINE double new_step_scale(double err_sq) const
     {
-        return opt_.safety
-               * fastpow(err_sq, 0.5 * (err_sq > 1 ? opt_.pshrink : opt_.pgrow));
+        double const power = 0.5 * (err_sq > 1 ? opt_.pshrink : opt_.pgrow);
+        if constexpr (sizeof(real_type) == sizeof(double))
+        {
+            return opt_.safety * fastpow(err_sq, power);
+        }
+        else
+        {
+            // Heuristic step-size factor in FP32 (the acceptance test that
+            // uses err_sq stays FP64); clamp the argument to FP32 range
+            float const e = float(min_of(max_of(err_sq, 1e-30), 1e30));
+            return opt_.safety * double(std::exp(float(power) * std::log(e)));
+        }
     }
 
     GBX_FUNCTION ChordSearch find_next_chord(double step, OdeState const& state) const

@@ -54,6 +54,13 @@ class MscHelper
     GBX_FORCEINLINE real_type calc_msc_mfp(real_type energy) const
     {
         real_type xsec = calc_grid_xs(p_, *xs_, energy) / ipow<2>(energy);
+        if constexpr (sizeof(real_type) < sizeof(double))
+        {
+            // FP32: in a near-vacuum the cross section underflows to zero;
+            // a finite mean free path far beyond any step keeps the
+            // path conversions finite (tau = step / lambda stays ~0)
+            return min_of(1 / xsec, real_type(1e20));
+        }
         return 1 / xsec;
     }
 
