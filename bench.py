@@ -1,10 +1,14 @@
 """Benchmark: track-steps/s and events/s of the EM-shower stepping loop.
 
 One benchmark step transports one batch of synthetic primaries (the
-workload below) to completion through the GB300 stepper. Prints one JSON
-line on rank 0.
+workload, default c2) to completion through the GB300 stepper. Prints one
+JSON line on rank 0. The headline is the mixed-precision build with
+action-sorted tracks; the plain FP64 build is timed the same way and
+reported under "fp64", with the per-layer energy-deposition difference
+between the two under "mixed_vs_fp64_edep".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1]
+                  [--precision mixed|double] [--track-order 0|5|6|7] [--no-fp64]
   python bench.py --impl reference ...   # CPU path of the reference loop
 
 Timing: W untimed warm-up steps, then K timed steps; each timed step is
@@ -60,6 +64,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.active = False  # keep only samples taken inside timed regions
 
     def __enter__(self):
         try:
@@ -75,7 +80,8 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            if self.active:
+                self.lines.append(line.strip())
 
     def __exit__(self, *exc):
         if self.proc:
@@ -189,11 +195,156 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
-def run_gb300(args, wl):
+DTYPES = {"mixed": "f32 physics + f64 positions/geometry/field/tally", "double": "f64"}
+
+
+def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks):
+    """Time one precision's stepping loop: device and end-to-end throughput,
+    per-transport tallies, and per-action times for the roofline."""
     import torch
 
     import celeritas_gb300 as gb
     from celeritas_gb300 import roofline
+
+    gb.load_library(precision=precision)
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                       field_tesla=wl["field"], msc=wl["msc"],
+                       track_order=args.track_order, precision=precision)
+    labels = params.action_labels()
+    stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
+    stream = stream_cls(stepper.stream_handle())
+    prim = make_primaries(wl, rank)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def finish(res):
+        # A shower of this workload ends in a few hundred steps; a run that
+        # hits the cap has a track that never terminates
+        res += stepper.run(max_steps=MAX_STEPS, batch=64)
+        if res[-1].alive or res[-1].queued:
+            raise RuntimeError(f"transport did not finish in {MAX_STEPS} steps")
+        return res
+
+    for _ in range(args.warmup):
+        finish([stepper.step(prim)])
+    torch.cuda.synchronize()
+
+    dev_ms, e2e_s, track_steps, iterations, tallies = [], [], [], [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        clocks.active = True
+        t0 = time.perf_counter()
+        stepper.clear_energy_deposition()
+        stepper.insert_primaries(prim)  # host -> device copy of primaries
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        res = finish([stepper.step()])
+        stop.record(stream)
+        edep = stepper.energy_deposition()  # device -> host tally
+        torch.cuda.synchronize()
+        e2e_s.append(time.perf_counter() - t0)
+        clocks.active = False
+        dev_ms.append(start.elapsed_time(stop))
+        track_steps.append(sum(r.active for r in res))
+        iterations.append(len(res))
+        tallies.append(edep)
+
+    # Per-action device times over one more (untimed) transport, stepped
+    # eagerly so that each step's action ranges can be read back
+    stepper.set_action_times(True)
+    processed = {lab: 0 for lab in labels}
+    res = [stepper.step(prim)]
+    while True:
+        offs = stepper.get_state("action_offsets", np.uint32).astype(np.int64)
+        half = len(offs) // 2
+        along, post = np.diff(offs[:half]), np.diff(offs[half:])
+        active = res[-1].active
+        for aid, lab in enumerate(labels):
+            if lab.startswith("along-step"):
+                processed[lab] += int(along[aid])
+            elif lab in roofline.MODEL_ACTIONS or lab in ("geo-boundary", "tracking-cut"):
+                processed[lab] += int(post[aid])
+            else:
+                processed[lab] += active
+        if not (res[-1].alive or res[-1].queued) or len(res) >= MAX_STEPS:
+            break
+        res.append(stepper.step())
+    ms, launches = stepper.action_times()
+    stepper.set_action_times(False)
+
+    real_bytes = 4 if precision == "mixed" else 8
+    per_action = {}
+    for aid, lab in enumerate(labels):
+        if launches[aid] == 0:
+            continue
+        nl = int(launches[aid])
+        proc = processed[lab]
+        idle = 0 if lab.startswith(("along-step", "sort-")) else wl["slots"] * nl - proc
+        b_proc, b_idle = roofline.bytes_per_slot(lab, real_bytes)
+        per_action[lab] = {"ms_per_launch": ms[aid] / nl,
+                           "bytes_per_launch": (proc * b_proc + max(idle, 0) * b_idle) / nl,
+                           "processed_per_launch": proc / nl}
+    dom = max(per_action, key=lambda lab: per_action[lab]["ms_per_launch"] * launches[labels.index(lab)])
+    total_ms = float(np.sum(dev_ms))
+    total_e2e = float(np.sum(e2e_s))
+    total_steps = float(np.sum(track_steps))
+    if dist:
+        t = torch.tensor([total_ms, total_e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, total_e2e = t.tolist()
+        st = torch.tensor([total_steps], device="cuda", dtype=torch.float64)
+        dist.all_reduce(st, op=dist.ReduceOp.SUM)
+        total_steps = st.item()
+    out = {
+        "precision": precision,
+        "value": total_steps / (total_ms / 1e3),
+        "e2e": total_steps / total_e2e,
+        "ms_per_step": total_ms / args.steps,
+        "events_per_s": wl["events"] * max(1, int(os.environ.get("WORLD_SIZE", "1")))
+        * args.steps / (total_ms / 1e3),
+        "track_steps_per_step": int(np.mean(track_steps)),
+        "iterations_per_step": int(np.mean(iterations)),
+        "tallies": np.array(tallies),
+        "per_action": per_action,
+        "dominant": dom,
+        "kernels_per_step": stepper.step_kernels(),
+        "iterations": iterations,
+        "h2d": int(len(prim)) * 80,
+        "d2h": len(tallies[0]) * 8 + 16 * 64,
+        "detectors": params.detector_labels(),
+    }
+    del stepper, params
+    return out
+
+
+def compare_tallies(mixed, fp64):
+    """Per-layer energy deposition of the mixed build against FP64, with
+    errors from the scatter of the independent timed transports."""
+    n = min(len(mixed), len(fp64))
+    mm, dm = mixed.mean(axis=0), fp64.mean(axis=0)
+    var = mixed.var(axis=0, ddof=1) / len(mixed) + fp64.var(axis=0, ddof=1) / len(fp64)
+    used = var > 0
+    chi2 = float((((mm - dm) ** 2)[used] / var[used]).sum())
+    dof = int(used.sum())
+    try:
+        from scipy import stats
+
+        p = float(stats.chi2.sf(chi2, dof))
+    except ImportError:
+        p = None
+    big = dm > 1e-3 * dm.max()
+    rel = np.abs(mm - dm)[big] / dm[big]
+    return {"transports": int(n), "total_rel_diff": float(abs(mm.sum() - dm.sum()) / dm.sum()),
+            "layer_chi2": chi2, "layer_dof": dof, "layer_p": p,
+            "max_layer_rel_diff": float(rel.max()), "mean_layer_rel_diff": float(rel.mean())}
+
+
+def run_gb300(args, wl):
+    import torch
+
     from celeritas_gb300.build import build
 
     rank = int(os.environ.get("RANK", "0"))
@@ -206,144 +357,84 @@ def run_gb300(args, wl):
 
         dist.init_process_group("nccl")
     if rank == 0:
-        build()
+        for prec in {args.precision, "double"}:
+            build(precision=prec)
     if dist:
         dist.barrier()
-    gb.load_library()
 
-    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
-                       field_tesla=wl["field"], msc=wl["msc"])
-    labels = params.action_labels()
-    stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
-    stream = torch.cuda.ExternalStream(stepper.stream_handle())
-    prim = make_primaries(wl, rank)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-
-    def transport():
-        return finish([stepper.step(prim)])
-
-    def finish(res):
-        # A shower of this workload ends in a few hundred steps; a run that
-        # hits the cap has a track that never terminates
-        res += stepper.run(max_steps=MAX_STEPS, batch=64)
-        if res[-1].alive or res[-1].queued:
-            raise RuntimeError(f"transport did not finish in {MAX_STEPS} steps")
-        return res
-
-    for _ in range(args.warmup):
-        transport()
-    torch.cuda.synchronize()
-
-    dev_ms, e2e_s, track_steps, iterations = [], [], [], []
+    precisions = [args.precision] + (["double"] if args.precision != "double"
+                                     and not args.no_fp64 else [])
+    results = {}
     with ClockSampler(local_rank) as clocks:
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            if dist:
-                dist.barrier()
-            t0 = time.perf_counter()
-            stepper.clear_energy_deposition()
-            stepper.insert_primaries(prim)  # host -> device copy of primaries
-            start = torch.cuda.Event(enable_timing=True)
-            stop = torch.cuda.Event(enable_timing=True)
-            start.record(stream)
-            res = finish([stepper.step()])
-            stop.record(stream)
-            edep = stepper.energy_deposition()  # device -> host tally
-            torch.cuda.synchronize()
-            e2e_s.append(time.perf_counter() - t0)
-            dev_ms.append(start.elapsed_time(stop))
-            track_steps.append(sum(r.active for r in res))
-            iterations.append(len(res))
-    total_steps = float(np.sum(track_steps))
-    total_ms = float(np.sum(dev_ms))
-    total_e2e = float(np.sum(e2e_s))
-    if dist:
-        t = torch.tensor([total_ms, total_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, total_e2e = t.tolist()
-        s = torch.tensor([total_steps], device="cuda", dtype=torch.float64)
-        dist.all_reduce(s, op=dist.ReduceOp.SUM)
-        total_steps = s.item()
-    value = total_steps / (total_ms / 1e3)
-    events_per_step = wl["events"] * world
-    e2e_value = total_steps / total_e2e
-
-    # Roofline of the dominant kernel: time every action with CUDA events on
-    # the stepper's stream over one more transport (not part of 'value')
-    stepper.set_action_times(True)
-    res = transport()
-    ms, launches = stepper.action_times()
-    stepper.set_action_times(False)
-    active = [r.active for r in res]
-    bytes_per_action = {}
-    for aid, label in enumerate(labels):
-        if launches[aid] == 0:
-            continue
-        # each action launches once per step over all slots
-        nbytes = sum(roofline.launch_bytes(label, a, wl["slots"]) for a in active[:launches[aid]])
-        bytes_per_action[label] = nbytes
-    dom = max((lab for lab in bytes_per_action), key=lambda lab: ms[labels.index(lab)])
-    dom_id = labels.index(dom)
-    dom_launch_ms = ms[dom_id] / max(launches[dom_id], 1)
-    dom_bytes = bytes_per_action[dom] / max(launches[dom_id], 1)
-    peak, peak_kind = load_peaks()
-    achieved = dom_bytes / (dom_launch_ms / 1e3) / 1e9
-    traffic = read_traffic(dom, float(np.mean(active)))
-
-    kernels_per_step = stepper.step_kernels()
-    launches_timed = int(sum(it * kernels_per_step + 2 for it in iterations))
+        for prec in precisions:
+            results[prec] = measure(args, wl, prec, torch.cuda.ExternalStream, dist,
+                                    rank, local_rank, clocks)
+    head = results[precisions[0]]
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
-    clk = clocks.summary()
-    h2d = int(len(prim)) * 80
-    d2h = len(edep) * 8 + 16 * int(np.mean(iterations)) // 64 * 64
+    dom = head["dominant"]
+    act = head["per_action"][dom]
+    peak, peak_kind = load_peaks()
+    achieved = act["bytes_per_launch"] / (act["ms_per_launch"] / 1e3) / 1e9
+    traffic = read_traffic(dom, act["processed_per_launch"], head["precision"])
     line = {
         "metric": "track-steps/s",
-        "value": value,
+        "value": head["value"],
         "unit": "track-steps/s",
-        "events_per_s": events_per_step * args.steps / (total_ms / 1e3),
+        "events_per_s": head["events_per_s"],
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps,
+        "ms_per_step": head["ms_per_step"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": DTYPES[head["precision"]],
         "data": "synthetic",
         "config": {"workload": wl["description"], "name": args.workload,
-                   "track_steps_per_step": int(np.mean(track_steps)),
-                   "iterations_per_step": int(np.mean(iterations)),
+                   "precision": head["precision"],
+                   "track_order": args.track_order,
+                   "track_steps_per_step": head["track_steps_per_step"],
+                   "iterations_per_step": head["iterations_per_step"],
                    "l2": "flushed (256 MiB write) between timed steps",
                    "parallelism": f"events sharded over {world} GPU(s)"},
-        "e2e": {"value": e2e_value, "unit": "track-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": {"value": head["e2e"], "unit": "track-steps/s",
+                "h2d_bytes_per_step": head["h2d"], "d2h_bytes_per_step": head["d2h"]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "launch_ms": dom_launch_ms,
-                     "action_ms_per_step": {labels[i]: ms[i] / max(launches[i], 1)
-                                            for i in range(len(labels)) if launches[i]}},
-        "gpu_launches": launches_timed,
-        "clocks": clk,
+                     "peak_source": peak_kind, "launch_ms": act["ms_per_launch"],
+                     "algorithmic_bytes_per_launch": act["bytes_per_launch"],
+                     "actions": {k: {"ms": round(v["ms_per_launch"], 4),
+                                     "GB/s": round(v["bytes_per_launch"]
+                                                   / max(v["ms_per_launch"], 1e-9) / 1e6, 2)}
+                                 for k, v in head["per_action"].items()}},
+        "gpu_launches": int(sum(it * head["kernels_per_step"] + 2 for it in head["iterations"])),
+        "clocks": clocks.summary(),
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    if "double" in results and head["precision"] != "double":
+        fp = results["double"]
+        line["fp64"] = {"value": fp["value"], "e2e": fp["e2e"], "ms_per_step": fp["ms_per_step"],
+                        "events_per_s": fp["events_per_s"],
+                        "iterations_per_step": fp["iterations_per_step"],
+                        "dominant_kernel_ms": fp["per_action"][fp["dominant"]]["ms_per_launch"]}
+        line["mixed_vs_fp64_edep"] = compare_tallies(head["tallies"], fp["tallies"])
+    if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 
 
-def read_traffic(kernel_label, mean_active):
+def read_traffic(kernel_label, processed, precision):
     """DRAM bytes per launch of a kernel, from the committed ncu capture.
 
-    The capture holds one launch's DRAM bytes and that launch's active track
-    slots; the figure is scaled to the mean active slots per launch of this
-    run (the traffic of a step action grows with the tracks it processes).
+    The capture holds one launch's DRAM bytes and the track slots that
+    launch processed; the figure is scaled to this run's mean processed
+    slots per launch (an action's traffic grows with the tracks it
+    processes). Only captures of the same precision are used.
     """
     path = os.path.join(REPO, "profiles", "traffic.txt")
     if not os.path.exists(path):
@@ -351,8 +442,8 @@ def read_traffic(kernel_label, mean_active):
     with open(path) as f:
         for line in f:
             tok = line.split()
-            if len(tok) >= 3 and tok[0] == kernel_label:
-                return float(tok[1]) * mean_active / float(tok[2])
+            if len(tok) >= 4 and tok[0] == kernel_label and tok[1] == precision:
+                return float(tok[2]) * processed / float(tok[3])
     return None
 
 
@@ -364,6 +455,11 @@ def main():
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     parser.add_argument("--workload", default="c2", choices=list(WORKLOADS))
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--precision", default="mixed", choices=["mixed", "double"])
+    parser.add_argument("--track-order", type=int, default=7,
+                        help="TrackOrder: 0 none, 5/6/7 action sorts")
+    parser.add_argument("--no-fp64", action="store_true",
+                        help="skip the plain FP64 comparison run")
     args = parser.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -149,6 +149,10 @@ FieldRef find_field(gbx::CoreState& st, std::string const& name)
     if (name == "rng")
         return FieldRef{s.rng.s[0], sizeof(std::uint32_t), 6 * n};
     if (name == "track_slots") return f(s.track_slots);
+    if (name == "action_offsets")
+        return FieldRef{s.action_offsets,
+                        sizeof(size_type),
+                        2 * std::size_t(st.context().sort.num_bins + 1)};
     if (name == "counters")
         return FieldRef{s.counters, sizeof(Counters), 1};
     if (name == "initializers")

@@ -406,7 +406,7 @@ CoreState::CoreState(CoreParams const& params,
     size_type const num_bins = params.host().scalars.num_actions + 1;
     size_type const sort_blocks = (n + sort_block_size - 1) / sort_block_size;
     std::size_t o_tslots = arr(4);
-    std::size_t o_aoff = L.reserve(4 * std::size_t(num_bins + 1));
+    std::size_t o_aoff = L.reserve(4 * 2 * std::size_t(num_bins + 1));
     std::size_t o_shist = L.reserve(4 * std::size_t(num_bins) * sort_blocks);
     std::size_t o_log = L.reserve(sizeof(StepRecord) * log_cap);
     std::size_t o_stepidx = L.reserve(sizeof(size_type));

@@ -453,7 +453,9 @@ __global__ __launch_bounds__(sort_block_size) void sort_count_kernel(
         srt.block_hist[i * srt.num_blocks + blockIdx.x] = hist[i];
 }
 
-__global__ __launch_bounds__(1024) void sort_scan_kernel(StateData s, SortScratch srt)
+__global__ __launch_bounds__(1024) void sort_scan_kernel(StateData s,
+                                                         SortScratch srt,
+                                                         size_type* offsets)
 {
     __shared__ size_type warp_sums[32];
     size_type const total = srt.num_bins * srt.num_blocks;
@@ -498,9 +500,9 @@ __global__ __launch_bounds__(1024) void sort_scan_kernel(StateData s, SortScratc
     }
     __syncthreads();
     for (size_type b = threadIdx.x; b < srt.num_bins; b += blockDim.x)
-        s.action_offsets[b] = srt.block_hist[b * srt.num_blocks];
+        offsets[b] = srt.block_hist[b * srt.num_blocks];
     if (threadIdx.x == 0)
-        s.action_offsets[srt.num_bins] = s.size;
+        offsets[srt.num_bins] = s.size;
 }
 
 __global__ __launch_bounds__(sort_block_size) void sort_scatter_kernel(
@@ -543,13 +545,13 @@ __global__ __launch_bounds__(sort_block_size) void sort_scatter_kernel(
 
 //! Slot of this thread within the sorted bins [first_bin, end_bin)
 __device__ __forceinline__ bool sorted_slot(StateData const& s,
+                                            size_type const* offsets,
                                             size_type first_bin,
                                             size_type end_bin,
                                             size_type* slot)
 {
-    size_type const t = s.action_offsets[first_bin] + blockIdx.x * blockDim.x
-                        + threadIdx.x;
-    if (t >= s.action_offsets[end_bin])
+    size_type const t = offsets[first_bin] + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= offsets[end_bin])
         return false;
     *slot = s.track_slots[t];
     return true;
@@ -564,19 +566,26 @@ __device__ __forceinline__ bool sorted_slot(StateData const& s,
 template<AlongKind K>
 __global__ __launch_bounds__(block_size,
                              K == AlongKind::charged ? GBX_ALONG_MIN_BLOCKS : 1) void
-along_step_sorted_kernel(
-    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+along_step_sorted_kernel(ParamsData p,
+                         StateData s,
+                         size_type const* offsets,
+                         size_type first_bin,
+                         size_type end_bin)
 {
     size_type slot;
-    if (sorted_slot(s, first_bin, end_bin, &slot))
+    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
         along_step_impl<K>(p, s, slot);
 }
 
 __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
-    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+    ParamsData p,
+    StateData s,
+    size_type const* offsets,
+    size_type first_bin,
+    size_type end_bin)
 {
     size_type slot;
-    if (sorted_slot(s, first_bin, end_bin, &slot))
+    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
     {
         size_type a = s.post_step_action[slot];
         if (a >= p.model_to_action && a < p.model_to_action + p.num_models)
@@ -585,19 +594,34 @@ __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
 }
 
 __global__ __launch_bounds__(block_size) void boundary_sorted_kernel(
-    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+    ParamsData p,
+    StateData s,
+    size_type const* offsets,
+    size_type first_bin,
+    size_type end_bin)
 {
     size_type slot;
-    if (sorted_slot(s, first_bin, end_bin, &slot))
+    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
         boundary_cross(p, s, slot);
 }
 
 __global__ __launch_bounds__(block_size) void tracking_cut_sorted_kernel(
-    ParamsData p, StateData s, size_type first_bin, size_type end_bin)
+    ParamsData p,
+    StateData s,
+    size_type const* offsets,
+    size_type first_bin,
+    size_type end_bin)
 {
     size_type slot;
-    if (sorted_slot(s, first_bin, end_bin, &slot))
+    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
         tracking_cut(p, s, slot);
+}
+
+//! Bin offsets written by the sort for a key
+inline size_type* sort_offsets(LaunchContext const& ctx, SortKey key)
+{
+    std::size_t const table = std::size_t(ctx.sort.num_bins) + 1;
+    return ctx.state.action_offsets + (key == SortKey::step_limit ? table : 0);
 }
 
 }  // namespace
@@ -639,15 +663,20 @@ void launch_along_step(LaunchContext const& ctx,
         // Launch each along-step action over its sorted range with a kernel
         // compiled for that action only; the grid covers the largest range
         unsigned int const nb = num_blocks_for(ctx.state.size);
+        size_type const* offsets = sort_offsets(ctx, SortKey::along_step);
         if (action == invalid_id || action == p.action_along_step)
         {
             along_step_sorted_kernel<AlongKind::charged><<<nb, block_size, 0, stream>>>(
-                p, ctx.state, p.action_along_step, p.action_along_step + 1);
+                p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
         }
         if (action == invalid_id || action == p.action_along_step_neutral)
         {
             along_step_sorted_kernel<AlongKind::neutral><<<nb, block_size, 0, stream>>>(
-                p, ctx.state, p.action_along_step_neutral, p.action_along_step_neutral + 1);
+                p,
+                ctx.state,
+                offsets,
+                p.action_along_step_neutral,
+                p.action_along_step_neutral + 1);
         }
         return;
     }
@@ -673,7 +702,7 @@ void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t st
             end = p.model_to_action + p.num_models;
         }
         interact_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p, ctx.state, first, end);
+            p, ctx.state, sort_offsets(ctx, SortKey::step_limit), first, end);
         return;
     }
     if (action == invalid_id)
@@ -694,7 +723,11 @@ void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
     if (sorts_step_limit(p.track_order))
     {
         boundary_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p, ctx.state, p.action_boundary, p.action_boundary + 1);
+            p,
+            ctx.state,
+            sort_offsets(ctx, SortKey::step_limit),
+            p.action_boundary,
+            p.action_boundary + 1);
         return;
     }
     boundary_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
@@ -707,7 +740,11 @@ void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
     if (sorts_step_limit(p.track_order))
     {
         tracking_cut_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p, ctx.state, p.action_tracking_cut, p.action_tracking_cut + 1);
+            p,
+            ctx.state,
+            sort_offsets(ctx, SortKey::step_limit),
+            p.action_tracking_cut,
+            p.action_tracking_cut + 1);
         return;
     }
     tracking_cut_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
@@ -742,7 +779,7 @@ void launch_sort_tracks(LaunchContext const& ctx, SortKey key, cudaStream_t stre
                         sort_block_size,
                         srt.num_bins * sizeof(size_type),
                         stream>>>(ctx.state, srt, key);
-    sort_scan_kernel<<<1, 1024, 0, stream>>>(ctx.state, srt);
+    sort_scan_kernel<<<1, 1024, 0, stream>>>(ctx.state, srt, sort_offsets(ctx, key));
     sort_scatter_kernel<<<srt.num_blocks,
                           sort_block_size,
                           (sort_block_size / 32) * srt.num_bins * sizeof(size_type),

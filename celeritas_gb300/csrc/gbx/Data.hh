@@ -479,8 +479,9 @@ struct StateData
     size_type primary_capacity;
 
     // Action-sorted thread -> slot indirection (CoreStateData::track_slots)
-    // and the first thread of each action bin; the last bin holds slots
-    // whose action is invalid (num_actions + 2 offsets)
+    // and the first thread of each action bin, one table per sort key:
+    // along-step sort at [0, num_actions + 2), step-limit sort after it.
+    // The last bin of a table holds slots whose action is invalid.
     size_type* track_slots;
     size_type* action_offsets;
 

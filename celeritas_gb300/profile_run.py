@@ -6,7 +6,8 @@
 
 Inserts the workload's primaries, then steps (eagerly by default, so that
 every kernel is its own launch) until the state empties or K iterations have
-run, and prints one line per iteration with the step counters. Meant to be
+run. The steps log holds each iteration's step counters and, with an action
+sort, the number of slots in each action's sorted range. Meant to be
 wrapped by ncu: the launch order is fixed (one launch per step action and
 iteration), so '-k <kernel> -s <n>' selects a known iteration.
 """
@@ -16,6 +17,8 @@ from __future__ import annotations
 import argparse
 import json
 import sys
+
+import numpy as np
 
 from . import Params, Stepper, load_library, physics_file
 from .workloads import WORKLOADS, make_primaries
@@ -39,15 +42,31 @@ def main(argv=None):
                     track_order=args.track_order, precision=args.precision)
     stepper = Stepper(params, wl["slots"], seed=wl["seed"], use_graph=args.graph)
     prim = make_primaries(wl, num=args.primaries)
+    labels = params.action_labels()
+    counts = []
+
+    def record():
+        # Slots per action in this step's sorted ranges (along-step sort,
+        # step-limit sort); empty without an action sort
+        if args.track_order:
+            offs = stepper.get_state("action_offsets", np.uint32).astype(np.int64)
+            half = len(offs) // 2
+            along, post = np.diff(offs[:half]), np.diff(offs[half:])
+            counts.append({lab: int(along[i] if lab.startswith("along-step") else post[i])
+                           for i, lab in enumerate(labels) if along[i] or post[i]})
+
     res = [stepper.step(prim)]
+    record()
     while len(res) < args.max_iterations and (res[-1].alive or res[-1].queued):
         res.append(stepper.step())
+        record()
     stepper.synchronize()
     rows = [[r.generated, r.queued, r.active, r.alive] for r in res]
     if args.steps_log:
         with open(args.steps_log, "w") as f:
             json.dump({"workload": args.workload, "primaries": len(prim),
-                       "steps": rows}, f)
+                       "precision": args.precision, "track_order": args.track_order,
+                       "steps": rows, "action_slots": counts}, f)
     print(f"iterations {len(res)} track-steps {sum(r[2] for r in rows)}")
     return 0
 
