@@ -166,9 +166,7 @@ FieldRef find_field(gbx::CoreState& st, std::string const& name)
 
 gbx::GeometrySpec geometry_by_name(std::string const& name)
 {
-    if (name == "calo")
-        return gbx::make_calorimeter_geometry();
-    throw std::runtime_error("unknown geometry '" + name + "'");
+    return gbx::make_geometry(name);
 }
 
 }  // namespace

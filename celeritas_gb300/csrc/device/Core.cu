@@ -297,8 +297,8 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_mscm = pk.add(h.msc_materials);
     std::size_t o_mscp = pk.add(h.msc_par_mat);
     std::size_t o_loop = pk.add(h.looping);
-    std::size_t o_pl = pk.add(h.planes);
-    std::size_t o_box = pk.add(h.boxes);
+    std::size_t o_pl = pk.add(h.surfaces);
+    std::size_t o_box = pk.add(h.volumes);
     std::size_t o_no = pk.add(h.neighbor_offset);
     std::size_t o_nb = pk.add(h.neighbors);
     std::size_t o_vm = pk.add(h.volume_material);
@@ -327,8 +327,8 @@ CoreParams::CoreParams(Input const& inp)
     device_.msc.material = reinterpret_cast<UrbanMscMaterialRecord const*>(base + o_mscm);
     device_.msc.par_mat = reinterpret_cast<UrbanMscParMatRecord const*>(base + o_mscp);
     device_.looping = reinterpret_cast<LoopingRecord const*>(base + o_loop);
-    device_.geo.planes = reinterpret_cast<PlaneRecord const*>(base + o_pl);
-    device_.geo.boxes = reinterpret_cast<BoxVolume const*>(base + o_box);
+    device_.geo.surfaces = reinterpret_cast<SurfaceRecord const*>(base + o_pl);
+    device_.geo.volumes = reinterpret_cast<VolumeRecord const*>(base + o_box);
     device_.geo.neighbor_offset = reinterpret_cast<size_type const*>(base + o_no);
     device_.geo.neighbors = reinterpret_cast<size_type const*>(base + o_nb);
     device_.geo.volume_material = reinterpret_cast<size_type const*>(base + o_vm);
@@ -358,7 +358,7 @@ CoreState::CoreState(CoreParams const& params,
     size_type const sec_cap = static_cast<size_type>(
         params.host().scalars.secondary_stack_factor * n);
     size_type const init_cap
-        = initializer_capacity ? initializer_capacity : std::max(1u << 20, 4 * n);
+        = initializer_capacity ? initializer_capacity : std::max(1u << 20, 16 * n);
     size_type const ndet = params.host().scalars.num_detectors;
     size_type const nblocks = (n + block_size - 1) / block_size;
     size_type const log_cap = 4096;

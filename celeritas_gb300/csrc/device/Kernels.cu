@@ -93,13 +93,17 @@ __device__ __forceinline__ size_type block_exclusive_scan(size_type value,
 __global__ void begin_primaries_kernel(StateData s, size_type num_primaries)
 {
     Counters& c = *s.counters;
+    if (num_primaries > s.initializer_capacity - c.num_initializers)
+    {
+        // The queue would overflow: drop the primaries, keep every queued
+        // initializer valid, and let the host report the overflow
+        c.error_flags |= error_initializer_overflow;
+        c.num_generated = 0;
+        c.num_pending_primaries = 0;
+        return;
+    }
     c.num_initializers += num_primaries;
     c.num_generated = num_primaries;
-    if (c.num_initializers > s.initializer_capacity)
-    {
-        c.error_flags |= error_initializer_overflow;
-        c.num_initializers = s.initializer_capacity;
-    }
     c.num_pending_primaries = num_primaries;
 }
 
@@ -348,11 +352,18 @@ __global__ __launch_bounds__(1024) void scan_blocks_kernel(StateData s,
     {
         Counters& c = *s.counters;
         c.num_vacancies = carry_vac;
-        c.num_secondaries = carry_cnt;
-        c.num_initializers += carry_cnt;
-        if (c.num_initializers > s.initializer_capacity)
+        if (carry_cnt > s.initializer_capacity - c.num_initializers)
         {
+            // The queue would overflow: this step's secondaries are dropped
+            // (the scatter skips them), the queued initializers stay valid
+            // and the host reports the overflow
             c.error_flags |= error_initializer_overflow;
+            c.num_secondaries = 0;
+        }
+        else
+        {
+            c.num_secondaries = carry_cnt;
+            c.num_initializers += carry_cnt;
         }
         c.num_alive = s.size - c.num_vacancies;
         StepRecord& r = log[*step_index % log_capacity];

@@ -439,10 +439,36 @@ GBX_FUNCTION void discrete_select(ParamsData const& p,
         }
     }
     size_type const model = phys.find_model(ppid, energy);
+    if (model == invalid_id)
+    {
+        // No model applies at this energy (possible only for a corrupted
+        // track state): fail the track instead of dispatching nowhere
+        apply_errored(p, s, slot);
+        return;
+    }
     MaterialRecord const& mat = p.materials[mid];
     if (mat.num_elements == 1)
     {
         s.element[slot] = 0;
+    }
+    else
+    {
+        // Sample the element from the model's tabulated cross-section CDF
+        // (TabulatedElementSelector, src/celeritas/mat/TabulatedElementSelector.hh)
+        size_type const table
+            = p.ints[p.element_tables
+                     + (model * p.num_particles + pid) * p.num_materials + mid];
+        if (table != invalid_id)
+        {
+            real_type const u = generate_canonical<real_type>(rng);
+            size_type i = 0;
+            for (; i + 1 < mat.num_elements; ++i)
+            {
+                if (calc_grid_xs(p, p.grids[p.ints[table + i]], energy) > u)
+                    break;
+            }
+            s.element[slot] = i;
+        }
     }
     action = model + p.model_to_action;
     s.post_step_action[slot] = action;
@@ -526,14 +552,45 @@ GBX_FUNCTION void interact(ParamsData const& p,
         XorwowEngine rng(s.rng, slot);
         MaterialRecord const& mat = p.materials[mid];
         size_type const elcomp = s.element[slot];
+        if ((action == p.action_bethe_heitler || action == p.action_seltzer_berger
+             || action == p.action_rel_brems)
+            && !(elcomp < mat.num_elements))
+        {
+            // Element-dependent model without a sampled element (possible
+            // only for a corrupted track state)
+            apply_errored(p, s, slot);
+            return;
+        }
         if (action == p.action_klein_nishina)
         {
             result = interact_klein_nishina(p, energy, dir, allocate, rng);
         }
         else if (action == p.action_livermore_pe)
         {
+            size_type el = elcomp;
+            if (el == invalid_id)
+            {
+                // Sample the element with on-the-fly micro cross sections
+                // (ElementSelector in LivermorePEExecutor.hh:41-54)
+                real_type micro[max_elements];
+                real_type material_xs = 0;
+                for (size_type j = 0; j < mat.num_elements; ++j)
+                {
+                    micro[j] = livermore_pe_micro_xs(p, mat.element[j], energy);
+                    material_xs += micro[j] * mat.fraction[j];
+                }
+                real_type accum = -material_xs * generate_canonical<real_type>(rng);
+                el = 0;
+                for (; el + 1 < mat.num_elements; ++el)
+                {
+                    accum += mat.fraction[el] * micro[el];
+                    if (accum > 0)
+                        break;
+                }
+                s.element[slot] = el;
+            }
             result = interact_livermore_pe(
-                p, mat.element[elcomp], energy, dir, allocate, rng);
+                p, mat.element[el], energy, dir, allocate, rng);
         }
         else if (action == p.action_bethe_heitler)
         {

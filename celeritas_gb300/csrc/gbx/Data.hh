@@ -234,30 +234,49 @@ struct LoopingRecord
 };
 
 //---------------------------------------------------------------------------//
-// Geometry: axis-aligned box volumes in a background world (the ORANGE
-// simple-unit subset used by the sampling calorimeter)
+// Geometry: volumes bounded by axis-aligned planes and z-axis cylinders in a
+// background world (the ORANGE single-level simple-unit subset used by the
+// sampling calorimeter and the CMS-like detector)
 //---------------------------------------------------------------------------//
-//! Surface: an axis-aligned plane
-struct PlaneRecord
+//! Surface types (ORANGE SurfaceType px, py, pz, czc)
+enum SurfaceType : int
 {
-    int axis;
-    double position;
+    surf_px = 0,
+    surf_py = 1,
+    surf_pz = 2,
+    surf_czc = 3,  //!< cylinder centered on the z axis
 };
 
-//! Volume bounded by faces; 'sense' gives the inside sense of each face
-struct BoxVolume
+//! Surface: a plane (value = position) or a z cylinder (value = radius^2)
+struct SurfaceRecord
 {
-    size_type faces[6];  //!< Plane (surface) IDs
-    std::int8_t inside_sense[6];  //!< +1: inside is pos > plane, -1: below
+    int type;
+    double value;
+};
+
+//! Volume: conjunction of face senses; inside_sense +1 means the inside is
+//! where the surface function is positive (pos > plane, r > radius)
+struct VolumeRecord
+{
+    size_type faces[6];  //!< Surface IDs, sorted
+    std::int8_t inside_sense[6];
+    size_type num_faces;
     size_type material;
+};
+
+//! How points are located among the volumes
+enum GeoLocate : int
+{
+    locate_stack_z = 2,  //!< binary search over boxes layered along z
+    locate_scan = 3,  //!< test every volume
 };
 
 struct GeoParams
 {
     size_type num_surfaces;
-    PlaneRecord const* planes;
+    SurfaceRecord const* surfaces;
     size_type num_volumes;  //!< Including exterior (0) and background
-    BoxVolume const* boxes;  //!< Indexed by volume id (exterior/background unused)
+    VolumeRecord const* volumes;  //!< Indexed by volume id (exterior/background unused)
     size_type exterior;  //!< Volume id of the exterior (0)
     size_type background;  //!< Volume id of the implicit background
     size_type world_faces[6];  //!< Boundary planes of the world box
@@ -265,8 +284,7 @@ struct GeoParams
     //! Neighbors of each surface: volumes that own it as a face
     size_type const* neighbor_offset;  //!< [num_surfaces + 1]
     size_type const* neighbors;
-    //! Uniform search grid along the layering axis for point location
-    int stack_axis;
+    int locate;  //!< GeoLocate
     double tol_abs;
     double tol_rel;
     size_type const* volume_material;  //!< [num_volumes], invalid if none
@@ -314,6 +332,10 @@ struct ParamsData
     size_type annihilation_process;
     real_type photoelectric_table_thresh;
     size_type livermore_model;
+    //! Element selection (PhysicsParams::build_model_xs): offset in ints of
+    //! [model][particle][material] entries, each the offset in ints of one
+    //! CDF grid ID per element component (invalid: no table)
+    size_type element_tables;
     size_type eplusgg_model;
 
     // Model data

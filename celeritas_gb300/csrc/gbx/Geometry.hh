@@ -1,17 +1,22 @@
-// Navigation through axis-aligned box volumes inside an implicit background
-// volume and a world box (the sampling-calorimeter geometry class).
+// Navigation through volumes bounded by axis-aligned planes and z-axis
+// cylinders inside an implicit background volume and a world box (the
+// sampling-calorimeter and CMS-like geometry classes).
 //
 // Semantics follow ORANGE's single-level simple unit:
-// - sense of a point w.r.t. a plane is "outside" when pos - plane >= 0
-//   (src/orange/OrangeTypes.hh:412-424);
-// - a box volume's logic is the conjunction of its face senses
+// - sense of a point w.r.t. a surface is "outside" when the surface function
+//   is >= 0: pos - plane for planes, x^2 + y^2 - r^2 for z cylinders
+//   (src/orange/OrangeTypes.hh:412-424, src/orange/surf/CylCentered.hh);
+// - a volume's logic is the conjunction of its face senses
 //   (src/orange/univ/detail/LogicEvaluator.hh);
 // - distance to a plane is (plane - pos) / dir, kept if positive and not on
-//   the current surface (src/orange/surf/PlaneAligned.hh);
-// - box volumes take the first minimum over faces
+//   the current surface (src/orange/surf/PlaneAligned.hh); a cylinder's
+//   distances are the positive roots of its quadratic, with the on-surface
+//   (c = 0) form on the current surface
+//   (src/orange/surf/detail/QuadraticSolver.hh);
+// - a volume takes the first minimum over its faces' intersections
 //   (src/orange/univ/SimpleUnitTracker.hh:271-330);
-// - the background volume scans crossings by increasing distance and accepts
-//   the first one whose bumped point lies inside a neighbor volume
+// - the background volume accepts the first crossing, by increasing
+//   (distance, surface), whose bumped point lies inside a neighbor volume
 //   (SimpleUnitTracker::background_intersect);
 // - crossing a surface flips the sense and locates the new volume among the
 //   surface's neighbors with the crossed face's sense forced
@@ -20,8 +25,8 @@
 //
 // The volume search used when a surface has many neighbors (the reference
 // uses a bounding-interval hierarchy) is a binary search over the layer
-// planes along the stacking axis followed by the same inside test, which
-// selects the same volume because box volumes do not overlap.
+// planes for boxes stacked along z, or a scan over the volumes; either
+// selects the same volume because volumes do not overlap.
 #pragma once
 
 #include "Data.hh"
@@ -144,42 +149,132 @@ class GeoTrackView
         s_.dir[2][slot_] = v.z;
     }
 
-    //! True if the point is on the "outside" (non-negative) side of a plane
+    //! True if the point is on the "outside" (non-negative) side of a surface
     static GBX_FORCEINLINE bool sense_outside(double q) { return !(q < 0); }
 
-    GBX_FORCEINLINE double plane_q(size_type surf, Real3 const& pos) const
+    //! Surface function at a point: its sign is the sense
+    GBX_FORCEINLINE double surface_q(size_type surf, Real3 const& pos) const
     {
-        PlaneRecord const& pl = p_.planes[surf];
-        return pos[pl.axis] - pl.position;
+        SurfaceRecord const& sr = p_.surfaces[surf];
+        if (sr.type == surf_czc)
+            return ipow<2>(pos.x) + ipow<2>(pos.y) - sr.value;
+        return pos[sr.type] - sr.value;
     }
 
-    //! Evaluate the inside logic of a box volume at 'pos'. A face whose
+    //! Positive distances to a surface along dir (+inf where none)
+    GBX_FUNCTION void intersect(size_type surf,
+                                Real3 const& pos,
+                                Real3 const& dir,
+                                bool on_surface,
+                                double* dist) const
+    {
+        dist[0] = dist[1] = INFINITY;
+        SurfaceRecord const& sr = p_.surfaces[surf];
+        if (sr.type != surf_czc)
+        {
+            if (on_surface)
+                return;
+            double const n_dir = dir[sr.type];
+            if (n_dir != 0)
+            {
+                double const d = (sr.value - pos[sr.type]) / n_dir;
+                if (d > 0)
+                    dist[0] = d;
+            }
+            return;
+        }
+        // 1 - (dir . z)^2; no intersection when traveling along the axis
+        double const a = 1 - ipow<2>(dir.z);
+        constexpr double sqrt_quadratic = 1e-5;
+        if (a < ipow<2>(sqrt_quadratic))
+            return;
+        double const half_b = dir.x * pos.x + dir.y * pos.y;
+        double const a_inv = 1 / a;
+        double const hba = half_b * a_inv;
+        if (on_surface)
+        {
+            double const r = -2 * hba;
+            if (r > 0)
+                dist[0] = r;
+            return;
+        }
+        double const c = (ipow<2>(pos.x) + ipow<2>(pos.y) - sr.value) * a_inv;
+        double const b2_4 = ipow<2>(hba);
+        if (b2_4 > c)
+        {
+            double const t2 = std::sqrt(b2_4 - c);
+            double const r0 = -hba - t2;
+            double const r1 = -hba + t2;
+            if (r1 > 0)
+            {
+                dist[1] = r1;
+                if (r0 > 0)
+                    dist[0] = r0;
+            }
+        }
+        else if (b2_4 == c)
+        {
+            double const r0 = -hba;
+            if (r0 > 0)
+                dist[0] = r0;
+        }
+    }
+
+    //! Distance from a point to a surface (for the safety): the nearest
+    //! intersection along the surface normal pointing toward the surface
+    //! (CalcSafetyDistance, src/orange/univ/detail/SurfaceFunctors.hh)
+    GBX_FUNCTION double surface_safety(size_type surf, Real3 const& pos) const
+    {
+        SurfaceRecord const& sr = p_.surfaces[surf];
+        if (sr.type != surf_czc)
+            return std::fabs(pos[sr.type] - sr.value);
+        Real3 n = make_unit_vector(Real3{pos.x, pos.y, 0});
+        if (std::isnan(n.x))
+        {
+            // On the axis: the cylinder is a long way off
+            return INFINITY;
+        }
+        double const q = this->surface_q(surf, pos);
+        if (q > 0)
+        {
+            n = {-n.x, -n.y, -n.z};
+        }
+        else if (q == 0)
+        {
+            return 0;
+        }
+        double d[2];
+        this->intersect(surf, pos, n, false, d);
+        return min_of(d[0], d[1]);
+    }
+
+    //! Evaluate the inside logic of a volume at 'pos'. A face whose
     //! surface equals 'forced' takes the given sense. Sets *on_surface if
-    //! any unforced face evaluates exactly on its plane.
-    GBX_FUNCTION bool box_inside(BoxVolume const& box,
-                                 Real3 const& pos,
-                                 size_type forced,
-                                 bool forced_outside,
-                                 bool* on_surface) const
+    //! any unforced face evaluates exactly on its surface.
+    GBX_FUNCTION bool volume_logic(VolumeRecord const& vol,
+                                   Real3 const& pos,
+                                   size_type forced,
+                                   bool forced_outside,
+                                   bool* on_surface) const
     {
         bool inside = true;
-        for (int f = 0; f < 6; ++f)
+        for (size_type f = 0; f < vol.num_faces; ++f)
         {
             bool s;
-            if (box.faces[f] == forced)
+            if (vol.faces[f] == forced)
             {
                 s = forced_outside;
             }
             else
             {
-                double q = this->plane_q(box.faces[f], pos);
+                double q = this->surface_q(vol.faces[f], pos);
                 s = sense_outside(q);
                 if (q == 0 && on_surface)
                 {
                     *on_surface = true;
                 }
             }
-            inside = inside && (box.inside_sense[f] > 0 ? s : !s);
+            inside = inside && (vol.inside_sense[f] > 0 ? s : !s);
         }
         return inside;
     }
@@ -190,13 +285,14 @@ class GeoTrackView
                                       bool forced_outside,
                                       bool* on_surface) const
     {
-        BoxVolume world;
+        VolumeRecord world;
         for (int f = 0; f < 6; ++f)
         {
             world.faces[f] = p_.world_faces[f];
             world.inside_sense[f] = p_.world_sense[f];
         }
-        return !this->box_inside(world, pos, forced, forced_outside, on_surface);
+        world.num_faces = 6;
+        return !this->volume_logic(world, pos, forced, forced_outside, on_surface);
     }
 
     GBX_FUNCTION bool volume_inside(size_type vol,
@@ -209,11 +305,11 @@ class GeoTrackView
         {
             return this->exterior_inside(pos, forced, forced_outside, on_surface);
         }
-        return this->box_inside(
-            p_.boxes[vol], pos, forced, forced_outside, on_surface);
+        return this->volume_logic(
+            p_.volumes[vol], pos, forced, forced_outside, on_surface);
     }
 
-    //! Locate the box volume containing a point among all volumes (the
+    //! Locate the volume containing a point among all volumes (the
     //! reference's BIH search), skipping 'exclude'; background if none.
     GBX_FUNCTION size_type find_volume_at(Real3 const& pos,
                                           size_type exclude,
@@ -240,16 +336,31 @@ GBX_FUNCTION size_type GeoTrackView::find_volume_at(Real3 const& pos,
             return p_.exterior;
         }
     }
-    // Candidate box volumes: binary search along the stacking axis over the
-    // volumes' lower planes (boxes are sorted by increasing lower plane)
-    int const axis = p_.stack_axis;
-    double const x = pos[axis];
+    if (p_.locate == locate_scan)
+    {
+        for (size_type cand = 1; cand < p_.background; ++cand)
+        {
+            if (cand == exclude)
+                continue;
+            bool on = false;
+            if (this->volume_logic(p_.volumes[cand], pos, forced, forced_outside, &on))
+            {
+                if (on_surface)
+                    *on_surface = on;
+                return cand;
+            }
+        }
+        return p_.background;
+    }
+    // Candidate box volumes: binary search along z over the volumes' lower
+    // planes (boxes are sorted by increasing lower plane)
+    double const x = pos.z;
     // Boxes occupy ids [1, background); find last box with lower <= x
     size_type lo = 1, hi = p_.background;  // search in [lo, hi)
     while (lo < hi)
     {
         size_type mid = lo + (hi - lo) / 2;
-        double lower = p_.planes[p_.boxes[mid].faces[4]].position;
+        double lower = p_.surfaces[p_.volumes[mid].faces[4]].value;
         if (lower <= x)
             lo = mid + 1;
         else
@@ -265,7 +376,7 @@ GBX_FUNCTION size_type GeoTrackView::find_volume_at(Real3 const& pos,
         if (cand == exclude)
             continue;
         bool on = false;
-        if (this->box_inside(p_.boxes[cand], pos, forced, forced_outside, &on))
+        if (this->volume_logic(p_.volumes[cand], pos, forced, forced_outside, &on))
         {
             if (on_surface)
                 *on_surface = on;
@@ -291,43 +402,33 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
     size_type const vol = s_.volume[slot_];
     size_type const cur_surf = s_.surface[slot_];
 
-    auto calc_dist = [&](size_type surf) -> double {
-        // Returns +inf if no valid crossing
-        if (surf == cur_surf)
-            return INFINITY;
-        PlaneRecord const& pl = p_.planes[surf];
-        double n_dir = dir[pl.axis];
-        if (n_dir != 0)
-        {
-            double d = (pl.position - pos[pl.axis]) / n_dir;
-            if (d > 0)
-                return d;
-        }
-        return INFINITY;
-    };
-
     size_type hit_surf = invalid_id;
     double hit_dist = max_step;
     std::int8_t hit_sense = 0;
 
     if (vol != p_.background)
     {
-        // Simple (convex) box volume: first minimum over faces in order
-        BoxVolume const& box = p_.boxes[vol];
+        // Volume of face conjunctions: first minimum over the faces'
+        // intersections in face order
+        VolumeRecord const& v = p_.volumes[vol];
         double best = INFINITY;
-        int best_face = -1;
-        for (int f = 0; f < 6; ++f)
+        size_type best_face = invalid_id;
+        for (size_type f = 0; f < v.num_faces; ++f)
         {
-            double d = calc_dist(box.faces[f]);
-            if (d <= max_step && d < best)
+            double d[2];
+            this->intersect(v.faces[f], pos, dir, v.faces[f] == cur_surf, d);
+            for (int k = 0; k < 2; ++k)
             {
-                best = d;
-                best_face = f;
+                if (d[k] <= max_step && d[k] < best)
+                {
+                    best = d[k];
+                    best_face = f;
+                }
             }
         }
-        if (best_face >= 0)
+        if (best_face != invalid_id)
         {
-            hit_surf = box.faces[best_face];
+            hit_surf = v.faces[best_face];
             hit_dist = best;
             if (hit_surf == cur_surf)
             {
@@ -335,7 +436,7 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
             }
             else
             {
-                hit_sense = sense_outside(this->plane_q(hit_surf, pos)) ? 1 : -1;
+                hit_sense = sense_outside(this->surface_q(hit_surf, pos)) ? 1 : -1;
             }
         }
     }
@@ -347,7 +448,8 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
         // alone, so the first accepted crossing is the (distance, surface)
         // minimum over accepted crossings: one pass over the surfaces, testing
         // only candidates that would improve the current best, gives the same
-        // hit with one distance per surface instead of one scan per crossing.
+        // hit with one intersection per surface instead of one scan per
+        // crossing.
         double bump = p_.tol_abs;
         for (int i = 0; i < 3; ++i)
         {
@@ -355,52 +457,59 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
         }
         for (size_type surf = 0; surf < p_.num_surfaces; ++surf)
         {
-            double const d = calc_dist(surf);
-            if (!(d <= max_step))
-                continue;
-            if (hit_surf != invalid_id
-                && !(d < hit_dist || (d == hit_dist && surf < hit_surf)))
+            double dd[2];
+            this->intersect(surf, pos, dir, surf == cur_surf, dd);
+            for (int k = 0; k < 2; ++k)
             {
-                continue;
-            }
-            Real3 bumped = pos;
-            axpy(d + bump, dir, &bumped);
-            // Neighbors of this surface
-            size_type nbeg = p_.neighbor_offset[surf];
-            size_type nend = p_.neighbor_offset[surf + 1];
-            bool found = false;
-            bool found_outside = false;
-            if (nend - nbeg >= 3)
-            {
-                // Many neighbors: locate by position (non-overlapping boxes)
-                size_type v = this->find_volume_at(
-                    bumped, invalid_id, invalid_id, nullptr);
-                if (v != p_.background && v != p_.exterior)
+                double const d = dd[k];
+                if (!(d <= max_step))
+                    continue;
+                if (hit_surf != invalid_id
+                    && !(d < hit_dist || (d == hit_dist && surf < hit_surf)))
                 {
-                    found = true;
-                    // Sense of the crossed surface evaluated at the bumped
-                    // point inside the new volume, flipped
-                    found_outside = !sense_outside(this->plane_q(surf, bumped));
+                    continue;
                 }
-            }
-            else
-            {
-                for (size_type n = nbeg; n < nend; ++n)
+                Real3 bumped = pos;
+                axpy(d + bump, dir, &bumped);
+                // Neighbors of this surface
+                size_type nbeg = p_.neighbor_offset[surf];
+                size_type nend = p_.neighbor_offset[surf + 1];
+                bool found = false;
+                bool found_outside = false;
+                if (nend - nbeg >= 3)
                 {
-                    size_type v = p_.neighbors[n];
-                    if (this->volume_inside(v, bumped, invalid_id, false, nullptr))
+                    // Many neighbors: locate by position (non-overlapping)
+                    size_type v = this->find_volume_at(
+                        bumped, invalid_id, invalid_id, nullptr);
+                    if (v != p_.background && v != p_.exterior)
                     {
                         found = true;
-                        found_outside = !sense_outside(this->plane_q(surf, bumped));
-                        break;
+                        // Sense of the crossed surface evaluated at the
+                        // bumped point inside the new volume, flipped
+                        found_outside
+                            = !sense_outside(this->surface_q(surf, bumped));
                     }
                 }
-            }
-            if (found)
-            {
-                hit_surf = surf;
-                hit_dist = d;
-                hit_sense = found_outside ? 1 : -1;
+                else
+                {
+                    for (size_type n = nbeg; n < nend; ++n)
+                    {
+                        size_type v = p_.neighbors[n];
+                        if (this->volume_inside(v, bumped, invalid_id, false, nullptr))
+                        {
+                            found = true;
+                            found_outside
+                                = !sense_outside(this->surface_q(surf, bumped));
+                            break;
+                        }
+                    }
+                }
+                if (found)
+                {
+                    hit_surf = surf;
+                    hit_dist = d;
+                    hit_sense = found_outside ? 1 : -1;
+                }
             }
         }
     }
@@ -486,10 +595,23 @@ GBX_FUNCTION void GeoTrackView::set_dir(Real3 const& newdir)
     size_type const surf = s_.surface[slot_];
     if (surf != invalid_id)
     {
-        // Normal of an axis-aligned plane is the unit axis vector
-        int axis = p_.planes[surf].axis;
+        // Sign of the direction along the surface normal: the unit axis for
+        // a plane, (x, y, 0) for a z cylinder
+        SurfaceRecord const& sr = p_.surfaces[surf];
         Real3 const olddir = this->dir();
-        if ((newdir[axis] >= 0) != (olddir[axis] >= 0))
+        double n_new, n_old;
+        if (sr.type == surf_czc)
+        {
+            Real3 const pos = this->pos();
+            n_new = newdir.x * pos.x + newdir.y * pos.y;
+            n_old = olddir.x * pos.x + olddir.y * pos.y;
+        }
+        else
+        {
+            n_new = newdir[sr.type];
+            n_old = olddir[sr.type];
+        }
+        if ((n_new >= 0) != (n_old >= 0))
         {
             s_.boundary[slot_] = (s_.boundary[slot_] == boundary_exiting)
                                      ? boundary_reentrant
@@ -508,17 +630,17 @@ GBX_FUNCTION double GeoTrackView::find_safety() const
     double result = INFINITY;
     if (vol != p_.background)
     {
-        BoxVolume const& box = p_.boxes[vol];
-        for (int f = 0; f < 6; ++f)
+        VolumeRecord const& v = p_.volumes[vol];
+        for (size_type f = 0; f < v.num_faces; ++f)
         {
-            result = min_of(result, std::fabs(this->plane_q(box.faces[f], pos)));
+            result = min_of(result, this->surface_safety(v.faces[f], pos));
         }
     }
     else
     {
         for (size_type s = 0; s < p_.num_surfaces; ++s)
         {
-            result = min_of(result, std::fabs(this->plane_q(s, pos)));
+            result = min_of(result, this->surface_safety(s, pos));
         }
     }
     return result;

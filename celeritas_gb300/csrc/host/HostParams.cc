@@ -204,6 +204,7 @@ class Builder
     void build_materials();
     void build_physics();
     void build_models();
+    void build_element_tables();
     void build_geometry();
 };
 
@@ -795,30 +796,42 @@ void Builder::build_msc_field()
 
 void Builder::build_geometry()
 {
-    // Surfaces: world box faces, then each box's faces in insertion order,
-    // deduplicated against existing planes (first inserted wins). Each box
-    // face is placed at center +/- half-width, as a translated box.
-    auto add_plane = [this](int axis, double pos) -> size_type {
-        for (size_type i = 0; i < hp_.planes.size(); ++i)
+    // Surfaces: world box faces, then each volume's surfaces in insertion
+    // order, deduplicated against existing surfaces (first inserted wins).
+    // Each box face is placed at center +/- half-width, as a translated box;
+    // a shell inserts its z planes, outer cylinder, then inner cylinder.
+    auto add_surface = [this](int type, double value) -> size_type {
+        for (size_type i = 0; i < hp_.surfaces.size(); ++i)
         {
-            auto const& pl = hp_.planes[i];
-            if (pl.axis == axis
-                && std::fabs(pl.position - pos)
-                       <= 1e-8 * std::max(1.0, std::fabs(pos)))
+            auto const& sr = hp_.surfaces[i];
+            if (sr.type == type
+                && std::fabs(sr.value - value)
+                       <= 1e-8 * std::max(1.0, std::fabs(value)))
             {
                 return i;
             }
         }
-        hp_.planes.push_back({axis, pos});
-        return static_cast<size_type>(hp_.planes.size() - 1);
+        hp_.surfaces.push_back({type, value});
+        return static_cast<size_type>(hp_.surfaces.size() - 1);
     };
     auto box_faces = [&](double const* lo, double const* hi, size_type* faces) {
         for (int ax = 0; ax < 3; ++ax)
         {
             double half = (hi[ax] - lo[ax]) / 2;
             double center = (hi[ax] + lo[ax]) / 2;
-            faces[2 * ax] = add_plane(ax, -half + center);
-            faces[2 * ax + 1] = add_plane(ax, half + center);
+            faces[2 * ax] = add_surface(ax, -half + center);
+            faces[2 * ax + 1] = add_surface(ax, half + center);
+        }
+    };
+    // Faces sorted by surface ID with their inside senses
+    auto set_faces = [](VolumeRecord* vr,
+                        std::vector<std::pair<size_type, std::int8_t>> fs) {
+        std::sort(fs.begin(), fs.end());
+        vr->num_faces = static_cast<size_type>(fs.size());
+        for (size_type f = 0; f < fs.size(); ++f)
+        {
+            vr->faces[f] = fs[f].first;
+            vr->inside_sense[f] = fs[f].second;
         }
     };
 
@@ -830,55 +843,79 @@ void Builder::build_geometry()
         g.world_faces[f] = world[f];
         g.world_sense[f] = (f % 2 == 0) ? 1 : -1;
     }
+    if (!geo_.boxes.empty() && !geo_.shells.empty())
+        throw std::runtime_error("a geometry holds either boxes or shells");
 
-    // Volumes: exterior (0), boxes (1..n), background (n+1)
-    size_type const nbox = static_cast<size_type>(geo_.boxes.size());
-    hp_.boxes.resize(nbox + 2);
+    // Volumes: exterior (0), boxes or shells (1..n), background (n+1)
+    size_type const nvol
+        = static_cast<size_type>(geo_.boxes.size() + geo_.shells.size());
+    hp_.volumes.resize(nvol + 2);
     hp_.volume_labels.push_back("[EXTERIOR]");
     hp_.volume_material.push_back(invalid_id);
-    for (size_type b = 0; b < nbox; ++b)
+    std::vector<std::string> labels;
+    for (size_type b = 0; b < geo_.boxes.size(); ++b)
     {
         BoxSpec const& spec = geo_.boxes[b];
         size_type faces[6];
         box_faces(spec.lo, spec.hi, faces);
-        // Faces sorted by surface ID, senses: lower planes need pos >= plane
+        // Lower planes need pos >= plane
         std::vector<std::pair<size_type, std::int8_t>> fs;
         for (int f = 0; f < 6; ++f)
             fs.push_back({faces[f], static_cast<std::int8_t>(f % 2 == 0 ? 1 : -1)});
-        std::sort(fs.begin(), fs.end());
-        BoxVolume& bv = hp_.boxes[b + 1];
-        for (int f = 0; f < 6; ++f)
-        {
-            bv.faces[f] = fs[f].first;
-            bv.inside_sense[f] = fs[f].second;
-        }
-        bv.material = spec.material;
-        hp_.volume_labels.push_back(spec.label);
+        VolumeRecord& vr = hp_.volumes[b + 1];
+        set_faces(&vr, fs);
+        vr.material = spec.material;
+        labels.push_back(spec.label);
         hp_.volume_material.push_back(spec.material);
     }
+    for (size_type k = 0; k < geo_.shells.size(); ++k)
+    {
+        ShellSpec const& spec = geo_.shells[k];
+        if (!(0 < spec.r_in && spec.r_in < spec.r_out && spec.z_lo < spec.z_hi))
+            throw std::runtime_error("invalid shell '" + spec.label + "'");
+        size_type zlo = add_surface(surf_pz, spec.z_lo);
+        size_type zhi = add_surface(surf_pz, spec.z_hi);
+        size_type cout = add_surface(surf_czc, spec.r_out * spec.r_out);
+        size_type cin = add_surface(surf_czc, spec.r_in * spec.r_in);
+        VolumeRecord& vr = hp_.volumes[k + 1];
+        set_faces(&vr, {{zlo, 1}, {zhi, -1}, {cout, -1}, {cin, 1}});
+        vr.material = spec.material;
+        labels.push_back(spec.label);
+        hp_.volume_material.push_back(spec.material);
+    }
+    hp_.volume_labels.insert(hp_.volume_labels.end(), labels.begin(), labels.end());
     hp_.volume_labels.push_back("world");
     hp_.volume_material.push_back(geo_.background_material);
 
-    // Box lookup along the stack axis requires the lower face in slot 4
-    for (size_type b = 1; b <= nbox; ++b)
+    if (geo_.shells.empty())
     {
-        BoxVolume const& bv = hp_.boxes[b];
-        auto const& pl = hp_.planes[bv.faces[4]];
-        if (pl.axis != geo_.stack_axis || bv.inside_sense[4] != 1)
-            throw std::runtime_error("boxes must be layered along the stack axis");
-        if (b > 1
-            && !(hp_.planes[hp_.boxes[b - 1].faces[4]].position < pl.position))
-            throw std::runtime_error("boxes must be sorted along the stack axis");
+        // Box lookup along z requires the lower z face in slot 4 and boxes
+        // sorted by it
+        g.locate = locate_stack_z;
+        for (size_type b = 1; b <= nvol; ++b)
+        {
+            VolumeRecord const& vr = hp_.volumes[b];
+            auto const& sr = hp_.surfaces[vr.faces[4]];
+            if (sr.type != surf_pz || vr.inside_sense[4] != 1)
+                throw std::runtime_error("boxes must be layered along z");
+            if (b > 1
+                && !(hp_.surfaces[hp_.volumes[b - 1].faces[4]].value < sr.value))
+                throw std::runtime_error("boxes must be sorted along z");
+        }
+    }
+    else
+    {
+        g.locate = locate_scan;
     }
 
     // Connectivity: volumes owning each surface
-    size_type const nsurf = static_cast<size_type>(hp_.planes.size());
+    size_type const nsurf = static_cast<size_type>(hp_.surfaces.size());
     std::vector<std::vector<size_type>> conn(nsurf);
     for (int f = 0; f < 6; ++f)
         conn[world[f]].push_back(0);
-    for (size_type b = 1; b <= nbox; ++b)
-        for (int f = 0; f < 6; ++f)
-            conn[hp_.boxes[b].faces[f]].push_back(b);
+    for (size_type b = 1; b <= nvol; ++b)
+        for (size_type f = 0; f < hp_.volumes[b].num_faces; ++f)
+            conn[hp_.volumes[b].faces[f]].push_back(b);
     hp_.neighbor_offset.push_back(0);
     for (auto const& c : conn)
     {
@@ -886,22 +923,86 @@ void Builder::build_geometry()
         hp_.neighbor_offset.push_back(static_cast<size_type>(hp_.neighbors.size()));
     }
 
-    // Detectors: every box, in order
-    hp_.volume_detector.assign(nbox + 2, invalid_id);
-    for (size_type b = 1; b <= nbox; ++b)
+    // Detectors: every volume, in order
+    hp_.volume_detector.assign(nvol + 2, invalid_id);
+    for (size_type b = 1; b <= nvol; ++b)
     {
         hp_.volume_detector[b] = b - 1;
-        hp_.detector_labels.push_back(geo_.boxes[b - 1].label);
+        hp_.detector_labels.push_back(labels[b - 1]);
     }
 
     g.num_surfaces = nsurf;
-    g.num_volumes = nbox + 2;
+    g.num_volumes = nvol + 2;
     g.exterior = 0;
-    g.background = nbox + 1;
-    g.stack_axis = geo_.stack_axis;
+    g.background = nvol + 1;
     g.tol_rel = 1.5e-8;
     g.tol_abs = 1.5e-8;
-    hp_.scalars.num_detectors = nbox;
+    hp_.scalars.num_detectors = nvol;
+}
+
+void Builder::build_element_tables()
+{
+    // For each model with imported per-element micro cross sections and
+    // each material of more than one element: the element-fraction-weighted
+    // cumulative cross section, normalized to 1 in each energy bin, one grid
+    // per element component (PhysicsParams::build_model_xs,
+    // src/celeritas/phys/PhysicsParams.cc:638-768)
+    size_type const nmat = static_cast<size_type>(hp_.materials.size());
+    size_type const npar = static_cast<size_type>(hp_.particles.size());
+    std::vector<size_type> index(std::size_t(model_size) * npar * nmat, invalid_id);
+    auto build = [&](size_type model, size_type particle, std::string const& prefix) {
+        for (size_type mi = 0; mi < nmat; ++mi)
+        {
+            MaterialRecord const& m = hp_.materials[mi];
+            std::string p = prefix + "." + std::to_string(mi);
+            if (m.num_elements <= 1 || !kv_.has(p + ".energy"))
+                continue;
+            auto energy = kv_.dbl(p + ".energy");
+            // Micro cross sections are listed in the input's element order
+            auto file_els = kv_.dbl("material." + std::to_string(mi) + ".elements");
+            std::vector<std::vector<double>> xs(m.num_elements);
+            for (size_type j = 0; j < m.num_elements; ++j)
+            {
+                std::size_t k = 0;
+                while (k < file_els.size()
+                       && static_cast<size_type>(file_els[k]) != m.element[j])
+                    ++k;
+                if (k == file_els.size())
+                    throw std::runtime_error("element missing from micro xs");
+                xs[j] = kv_.dbl(p + ".micro." + std::to_string(k));
+                if (xs[j].size() != energy.size())
+                    throw std::runtime_error("bad micro xs size");
+            }
+            for (std::size_t bin = 0; bin < energy.size(); ++bin)
+            {
+                double cum_xs = 0;
+                for (size_type j = 0; j < m.num_elements; ++j)
+                {
+                    cum_xs += xs[j][bin] * m.fraction[j];
+                    xs[j][bin] = cum_xs;
+                }
+                if (cum_xs > 0)
+                {
+                    for (size_type j = 0; j < m.num_elements; ++j)
+                        xs[j][bin] /= cum_xs;
+                }
+            }
+            std::vector<size_type> grid_ids(m.num_elements);
+            for (size_type j = 0; j < m.num_elements; ++j)
+                grid_ids[j] = this->add_log_grid(energy, xs[j]);
+            index[(std::size_t(model) * npar + particle) * nmat + mi]
+                = this->add_ints(grid_ids);
+        }
+    };
+    ParamsData const& s = hp_.scalars;
+    build(model_bethe_heitler, s.gamma_id, "model.22.conversion.bethe_heitler");
+    for (size_type pid : {s.electron_id, s.positron_id})
+    {
+        std::string pdg = pid == s.electron_id ? "11" : "-11";
+        build(model_seltzer_berger, pid, "model." + pdg + ".e_brems.e_brems_sb");
+        build(model_rel_brems, pid, "model." + pdg + ".e_brems.e_brems_lpm");
+    }
+    hp_.scalars.element_tables = this->add_ints(index);
 }
 
 HostParams Builder::build()
@@ -913,12 +1014,18 @@ HostParams Builder::build()
     this->build_materials();
     this->build_physics();
     this->build_models();
+    this->build_element_tables();
     this->build_msc_field();
     this->build_geometry();
     for (auto const& b : geo_.boxes)
     {
         if (b.material >= hp_.materials.size())
             throw std::runtime_error("box material out of range");
+    }
+    for (auto const& sh : geo_.shells)
+    {
+        if (sh.material >= hp_.materials.size())
+            throw std::runtime_error("shell material out of range");
     }
     return std::move(hp_);
 }
@@ -939,7 +1046,6 @@ GeometrySpec make_calorimeter_geometry(int num_layers,
     g.world_lo[2] = -10;
     g.world_hi[2] = 50;
     g.background_material = 0;
-    g.stack_axis = 2;
     for (int k = 0; k < num_layers; ++k)
     {
         double z0 = k * pitch;
@@ -957,6 +1063,46 @@ GeometrySpec make_calorimeter_geometry(int num_layers,
         g.boxes.push_back(ar);
     }
     return g;
+}
+
+GeometrySpec make_cms_geometry()
+{
+    GeometrySpec g;
+    g.name = "cms";
+    g.world_lo[0] = g.world_lo[1] = -310;
+    g.world_hi[0] = g.world_hi[1] = 310;
+    g.world_lo[2] = -320;
+    g.world_hi[2] = 320;
+    g.background_material = 0;
+    // Silicon tracker: 10 layers of 0.3 mm, inner radii evenly from 4 to 110
+    constexpr int num_si = 10;
+    for (int k = 0; k < num_si; ++k)
+    {
+        double r = 4.0 + k * (110.0 - 4.0) / (num_si - 1);
+        g.shells.push_back({"si_" + std::to_string(k), r, r + 0.03, -270, 270, 1});
+    }
+    // Electromagnetic calorimeter: PbWO4 crystals
+    g.shells.push_back({"ecal", 129, 152, -300, 300, 2});
+    // Hadron calorimeter: 17 brass + scintillator pairs between 180 and 295
+    constexpr int num_hcal = 17;
+    double const pitch = (295.0 - 180.0) / num_hcal;
+    for (int k = 0; k < num_hcal; ++k)
+    {
+        double r = 180.0 + k * pitch;
+        g.shells.push_back({"brass_" + std::to_string(k), r, r + 5.0, -300, 300, 3});
+        g.shells.push_back(
+            {"scint_" + std::to_string(k), r + 5.0, r + 5.4, -300, 300, 4});
+    }
+    return g;
+}
+
+GeometrySpec make_geometry(std::string const& name)
+{
+    if (name == "calo")
+        return make_calorimeter_geometry();
+    if (name == "cms")
+        return make_cms_geometry();
+    throw std::runtime_error("unknown geometry '" + name + "'");
 }
 
 HostParams build_params(std::string const& physics_path,
@@ -987,8 +1133,8 @@ ParamsData make_host_view(HostParams const& hp)
     p.msc.material = hp.msc_materials.data();
     p.msc.par_mat = hp.msc_par_mat.data();
     p.looping = hp.looping.data();
-    p.geo.planes = hp.planes.data();
-    p.geo.boxes = hp.boxes.data();
+    p.geo.surfaces = hp.surfaces.data();
+    p.geo.volumes = hp.volumes.data();
     p.geo.neighbor_offset = hp.neighbor_offset.data();
     p.geo.neighbors = hp.neighbors.data();
     p.geo.volume_material = hp.volume_material.data();

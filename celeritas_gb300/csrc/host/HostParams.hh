@@ -18,7 +18,19 @@ struct BoxSpec
     size_type material;
 };
 
-//! Boxes (non-overlapping, sorted along the stacking axis) in a world box
+//! Cylindrical shell about the z axis: r_in < r < r_out, z_lo < z < z_hi
+struct ShellSpec
+{
+    std::string label;
+    double r_in;
+    double r_out;
+    double z_lo;
+    double z_hi;
+    size_type material;
+};
+
+//! Non-overlapping volumes in a world box: either boxes (sorted along z) or
+//! cylindrical shells
 struct GeometrySpec
 {
     std::string name;
@@ -26,7 +38,7 @@ struct GeometrySpec
     double world_hi[3];
     size_type background_material{0};
     std::vector<BoxSpec> boxes;
-    int stack_axis{2};
+    std::vector<ShellSpec> shells;
 };
 
 //! Sampling calorimeter: layers of (absorber, gap) along +z
@@ -34,6 +46,16 @@ GeometrySpec make_calorimeter_geometry(int num_layers = 50,
                                        double absorber = 0.23,
                                        double gap = 0.57,
                                        double half_xy = 20.0);
+
+//! CMS-like detector of concentric shells about z: 10 silicon layers
+//! (0.3 mm, r = 4-110 cm, |z| < 270 cm), a PbWO4 barrel (r = 129-152 cm,
+//! |z| < 300 cm) and 17 brass (5 cm) / plastic scintillator (0.4 cm) pairs
+//! (r = 180-295 cm, |z| < 300 cm) in a vacuum world box. Materials: 0
+//! vacuum, 1 Si, 2 PbWO4, 3 brass, 4 scintillator.
+GeometrySpec make_cms_geometry();
+
+//! Geometry by name: "calo" or "cms"
+GeometrySpec make_geometry(std::string const& name);
 
 //! Options mirroring celer-sim's RunnerInput physics/transport knobs
 struct ParamsOptions
@@ -68,8 +90,8 @@ struct HostParams
     std::vector<UrbanMscParMatRecord> msc_par_mat;
     std::vector<LoopingRecord> looping;
     // Geometry
-    std::vector<PlaneRecord> planes;
-    std::vector<BoxVolume> boxes;
+    std::vector<SurfaceRecord> surfaces;
+    std::vector<VolumeRecord> volumes;
     std::vector<size_type> neighbor_offset;
     std::vector<size_type> neighbors;
     std::vector<size_type> volume_material;

@@ -95,6 +95,10 @@ def log_grid(emin: float, emax: float) -> np.ndarray:
 class Mat:
     def __init__(self, name):
         density, state, comp = MATERIALS[name]
+        # Components in increasing element order, the order in which the
+        # reference stores a material's components (and so pairs them with
+        # the per-element micro cross sections)
+        comp = sorted(comp, key=lambda c: ELEMENTS[c[0]][0])
         self.name, self.density, self.state = name, density, state
         self.els = [e for e, _ in comp]
         self.frac = np.array([f for _, f in comp])

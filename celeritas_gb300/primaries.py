@@ -59,3 +59,28 @@ def write_primaries_text(path: str, primaries: np.ndarray):
             vals += [repr(float(v)) for v in p["dir"]]
             vals += [repr(float(p["time"])), str(int(p["event"]))]
             f.write(f"{int(p['pdg'])} " + " ".join(vals) + "\n")
+
+
+def eta_beam(num: int, emin: float = 1000.0, emax: float | None = None,
+             pdgs=(11, 22), eta_max: float = 1.5, seed: int = 0,
+             num_events: int = 1) -> np.ndarray:
+    """Primaries from the origin, directions isotropic in azimuth and uniform
+    in pseudorapidity |eta| < eta_max; energies log-uniform in [emin, emax]
+    MeV (fixed at emin if emax is None); particle types cycle through pdgs;
+    events assigned in blocks of num / num_events."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(num, dtype=PRIMARY_DTYPE)
+    p["pdg"] = np.array(pdgs)[np.arange(num) % len(pdgs)]
+    if emax is None:
+        p["energy"] = emin
+    else:
+        p["energy"] = np.exp(rng.uniform(np.log(emin), np.log(emax), num))
+    eta = rng.uniform(-eta_max, eta_max, num)
+    phi = rng.uniform(0.0, 2 * np.pi, num)
+    theta = 2 * np.arctan(np.exp(-eta))
+    p["dir"][:, 0] = np.sin(theta) * np.cos(phi)
+    p["dir"][:, 1] = np.sin(theta) * np.sin(phi)
+    p["dir"][:, 2] = np.cos(theta)
+    per_event = max(1, -(-num // max(num_events, 1)))
+    p["event"] = np.arange(num) // per_event
+    return p

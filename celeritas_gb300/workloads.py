@@ -16,7 +16,7 @@ PrimaryGenerator (src/celeritas/phys/PrimaryGenerator.cc).
 
 from __future__ import annotations
 
-from .primaries import pencil_beam, spread_beam
+from .primaries import eta_beam, pencil_beam, spread_beam
 
 WORKLOADS = {
     "c1": dict(geometry="calo", physics="calo", num_primaries=100, energy=1000.0,
@@ -30,12 +30,29 @@ WORKLOADS = {
                description="calorimeter 50x(2.3mm Pb+5.7mm lAr), Urban MSC, 1 T "
                            "uniform field along x, 10^4 e- log-uniform 0.1-10 GeV, "
                            "sigma 1 cm, 2^20 track slots, FP64"),
+    # CMS-like detector (concentric shells, 3.8 T along z): 1300 events of
+    # 50 primaries, e-/gamma alternating, log-uniform 1-100 GeV, uniform in
+    # |eta| < 1.5 from the origin, 2^21 slots
+    "c3": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
+               emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
+               seed=0, events=1300, msc=True, field=(0.0, 0.0, 3.8),
+               description="CMS-like: 10 Si shells (0.3 mm, r 4-110 cm), PbWO4 barrel "
+                           "(r 129-152 cm), 17 x (5 cm brass + 0.4 cm scintillator) "
+                           "(r 180-295 cm), 3.8 T along z, Urban MSC; 1300 events x 50 "
+                           "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots"),
 }
 
 
 def make_primaries(wl: dict, rank: int = 0, num: int | None = None, seed_offset: int = 0):
     """Primaries of a workload; 'rank' offsets the event IDs and the seed."""
     num = wl["num_primaries"] if num is None else num
+    if wl.get("pdgs"):
+        events = max(1, round(wl["events"] * num / wl["num_primaries"]))
+        p = eta_beam(num, emin=wl["energy"], emax=wl["emax"], pdgs=wl["pdgs"],
+                     eta_max=wl["eta_max"], seed=wl["seed"] + 1000 * rank + seed_offset,
+                     num_events=events)
+        p["event"] += rank * wl["events"]
+        return p
     if wl["emax"] is None:
         p = pencil_beam(num, energy=wl["energy"], pdg=wl["pdg"],
                         num_events=min(wl["events"], num))

@@ -286,10 +286,7 @@ int run(int argc, char** argv)
         else if (a == "--quiet")
             quiet = true;
     }
-    if (geo != "calo")
-        throw std::runtime_error("unknown geometry " + geo);
-    HostParams hp
-        = build_params(phys, make_calorimeter_geometry(), physics_options(argc, argv));
+    HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
     size_type max_event = 0;
     for (auto const& pr : primaries)
@@ -354,10 +351,7 @@ int bench(int argc, char** argv)
         if (a == "--threads")
             threads = std::stoul(argv[++i]);
     }
-    if (geo != "calo")
-        throw std::runtime_error("unknown geometry " + geo);
-    HostParams hp
-        = build_params(phys, make_calorimeter_geometry(), physics_options(argc, argv));
+    HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
     // Group primaries by event
     std::map<size_type, std::vector<TrackInitializer>> events;
@@ -429,13 +423,13 @@ int main(int argc, char** argv)
         if (mode == "geo" && argc >= 4)
         {
             // Geometry tables built by the GB300 path's host code
-            HostParams hp = build_params(
-                argv[2], make_calorimeter_geometry(), ParamsOptions{});
-            for (std::size_t i = 0; i < hp.planes.size(); ++i)
+            HostParams hp
+                = build_params(argv[2], make_geometry(argv[3]), ParamsOptions{});
+            for (std::size_t i = 0; i < hp.surfaces.size(); ++i)
                 std::printf("surf %zu axis %d position %.17g\n",
                             i,
-                            hp.planes[i].axis,
-                            hp.planes[i].position);
+                            hp.surfaces[i].type,
+                            hp.surfaces[i].value);
             for (std::size_t i = 0; i < hp.volume_labels.size(); ++i)
                 std::printf("volume %zu %s\n", i, hp.volume_labels[i].c_str());
             return 0;

@@ -39,6 +39,7 @@
 #include "orange/orangeinp/IntersectRegion.hh"
 #include "orange/orangeinp/Shape.hh"
 #include "orange/orangeinp/Transformed.hh"
+#include "orange/orangeinp/Solid.hh"
 #include "orange/orangeinp/UnitProto.hh"
 #include "orange/transform/VariantTransform.hh"
 #include "celeritas/Quantities.hh"
@@ -51,6 +52,7 @@
 #include "celeritas/global/ActionSequence.hh"
 #include "celeritas/global/CoreParams.hh"
 #include "celeritas/global/CoreState.hh"
+#include "celeritas/global/CoreTrackView.hh"
 #include "celeritas/global/Stepper.hh"
 #include "celeritas/global/alongstep/AlongStepGeneralLinearAction.hh"
 #include "celeritas/global/alongstep/AlongStepUniformMscAction.hh"
@@ -462,10 +464,62 @@ GeoSpec build_calo()
     return spec;
 }
 
+//! CMS-like detector of concentric shells about z (the GB300 build's
+//! make_cms_geometry): 10 Si layers of 0.3 mm with inner radii evenly from 4
+//! to 110 cm (|z| < 270), a PbWO4 barrel (129-152 cm, |z| < 300) and 17 brass
+//! (5 cm) + scintillator (0.4 cm) pairs from 180 cm with pitch 115/17 cm
+//! (|z| < 300), in a vacuum world box 620 x 620 x 640 cm.
+GeoSpec build_cms()
+{
+    UnitProto::Input inp;
+    inp.label = "cms";
+    inp.boundary.interior = make_box("world", {-310, -310, -320}, {310, 310, 320});
+    inp.boundary.zorder = ZOrder::exterior;
+    inp.background.fill = GeoMaterialId{0};
+    inp.background.label = Label{"world"};
+
+    GeoSpec spec;
+    spec.label_to_mat["world"] = MaterialId{0};
+    auto add_shell = [&](std::string const& label,
+                         double r_in,
+                         double r_out,
+                         double hz,
+                         int mat) {
+        auto shell = std::make_shared<CylinderSolid>(
+            std::string(label), Cylinder{r_out, hz}, Cylinder{r_in, hz});
+        inp.materials.push_back(
+            {std::move(shell), GeoMaterialId{static_cast<size_type>(mat)}, Label{label}});
+        spec.label_to_mat[label] = MaterialId{static_cast<size_type>(mat)};
+        spec.vol_labels.push_back(label);
+    };
+    for (int k = 0; k < 10; ++k)
+    {
+        double r = 4.0 + k * (110.0 - 4.0) / 9;
+        add_shell("si_" + std::to_string(k), r, r + 0.03, 270, 1);
+    }
+    add_shell("ecal", 129, 152, 300, 2);
+    double const pitch = (295.0 - 180.0) / 17;
+    for (int k = 0; k < 17; ++k)
+    {
+        double r = 180.0 + k * pitch;
+        add_shell("brass_" + std::to_string(k), r, r + 5.0, 300, 3);
+        add_shell("scint_" + std::to_string(k), r + 5.0, r + 5.4, 300, 4);
+    }
+
+    InputBuilder::Options opts;
+    opts.tol = Tolerance<>::from_default();
+    InputBuilder build(std::move(opts));
+    UnitProto global(std::move(inp));
+    spec.geo = std::make_shared<OrangeParams>(build(global));
+    return spec;
+}
+
 GeoSpec build_geometry(std::string const& name)
 {
     if (name == "calo")
         return build_calo();
+    if (name == "cms")
+        return build_cms();
     throw std::runtime_error("unknown geometry " + name);
 }
 
@@ -625,6 +679,43 @@ load_primaries(std::string const& path, ParticleParams const& particles)
     return result;
 }
 
+//! Print every non-inactive track slot (same fields as the port's trace)
+void trace_state(Stepper<MemSpace::host>& step, CoreParams const& core, size_type iter)
+{
+    auto const& st
+        = dynamic_cast<CoreState<MemSpace::host> const&>(step.state());
+    auto const& pref = core.ref<MemSpace::host>();
+    auto const& sref = st.ref();
+    for (size_type i = 0; i < st.size(); ++i)
+    {
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        auto sim = track.make_sim_view();
+        if (sim.status() == TrackStatus::inactive)
+            continue;
+        auto par = track.make_particle_view();
+        auto geo = track.make_geo_view();
+        auto phys = track.make_physics_view();
+        auto pstep = track.make_physics_step_view();
+        auto const& pos = geo.pos();
+        auto const& dir = geo.dir();
+        std::printf("trace %u %u st=%d pid=%u E=%.17g pos=(%.17g,%.17g,%.17g) "
+                    "dir=(%.17g,%.17g,%.17g) vol=%u act=%d len=%.17g mfp=%.17g "
+                    "edep=%.17g nsec=%u\n",
+                    iter,
+                    i,
+                    static_cast<int>(sim.status()),
+                    par.particle_id().unchecked_get(),
+                    par.energy().value(),
+                    pos[0], pos[1], pos[2], dir[0], dir[1], dir[2],
+                    geo.is_outside() ? 0u : geo.volume_id().unchecked_get(),
+                    static_cast<int>(sim.post_step_action().unchecked_get()),
+                    sim.step_length(),
+                    phys.interaction_mfp(),
+                    pstep.energy_deposition().value(),
+                    static_cast<unsigned>(pstep.secondaries().size()));
+    }
+}
+
 int run(int argc, char** argv)
 {
     if (argc < 7)
@@ -641,6 +732,7 @@ int run(int argc, char** argv)
     bool msc = false;
     size_type max_steps = static_cast<size_type>(-1);
     TrackOrder track_order = TrackOrder::none;
+    bool trace = false;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -657,6 +749,8 @@ int run(int argc, char** argv)
             max_steps = std::stoul(argv[++i]);
         else if (a == "--track-order")
             track_order = static_cast<TrackOrder>(std::stoi(argv[++i]));
+        else if (a == "--trace")
+            trace = true;
     }
 
     KvFile kv(phys_path);
@@ -684,6 +778,8 @@ int run(int argc, char** argv)
 
     StepperResult counts = step(make_span(primaries));
     size_type iter = 0;
+    if (trace)
+        trace_state(step, *prob.core, iter);
     unsigned long long track_steps = counts.active;
     std::printf("step %u %u %u %u %u\n",
                 iter,
@@ -694,6 +790,8 @@ int run(int argc, char** argv)
     while (counts && ++iter < max_steps)
     {
         counts = step();
+        if (trace)
+            trace_state(step, *prob.core, iter);
         track_steps += counts.active;
         std::printf("step %u %u %u %u %u\n",
                     iter,

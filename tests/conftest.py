@@ -27,7 +27,20 @@ GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
                 "calo_ep500_n4", "calo_e1000_n100", "calo_e10000_n2",
                 "calo_msc_e1000_n4", "calo_field_e1000_n4", "calo_msc_field_e5000_n2",
                 "calo_msc_field_ep2000_n2", "calo_sorted_both_e1000_n4",
-                "calo_sorted_post_g100_n16", "calo_msc_field_sorted_along_e2000_n2"]
+                "calo_sorted_post_g100_n16", "calo_msc_field_sorted_along_e2000_n2",
+                "cms_mix_e10000_n4", "cms_mix_logu_n6", "cms_sorted_both_mix_e5000_n4"]
+
+
+def case_primaries(case: dict):
+    """Primaries of a golden case (pencil beam along z, or eta-uniform from
+    the origin), as tests/golden/make_golden.py made them."""
+    from celeritas_gb300.primaries import eta_beam, pencil_beam
+
+    if case.get("beam", "pencil") == "eta":
+        return eta_beam(case["num_primaries"], emin=case["energy"], emax=case.get("emax"),
+                        pdgs=tuple(case["pdgs"]), seed=case["beam_seed"])
+    return pencil_beam(case["num_primaries"], energy=case["energy"], pdg=case["pdg"],
+                       z0=case.get("z0", -5.0))
 
 
 def case_options(case: dict) -> list[str]:

@@ -26,7 +26,7 @@ sys.path.insert(0, REPO)
 
 import oracle  # noqa: E402
 from celeritas_gb300 import physics_file  # noqa: E402
-from celeritas_gb300.primaries import pencil_beam, write_primaries_text  # noqa: E402
+from celeritas_gb300.primaries import eta_beam, pencil_beam, write_primaries_text  # noqa: E402
 
 # name: primaries (pdg, energy [MeV], count), track slots, seed, msc, field [T]
 CASES = {
@@ -51,7 +51,29 @@ CASES = {
     "calo_msc_field_sorted_along_e2000_n2": dict(pdg=11, energy=2000.0, num=2, slots=65536,
                                                  seed=3, msc=True, field=[1.0, 0.0, 0.0],
                                                  track_order=5),
+    # CMS-like detector: shells about z, 3.8 T along z, Urban MSC; e-/gamma
+    # from the origin, uniform in |eta| < 1.5
+    "cms_mix_e10000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=10000.0,
+                              num=4, slots=65536, seed=0, beam_seed=1, msc=True,
+                              field=[0.0, 0.0, 3.8]),
+    "cms_mix_logu_n6": dict(geometry="cms", beam="eta", pdgs=[22, 11], energy=1000.0,
+                            emax=30000.0, num=6, slots=65536, seed=4, beam_seed=2, msc=True,
+                            field=[0.0, 0.0, 3.8]),
+    "cms_sorted_both_mix_e5000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22],
+                                         energy=5000.0, num=4, slots=16384, seed=9,
+                                         beam_seed=3, msc=True, field=[0.0, 0.0, 3.8],
+                                         track_order=7),
 }
+
+
+def case_primaries(c: dict):
+    """Primaries of a golden case (the case dict as stored in a fixture)."""
+    if c.get("beam", "pencil") == "eta":
+        return eta_beam(c["num_primaries"] if "num_primaries" in c else c["num"],
+                        emin=c["energy"], emax=c.get("emax"), pdgs=tuple(c["pdgs"]),
+                        seed=c["beam_seed"])
+    return pencil_beam(c["num_primaries"] if "num_primaries" in c else c["num"],
+                       energy=c["energy"], pdg=c["pdg"], z0=c.get("z0", -5.0))
 
 
 def case_options(c: dict) -> list[str]:
@@ -69,18 +91,25 @@ def case_options(c: dict) -> list[str]:
 
 def make_case(name: str) -> dict:
     c = CASES[name]
-    prim = pencil_beam(c["num"], energy=c["energy"], pdg=c["pdg"])
+    geometry = c.get("geometry", "calo")
+    case = {"geometry": geometry, "energy": c["energy"],
+            "num_primaries": c["num"], "num_track_slots": c["slots"],
+            "seed": c["seed"], "msc": bool(c.get("msc", False)),
+            "field": list(c.get("field", [0.0, 0.0, 0.0])),
+            "track_order": int(c.get("track_order", 0))}
+    if c.get("beam", "pencil") == "eta":
+        case.update(beam="eta", pdgs=list(c["pdgs"]), emax=c.get("emax"),
+                    beam_seed=c["beam_seed"])
+    else:
+        case.update(beam="pencil", pdg=c["pdg"], z0=-5.0)
+    prim = case_primaries(case)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "primaries.txt")
         write_primaries_text(ptxt, prim)
-        out = oracle.run_reference(physics_file("calo"), ptxt, c["slots"], c["seed"],
-                                   extra=case_options(c))
+        out = oracle.run_reference(physics_file(geometry), ptxt, c["slots"], c["seed"],
+                                   extra=case_options(c), geometry=geometry)
     return {
-        "case": {"geometry": "calo", "pdg": c["pdg"], "energy": c["energy"],
-                 "num_primaries": c["num"], "num_track_slots": c["slots"],
-                 "seed": c["seed"], "z0": -5.0, "msc": bool(c.get("msc", False)),
-                 "field": list(c.get("field", [0.0, 0.0, 0.0])),
-                 "track_order": int(c.get("track_order", 0))},
+        "case": case,
         "actions": [out["actions"][i] for i in sorted(out["actions"])],
         "steps": out["steps"],
         "total_steps": out["total_steps"],

@@ -13,21 +13,22 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, case_options, load_golden
+from conftest import GOLDEN_CASES, case_options, case_primaries, load_golden
 
 import oracle
 from celeritas_gb300 import physics_file
-from celeritas_gb300.primaries import pencil_beam, write_primaries_text
+from celeritas_gb300.primaries import write_primaries_text
 
 
 def run_case(golden):
     c = golden["case"]
-    prim = pencil_beam(c["num_primaries"], energy=c["energy"], pdg=c["pdg"], z0=c["z0"])
+    geometry = c.get("geometry", "calo")
+    prim = case_primaries(c)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
-        return oracle.run_port(physics_file("calo"), ptxt, c["num_track_slots"], c["seed"],
-                               extra=case_options(c))
+        return oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
+                               geometry=geometry, extra=case_options(c))
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
