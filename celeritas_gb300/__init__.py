@@ -43,7 +43,8 @@ class _Primary(ctypes.Structure):
 
 class _ParamsOptions(ctypes.Structure):
     _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int),
-                ("track_order", ctypes.c_uint)]
+                ("track_order", ctypes.c_uint), ("rng_per_track", ctypes.c_int),
+                ("event_tallies", ctypes.c_int)]
 
 
 class _StepResult(ctypes.Structure):
@@ -110,6 +111,10 @@ _PROTOTYPES = [
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
       ctypes.POINTER(ctypes.c_size_t)]),
     ("gbx_stepper_extend_from_secondaries_static", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_event_live", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint), ctypes.c_size_t]),
+    ("gbx_stepper_event_energy_deposition", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int]),
 ]
 
 EXPORTED_SYMBOLS = [name for name, _, _ in _PROTOTYPES]
@@ -164,7 +169,8 @@ class Params:
 
     def __init__(self, physics: str, geometry: str = "calo",
                  field_tesla=(0.0, 0.0, 0.0), msc: bool = False,
-                 track_order: int | str = "none", precision: str = "double"):
+                 track_order: int | str = "none", precision: str = "double",
+                 rng_per_track: bool = False, event_tallies: bool = False):
         lib = load_library(precision=precision)
         self._lib = lib
         self.precision = precision
@@ -176,6 +182,8 @@ class Params:
         if isinstance(track_order, str):
             track_order = TRACK_ORDERS[track_order]
         opts.track_order = int(track_order)
+        opts.rng_per_track = int(rng_per_track)
+        opts.event_tallies = int(event_tallies)
         _check(lib, lib.gbx_params_create(physics.encode(), geometry.encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle
@@ -281,6 +289,21 @@ class Stepper:
 
     def kill_active(self):
         _check(self._lib, self._lib.gbx_stepper_kill_active(self._handle))
+
+    def event_live(self, num_events: int) -> np.ndarray:
+        """Live tracks (slots + queued initializers) of events [0, n)."""
+        out = np.zeros(num_events, dtype=np.uint32)
+        _check(self._lib, self._lib.gbx_stepper_event_live(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), num_events))
+        return out
+
+    def event_energy_deposition(self, num_events: int, clear: bool = False) -> np.ndarray:
+        """Energy deposited in detectors per event [MeV] (event tallies)."""
+        out = np.zeros(num_events, dtype=np.float64)
+        _check(self._lib, self._lib.gbx_stepper_event_energy_deposition(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            num_events, int(clear)))
+        return out
 
     def extend_from_secondaries_static(self):
         """Extend-from-secondaries with the library's static scratch array.

@@ -1,6 +1,7 @@
 // Implementation of the C ABI declared in include/celeritas_gb300.h.
 #include "../../include/celeritas_gb300.h"
 
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -193,6 +194,8 @@ int gbx_params_create(const char* physics_file,
         {
             inp.options.msc = options->msc != 0;
             inp.options.track_order = options->track_order;
+            inp.options.rng_per_track = options->rng_per_track != 0;
+            inp.options.event_tallies = options->event_tallies != 0;
             for (int i = 0; i < 3; ++i)
                 inp.options.field_tesla[i] = options->field_tesla[i];
         }
@@ -333,6 +336,35 @@ int gbx_stepper_insert_primaries(gbx_stepper* stepper,
             st.params().host().scalars, primaries, num_primaries);
         st.state().insert_primaries(inits.data(),
                                     static_cast<gbx::size_type>(inits.size()));
+    });
+}
+
+int gbx_stepper_event_live(gbx_stepper* stepper,
+                           unsigned int* counts,
+                           size_t num_events)
+{
+    return guarded([&] {
+        if (num_events && !counts)
+            throw std::runtime_error("null argument");
+        auto v = stepper->stepper->state().event_live(
+            static_cast<gbx::size_type>(num_events));
+        std::copy(v.begin(), v.end(), counts);
+    });
+}
+
+int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
+                                        double* out,
+                                        size_t num_events,
+                                        int clear)
+{
+    return guarded([&] {
+        if (num_events && !out)
+            throw std::runtime_error("null argument");
+        if (!stepper->stepper->params().host().scalars.event_tallies)
+            throw std::runtime_error("per-event tallies are not enabled");
+        auto v = stepper->stepper->state().event_energy_deposition(
+            static_cast<gbx::size_type>(num_events), clear != 0);
+        std::copy(v.begin(), v.end(), out);
     });
 }
 

@@ -1,6 +1,7 @@
 // Device-side implementation of the host API: parameter upload, state
 // allocation, the registered step actions and the graph-replayed stepper.
 #include "../host/Core.hh"
+#include "../gbx/Random.hh"
 
 #include <algorithm>
 #include <cstring>
@@ -350,7 +351,7 @@ CoreState::CoreState(CoreParams const& params,
                      size_type initializer_capacity,
                      size_type max_events,
                      cudaStream_t stream)
-    : stream_(stream)
+    : seed_(seed), stream_(stream)
 {
     if (num_track_slots == 0)
         throw std::runtime_error("number of track slots must be positive");
@@ -392,6 +393,8 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_vac = arr(4), o_cnts = arr(4), o_parents = arr(4);
     std::size_t o_inits = L.reserve(sizeof(TrackInitializer) * std::size_t(init_cap));
     std::size_t o_tcount = L.reserve(4 * std::size_t(max_events));
+    std::size_t o_evedep = L.reserve(8 * std::size_t(max_events));
+    std::size_t o_evlive = L.reserve(4 * std::size_t(max_events));
     std::size_t o_secs = L.reserve(sizeof(Secondary) * std::size_t(sec_cap));
     std::size_t o_det = arr(4);
     std::size_t o_calo = L.reserve(8 * std::size_t(std::max<size_type>(ndet, 1)));
@@ -470,6 +473,8 @@ CoreState::CoreState(CoreParams const& params,
     s.initializers = static_cast<TrackInitializer*>(at(o_inits));
     s.initializer_capacity = init_cap;
     s.track_counters = static_cast<size_type*>(at(o_tcount));
+    s.event_edep = static_cast<double*>(at(o_evedep));
+    s.event_live = static_cast<size_type*>(at(o_evlive));
     s.max_events = max_events;
     s.secondaries = static_cast<Secondary*>(at(o_secs));
     s.secondary_capacity = sec_cap;
@@ -558,12 +563,64 @@ void CoreState::insert_primaries(TrackInitializer const* host_primaries, size_ty
     // Stage through pinned memory so the copy is asynchronous
     GBX_CUDA(cudaStreamSynchronize(stream_));
     std::memcpy(pinned_primaries_, host_primaries, sizeof(TrackInitializer) * n);
+    for (size_type i = 0; i < n; ++i)
+    {
+        TrackInitializer& ti = pinned_primaries_[i];
+        if (ti.event_id >= ref_.max_events)
+            throw std::runtime_error("primary event ID " + std::to_string(ti.event_id)
+                                     + " exceeds the stepper's event capacity "
+                                     + std::to_string(ref_.max_events));
+        // Seed of a per-track random stream: the stepper seed, the event
+        // and the primary's index among that event's primaries
+        size_type const index = primaries_per_event_[ti.event_id]++;
+        SplitMix64 sm{(std::uint64_t(seed_) << 32) | ti.event_id};
+        SplitMix64 sm2{sm() + 0x9e3779b97f4a7c15ull * (std::uint64_t(index) + 1)};
+        ti.rng_key = sm2();
+    }
     GBX_CUDA(cudaMemcpyAsync(ref_.primaries,
                              pinned_primaries_,
                              sizeof(TrackInitializer) * n,
                              cudaMemcpyHostToDevice,
                              stream_));
     pending_primaries_ = n;
+}
+
+std::vector<size_type> CoreState::event_live(size_type n) const
+{
+    if (n > ref_.max_events)
+        throw std::runtime_error("more events requested than the stepper holds");
+    std::vector<size_type> out(n);
+    if (n == 0)
+        return out;
+    launch_count_event_live(ctx_, n, stream_);
+    GBX_CUDA(cudaGetLastError());
+    GBX_CUDA(cudaMemcpyAsync(out.data(),
+                             ref_.event_live,
+                             sizeof(size_type) * n,
+                             cudaMemcpyDeviceToHost,
+                             stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return out;
+}
+
+std::vector<double> CoreState::event_energy_deposition(size_type n, bool clear)
+{
+    if (n > ref_.max_events)
+        throw std::runtime_error("more events requested than the stepper holds");
+    std::vector<double> out(n);
+    if (n == 0)
+        return out;
+    GBX_CUDA(cudaMemcpyAsync(out.data(),
+                             ref_.event_edep,
+                             sizeof(double) * n,
+                             cudaMemcpyDeviceToHost,
+                             stream_));
+    if (clear)
+    {
+        GBX_CUDA(cudaMemsetAsync(ref_.event_edep, 0, sizeof(double) * n, stream_));
+    }
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return out;
 }
 
 Counters CoreState::counters() const

@@ -249,13 +249,16 @@ __global__ __launch_bounds__(block_size) void post_kernel(ParamsData p,
             size_type det = s.detector[slot];
             if (det != invalid_id)
             {
-                atomicAdd(s.calo_edep + det, double(s.energy_deposition[slot]));
+                double const edep = s.energy_deposition[slot];
+                atomicAdd(s.calo_edep + det, edep);
+                if (p.event_tallies)
+                    atomicAdd(s.event_edep + s.event_id[slot], edep);
             }
         }
     }
 }
 
-__global__ __launch_bounds__(block_size) void calo_kernel(ParamsData, StateData s)
+__global__ __launch_bounds__(block_size) void calo_kernel(ParamsData p, StateData s)
 {
     size_type slot = thread_slot();
     if (slot < s.size && s.status[slot] != status_inactive)
@@ -263,8 +266,31 @@ __global__ __launch_bounds__(block_size) void calo_kernel(ParamsData, StateData 
         size_type det = s.detector[slot];
         if (det != invalid_id)
         {
-            atomicAdd(s.calo_edep + det, double(s.energy_deposition[slot]));
+            double const edep = s.energy_deposition[slot];
+            atomicAdd(s.calo_edep + det, edep);
+            if (p.event_tallies)
+                atomicAdd(s.event_edep + s.event_id[slot], edep);
         }
+    }
+}
+
+//! Live tracks per event: occupied slots plus queued initializers
+__global__ void count_event_live_kernel(StateData s, size_type num_events)
+{
+    size_type const stride = gridDim.x * blockDim.x;
+    size_type const tid = thread_slot();
+    for (size_type i = tid; i < s.size; i += stride)
+    {
+        size_type const ev = s.event_id[i];
+        if (s.status[i] != status_inactive && ev < num_events)
+            atomicAdd(s.event_live + ev, size_type(1));
+    }
+    size_type const nq = s.counters->num_initializers;
+    for (size_type i = tid; i < nq; i += stride)
+    {
+        size_type const ev = s.initializers[i].event_id;
+        if (ev < num_events)
+            atomicAdd(s.event_live + ev, size_type(1));
     }
 }
 
@@ -775,6 +801,14 @@ void launch_extend_from_secondaries(LaunchContext const& ctx, cudaStream_t strea
     scan_blocks_kernel<<<1, 1024, 0, stream>>>(
         ctx.state, ctx.scratch, ctx.log, ctx.log_capacity, ctx.step_index);
     scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, ctx.scratch);
+}
+
+void launch_count_event_live(LaunchContext const& ctx,
+                             size_type num_events,
+                             cudaStream_t stream)
+{
+    cudaMemsetAsync(ctx.state.event_live, 0, sizeof(size_type) * num_events, stream);
+    count_event_live_kernel<<<4 * 152, block_size, 0, stream>>>(ctx.state, num_events);
 }
 
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream)

@@ -83,6 +83,11 @@ void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream);
 void launch_extend_from_secondaries(LaunchContext const& ctx,
                                     cudaStream_t stream);
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
+//! Count live tracks (slots and queued initializers) of events [0, n) into
+//! state.event_live
+void launch_count_event_live(LaunchContext const& ctx,
+                             size_type num_events,
+                             cudaStream_t stream);
 //! Stable counting sort of the track slots by action (SortTracksAction):
 //! fills state.track_slots and state.action_offsets
 void launch_sort_tracks(LaunchContext const& ctx, SortKey key, cudaStream_t stream);

@@ -371,6 +371,11 @@ struct ParamsData
     size_type action_klein_nishina;
     size_type action_bethe_heitler;
     size_type action_eplusgg;
+    // Serving: per-track random streams (each track seeded from its parent's
+    // stream, primaries from (seed, event, index)) so that an event's result
+    // does not depend on the other events in flight; per-event tallies
+    bool rng_per_track;
+    bool event_tallies;
     // Track sorting: policy, sort actions (invalid if absent), action count
     unsigned int track_order;
     size_type action_sort_along;
@@ -404,6 +409,8 @@ struct TrackInitializer
     Real3 dir;
     size_type particle_id;
     real_type energy;
+    //! Seed of the track's own random stream (per-track streams only)
+    std::uint64_t rng_key;
 };
 
 //! Device-resident counters (src/celeritas/track/CoreStateCounters.hh:24-47)
@@ -499,6 +506,11 @@ struct StateData
     // Primaries staging
     TrackInitializer* primaries;
     size_type primary_capacity;
+
+    // Per-event energy deposition in detectors and live-track counts
+    // ([max_events]; null without per-event tallies)
+    double* event_edep;
+    size_type* event_live;
 
     // Action-sorted thread -> slot indirection (CoreStateData::track_slots)
     // and the first thread of each action bin, one table per sort key:

@@ -23,6 +23,45 @@ struct RngStateRef
     std::uint32_t* weyl;
 };
 
+//! SplitMix64 (Steele, Lea and Flood 2014; Vigna's constants): a 64-bit
+//! counter-based generator used only to expand a seed into XORWOW states
+struct SplitMix64
+{
+    std::uint64_t state;
+
+    GBX_FORCEINLINE std::uint64_t operator()()
+    {
+        std::uint64_t z = (state += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    }
+};
+
+//! Seed one slot's XORWOW state from a 64-bit key: three SplitMix64 outputs
+//! fill the five xor words and the Weyl word, as the reference's
+//! XorwowRngEngine initializer does (without its subsequence skip-ahead)
+GBX_FORCEINLINE void seed_xorwow(RngStateRef const& ref, size_type slot, std::uint64_t key)
+{
+    SplitMix64 sm{key};
+    std::uint64_t v = sm();
+    ref.s[0][slot] = static_cast<std::uint32_t>(v);
+    ref.s[1][slot] = static_cast<std::uint32_t>(v >> 32);
+    v = sm();
+    ref.s[2][slot] = static_cast<std::uint32_t>(v);
+    ref.s[3][slot] = static_cast<std::uint32_t>(v >> 32);
+    v = sm();
+    ref.s[4][slot] = static_cast<std::uint32_t>(v);
+    ref.weyl[slot] = static_cast<std::uint32_t>(v >> 32);
+    if ((ref.s[0][slot] | ref.s[1][slot] | ref.s[2][slot] | ref.s[3][slot]
+         | ref.s[4][slot])
+        == 0)
+    {
+        // XORWOW's xor words must not all vanish
+        ref.s[0][slot] = 1;
+    }
+}
+
 class XorwowEngine
 {
   public:

@@ -104,6 +104,10 @@ GBX_FUNCTION void init_track(ParamsData const& p,
     s.material[slot] = matid;
     // Physics state reset
     reset_physics_state(s, slot);
+    if (p.rng_per_track)
+    {
+        seed_xorwow(s.rng, slot, init.rng_key);
+    }
 }
 
 //! Flag the slot as vacant or occupied and count secondaries that need a
@@ -157,12 +161,23 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
     size_type const parent_track = s.track_id[slot];
     Secondary const* sec = s.secondaries + s.secondaries_offset[slot];
     size_type const n = s.secondaries_count[slot];
+    // Per-track streams: each secondary's seed is drawn from its parent's
+    // stream, in secondary order, before the slot is reused
+    std::uint64_t in_place_key = 0;
     for (size_type i = 0; i < n; ++i)
     {
         Secondary const& secondary = sec[i];
         if (secondary.particle_id == invalid_id)
             continue;
         TrackInitializer ti;
+        ti.rng_key = 0;
+        if (p.rng_per_track)
+        {
+            XorwowEngine parent_rng(s.rng, slot);
+            std::uint64_t const lo = parent_rng();
+            std::uint64_t const hi = parent_rng();
+            ti.rng_key = (hi << 32) | lo;
+        }
         ti.track_id = make_track_id(s, s.event_id[slot]);
         ti.parent_id = parent_track;
         ti.event_id = s.event_id[slot];
@@ -190,6 +205,7 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
             s.particle_id[slot] = ti.particle_id;
             s.energy[slot] = ti.energy;
             reset_physics_state(s, slot);
+            in_place_key = ti.rng_key;
             initialized = true;
             status = status_initializing;
         }
@@ -202,6 +218,10 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
             }
             --offset;
         }
+    }
+    if (initialized && p.rng_per_track)
+    {
+        seed_xorwow(s.rng, slot, in_place_key);
     }
     if (!initialized && s.status[slot] == status_killed)
     {

@@ -15,6 +15,7 @@
 #include <memory>
 #include <string>
 #include <string_view>
+#include <unordered_map>
 #include <vector>
 
 #include "../device/Kernels.cuh"
@@ -169,6 +170,10 @@ class CoreState
     Counters counters() const;
     //! Number of completed steps recorded on the device
     size_type step_index() const;
+    //! Live tracks (slots and queued initializers) per event [0, n)
+    std::vector<size_type> event_live(size_type n) const;
+    //! Energy deposited in detectors per event [0, n); optionally cleared
+    std::vector<double> event_energy_deposition(size_type n, bool clear);
     //! Read the step log entries [first, first + n)
     std::vector<StepRecord> step_log(size_type first, size_type n) const;
     size_type log_capacity() const { return ctx_.log_capacity; }
@@ -180,6 +185,9 @@ class CoreState
     TrackInitializer* pinned_primaries_{nullptr};
     size_type pinned_capacity_{0};
     size_type pending_primaries_{0};
+    unsigned int seed_{0};
+    //! Primaries inserted so far per event (seeds of per-track streams)
+    std::unordered_map<size_type, size_type> primaries_per_event_;
     cudaStream_t stream_{nullptr};
 };
 

@@ -1017,6 +1017,8 @@ HostParams Builder::build()
     this->build_element_tables();
     this->build_msc_field();
     this->build_geometry();
+    hp_.scalars.rng_per_track = opts_.rng_per_track;
+    hp_.scalars.event_tallies = opts_.event_tallies;
     for (auto const& b : geo_.boxes)
     {
         if (b.material >= hp_.materials.size())

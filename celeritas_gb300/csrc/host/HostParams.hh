@@ -68,6 +68,10 @@ struct ParamsOptions
     double field_tesla[3]{0, 0, 0};
     //! TrackOrder policy (none or one of the action sorts)
     unsigned int track_order{0};
+    //! Per-track random streams (results independent of the other events)
+    bool rng_per_track{false};
+    //! Per-event energy-deposition tallies
+    bool event_tallies{false};
 };
 
 //! All parameter tables in host memory

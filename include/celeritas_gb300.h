@@ -79,6 +79,14 @@ typedef struct
     double field_tesla[3];
     int msc;
     unsigned int track_order;
+    /* Serving options, without counterparts in the reference. Nonzero
+     * rng_per_track gives every track its own random stream, seeded from its
+     * parent's stream (primaries: from the stepper seed, the event ID and
+     * the primary's index within its event), so that an event's result does
+     * not depend on which other events share the stepper. Nonzero
+     * event_tallies accumulates detector energy deposition per event. */
+    int rng_per_track;
+    int event_tallies;
 } gbx_params_options;
 
 /* Build problem parameters from a physics input file and a named geometry
@@ -193,6 +201,22 @@ int gbx_stepper_state_info(gbx_stepper* stepper,
                            const char* field,
                            size_t* elem_bytes,
                            size_t* count);
+
+/* Live tracks per event, for events [0, num_events): occupied track slots
+ * plus queued track initializers; synchronizes the stepper's stream. A
+ * serving loop reads it to detect completed events. No counterpart in the
+ * reference. */
+int gbx_stepper_event_live(gbx_stepper* stepper,
+                           unsigned int* counts,
+                           size_t num_events);
+
+/* Energy deposited in detectors per event [MeV], for events
+ * [0, num_events), with the event_tallies option; 'clear' resets the
+ * tallies after reading. No counterpart in the reference. */
+int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
+                                        double* out,
+                                        size_t num_events,
+                                        int clear);
 
 /* Largest stepper (track slots) accepted by
  * gbx_stepper_extend_from_secondaries_static */

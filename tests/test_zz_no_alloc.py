@@ -56,10 +56,10 @@ PER_SLOT_FIELDS = [
 
 INIT_DTYPE = np.dtype({
     "names": ["track_id", "parent_id", "event_id", "time", "pos", "dir", "particle_id",
-              "energy"],
-    "formats": ["<u4", "<u4", "<u4", "<f8", ("<f8", 3), ("<f8", 3), "<u4", "<f8"],
-    "offsets": [0, 4, 8, 16, 24, 48, 72, 80],
-    "itemsize": 88,
+              "energy", "rng_key"],
+    "formats": ["<u4", "<u4", "<u4", "<f8", ("<f8", 3), ("<f8", 3), "<u4", "<f8", "<u8"],
+    "offsets": [0, 4, 8, 16, 24, 48, 72, 80, 88],
+    "itemsize": 96,
 })
 
 COUNTER_NAMES = ["num_vacancies", "num_initializers", "num_secondaries", "num_active",
@@ -114,6 +114,11 @@ def assert_same_state(a, b):
     ea, eb = a.energy_deposition(), b.energy_deposition()
     np.testing.assert_allclose(ea.sum(), eb.sum(), rtol=TOTAL_RTOL)
     np.testing.assert_allclose(ea, eb, rtol=TOTAL_RTOL, atol=1e-12)
+
+
+def test_initializer_layout(gb, params):
+    st = gb.Stepper(params, 1024, seed=0, use_graph=False)
+    assert st.state_info("initializers")[0] == INIT_DTYPE.itemsize
 
 
 def test_static_scratch_matches_allocated_scratch(gb, params):
