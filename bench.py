@@ -198,7 +198,8 @@ def run_reference(args, wl):
 DTYPES = {"mixed": "f32 physics + f64 positions/geometry/field/tally", "double": "f64"}
 
 
-def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks):
+def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
+            track_order=None):
     """Time one precision's stepping loop: device and end-to-end throughput,
     per-transport tallies, and per-action times for the roofline."""
     import torch
@@ -206,14 +207,16 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks):
     import celeritas_gb300 as gb
     from celeritas_gb300 import roofline
 
+    track_order = args.track_order if track_order is None else track_order
     gb.load_library(precision=precision)
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"],
-                       track_order=args.track_order, precision=precision)
+                       track_order=track_order, precision=precision)
     labels = params.action_labels()
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     stream = stream_cls(stepper.stream_handle())
-    prim = make_primaries(wl, rank)
+    prim = make_primaries(wl, rank, num=wl.get("bench_primaries"))
+    events_per_step = len(np.unique(prim["event"]))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     def finish(res):
@@ -303,8 +306,9 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks):
         "value": total_steps / (total_ms / 1e3),
         "e2e": total_steps / total_e2e,
         "ms_per_step": total_ms / args.steps,
-        "events_per_s": wl["events"] * max(1, int(os.environ.get("WORLD_SIZE", "1")))
+        "events_per_s": events_per_step * max(1, int(os.environ.get("WORLD_SIZE", "1")))
         * args.steps / (total_ms / 1e3),
+        "track_order": track_order,
         "track_steps_per_step": int(np.mean(track_steps)),
         "iterations_per_step": int(np.mean(iterations)),
         "tallies": np.array(tallies),
@@ -318,6 +322,39 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks):
     }
     del stepper, params
     return out
+
+
+def measure_served(args, wl, rank):
+    """Batched and served form: the workload's events streamed through the
+    continuous-batching server (mixed precision, action-sorted, per-track
+    streams), all arriving at once and admitted as queue space frees up, so
+    the tail of one event overlaps the start of the next."""
+    import celeritas_gb300 as gb
+    from celeritas_gb300 import serving
+
+    gb.load_library(precision="mixed")
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                       field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
+                       precision="mixed", rng_per_track=True, event_tallies=True)
+    stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
+    per_event = wl["num_primaries"] // wl["events"]
+    server = serving.EventServer({wl["geometry"]: stepper},
+                                 {wl["geometry"]: 16 * wl["slots"]}, 1 << 16)
+
+    def requests(num_events, first, seed):
+        prim = make_primaries(wl, rank, num=num_events * per_event, seed_offset=seed)
+        out = []
+        for k in range(num_events):
+            p = prim[k * per_event:(k + 1) * per_event].copy()
+            p["event"] = first + k
+            out.append(serving.Request(first + k, wl["geometry"], p, 0.0))
+        return out
+
+    server.serve(requests(max(4, args.served_events // 8), 0, 99))  # warm-up
+    reqs = requests(args.served_events, 1 << 12, 0)
+    summary = server.serve(reqs)
+    summary["primaries_per_event"] = per_event
+    return summary
 
 
 def compare_tallies(mixed, fp64):
@@ -369,6 +406,10 @@ def run_gb300(args, wl):
         for prec in precisions:
             results[prec] = measure(args, wl, prec, torch.cuda.ExternalStream, dist,
                                     rank, local_rank, clocks)
+        if args.plain:
+            # The plain FP64 path: no action sort
+            results["plain"] = measure(args, wl, "double", torch.cuda.ExternalStream,
+                                       dist, rank, local_rank, clocks, track_order=0)
     head = results[precisions[0]]
 
     if rank != 0:
@@ -421,8 +462,146 @@ def run_gb300(args, wl):
                         "iterations_per_step": fp["iterations_per_step"],
                         "dominant_kernel_ms": fp["per_action"][fp["dominant"]]["ms_per_launch"]}
         line["mixed_vs_fp64_edep"] = compare_tallies(head["tallies"], fp["tallies"])
+    if "plain" in results:
+        pl = results["plain"]
+        line["fp64_plain"] = {"value": pl["value"], "e2e": pl["e2e"],
+                              "events_per_s": pl["events_per_s"],
+                              "ms_per_step": pl["ms_per_step"], "track_order": 0}
+        line["events_per_s_vs_fp64_plain"] = head["events_per_s"] / pl["events_per_s"]
+        if args.served_events:
+            served = measure_served(args, wl, rank)
+            line["served"] = served
+            line["served_events_per_s_vs_fp64_plain"] = (served["events_per_s"]
+                                                         / pl["events_per_s"])
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, os.cpu_count() or 1)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_serving(args, wl):
+    """Serving benchmark (c5): the continuous-batching server at several
+    Poisson arrival rates, beside the plain FP64 path serving the same
+    requests one at a time in arrival order."""
+    import torch
+
+    import celeritas_gb300 as gb
+    from celeritas_gb300 import serving
+    from celeritas_gb300.build import build
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    if rank == 0:
+        build(precision="mixed")
+        build(precision="double")
+    if dist:
+        dist.barrier()
+
+    fields = {"calo": (1.0, 0.0, 0.0), "cms": (0.0, 0.0, 3.8)}
+    slots = wl["slots"]
+    num_events = 1 << 16
+
+    def make_steppers(precision, track_order, per_track):
+        gb.load_library(precision=precision)
+        out = {}
+        for geo, field in fields.items():
+            params = gb.Params(gb.physics_file(geo), geo, field_tesla=field, msc=True,
+                               track_order=track_order, precision=precision,
+                               rng_per_track=per_track, event_tallies=per_track)
+            out[geo] = gb.Stepper(params, slots, seed=wl["seed"] + rank)
+        return out
+
+    steppers = make_steppers("mixed", 7, True)
+    server = serving.EventServer(steppers, {g: 16 * slots for g in steppers}, num_events)
+    next_event = 0
+
+    def stream(rate, duration, seed):
+        nonlocal next_event
+        reqs = serving.make_requests(rate, duration, seed=seed + 7919 * rank,
+                                     first_event=next_event)
+        next_event += len(reqs)
+        if next_event >= num_events:
+            raise RuntimeError("serving benchmark ran out of event IDs")
+        return reqs
+
+    for i in range(args.warmup):
+        server.serve(stream(200.0, 0.25, 1000 + i))
+    runs = []
+    with ClockSampler(local_rank) as clocks:
+        clocks.active = True
+        for rate in wl["rates"]:
+            reqs = stream(float(rate), wl["duration"], rate)
+            summary = server.serve(reqs)
+            summary["rate"] = rate
+            summary["arrivals"] = [r.arrival for r in reqs]
+            runs.append(summary)
+        clocks.active = False
+    del server, steppers
+
+    # Plain FP64 path, one request at a time: service times of a sample of
+    # requests (each inserted alone and stepped until empty)
+    plain = make_steppers("double", 0, False)
+    sample = stream(200.0, 0.25, 424242)[:args.sequential_sample]
+    service = []
+    for r in sample:
+        st = plain[r.geometry]
+        t0 = time.perf_counter()
+        res = [st.step(r.primaries)] + st.run(max_steps=MAX_STEPS, batch=64)
+        service.append(time.perf_counter() - t0)
+        if res[-1].alive or res[-1].queued:
+            raise RuntimeError("plain FP64 transport did not finish")
+    service = np.array(service)
+    rng = np.random.default_rng(wl["seed"])
+    for run in runs:
+        arr = np.array(run.pop("arrivals"))
+        svc = rng.choice(service, size=len(arr))
+        lat = serving.sequential_latencies(arr, svc)
+        span = max(float((arr + lat).max() - arr.min()), 1e-9)
+        run["sequential_fp64"] = {"p50_ms": float(np.percentile(lat, 50) * 1e3),
+                                  "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                                  "events_per_s": len(arr) / span}
+    served = runs[-1]["events_per_s"]
+    if dist:
+        t = torch.tensor([served], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        served = t.item()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": "events/s",
+        "value": served,
+        "unit": "events/s",
+        "n_gpus": world,
+        "steps": len(runs),
+        "warmup": args.warmup,
+        "ms_per_step": None,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": DTYPES["mixed"],
+        "data": "synthetic",
+        "config": {"workload": wl["description"], "name": args.workload,
+                   "precision": "mixed", "track_order": 7, "rng": "per-track streams",
+                   "value": "served events/s at the highest offered rate, host clock"},
+        "e2e": {"value": served, "unit": "events/s",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "serving": runs,
+        "sequential_fp64": {"service_ms_mean": float(service.mean() * 1e3),
+                            "service_ms_p99": float(np.percentile(service, 99) * 1e3),
+                            "events_per_s": 1.0 / float(service.mean()),
+                            "sample": len(service)},
+        "clocks": clocks.summary(),
+    }
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -459,12 +638,26 @@ def main():
     parser.add_argument("--track-order", type=int, default=7,
                         help="TrackOrder: 0 none, 5/6/7 action sorts")
     parser.add_argument("--no-fp64", action="store_true",
-                        help="skip the plain FP64 comparison run")
+                        help="skip the FP64 comparison run")
+    parser.add_argument("--served-events", type=int, default=0,
+                        help="events streamed through the server (c3: 195)")
+    parser.add_argument("--sequential-sample", type=int, default=40,
+                        help="c5: requests timed alone on the plain FP64 path")
+    parser.add_argument("--plain", action="store_true",
+                        help="also time the plain FP64 path (no action sort); on for c3")
     args = parser.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]
-    if args.impl == "reference":
+    if args.workload == "c3":
+        args.plain = True
+        args.served_events = args.served_events or 195
+    if args.workload == "c5":
+        if args.impl == "reference":
+            run_reference(args, WORKLOADS["c3"])
+        else:
+            run_serving(args, wl)
+    elif args.impl == "reference":
         run_reference(args, wl)
     else:
         run_gb300(args, wl)

@@ -161,18 +161,26 @@ class GeoTrackView
         return pos[sr.type] - sr.value;
     }
 
-    //! Positive distances to a surface along dir (+inf where none)
+    //! Positive distances to a surface along dir (+inf where none). Surfaces
+    //! whose nearest point is farther than max_dist are skipped without
+    //! solving: every distance along the ray is at least that far, so the
+    //! caller's "d <= max_dist" test would reject them anyway.
     GBX_FUNCTION void intersect(size_type surf,
                                 Real3 const& pos,
                                 Real3 const& dir,
                                 bool on_surface,
-                                double* dist) const
+                                double* dist,
+                                double max_dist = INFINITY) const
     {
         dist[0] = dist[1] = INFINITY;
         SurfaceRecord const& sr = p_.surfaces[surf];
         if (sr.type != surf_czc)
         {
             if (on_surface)
+                return;
+            // |d| = |plane - pos| / |dir_axis| >= |plane - pos|, also after
+            // rounding since |dir_axis| <= 1
+            if (!(std::fabs(sr.value - pos[sr.type]) <= max_dist))
                 return;
             double const n_dir = dir[sr.type];
             if (n_dir != 0)
@@ -182,6 +190,19 @@ class GeoTrackView
                     dist[0] = d;
             }
             return;
+        }
+        if (!on_surface && max_dist < INFINITY)
+        {
+            // The radial distance |r - R| bounds the distance along any ray;
+            // skip the cylinder unless r lies within max_dist of R, with a
+            // margin far above the rounding of the quadratic's roots
+            double const r2 = ipow<2>(pos.x) + ipow<2>(pos.y);
+            double const radius = std::sqrt(sr.value);
+            double const margin = 1e-6 * (radius + max_dist) + 1e-9;
+            double const hi = radius + max_dist + margin;
+            double const lo = radius - max_dist - margin;
+            if (r2 > hi * hi || (lo > 0 && r2 < lo * lo))
+                return;
         }
         // 1 - (dir . z)^2; no intersection when traveling along the axis
         double const a = 1 - ipow<2>(dir.z);
@@ -416,7 +437,7 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
         for (size_type f = 0; f < v.num_faces; ++f)
         {
             double d[2];
-            this->intersect(v.faces[f], pos, dir, v.faces[f] == cur_surf, d);
+            this->intersect(v.faces[f], pos, dir, v.faces[f] == cur_surf, d, max_step);
             for (int k = 0; k < 2; ++k)
             {
                 if (d[k] <= max_step && d[k] < best)
@@ -458,7 +479,7 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
         for (size_type surf = 0; surf < p_.num_surfaces; ++surf)
         {
             double dd[2];
-            this->intersect(surf, pos, dir, surf == cur_surf, dd);
+            this->intersect(surf, pos, dir, surf == cur_surf, dd, max_step);
             for (int k = 0; k < 2; ++k)
             {
                 double const d = dd[k];

@@ -36,10 +36,20 @@ WORKLOADS = {
     "c3": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
                emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
                seed=0, events=1300, msc=True, field=(0.0, 0.0, 3.8),
+               bench_primaries=3250,
                description="CMS-like: 10 Si shells (0.3 mm, r 4-110 cm), PbWO4 barrel "
                            "(r 129-152 cm), 17 x (5 cm brass + 0.4 cm scintillator) "
-                           "(r 180-295 cm), 3.8 T along z, Urban MSC; 1300 events x 50 "
-                           "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots"),
+                           "(r 180-295 cm), 3.8 T along z, Urban MSC; events of 50 "
+                           "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
+                           "one bench step = 65 of the 1300 events"),
+    # Serving: Poisson arrivals, Pareto(1.5) primaries per event capped at
+    # 5000, CMS-like (as c3) or calorimeter (as c2) 50/50, one pool of 2^21
+    # slots per geometry (2^22 in all) with queues of 16 x slots
+    "c5": dict(geometry="cms+calo", slots=1 << 21, rates=(50, 200, 1000, 2000),
+               duration=2.0, seed=0,
+               description="serving: Poisson arrivals at 50-2000 events/s for 2 s each, "
+                           "Pareto(1.5) primaries capped at 5000, CMS-like or "
+                           "calorimeter 50/50, 2 x 2^21 track slots"),
 }
 
 
