@@ -411,6 +411,7 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_tslots = arr(4);
     std::size_t o_aoff = L.reserve(4 * 2 * std::size_t(num_bins + 1));
     std::size_t o_shist = L.reserve(4 * std::size_t(num_bins) * sort_blocks);
+    std::size_t o_work = L.reserve(sizeof(size_type));
     std::size_t o_log = L.reserve(sizeof(StepRecord) * log_cap);
     std::size_t o_stepidx = L.reserve(sizeof(size_type));
 
@@ -535,6 +536,12 @@ CoreState::CoreState(CoreParams const& params,
     ctx_.sort.block_hist = static_cast<size_type*>(at(o_shist));
     ctx_.sort.num_bins = num_bins;
     ctx_.sort.num_blocks = sort_blocks;
+    ctx_.work_counter = static_cast<size_type*>(at(o_work));
+    // Persistent charged along-step: on by default in the mixed-precision
+    // build, where it outruns the one-thread-per-track kernel; in FP64 the
+    // diverged FP64 multiple-scattering code makes it slower
+    ctx_.persistent_blocks
+        = sizeof(real_type) < sizeof(double) ? persistent_along_blocks() : 0;
     ctx_.log = static_cast<StepRecord*>(at(o_log));
     ctx_.log_capacity = log_cap;
     ctx_.step_index = static_cast<size_type*>(at(o_stepidx));

@@ -166,7 +166,7 @@ __global__ __launch_bounds__(block_size) void pre_step_kernel(ParamsData p,
     }
 }
 
-__global__ __launch_bounds__(block_size) void along_step_kernel(ParamsData p,
+__global__ __launch_bounds__(block_size, 1) void along_step_kernel(ParamsData p,
                                                                 StateData s,
                                                                 size_type action)
 {
@@ -614,6 +614,66 @@ along_step_sorted_kernel(ParamsData p,
         along_step_impl<K>(p, s, slot);
 }
 
+//! Charged along-step in a uniform field over the sorted charged range, as
+//! a persistent kernel: each thread takes tracks from a work counter
+//! (warp-aggregated), keeps the track's propagation in registers, and runs
+//! one field substep per loop iteration, taking the next track as soon as
+//! its own finishes. Lanes of a warp thus stay busy on different tracks
+//! instead of waiting for the one with the most substeps. Every track runs
+//! the same sequence of operations as along_step_impl.
+__global__ __launch_bounds__(block_size, 1) void along_charged_persistent_kernel(
+    ParamsData p,
+    StateData s,
+    size_type const* offsets,
+    size_type bin,
+    size_type* work_counter)
+{
+    size_type const first = offsets[bin];
+    size_type const count = offsets[bin + 1] - first;
+    unsigned int const lane = threadIdx.x & 31u;
+    FieldOptions const opt;
+    FieldPropagation fp(opt, UniformFieldEquation{});
+    size_type slot = invalid_id;
+    bool have = false;
+    for (;;)
+    {
+        if (!have)
+        {
+            // Claim the next track for every lane that needs one
+            unsigned int const need = __activemask();
+            unsigned int const rank = __popc(need & ((1u << lane) - 1u));
+            unsigned int const leader = __ffs(need) - 1;
+            size_type base = 0;
+            if (lane == leader)
+                base = atomicAdd(work_counter, size_type(__popc(need)));
+            base = __shfl_sync(need, base, leader);
+            size_type const idx = base + rank;
+            if (idx >= count)
+                break;
+            slot = s.track_slots[first + idx];
+            bool charged;
+            if (!along_prologue<AlongKind::charged>(p, s, slot, &charged))
+                continue;
+            if (s.step_length[slot] == 0)
+            {
+                along_epilogue(p, s, slot, true);
+                continue;
+            }
+            GeoTrackView geo(p.geo, s, slot);
+            field_setup(p, s, slot, geo, &fp);
+            have = true;
+        }
+        GeoTrackView geo(p.geo, s, slot);
+        fp.substep(geo);
+        if (fp.done())
+        {
+            field_result(p, s, slot, fp.finish(geo));
+            along_epilogue(p, s, slot, true);
+            have = false;
+        }
+    }
+}
+
 __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
     ParamsData p,
     StateData s,
@@ -703,8 +763,17 @@ void launch_along_step(LaunchContext const& ctx,
         size_type const* offsets = sort_offsets(ctx, SortKey::along_step);
         if (action == invalid_id || action == p.action_along_step)
         {
-            along_step_sorted_kernel<AlongKind::charged><<<nb, block_size, 0, stream>>>(
-                p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
+            if (p.has_field && ctx.persistent_blocks > 0)
+            {
+                cudaMemsetAsync(ctx.work_counter, 0, sizeof(size_type), stream);
+                along_charged_persistent_kernel<<<ctx.persistent_blocks, block_size, 0, stream>>>(
+                    p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
+            }
+            else
+            {
+                along_step_sorted_kernel<AlongKind::charged><<<nb, block_size, 0, stream>>>(
+                    p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
+            }
         }
         if (action == invalid_id || action == p.action_along_step_neutral)
         {
@@ -801,6 +870,21 @@ void launch_extend_from_secondaries(LaunchContext const& ctx, cudaStream_t strea
     scan_blocks_kernel<<<1, 1024, 0, stream>>>(
         ctx.state, ctx.scratch, ctx.log, ctx.log_capacity, ctx.step_index);
     scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, ctx.scratch);
+}
+
+int persistent_along_blocks()
+{
+    int device = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&device) != cudaSuccess
+        || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)
+               != cudaSuccess
+        || cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+               &per_sm, along_charged_persistent_kernel, block_size, 0)
+               != cudaSuccess)
+    {
+        return 0;
+    }
+    return sms * per_sm;
 }
 
 void launch_count_event_live(LaunchContext const& ctx,

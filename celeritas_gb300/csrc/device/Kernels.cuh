@@ -58,6 +58,10 @@ struct LaunchContext
     StateData state;
     ScanScratch scratch;
     SortScratch sort;
+    //! Grid of the persistent charged along-step kernel (0: not used) and
+    //! its device work counter
+    int persistent_blocks;
+    size_type* work_counter;
     StepRecord* log;  //!< Step log (ring buffer)
     size_type log_capacity;
     size_type* step_index;  //!< Device-resident step counter
@@ -83,6 +87,9 @@ void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream);
 void launch_extend_from_secondaries(LaunchContext const& ctx,
                                     cudaStream_t stream);
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
+//! Resident blocks of the persistent charged along-step kernel on the
+//! current device (SMs x blocks per SM at full occupancy), 0 on failure
+int persistent_along_blocks();
 //! Count live tracks (slots and queued initializers) of events [0, n) into
 //! state.event_live
 void launch_count_event_live(LaunchContext const& ctx,

@@ -236,12 +236,18 @@ enum class AlongKind
     neutral,
 };
 
+//! Start of the along-step: track and action checks and the multiple-
+//! scattering step limit. Returns false if this function kind does not
+//! handle the slot (nothing was done).
 template<AlongKind K>
-GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_type slot)
+GBX_FUNCTION bool along_prologue(ParamsData const& p,
+                                 StateData const& s,
+                                 size_type slot,
+                                 bool* charged)
 {
     size_type const along = s.along_step_action[slot];
     if (!is_track_valid(s.status[slot]))
-        return;
+        return false;
     if (K != AlongKind::neutral && along == p.action_along_step)
     {
     }
@@ -250,83 +256,107 @@ GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_
     }
     else
     {
-        return;
+        return false;
     }
-    bool const charged = (K == AlongKind::charged)
-                         || (K == AlongKind::any && along == p.action_along_step);
+    *charged = (K == AlongKind::charged)
+               || (K == AlongKind::any && along == p.action_along_step);
 
     // MscStepLimitApplier
-    if (charged && p.msc.enabled)
+    if (*charged && p.msc.enabled)
     {
         XorwowEngine rng(s.rng, slot);
         msc_limit_step(p, s, slot, rng);
     }
+    return true;
+}
 
-    // PropagationApplier: straight line, or the uniform-field integrator for
-    // charged tracks (which can loop)
+//! Set up the uniform-field propagation of a charged slot over its step
+GBX_FUNCTION void field_setup(ParamsData const& p,
+                              StateData const& s,
+                              size_type slot,
+                              GeoTrackView& geo,
+                              FieldPropagation* fp)
+{
+    size_type const pid = s.particle_id[slot];
+    real_type const mass = p.particles[pid].mass;
+    real_type const energy = s.energy[slot];
+    double const momentum = std::sqrt(double(momentum_sq(mass, energy)));
+    UniformFieldEquation rhs;
+    rhs.field = {p.field[0], p.field[1], p.field[2]};
+    rhs.coeffi = (p.particles[pid].charge * detail::e_electron)
+                 / (1 * (detail::mev_value / constants::c_light));
+    fp->set_rhs(rhs);
+    fp->init(geo, momentum, s.step_length[slot]);
+}
+
+//! Step limit and looping bookkeeping after a field propagation
+GBX_FUNCTION void field_result(ParamsData const& p,
+                               StateData const& s,
+                               size_type slot,
+                               Propagation const& prop)
+{
+    size_type const pid = s.particle_id[slot];
+    real_type const energy = s.energy[slot];
     double const step_length = s.step_length[slot];
-    if (step_length != 0)
+    // update_looping
+    if (prop.looping)
+        ++s.num_looping_steps[slot];
+    else
+        s.num_looping_steps[slot] = 0;
+    if (prop.looping)
     {
-        GeoTrackView geo(p.geo, s, slot);
-        if (charged && p.has_field)
-        {
-            size_type const pid = s.particle_id[slot];
-            real_type const mass = p.particles[pid].mass;
-            real_type const energy = s.energy[slot];
-            double const momentum = std::sqrt(double(momentum_sq(mass, energy)));
-            UniformFieldEquation rhs;
-            rhs.field = {p.field[0], p.field[1], p.field[2]};
-            rhs.coeffi = (p.particles[pid].charge * detail::e_electron)
-                         / (1 * (detail::mev_value / constants::c_light));
-            FieldOptions const opt;
-            Propagation prop = propagate_in_field(opt, rhs, momentum, geo, step_length);
-            // update_looping
-            if (prop.looping)
-                ++s.num_looping_steps[slot];
-            else
-                s.num_looping_steps[slot] = 0;
-            if (prop.looping)
-            {
-                s.step_length[slot] = prop.distance;
-                LoopingRecord const& lr = p.looping[pid];
-                size_type const max_steps = (energy < real_type(lr.threshold_energy))
-                                                ? lr.max_subthreshold_steps
-                                                : lr.max_steps;
-                s.post_step_action[slot] = (s.num_looping_steps[slot] >= max_steps)
-                                               ? p.action_tracking_cut
-                                               : p.action_propagation_limit;
-            }
-            else if (prop.boundary)
-            {
-                s.step_length[slot] = prop.distance;
-                s.post_step_action[slot] = p.action_boundary;
-            }
-            else if (prop.distance < step_length)
-            {
-                s.step_length[slot] = prop.distance;
-                s.post_step_action[slot] = p.action_propagation_limit;
-            }
-        }
-        else
-        {
-            Propagation prop = geo.find_next_step(step_length);
-            if (prop.boundary)
-                geo.move_to_boundary();
-            else
-                geo.move_internal(step_length);
-            if (prop.boundary)
-            {
-                s.step_length[slot] = prop.distance;
-                s.post_step_action[slot] = p.action_boundary;
-            }
-            else if (prop.distance < step_length)
-            {
-                s.step_length[slot] = prop.distance;
-                s.post_step_action[slot] = p.action_propagation_limit;
-            }
-        }
+        s.step_length[slot] = prop.distance;
+        LoopingRecord const& lr = p.looping[pid];
+        size_type const max_steps = (energy < real_type(lr.threshold_energy))
+                                        ? lr.max_subthreshold_steps
+                                        : lr.max_steps;
+        s.post_step_action[slot] = (s.num_looping_steps[slot] >= max_steps)
+                                       ? p.action_tracking_cut
+                                       : p.action_propagation_limit;
     }
+    else if (prop.boundary)
+    {
+        s.step_length[slot] = prop.distance;
+        s.post_step_action[slot] = p.action_boundary;
+    }
+    else if (prop.distance < step_length)
+    {
+        s.step_length[slot] = prop.distance;
+        s.post_step_action[slot] = p.action_propagation_limit;
+    }
+}
 
+//! Straight-line propagation over the slot's step
+GBX_FUNCTION void linear_propagation(ParamsData const& p,
+                                     StateData const& s,
+                                     size_type slot,
+                                     GeoTrackView& geo)
+{
+    double const step_length = s.step_length[slot];
+    Propagation prop = geo.find_next_step(step_length);
+    if (prop.boundary)
+        geo.move_to_boundary();
+    else
+        geo.move_internal(step_length);
+    if (prop.boundary)
+    {
+        s.step_length[slot] = prop.distance;
+        s.post_step_action[slot] = p.action_boundary;
+    }
+    else if (prop.distance < step_length)
+    {
+        s.step_length[slot] = prop.distance;
+        s.post_step_action[slot] = p.action_propagation_limit;
+    }
+}
+
+//! End of the along-step after propagation: multiple-scattering
+//! deflection and displacement, time, energy loss and track update
+GBX_FUNCTION void along_epilogue(ParamsData const& p,
+                                 StateData const& s,
+                                 size_type slot,
+                                 bool charged)
+{
     // MscApplier
     if (charged && p.msc.enabled)
     {
@@ -390,6 +420,38 @@ GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_
         }
     }
     ++s.num_steps[slot];
+}
+
+//! The whole along-step of one slot (PropagationApplier between the MSC
+//! step limit and the MSC applier, then time, energy loss, track update)
+template<AlongKind K>
+GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_type slot)
+{
+    bool charged;
+    if (!along_prologue<K>(p, s, slot, &charged))
+        return;
+    // PropagationApplier: straight line, or the uniform-field integrator for
+    // charged tracks (which can loop)
+    if (s.step_length[slot] != 0)
+    {
+        GeoTrackView geo(p.geo, s, slot);
+        if (charged && p.has_field)
+        {
+            FieldOptions const opt;
+            FieldPropagation fp(opt, UniformFieldEquation{});
+            field_setup(p, s, slot, geo, &fp);
+            do
+            {
+                fp.substep(geo);
+            } while (!fp.done());
+            field_result(p, s, slot, fp.finish(geo));
+        }
+        else
+        {
+            linear_propagation(p, s, slot, geo);
+        }
+    }
+    along_epilogue(p, s, slot, charged);
 }
 
 GBX_FORCEINLINE void along_step(ParamsData const& p, StateData const& s, size_type slot)

@@ -355,6 +355,10 @@ class FieldDriver
         return output.end;
     }
 
+    //! Forget the chord limit of the previous propagation
+    GBX_FORCEINLINE void reset() { max_chord_ = INFINITY; }
+    GBX_FORCEINLINE void set_rhs(UniformFieldEquation const& rhs) { rhs_ = rhs; }
+
     GBX_FORCEINLINE double minimum_step() const { return opt_.minimum_step; }
     GBX_FORCEINLINE double delta_intersection() const
     {
@@ -529,34 +533,51 @@ class FieldDriver
 //---------------------------------------------------------------------------//
 // Field propagator
 //---------------------------------------------------------------------------//
-//! Propagate a charged track up to 'step' along its curved trajectory,
-//! stopping at the first boundary crossing (FieldPropagator::operator())
-GBX_FUNCTION Propagation propagate_in_field(FieldOptions const& opt,
-                                            UniformFieldEquation const& rhs,
-                                            double momentum,
-                                            GeoTrackView& geo,
-                                            double step)
+//! Propagation of a charged track up to 'step' along its curved trajectory,
+//! stopping at the first boundary crossing (FieldPropagator::operator()),
+//! split into its set-up, one substep of its loop and its completion so that
+//! a kernel can interleave the substeps of different tracks. Running
+//! init(), then substep() until done(), then finish() is the reference's
+//! sequence of operations.
+class FieldPropagation
 {
-    FieldDriver driver(opt, rhs);
-    OdeState state;
-    state.pos = geo.pos();
-    Real3 const dir0 = geo.dir();
-    state.mom = {momentum * dir0.x, momentum * dir0.y, momentum * dir0.z};
-
-    double const delta_intersection = driver.delta_intersection();
-    double const minimum_substep = driver.minimum_step();
-    double const bump_distance = delta_intersection * double(0.1);
-
-    Propagation result{0, geo.is_on_boundary(), false};
-    double remaining = step;
-    auto remaining_substeps = driver.max_substeps();
-    do
+  public:
+    GBX_FORCEINLINE FieldPropagation(FieldOptions const& opt,
+                                     UniformFieldEquation const& rhs)
+        : driver_(opt, rhs)
     {
-        DriverResult substep = driver.advance(remaining, state);
+    }
+
+    GBX_FORCEINLINE void init(GeoTrackView& geo, double momentum, double step)
+    {
+        driver_.reset();
+        state_.pos = geo.pos();
+        Real3 const dir0 = geo.dir();
+        state_.mom = {momentum * dir0.x, momentum * dir0.y, momentum * dir0.z};
+        result_ = {0, geo.is_on_boundary(), false};
+        step_ = step;
+        remaining_ = step;
+        remaining_substeps_ = driver_.max_substeps();
+    }
+
+    //! Whether the substep loop has ended (checked after each substep)
+    GBX_FORCEINLINE bool done() const
+    {
+        return !(remaining_ > driver_.minimum_step() && remaining_substeps_ > 0);
+    }
+
+    //! One iteration of the substep loop
+    GBX_FUNCTION void substep(GeoTrackView& geo)
+    {
+        double const delta_intersection = driver_.delta_intersection();
+        double const minimum_substep = driver_.minimum_step();
+        double const bump_distance = delta_intersection * double(0.1);
+
+        DriverResult substep = driver_.advance(remaining_, state_);
         // Chord from the current position to the substep end
-        Real3 cdir{substep.state.pos.x - state.pos.x,
-                   substep.state.pos.y - state.pos.y,
-                   substep.state.pos.z - state.pos.z};
+        Real3 cdir{substep.state.pos.x - state_.pos.x,
+                   substep.state.pos.y - state_.pos.y,
+                   substep.state.pos.z - state_.pos.z};
         double const clen = norm(cdir);
         cdir.x /= clen;
         cdir.y /= clen;
@@ -571,71 +592,106 @@ GBX_FUNCTION Propagation propagate_in_field(FieldOptions const& opt,
             double delta_sq = 0;
             for (int i = 0; i < 3; ++i)
             {
-                delta_sq += ipow<2>(state.pos[i] - substep.state.pos[i]
+                delta_sq += ipow<2>(state_.pos[i] - substep.state.pos[i]
                                     + linear_step.distance * cdir[i]);
             }
             return delta_sq <= ipow<2>(delta_intersection);
         };
         if (!linear_step.boundary)
         {
-            state = substep.state;
-            result.boundary = false;
-            result.distance += substep.step;
-            remaining = step - result.distance;
-            geo.move_internal_to(state.pos);
-            --remaining_substeps;
+            state_ = substep.state;
+            result_.boundary = false;
+            result_.distance += substep.step;
+            remaining_ = step_ - result_.distance;
+            geo.move_internal_to(state_.pos);
+            --remaining_substeps_;
         }
-        else if (result.boundary && (linear_step.distance) < bump_distance)
+        else if (result_.boundary && (linear_step.distance) < bump_distance)
         {
-            remaining = substep.step / 2;
+            remaining_ = substep.step / 2;
         }
         else if (update_length <= minimum_substep || is_intercept_close()
                  || clen == 0)
         {
-            result.boundary = (linear_step.distance <= clen
-                               || result.distance + update_length <= step
-                               || clen == 0);
-            if (!result.boundary)
+            result_.boundary = (linear_step.distance <= clen
+                                || result_.distance + update_length <= step_
+                                || clen == 0);
+            if (!result_.boundary)
             {
-                state.pos = substep.state.pos;
+                state_.pos = substep.state.pos;
                 geo.move_internal_to(substep.state.pos);
             }
-            result.distance += min_of(update_length, substep.step);
-            state.mom = substep.state.mom;
-            remaining = 0;
+            result_.distance += min_of(update_length, substep.step);
+            state_.mom = substep.state.mom;
+            remaining_ = 0;
         }
         else
         {
-            remaining = update_length;
+            remaining_ = update_length;
         }
-    } while (remaining > minimum_substep && remaining_substeps > 0);
+    }
 
-    if (remaining_substeps == 0 && result.distance < step)
+    //! Complete the propagation after the loop
+    GBX_FUNCTION Propagation finish(GeoTrackView& geo)
     {
-        result.looping = true;
-    }
-    else if (result.distance > 0)
-    {
-        if (result.boundary)
+        double const bump_distance = driver_.delta_intersection() * double(0.1);
+        if (remaining_substeps_ == 0 && result_.distance < step_)
         {
-            geo.move_to_boundary();
-            state.pos = geo.pos();
+            result_.looping = true;
         }
-        else if (result.distance < step)
+        else if (result_.distance > 0)
         {
-            result.distance = step;
+            if (result_.boundary)
+            {
+                geo.move_to_boundary();
+                state_.pos = geo.pos();
+            }
+            else if (result_.distance < step_)
+            {
+                result_.distance = step_;
+            }
         }
+        Real3 dir = make_unit_vector(state_.mom);
+        geo.set_dir(dir);
+        if (result_.distance == 0)
+        {
+            result_.distance = min_of(bump_distance, step_);
+            result_.boundary = false;
+            axpy(result_.distance, dir, &state_.pos);
+            geo.move_internal_to(state_.pos);
+        }
+        return result_;
     }
-    Real3 dir = make_unit_vector(state.mom);
-    geo.set_dir(dir);
-    if (result.distance == 0)
+
+    GBX_FORCEINLINE void set_rhs(UniformFieldEquation const& rhs)
     {
-        result.distance = min_of(bump_distance, step);
-        result.boundary = false;
-        axpy(result.distance, dir, &state.pos);
-        geo.move_internal_to(state.pos);
+        driver_.set_rhs(rhs);
     }
-    return result;
+
+  private:
+    FieldDriver driver_;
+    OdeState state_;
+    Propagation result_;
+    double step_;
+    double remaining_;
+    short remaining_substeps_;
+};
+
+//! Propagate a charged track up to 'step' along its curved trajectory,
+//! stopping at the first boundary crossing (FieldPropagator::operator())
+GBX_FUNCTION Propagation propagate_in_field(FieldOptions const& opt,
+                                            UniformFieldEquation const& rhs,
+                                            double momentum,
+                                            GeoTrackView& geo,
+                                            double step)
+{
+    FieldPropagation fp(opt, rhs);
+    fp.init(geo, momentum, step);
+    do
+    {
+        fp.substep(geo);
+    } while (!fp.done());
+    return fp.finish(geo);
 }
 
 }  // namespace gbx
