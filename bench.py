@@ -607,6 +607,111 @@ def run_serving(args, wl):
         dist.destroy_process_group()
 
 
+def run_batching(args, wl):
+    """Batching benchmark (c4): uneven events all in flight in one stepper,
+    launch configuration chosen by the autotuner on calibration events."""
+    import torch
+
+    import celeritas_gb300 as gb
+    from celeritas_gb300 import autotune
+    from celeritas_gb300.build import build
+    from celeritas_gb300.workloads import make_uneven_events
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    if rank == 0:
+        build(precision="mixed")
+    if dist:
+        dist.barrier()
+    gb.load_library(precision="mixed")
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                       field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
+                       precision="mixed", rng_per_track=True)
+
+    def make_stepper(slots):
+        return gb.Stepper(params, slots, seed=wl["seed"] + rank)
+
+    calib = make_uneven_events(wl, wl["calibration_events"], seed=1000 + rank)
+    t0 = time.perf_counter()
+    best, trials = autotune.autotune(make_stepper, calib)
+    tune_s = time.perf_counter() - t0
+
+    prim = make_uneven_events(wl, wl["bench_events"], seed=rank)
+    nev = wl["bench_events"]
+
+    def timed(stepper):
+        for _ in range(args.warmup):
+            autotune.transport(stepper, prim)
+        secs, steps = [], []
+        for _ in range(args.steps):
+            s_, n_ = autotune.transport(stepper, prim)
+            secs.append(s_)
+            steps.append(n_)
+        return float(np.sum(secs)), float(np.sum(steps))
+
+    with ClockSampler(local_rank) as clocks:
+        clocks.active = True
+        tuned = make_stepper(best["slots"])
+        tuned.set_tuning(**{k: v for k, v in best.items() if k != "slots"})
+        t_tuned, n_tuned = timed(tuned)
+        del tuned
+        default = make_stepper(wl["slots"])
+        t_def, n_def = timed(default)
+        del default
+        clocks.active = False
+    if dist:
+        t = torch.tensor([t_tuned, t_def], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_tuned, t_def = t.tolist()
+        n = torch.tensor([n_tuned, n_def], device="cuda", dtype=torch.float64)
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+        n_tuned, n_def = n.tolist()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": "track-steps/s",
+        "value": n_tuned / t_tuned,
+        "unit": "track-steps/s",
+        "events_per_s": world * nev * args.steps / t_tuned,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_tuned / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": DTYPES["mixed"],
+        "data": "synthetic",
+        "config": {"workload": wl["description"], "name": args.workload,
+                   "precision": "mixed", "track_order": args.track_order,
+                   "rng": "per-track streams", "events_per_step": nev,
+                   "primaries_per_step": int(len(prim)),
+                   "timing": "host clock around each transport (synchronized)"},
+        "e2e": {"value": n_tuned / t_tuned, "unit": "track-steps/s",
+                "h2d_bytes_per_step": int(len(prim)) * 80, "d2h_bytes_per_step": 16 * 64},
+        "autotune": {"best": best, "seconds": tune_s,
+                     "calibration_events": wl["calibration_events"],
+                     "trials": [{"config": t.config,
+                                 "track_steps_per_s": t.rate if t.seconds else None,
+                                 "note": t.note} for t in trials]},
+        "untuned": {"value": n_def / t_def, "events_per_s": world * nev * args.steps / t_def,
+                    "slots": wl["slots"]},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def read_traffic(kernel_label, processed, precision):
     """DRAM bytes per launch of a kernel, from the committed ncu capture.
 
@@ -657,6 +762,11 @@ def main():
             run_reference(args, WORKLOADS["c3"])
         else:
             run_serving(args, wl)
+    elif args.workload == "c4":
+        if args.impl == "reference":
+            run_reference(args, WORKLOADS["c3"])
+        else:
+            run_batching(args, wl)
     elif args.impl == "reference":
         run_reference(args, wl)
     else:

@@ -111,6 +111,10 @@ _PROTOTYPES = [
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
       ctypes.POINTER(ctypes.c_size_t)]),
     ("gbx_stepper_extend_from_secondaries_static", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_set_tuning", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong]),
+    ("gbx_stepper_get_tuning", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]),
     ("gbx_stepper_event_live", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint), ctypes.c_size_t]),
     ("gbx_stepper_event_energy_deposition", ctypes.c_int,
@@ -289,6 +293,18 @@ class Stepper:
 
     def kill_active(self):
         _check(self._lib, self._lib.gbx_stepper_kill_active(self._handle))
+
+    def set_tuning(self, **settings):
+        """Launch tuning: along_block_size, along_persistent, sort_threshold."""
+        for name, value in settings.items():
+            _check(self._lib, self._lib.gbx_stepper_set_tuning(
+                self._handle, name.encode(), int(value)))
+
+    def get_tuning(self, name: str) -> int:
+        v = ctypes.c_longlong()
+        _check(self._lib, self._lib.gbx_stepper_get_tuning(
+            self._handle, name.encode(), ctypes.byref(v)))
+        return v.value
 
     def event_live(self, num_events: int) -> np.ndarray:
         """Live tracks (slots + queued initializers) of events [0, n)."""

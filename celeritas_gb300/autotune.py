@@ -1,0 +1,102 @@
+"""Autotuner for batched transport of many uneven events.
+
+The launch configuration of a stepper changes its speed but not its results
+when every track has its own random stream (rng_per_track): the same
+calibration events then cost the same physics work under every candidate, so
+their transport times compare directly. The tuner runs a coordinate descent
+over
+
+* the number of track slots (one stepper per candidate),
+* threads per block of the charged along-step kernel (64, 128, 256; 512 is
+  reported as invalid: it exceeds the register file of that kernel),
+* the charged along-step as a persistent kernel or one thread per track,
+* the sort threshold: action sorts only in steps that start with at least
+  this many live tracks (0: always),
+
+keeping the best value of each parameter before tuning the next.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import time
+from typing import Callable, Sequence
+
+import numpy as np
+
+SLOT_COUNTS = (1 << 20, 1 << 21, 1 << 22)
+BLOCK_SIZES = (64, 128, 256, 512)
+THRESHOLDS = (0, 1 << 14, 1 << 17)
+
+
+@dataclasses.dataclass
+class Trial:
+    config: dict
+    seconds: float | None
+    track_steps: int | None
+    note: str = ""
+
+    @property
+    def rate(self) -> float:
+        return self.track_steps / self.seconds if self.seconds else 0.0
+
+
+def transport(stepper, primaries, max_steps: int = 20000) -> tuple[float, int]:
+    """Seconds and track-steps to transport the primaries to completion."""
+    stepper.synchronize()
+    t0 = time.perf_counter()
+    res = [stepper.step(primaries)] + stepper.run(max_steps=max_steps, batch=64)
+    stepper.synchronize()
+    seconds = time.perf_counter() - t0
+    if res[-1].alive or res[-1].queued:
+        raise RuntimeError("calibration transport did not finish")
+    return seconds, sum(r.active for r in res)
+
+
+def autotune(make_stepper: Callable[[int], object], primaries: np.ndarray,
+             slot_counts: Sequence[int] = SLOT_COUNTS,
+             block_sizes: Sequence[int] = BLOCK_SIZES,
+             thresholds: Sequence[int] = THRESHOLDS,
+             start: dict | None = None) -> tuple[dict, list[Trial]]:
+    """Tune on 'primaries'; return the best configuration and every trial."""
+    trials: list[Trial] = []
+    best = dict(start or {})
+    best.setdefault("slots", slot_counts[len(slot_counts) // 2])
+
+    def run(stepper, config):
+        settings = {k: v for k, v in config.items() if k != "slots"}
+        try:
+            stepper.set_tuning(**settings)
+        except RuntimeError as e:
+            trials.append(Trial(dict(config), None, None, str(e)))
+            return None
+        seconds, steps = transport(stepper, primaries)
+        trial = Trial(dict(config), seconds, steps)
+        trials.append(trial)
+        return trial
+
+    # Slot count: one stepper per candidate, warmed up once
+    winner = None
+    for slots in slot_counts:
+        stepper = make_stepper(slots)
+        config = dict(best, slots=slots)
+        transport(stepper, primaries)  # warm-up (graph capture, first touch)
+        t = run(stepper, config)
+        if t and (winner is None or t.seconds < winner.seconds):
+            winner = t
+        del stepper
+    best = dict(winner.config)
+    stepper = make_stepper(best["slots"])
+    transport(stepper, primaries)
+
+    for name, values in (("along_block_size", block_sizes),
+                         ("along_persistent", (0, 1)),
+                         ("sort_threshold", thresholds)):
+        winner = None
+        for v in values:
+            t = run(stepper, dict(best, **{name: v}))
+            if t and (winner is None or t.seconds < winner.seconds):
+                winner = t
+        if winner is not None:
+            best = dict(winner.config)
+    return best, trials

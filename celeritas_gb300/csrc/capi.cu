@@ -368,6 +368,24 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
     });
 }
 
+int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value)
+{
+    return guarded([&] {
+        if (!name)
+            throw std::runtime_error("null argument");
+        stepper->stepper->set_tuning(name, value);
+    });
+}
+
+int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* value)
+{
+    return guarded([&] {
+        if (!name || !value)
+            throw std::runtime_error("null argument");
+        *value = stepper->stepper->tuning(name);
+    });
+}
+
 static_assert(GBX_STATIC_SCRATCH_MAX_SLOTS == gbx::static_scratch_max_slots,
               "public and internal static scratch limits differ");
 

@@ -137,11 +137,13 @@ void step_secondaries(CoreParams const&, CoreState& state, ActionId)
 }
 void step_sort_along(CoreParams const&, CoreState& state, ActionId)
 {
-    launch_sort_tracks(state.context(), SortKey::along_step, state.stream());
+    if (state.context().sort_enabled)
+        launch_sort_tracks(state.context(), SortKey::along_step, state.stream());
 }
 void step_sort_post(CoreParams const&, CoreState& state, ActionId)
 {
-    launch_sort_tracks(state.context(), SortKey::step_limit, state.stream());
+    if (state.context().sort_enabled)
+        launch_sort_tracks(state.context(), SortKey::step_limit, state.stream());
 }
 
 }  // namespace
@@ -540,8 +542,11 @@ CoreState::CoreState(CoreParams const& params,
     // Persistent charged along-step: on by default in the mixed-precision
     // build, where it outruns the one-thread-per-track kernel; in FP64 the
     // diverged FP64 multiple-scattering code makes it slower
-    ctx_.persistent_blocks
-        = sizeof(real_type) < sizeof(double) ? persistent_along_blocks() : 0;
+    ctx_.along_block_size = block_size;
+    ctx_.sort_enabled = true;
+    ctx_.persistent_blocks = sizeof(real_type) < sizeof(double)
+                                 ? persistent_along_blocks(ctx_.along_block_size)
+                                 : 0;
     ctx_.log = static_cast<StepRecord*>(at(o_log));
     ctx_.log_capacity = log_cap;
     ctx_.step_index = static_cast<size_type*>(at(o_stepidx));
@@ -590,6 +595,48 @@ void CoreState::insert_primaries(TrackInitializer const* host_primaries, size_ty
                              cudaMemcpyHostToDevice,
                              stream_));
     pending_primaries_ = n;
+}
+
+void CoreState::set_tuning(std::string const& name, long long value)
+{
+    if (name == "along_block_size")
+    {
+        if (value != 64 && value != 128 && value != 256)
+        {
+            throw std::runtime_error(
+                "along_block_size must be 64, 128 or 256 (512 threads exceed the "
+                "register file of the charged along-step kernel)");
+        }
+        ctx_.along_block_size = static_cast<int>(value);
+        if (ctx_.persistent_blocks > 0)
+            ctx_.persistent_blocks = persistent_along_blocks(ctx_.along_block_size);
+    }
+    else if (name == "along_persistent")
+    {
+        ctx_.persistent_blocks
+            = value ? persistent_along_blocks(ctx_.along_block_size) : 0;
+        if (value && ctx_.persistent_blocks == 0)
+            throw std::runtime_error("persistent along-step kernel cannot be resident");
+    }
+    else if (name == "sort")
+    {
+        ctx_.sort_enabled = value != 0;
+    }
+    else
+    {
+        throw std::runtime_error("unknown tuning parameter '" + name + "'");
+    }
+}
+
+long long CoreState::tuning(std::string const& name) const
+{
+    if (name == "along_block_size")
+        return ctx_.along_block_size;
+    if (name == "along_persistent")
+        return ctx_.persistent_blocks > 0;
+    if (name == "sort")
+        return ctx_.sort_enabled;
+    throw std::runtime_error("unknown tuning parameter '" + name + "'");
 }
 
 std::vector<size_type> CoreState::event_live(size_type n) const
@@ -784,31 +831,76 @@ Stepper::Stepper(StepperInput const& input)
 
 Stepper::~Stepper()
 {
-    if (graph_exec_)
-        cudaGraphExecDestroy(graph_exec_);
-    if (graph_)
-        cudaGraphDestroy(graph_);
+    this->clear_graphs();
     state_.reset();
     if (stream_)
         cudaStreamDestroy(stream_);
 }
 
+void Stepper::clear_graphs()
+{
+    for (int i = 0; i < 2; ++i)
+    {
+        if (graph_exec_[i])
+            cudaGraphExecDestroy(graph_exec_[i]);
+        if (graph_[i])
+            cudaGraphDestroy(graph_[i]);
+        graph_exec_[i] = nullptr;
+        graph_[i] = nullptr;
+    }
+}
+
 void Stepper::build_graph()
 {
+    int const k = state_->context().sort_enabled ? 1 : 0;
     GBX_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     actions_->step(*params_, *state_);
-    GBX_CUDA(cudaStreamEndCapture(stream_, &graph_));
-    GBX_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+    GBX_CUDA(cudaStreamEndCapture(stream_, &graph_[k]));
+    GBX_CUDA(cudaGraphInstantiate(&graph_exec_[k], graph_[k], 0));
+}
+
+void Stepper::update_sort_policy()
+{
+    if (sort_threshold_ <= 0)
+        return;
+    bool const sort = static_cast<long long>(last_active_) >= sort_threshold_;
+    if (sort != state_->context().sort_enabled)
+        state_->set_tuning("sort", sort);
+}
+
+void Stepper::set_tuning(std::string const& name, long long value)
+{
+    if (name == "sort_threshold")
+    {
+        if (value < 0)
+            throw std::runtime_error("sort_threshold must be nonnegative");
+        sort_threshold_ = value;
+        if (value == 0)
+            state_->set_tuning("sort", 1);
+    }
+    else
+    {
+        state_->set_tuning(name, value);
+    }
+    this->clear_graphs();
+}
+
+long long Stepper::tuning(std::string const& name) const
+{
+    if (name == "sort_threshold")
+        return sort_threshold_;
+    return state_->tuning(name);
 }
 
 size_type Stepper::graph_kernel_count()
 {
-    if (!graph_exec_)
+    int const k = state_->context().sort_enabled ? 1 : 0;
+    if (!graph_exec_[k])
         this->build_graph();
     std::size_t num_nodes = 0;
-    GBX_CUDA(cudaGraphGetNodes(graph_, nullptr, &num_nodes));
+    GBX_CUDA(cudaGraphGetNodes(graph_[k], nullptr, &num_nodes));
     std::vector<cudaGraphNode_t> nodes(num_nodes);
-    GBX_CUDA(cudaGraphGetNodes(graph_, nodes.data(), &num_nodes));
+    GBX_CUDA(cudaGraphGetNodes(graph_[k], nodes.data(), &num_nodes));
     size_type kernels = 0;
     for (auto node : nodes)
     {
@@ -827,9 +919,10 @@ void Stepper::launch_steps(size_type count)
         if (use_graph_ && state_->pending_primaries() == 0
             && !actions_->action_times_enabled())
         {
-            if (!graph_exec_)
+            int const k = state_->context().sort_enabled ? 1 : 0;
+            if (!graph_exec_[k])
                 this->build_graph();
-            GBX_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+            GBX_CUDA(cudaGraphLaunch(graph_exec_[k], stream_));
         }
         else
         {
@@ -859,12 +952,15 @@ StepperResult Stepper::operator()(std::vector<TrackInitializer> const& primaries
 
 StepperResult Stepper::operator()()
 {
+    this->update_sort_policy();
     size_type idx = state_->step_index();
     this->launch_steps(1);
     Counters c = state_->counters();
     if (c.error_flags & error_initializer_overflow)
         throw std::runtime_error("insufficient capacity for track initializers");
-    return this->read_record(idx);
+    StepperResult r = this->read_record(idx);
+    last_active_ = r.alive + r.queued;
+    return r;
 }
 
 std::vector<StepperResult> Stepper::run_until_empty(size_type max_steps,
@@ -878,6 +974,7 @@ std::vector<StepperResult> Stepper::run_until_empty(size_type max_steps,
     while (!done && taken < max_steps)
     {
         size_type n = std::min(batch, max_steps - taken);
+        this->update_sort_policy();
         this->launch_steps(n);
         Counters c = state_->counters();
         if (c.error_flags & error_initializer_overflow)
@@ -891,6 +988,7 @@ std::vector<StepperResult> Stepper::run_until_empty(size_type max_steps,
             out.active = r.active;
             out.alive = r.alive;
             results.push_back(out);
+            last_active_ = out.alive + out.queued;
             if (!out)
             {
                 done = true;

@@ -166,18 +166,6 @@ __global__ __launch_bounds__(block_size) void pre_step_kernel(ParamsData p,
     }
 }
 
-__global__ __launch_bounds__(block_size, 1) void along_step_kernel(ParamsData p,
-                                                                StateData s,
-                                                                size_type action)
-{
-    size_type slot = thread_slot();
-    if (slot < s.size
-        && (action == invalid_id || s.along_step_action[slot] == action))
-    {
-        along_step(p, s, slot);
-    }
-}
-
 __global__ __launch_bounds__(block_size) void discrete_select_kernel(
     ParamsData p, StateData s)
 {
@@ -185,76 +173,6 @@ __global__ __launch_bounds__(block_size) void discrete_select_kernel(
     if (slot < s.size)
     {
         discrete_select(p, s, slot);
-    }
-}
-
-__global__ __launch_bounds__(block_size) void interact_kernel(ParamsData p,
-                                                              StateData s,
-                                                              size_type action)
-{
-    size_type slot = thread_slot();
-    if (slot < s.size)
-    {
-        interact(p, s, slot, action);
-    }
-}
-
-//! All model actions for the slots that selected one (the model actions are
-//! mutually exclusive per slot, so one launch applies each slot's model)
-__global__ __launch_bounds__(block_size) void interact_all_kernel(ParamsData p,
-                                                                  StateData s)
-{
-    size_type slot = thread_slot();
-    if (slot < s.size)
-    {
-        size_type a = s.post_step_action[slot];
-        if (a >= p.model_to_action && a < p.model_to_action + p.num_models)
-        {
-            interact(p, s, slot, a);
-        }
-    }
-}
-
-__global__ __launch_bounds__(block_size) void boundary_kernel(ParamsData p,
-                                                              StateData s)
-{
-    size_type slot = thread_slot();
-    if (slot < s.size)
-    {
-        boundary_cross(p, s, slot);
-    }
-}
-
-__global__ __launch_bounds__(block_size) void tracking_cut_kernel(ParamsData p,
-                                                                  StateData s)
-{
-    size_type slot = thread_slot();
-    if (slot < s.size)
-    {
-        tracking_cut(p, s, slot);
-    }
-}
-
-//! Post-step boundary crossing, tracking cut and calorimeter tally fused
-__global__ __launch_bounds__(block_size) void post_kernel(ParamsData p,
-                                                          StateData s)
-{
-    size_type slot = thread_slot();
-    if (slot < s.size)
-    {
-        boundary_cross(p, s, slot);
-        tracking_cut(p, s, slot);
-        if (s.status[slot] != status_inactive)
-        {
-            size_type det = s.detector[slot];
-            if (det != invalid_id)
-            {
-                double const edep = s.energy_deposition[slot];
-                atomicAdd(s.calo_edep + det, edep);
-                if (p.event_tallies)
-                    atomicAdd(s.event_edep + s.event_id[slot], edep);
-            }
-        }
     }
 }
 
@@ -580,14 +498,22 @@ __global__ __launch_bounds__(sort_block_size) void sort_scatter_kernel(
     }
 }
 
-//! Slot of this thread within the sorted bins [first_bin, end_bin)
+//! Slot of this thread within the sorted bins [first_bin, end_bin), or,
+//! without offsets (sorting off), the thread's own slot: the action
+//! functions then skip slots whose action is not theirs, as the sort would
 __device__ __forceinline__ bool sorted_slot(StateData const& s,
                                             size_type const* offsets,
                                             size_type first_bin,
                                             size_type end_bin,
                                             size_type* slot)
 {
-    size_type const t = offsets[first_bin] + blockIdx.x * blockDim.x + threadIdx.x;
+    size_type const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!offsets)
+    {
+        *slot = i;
+        return i < s.size;
+    }
+    size_type const t = offsets[first_bin] + i;
     if (t >= offsets[end_bin])
         return false;
     *slot = s.track_slots[t];
@@ -628,8 +554,8 @@ __global__ __launch_bounds__(block_size, 1) void along_charged_persistent_kernel
     size_type bin,
     size_type* work_counter)
 {
-    size_type const first = offsets[bin];
-    size_type const count = offsets[bin + 1] - first;
+    size_type const first = offsets ? offsets[bin] : 0;
+    size_type const count = offsets ? offsets[bin + 1] - first : s.size;
     unsigned int const lane = threadIdx.x & 31u;
     FieldOptions const opt;
     FieldPropagation fp(opt, UniformFieldEquation{});
@@ -650,7 +576,7 @@ __global__ __launch_bounds__(block_size, 1) void along_charged_persistent_kernel
             size_type const idx = base + rank;
             if (idx >= count)
                 break;
-            slot = s.track_slots[first + idx];
+            slot = offsets ? s.track_slots[first + idx] : idx;
             bool charged;
             if (!along_prologue<AlongKind::charged>(p, s, slot, &charged))
                 continue;
@@ -685,7 +611,7 @@ __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
     if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
     {
         size_type a = s.post_step_action[slot];
-        if (a >= p.model_to_action && a < p.model_to_action + p.num_models)
+        if (a >= first_bin && a < end_bin)
             interact(p, s, slot, a);
     }
 }
@@ -750,44 +676,50 @@ void launch_pre_step(LaunchContext const& ctx, cudaStream_t stream)
         ctx.params, ctx.state);
 }
 
+//! Bin offsets of a sort key, or none (slots in their own order) when the
+//! track order does not sort by that key or sorting is switched off
+inline size_type const* key_offsets(LaunchContext const& ctx, SortKey key, bool sorts)
+{
+    return sorts && ctx.sort_enabled ? sort_offsets(ctx, key) : nullptr;
+}
+
 void launch_along_step(LaunchContext const& ctx,
                        size_type action,
                        cudaStream_t stream)
 {
+    // Each along-step action runs a kernel compiled for that action only,
+    // over its sorted range or (sorting off) over all slots; the grid covers
+    // the largest range. Sorted and unsorted orders thus run the same code,
+    // and a track's result does not depend on the track order.
     ParamsData const& p = ctx.params;
-    if (sorts_along_step(p.track_order))
+    unsigned int const nb = num_blocks_for(ctx.state.size);
+    unsigned int const abs = static_cast<unsigned int>(ctx.along_block_size);
+    unsigned int const anb = (ctx.state.size + abs - 1) / abs;
+    size_type const* offsets
+        = key_offsets(ctx, SortKey::along_step, sorts_along_step(p.track_order));
+    if (action == invalid_id || action == p.action_along_step)
     {
-        // Launch each along-step action over its sorted range with a kernel
-        // compiled for that action only; the grid covers the largest range
-        unsigned int const nb = num_blocks_for(ctx.state.size);
-        size_type const* offsets = sort_offsets(ctx, SortKey::along_step);
-        if (action == invalid_id || action == p.action_along_step)
+        if (p.has_field && ctx.persistent_blocks > 0)
         {
-            if (p.has_field && ctx.persistent_blocks > 0)
-            {
-                cudaMemsetAsync(ctx.work_counter, 0, sizeof(size_type), stream);
-                along_charged_persistent_kernel<<<ctx.persistent_blocks, block_size, 0, stream>>>(
-                    p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
-            }
-            else
-            {
-                along_step_sorted_kernel<AlongKind::charged><<<nb, block_size, 0, stream>>>(
-                    p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
-            }
+            cudaMemsetAsync(ctx.work_counter, 0, sizeof(size_type), stream);
+            along_charged_persistent_kernel<<<ctx.persistent_blocks, abs, 0, stream>>>(
+                p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
         }
-        if (action == invalid_id || action == p.action_along_step_neutral)
+        else
         {
-            along_step_sorted_kernel<AlongKind::neutral><<<nb, block_size, 0, stream>>>(
-                p,
-                ctx.state,
-                offsets,
-                p.action_along_step_neutral,
-                p.action_along_step_neutral + 1);
+            along_step_sorted_kernel<AlongKind::charged><<<anb, abs, 0, stream>>>(
+                p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
         }
-        return;
     }
-    along_step_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-        ctx.params, ctx.state, action);
+    if (action == invalid_id || action == p.action_along_step_neutral)
+    {
+        along_step_sorted_kernel<AlongKind::neutral><<<nb, block_size, 0, stream>>>(
+            p,
+            ctx.state,
+            offsets,
+            p.action_along_step_neutral,
+            p.action_along_step_neutral + 1);
+    }
 }
 
 void launch_discrete_select(LaunchContext const& ctx, cudaStream_t stream)
@@ -799,62 +731,41 @@ void launch_discrete_select(LaunchContext const& ctx, cudaStream_t stream)
 void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
-    if (sorts_step_limit(p.track_order))
-    {
-        size_type first = action, end = action + 1;
-        if (action == invalid_id)
-        {
-            first = p.model_to_action;
-            end = p.model_to_action + p.num_models;
-        }
-        interact_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p, ctx.state, sort_offsets(ctx, SortKey::step_limit), first, end);
-        return;
-    }
+    size_type first = action, end = action + 1;
     if (action == invalid_id)
     {
-        interact_all_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            ctx.params, ctx.state);
+        // All models at once: they are mutually exclusive per slot
+        first = p.model_to_action;
+        end = p.model_to_action + p.num_models;
     }
-    else
-    {
-        interact_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            ctx.params, ctx.state, action);
-    }
+    interact_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        p,
+        ctx.state,
+        key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
+        first,
+        end);
 }
 
 void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
-    if (sorts_step_limit(p.track_order))
-    {
-        boundary_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p,
-            ctx.state,
-            sort_offsets(ctx, SortKey::step_limit),
-            p.action_boundary,
-            p.action_boundary + 1);
-        return;
-    }
-    boundary_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-        ctx.params, ctx.state);
+    boundary_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        p,
+        ctx.state,
+        key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
+        p.action_boundary,
+        p.action_boundary + 1);
 }
 
 void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
-    if (sorts_step_limit(p.track_order))
-    {
-        tracking_cut_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            p,
-            ctx.state,
-            sort_offsets(ctx, SortKey::step_limit),
-            p.action_tracking_cut,
-            p.action_tracking_cut + 1);
-        return;
-    }
-    tracking_cut_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-        ctx.params, ctx.state);
+    tracking_cut_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        p,
+        ctx.state,
+        key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
+        p.action_tracking_cut,
+        p.action_tracking_cut + 1);
 }
 
 void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream)
@@ -872,14 +783,14 @@ void launch_extend_from_secondaries(LaunchContext const& ctx, cudaStream_t strea
     scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, ctx.scratch);
 }
 
-int persistent_along_blocks()
+int persistent_along_blocks(int threads_per_block)
 {
     int device = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&device) != cudaSuccess
         || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)
                != cudaSuccess
         || cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-               &per_sm, along_charged_persistent_kernel, block_size, 0)
+               &per_sm, along_charged_persistent_kernel, threads_per_block, 0)
                != cudaSuccess)
     {
         return 0;
@@ -913,22 +824,6 @@ void launch_sort_tracks(LaunchContext const& ctx, SortKey key, cudaStream_t stre
                           sort_block_size,
                           (sort_block_size / 32) * srt.num_bins * sizeof(size_type),
                           stream>>>(ctx.state, srt, key);
-}
-
-void launch_step(LaunchContext const& ctx, cudaStream_t stream)
-{
-    launch_initialize_tracks(ctx, stream);
-    launch_pre_step(ctx, stream);
-    if (sorts_along_step(ctx.params.track_order))
-        launch_sort_tracks(ctx, SortKey::along_step, stream);
-    launch_along_step(ctx, invalid_id, stream);
-    launch_discrete_select(ctx, stream);
-    if (sorts_step_limit(ctx.params.track_order))
-        launch_sort_tracks(ctx, SortKey::step_limit, stream);
-    launch_interact(ctx, invalid_id, stream);
-    post_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-        ctx.params, ctx.state);
-    launch_extend_from_secondaries(ctx, stream);
 }
 
 //---------------------------------------------------------------------------//

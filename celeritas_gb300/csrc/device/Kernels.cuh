@@ -62,6 +62,10 @@ struct LaunchContext
     //! its device work counter
     int persistent_blocks;
     size_type* work_counter;
+    //! Tuning: threads per block of the charged along-step kernels (at most
+    //! block_size) and whether the action sorts run this step
+    int along_block_size;
+    bool sort_enabled;
     StepRecord* log;  //!< Step log (ring buffer)
     size_type log_capacity;
     size_type* step_index;  //!< Device-resident step counter
@@ -89,7 +93,7 @@ void launch_extend_from_secondaries(LaunchContext const& ctx,
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
 //! Resident blocks of the persistent charged along-step kernel on the
 //! current device (SMs x blocks per SM at full occupancy), 0 on failure
-int persistent_along_blocks();
+int persistent_along_blocks(int threads_per_block);
 //! Count live tracks (slots and queued initializers) of events [0, n) into
 //! state.event_live
 void launch_count_event_live(LaunchContext const& ctx,
@@ -106,8 +110,5 @@ constexpr size_type static_scratch_max_slots = 131072;
 //! first call on a device looks up the array's address on that device.
 void launch_extend_from_secondaries_static(LaunchContext const& ctx,
                                            cudaStream_t stream);
-
-//! One full step without primary insertion (graph-capturable)
-void launch_step(LaunchContext const& ctx, cudaStream_t stream);
 
 }  // namespace gbx

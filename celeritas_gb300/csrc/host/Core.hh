@@ -170,6 +170,11 @@ class CoreState
     Counters counters() const;
     //! Number of completed steps recorded on the device
     size_type step_index() const;
+    //! Launch tuning: "along_block_size" (64, 128, 256), "along_persistent"
+    //! (0/1), "sort" (0/1: whether the action sorts run)
+    void set_tuning(std::string const& name, long long value);
+    long long tuning(std::string const& name) const;
+
     //! Live tracks (slots and queued initializers) per event [0, n)
     std::vector<size_type> event_live(size_type n) const;
     //! Energy deposited in detectors per event [0, n); optionally cleared
@@ -280,14 +285,26 @@ class Stepper
     std::vector<double> energy_deposition() const;
     void clear_energy_deposition();
 
+    //! Launch tuning (see CoreState::set_tuning) plus "sort_threshold": the
+    //! action sorts run only in steps that start with at least this many
+    //! active tracks (0: always). Drops the captured step graphs.
+    void set_tuning(std::string const& name, long long value);
+    long long tuning(std::string const& name) const;
+
   private:
     std::shared_ptr<CoreParams const> params_;
     std::unique_ptr<CoreState> state_;
     std::unique_ptr<ActionSequence> actions_;
     cudaStream_t stream_{nullptr};
-    cudaGraphExec_t graph_exec_{nullptr};
-    cudaGraph_t graph_{nullptr};
+    // Captured step graphs, without (0) and with (1) the action sorts
+    cudaGraphExec_t graph_exec_[2]{nullptr, nullptr};
+    cudaGraph_t graph_[2]{nullptr, nullptr};
     bool use_graph_{true};
+    long long sort_threshold_{0};
+    size_type last_active_{0};
+
+    void clear_graphs();
+    void update_sort_policy();
 
     void launch_steps(size_type count);
     void build_graph();

@@ -16,6 +16,8 @@ PrimaryGenerator (src/celeritas/phys/PrimaryGenerator.cc).
 
 from __future__ import annotations
 
+import numpy as np
+
 from .primaries import eta_beam, pencil_beam, spread_beam
 
 WORKLOADS = {
@@ -42,6 +44,18 @@ WORKLOADS = {
                            "(r 180-295 cm), 3.8 T along z, Urban MSC; events of 50 "
                            "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
                            "one bench step = 65 of the 1300 events"),
+    # Batching of uneven events: CMS-like detector, 4096 events with primaries
+    # per event log-uniform in 1-1000 and energies log-uniform in
+    # 0.1-100 GeV (e-/gamma alternating, |eta| < 1.5), all in flight
+    # together, per-track random streams, autotuned launch configuration
+    "c4": dict(geometry="cms", physics="cms", events=4096, min_primaries=1,
+               max_primaries=1000, energy=100.0, emax=1e5, pdgs=(11, 22), eta_max=1.5,
+               slots=1 << 21, seed=0, msc=True, field=(0.0, 0.0, 3.8),
+               bench_events=64, calibration_events=8,
+               description="batching: CMS-like, events with log-uniform 1-1000 "
+                           "e-/gamma primaries of log-uniform 0.1-100 GeV, |eta| < 1.5, "
+                           "3.8 T; one bench step = 64 of the 4096 events in flight "
+                           "together; launch configuration autotuned"),
     # Serving: Poisson arrivals, Pareto(1.5) primaries per event capped at
     # 5000, CMS-like (as c3) or calorimeter (as c2) 50/50, one pool of 2^21
     # slots per geometry (2^22 in all) with queues of 16 x slots
@@ -82,3 +96,19 @@ def physics_args(wl: dict) -> list[str]:
     if any(wl["field"]):
         args += ["--field"] + [repr(float(f)) for f in wl["field"]]
     return args
+
+
+def make_uneven_events(wl: dict, num_events: int, first_event: int = 0, seed: int = 0):
+    """Primaries of 'num_events' events of the batching workload: each event
+    draws its primary count log-uniformly in [min, max] primaries."""
+    rng = np.random.default_rng(wl["seed"] + 7 * seed)
+    counts = np.exp(rng.uniform(np.log(wl["min_primaries"]),
+                                np.log(wl["max_primaries"] + 1), num_events))
+    counts = np.minimum(counts.astype(int), wl["max_primaries"])
+    parts = []
+    for k, n in enumerate(counts):
+        p = eta_beam(int(max(n, 1)), emin=wl["energy"], emax=wl["emax"], pdgs=wl["pdgs"],
+                     eta_max=wl["eta_max"], seed=int(rng.integers(1 << 31)))
+        p["event"] = first_event + k
+        parts.append(p)
+    return np.concatenate(parts)

@@ -218,6 +218,19 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
                                         size_t num_events,
                                         int clear);
 
+/* Launch tuning of a stepper, for an autotuner (no counterpart in the
+ * reference, whose block sizes and sort policy are build and run options):
+ *   "along_block_size"  threads per block of the charged along-step (64, 128, 256)
+ *   "along_persistent"  1: charged along-step as a persistent kernel that
+ *                       interleaves field substeps of different tracks
+ *   "sort_threshold"    with an action-sorting track order, sort only in
+ *                       steps that start with at least this many live
+ *                       tracks (0: always)
+ * Results do not depend on these settings. Setting one drops the captured
+ * step graphs. */
+int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value);
+int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* value);
+
 /* Largest stepper (track slots) accepted by
  * gbx_stepper_extend_from_secondaries_static */
 #define GBX_STATIC_SCRATCH_MAX_SLOTS 131072

@@ -1,0 +1,113 @@
+"""Launch tuning and the autotuner (GB300, batching configuration).
+
+With per-track random streams the launch configuration of a stepper changes
+its speed, not its results: every event's energy deposition must be the same
+under each tuning (threads per block of the charged along-step, persistent
+charged kernel, action sorts on or off) and each track order to 1e-12
+relative (the device tally sums with atomics, so only the summation order
+differs). This holds in the mixed-precision build too, whose compiler may
+contract multiply-adds, because sorted and unsorted orders run the same
+per-action kernels. Invalid settings
+are rejected without touching the stepper. The autotuner returns a valid
+configuration from the candidates it measured.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EDEP_RTOL = 1e-12
+SLOTS = 1 << 15
+NUM_EVENTS = 6
+
+
+@pytest.fixture(scope="module")
+def gb(built_lib):
+    import celeritas_gb300 as gb
+    from celeritas_gb300.build import build
+
+    gb.load_library(built_lib)
+    gb.load_library(build(precision="mixed"), precision="mixed")
+    return gb
+
+
+def cms_params(gb, precision, track_order="reindex_both_action"):
+    return gb.Params(gb.physics_file("cms"), "cms", field_tesla=(0.0, 0.0, 3.8), msc=True,
+                     track_order=track_order, precision=precision,
+                     rng_per_track=True, event_tallies=True)
+
+
+def events():
+    from celeritas_gb300.workloads import WORKLOADS, make_uneven_events
+
+    wl = dict(WORKLOADS["c4"], max_primaries=12, emax=3000.0, energy=100.0)
+    return make_uneven_events(wl, NUM_EVENTS, seed=3)
+
+
+def per_event_edep(stepper, prim):
+    from celeritas_gb300 import autotune
+
+    autotune.transport(stepper, prim)
+    return stepper.event_energy_deposition(NUM_EVENTS)
+
+
+TUNINGS = [
+    {},
+    {"along_block_size": 64},
+    {"along_block_size": 128, "along_persistent": 0},
+    {"sort": 0},
+    {"sort_threshold": 1 << 30},
+    {"along_persistent": 1, "along_block_size": 128},
+]
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_results_independent_of_tuning(gb, precision):
+    params = cms_params(gb, precision)
+    prim = events()
+    base = per_event_edep(gb.Stepper(params, SLOTS, seed=5), prim)
+    assert np.all(base > 0)
+    for tuning in TUNINGS[1:]:
+        st = gb.Stepper(params, SLOTS, seed=5)
+        st.set_tuning(**tuning)
+        for key, value in tuning.items():
+            if key != "sort_threshold":
+                assert st.get_tuning(key) == value
+        np.testing.assert_allclose(per_event_edep(st, prim), base, rtol=EDEP_RTOL,
+                                   err_msg=str(tuning))
+    for order in ("none", "reindex_along_step_action", "reindex_step_limit_action"):
+        st = gb.Stepper(cms_params(gb, precision, order), SLOTS, seed=5)
+        np.testing.assert_allclose(per_event_edep(st, prim), base, rtol=EDEP_RTOL,
+                                   err_msg=order)
+
+
+def test_invalid_tuning_rejected(gb):
+    params = cms_params(gb, "mixed")
+    st = gb.Stepper(params, SLOTS, seed=5)
+    before = st.get_tuning("along_block_size")
+    for bad in ({"along_block_size": 512}, {"along_block_size": 96},
+                {"no_such_setting": 1}):
+        with pytest.raises(gb.GbxError):
+            st.set_tuning(**bad)
+    assert st.get_tuning("along_block_size") == before
+    # The stepper still transports after the rejected settings
+    assert per_event_edep(st, events()).sum() > 0
+
+
+def test_autotuner_picks_a_measured_candidate(gb):
+    from celeritas_gb300 import autotune
+
+    params = cms_params(gb, "mixed")
+    prim = events()
+    best, trials = autotune.autotune(lambda n: gb.Stepper(params, n, seed=5), prim,
+                                     slot_counts=(1 << 14, 1 << 15),
+                                     block_sizes=(128, 256, 512), thresholds=(0, 1 << 30))
+    measured = [t for t in trials if t.seconds]
+    assert best in [t.config for t in measured]
+    assert all(t.track_steps > 0 for t in measured)
+    rejected = [t for t in trials if not t.seconds]
+    assert [t.config["along_block_size"] for t in rejected] == [512]
+    assert "512" in rejected[0].note
+    assert best["along_block_size"] in (128, 256)
+    assert best["slots"] in (1 << 14, 1 << 15)
