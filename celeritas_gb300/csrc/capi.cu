@@ -130,6 +130,7 @@ FieldRef find_field(gbx::CoreState& st, std::string const& name)
     if (name == "next_surface") return f(s.next_surface);
     if (name == "next_sense") return f(s.next_sense);
     if (name == "geo_failed") return f(s.geo_failed);
+    if (name == "num_looping_steps") return f(s.num_looping_steps);
     if (name == "material") return f(s.material);
     if (name == "interaction_mfp") return f(s.interaction_mfp);
     if (name == "dedx_range") return f(s.dedx_range);

@@ -580,9 +580,7 @@ GBX_FUNCTION void apply_interaction(ParamsData const& p,
     if (result.action != Interaction::absorbed)
     {
         GeoTrackView geo(p.geo, s, slot);
-        geo.set_dir(Real3{double(result.direction.x),
-                          double(result.direction.y),
-                          double(result.direction.z)});
+        geo.set_dir(to_geo_dir(result.direction));
     }
     else
     {

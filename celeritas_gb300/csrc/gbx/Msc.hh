@@ -621,7 +621,7 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
         }
     }
     RVec3 newdir = rotate(from_spherical(costheta, phi), inc_dir);
-    geo.set_dir(Real3{double(newdir.x), double(newdir.y), double(newdir.z)});
+    geo.set_dir(to_geo_dir(newdir));
     if (displace)
     {
         Real3 pos = geo.pos();

@@ -183,9 +183,7 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
         ti.event_id = s.event_id[slot];
         ti.time = s.time[slot];
         ti.pos = {s.pos[0][slot], s.pos[1][slot], s.pos[2][slot]};
-        ti.dir = {double(secondary.direction.x),
-                  double(secondary.direction.y),
-                  double(secondary.direction.z)};
+        ti.dir = to_geo_dir(secondary.direction);
         ti.particle_id = secondary.particle_id;
         ti.energy = secondary.energy;
         if (!initialized && status != status_alive)

@@ -135,6 +135,24 @@ GBX_FORCEINLINE Vec3<T> make_unit_vector(Vec3<T> const& v)
     return {v.x * scale, v.y * scale, v.z * scale};
 }
 
+//! Geometry direction from a physics direction. The geometry solves its
+//! surface intersections for a unit direction (the cylinder quadratic takes
+//! dx^2 + dy^2 as 1 - dz^2); a direction computed in FP32 is a unit vector
+//! only to FP32 rounding (|d|^2 - 1 up to ~1e-7), which moves the roots by
+//! ~1e-7 of the distance, far more than the bump that decides which volume
+//! lies across a crossing. FP32 directions are therefore renormalized in
+//! FP64; FP64 directions pass through unchanged.
+template<class T>
+GBX_FORCEINLINE Vec3<double> to_geo_dir(Vec3<T> const& d)
+{
+    Vec3<double> r{double(d.x), double(d.y), double(d.z)};
+    if constexpr (sizeof(T) < sizeof(double))
+    {
+        r = make_unit_vector(r);
+    }
+    return r;
+}
+
 //! y <- a * x + y, with fma per component
 template<class T>
 GBX_FORCEINLINE void axpy(T a, Vec3<T> const& x, Vec3<T>* y)

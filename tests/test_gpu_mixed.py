@@ -80,3 +80,52 @@ def test_track_steps_agree(results):
     sd = results["double"][1].sum()
     sm = results["mixed"][1].sum()
     assert abs(sm - sd) / sd < STEPS_RTOL, (sm, sd)
+
+
+# Silicon tracker shells of the CMS-like geometry: inner radius of layer k,
+# 0.3 mm thick
+def si_inner_radius(k):
+    return 4.0 + k * (110.0 - 4.0) / 9
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_cms_tracks_stay_in_their_volumes(built_lib, precision):
+    """Every live track logically inside a silicon shell lies within it.
+
+    FP32 physics directions are unit vectors only to FP32 rounding; the
+    geometry must receive them renormalized, or its crossing distances are off
+    by ~1e-7 of the distance and a track can be placed across a 0.3 mm shell
+    into the wrong volume (it then deposits silicon energy loss over
+    centimetres of gap).
+    """
+    import celeritas_gb300 as gb
+    from celeritas_gb300.build import build
+    from celeritas_gb300.workloads import WORKLOADS, make_primaries
+
+    gb.load_library(build(precision=precision), precision=precision)
+    wl = WORKLOADS["c3"]
+    params = gb.Params(gb.physics_file("cms"), "cms", field_tesla=wl["field"], msc=True,
+                       track_order="reindex_both_action", precision=precision)
+    det = params.detector_labels()
+    inner = np.full(len(det) + 1, np.nan)
+    for k in range(10):
+        inner[det.index(f"si_{k}")] = si_inner_radius(k)
+    st = gb.Stepper(params, 1 << 16, seed=3, use_graph=False)
+    st.step(make_primaries(wl, num=100))
+    checked = 0
+    for _ in range(60):
+        st.step()
+        status = st.get_state("status", np.uint8)
+        d = st.get_state("detector", np.uint32).astype(np.int64)
+        d = np.where(d < len(det), d, len(det))
+        x = st.get_state("pos_x", np.float64)
+        y = st.get_state("pos_y", np.float64)
+        r = np.hypot(x, y)
+        lo = inner[d]
+        sel = np.isfinite(lo) & (status == 2)
+        checked += int(sel.sum())
+        outside = sel & ((r < lo - 1e-6) | (r > lo + 0.03 + 1e-6))
+        assert not outside.any(), (
+            f"{int(outside.sum())} tracks outside their silicon shell, e.g. r = "
+            f"{r[outside][:3]} in layers {[det[i] for i in d[outside][:3]]}")
+    assert checked > 100
