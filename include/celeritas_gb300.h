@@ -226,6 +226,8 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
  *   "sort_threshold"    with an action-sorting track order, sort only in
  *                       steps that start with at least this many live
  *                       tracks (0: always)
+ *   "sort"              0: action sorts off (each action kernel visits
+ *                       every slot), 1: on; reset by the sort threshold
  * Results do not depend on these settings. Setting one drops the captured
  * step graphs. */
 int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value);
