@@ -111,6 +111,7 @@ _PROTOTYPES = [
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_size_t),
       ctypes.POINTER(ctypes.c_size_t)]),
     ("gbx_stepper_extend_from_secondaries_static", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_stepper_reseed", ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong]),
     ("gbx_stepper_set_tuning", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong]),
     ("gbx_stepper_get_tuning", ctypes.c_int,
@@ -293,6 +294,10 @@ class Stepper:
 
     def kill_active(self):
         _check(self._lib, self._lib.gbx_stepper_kill_active(self._handle))
+
+    def reseed(self, event_id: int):
+        """Reseed every slot's random state for an event (Stepper::reseed)."""
+        _check(self._lib, self._lib.gbx_stepper_reseed(self._handle, int(event_id)))
 
     def set_tuning(self, **settings):
         """Launch tuning: along_block_size, along_persistent, sort_threshold."""

@@ -405,6 +405,11 @@ int gbx_stepper_kill_active(gbx_stepper* stepper)
     return guarded([&] { stepper->stepper->kill_active(); });
 }
 
+int gbx_stepper_reseed(gbx_stepper* stepper, unsigned long long event_id)
+{
+    return guarded([&] { stepper->stepper->reseed(event_id); });
+}
+
 int gbx_stepper_synchronize(gbx_stepper* stepper)
 {
     return guarded([&] {

@@ -300,6 +300,7 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_mscm = pk.add(h.msc_materials);
     std::size_t o_mscp = pk.add(h.msc_par_mat);
     std::size_t o_loop = pk.add(h.looping);
+    std::size_t o_jump = pk.add(h.rng_jump);
     std::size_t o_pl = pk.add(h.surfaces);
     std::size_t o_box = pk.add(h.volumes);
     std::size_t o_no = pk.add(h.neighbor_offset);
@@ -330,6 +331,7 @@ CoreParams::CoreParams(Input const& inp)
     device_.msc.material = reinterpret_cast<UrbanMscMaterialRecord const*>(base + o_mscm);
     device_.msc.par_mat = reinterpret_cast<UrbanMscParMatRecord const*>(base + o_mscp);
     device_.looping = reinterpret_cast<LoopingRecord const*>(base + o_loop);
+    device_.rng_jump = reinterpret_cast<std::uint32_t const*>(base + o_jump);
     device_.geo.surfaces = reinterpret_cast<SurfaceRecord const*>(base + o_pl);
     device_.geo.volumes = reinterpret_cast<VolumeRecord const*>(base + o_box);
     device_.geo.neighbor_offset = reinterpret_cast<size_type const*>(base + o_no);
@@ -637,6 +639,15 @@ long long CoreState::tuning(std::string const& name) const
     if (name == "sort")
         return ctx_.sort_enabled;
     throw std::runtime_error("unknown tuning parameter '" + name + "'");
+}
+
+void CoreState::reseed(unsigned long long event_id)
+{
+    launch_reseed(ctx_, seed_, event_id, stream_);
+    GBX_CUDA(cudaGetLastError());
+    // TrackInitParams::reset_track_ids: every per-event counter restarts
+    GBX_CUDA(cudaMemsetAsync(
+        ref_.track_counters, 0, sizeof(size_type) * ref_.max_events, stream_));
 }
 
 std::vector<size_type> CoreState::event_live(size_type n) const
@@ -998,6 +1009,12 @@ std::vector<StepperResult> Stepper::run_until_empty(size_type max_steps,
         taken += n;
     }
     return results;
+}
+
+void Stepper::reseed(unsigned long long event_id)
+{
+    state_->reseed(event_id);
+    GBX_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void Stepper::kill_active()

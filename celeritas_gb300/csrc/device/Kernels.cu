@@ -806,6 +806,31 @@ void launch_count_event_live(LaunchContext const& ctx,
     count_event_live_kernel<<<4 * 152, block_size, 0, stream>>>(ctx.state, num_events);
 }
 
+__global__ __launch_bounds__(block_size) void reseed_kernel(ParamsData p,
+                                                            StateData s,
+                                                            unsigned int seed,
+                                                            unsigned long long event_id)
+{
+    size_type const slot = thread_slot();
+    if (slot < s.size)
+    {
+        reseed_xorwow_slot(s.rng,
+                           p.rng_jump + 32 * 5,
+                           seed,
+                           event_id * s.size + slot,
+                           slot);
+    }
+}
+
+void launch_reseed(LaunchContext const& ctx,
+                   unsigned int seed,
+                   unsigned long long event_id,
+                   cudaStream_t stream)
+{
+    reseed_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+        ctx.params, ctx.state, seed, event_id);
+}
+
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream)
 {
     kill_active_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(

@@ -91,6 +91,12 @@ void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream);
 void launch_extend_from_secondaries(LaunchContext const& ctx,
                                     cudaStream_t stream);
 void launch_kill_active(LaunchContext const& ctx, cudaStream_t stream);
+//! Reseed every slot's XORWOW state for an event: slot i gets the state of
+//! 'seed' advanced event * size + i subsequences (reseed_rng)
+void launch_reseed(LaunchContext const& ctx,
+                   unsigned int seed,
+                   unsigned long long event_id,
+                   cudaStream_t stream);
 //! Resident blocks of the persistent charged along-step kernel on the
 //! current device (SMs x blocks per SM at full occupancy), 0 on failure
 int persistent_along_blocks(int threads_per_block);

@@ -350,6 +350,9 @@ struct ParamsData
     bool has_field;
     double field[3];  //!< Uniform field [native units: gauss]
     LoopingRecord const* looping;  //!< [particle]
+    //! XORWOW jump polynomials [2][32][5]: 4^i steps, then 4^i subsequences
+    //! of 2^67 steps (XorwowRngParamsData, XorwowRngData.hh:46-47)
+    std::uint32_t const* rng_jump;
 
     // Action IDs (the reference's registration order)
     size_type action_pre_step;

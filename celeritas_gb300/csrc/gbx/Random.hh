@@ -62,6 +62,83 @@ GBX_FORCEINLINE void seed_xorwow(RngStateRef const& ref, size_type slot, std::ui
     }
 }
 
+//! XORWOW's F2-linear state transition (the xor words only; the Weyl word
+//! is advanced separately)
+GBX_FORCEINLINE void xorwow_transition(std::uint32_t* x)
+{
+    std::uint32_t const t = x[0] ^ (x[0] >> 2u);
+    x[0] = x[1];
+    x[1] = x[2];
+    x[2] = x[3];
+    x[3] = x[4];
+    x[4] = (x[4] ^ (x[4] << 4u)) ^ (t ^ (t << 1u));
+}
+
+//! Apply T^d to the xor words given g(z) = z^d mod p(z), p the
+//! characteristic polynomial of the transition T: since p(T) = 0,
+//! T^d = g(T) = sum_m g_m T^m. 'poly' holds the 160 coefficients g_m, bit m
+//! of the 160-bit integer whose 32-bit words are poly[0] (low) .. poly[4].
+GBX_FORCEINLINE void xorwow_apply_poly(std::uint32_t const* poly, std::uint32_t* x)
+{
+    std::uint32_t acc[5] = {0, 0, 0, 0, 0};
+    for (int w = 0; w < 5; ++w)
+    {
+        std::uint32_t const word = poly[w];
+        for (int b = 0; b < 32; ++b)
+        {
+            if ((word >> b) & 1u)
+            {
+                for (int k = 0; k < 5; ++k)
+                    acc[k] ^= x[k];
+            }
+            xorwow_transition(x);
+        }
+    }
+    for (int k = 0; k < 5; ++k)
+        x[k] = acc[k];
+}
+
+//! Advance the xor words by 'count' units, where table[i] is the jump
+//! polynomial of 4^i units (one unit: one step, or one subsequence of 2^67
+//! steps): base-4 digits of the count, smallest jump first
+//! (XorwowRngEngine::jump, src/celeritas/random/XorwowRngEngine.hh:247-265)
+GBX_FORCEINLINE void
+xorwow_jump(std::uint32_t const* table, unsigned long long count, std::uint32_t* x)
+{
+    for (int i = 0; count > 0; ++i, count >>= 2)
+    {
+        for (unsigned int n = static_cast<unsigned int>(count & 3u); n > 0; --n)
+            xorwow_apply_poly(table + 5 * i, x);
+    }
+}
+
+//! Reseed one slot for an event as the reference's reseed_rng does
+//! (src/celeritas/random/RngReseed.cc:27-47): state from SplitMix64 of the
+//! seed (XorwowRngEngine::operator=(Initializer_t), XorwowRngEngine.hh:164-185),
+//! then 'event * num_slots + slot' subsequences ahead; the Weyl word is
+//! unchanged by whole subsequences (its period 2^32 divides 2^67).
+GBX_FORCEINLINE void reseed_xorwow_slot(RngStateRef const& ref,
+                                        std::uint32_t const* subsequence_table,
+                                        unsigned int seed,
+                                        unsigned long long subsequence,
+                                        size_type slot)
+{
+    SplitMix64 sm{seed};
+    std::uint32_t x[5];
+    std::uint64_t v = sm();
+    x[0] = static_cast<std::uint32_t>(v);
+    x[1] = static_cast<std::uint32_t>(v >> 32);
+    v = sm();
+    x[2] = static_cast<std::uint32_t>(v);
+    x[3] = static_cast<std::uint32_t>(v >> 32);
+    v = sm();
+    x[4] = static_cast<std::uint32_t>(v);
+    ref.weyl[slot] = static_cast<std::uint32_t>(v >> 32);
+    xorwow_jump(subsequence_table, subsequence, x);
+    for (int k = 0; k < 5; ++k)
+        ref.s[k][slot] = x[k];
+}
+
 class XorwowEngine
 {
   public:

@@ -175,6 +175,10 @@ class CoreState
     void set_tuning(std::string const& name, long long value);
     long long tuning(std::string const& name) const;
 
+    //! Reseed every slot's random state for an event and restart the
+    //! per-event track IDs (Stepper::reseed)
+    void reseed(unsigned long long event_id);
+
     //! Live tracks (slots and queued initializers) per event [0, n)
     std::vector<size_type> event_live(size_type n) const;
     //! Energy deposited in detectors per event [0, n); optionally cleared
@@ -269,6 +273,9 @@ class Stepper
                                                size_type batch = 16);
     //! Kill all tracks in flight
     void kill_active();
+    //! Reseed the random states of all slots for an event and restart its
+    //! track IDs (Stepper::reseed, src/celeritas/global/Stepper.cc:194-201)
+    void reseed(unsigned long long event_id);
 
     CoreState& state() { return *state_; }
     CoreParams const& params() const { return *params_; }

@@ -15,11 +15,13 @@
 #include "HostParams.hh"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <map>
 #include <stdexcept>
 
 #include "KvFile.hh"
+#include "../gbx/Random.hh"
 
 namespace gbx
 {
@@ -1005,6 +1007,149 @@ void Builder::build_element_tables()
     hp_.scalars.element_tables = this->add_ints(index);
 }
 
+//---------------------------------------------------------------------------//
+// XORWOW jump polynomials
+//---------------------------------------------------------------------------//
+// Polynomials over GF(2) of degree below 192, bit m of the three 64-bit
+// words holding the coefficient of z^m. The method (jump ahead by
+// g(z) = z^d mod p(z), p the characteristic polynomial of the transition) is
+// Haramoto et al. 2008, "Efficient jump ahead for F2-linear random number
+// generators", which the reference cites (XorwowRngEngine.hh:38-52); the
+// polynomials are computed here from the transition itself.
+using GF2Poly = std::array<std::uint64_t, 3>;
+
+bool gf2_bit(GF2Poly const& a, int m)
+{
+    return (a[m >> 6] >> (m & 63)) & 1u;
+}
+
+//! Characteristic polynomial of XORWOW's transition by Berlekamp-Massey over
+//! 400 output bits (bit 0 of the last xor word after each transition). The
+//! transition has period 2^160 - 1, so its characteristic polynomial is
+//! primitive and is the minimal polynomial of this sequence.
+GF2Poly xorwow_charpoly()
+{
+    std::uint32_t x[5] = {0x12345678u, 0x9abcdef0u, 0x0fedcba9u, 0x87654321u, 0x13579bdfu};
+    constexpr int n = 400;
+    std::vector<int> u(n);
+    for (int i = 0; i < n; ++i)
+    {
+        xorwow_transition(x);
+        u[i] = static_cast<int>(x[4] & 1u);
+    }
+    // Connection polynomial c: u[i] = sum_{j=1..len} c[j] u[i-j]
+    std::vector<int> c(n + 1, 0), b(n + 1, 0);
+    c[0] = b[0] = 1;
+    int len = 0, shift = 1;
+    for (int i = 0; i < n; ++i)
+    {
+        int d = u[i];
+        for (int j = 1; j <= len; ++j)
+            d ^= c[j] & u[i - j];
+        if (!d)
+        {
+            ++shift;
+            continue;
+        }
+        std::vector<int> const prev = c;
+        for (int j = 0; j + shift <= n; ++j)
+            c[j + shift] ^= b[j];
+        if (2 * len <= i)
+        {
+            len = i + 1 - len;
+            b = prev;
+            shift = 1;
+        }
+        else
+        {
+            ++shift;
+        }
+    }
+    if (len != 160)
+        throw std::runtime_error("XORWOW characteristic polynomial has the wrong degree");
+    // p(z) = z^160 + c1 z^159 + ... + c160: the reciprocal of c
+    GF2Poly p{0, 0, 0};
+    for (int j = 0; j <= len; ++j)
+    {
+        if (c[j])
+            p[(len - j) >> 6] |= std::uint64_t(1) << ((len - j) & 63);
+    }
+    return p;
+}
+
+//! a z mod p, for deg a < 160
+GF2Poly gf2_mul_z(GF2Poly a, GF2Poly const& p)
+{
+    a[2] = (a[2] << 1) | (a[1] >> 63);
+    a[1] = (a[1] << 1) | (a[0] >> 63);
+    a[0] <<= 1;
+    if (gf2_bit(a, 160))
+    {
+        for (int k = 0; k < 3; ++k)
+            a[k] ^= p[k];
+    }
+    return a;
+}
+
+//! a b mod p, by Horner's rule over the coefficients of b
+GF2Poly gf2_mul_mod(GF2Poly const& a, GF2Poly const& b, GF2Poly const& p)
+{
+    GF2Poly r{0, 0, 0};
+    for (int m = 159; m >= 0; --m)
+    {
+        r = gf2_mul_z(r, p);
+        if (gf2_bit(b, m))
+        {
+            for (int k = 0; k < 3; ++k)
+                r[k] ^= a[k];
+        }
+    }
+    return r;
+}
+
+//! The five 32-bit words of a polynomial of degree below 160, low first
+void store_jump_poly(GF2Poly const& g, std::uint32_t* out)
+{
+    for (int w = 0; w < 5; ++w)
+        out[w] = static_cast<std::uint32_t>(g[w >> 1] >> (32 * (w & 1)));
+}
+
+//! Jump polynomials z^(4^i) and z^(4^i 2^67) mod p(z), i < 32, with the
+//! first six checked against 4^i direct transitions
+std::vector<std::uint32_t> make_xorwow_jump_polys()
+{
+    GF2Poly const p = xorwow_charpoly();
+    std::vector<std::uint32_t> table(2 * 32 * 5);
+    auto fill = [&](GF2Poly g, std::uint32_t* out) {
+        for (int i = 0; i < 32; ++i)
+        {
+            store_jump_poly(g, out + 5 * i);
+            g = gf2_mul_mod(g, g, p);
+            g = gf2_mul_mod(g, g, p);
+        }
+    };
+    GF2Poly const z{2, 0, 0};
+    fill(z, table.data());
+    GF2Poly sub = z;
+    for (int k = 0; k < 67; ++k)
+        sub = gf2_mul_mod(sub, sub, p);
+    fill(sub, table.data() + 32 * 5);
+    for (int i = 0; i < 6; ++i)
+    {
+        std::uint32_t a[5] = {1u, 2u, 3u, 4u, 5u};
+        std::uint32_t b[5] = {1u, 2u, 3u, 4u, 5u};
+        xorwow_apply_poly(table.data() + 5 * i, a);
+        for (long n = 0; n < (1L << (2 * i)); ++n)
+            xorwow_transition(b);
+        for (int k = 0; k < 5; ++k)
+        {
+            if (a[k] != b[k])
+                throw std::runtime_error("XORWOW jump polynomial check failed");
+        }
+    }
+    return table;
+}
+
 HostParams Builder::build()
 {
     if (kv_.s("format") != "gbx-physics-1")
@@ -1017,6 +1162,7 @@ HostParams Builder::build()
     this->build_element_tables();
     this->build_msc_field();
     this->build_geometry();
+    hp_.rng_jump = make_xorwow_jump_polys();
     hp_.scalars.rng_per_track = opts_.rng_per_track;
     hp_.scalars.event_tallies = opts_.event_tallies;
     for (auto const& b : geo_.boxes)
@@ -1135,6 +1281,7 @@ ParamsData make_host_view(HostParams const& hp)
     p.msc.material = hp.msc_materials.data();
     p.msc.par_mat = hp.msc_par_mat.data();
     p.looping = hp.looping.data();
+    p.rng_jump = hp.rng_jump.data();
     p.geo.surfaces = hp.surfaces.data();
     p.geo.volumes = hp.volumes.data();
     p.geo.neighbor_offset = hp.neighbor_offset.data();

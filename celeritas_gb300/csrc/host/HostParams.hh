@@ -93,6 +93,7 @@ struct HostParams
     std::vector<UrbanMscMaterialRecord> msc_materials;
     std::vector<UrbanMscParMatRecord> msc_par_mat;
     std::vector<LoopingRecord> looping;
+    std::vector<std::uint32_t> rng_jump;  //!< [2][32][5] jump polynomials
     // Geometry
     std::vector<SurfaceRecord> surfaces;
     std::vector<VolumeRecord> volumes;

@@ -154,6 +154,14 @@ int gbx_stepper_insert_primaries(gbx_stepper* stepper,
 /* Kill all active tracks (Stepper::kill_active) */
 int gbx_stepper_kill_active(gbx_stepper* stepper);
 
+/* Reseed the random state of every track slot for an event and restart the
+ * per-event track IDs (Stepper::reseed(UniqueEventId),
+ * src/celeritas/global/Stepper.hh:111,175 and Stepper.cc:194-201): slot i
+ * gets the XORWOW state of the stepper's seed advanced
+ * event_id * num_track_slots + i subsequences of 2^67 draws
+ * (src/celeritas/random/RngReseed.cc:27-47). */
+int gbx_stepper_reseed(gbx_stepper* stepper, unsigned long long event_id);
+
 /* Wait for all work on the stepper's stream */
 int gbx_stepper_synchronize(gbx_stepper* stepper);
 

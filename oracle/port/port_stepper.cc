@@ -19,6 +19,7 @@
 //   port_stepper run <physics.txt> calo <primaries.txt> <slots> <seed>
 //                    [--steps N] [--quiet] [--threads T --events E]
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -62,7 +63,29 @@ class PortStepper
                  hp.scalars.num_detectors,
                  seed)
         , action_labels_(hp.action_labels)
+        , seed_(seed)
     {
+    }
+
+    //! Stepper::reseed: every slot's XORWOW state from the seed, advanced
+    //! event * size + slot subsequences; per-event track IDs restart
+    void reseed(unsigned long long event_id)
+    {
+        StateData s = state_.view();
+        for (size_type i = 0; i < s.size; ++i)
+        {
+            reseed_xorwow_slot(
+                s.rng, params_.rng_jump + 32 * 5, seed_, event_id * s.size + i, i);
+        }
+        std::fill(state_.track_counters.begin(), state_.track_counters.end(), 0);
+    }
+
+    //! XORWOW words of slot i: five xor words, then the Weyl word
+    std::array<std::uint32_t, 6> rng_words(size_type i)
+    {
+        StateData s = state_.view();
+        return {s.rng.s[0][i], s.rng.s[1][i], s.rng.s[2][i],
+                s.rng.s[3][i], s.rng.s[4][i], s.rng.weyl[i]};
     }
 
     StepCounts operator()(std::vector<TrackInitializer> const& primaries)
@@ -109,6 +132,7 @@ class PortStepper
     ParamsData params_;
     HostState state_;
     std::vector<std::string> action_labels_;
+    unsigned int seed_;
 
     StepCounts step(bool with_primaries)
     {
@@ -276,6 +300,8 @@ int run(int argc, char** argv)
     size_type max_steps = static_cast<size_type>(-1);
     bool quiet = false;
     bool trace = false;
+    long long reseed = -1;
+    size_type dump_rng = 0;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -285,6 +311,10 @@ int run(int argc, char** argv)
             max_steps = std::stoul(argv[++i]);
         else if (a == "--quiet")
             quiet = true;
+        else if (a == "--reseed")
+            reseed = std::stoll(argv[++i]);
+        else if (a == "--dump-rng")
+            dump_rng = std::stoul(argv[++i]);
     }
     HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
@@ -299,6 +329,13 @@ int run(int argc, char** argv)
     }
     auto t0 = std::chrono::steady_clock::now();
     PortStepper step(hp, slots, seed, max_event + 1);
+    if (reseed >= 0)
+        step.reseed(static_cast<unsigned long long>(reseed));
+    for (size_type i = 0; i < std::min(dump_rng, slots); ++i)
+    {
+        auto w = step.rng_words(i);
+        std::printf("rng %u %u %u %u %u %u %u\n", i, w[0], w[1], w[2], w[3], w[4], w[5]);
+    }
     StepCounts counts = step(primaries);
     size_type iter = 0;
     if (trace)

@@ -722,7 +722,7 @@ int run(int argc, char** argv)
     {
         std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
                      "<seed> [--field Bx By Bz] [--msc] [--steps N] "
-                     "[--track-order N]\n";
+                     "[--track-order N] [--reseed EVENT] [--dump-rng N]\n";
         return 2;
     }
     std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
@@ -733,6 +733,8 @@ int run(int argc, char** argv)
     size_type max_steps = static_cast<size_type>(-1);
     TrackOrder track_order = TrackOrder::none;
     bool trace = false;
+    long long reseed = -1;
+    size_type dump_rng = 0;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -751,6 +753,10 @@ int run(int argc, char** argv)
             track_order = static_cast<TrackOrder>(std::stoi(argv[++i]));
         else if (a == "--trace")
             trace = true;
+        else if (a == "--reseed")
+            reseed = std::stoull(argv[++i]);
+        else if (a == "--dump-rng")
+            dump_rng = std::stoul(argv[++i]);
     }
 
     KvFile kv(phys_path);
@@ -764,6 +770,23 @@ int run(int argc, char** argv)
     sinp.stream_id = StreamId{0};
     sinp.num_track_slots = num_slots;
     Stepper<MemSpace::host> step(std::move(sinp));
+    if (reseed >= 0)
+    {
+        // Stepper::reseed before the event, as accel::LocalTransporter does
+        step.reseed(UniqueEventId(static_cast<UniqueEventId::size_type>(reseed)));
+    }
+    for (size_type i = 0; i < std::min<size_type>(dump_rng, num_slots); ++i)
+    {
+        auto const& r = step.state_ref().rng.state[TrackSlotId{i}];
+        std::printf("rng %u %u %u %u %u %u %u\n",
+                    i,
+                    r.xorstate[0],
+                    r.xorstate[1],
+                    r.xorstate[2],
+                    r.xorstate[3],
+                    r.xorstate[4],
+                    r.weylstate);
+    }
 
     // Print action list (ordered) for the action-ID contract
     {

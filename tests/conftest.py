@@ -28,7 +28,8 @@ GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
                 "calo_msc_e1000_n4", "calo_field_e1000_n4", "calo_msc_field_e5000_n2",
                 "calo_msc_field_ep2000_n2", "calo_sorted_both_e1000_n4",
                 "calo_sorted_post_g100_n16", "calo_msc_field_sorted_along_e2000_n2",
-                "cms_mix_e10000_n4", "cms_mix_logu_n6", "cms_sorted_both_mix_e5000_n4"]
+                "cms_mix_e10000_n4", "cms_mix_logu_n6", "cms_sorted_both_mix_e5000_n4",
+                "calo_reseed7_msc_e1000_n4"]
 
 
 def case_primaries(case: dict):
@@ -53,6 +54,8 @@ def case_options(case: dict) -> list[str]:
         opts += ["--field"] + [repr(float(f)) for f in field]
     if case.get("track_order"):
         opts += ["--track-order", str(int(case["track_order"]))]
+    if case.get("reseed") is not None:
+        opts += ["--reseed", str(int(case["reseed"]))]
     return opts
 
 

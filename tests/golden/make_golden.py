@@ -63,7 +63,16 @@ CASES = {
                                          energy=5000.0, num=4, slots=16384, seed=9,
                                          beam_seed=3, msc=True, field=[0.0, 0.0, 3.8],
                                          track_order=7),
+    # Stepper::reseed(event 7) before the first step
+    "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
+                                      msc=True, reseed=7),
 }
+
+# Reseeded XORWOW states: seed, track slots, events, and the slots recorded
+RNG_SEED = 5
+RNG_SLOTS = 4096
+RNG_EVENTS = [0, 1, 7, 123456789, (1 << 40) + 3]
+RNG_RECORDED = list(range(32)) + [RNG_SLOTS - 1]
 
 
 def case_primaries(c: dict):
@@ -86,6 +95,8 @@ def case_options(c: dict) -> list[str]:
         opts += ["--field"] + [repr(float(f)) for f in field]
     if c.get("track_order"):
         opts += ["--track-order", str(int(c["track_order"]))]
+    if c.get("reseed") is not None:
+        opts += ["--reseed", str(int(c["reseed"]))]
     return opts
 
 
@@ -97,6 +108,8 @@ def make_case(name: str) -> dict:
             "seed": c["seed"], "msc": bool(c.get("msc", False)),
             "field": list(c.get("field", [0.0, 0.0, 0.0])),
             "track_order": int(c.get("track_order", 0))}
+    if c.get("reseed") is not None:
+        case["reseed"] = int(c["reseed"])
     if c.get("beam", "pencil") == "eta":
         case.update(beam="eta", pdgs=list(c["pdgs"]), emax=c.get("emax"),
                     beam_seed=c["beam_seed"])
@@ -116,6 +129,28 @@ def make_case(name: str) -> dict:
         "iterations": out["iterations"],
         "edep": out["edep"],
     }
+
+
+def rng_reseed_dump() -> dict:
+    """XORWOW states of the recorded slots after Stepper::reseed, per event."""
+    prim = pencil_beam(1, energy=10.0)
+    out = {"seed": RNG_SEED, "num_track_slots": RNG_SLOTS, "slots": RNG_RECORDED,
+           "events": {}}
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "primaries.txt")
+        write_primaries_text(ptxt, prim)
+        for ev in RNG_EVENTS:
+            res = subprocess.run([oracle.REF_BIN, "run", physics_file("calo"), "calo", ptxt,
+                                  str(RNG_SLOTS), str(RNG_SEED), "--reseed", str(ev),
+                                  "--dump-rng", str(RNG_SLOTS), "--steps", "1"],
+                                 capture_output=True, text=True, check=True)
+            words = {}
+            for line in res.stdout.splitlines():
+                tok = line.split()
+                if tok and tok[0] == "rng":
+                    words[int(tok[1])] = [int(t) for t in tok[2:8]]
+            out["events"][str(ev)] = [words[i] for i in RNG_RECORDED]
+    return out
 
 
 def geometry_dump() -> dict:
@@ -146,6 +181,8 @@ def main():
         print(name, data["iterations"], data["total_steps"])
     with open(os.path.join(HERE, "calo_geometry.json"), "w") as f:
         json.dump(geometry_dump(), f, indent=0)
+    with open(os.path.join(HERE, "xorwow_reseed.json"), "w") as f:
+        json.dump(rng_reseed_dump(), f, indent=0)
 
 
 if __name__ == "__main__":

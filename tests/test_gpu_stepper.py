@@ -52,6 +52,8 @@ def params_for(gb, case):
 def transport(gb, params, case, use_graph=True, batch=32):
     prim = case_primaries(case)
     st = gb.Stepper(params, case["num_track_slots"], seed=case["seed"], use_graph=use_graph)
+    if case.get("reseed") is not None:
+        st.reseed(case["reseed"])
     res = [st.step(prim)] + st.run(max_steps=100000, batch=batch)
     return st, res
 
@@ -153,3 +155,39 @@ def test_state_roundtrip(gb, calo_params):
     assert (st.get_state("energy", np.float64) == 3.0).all()
     with pytest.raises(gb.GbxError, match="unknown state field"):
         st.get_state("nope", np.uint8)
+
+
+def test_reseed_states_match_reference(gb, calo_params):
+    """gbx_stepper_reseed gives every slot the reference's reseeded XORWOW
+    state (tests/golden/xorwow_reseed.json, from Stepper<host>::reseed)."""
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "xorwow_reseed.json")) as f:
+        golden = json.load(f)
+    n = golden["num_track_slots"]
+    st = gb.Stepper(calo_params, n, seed=golden["seed"], use_graph=False)
+    for ev, expected in golden["events"].items():
+        st.reseed(int(ev))
+        words = st.get_state("rng", np.uint32).reshape(6, n)
+        got = [[int(words[w, i]) for w in range(6)] for i in golden["slots"]]
+        assert got == expected, ev
+
+
+def test_reseed_restarts_event(gb, calo_params):
+    """Reseeding for the same event reproduces a transport exactly; another
+    event gives another history."""
+    from celeritas_gb300.primaries import pencil_beam
+
+    prim = pencil_beam(4, energy=1000.0)
+    st = gb.Stepper(calo_params, 4096, seed=3)
+    results = []
+    for ev in (5, 5, 6):
+        st.reseed(ev)
+        st.clear_energy_deposition()
+        res = [st.step(prim)] + st.run(max_steps=100000)
+        results.append(([[r.generated, r.queued, r.active, r.alive] for r in res],
+                        st.energy_deposition()))
+    assert results[0][0] == results[1][0]
+    np.testing.assert_allclose(results[0][1], results[1][1], rtol=1e-12)
+    assert results[0][0] != results[2][0]
