@@ -205,7 +205,7 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     import torch
 
     import celeritas_gb300 as gb
-    from celeritas_gb300 import roofline
+    from celeritas_gb300 import roofline, sharding
 
     track_order = args.track_order if track_order is None else track_order
     gb.load_library(precision=precision)
@@ -215,7 +215,7 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     labels = params.action_labels()
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     stream = stream_cls(stepper.stream_handle())
-    prim = make_primaries(wl, rank, num=wl.get("bench_primaries"))
+    prim = sharding.rank_primaries(wl, rank, num=wl.get("bench_primaries"))
     events_per_step = len(np.unique(prim["event"]))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
@@ -294,13 +294,9 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     total_ms = float(np.sum(dev_ms))
     total_e2e = float(np.sum(e2e_s))
     total_steps = float(np.sum(track_steps))
-    if dist:
-        t = torch.tensor([total_ms, total_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, total_e2e = t.tolist()
-        st = torch.tensor([total_steps], device="cuda", dtype=torch.float64)
-        dist.all_reduce(st, op=dist.ReduceOp.SUM)
-        total_steps = st.item()
+    # Slowest rank's times, all ranks' track-steps (no-op for one process)
+    red = sharding.reduce_run(dist, "cuda", total_ms, total_e2e, total_steps)
+    total_ms, total_e2e, total_steps = red["time_ms"], red["e2e_s"], red["track_steps"]
     out = {
         "precision": precision,
         "value": total_steps / (total_ms / 1e3),
