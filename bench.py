@@ -199,9 +199,10 @@ DTYPES = {"mixed": "f32 physics + f64 positions/geometry/field/tally", "double":
 
 
 def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
-            track_order=None):
+            track_order=None, tuning=None):
     """Time one precision's stepping loop: device and end-to-end throughput,
-    per-transport tallies, and per-action times for the roofline."""
+    per-transport tallies, and per-action times for the roofline. 'tuning'
+    is a launch configuration (gbx_stepper_set_tuning settings)."""
     import torch
 
     import celeritas_gb300 as gb
@@ -211,9 +212,12 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     gb.load_library(precision=precision)
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"],
-                       track_order=track_order, precision=precision)
+                       track_order=track_order, precision=precision,
+                       reentrant_looping=wl.get("reentrant_looping", False))
     labels = params.action_labels()
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
+    if tuning:
+        stepper.set_tuning(**tuning)
     stream = stream_cls(stepper.stream_handle())
     prim = sharding.rank_primaries(wl, rank, num=wl.get("bench_primaries"))
     events_per_step = len(np.unique(prim["event"]))
@@ -320,7 +324,7 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     return out
 
 
-def measure_served(args, wl, rank):
+def measure_served(args, wl, rank, tuning=None):
     """Batched and served form: the workload's events streamed through the
     continuous-batching server (mixed precision, action-sorted, per-track
     streams), all arriving at once and admitted as queue space frees up, so
@@ -331,8 +335,11 @@ def measure_served(args, wl, rank):
     gb.load_library(precision="mixed")
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
-                       precision="mixed", rng_per_track=True, event_tallies=True)
+                       precision="mixed", rng_per_track=True, event_tallies=True,
+                       reentrant_looping=wl.get("reentrant_looping", False))
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
+    if tuning:
+        stepper.set_tuning(**tuning)
     per_event = wl["num_primaries"] // wl["events"]
     server = serving.EventServer({wl["geometry"]: stepper},
                                  {wl["geometry"]: 16 * wl["slots"]}, 1 << 16)
@@ -351,6 +358,32 @@ def measure_served(args, wl, rank):
     summary = server.serve(reqs)
     summary["primaries_per_event"] = per_event
     return summary
+
+
+def tune_workload(wl, precision, rank):
+    """Launch configuration for a workload from the autotuner: charged
+    along-step block size, persistent kernel and sort threshold, tuned on the
+    transport time of the workload's calibration events (its slot count is
+    fixed by the workload)."""
+    import celeritas_gb300 as gb
+    from celeritas_gb300 import autotune
+
+    gb.load_library(precision=precision)
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                       field_tesla=wl["field"], msc=wl["msc"], track_order=7,
+                       precision=precision, rng_per_track=True,
+                       reentrant_looping=wl.get("reentrant_looping", False))
+    # Calibration events drawn with another beam seed than the timed ones
+    prim = make_primaries(wl, rank, num=wl["tune_primaries"], seed_offset=77)
+    t0 = time.perf_counter()
+    best, trials = autotune.autotune(
+        lambda slots: gb.Stepper(params, slots, seed=wl["seed"] + rank), prim,
+        slot_counts=(wl["slots"],))
+    best.pop("slots", None)
+    report = {"settings": best, "calibration_primaries": int(len(prim)),
+              "trials": len(trials), "seconds": round(time.perf_counter() - t0, 1)}
+    del params
+    return best, report
 
 
 def compare_tallies(mixed, fp64):
@@ -398,10 +431,14 @@ def run_gb300(args, wl):
     precisions = [args.precision] + (["double"] if args.precision != "double"
                                      and not args.no_fp64 else [])
     results = {}
+    tuning, tuning_report = None, None
+    if wl.get("tune_primaries") and not args.no_tune:
+        tuning, tuning_report = tune_workload(wl, precisions[0], rank)
     with ClockSampler(local_rank) as clocks:
         for prec in precisions:
             results[prec] = measure(args, wl, prec, torch.cuda.ExternalStream, dist,
-                                    rank, local_rank, clocks)
+                                    rank, local_rank, clocks,
+                                    tuning=tuning if prec == precisions[0] else None)
         if args.plain:
             # The plain FP64 path: no action sort
             results["plain"] = measure(args, wl, "double", torch.cuda.ExternalStream,
@@ -437,7 +474,9 @@ def run_gb300(args, wl):
                    "track_steps_per_step": head["track_steps_per_step"],
                    "iterations_per_step": head["iterations_per_step"],
                    "l2": "flushed (256 MiB write) between timed steps",
-                   "parallelism": f"events sharded over {world} GPU(s)"},
+                   "parallelism": f"events sharded over {world} GPU(s)",
+                   "reentrant_looping": bool(wl.get("reentrant_looping", False)),
+                   "tuning": tuning_report},
         "e2e": {"value": head["e2e"], "unit": "track-steps/s",
                 "h2d_bytes_per_step": head["h2d"], "d2h_bytes_per_step": head["d2h"]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
@@ -465,7 +504,7 @@ def run_gb300(args, wl):
                               "ms_per_step": pl["ms_per_step"], "track_order": 0}
         line["events_per_s_vs_fp64_plain"] = head["events_per_s"] / pl["events_per_s"]
         if args.served_events:
-            served = measure_served(args, wl, rank)
+            served = measure_served(args, wl, rank, tuning=tuning)
             line["served"] = served
             line["served_events_per_s_vs_fp64_plain"] = (served["events_per_s"]
                                                          / pl["events_per_s"])
@@ -511,7 +550,8 @@ def run_serving(args, wl):
         for geo, field in fields.items():
             params = gb.Params(gb.physics_file(geo), geo, field_tesla=field, msc=True,
                                track_order=track_order, precision=precision,
-                               rng_per_track=per_track, event_tallies=per_track)
+                               rng_per_track=per_track, event_tallies=per_track,
+                               reentrant_looping=wl.get("reentrant_looping", False))
             out[geo] = gb.Stepper(params, slots, seed=wl["seed"] + rank)
         return out
 
@@ -629,7 +669,8 @@ def run_batching(args, wl):
     gb.load_library(precision="mixed")
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
-                       precision="mixed", rng_per_track=True)
+                       precision="mixed", rng_per_track=True,
+                       reentrant_looping=wl.get("reentrant_looping", False))
 
     def make_stepper(slots):
         return gb.Stepper(params, slots, seed=wl["seed"] + rank)
@@ -744,6 +785,8 @@ def main():
                         help="events streamed through the server (c3: 195)")
     parser.add_argument("--sequential-sample", type=int, default=40,
                         help="c5: requests timed alone on the plain FP64 path")
+    parser.add_argument("--no-tune", action="store_true",
+                        help="skip the autotuner where the workload uses it (c3)")
     parser.add_argument("--plain", action="store_true",
                         help="also time the plain FP64 path (no action sort); on for c3")
     args = parser.parse_args()

@@ -44,7 +44,7 @@ class _Primary(ctypes.Structure):
 class _ParamsOptions(ctypes.Structure):
     _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int),
                 ("track_order", ctypes.c_uint), ("rng_per_track", ctypes.c_int),
-                ("event_tallies", ctypes.c_int)]
+                ("event_tallies", ctypes.c_int), ("reentrant_looping", ctypes.c_int)]
 
 
 class _StepResult(ctypes.Structure):
@@ -175,7 +175,8 @@ class Params:
     def __init__(self, physics: str, geometry: str = "calo",
                  field_tesla=(0.0, 0.0, 0.0), msc: bool = False,
                  track_order: int | str = "none", precision: str = "double",
-                 rng_per_track: bool = False, event_tallies: bool = False):
+                 rng_per_track: bool = False, event_tallies: bool = False,
+                 reentrant_looping: bool = False):
         lib = load_library(precision=precision)
         self._lib = lib
         self.precision = precision
@@ -189,6 +190,7 @@ class Params:
         opts.track_order = int(track_order)
         opts.rng_per_track = int(rng_per_track)
         opts.event_tallies = int(event_tallies)
+        opts.reentrant_looping = int(reentrant_looping)
         _check(lib, lib.gbx_params_create(physics.encode(), geometry.encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle

@@ -197,6 +197,7 @@ int gbx_params_create(const char* physics_file,
             inp.options.track_order = options->track_order;
             inp.options.rng_per_track = options->rng_per_track != 0;
             inp.options.event_tallies = options->event_tallies != 0;
+            inp.options.reentrant_looping = options->reentrant_looping != 0;
             for (int i = 0; i < 3; ++i)
                 inp.options.field_tesla[i] = options->field_tesla[i];
         }

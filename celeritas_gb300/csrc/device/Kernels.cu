@@ -176,20 +176,54 @@ __global__ __launch_bounds__(block_size) void discrete_select_kernel(
     }
 }
 
+//! Add each lane's value to bins[key] with one atomic per distinct key of
+//! the warp: lanes with equal keys are grouped (__match_any_sync), each
+//! group's values are summed in lane order, and the group's lowest lane adds
+//! the sum. Lanes with an invalid key take part in the exchange only. Every
+//! lane of the warp must call this.
+__device__ __forceinline__ void warp_tally(double* bins, size_type key, double value)
+{
+    unsigned int const active = __activemask();
+    if (__ballot_sync(active, key != invalid_id) == 0)
+        return;
+    unsigned int const lane = threadIdx.x & 31u;
+    unsigned int const group = __match_any_sync(active, key);
+    double sum = 0;
+    for (unsigned int k = 0; k < 32; ++k)
+    {
+        if (!((active >> k) & 1u))
+            continue;
+        double const v = __shfl_sync(active, value, k);
+        if ((group >> k) & 1u)
+            sum += v;
+    }
+    if (key != invalid_id && lane == static_cast<unsigned int>(__ffs(group) - 1))
+        atomicAdd(bins + key, sum);
+}
+
+//! SimpleCalo tally (SimpleCaloExecutor, src/celeritas/user/detail/
+//! SimpleCaloExecutor.hh:48-67): the step's deposition of every track in a
+//! detector volume. A zero deposit leaves the sums unchanged and is skipped,
+//! as the reference's step filter does; the rest is aggregated per warp.
 __global__ __launch_bounds__(block_size) void calo_kernel(ParamsData p, StateData s)
 {
-    size_type slot = thread_slot();
+    size_type const slot = thread_slot();
+    size_type det = invalid_id;
+    size_type event = invalid_id;
+    double edep = 0;
     if (slot < s.size && s.status[slot] != status_inactive)
     {
-        size_type det = s.detector[slot];
-        if (det != invalid_id)
+        edep = s.energy_deposition[slot];
+        if (edep != 0)
         {
-            double const edep = s.energy_deposition[slot];
-            atomicAdd(s.calo_edep + det, edep);
-            if (p.event_tallies)
-                atomicAdd(s.event_edep + s.event_id[slot], edep);
+            det = s.detector[slot];
+            if (p.event_tallies && det != invalid_id)
+                event = s.event_id[slot];
         }
     }
+    warp_tally(s.calo_edep, det, edep);
+    if (p.event_tallies)
+        warp_tally(s.event_edep, event, edep);
 }
 
 //! Live tracks per event: occupied slots plus queued initializers

@@ -298,10 +298,14 @@ GBX_FUNCTION void field_result(ParamsData const& p,
     size_type const pid = s.particle_id[slot];
     real_type const energy = s.energy[slot];
     double const step_length = s.step_length[slot];
-    // update_looping
+    // update_looping. With reentrant_looping, a step that ends on a boundary
+    // the track re-enters at once (its direction at the boundary points back
+    // into the volume it came from) is no progress and keeps the count.
+    bool const reentry = p.reentrant_looping && prop.boundary
+                         && s.boundary[slot] == boundary_reentrant;
     if (prop.looping)
         ++s.num_looping_steps[slot];
-    else
+    else if (!reentry)
         s.num_looping_steps[slot] = 0;
     if (prop.looping)
     {

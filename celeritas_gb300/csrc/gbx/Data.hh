@@ -251,6 +251,9 @@ enum SurfaceType : int
 struct SurfaceRecord
 {
     int type;
+    //! sqrt(value) rounded to FP32 for a z cylinder (0 for a plane): only
+    //! for conservative reachability bounds, never for a distance
+    float radius;
     double value;
 };
 
@@ -379,6 +382,9 @@ struct ParamsData
     // does not depend on the other events in flight; per-event tallies
     bool rng_per_track;
     bool event_tallies;
+    // A field step ending in a reentrant boundary crossing keeps the
+    // looping-step count (off: the reference's reset on any non-looping step)
+    bool reentrant_looping;
     // Track sorting: policy, sort actions (invalid if absent), action count
     unsigned int track_order;
     size_type action_sort_along;

@@ -10,8 +10,10 @@
 // FP64 build: the whole integration is FP64, operation for operation as in
 // the reference. Mixed-precision build: the Runge-Kutta stages (field
 // evaluations and stage momenta) are FP32; the positions are accumulated in
-// FP64 from FP32 increments, and the error estimate, the acceptance test and
-// the chord test are FP64. Only the step-size scale factor err^(-1/5) is FP32.
+// FP64 from FP32 increments; the embedded error vector and the chord
+// distance are formed in FP32 from the FP32 stages, and the error norms, the
+// acceptance test, the step and the path length are FP64. The step-size
+// scale factor err^(-1/5) is FP32.
 #pragma once
 
 #include "Geometry.hh"
@@ -84,9 +86,14 @@ struct UniformFieldEquation
 
 struct FieldStepperResult
 {
-    OdeState mid_state;
+    OdeState mid_state;  //!< FP64 build only
     OdeState end_state;
-    OdeState err_state;
+    OdeState err_state;  //!< FP64 build only
+    // Mixed-precision build only: the embedded error estimate and the chord
+    // distance, formed in FP32 from the FP32 stages
+    Vec3<float> err_pos_rate;  //!< position error / step = sum_i d_i k_pos_i
+    Vec3<float> err_mom;  //!< momentum error = step * sum_i d_i k_mom_i
+    float dchord;  //!< sagitta of the midpoint from the chord
 };
 
 //! Dormand-Prince 5(4) step with Shampine's midpoint interpolation
@@ -183,8 +190,12 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_fp64(UniformFieldEquation co
 
 //! Mixed-precision Dormand-Prince 5(4) step for a uniform field. The field
 //! equation depends on the momentum only, so the stages carry FP32 momenta
-//! and FP32 derivatives; positions are the FP64 start plus an FP32
-//! increment; the embedded error estimate is accumulated in FP64.
+//! and FP32 derivatives; the end position is the FP64 start plus an FP32
+//! increment. The embedded error estimate (a weighted sum of the FP32 stage
+//! derivatives) and the chord distance (from the FP32 increments to the end
+//! and to Shampine's midpoint) are formed in FP32: their inputs carry FP32
+//! rounding, which FP64 arithmetic on them would not remove. The driver
+//! takes the error norms and the acceptance test in FP64.
 GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation const& rhs,
                                                           double step,
                                                           OdeState const& beg_state)
@@ -263,44 +274,49 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation c
     eval(m_end, &kp[6], &km[6]);
 
     FieldStepperResult result;
-    result.end_state.pos = {beg_state.pos.x + double(h * dpos.x),
-                            beg_state.pos.y + double(h * dpos.y),
-                            beg_state.pos.z + double(h * dpos.z)};
+    F3 const end_inc{h * dpos.x, h * dpos.y, h * dpos.z};
+    result.end_state.pos = {beg_state.pos.x + double(end_inc.x),
+                            beg_state.pos.y + double(end_inc.y),
+                            beg_state.pos.z + double(end_inc.z)};
     result.end_state.mom = {double(m_end.x), double(m_end.y), double(m_end.z)};
 
-    // Embedded error estimate in FP64
-    double const dd[7] = {d1, 0, d3, d4, d5, d6, d7};
-    result.err_state = {{0, 0, 0}, {0, 0, 0}};
+    // Embedded error estimate: difference of the fifth- and fourth-order
+    // solutions, sum_i d_i k_i (times the step for the momentum)
+    F const df[7] = {F(d1), 0, F(d3), F(d4), F(d5), F(d6), F(d7)};
+    F3 epos{0, 0, 0}, emom{0, 0, 0};
 #pragma unroll
     for (int i = 0; i < 7; ++i)
     {
         if (i == 1)
             continue;
-        double const w = dd[i] * step;
-        axpy(w, Real3{double(kp[i].x), double(kp[i].y), double(kp[i].z)},
-             &result.err_state.pos);
-        axpy(w, Real3{double(km[i].x), double(km[i].y), double(km[i].z)},
-             &result.err_state.mom);
+        epos.x += df[i] * kp[i].x;
+        epos.y += df[i] * kp[i].y;
+        epos.z += df[i] * kp[i].z;
+        emom.x += df[i] * km[i].x;
+        emom.y += df[i] * km[i].y;
+        emom.z += df[i] * km[i].z;
     }
+    result.err_pos_rate = epos;
+    result.err_mom = {h * emom.x, h * emom.y, h * emom.z};
 
-    // Shampine midpoint for the chord test
+    // Shampine midpoint increment, and its distance from the chord
     F const cf[7] = {c1, 0, c3, c4, c5, c6, c7};
-    F3 mpos{0, 0, 0}, m_mid = m0;
-    F const half = F(0.5) * h;
+    F3 mpos{0, 0, 0};
 #pragma unroll
     for (int i = 0; i < 7; ++i)
     {
         mpos.x += cf[i] * kp[i].x;
         mpos.y += cf[i] * kp[i].y;
         mpos.z += cf[i] * kp[i].z;
-        m_mid.x += half * cf[i] * km[i].x;
-        m_mid.y += half * cf[i] * km[i].y;
-        m_mid.z += half * cf[i] * km[i].z;
     }
-    result.mid_state.pos = {beg_state.pos.x + double(half * mpos.x),
-                            beg_state.pos.y + double(half * mpos.y),
-                            beg_state.pos.z + double(half * mpos.z)};
-    result.mid_state.mom = {double(m_mid.x), double(m_mid.y), double(m_mid.z)};
+    F const half = F(0.5) * h;
+    F3 const mid_inc{half * mpos.x, half * mpos.y, half * mpos.z};
+    F3 const cr{end_inc.y * mid_inc.z - end_inc.z * mid_inc.y,
+                end_inc.z * mid_inc.x - end_inc.x * mid_inc.z,
+                end_inc.x * mid_inc.y - end_inc.y * mid_inc.x};
+    result.dchord = std::sqrt((cr.x * cr.x + cr.y * cr.y + cr.z * cr.z)
+                              / (end_inc.x * end_inc.x + end_inc.y * end_inc.y
+                                 + end_inc.z * end_inc.z));
     return result;
 }
 
@@ -393,6 +409,42 @@ class FieldDriver
         return max_of(errpos2, errvel2);
     }
 
+    //! Scaled error of a stepper result: above 1 the step is rejected
+    GBX_FORCEINLINE double step_err_sq(FieldStepperResult const& result,
+                                       double step,
+                                       Real3 const& mom) const
+    {
+        if constexpr (sizeof(real_type) == sizeof(double))
+        {
+            return rel_err_sq(result.err_state, step, mom)
+                   / ipow<2>(opt_.epsilon_rel_max);
+        }
+        else
+        {
+            // FP64 norms of the FP32 error estimate; the position error
+            // comes as a rate, so no division by the step is needed
+            Real3 const ep{double(result.err_pos_rate.x),
+                           double(result.err_pos_rate.y),
+                           double(result.err_pos_rate.z)};
+            Real3 const em{double(result.err_mom.x),
+                           double(result.err_mom.y),
+                           double(result.err_mom.z)};
+            double const errpos2 = dot_product(ep, ep);
+            double const errvel2 = dot_product(em, em) / dot_product(mom, mom);
+            return max_of(errpos2, errvel2) / ipow<2>(opt_.epsilon_rel_max);
+        }
+    }
+
+    //! Distance of the stepper's midpoint from the chord
+    static GBX_FORCEINLINE double chord_distance(FieldStepperResult const& result,
+                                                 OdeState const& state)
+    {
+        if constexpr (sizeof(real_type) == sizeof(double))
+            return distance_chord(state.pos, result.mid_state.pos, result.end_state.pos);
+        else
+            return double(result.dchord);
+    }
+
     static GBX_FORCEINLINE double distance_chord(Real3 const& beg_pos,
                                                  Real3 const& mid_pos,
                                                  Real3 const& end_pos)
@@ -428,8 +480,7 @@ class FieldDriver
         do
         {
             result = dormand_prince_step(rhs_, step, state);
-            double dchord = distance_chord(
-                state.pos, result.mid_state.pos, result.end_state.pos);
+            double dchord = chord_distance(result, state);
             if (dchord > opt_.delta_chord + FieldOptions::dchord_tol)
             {
                 double scale_step = max_of(std::sqrt(opt_.delta_chord / dchord),
@@ -443,8 +494,7 @@ class FieldDriver
         } while (!succeeded && --remaining_steps > 0);
         output.end.step = step;
         output.end.state = result.end_state;
-        output.err_sq = rel_err_sq(result.err_state, step, state.mom)
-                        / ipow<2>(opt_.epsilon_rel_max);
+        output.err_sq = this->step_err_sq(result, step, state.mom);
         return output;
     }
 
@@ -458,8 +508,7 @@ class FieldDriver
         do
         {
             result = dormand_prince_step(rhs_, step, state);
-            err_sq = rel_err_sq(result.err_state, step, state.mom)
-                     / ipow<2>(opt_.epsilon_rel_max);
+            err_sq = this->step_err_sq(result, step, state.mom);
             if (err_sq > 1)
             {
                 step *= max_of(this->new_step_scale(err_sq),
@@ -489,8 +538,7 @@ class FieldDriver
             FieldStepperResult result = dormand_prince_step(rhs_, step, state);
             output.end.state = result.end_state;
             output.end.step = step;
-            double err_sq = rel_err_sq(result.err_state, step, state.mom)
-                            / ipow<2>(opt_.epsilon_rel_max);
+            double err_sq = this->step_err_sq(result, step, state.mom);
             output.proposed_step = step * this->new_step_scale(err_sq);
         }
         return output;
@@ -579,9 +627,20 @@ class FieldPropagation
                    substep.state.pos.y - state_.pos.y,
                    substep.state.pos.z - state_.pos.z};
         double const clen = norm(cdir);
-        cdir.x /= clen;
-        cdir.y /= clen;
-        cdir.z /= clen;
+        if constexpr (sizeof(real_type) == sizeof(double))
+        {
+            cdir.x /= clen;
+            cdir.y /= clen;
+            cdir.z /= clen;
+        }
+        else
+        {
+            // One FP64 division instead of three
+            double const inv_clen = 1 / clen;
+            cdir.x *= inv_clen;
+            cdir.y *= inv_clen;
+            cdir.z *= inv_clen;
+        }
         if (clen >= minimum_substep)
         {
             geo.set_dir(cdir);

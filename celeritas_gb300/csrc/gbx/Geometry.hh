@@ -194,13 +194,20 @@ class GeoTrackView
         if (!on_surface && max_dist < INFINITY)
         {
             // The radial distance |r - R| bounds the distance along any ray;
-            // skip the cylinder unless r lies within max_dist of R, with a
-            // margin far above the rounding of the quadratic's roots
-            double const r2 = ipow<2>(pos.x) + ipow<2>(pos.y);
-            double const radius = std::sqrt(sr.value);
-            double const margin = 1e-6 * (radius + max_dist) + 1e-9;
-            double const hi = radius + max_dist + margin;
-            double const lo = radius - max_dist - margin;
+            // skip the cylinder unless r lies within max_dist of R. The test
+            // runs in FP32 (the FP64 pipe is the scarce one) with a margin of
+            // 1e-5 (R + max_dist) + 1e-6 cm: FP32 rounding of r^2 and of the
+            // bounds is below 1e-6 relative, and the rounding of the
+            // quadratic's FP64 roots far below that, so a skipped cylinder
+            // has no root within max_dist and the hit is unchanged. Distances
+            // beyond FP32 range give infinite bounds: nothing is skipped.
+            float const xf = static_cast<float>(pos.x);
+            float const yf = static_cast<float>(pos.y);
+            float const r2 = xf * xf + yf * yf;
+            float const df = static_cast<float>(max_dist);
+            float const margin = 1e-5f * (sr.radius + df) + 1e-6f;
+            float const hi = sr.radius + df + margin;
+            float const lo = sr.radius - df - margin;
             if (r2 > hi * hi || (lo > 0 && r2 < lo * lo))
                 return;
         }
@@ -649,19 +656,39 @@ GBX_FUNCTION double GeoTrackView::find_safety() const
     Real3 const pos = this->pos();
     size_type const vol = s_.volume[slot_];
     double result = INFINITY;
+    // A cylinder's safety distance is |r - R| up to FP64 rounding (~1e-13
+    // relative). Its FP32 lower bound |r - R| - 1e-5 (R + r + best) - 1e-6
+    // stays below the exact value by far more than FP32 rounding (below
+    // 1e-6 relative), so a cylinder whose bound exceeds the best distance so
+    // far cannot lower the minimum and its FP64 solve is skipped: the result
+    // is unchanged, and far cylinders cost a few FP32 operations.
+    float const xf = static_cast<float>(pos.x);
+    float const yf = static_cast<float>(pos.y);
+    float const rf = std::sqrt(xf * xf + yf * yf);
+    auto visit = [&](size_type surf) {
+        SurfaceRecord const& sr = p_.surfaces[surf];
+        if (sr.type == surf_czc)
+        {
+            float const best = static_cast<float>(result);
+            float const margin = 1e-5f * (sr.radius + rf + best) + 1e-6f;
+            if (std::fabs(rf - sr.radius) - margin > best)
+                return;
+        }
+        result = min_of(result, this->surface_safety(surf, pos));
+    };
     if (vol != p_.background)
     {
         VolumeRecord const& v = p_.volumes[vol];
         for (size_type f = 0; f < v.num_faces; ++f)
         {
-            result = min_of(result, this->surface_safety(v.faces[f], pos));
+            visit(v.faces[f]);
         }
     }
     else
     {
         for (size_type s = 0; s < p_.num_surfaces; ++s)
         {
-            result = min_of(result, this->surface_safety(s, pos));
+            visit(s);
         }
     }
     return result;

@@ -813,7 +813,9 @@ void Builder::build_geometry()
                 return i;
             }
         }
-        hp_.surfaces.push_back({type, value});
+        float const radius
+            = (type == surf_czc) ? static_cast<float>(std::sqrt(value)) : 0.0f;
+        hp_.surfaces.push_back({type, radius, value});
         return static_cast<size_type>(hp_.surfaces.size() - 1);
     };
     auto box_faces = [&](double const* lo, double const* hi, size_type* faces) {
@@ -1164,6 +1166,7 @@ HostParams Builder::build()
     this->build_geometry();
     hp_.rng_jump = make_xorwow_jump_polys();
     hp_.scalars.rng_per_track = opts_.rng_per_track;
+    hp_.scalars.reentrant_looping = opts_.reentrant_looping;
     hp_.scalars.event_tallies = opts_.event_tallies;
     for (auto const& b : geo_.boxes)
     {

@@ -72,6 +72,8 @@ struct ParamsOptions
     bool rng_per_track{false};
     //! Per-event energy-deposition tallies
     bool event_tallies{false};
+    //! A reentrant boundary step keeps the looping-step count
+    bool reentrant_looping{false};
 };
 
 //! All parameter tables in host memory

@@ -1,6 +1,6 @@
 """Benchmark workloads of the EM-shower stepping loop and their primaries.
 
-Two workloads, both on the 50-layer Pb/lAr sampling calorimeter that the
+Five workloads. Two on the 50-layer Pb/lAr sampling calorimeter that the
 reference's benchmark problems use (world box 60 x 60 x 60 cm of vacuum;
 layers of 2.3 mm Pb + 5.7 mm lAr, 40 x 40 cm, starting at z = 0):
 
@@ -10,8 +10,19 @@ layers of 2.3 mm Pb + 5.7 mm lAr, 40 x 40 cm, starting at z = 0):
   10^4 e-, energies log-uniform in 0.1-10 GeV, Gaussian transverse spread of
   1 cm, one primary per event with all events in flight, 2^20 track slots.
 
+and three on the CMS-like detector (concentric shells, 3.8 T along z):
+``c3`` events of 50 primaries, ``c4`` uneven events for the batching
+autotuner, ``c5`` a served stream of events on both geometries.
+
 Primaries are synthetic (seeded numpy), standing in for the reference's
 PrimaryGenerator (src/celeritas/phys/PrimaryGenerator.cc).
+
+The workloads with a magnetic field run with ``reentrant_looping``: a
+field step that ends on a boundary the track re-enters at once keeps its
+looping-step count, so that an electron circling in vacuum with its orbit
+grazing a surface reaches the looping cut (the reference resets the count
+there and such a track never ends; celer-sim stops the whole run at its
+global step limit instead).
 """
 
 from __future__ import annotations
@@ -29,6 +40,7 @@ WORKLOADS = {
     "c2": dict(geometry="calo", physics="calo", num_primaries=10000, energy=100.0,
                emax=1e4, sigma=1.0, pdg=11, slots=1 << 20, seed=0, events=10000,
                msc=True, field=(1.0, 0.0, 0.0),
+               reentrant_looping=True,
                description="calorimeter 50x(2.3mm Pb+5.7mm lAr), Urban MSC, 1 T "
                            "uniform field along x, 10^4 e- log-uniform 0.1-10 GeV, "
                            "sigma 1 cm, 2^20 track slots, FP64"),
@@ -38,12 +50,14 @@ WORKLOADS = {
     "c3": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
                emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
                seed=0, events=1300, msc=True, field=(0.0, 0.0, 3.8),
-               bench_primaries=3250,
+               bench_primaries=3250, tune_primaries=800,
+               reentrant_looping=True,
                description="CMS-like: 10 Si shells (0.3 mm, r 4-110 cm), PbWO4 barrel "
                            "(r 129-152 cm), 17 x (5 cm brass + 0.4 cm scintillator) "
                            "(r 180-295 cm), 3.8 T along z, Urban MSC; events of 50 "
                            "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
-                           "one bench step = 65 of the 1300 events"),
+                           "one bench step = 65 of the 1300 events; launch "
+                           "configuration autotuned on 16 other events"),
     # Batching of uneven events: CMS-like detector, 4096 events with primaries
     # per event log-uniform in 1-1000 and energies log-uniform in
     # 0.1-100 GeV (e-/gamma alternating, |eta| < 1.5), all in flight
@@ -52,6 +66,7 @@ WORKLOADS = {
                max_primaries=1000, energy=100.0, emax=1e5, pdgs=(11, 22), eta_max=1.5,
                slots=1 << 21, seed=0, msc=True, field=(0.0, 0.0, 3.8),
                bench_events=64, calibration_events=8,
+               reentrant_looping=True,
                description="batching: CMS-like, events with log-uniform 1-1000 "
                            "e-/gamma primaries of log-uniform 0.1-100 GeV, |eta| < 1.5, "
                            "3.8 T; one bench step = 64 of the 4096 events in flight "
@@ -61,6 +76,7 @@ WORKLOADS = {
     # slots per geometry (2^22 in all) with queues of 16 x slots
     "c5": dict(geometry="cms+calo", slots=1 << 21, rates=(50, 200, 1000, 2000),
                duration=2.0, seed=0,
+               reentrant_looping=True,
                description="serving: Poisson arrivals at 50-2000 events/s for 2 s each, "
                            "Pareto(1.5) primaries capped at 5000, CMS-like or "
                            "calorimeter 50/50, 2 x 2^21 track slots"),
@@ -93,6 +109,8 @@ def physics_args(wl: dict) -> list[str]:
     args = []
     if wl["msc"]:
         args.append("--msc")
+    if wl.get("reentrant_looping"):
+        args.append("--reentrant-looping")
     if any(wl["field"]):
         args += ["--field"] + [repr(float(f)) for f in wl["field"]]
     return args

@@ -87,6 +87,18 @@ typedef struct
      * event_tallies accumulates detector energy deposition per event. */
     int rng_per_track;
     int event_tallies;
+    /* Nonzero: a field-propagation step that ends on a boundary which the
+     * track re-enters at once (ORANGE's reentrant crossing, back into the
+     * volume it came from) keeps a looping track's looping-step count
+     * instead of resetting it. Without counterpart in the reference, whose
+     * looping cut (PropagationApplier,
+     * src/celeritas/global/alongstep/detail/PropagationApplier.hh:147-170)
+     * resets the count on any step that is not looping: a low-energy
+     * electron circling in vacuum with its orbit grazing a surface then
+     * never reaches the cut, and celer-sim ends such a run only by its
+     * global step limit (app/celer-sim/Transporter.cc:135-150). Zero keeps
+     * the reference's behaviour. */
+    int reentrant_looping;
 } gbx_params_options;
 
 /* Build problem parameters from a physics input file and a named geometry

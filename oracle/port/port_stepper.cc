@@ -241,7 +241,9 @@ class PortStepper
 
 //! Physics options from the command line: --msc, --field Bx By Bz [tesla],
 //! --track-order N (changes the registered actions only: the host loop's
-//! results do not depend on the thread order)
+//! results do not depend on the thread order), --reentrant-looping (a
+//! reentrant boundary step keeps the looping-step count; off in the
+//! reference)
 ParamsOptions physics_options(int argc, char** argv)
 {
     ParamsOptions opts;
@@ -258,6 +260,10 @@ ParamsOptions physics_options(int argc, char** argv)
         else if (a == "--track-order" && i + 1 < argc)
         {
             opts.track_order = std::stoul(argv[i + 1]);
+        }
+        else if (a == "--reentrant-looping")
+        {
+            opts.reentrant_looping = true;
         }
     }
     return opts;

@@ -191,3 +191,23 @@ def test_reseed_restarts_event(gb, calo_params):
     assert results[0][0] == results[1][0]
     np.testing.assert_allclose(results[0][1], results[1][1], rtol=1e-12)
     assert results[0][0] != results[2][0]
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_reentrant_looping_ends_grazing_orbit(gb, precision):
+    """The grazing vacuum orbit of tests/test_oracle.py on the device: with
+    reentrant_looping the looping cut ends the track within 200 steps."""
+    from celeritas_gb300.primaries import PRIMARY_DTYPE
+
+    p = np.zeros(1, dtype=PRIMARY_DTYPE)
+    p["pdg"] = 11
+    p["energy"] = 0.01845506951212883
+    p["pos"][0] = (-108.25911568208411, 19.777196382226563, 179.9582562600299)
+    d = np.array([-0.7892325346384539, -0.6140944603789887, 1.065034111781243e-43])
+    p["dir"][0] = d / np.linalg.norm(d)
+    params = gb.Params(gb.physics_file("cms"), "cms", field_tesla=(0.0, 0.0, 3.8), msc=True,
+                       precision=precision, reentrant_looping=True)
+    st = gb.Stepper(params, 256, seed=0)
+    res = [st.step(p)] + st.run(max_steps=199)
+    assert res[-1].alive == 0 and res[-1].queued == 0
+    assert len(res) < 200

@@ -42,6 +42,64 @@ def test_port_matches_reference(built_port, name):
     assert out["edep"] == golden["edep"]  # bit-exact FP64
 
 
+FIELD_CASES = [n for n in GOLDEN_CASES if "field" in n or n.startswith("cms")]
+
+
+@pytest.mark.parametrize("name", FIELD_CASES)
+def test_reentrant_looping_inert_in_normal_transport(built_port, name):
+    """The reentrant_looping option only changes tracks that loop and then
+    hit a surface they re-enter at once; in the golden transports (fields of
+    1-3.8 T, calorimeter and CMS-like) the results stay the reference's."""
+    golden = load_golden(name)
+    c = golden["case"]
+    geometry = c.get("geometry", "calo")
+    prim = case_primaries(c)
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "p.txt")
+        write_primaries_text(ptxt, prim)
+        out = oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
+                              geometry=geometry,
+                              extra=case_options(c) + ["--reentrant-looping"])
+    assert [list(s) for s in out["steps"]] == golden["steps"]
+    assert out["edep"] == golden["edep"]
+
+
+def test_reentrant_looping_ends_grazing_orbit(built_port):
+    """An 18 keV electron in the CMS-like detector's vacuum just outside the
+    last silicon shell, moving perpendicular to the 3.8 T field: its 0.12 mm
+    orbit grazes the shell's outer cylinder every few steps, each graze is a
+    reentrant boundary step (back into the vacuum), and the reference's
+    looping cut, which resets its count on every non-looping step, never
+    ends the track (the compiled reference agrees where it is built). With
+    reentrant_looping the looping cut ends it."""
+    from celeritas_gb300.primaries import PRIMARY_DTYPE
+
+    p = np.zeros(1, dtype=PRIMARY_DTYPE)
+    p["pdg"] = 11
+    p["energy"] = 0.01845506951212883
+    p["pos"][0] = (-108.25911568208411, 19.777196382226563, 179.9582562600299)
+    d = np.array([-0.7892325346384539, -0.6140944603789887, 1.065034111781243e-43])
+    p["dir"][0] = d / np.linalg.norm(d)
+    base = ["--msc", "--field", "0", "0", "3.8", "--steps", "200"]
+    runs = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "p.txt")
+        write_primaries_text(ptxt, p)
+        for name, extra in (("reference", []), ("reentrant", ["--reentrant-looping"])):
+            runs[name] = oracle.run_port(physics_file("cms"), ptxt, 256, 0, geometry="cms",
+                                         extra=base + extra)
+        if os.path.exists(oracle.REF_BIN):
+            runs["compiled"] = oracle.run_reference(physics_file("cms"), ptxt, 256, 0,
+                                                    geometry="cms", extra=base)
+    # Still alive after 200 steps with the reference's looping logic
+    assert runs["reference"]["steps"][-1][3] == 1
+    if "compiled" in runs:
+        assert runs["compiled"]["steps"] == runs["reference"]["steps"]
+    # Ended by the looping cut with the option
+    assert runs["reentrant"]["steps"][-1][3] == 0
+    assert runs["reentrant"]["iterations"] < 200
+
+
 def test_action_labels_match_reference(built_port):
     golden = load_golden("calo_e1000_n4")
     out = run_case(golden)
