@@ -8,12 +8,15 @@ over
 
 * the number of track slots (one stepper per candidate),
 * threads per block of the charged along-step kernel (64, 128, 256; 512 is
-  reported as invalid: it exceeds the register file of that kernel),
-* the charged along-step as a persistent kernel or one thread per track,
+  reported as invalid: it exceeds the register file of that kernel) together
+  with its form, a persistent kernel or one thread per track (the best block
+  size differs between the two forms, so they are tuned as pairs),
 * the sort threshold: action sorts only in steps that start with at least
   this many live tracks (0: always),
 
-keeping the best value of each parameter before tuning the next.
+keeping the best value of each parameter before tuning the next. Every
+candidate first transports the calibration events once untimed (a new
+setting may capture new CUDA graphs), then once timed.
 """
 
 from __future__ import annotations
@@ -70,6 +73,7 @@ def autotune(make_stepper: Callable[[int], object], primaries: np.ndarray,
         except RuntimeError as e:
             trials.append(Trial(dict(config), None, None, str(e)))
             return None
+        transport(stepper, primaries)  # warm-up: graph capture for the setting
         seconds, steps = transport(stepper, primaries)
         trial = Trial(dict(config), seconds, steps)
         trials.append(trial)
@@ -89,12 +93,14 @@ def autotune(make_stepper: Callable[[int], object], primaries: np.ndarray,
     stepper = make_stepper(best["slots"])
     transport(stepper, primaries)
 
-    for name, values in (("along_block_size", block_sizes),
-                         ("along_persistent", (0, 1)),
-                         ("sort_threshold", thresholds)):
+    stages = (
+        [{"along_block_size": b, "along_persistent": f} for f in (1, 0) for b in block_sizes],
+        [{"sort_threshold": v} for v in thresholds],
+    )
+    for candidates in stages:
         winner = None
-        for v in values:
-            t = run(stepper, dict(best, **{name: v}))
+        for settings in candidates:
+            t = run(stepper, dict(best, **settings))
             if t and (winner is None or t.seconds < winner.seconds):
                 winner = t
         if winner is not None:

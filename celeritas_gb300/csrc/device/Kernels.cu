@@ -560,9 +560,20 @@ __device__ __forceinline__ bool sorted_slot(StateData const& s,
 #    define GBX_ALONG_MIN_BLOCKS 1
 #endif
 
+// Register cap of the charged along-step kernels (0: none). An SM
+// sub-partition holds 16,384 registers, so a cap of 168 per thread keeps 3
+// warps resident on each (12 per SM) where 174 keeps 2.
+#ifndef GBX_ALONG_MAXNREG
+#    define GBX_ALONG_MAXNREG 0
+#endif
+#if GBX_ALONG_MAXNREG > 0
+#    define GBX_ALONG_BOUNDS(MINB) __maxnreg__(GBX_ALONG_MAXNREG)
+#else
+#    define GBX_ALONG_BOUNDS(MINB) __launch_bounds__(block_size, MINB)
+#endif
+
 template<AlongKind K>
-__global__ __launch_bounds__(block_size,
-                             K == AlongKind::charged ? GBX_ALONG_MIN_BLOCKS : 1) void
+__global__ GBX_ALONG_BOUNDS(K == AlongKind::charged ? GBX_ALONG_MIN_BLOCKS : 1) void
 along_step_sorted_kernel(ParamsData p,
                          StateData s,
                          size_type const* offsets,
@@ -581,7 +592,7 @@ along_step_sorted_kernel(ParamsData p,
 //! its own finishes. Lanes of a warp thus stay busy on different tracks
 //! instead of waiting for the one with the most substeps. Every track runs
 //! the same sequence of operations as along_step_impl.
-__global__ __launch_bounds__(block_size, 1) void along_charged_persistent_kernel(
+__global__ GBX_ALONG_BOUNDS(1) void along_charged_persistent_kernel(
     ParamsData p,
     StateData s,
     size_type const* offsets,

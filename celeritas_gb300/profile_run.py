@@ -2,7 +2,8 @@
 
     python -m celeritas_gb300.profile_run --workload c2 [--primaries N]
         [--max-iterations K] [--steps-log FILE] [--graph]
-        [--precision double|mixed] [--track-order N]
+        [--precision double|mixed] [--track-order N] [--slots S]
+        [--tuning name=value,...]
 
 Inserts the workload's primaries, then steps (eagerly by default, so that
 every kernel is its own launch) until the state empties or K iterations have
@@ -33,14 +34,23 @@ def main(argv=None):
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--precision", default="double", choices=["double", "mixed"])
     ap.add_argument("--track-order", type=int, default=0)
+    ap.add_argument("--slots", type=int, default=None,
+                    help="track slots (default: the workload's)")
+    ap.add_argument("--tuning", default="",
+                    help="launch settings, e.g. along_block_size=64,along_persistent=0")
     args = ap.parse_args(argv)
 
     wl = WORKLOADS[args.workload]
     load_library(precision=args.precision)
     params = Params(physics_file(wl["physics"]), wl["geometry"],
                     field_tesla=wl["field"], msc=wl["msc"],
-                    track_order=args.track_order, precision=args.precision)
-    stepper = Stepper(params, wl["slots"], seed=wl["seed"], use_graph=args.graph)
+                    track_order=args.track_order, precision=args.precision,
+                    reentrant_looping=wl.get("reentrant_looping", False))
+    stepper = Stepper(params, args.slots or wl["slots"], seed=wl["seed"],
+                      use_graph=args.graph)
+    if args.tuning:
+        stepper.set_tuning(**{k: int(v) for k, v in
+                              (kv.split("=") for kv in args.tuning.split(","))})
     prim = make_primaries(wl, num=args.primaries)
     labels = params.action_labels()
     counts = []

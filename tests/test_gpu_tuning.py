@@ -107,7 +107,9 @@ def test_autotuner_picks_a_measured_candidate(gb):
     assert best in [t.config for t in measured]
     assert all(t.track_steps > 0 for t in measured)
     rejected = [t for t in trials if not t.seconds]
-    assert [t.config["along_block_size"] for t in rejected] == [512]
+    # 512 threads are rejected in both kernel forms
+    assert [t.config["along_block_size"] for t in rejected] == [512, 512]
+    assert sorted(t.config["along_persistent"] for t in rejected) == [0, 1]
     assert "512" in rejected[0].note
     assert best["along_block_size"] in (128, 256)
     assert best["slots"] in (1 << 14, 1 << 15)
