@@ -47,6 +47,28 @@ class _ParamsOptions(ctypes.Structure):
                 ("event_tallies", ctypes.c_int), ("reentrant_looping", ctypes.c_int)]
 
 
+#: Step data of a hit (GBX_STEP_* bits of the C header, the reference's
+#: StepSelection); step, detector and track_id are always recorded
+STEP_SELECT = {
+    "pre_time": 1 << 0, "pre_pos": 1 << 1, "pre_dir": 1 << 2, "pre_energy": 1 << 3,
+    "post_time": 1 << 4, "post_pos": 1 << 5, "post_dir": 1 << 6, "post_energy": 1 << 7,
+    "event_id": 1 << 8, "parent_id": 1 << 9, "track_step_count": 1 << 10,
+    "step_length": 1 << 11, "particle": 1 << 12, "energy_deposition": 1 << 13,
+}
+STEP_SELECT_ALL = (1 << 14) - 1
+_HIT_UINT = ("step", "detector", "track_id", "event_id", "parent_id", "track_step_count",
+             "particle")
+_HIT_DOUBLE = ("step_length", "energy_deposition", "pre_time", "pre_pos", "pre_dir",
+               "pre_energy", "post_time", "post_pos", "post_dir", "post_energy")
+_HIT_VEC3 = ("pre_pos", "pre_dir", "post_pos", "post_dir")
+
+
+class _StepHits(ctypes.Structure):
+    _fields_ = ([("capacity", ctypes.c_size_t)]
+                + [(n, ctypes.POINTER(ctypes.c_uint)) for n in _HIT_UINT]
+                + [(n, ctypes.POINTER(ctypes.c_double)) for n in _HIT_DOUBLE])
+
+
 class _StepResult(ctypes.Structure):
     _fields_ = [
         ("generated", ctypes.c_uint),
@@ -114,6 +136,10 @@ _PROTOTYPES = [
     ("gbx_stepper_reseed", ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong]),
     ("gbx_stepper_set_tuning", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong]),
+    ("gbx_stepper_set_step_output", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_size_t]),
+    ("gbx_stepper_read_step_output", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(_StepHits), ctypes.POINTER(ctypes.c_size_t)]),
     ("gbx_stepper_get_tuning", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]),
     ("gbx_stepper_event_live", ctypes.c_int,
@@ -306,6 +332,53 @@ class Stepper:
         for name, value in settings.items():
             _check(self._lib, self._lib.gbx_stepper_set_tuning(
                 self._handle, name.encode(), int(value)))
+
+    def set_step_output(self, selection="all", nonzero_energy_deposition: bool = True,
+                        capacity: int = 1 << 20):
+        """Collect the hits of every step (StepCollector + DetectorSteps).
+
+        ``selection`` is "all", an int mask of STEP_SELECT bits, or an
+        iterable of STEP_SELECT names; ``capacity`` records are held on the
+        device between reads (0 turns the output off). Host buffers of the
+        same capacity are kept for ``read_step_output``.
+        """
+        if isinstance(selection, str) and selection == "all":
+            mask = STEP_SELECT_ALL
+        elif isinstance(selection, int):
+            mask = selection
+        else:
+            mask = 0
+            for name in selection:
+                mask |= STEP_SELECT[name]
+        _check(self._lib, self._lib.gbx_stepper_set_step_output(
+            self._handle, mask, int(nonzero_energy_deposition), int(capacity)))
+        self._hit_mask = mask
+        self._hit_bufs = {}
+        if capacity:
+            wanted = {"step", "detector", "track_id"} | {
+                n for n, b in STEP_SELECT.items() if mask & b}
+            for n in _HIT_UINT + _HIT_DOUBLE:
+                if n in wanted:
+                    shape = (capacity, 3) if n in _HIT_VEC3 else (capacity,)
+                    dtype = np.uint32 if n in _HIT_UINT else np.float64
+                    self._hit_bufs[n] = np.zeros(shape, dtype=dtype)
+        self._hit_capacity = int(capacity)
+
+    def read_step_output(self) -> dict:
+        """Hits recorded since the last read, as numpy arrays (copies) keyed
+        by field; positions and directions have shape (n, 3)."""
+        bufs = getattr(self, "_hit_bufs", None)
+        if not bufs:
+            raise GbxError("step output is not enabled")
+        hits = _StepHits()
+        hits.capacity = self._hit_capacity
+        for n, arr in bufs.items():
+            ctype = ctypes.c_uint if n in _HIT_UINT else ctypes.c_double
+            setattr(hits, n, arr.ctypes.data_as(ctypes.POINTER(ctype)))
+        count = ctypes.c_size_t()
+        _check(self._lib, self._lib.gbx_stepper_read_step_output(
+            self._handle, ctypes.byref(hits), ctypes.byref(count)))
+        return {n: arr[:count.value].copy() for n, arr in bufs.items()}
 
     def get_tuning(self, name: str) -> int:
         v = ctypes.c_longlong()

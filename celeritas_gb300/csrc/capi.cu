@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstring>
 #include <exception>
+#include <limits>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -369,6 +370,57 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
         std::copy(v.begin(), v.end(), out);
     });
 }
+
+int gbx_stepper_set_step_output(gbx_stepper* stepper,
+                                unsigned int selection,
+                                int nonzero_energy_deposition,
+                                size_t capacity)
+{
+    return guarded([&] {
+        if (!stepper)
+            throw std::runtime_error("null argument");
+        if (capacity > size_t(std::numeric_limits<gbx::size_type>::max()))
+            throw std::runtime_error("step output capacity too large");
+        stepper->stepper->set_step_output(
+            selection, nonzero_energy_deposition != 0, static_cast<gbx::size_type>(capacity));
+    });
+}
+
+int gbx_stepper_read_step_output(gbx_stepper* stepper,
+                                 const gbx_step_hits* out,
+                                 size_t* num_hits)
+{
+    return guarded([&] {
+        if (!stepper || !out || !num_hits)
+            throw std::runtime_error("null argument");
+        gbx::StepHitsRef dst;
+        dst.capacity = static_cast<gbx::size_type>(
+            std::min<size_t>(out->capacity, std::numeric_limits<gbx::size_type>::max()));
+        dst.step = out->step;
+        dst.detector = out->detector;
+        dst.track_id = out->track_id;
+        dst.event_id = out->event_id;
+        dst.parent_id = out->parent_id;
+        dst.track_step_count = out->track_step_count;
+        dst.particle = out->particle;
+        dst.step_length = out->step_length;
+        dst.energy_deposition = out->energy_deposition;
+        dst.pre_time = out->pre_time;
+        dst.pre_pos = out->pre_pos;
+        dst.pre_dir = out->pre_dir;
+        dst.pre_energy = out->pre_energy;
+        dst.post_time = out->post_time;
+        dst.post_pos = out->post_pos;
+        dst.post_dir = out->post_dir;
+        dst.post_energy = out->post_energy;
+        *num_hits = stepper->stepper->state().read_step_output(dst);
+    });
+}
+
+static_assert(GBX_STEP_ALL == gbx::step_select_all, "step selection bits differ");
+static_assert(GBX_STEP_ENERGY_DEPOSITION == gbx::step_energy_deposition,
+              "step selection bits differ");
+static_assert(sizeof(unsigned int) == sizeof(gbx::size_type), "index type differs");
 
 int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value)
 {

@@ -560,10 +560,165 @@ CoreState::CoreState(CoreParams const& params,
 
 CoreState::~CoreState()
 {
+    if (hits_storage_)
+        cudaFree(hits_storage_);
     if (storage_)
         cudaFree(storage_);
     if (pinned_primaries_)
         cudaFreeHost(pinned_primaries_);
+}
+
+void CoreState::set_step_output(unsigned int selection,
+                                bool nonzero_energy_deposition,
+                                size_type capacity)
+{
+    if (selection & ~unsigned(step_select_all))
+        throw std::runtime_error("unknown step output selection bits");
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    if (hits_storage_)
+    {
+        GBX_CUDA(cudaFree(hits_storage_));
+        hits_storage_ = nullptr;
+    }
+    ref_.pre_time = ref_.pre_pos = ref_.pre_dir = ref_.pre_energy = nullptr;
+    ctx_.hits = StepHitsRef{};
+    ctx_.hit_block_offsets = nullptr;
+    // Start from an empty output without a pending overflow
+    Counters c = this->counters();
+    c.num_hits = 0;
+    c.error_flags &= ~size_type(error_hit_overflow);
+    GBX_CUDA(cudaMemcpyAsync(
+        ref_.counters, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    if (capacity == 0)
+    {
+        ctx_.state = ref_;
+        return;
+    }
+
+    // One allocation: pre-step points per slot, records, block offsets
+    std::size_t const n = ref_.size;
+    std::size_t const cap = capacity;
+    size_type const nblocks = (ref_.size + block_size - 1) / block_size;
+    Layout L;
+    auto slot_array = [&](unsigned int bit, std::size_t per_slot) {
+        return (selection & bit) ? L.reserve(per_slot * n) : std::size_t(-1);
+    };
+    auto hit_array = [&](unsigned int bit, std::size_t per_hit) {
+        return (bit == 0 || (selection & bit)) ? L.reserve(per_hit * cap)
+                                               : std::size_t(-1);
+    };
+    std::size_t const o_ptime = slot_array(step_pre_time, 8);
+    std::size_t const o_ppos = slot_array(step_pre_pos, 24);
+    std::size_t const o_pdir = slot_array(step_pre_dir, 24);
+    std::size_t const o_pen = slot_array(step_pre_energy, 8);
+    std::size_t const o_step = hit_array(0, 4), o_det = hit_array(0, 4),
+                      o_track = hit_array(0, 4);
+    std::size_t const o_event = hit_array(step_event_id, 4),
+                      o_parent = hit_array(step_parent_id, 4),
+                      o_count = hit_array(step_track_step_count, 4),
+                      o_particle = hit_array(step_particle, 4),
+                      o_len = hit_array(step_step_length, 8),
+                      o_edep = hit_array(step_energy_deposition, 8),
+                      o_htime = hit_array(step_pre_time, 8),
+                      o_hpos = hit_array(step_pre_pos, 24),
+                      o_hdir = hit_array(step_pre_dir, 24),
+                      o_hen = hit_array(step_pre_energy, 8),
+                      o_qtime = hit_array(step_post_time, 8),
+                      o_qpos = hit_array(step_post_pos, 24),
+                      o_qdir = hit_array(step_post_dir, 24),
+                      o_qen = hit_array(step_post_energy, 8);
+    std::size_t const o_blocks = L.reserve(4 * std::size_t(nblocks));
+    GBX_CUDA(cudaMalloc(&hits_storage_, L.size()));
+    GBX_CUDA(cudaMemsetAsync(hits_storage_, 0, L.size(), stream_));
+    auto* b = static_cast<unsigned char*>(hits_storage_);
+    auto at = [b](std::size_t off) -> void* {
+        return off == std::size_t(-1) ? nullptr : static_cast<void*>(b + off);
+    };
+    ref_.pre_time = static_cast<double*>(at(o_ptime));
+    ref_.pre_pos = static_cast<double*>(at(o_ppos));
+    ref_.pre_dir = static_cast<double*>(at(o_pdir));
+    ref_.pre_energy = static_cast<double*>(at(o_pen));
+    StepHitsRef& h = ctx_.hits;
+    h.capacity = capacity;
+    h.selection = selection;
+    h.nonzero_energy_deposition = nonzero_energy_deposition;
+    h.step = static_cast<size_type*>(at(o_step));
+    h.detector = static_cast<size_type*>(at(o_det));
+    h.track_id = static_cast<size_type*>(at(o_track));
+    h.event_id = static_cast<size_type*>(at(o_event));
+    h.parent_id = static_cast<size_type*>(at(o_parent));
+    h.track_step_count = static_cast<size_type*>(at(o_count));
+    h.particle = static_cast<size_type*>(at(o_particle));
+    h.step_length = static_cast<double*>(at(o_len));
+    h.energy_deposition = static_cast<double*>(at(o_edep));
+    h.pre_time = static_cast<double*>(at(o_htime));
+    h.pre_pos = static_cast<double*>(at(o_hpos));
+    h.pre_dir = static_cast<double*>(at(o_hdir));
+    h.pre_energy = static_cast<double*>(at(o_hen));
+    h.post_time = static_cast<double*>(at(o_qtime));
+    h.post_pos = static_cast<double*>(at(o_qpos));
+    h.post_dir = static_cast<double*>(at(o_qdir));
+    h.post_energy = static_cast<double*>(at(o_qen));
+    ctx_.hit_block_offsets = static_cast<size_type*>(at(o_blocks));
+    ctx_.state = ref_;
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+}
+
+size_type CoreState::read_step_output(StepHitsRef const& out)
+{
+    StepHitsRef const& h = ctx_.hits;
+    if (!h.enabled())
+        throw std::runtime_error("step output is not enabled");
+    Counters c = this->counters();
+    if (c.error_flags & error_hit_overflow)
+    {
+        size_type const held = c.num_hits;
+        c.num_hits = 0;
+        c.error_flags &= ~size_type(error_hit_overflow);
+        GBX_CUDA(cudaMemcpyAsync(
+            ref_.counters, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+        GBX_CUDA(cudaStreamSynchronize(stream_));
+        throw std::runtime_error(
+            "step output overflowed its capacity of " + std::to_string(h.capacity)
+            + " records (" + std::to_string(held)
+            + " held): hits of later steps were dropped; read the output more "
+              "often or raise its capacity");
+    }
+    size_type const n = c.num_hits;
+    if (n > out.capacity)
+        throw std::runtime_error("step output holds " + std::to_string(n)
+                                 + " records, more than the "
+                                 + std::to_string(out.capacity)
+                                 + " the destination arrays hold");
+    auto copy = [&](void* dst, void const* src, std::size_t per_hit) {
+        if (dst && src && n > 0)
+        {
+            GBX_CUDA(cudaMemcpyAsync(
+                dst, src, per_hit * n, cudaMemcpyDeviceToHost, stream_));
+        }
+    };
+    copy(out.step, h.step, 4);
+    copy(out.detector, h.detector, 4);
+    copy(out.track_id, h.track_id, 4);
+    copy(out.event_id, h.event_id, 4);
+    copy(out.parent_id, h.parent_id, 4);
+    copy(out.track_step_count, h.track_step_count, 4);
+    copy(out.particle, h.particle, 4);
+    copy(out.step_length, h.step_length, 8);
+    copy(out.energy_deposition, h.energy_deposition, 8);
+    copy(out.pre_time, h.pre_time, 8);
+    copy(out.pre_pos, h.pre_pos, 24);
+    copy(out.pre_dir, h.pre_dir, 24);
+    copy(out.pre_energy, h.pre_energy, 8);
+    copy(out.post_time, h.post_time, 8);
+    copy(out.post_pos, h.post_pos, 24);
+    copy(out.post_dir, h.post_dir, 24);
+    copy(out.post_energy, h.post_energy, 8);
+    GBX_CUDA(cudaMemsetAsync(
+        &ref_.counters->num_hits, 0, sizeof(size_type), stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return n;
 }
 
 void CoreState::insert_primaries(TrackInitializer const* host_primaries, size_type n)
@@ -877,6 +1032,14 @@ void Stepper::update_sort_policy()
     bool const sort = static_cast<long long>(last_active_) >= sort_threshold_;
     if (sort != state_->context().sort_enabled)
         state_->set_tuning("sort", sort);
+}
+
+void Stepper::set_step_output(unsigned int selection,
+                              bool nonzero_energy_deposition,
+                              size_type capacity)
+{
+    state_->set_step_output(selection, nonzero_energy_deposition, capacity);
+    this->clear_graphs();
 }
 
 void Stepper::set_tuning(std::string const& name, long long value)

@@ -226,6 +226,89 @@ __global__ __launch_bounds__(block_size) void calo_kernel(ParamsData p, StateDat
         warp_tally(s.event_edep, event, edep);
 }
 
+//---------------------------------------------------------------------------//
+// Step output: each step's hits appended in slot order (DetectorSteps)
+//---------------------------------------------------------------------------//
+//! Hits of each block of slots
+__global__ __launch_bounds__(block_size) void hits_count_kernel(StateData s,
+                                                                StepHitsRef h,
+                                                                size_type* block_hits)
+{
+    size_type const slot = thread_slot();
+    bool const hit = slot < s.size && has_step_hit(s, h, slot);
+    int const count = __syncthreads_count(hit);
+    if (threadIdx.x == 0)
+        block_hits[blockIdx.x] = static_cast<size_type>(count);
+}
+
+//! Record offsets of the blocks: the hits already held plus an exclusive
+//! scan of the block counts, by one block of 1024 threads. A step whose hits
+//! do not fit sets the overflow flag and records none.
+__global__ __launch_bounds__(1024) void hits_scan_kernel(StateData s,
+                                                         size_type* block_hits,
+                                                         size_type num_blocks,
+                                                         size_type capacity)
+{
+    __shared__ size_type sh[1024];
+    __shared__ size_type carry;
+    Counters& c = *s.counters;
+    if (threadIdx.x == 0)
+        carry = c.num_hits;
+    __syncthreads();
+    for (size_type base = 0; base < num_blocks; base += 1024)
+    {
+        size_type const i = base + threadIdx.x;
+        size_type const v = i < num_blocks ? block_hits[i] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1)
+        {
+            size_type const a = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += a;
+            __syncthreads();
+        }
+        if (i < num_blocks)
+            block_hits[i] = carry + sh[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023)
+            carry += sh[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        if (carry > capacity)
+            c.error_flags |= error_hit_overflow;
+        else if (!(c.error_flags & error_hit_overflow))
+            c.num_hits = carry;
+    }
+}
+
+//! Write each hit at its block offset plus its rank among the block's hits
+__global__ __launch_bounds__(block_size) void hits_scatter_kernel(
+    ParamsData p,
+    StateData s,
+    StepHitsRef h,
+    size_type const* block_offsets,
+    size_type const* step_index)
+{
+    __shared__ size_type warp_hits[block_size / 32];
+    size_type const slot = thread_slot();
+    bool const hit = slot < s.size && has_step_hit(s, h, slot);
+    unsigned int const ballot = __ballot_sync(0xffffffffu, hit);
+    int const lane = threadIdx.x & 31;
+    int const warp = threadIdx.x >> 5;
+    if (lane == 0)
+        warp_hits[warp] = __popc(ballot);
+    __syncthreads();
+    if (!hit || (s.counters->error_flags & error_hit_overflow))
+        return;
+    size_type index = block_offsets[blockIdx.x] + __popc(ballot & ((1u << lane) - 1u));
+    for (int w = 0; w < warp; ++w)
+        index += warp_hits[w];
+    write_step_hit(p, s, h, slot, index, *step_index);
+}
+
 //! Live tracks per event: occupied slots plus queued initializers
 __global__ void count_event_live_kernel(StateData s, size_type num_events)
 {
@@ -815,8 +898,17 @@ void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
 
 void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream)
 {
-    calo_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-        ctx.params, ctx.state);
+    unsigned int const nb = num_blocks_for(ctx.state.size);
+    calo_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state);
+    if (ctx.hits.enabled())
+    {
+        hits_count_kernel<<<nb, block_size, 0, stream>>>(
+            ctx.state, ctx.hits, ctx.hit_block_offsets);
+        hits_scan_kernel<<<1, 1024, 0, stream>>>(
+            ctx.state, ctx.hit_block_offsets, nb, ctx.hits.capacity);
+        hits_scatter_kernel<<<nb, block_size, 0, stream>>>(
+            ctx.params, ctx.state, ctx.hits, ctx.hit_block_offsets, ctx.step_index);
+    }
 }
 
 void launch_extend_from_secondaries(LaunchContext const& ctx, cudaStream_t stream)

@@ -47,6 +47,9 @@ enum ErrorFlag : size_type
 {
     error_initializer_overflow = 1u << 0,
     error_primary_overflow = 1u << 1,
+    //! A step's hits did not fit in the step output: that step's and later
+    //! steps' hits are dropped until the host reads the output
+    error_hit_overflow = 1u << 2,
 };
 
 constexpr int block_size = 256;
@@ -69,6 +72,9 @@ struct LaunchContext
     StepRecord* log;  //!< Step log (ring buffer)
     size_type log_capacity;
     size_type* step_index;  //!< Device-resident step counter
+    //! Step output (disabled: zero capacity) and its per-block hit counts
+    StepHitsRef hits;
+    size_type* hit_block_offsets;  //!< [num_blocks_for(size)]
 };
 
 // Individual action launchers (one thread per track slot)
@@ -87,6 +93,7 @@ void launch_interact(LaunchContext const& ctx,
                      cudaStream_t stream);
 void launch_boundary(LaunchContext const& ctx, cudaStream_t stream);
 void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream);
+//! SimpleCalo tally and, when enabled, the step output (step-gather-post)
 void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream);
 void launch_extend_from_secondaries(LaunchContext const& ctx,
                                     cudaStream_t stream);

@@ -760,7 +760,9 @@ GBX_FUNCTION void tracking_cut(ParamsData const& p,
 //---------------------------------------------------------------------------//
 // Step gathering and calorimeter tally
 //---------------------------------------------------------------------------//
-//! Record the detector of the pre-step volume (StepGatherExecutor<pre>)
+//! Record the detector of the pre-step volume and, when hits are collected,
+//! the pre-step point of a slot in a detector (StepGatherExecutor<pre>,
+//! src/celeritas/user/detail/StepGatherExecutor.hh:52-150)
 GBX_FUNCTION void gather_pre(ParamsData const& p, StateData const& s, size_type slot)
 {
     if (s.status[slot] == status_inactive)
@@ -769,7 +771,83 @@ GBX_FUNCTION void gather_pre(ParamsData const& p, StateData const& s, size_type 
         return;
     }
     size_type vol = s.volume[slot];
-    s.detector[slot] = p.geo.volume_detector[vol];
+    size_type const det = p.geo.volume_detector[vol];
+    s.detector[slot] = det;
+    if (det == invalid_id)
+        return;
+    if (s.pre_time)
+        s.pre_time[slot] = s.time[slot];
+    if (s.pre_pos)
+    {
+        for (int i = 0; i < 3; ++i)
+            s.pre_pos[3 * std::size_t(slot) + i] = s.pos[i][slot];
+    }
+    if (s.pre_dir)
+    {
+        for (int i = 0; i < 3; ++i)
+            s.pre_dir[3 * std::size_t(slot) + i] = s.dir[i][slot];
+    }
+    if (s.pre_energy)
+        s.pre_energy[slot] = double(s.energy[slot]);
+}
+
+//! Whether a slot's step is a hit: an active track that started the step in
+//! a detector volume and, with the filter, deposited energy
+//! (StepGatherExecutor<post>; DetectorSteps keeps the slots whose detector
+//! is still set, src/celeritas/user/DetectorSteps.cc)
+GBX_FUNCTION bool has_step_hit(StateData const& s, StepHitsRef const& h, size_type slot)
+{
+    if (s.status[slot] == status_inactive || s.detector[slot] == invalid_id)
+        return false;
+    return !(h.nonzero_energy_deposition && s.energy_deposition[slot] == 0);
+}
+
+//! Write a slot's hit as record 'i' of the step output: the selected
+//! post-step data gathered from the track now, the pre-step point gathered
+//! at pre-step; the particle as the reference's ParticleId
+GBX_FUNCTION void write_step_hit(ParamsData const& p,
+                                 StateData const& s,
+                                 StepHitsRef const& h,
+                                 size_type slot,
+                                 size_type i,
+                                 size_type step)
+{
+    std::size_t const i3 = 3 * std::size_t(i);
+    std::size_t const s3 = 3 * std::size_t(slot);
+    h.step[i] = step;
+    h.detector[i] = s.detector[slot];
+    h.track_id[i] = s.track_id[slot];
+    if (h.event_id)
+        h.event_id[i] = s.event_id[slot];
+    if (h.parent_id)
+        h.parent_id[i] = s.parent_id[slot];
+    if (h.track_step_count)
+        h.track_step_count[i] = s.num_steps[slot];
+    if (h.particle)
+        h.particle[i] = p.particles[s.particle_id[slot]].ref_id;
+    if (h.step_length)
+        h.step_length[i] = s.step_length[slot];
+    if (h.energy_deposition)
+        h.energy_deposition[i] = double(s.energy_deposition[slot]);
+    if (h.pre_time)
+        h.pre_time[i] = s.pre_time[slot];
+    if (h.pre_energy)
+        h.pre_energy[i] = s.pre_energy[slot];
+    for (int k = 0; k < 3; ++k)
+    {
+        if (h.pre_pos)
+            h.pre_pos[i3 + k] = s.pre_pos[s3 + k];
+        if (h.pre_dir)
+            h.pre_dir[i3 + k] = s.pre_dir[s3 + k];
+        if (h.post_pos)
+            h.post_pos[i3 + k] = s.pos[k][slot];
+        if (h.post_dir)
+            h.post_dir[i3 + k] = s.dir[k][slot];
+    }
+    if (h.post_time)
+        h.post_time[i] = s.time[slot];
+    if (h.post_energy)
+        h.post_energy[i] = double(s.energy[slot]);
 }
 
 }  // namespace gbx

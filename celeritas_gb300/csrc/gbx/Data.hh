@@ -104,6 +104,10 @@ struct ParticleRecord
     real_type charge;  //!< [e]
     int pdg;
     bool is_antiparticle;
+    //! The reference's ParticleId of this particle, which orders particles
+    //! by mass, then |PDG|, particles before antiparticles
+    //! (ParticleParams::from_import, src/celeritas/phys/ParticleParams.cc:57-71)
+    size_type ref_id;
 };
 
 struct ElementRecord
@@ -434,7 +438,67 @@ struct Counters
     size_type secondary_stack_size;  //!< Bump allocator top
     size_type num_pending_primaries;
     size_type error_flags;
-    size_type pad[7];
+    size_type num_hits;  //!< Step-output records held on the device
+    size_type pad[6];
+};
+
+//---------------------------------------------------------------------------//
+// Step output: detector hits (StepCollector / DetectorSteps)
+//---------------------------------------------------------------------------//
+//! Selected step data (StepSelection, src/celeritas/user/StepData.hh:19-117):
+//! the pre- and post-step points and the per-step attributes that
+//! DetectorStepOutput holds (src/celeritas/user/DetectorSteps.hh:49-80).
+//! The step index, detector and track ID are always recorded.
+enum StepSelect : unsigned int
+{
+    step_pre_time = 1u << 0,
+    step_pre_pos = 1u << 1,
+    step_pre_dir = 1u << 2,
+    step_pre_energy = 1u << 3,
+    step_post_time = 1u << 4,
+    step_post_pos = 1u << 5,
+    step_post_dir = 1u << 6,
+    step_post_energy = 1u << 7,
+    step_event_id = 1u << 8,
+    step_parent_id = 1u << 9,
+    step_track_step_count = 1u << 10,
+    step_step_length = 1u << 11,
+    step_particle = 1u << 12,
+    step_energy_deposition = 1u << 13,
+    step_select_all = (1u << 14) - 1,
+    step_pre_any = step_pre_time | step_pre_pos | step_pre_dir | step_pre_energy,
+};
+
+//! Hit records, one per step of a track in a detector volume: structure of
+//! arrays of 'capacity' entries, positions and directions three doubles per
+//! record. Arrays of unselected data are null.
+struct StepHitsRef
+{
+    size_type capacity{0};
+    unsigned int selection{0};
+    //! Drop steps that deposited no energy (StepParamsData::
+    //! nonzero_energy_deposition)
+    bool nonzero_energy_deposition{true};
+    size_type* step{nullptr};  //!< Step iteration of the stepper
+    size_type* detector{nullptr};
+    size_type* track_id{nullptr};
+    size_type* event_id{nullptr};
+    size_type* parent_id{nullptr};
+    size_type* track_step_count{nullptr};
+    size_type* particle{nullptr};
+    double* step_length{nullptr};
+    double* energy_deposition{nullptr};
+    double* pre_time{nullptr};
+    double* pre_pos{nullptr};
+    double* pre_dir{nullptr};
+    double* pre_energy{nullptr};
+    double* post_time{nullptr};
+    double* post_pos{nullptr};
+    double* post_dir{nullptr};
+    double* post_energy{nullptr};
+
+    //! Whether hits are collected
+    GBX_FORCEINLINE bool enabled() const { return capacity > 0; }
 };
 
 struct StateData
@@ -509,6 +573,13 @@ struct StateData
 
     // Step gather: detector ID at pre-step
     size_type* detector;
+    // Step output: pre-step point of slots in a detector volume, per slot
+    // (positions and directions three doubles per slot); null unless hits
+    // with that datum are collected
+    double* pre_time;
+    double* pre_pos;
+    double* pre_dir;
+    double* pre_energy;
     // Tally: energy deposition per detector (FP64 accumulation)
     double* calo_edep;
 

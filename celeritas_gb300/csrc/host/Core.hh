@@ -187,10 +187,27 @@ class CoreState
     std::vector<StepRecord> step_log(size_type first, size_type n) const;
     size_type log_capacity() const { return ctx_.log_capacity; }
 
+    //! Collect the hits of every step (StepCollector with DetectorSteps):
+    //! the selected data of each track step in a detector volume, dropping
+    //! steps without deposition if asked, into device buffers of 'capacity'
+    //! records that the host empties with read_step_output. Zero capacity
+    //! turns the output off. Allocates the buffers (outside the step loop).
+    void set_step_output(unsigned int selection,
+                         bool nonzero_energy_deposition,
+                         size_type capacity);
+    StepHitsRef const& step_output() const { return ctx_.hits; }
+    //! Copy the records held on the device into the arrays of 'out' (host
+    //! memory, null where not wanted; 'out.capacity' entries each), empty the
+    //! device buffers and return the number of records. Throws if the device
+    //! buffers overflowed since the last read (they are emptied) or if 'out'
+    //! is too small (they are kept).
+    size_type read_step_output(StepHitsRef const& out);
+
   private:
     StateData ref_{};
     LaunchContext ctx_{};
     void* storage_{nullptr};
+    void* hits_storage_{nullptr};
     TrackInitializer* pinned_primaries_{nullptr};
     size_type pinned_capacity_{0};
     size_type pending_primaries_{0};
@@ -291,6 +308,12 @@ class Stepper
     //! Energy deposition per detector [MeV] (synchronizes)
     std::vector<double> energy_deposition() const;
     void clear_energy_deposition();
+
+    //! Step output (see CoreState::set_step_output); drops the captured
+    //! step graphs, whose gather action gains or loses the hit kernels
+    void set_step_output(unsigned int selection,
+                         bool nonzero_energy_deposition,
+                         size_type capacity);
 
     //! Launch tuning (see CoreState::set_tuning) plus "sort_threshold": the
     //! action sorts run only in steps that start with at least this many

@@ -15,6 +15,7 @@
 #include "HostParams.hh"
 
 #include <algorithm>
+#include <tuple>
 #include <array>
 #include <cmath>
 #include <map>
@@ -335,6 +336,20 @@ void Builder::build_particles()
     if (s.electron_id != 0 || s.positron_id != 1 || s.gamma_id != 2)
         throw std::runtime_error("expected particles e-, e+, gamma in order");
     s.num_particles = static_cast<size_type>(npar);
+    // The reference's particle order: increasing mass, then |PDG|, then
+    // particles before antiparticles
+    std::vector<size_type> order(hp_.particles.size());
+    for (size_type i = 0; i < order.size(); ++i)
+        order[i] = i;
+    auto key = [this](size_type i) {
+        auto const& pr = hp_.particles[i];
+        return std::make_tuple(double(pr.mass), std::abs(pr.pdg), pr.pdg < 0);
+    };
+    std::sort(order.begin(), order.end(), [&key](size_type a, size_type b) {
+        return key(a) < key(b);
+    });
+    for (size_type r = 0; r < order.size(); ++r)
+        hp_.particles[order[r]].ref_id = r;
 }
 
 void Builder::build_materials()

@@ -66,6 +66,8 @@ struct HostState
     std::vector<Secondary> secondaries;
     std::vector<size_type> detector;
     std::vector<double> calo_edep;
+    // Step output: pre-step points (empty unless hits are collected)
+    std::vector<double> pre_time, pre_pos, pre_dir, pre_energy;
     std::vector<TrackInitializer> primaries;
     Counters counters{};
 
@@ -195,6 +197,13 @@ struct HostState
         s.secondary_capacity = static_cast<size_type>(secondaries.size());
         s.detector = detector.data();
         s.calo_edep = calo_edep.data();
+        auto data_or_null = [](std::vector<double>& v) {
+            return v.empty() ? nullptr : v.data();
+        };
+        s.pre_time = data_or_null(pre_time);
+        s.pre_pos = data_or_null(pre_pos);
+        s.pre_dir = data_or_null(pre_dir);
+        s.pre_energy = data_or_null(pre_energy);
         s.primaries = primaries.data();
         s.primary_capacity = static_cast<size_type>(primaries.size());
         s.counters = &counters;

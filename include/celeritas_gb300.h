@@ -238,6 +238,81 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
                                         size_t num_events,
                                         int clear);
 
+/* Step data recorded for each hit (StepSelection's fields,
+ * src/celeritas/user/StepData.hh:19-117, as DetectorStepOutput holds them,
+ * src/celeritas/user/DetectorSteps.hh:49-80). The step index, detector and
+ * track ID of a hit are always recorded. */
+enum
+{
+    GBX_STEP_PRE_TIME = 1u << 0,
+    GBX_STEP_PRE_POS = 1u << 1,
+    GBX_STEP_PRE_DIR = 1u << 2,
+    GBX_STEP_PRE_ENERGY = 1u << 3,
+    GBX_STEP_POST_TIME = 1u << 4,
+    GBX_STEP_POST_POS = 1u << 5,
+    GBX_STEP_POST_DIR = 1u << 6,
+    GBX_STEP_POST_ENERGY = 1u << 7,
+    GBX_STEP_EVENT_ID = 1u << 8,
+    GBX_STEP_PARENT_ID = 1u << 9,
+    GBX_STEP_TRACK_STEP_COUNT = 1u << 10,
+    GBX_STEP_STEP_LENGTH = 1u << 11,
+    GBX_STEP_PARTICLE = 1u << 12,
+    GBX_STEP_ENERGY_DEPOSITION = 1u << 13,
+    GBX_STEP_ALL = (1u << 14) - 1
+};
+
+/* Hit records in the caller's host memory: each non-null array holds
+ * 'capacity' entries (positions and directions three doubles per record).
+ * 'step' is the stepper's step iteration of the hit; 'particle' is the
+ * reference's ParticleId; energies in MeV, times in seconds, lengths in cm.
+ * The records of a step come in track-slot order, as copy_steps writes
+ * them (src/celeritas/user/DetectorSteps.cc). */
+typedef struct
+{
+    size_t capacity;
+    unsigned int* step;
+    unsigned int* detector;
+    unsigned int* track_id;
+    unsigned int* event_id;
+    unsigned int* parent_id;
+    unsigned int* track_step_count;
+    unsigned int* particle;
+    double* step_length;
+    double* energy_deposition;
+    double* pre_time;
+    double* pre_pos;
+    double* pre_dir;
+    double* pre_energy;
+    double* post_time;
+    double* post_pos;
+    double* post_dir;
+    double* post_energy;
+} gbx_step_hits;
+
+/* Collect the hits of every step: a StepCollector with one step interface
+ * over the detector volumes of the energy-deposition tally
+ * (src/celeritas/user/StepCollector.hh:33-80, StepInterface.hh:40-75), whose
+ * process_steps copies the hits out (copy_steps,
+ * src/celeritas/user/DetectorSteps.hh:83-90). 'selection' is a mask of
+ * GBX_STEP_* bits; nonzero 'nonzero_energy_deposition' drops steps without
+ * deposition (StepInterface::Filters). Hits accumulate on the device, up to
+ * 'capacity' records, between calls of gbx_stepper_read_step_output; zero
+ * capacity turns the output off. Allocates the device buffers here, never
+ * inside the step loop. */
+int gbx_stepper_set_step_output(gbx_stepper* stepper,
+                                unsigned int selection,
+                                int nonzero_energy_deposition,
+                                size_t capacity);
+
+/* Copy the hits held on the device into 'out' (synchronizes the stream),
+ * write their number to 'num_hits' and empty the device buffers. Fails if
+ * the device buffers overflowed since the last read (they are emptied; the
+ * steps' other results are unaffected) or if 'out->capacity' is below the
+ * number held (they are kept). */
+int gbx_stepper_read_step_output(gbx_stepper* stepper,
+                                 const gbx_step_hits* out,
+                                 size_t* num_hits);
+
 /* Launch tuning of a stepper, for an autotuner (no counterpart in the
  * reference, whose block sizes and sort policy are build and run options):
  *   "along_block_size"  threads per block of the charged along-step (64, 128, 256)

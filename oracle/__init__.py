@@ -67,9 +67,20 @@ def build_reference(reference: str = REFERENCE_DEFAULT, jobs: int = 8) -> str | 
     return REF_BIN
 
 
+#: Columns of a 'hit' line of the oracle programs (--hits): the step
+#: iteration, then DetectorStepOutput's fields (src/celeritas/user/
+#: DetectorSteps.hh:49-80) with positions and directions as three columns
+HIT_COLUMNS = ("step", "detector", "track_id", "event_id", "parent_id", "track_step_count",
+               "particle", "step_length", "energy_deposition",
+               "pre_time", "pre_x", "pre_y", "pre_z", "pre_u", "pre_v", "pre_w", "pre_energy",
+               "post_time", "post_x", "post_y", "post_z", "post_u", "post_v", "post_w",
+               "post_energy")
+HIT_INT_COLUMNS = 7
+
+
 def parse_run_output(text: str) -> dict:
-    """Parse 'step', 'total_steps', 'edep', 'action' lines of a run."""
-    steps, edep, actions = [], {}, {}
+    """Parse 'step', 'total_steps', 'edep', 'action' and 'hit' lines of a run."""
+    steps, edep, actions, hits = [], {}, {}, []
     total = iters = None
     seconds = None
     for line in text.splitlines():
@@ -86,8 +97,12 @@ def parse_run_output(text: str) -> dict:
             total, iters = int(tok[1]), int(tok[3])
         elif tok[0] == "seconds":
             seconds = float(tok[1])
+        elif tok[0] == "hit":
+            hits.append([int(t) for t in tok[1:1 + HIT_INT_COLUMNS]]
+                        + [float(t) for t in tok[1 + HIT_INT_COLUMNS:]])
     return {"steps": steps, "edep": edep, "actions": actions,
-            "total_steps": total, "iterations": iters, "seconds": seconds}
+            "total_steps": total, "iterations": iters, "seconds": seconds,
+            "hits": hits}
 
 
 def run_port(physics: str, primaries_txt: str, slots: int, seed: int = 0,

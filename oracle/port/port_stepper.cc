@@ -17,7 +17,7 @@
 //
 // Usage:
 //   port_stepper run <physics.txt> calo <primaries.txt> <slots> <seed>
-//                    [--steps N] [--quiet] [--threads T --events E]
+//                    [--steps N] [--quiet] [--threads T --events E] [--hits]
 #include <algorithm>
 #include <array>
 #include <chrono>
@@ -97,6 +97,45 @@ class PortStepper
 
     std::vector<double> const& edep() const { return state_.calo_edep; }
 
+    //! Print every step's hits (all step data, steps without deposition
+    //! dropped) as 'hit' lines
+    void enable_hits()
+    {
+        std::size_t const n = state_.size;
+        state_.pre_time.assign(n, 0);
+        state_.pre_pos.assign(3 * n, 0);
+        state_.pre_dir.assign(3 * n, 0);
+        state_.pre_energy.assign(n, 0);
+        for (auto* v : {&hb_.step, &hb_.detector, &hb_.track_id, &hb_.event_id,
+                        &hb_.parent_id, &hb_.track_step_count, &hb_.particle})
+            v->assign(n, 0);
+        for (auto* v : {&hb_.step_length, &hb_.energy_deposition, &hb_.pre_time,
+                        &hb_.pre_energy, &hb_.post_time, &hb_.post_energy})
+            v->assign(n, 0);
+        for (auto* v : {&hb_.pre_pos, &hb_.pre_dir, &hb_.post_pos, &hb_.post_dir})
+            v->assign(3 * n, 0);
+        hits_.capacity = state_.size;
+        hits_.selection = step_select_all;
+        hits_.nonzero_energy_deposition = true;
+        hits_.step = hb_.step.data();
+        hits_.detector = hb_.detector.data();
+        hits_.track_id = hb_.track_id.data();
+        hits_.event_id = hb_.event_id.data();
+        hits_.parent_id = hb_.parent_id.data();
+        hits_.track_step_count = hb_.track_step_count.data();
+        hits_.particle = hb_.particle.data();
+        hits_.step_length = hb_.step_length.data();
+        hits_.energy_deposition = hb_.energy_deposition.data();
+        hits_.pre_time = hb_.pre_time.data();
+        hits_.pre_pos = hb_.pre_pos.data();
+        hits_.pre_dir = hb_.pre_dir.data();
+        hits_.pre_energy = hb_.pre_energy.data();
+        hits_.post_time = hb_.post_time.data();
+        hits_.post_pos = hb_.post_pos.data();
+        hits_.post_dir = hb_.post_dir.data();
+        hits_.post_energy = hb_.post_energy.data();
+    }
+
     //! Print the state of every non-inactive slot
     void trace(size_type iter) const
     {
@@ -133,6 +172,35 @@ class PortStepper
     HostState state_;
     std::vector<std::string> action_labels_;
     unsigned int seed_;
+    unsigned int iteration_{0};
+    struct HitBuffers
+    {
+        std::vector<size_type> step, detector, track_id, event_id, parent_id,
+            track_step_count, particle;
+        std::vector<double> step_length, energy_deposition, pre_time, pre_pos,
+            pre_dir, pre_energy, post_time, post_pos, post_dir, post_energy;
+    } hb_;
+    StepHitsRef hits_;
+
+    void print_hits(size_type count) const
+    {
+        StepHitsRef const& h = hits_;
+        for (size_type i = 0; i < count; ++i)
+        {
+            std::printf(
+                "hit %u %u %u %u %u %u %u %.17g %.17g %.17g %.17g %.17g %.17g "
+                "%.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g "
+                "%.17g %.17g\n",
+                h.step[i], h.detector[i], h.track_id[i], h.event_id[i],
+                h.parent_id[i], h.track_step_count[i], h.particle[i],
+                h.step_length[i], h.energy_deposition[i], h.pre_time[i],
+                h.pre_pos[3 * i], h.pre_pos[3 * i + 1], h.pre_pos[3 * i + 2],
+                h.pre_dir[3 * i], h.pre_dir[3 * i + 1], h.pre_dir[3 * i + 2],
+                h.pre_energy[i], h.post_time[i], h.post_pos[3 * i],
+                h.post_pos[3 * i + 1], h.post_pos[3 * i + 2], h.post_dir[3 * i],
+                h.post_dir[3 * i + 1], h.post_dir[3 * i + 2], h.post_energy[i]);
+        }
+    }
 
     StepCounts step(bool with_primaries)
     {
@@ -197,6 +265,18 @@ class PortStepper
             if (det != invalid_id)
                 s.calo_edep[det] += s.energy_deposition[i];
         }
+        // ... and the step output: hits in slot order (DetectorSteps)
+        if (hits_.enabled())
+        {
+            size_type count = 0;
+            for (size_type i = 0; i < n; ++i)
+            {
+                if (has_step_hit(s, hits_, i))
+                    write_step_hit(p, s, hits_, i, count++, iteration_);
+            }
+            this->print_hits(count);
+        }
+        ++iteration_;
         // extend-from-secondaries (end)
         {
             std::vector<char> vacant(n);
@@ -308,6 +388,7 @@ int run(int argc, char** argv)
     bool trace = false;
     long long reseed = -1;
     size_type dump_rng = 0;
+    bool hits = false;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -321,6 +402,8 @@ int run(int argc, char** argv)
             reseed = std::stoll(argv[++i]);
         else if (a == "--dump-rng")
             dump_rng = std::stoul(argv[++i]);
+        else if (a == "--hits")
+            hits = true;
     }
     HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
@@ -337,6 +420,8 @@ int run(int argc, char** argv)
     PortStepper step(hp, slots, seed, max_event + 1);
     if (reseed >= 0)
         step.reseed(static_cast<unsigned long long>(reseed));
+    if (hits)
+        step.enable_hits();
     for (size_type i = 0; i < std::min(dump_rng, slots); ++i)
     {
         auto w = step.rng_words(i);

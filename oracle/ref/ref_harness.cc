@@ -66,8 +66,10 @@
 #include "celeritas/random/RngParams.hh"
 #include "celeritas/track/SimParams.hh"
 #include "celeritas/track/TrackInitParams.hh"
+#include "celeritas/user/DetectorSteps.hh"
 #include "celeritas/user/SimpleCalo.hh"
 #include "celeritas/user/StepCollector.hh"
+#include "celeritas/user/StepInterface.hh"
 
 using namespace celeritas;
 
@@ -526,10 +528,84 @@ GeoSpec build_geometry(std::string const& name)
 //---------------------------------------------------------------------------//
 // Problem construction (mirrors Runner::build_core_params)
 //---------------------------------------------------------------------------//
+//---------------------------------------------------------------------------//
+// Hit printer: a step interface over SimpleCalo's detector volumes (same
+// volume -> detector map, steps without deposition dropped) that gathers
+// every step datum, copies each step's hits with the reference's own
+// copy_steps and prints them; it also sums the deposition per detector so
+// that the run still prints its 'edep' lines
+//---------------------------------------------------------------------------//
+class HitPrinter final : public StepInterface
+{
+  public:
+    HitPrinter(Filters filters, size_type num_detectors)
+        : filters_(std::move(filters)), edep_(num_detectors, 0.0)
+    {
+    }
+
+    Filters filters() const final { return filters_; }
+    StepSelection selection() const final { return StepSelection::all(); }
+
+    void process_steps(HostStepState state) final
+    {
+        DetectorStepOutput out;
+        copy_steps<MemSpace::host>(&out, state.steps);
+        auto const& pre = out.points[StepPoint::pre];
+        auto const& post = out.points[StepPoint::post];
+        for (size_type i = 0; i < out.size(); ++i)
+        {
+            std::printf(
+                "hit %u %u %u %u %u %u %u %.17g %.17g %.17g %.17g %.17g %.17g "
+                "%.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g "
+                "%.17g %.17g\n",
+                step_,
+                out.detector[i].unchecked_get(),
+                out.track_id[i].unchecked_get(),
+                out.event_id[i].unchecked_get(),
+                out.parent_id[i].unchecked_get(),
+                out.track_step_count[i],
+                out.particle[i].unchecked_get(),
+                out.step_length[i],
+                out.energy_deposition[i].value(),
+                pre.time[i],
+                pre.pos[i][0],
+                pre.pos[i][1],
+                pre.pos[i][2],
+                pre.dir[i][0],
+                pre.dir[i][1],
+                pre.dir[i][2],
+                pre.energy[i].value(),
+                post.time[i],
+                post.pos[i][0],
+                post.pos[i][1],
+                post.pos[i][2],
+                post.dir[i][0],
+                post.dir[i][1],
+                post.dir[i][2],
+                post.energy[i].value());
+            edep_[out.detector[i].unchecked_get()]
+                += out.energy_deposition[i].value();
+        }
+        ++step_;
+    }
+    void process_steps(DeviceStepState) final
+    {
+        throw std::runtime_error("host-only hit printer");
+    }
+
+    std::vector<double> const& edep() const { return edep_; }
+
+  private:
+    Filters filters_;
+    std::vector<double> edep_;
+    unsigned int step_{0};
+};
+
 struct Problem
 {
     std::shared_ptr<CoreParams> core;
     std::shared_ptr<SimpleCalo> calo;
+    std::shared_ptr<HitPrinter> hits;
     std::shared_ptr<StepCollector> collector;
     GeoSpec geo;
 };
@@ -539,7 +615,8 @@ Problem build_problem(ImportData const& imported,
                       unsigned int seed,
                       Real3 field,
                       bool msc,
-                      TrackOrder track_order)
+                      TrackOrder track_order,
+                      bool print_hits)
 {
     Problem prob;
     prob.geo = build_geometry(geo_name);
@@ -643,6 +720,14 @@ Problem build_problem(ImportData const& imported,
         prob.calo = std::make_shared<SimpleCalo>(
             std::move(labels), *prob.core->geometry(), 1);
         StepCollector::VecInterface ifaces{prob.calo};
+        if (print_hits)
+        {
+            // The printer takes the calorimeter's volumes (one step
+            // interface per volume): same registered actions
+            prob.hits = std::make_shared<HitPrinter>(prob.calo->filters(),
+                                                     prob.calo->num_detectors());
+            ifaces = {prob.hits};
+        }
         prob.collector = std::make_shared<StepCollector>(
             prob.core->geometry(),
             std::move(ifaces),
@@ -722,7 +807,7 @@ int run(int argc, char** argv)
     {
         std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
                      "<seed> [--field Bx By Bz] [--msc] [--steps N] "
-                     "[--track-order N] [--reseed EVENT] [--dump-rng N]\n";
+                     "[--track-order N] [--reseed EVENT] [--dump-rng N] [--hits]\n";
         return 2;
     }
     std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
@@ -735,6 +820,7 @@ int run(int argc, char** argv)
     bool trace = false;
     long long reseed = -1;
     size_type dump_rng = 0;
+    bool print_hits = false;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -757,12 +843,14 @@ int run(int argc, char** argv)
             reseed = std::stoull(argv[++i]);
         else if (a == "--dump-rng")
             dump_rng = std::stoul(argv[++i]);
+        else if (a == "--hits")
+            print_hits = true;
     }
 
     KvFile kv(phys_path);
     ImportData imported = load_import(kv, msc);
     Problem prob
-        = build_problem(imported, geo_name, seed, field, msc, track_order);
+        = build_problem(imported, geo_name, seed, field, msc, track_order, print_hits);
     auto primaries = load_primaries(prim_path, *prob.core->particle());
 
     StepperInput sinp;
@@ -824,7 +912,8 @@ int run(int argc, char** argv)
                     counts.alive);
     }
     std::printf("total_steps %llu iterations %u\n", track_steps, iter + 1);
-    auto edep = prob.calo->calc_total_energy_deposition();
+    auto edep = prob.hits ? prob.hits->edep()
+                          : prob.calo->calc_total_energy_deposition();
     for (std::size_t i = 0; i < edep.size(); ++i)
     {
         std::printf("edep %s %.17g\n", prob.geo.vol_labels[i].c_str(), edep[i]);

@@ -4,8 +4,10 @@ Runs the reference's own host stepping loop (oracle/ref, compiled from the
 reference sources) on the committed synthetic physics input and records,
 per case: the ordered action labels, the per-step StepperResult counters
 (generated, queued, active, alive), the total track-steps and the energy
-deposition per calorimeter volume. Also records the ORANGE surface data of
-the calorimeter geometry.
+deposition per calorimeter volume; for the hit cases, the reference's
+DetectorStepOutput of every step (the first records in full, per-step counts
+and column sums). Also records the ORANGE surface data of the calorimeter
+geometry and reseeded XORWOW states.
 
 Usage (where the reference sources are present):
     python tests/golden/make_golden.py [--reference /path/to/reference]
@@ -68,6 +70,18 @@ CASES = {
                                       msc=True, reseed=7),
 }
 
+# Step output (detector hits of every step, StepCollector/DetectorSteps):
+# the first HIT_RECORDS records in full, and per step the number of hits and
+# the sum of every column
+HIT_CASES = {
+    "hits_calo_msc_field_e300_n1": dict(pdg=11, energy=300.0, num=1, slots=1024, seed=4,
+                                        msc=True, field=[1.0, 0.0, 0.0]),
+    "hits_cms_mix_e2000_n2": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=2000.0,
+                                  num=2, slots=4096, seed=6, beam_seed=5, msc=True,
+                                  field=[0.0, 0.0, 3.8]),
+}
+HIT_RECORDS = 150
+
 # Reseeded XORWOW states: seed, track slots, events, and the slots recorded
 RNG_SEED = 5
 RNG_SLOTS = 4096
@@ -100,8 +114,8 @@ def case_options(c: dict) -> list[str]:
     return opts
 
 
-def make_case(name: str) -> dict:
-    c = CASES[name]
+def make_case(name: str, hits: bool = False) -> dict:
+    c = (HIT_CASES if hits else CASES)[name]
     geometry = c.get("geometry", "calo")
     case = {"geometry": geometry, "energy": c["energy"],
             "num_primaries": c["num"], "num_track_slots": c["slots"],
@@ -120,7 +134,24 @@ def make_case(name: str) -> dict:
         ptxt = os.path.join(tmp, "primaries.txt")
         write_primaries_text(ptxt, prim)
         out = oracle.run_reference(physics_file(geometry), ptxt, c["slots"], c["seed"],
-                                   extra=case_options(c), geometry=geometry)
+                                   extra=case_options(c) + (["--hits"] if hits else []),
+                                   geometry=geometry)
+    if hits:
+        per_step = {}
+        for h in out["hits"]:
+            row = per_step.setdefault(h[0], [h[0], 0] + [0] * (len(h) - 1))
+            row[1] += 1
+            for k, v in enumerate(h[1:]):
+                row[2 + k] += v
+        return {
+            "case": case,
+            "columns": list(oracle.HIT_COLUMNS),
+            "steps": out["steps"],
+            "edep": out["edep"],
+            "num_hits": len(out["hits"]),
+            "records": out["hits"][:HIT_RECORDS],
+            "per_step": [per_step[k] for k in sorted(per_step)],
+        }
     return {
         "case": case,
         "actions": [out["actions"][i] for i in sorted(out["actions"])],
@@ -171,6 +202,7 @@ def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--reference", default=oracle.REFERENCE_DEFAULT)
     parser.add_argument("--cases", nargs="*", default=list(CASES))
+    parser.add_argument("--hit-cases", nargs="*", default=list(HIT_CASES))
     args = parser.parse_args()
     if oracle.build_reference(args.reference) is None:
         sys.exit("reference sources not found")
@@ -179,6 +211,11 @@ def main():
         with open(os.path.join(HERE, f"{name}.json"), "w") as f:
             json.dump(data, f, indent=0)
         print(name, data["iterations"], data["total_steps"])
+    for name in args.hit_cases:
+        data = make_case(name, hits=True)
+        with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+            json.dump(data, f, indent=0)
+        print(name, data["num_hits"], "hits")
     with open(os.path.join(HERE, "calo_geometry.json"), "w") as f:
         json.dump(geometry_dump(), f, indent=0)
     with open(os.path.join(HERE, "xorwow_reseed.json"), "w") as f:

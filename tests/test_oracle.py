@@ -153,3 +153,38 @@ def test_port_reseed_matches_reference(built_port):
                 if tok and tok[0] == "rng":
                     words[int(tok[1])] = [int(t) for t in tok[2:8]]
             assert [words[i] for i in golden["slots"]] == expected, ev
+
+
+HIT_CASES = ["hits_calo_msc_field_e300_n1", "hits_cms_mix_e2000_n2"]
+
+
+def hit_summary(hits):
+    """Per-step hit count and column sums, as the golden fixtures hold them."""
+    per_step = {}
+    for h in hits:
+        row = per_step.setdefault(h[0], [h[0], 0] + [0] * (len(h) - 1))
+        row[1] += 1
+        for k, v in enumerate(h[1:]):
+            row[2 + k] += v
+    return [per_step[k] for k in sorted(per_step)]
+
+
+@pytest.mark.parametrize("name", HIT_CASES)
+def test_port_hits_match_reference(built_port, name):
+    """Step output: every step's detector hits (the reference's
+    DetectorStepOutput via its own copy_steps) are reproduced bit for bit,
+    in the same order, by the restatement's has_step_hit/write_step_hit."""
+    golden = load_golden(name)
+    c = golden["case"]
+    geometry = c.get("geometry", "calo")
+    prim = case_primaries(c)
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "p.txt")
+        write_primaries_text(ptxt, prim)
+        out = oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
+                              geometry=geometry, extra=case_options(c) + ["--hits"])
+    assert [list(s) for s in out["steps"]] == golden["steps"]
+    assert len(out["hits"]) == golden["num_hits"]
+    assert out["hits"][:len(golden["records"])] == golden["records"]
+    assert hit_summary(out["hits"]) == golden["per_step"]
+    assert out["edep"] == golden["edep"]
