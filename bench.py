@@ -386,6 +386,80 @@ def tune_workload(wl, precision, rank):
     return best, report
 
 
+def measure_step_output(args, wl, rank, batch=8):
+    """Cost of the step output (every detector hit with all step data) on the
+    mixed path. A transport without the output and one that reads the hits
+    back every 'batch' steps into the stepper's host buffers are timed by the
+    host clock; the step-gather-post action (tally plus the hit kernels) is
+    timed per launch with CUDA events, with and without the output."""
+    import torch
+
+    import celeritas_gb300 as gb
+    from celeritas_gb300 import sharding
+
+    gb.load_library(precision="mixed")
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                       field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
+                       precision="mixed",
+                       reentrant_looping=wl.get("reentrant_looping", False))
+    labels = params.action_labels()
+    gather = labels.index("step-gather-post")
+    st = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
+    prim = sharding.rank_primaries(wl, rank, num=wl.get("bench_primaries"))
+    capacity = (batch + 1) * wl["slots"]  # every slot hitting in every step
+
+    def transport(read):
+        hits = 0
+        res = [st.step(prim)]
+        while res[-1].alive or res[-1].queued:
+            res += st.run(max_steps=batch, batch=batch)
+            if read:
+                hits += len(st.read_step_output(copy=False)["step"])
+        if read:
+            hits += len(st.read_step_output(copy=False)["step"])
+        return sum(r.active for r in res), hits
+
+    def timed(read):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        steps, hits = transport(read)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, steps, hits
+
+    def gather_ms(read):
+        st.set_action_times(True)
+        transport(read)
+        ms, launches = st.action_times()
+        st.set_action_times(False)
+        return float(ms[gather] / max(launches[gather], 1))
+
+    transport(read=False)  # warm-up
+    off_s, steps, _ = timed(read=False)
+    off_gather = gather_ms(read=False)
+    st.set_step_output("all", True, capacity=capacity)
+    transport(read=True)  # warm-up: graph capture with the hit kernels
+    on_s, steps_on, hits = timed(read=True)
+    on_gather = gather_ms(read=True)
+    bytes_per_hit = 4 * 7 + 8 * 16  # 7 integers, 16 doubles
+    out = {
+        "read_every_steps": batch, "selection": "all", "nonzero_energy_deposition": True,
+        "track_steps_per_transport": int(steps_on),
+        "hits_per_transport": int(hits),
+        "bytes_per_hit": bytes_per_hit,
+        "transport_s_without": off_s,
+        "transport_s_with_reads": on_s,
+        "hits_per_s": hits / on_s,
+        "hit_bytes_per_s": hits * bytes_per_hit / on_s,
+        "gather_post_ms_without": off_gather,
+        "gather_post_ms_with": on_gather,
+        "timing": "host clock around each transport (synchronized); gather-post per "
+                  "launch from CUDA events of an eager transport",
+    }
+    st.set_step_output(capacity=0)
+    del st, params
+    return out
+
+
 def compare_tallies(mixed, fp64):
     """Per-layer energy deposition of the mixed build against FP64, with
     errors from the scatter of the independent timed transports."""
@@ -508,6 +582,8 @@ def run_gb300(args, wl):
             line["served"] = served
             line["served_events_per_s_vs_fp64_plain"] = (served["events_per_s"]
                                                          / pl["events_per_s"])
+    if args.step_output:
+        line["step_output"] = measure_step_output(args, wl, rank)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
@@ -785,6 +861,8 @@ def main():
                         help="events streamed through the server (c3: 195)")
     parser.add_argument("--sequential-sample", type=int, default=40,
                         help="c5: requests timed alone on the plain FP64 path")
+    parser.add_argument("--step-output", action="store_true",
+                        help="also time the step output (detector hits) on the mixed path")
     parser.add_argument("--no-tune", action="store_true",
                         help="skip the autotuner where the workload uses it (c3)")
     parser.add_argument("--plain", action="store_true",

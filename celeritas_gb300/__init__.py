@@ -364,9 +364,11 @@ class Stepper:
                     self._hit_bufs[n] = np.zeros(shape, dtype=dtype)
         self._hit_capacity = int(capacity)
 
-    def read_step_output(self) -> dict:
-        """Hits recorded since the last read, as numpy arrays (copies) keyed
-        by field; positions and directions have shape (n, 3)."""
+    def read_step_output(self, copy: bool = True) -> dict:
+        """Hits recorded since the last read, as numpy arrays keyed by field;
+        positions and directions have shape (n, 3). With ``copy=False`` the
+        arrays are views of the stepper's host buffers, valid until the next
+        read."""
         bufs = getattr(self, "_hit_bufs", None)
         if not bufs:
             raise GbxError("step output is not enabled")
@@ -378,7 +380,8 @@ class Stepper:
         count = ctypes.c_size_t()
         _check(self._lib, self._lib.gbx_stepper_read_step_output(
             self._handle, ctypes.byref(hits), ctypes.byref(count)))
-        return {n: arr[:count.value].copy() for n, arr in bufs.items()}
+        n = count.value
+        return {k: (arr[:n].copy() if copy else arr[:n]) for k, arr in bufs.items()}
 
     def get_tuning(self, name: str) -> int:
         v = ctypes.c_longlong()
