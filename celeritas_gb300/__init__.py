@@ -69,6 +69,18 @@ class _StepHits(ctypes.Structure):
                 + [(n, ctypes.POINTER(ctypes.c_double)) for n in _HIT_DOUBLE])
 
 
+#: Primary generator distributions (GBX_DIST_*, DistributionSelection)
+DISTRIBUTIONS = {"delta": 0, "isotropic": 1, "box": 2}
+
+
+class _GeneratorOptions(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint), ("pdg", ctypes.c_int * 8), ("num_pdg", ctypes.c_uint),
+                ("num_events", ctypes.c_uint), ("primaries_per_event", ctypes.c_uint),
+                ("energy_distribution", ctypes.c_int), ("energy", ctypes.c_double * 1),
+                ("position_distribution", ctypes.c_int), ("position", ctypes.c_double * 6),
+                ("direction_distribution", ctypes.c_int), ("direction", ctypes.c_double * 3)]
+
+
 class _StepResult(ctypes.Structure):
     _fields_ = [
         ("generated", ctypes.c_uint),
@@ -136,6 +148,8 @@ _PROTOTYPES = [
     ("gbx_stepper_reseed", ctypes.c_int, [ctypes.c_void_p, ctypes.c_ulonglong]),
     ("gbx_stepper_set_tuning", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_longlong]),
+    ("gbx_stepper_generate_primaries", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(_GeneratorOptions), ctypes.c_uint]),
     ("gbx_stepper_set_step_output", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_size_t]),
     ("gbx_stepper_read_step_output", ctypes.c_int,
@@ -332,6 +346,34 @@ class Stepper:
         for name, value in settings.items():
             _check(self._lib, self._lib.gbx_stepper_set_tuning(
                 self._handle, name.encode(), int(value)))
+
+    def generate_primaries(self, pdg, energy, position=("delta", (0.0, 0.0, 0.0)),
+                           direction=("isotropic", ()), num_events: int = 1,
+                           primaries_per_event: int = 1, first_event: int = 0,
+                           seed: int = 0):
+        """Sample primaries on the device for the next step()
+        (PrimaryGenerator with PrimaryGeneratorOptions): ``pdg`` codes cycled
+        over each event's primaries, ``energy`` a delta in MeV (a number or
+        ("delta", (E,))), ``position`` ("delta", (x, y, z)) or ("box", lo +
+        hi) in cm, ``direction`` ("delta", (u, v, w)) or ("isotropic", ())."""
+        o = _GeneratorOptions()
+        pdgs = [int(p) for p in (pdg if hasattr(pdg, "__len__") else [pdg])]
+        o.seed = int(seed)
+        o.num_pdg = len(pdgs)
+        for i, p in enumerate(pdgs[:8]):
+            o.pdg[i] = p
+        o.num_events = int(num_events)
+        o.primaries_per_event = int(primaries_per_event)
+        if not isinstance(energy, tuple):
+            energy = ("delta", (float(energy),))
+        for prefix, (kind, params), size in (("energy", energy, 1), ("position", position, 6),
+                                             ("direction", direction, 3)):
+            setattr(o, prefix + "_distribution", DISTRIBUTIONS.get(kind, -1))
+            arr = getattr(o, prefix)
+            for i, v in enumerate(list(params)[:size]):
+                arr[i] = float(v)
+        _check(self._lib, self._lib.gbx_stepper_generate_primaries(
+            self._handle, ctypes.byref(o), int(first_event)))
 
     def set_step_output(self, selection="all", nonzero_energy_deposition: bool = True,
                         capacity: int = 1 << 20):

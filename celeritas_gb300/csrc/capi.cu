@@ -158,6 +158,8 @@ FieldRef find_field(gbx::CoreState& st, std::string const& name)
                         2 * std::size_t(st.context().sort.num_bins + 1)};
     if (name == "counters")
         return FieldRef{s.counters, sizeof(Counters), 1};
+    if (name == "primaries")
+        return FieldRef{s.primaries, sizeof(TrackInitializer), s.primary_capacity};
     if (name == "initializers")
         return FieldRef{s.initializers, sizeof(TrackInitializer), s.initializer_capacity};
     if (name == "secondaries")
@@ -370,6 +372,75 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
         std::copy(v.begin(), v.end(), out);
     });
 }
+
+int gbx_stepper_generate_primaries(gbx_stepper* stepper,
+                                   const gbx_primary_generator_options* options,
+                                   unsigned int first_event)
+{
+    return guarded([&] {
+        if (!stepper || !options)
+            throw std::runtime_error("null argument");
+        gbx_primary_generator_options const& o = *options;
+        if (o.num_pdg == 0 || o.num_pdg > 8)
+            throw std::runtime_error("primary generator needs 1 to 8 PDG codes");
+        if (o.num_events == 0 || o.primaries_per_event == 0)
+            throw std::runtime_error("primary generator needs events and primaries");
+        // The reference's samplers (make_*_sampler,
+        // src/celeritas/phys/PrimaryGeneratorOptions.cc)
+        auto invalid = [](char const* dist, char const* sampler) {
+            return std::runtime_error(std::string("invalid distribution type '") + dist
+                                      + "' for " + sampler);
+        };
+        auto name = [](int d) {
+            return d == GBX_DIST_DELTA       ? "delta"
+                   : d == GBX_DIST_ISOTROPIC ? "isotropic"
+                   : d == GBX_DIST_BOX       ? "box"
+                                             : "unknown";
+        };
+        if (o.energy_distribution != GBX_DIST_DELTA)
+            throw invalid(name(o.energy_distribution), "energy");
+        if (o.position_distribution != GBX_DIST_DELTA
+            && o.position_distribution != GBX_DIST_BOX)
+            throw invalid(name(o.position_distribution), "position");
+        if (o.direction_distribution != GBX_DIST_DELTA
+            && o.direction_distribution != GBX_DIST_ISOTROPIC)
+            throw invalid(name(o.direction_distribution), "direction");
+        if (!(o.energy[0] > 0))
+            throw std::runtime_error("primary energy must be positive");
+
+        gbx::PrimaryGeneratorData g{};
+        g.seed = o.seed;
+        g.num_particles = o.num_pdg;
+        auto const& particles = stepper->stepper->params().host().particles;
+        for (unsigned int i = 0; i < o.num_pdg; ++i)
+        {
+            g.particle_ids[i] = gbx::invalid_id;
+            for (gbx::size_type p = 0; p < particles.size(); ++p)
+            {
+                if (particles[p].pdg == o.pdg[i])
+                    g.particle_ids[i] = p;
+            }
+            if (g.particle_ids[i] == gbx::invalid_id)
+                throw std::runtime_error("no particle with PDG code "
+                                         + std::to_string(o.pdg[i]));
+        }
+        g.primaries_per_event = o.primaries_per_event;
+        g.first_event = first_event;
+        g.num_events = o.num_events;
+        g.energy_dist = o.energy_distribution;
+        g.energy = o.energy[0];
+        g.position_dist = o.position_distribution;
+        for (int i = 0; i < 6; ++i)
+            g.position[i] = o.position[i];
+        g.direction_dist = o.direction_distribution;
+        for (int i = 0; i < 3; ++i)
+            g.direction[i] = o.direction[i];
+        stepper->stepper->state().generate_primaries(g);
+    });
+}
+
+static_assert(GBX_DIST_BOX == gbx::dist_box && GBX_DIST_ISOTROPIC == gbx::dist_isotropic,
+              "distribution values differ");
 
 int gbx_stepper_set_step_output(gbx_stepper* stepper,
                                 unsigned int selection,

@@ -721,6 +721,33 @@ size_type CoreState::read_step_output(StepHitsRef const& out)
     return n;
 }
 
+void CoreState::generate_primaries(PrimaryGeneratorData gen)
+{
+    if (pending_primaries_ != 0)
+        throw std::runtime_error("multiple consecutive primary insertions");
+    std::size_t const n = std::size_t(gen.num_events) * gen.primaries_per_event;
+    if (n == 0)
+        return;
+    if (n > pinned_capacity_)
+        throw std::runtime_error("too many primaries for one insertion");
+    if (std::size_t(gen.first_event) + gen.num_events > ref_.max_events)
+        throw std::runtime_error("generated event IDs exceed the stepper's event capacity "
+                                 + std::to_string(ref_.max_events));
+    for (size_type e = 0; e < gen.num_events; ++e)
+    {
+        if (primaries_per_event_.count(gen.first_event + e))
+            throw std::runtime_error("event " + std::to_string(gen.first_event + e)
+                                     + " already has primaries");
+    }
+    for (size_type e = 0; e < gen.num_events; ++e)
+        primaries_per_event_[gen.first_event + e] = gen.primaries_per_event;
+    gen.stepper_seed = seed_;
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    launch_generate_primaries(ctx_, gen, stream_);
+    GBX_CUDA(cudaGetLastError());
+    pending_primaries_ = static_cast<size_type>(n);
+}
+
 void CoreState::insert_primaries(TrackInitializer const* host_primaries, size_type n)
 {
     if (pending_primaries_ != 0)

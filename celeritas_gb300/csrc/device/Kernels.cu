@@ -122,6 +122,14 @@ __global__ void process_primaries_kernel(StateData s, size_type num_primaries)
     }
 }
 
+__global__ __launch_bounds__(block_size) void generate_primaries_kernel(
+    PrimaryGeneratorData g, StateData s, size_type num)
+{
+    size_type const tid = thread_slot();
+    if (tid < num)
+        generate_primary(g, s.primaries, tid);
+}
+
 __global__ __launch_bounds__(block_size) void initialize_tracks_kernel(
     ParamsData p, StateData s)
 {
@@ -788,6 +796,15 @@ void launch_process_primaries(LaunchContext const& ctx,
     size_type n = max_of(num_primaries, ctx.state.size);
     process_primaries_kernel<<<num_blocks_for(n), block_size, 0, stream>>>(
         ctx.state, num_primaries);
+}
+
+void launch_generate_primaries(LaunchContext const& ctx,
+                               PrimaryGeneratorData const& gen,
+                               cudaStream_t stream)
+{
+    size_type const n = gen.num_events * gen.primaries_per_event;
+    generate_primaries_kernel<<<num_blocks_for(n), block_size, 0, stream>>>(
+        gen, ctx.state, n);
 }
 
 void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream)

@@ -82,6 +82,11 @@ void launch_process_primaries(LaunchContext const& ctx,
                               size_type num_primaries,
                               cudaStream_t stream);
 void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream);
+//! Sample num_events x primaries_per_event primaries into the staged
+//! primaries (PrimaryGenerator on the device)
+void launch_generate_primaries(LaunchContext const& ctx,
+                               PrimaryGeneratorData const& gen,
+                               cudaStream_t stream);
 void launch_pre_step(LaunchContext const& ctx, cudaStream_t stream);
 //! Along-step for tracks whose along-step action matches (all if invalid)
 void launch_along_step(LaunchContext const& ctx,

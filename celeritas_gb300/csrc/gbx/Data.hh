@@ -469,6 +469,38 @@ enum StepSelect : unsigned int
     step_pre_any = step_pre_time | step_pre_pos | step_pre_dir | step_pre_energy,
 };
 
+//---------------------------------------------------------------------------//
+// Primary generation (PrimaryGenerator, src/celeritas/phys/PrimaryGenerator.cc)
+//---------------------------------------------------------------------------//
+//! Distribution types (DistributionSelection,
+//! src/celeritas/phys/PrimaryGeneratorOptions.hh:21-27)
+enum PrimaryDistribution : int
+{
+    dist_delta = 0,
+    dist_isotropic = 1,
+    dist_box = 2,
+};
+
+//! Generator options (PrimaryGeneratorOptions) for one launch: events
+//! [first_event, first_event + num_events) of 'primaries_per_event'
+//! primaries each, particles cycling through 'particle_ids'
+struct PrimaryGeneratorData
+{
+    unsigned int seed;
+    unsigned int stepper_seed;  //!< Seed of the per-track stream keys
+    size_type num_particles;
+    size_type particle_ids[8];
+    size_type primaries_per_event;
+    size_type first_event;
+    size_type num_events;
+    int energy_dist;
+    double energy;
+    int position_dist;
+    double position[6];
+    int direction_dist;
+    double direction[3];
+};
+
 //! Hit records, one per step of a track in a detector volume: structure of
 //! arrays of 'capacity' entries, positions and directions three doubles per
 //! record. Arrays of unselected data are null.

@@ -38,6 +38,103 @@ GBX_FORCEINLINE void reset_physics_state(StateData const& s, size_type slot)
     s.num_looping_steps[slot] = 0;
 }
 
+//---------------------------------------------------------------------------//
+// Primary generation (PrimaryGenerator, src/celeritas/phys/PrimaryGenerator.cc)
+//---------------------------------------------------------------------------//
+//! XORWOW stream of its own for one primary's sampling, seeded from a
+//! 64-bit key like a per-track stream
+struct PrimaryStream
+{
+    std::uint32_t s[5];
+    std::uint32_t w;
+
+    GBX_FORCEINLINE explicit PrimaryStream(std::uint64_t key)
+    {
+        SplitMix64 sm{key};
+        std::uint64_t v = sm();
+        s[0] = static_cast<std::uint32_t>(v);
+        s[1] = static_cast<std::uint32_t>(v >> 32);
+        v = sm();
+        s[2] = static_cast<std::uint32_t>(v);
+        s[3] = static_cast<std::uint32_t>(v >> 32);
+        v = sm();
+        s[4] = static_cast<std::uint32_t>(v);
+        w = static_cast<std::uint32_t>(v >> 32);
+        if ((s[0] | s[1] | s[2] | s[3] | s[4]) == 0)
+            s[0] = 1;
+    }
+    GBX_FORCEINLINE std::uint32_t operator()()
+    {
+        std::uint32_t const t = (s[0] ^ (s[0] >> 2u));
+        s[0] = s[1];
+        s[1] = s[2];
+        s[2] = s[3];
+        s[3] = s[4];
+        s[4] = (s[4] ^ (s[4] << 4u)) ^ (t ^ (t << 1u));
+        w += 362437u;
+        return w + s[4];
+    }
+};
+
+//! Key of the per-track stream of primary 'index' of an event: the
+//! stepper seed, the event and the primary's index among its event's
+//! primaries (the same key as a primary inserted from the host)
+GBX_FORCEINLINE std::uint64_t
+primary_stream_key(unsigned int seed, size_type event, size_type index)
+{
+    SplitMix64 sm{(std::uint64_t(seed) << 32) | event};
+    SplitMix64 sm2{sm() + 0x9e3779b97f4a7c15ull * (std::uint64_t(index) + 1)};
+    return sm2();
+}
+
+//! Sample primary 'tid' of a generator launch into the staged primaries
+//! (PrimaryGenerator::operator(): particle cycled by index within the
+//! event, energy, then position, then direction, time zero). Each primary
+//! samples from its own stream, keyed by the generator seed, the event and
+//! the index, so any subset of primaries can be generated in parallel.
+GBX_FUNCTION void generate_primary(PrimaryGeneratorData const& g,
+                                   TrackInitializer* primaries,
+                                   size_type tid)
+{
+    size_type const index = tid % g.primaries_per_event;
+    size_type const event = g.first_event + tid / g.primaries_per_event;
+    PrimaryStream rng(primary_stream_key(g.seed, event, index) ^ 0x6a09e667f3bcc909ull);
+    TrackInitializer& p = primaries[tid];
+    p.track_id = invalid_id;
+    p.parent_id = invalid_id;
+    p.event_id = event;
+    p.time = 0;
+    p.particle_id = g.particle_ids[index % g.num_particles];
+    p.energy = real_type(g.energy);
+    if (g.position_dist == dist_box)
+    {
+        // UniformBoxDistribution: each coordinate uniform in [lo, hi)
+        for (int i = 0; i < 3; ++i)
+        {
+            double const u = generate_canonical<double>(rng);
+            p.pos[i] = g.position[i] + u * (g.position[3 + i] - g.position[i]);
+        }
+    }
+    else
+    {
+        p.pos = {g.position[0], g.position[1], g.position[2]};
+    }
+    if (g.direction_dist == dist_isotropic)
+    {
+        // IsotropicDistribution: cos(theta) uniform in [-1, 1), phi in
+        // [0, 2 pi)
+        double const mu = 2 * generate_canonical<double>(rng) - 1;
+        double const phi = 2 * constants::pi * generate_canonical<double>(rng);
+        double const sintheta = std::sqrt(1 - mu * mu);
+        p.dir = {sintheta * std::cos(phi), sintheta * std::sin(phi), mu};
+    }
+    else
+    {
+        p.dir = {g.direction[0], g.direction[1], g.direction[2]};
+    }
+    p.rng_key = primary_stream_key(g.stepper_seed, event, index);
+}
+
 //! Copy primary 'tid' into the initializer list (ProcessPrimariesExecutor)
 GBX_FUNCTION void process_primary(StateData const& s,
                                   size_type num_initializers,

@@ -163,6 +163,10 @@ class CoreState
 
     //! Stage primaries on the device for the next generate action
     void insert_primaries(TrackInitializer const* host_primaries, size_type n);
+    //! Sample primaries on the device into the staging buffer for the next
+    //! generate action (PrimaryGenerator; no host copy). The events must
+    //! have no primaries yet. 'gen' holds particle indices of these params.
+    void generate_primaries(PrimaryGeneratorData gen);
     size_type pending_primaries() const { return pending_primaries_; }
     void clear_pending_primaries() { pending_primaries_ = 0; }
 

@@ -163,6 +163,48 @@ int gbx_stepper_insert_primaries(gbx_stepper* stepper,
                                  const gbx_primary* primaries,
                                  size_t num_primaries);
 
+/* Distributions of the primary generator (DistributionSelection,
+ * src/celeritas/phys/PrimaryGeneratorOptions.hh:21-27, same values) */
+enum
+{
+    GBX_DIST_DELTA = 0,
+    GBX_DIST_ISOTROPIC = 1,
+    GBX_DIST_BOX = 2
+};
+
+/* Primary generator options (PrimaryGeneratorOptions,
+ * src/celeritas/phys/PrimaryGeneratorOptions.hh:47-73, as celer-sim reads
+ * them): 'num_pdg' PDG codes cycled over the primaries of each event;
+ * energy [MeV]: delta (1 parameter); position [cm]: delta (x, y, z) or box
+ * (lower x, y, z, then upper x, y, z); direction: delta (a unit vector) or
+ * isotropic (no parameter). */
+typedef struct
+{
+    unsigned int seed;
+    int pdg[8];
+    unsigned int num_pdg;
+    unsigned int num_events;
+    unsigned int primaries_per_event;
+    int energy_distribution;
+    double energy[1];
+    int position_distribution;
+    double position[6];
+    int direction_distribution;
+    double direction[3];
+} gbx_primary_generator_options;
+
+/* Sample the primaries of events [first_event, first_event + num_events)
+ * on the device, into the stepper's staging buffer, for the next
+ * gbx_stepper_step (PrimaryGenerator::operator() for each event,
+ * src/celeritas/phys/PrimaryGenerator.cc:63-83): no host memory and no
+ * host-to-device copy. Each primary samples from its own XORWOW stream keyed
+ * by the seed, its event and its index in the event, so the sequence is not
+ * the reference's mt19937 one; the distributions are. The events must not
+ * have primaries yet. Invalid options fail with the reference's messages. */
+int gbx_stepper_generate_primaries(gbx_stepper* stepper,
+                                   const gbx_primary_generator_options* options,
+                                   unsigned int first_event);
+
 /* Kill all active tracks (Stepper::kill_active) */
 int gbx_stepper_kill_active(gbx_stepper* stepper);
 
