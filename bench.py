@@ -460,6 +460,64 @@ def measure_step_output(args, wl, rank, batch=8):
     return out
 
 
+def measure_primary_generation(wl, rank, reps=5):
+    """Staging one batch of primaries for the next step: generated on the
+    device (PrimaryGenerator options: delta energy, box position, isotropic
+    direction) against built on the host and inserted (host->device copy),
+    host clock around each call with the stream synchronized. The primaries
+    are 1 keV electrons, which stop in their first step."""
+    import torch
+
+    import celeritas_gb300 as gb
+    from celeritas_gb300.primaries import PRIMARY_DTYPE
+
+    gb.load_library(precision="mixed")
+    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"], precision="mixed")
+    st = gb.Stepper(params, wl["slots"], seed=rank)
+    n = wl["slots"]
+    lo, hi = np.array([-1.0, -1.0, -6.0]), np.array([1.0, 1.0, -5.0])
+    energy = 1e-3  # 1 keV: stopped in the first step, so draining is quick
+
+    def host_batch():
+        rng = np.random.default_rng(0)
+        p = np.zeros(n, dtype=PRIMARY_DTYPE)
+        p["pdg"] = 11
+        p["energy"] = energy
+        p["pos"] = lo + (hi - lo) * rng.random((n, 3))
+        mu = 2 * rng.random(n) - 1
+        phi = 2 * np.pi * rng.random(n)
+        s = np.sqrt(1 - mu * mu)
+        p["dir"] = np.stack([s * np.cos(phi), s * np.sin(phi), mu], axis=1)
+        return p
+
+    def drain():
+        st.step()
+        st.kill_active()
+        st.run(max_steps=100000)
+
+    host_s, dev_s = [], []
+    for rep in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st.insert_primaries(host_batch())
+        st.synchronize()
+        t1 = time.perf_counter()
+        drain()
+        st.generate_primaries(pdg=11, energy=energy, position=("box", tuple(lo) + tuple(hi)),
+                              direction=("isotropic", ()), num_events=1, primaries_per_event=n,
+                              first_event=rep + 1, seed=rep)
+        st.synchronize()
+        t2 = time.perf_counter()
+        drain()
+        if rep:
+            host_s.append(t1 - t0)
+            dev_s.append(t2 - t1)
+    del st, params
+    return {"primaries": n, "host_build_and_insert_ms": 1e3 * float(np.median(host_s)),
+            "device_generate_ms": 1e3 * float(np.median(dev_s)),
+            "h2d_bytes_saved": n * 80}
+
+
 def compare_tallies(mixed, fp64):
     """Per-layer energy deposition of the mixed build against FP64, with
     errors from the scatter of the independent timed transports."""
@@ -584,6 +642,8 @@ def run_gb300(args, wl):
                                                          / pl["events_per_s"])
     if args.step_output:
         line["step_output"] = measure_step_output(args, wl, rank)
+    if args.primary_generation:
+        line["primary_generation"] = measure_primary_generation(wl, rank)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
@@ -861,6 +921,8 @@ def main():
                         help="events streamed through the server (c3: 195)")
     parser.add_argument("--sequential-sample", type=int, default=40,
                         help="c5: requests timed alone on the plain FP64 path")
+    parser.add_argument("--primary-generation", action="store_true",
+                        help="also time device primary generation against host insertion")
     parser.add_argument("--step-output", action="store_true",
                         help="also time the step output (detector hits) on the mixed path")
     parser.add_argument("--no-tune", action="store_true",

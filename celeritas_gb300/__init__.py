@@ -269,19 +269,26 @@ class Params:
         return out
 
 
+#: gbx_primary as a numpy record (field offsets of the C struct)
+_PRIMARY_RECORD = np.dtype({
+    "names": [name for name, _ in _Primary._fields_],
+    "formats": ["<i4", "<f8", ("<f8", 3), ("<f8", 3), "<f8", "<u4"],
+    "offsets": [getattr(_Primary, name).offset for name, _ in _Primary._fields_],
+    "itemsize": ctypes.sizeof(_Primary)})
+
+
 def make_primary_array(primaries: np.ndarray):
-    """Convert a structured primary array (see primaries.PRIMARY_DTYPE)."""
+    """Convert a structured primary array (see primaries.PRIMARY_DTYPE)
+    into gbx_primary records, column by column."""
     n = len(primaries)
     arr = (_Primary * max(n, 1))()
-    for i in range(n):
-        p = primaries[i]
-        arr[i].pdg = int(p["pdg"])
-        arr[i].energy = float(p["energy"])
-        for k in range(3):
-            arr[i].pos[k] = float(p["pos"][k])
-            arr[i].dir[k] = float(p["dir"][k])
-        arr[i].time = float(p["time"])
-        arr[i].event_id = int(p["event"])
+    rec = np.frombuffer(arr, dtype=_PRIMARY_RECORD, count=max(n, 1))[:n]
+    rec["pdg"] = primaries["pdg"]
+    rec["energy"] = primaries["energy"]
+    rec["pos"] = primaries["pos"]
+    rec["dir"] = primaries["dir"]
+    rec["time"] = primaries["time"]
+    rec["event_id"] = primaries["event"]
     return arr, n
 
 
