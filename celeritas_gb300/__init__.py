@@ -44,7 +44,8 @@ class _Primary(ctypes.Structure):
 class _ParamsOptions(ctypes.Structure):
     _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int),
                 ("track_order", ctypes.c_uint), ("rng_per_track", ctypes.c_int),
-                ("event_tallies", ctypes.c_int), ("reentrant_looping", ctypes.c_int)]
+                ("event_tallies", ctypes.c_int), ("reentrant_looping", ctypes.c_int),
+                ("rz_field_file", ctypes.c_char_p)]
 
 
 #: Step data of a hit (GBX_STEP_* bits of the C header, the reference's
@@ -204,6 +205,11 @@ def _check(lib: ctypes.CDLL, rc: int):
         raise GbxError(msg or f"GB300 call failed with status {rc}")
 
 
+def field_map_file(problem: str = "cms") -> str:
+    """Path of a committed synthetic R-Z field map ("cms")."""
+    return os.path.join(DATA_DIR, f"{problem}.rzmap.txt")
+
+
 def physics_file(problem: str) -> str:
     """Path of a committed synthetic physics input ("calo" or "cms")."""
     return os.path.join(DATA_DIR, f"{problem}.physics.txt")
@@ -216,7 +222,7 @@ class Params:
                  field_tesla=(0.0, 0.0, 0.0), msc: bool = False,
                  track_order: int | str = "none", precision: str = "double",
                  rng_per_track: bool = False, event_tallies: bool = False,
-                 reentrant_looping: bool = False):
+                 reentrant_looping: bool = False, rz_field: str | None = None):
         lib = load_library(precision=precision)
         self._lib = lib
         self.precision = precision
@@ -231,6 +237,8 @@ class Params:
         opts.rng_per_track = int(rng_per_track)
         opts.event_tallies = int(event_tallies)
         opts.reentrant_looping = int(reentrant_looping)
+        self._rz_field = rz_field.encode() if rz_field else None
+        opts.rz_field_file = self._rz_field
         _check(lib, lib.gbx_params_create(physics.encode(), geometry.encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle

@@ -201,6 +201,8 @@ int gbx_params_create(const char* physics_file,
             inp.options.rng_per_track = options->rng_per_track != 0;
             inp.options.event_tallies = options->event_tallies != 0;
             inp.options.reentrant_looping = options->reentrant_looping != 0;
+            if (options->rz_field_file)
+                inp.options.rz_field_file = options->rz_field_file;
             for (int i = 0; i < 3; ++i)
                 inp.options.field_tesla[i] = options->field_tesla[i];
         }

@@ -171,6 +171,7 @@ ActionId ActionRegistry::find_action(std::string_view label) const
 
 void register_core_actions(ActionRegistry* reg,
                            bool uniform_field,
+                           bool rz_map,
                            unsigned int track_order)
 {
     using O = StepActionOrder;
@@ -220,9 +221,12 @@ void register_core_actions(ActionRegistry* reg,
     implicit("physics-failure",
              "mark a track that failed to sample an interaction");
     // Along-step action registered by the driver
-    add(uniform_field ? "along-step-uniform-msc" : "along-step-general-linear",
-        uniform_field ? "apply along-step in a uniform field"
-                      : "apply along-step for particles with no field",
+    add(rz_map          ? "along-step-rzmap-msc"
+        : uniform_field ? "along-step-uniform-msc"
+                        : "along-step-general-linear",
+        rz_map          ? "apply along-step in a R-Z map field"
+        : uniform_field ? "apply along-step in a uniform field"
+                        : "apply along-step for particles with no field",
         O::along,
         step_along);
     // CoreParams actions
@@ -273,8 +277,10 @@ CoreParams::CoreParams(Input const& inp)
     : host_(build_params(inp.physics_file, inp.geometry, inp.options))
     , actions_(std::make_shared<ActionRegistry>())
 {
-    register_core_actions(
-        actions_.get(), host_.scalars.has_field, host_.scalars.track_order);
+    register_core_actions(actions_.get(),
+                          host_.scalars.has_field && !host_.scalars.has_rzmap,
+                          host_.scalars.has_rzmap,
+                          host_.scalars.track_order);
     for (size_type i = 0; i < host_.action_labels.size(); ++i)
     {
         if (actions_->id_to_label(i) != host_.action_labels[i])
@@ -301,6 +307,8 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_mscp = pk.add(h.msc_par_mat);
     std::size_t o_loop = pk.add(h.looping);
     std::size_t o_jump = pk.add(h.rng_jump);
+    std::size_t o_rzmap = pk.add(h.rzmap);
+    std::size_t o_rzdesc = pk.add(std::vector<RZMapData>(1, h.rzmap_desc));
     std::size_t o_pl = pk.add(h.surfaces);
     std::size_t o_box = pk.add(h.volumes);
     std::size_t o_no = pk.add(h.neighbor_offset);
@@ -332,6 +340,15 @@ CoreParams::CoreParams(Input const& inp)
     device_.msc.par_mat = reinterpret_cast<UrbanMscParMatRecord const*>(base + o_mscp);
     device_.looping = reinterpret_cast<LoopingRecord const*>(base + o_loop);
     device_.rng_jump = reinterpret_cast<std::uint32_t const*>(base + o_jump);
+    device_.rzmap = nullptr;
+    if (!h.rzmap.empty())
+    {
+        // The map's description, pointing at its nodes on the device
+        RZMapData desc = h.rzmap_desc;
+        desc.values = reinterpret_cast<FieldMapElement const*>(base + o_rzmap);
+        GBX_CUDA(cudaMemcpy(base + o_rzdesc, &desc, sizeof(desc), cudaMemcpyHostToDevice));
+        device_.rzmap = reinterpret_cast<RZMapData const*>(base + o_rzdesc);
+    }
     device_.geo.surfaces = reinterpret_cast<SurfaceRecord const*>(base + o_pl);
     device_.geo.volumes = reinterpret_cast<VolumeRecord const*>(base + o_box);
     device_.geo.neighbor_offset = reinterpret_cast<size_type const*>(base + o_no);

@@ -283,6 +283,7 @@ GBX_FUNCTION void field_setup(ParamsData const& p,
     double const momentum = std::sqrt(double(momentum_sq(mass, energy)));
     UniformFieldEquation rhs;
     rhs.field = {p.field[0], p.field[1], p.field[2]};
+    rhs.map = p.has_rzmap ? p.rzmap : nullptr;
     rhs.coeffi = (p.particles[pid].charge * detail::e_electron)
                  / (1 * (detail::mev_value / constants::c_light));
     fp->set_rhs(rhs);

@@ -299,6 +299,34 @@ struct GeoParams
 };
 
 //---------------------------------------------------------------------------//
+// R-Z magnetic field map (RZMapFieldParamsData,
+// src/celeritas/field/RZMapFieldData.hh)
+//---------------------------------------------------------------------------//
+//! Uniform grid of a field-map axis (UniformGridData::from_bounds)
+struct FieldMapGrid
+{
+    double front;
+    double back;
+    double delta;
+    size_type size;
+};
+
+//! Field at a map node [native units]
+struct FieldMapElement
+{
+    double value_z;
+    double value_r;
+};
+
+//! R-Z map: nodes [z][r] with r fastest
+struct RZMapData
+{
+    FieldMapGrid z;
+    FieldMapGrid r;
+    FieldMapElement const* values;
+};
+
+//---------------------------------------------------------------------------//
 // All parameters
 //---------------------------------------------------------------------------//
 struct ParamsData
@@ -356,6 +384,9 @@ struct ParamsData
     UrbanMscParams msc;
     bool has_field;
     double field[3];  //!< Uniform field [native units: gauss]
+    //! R-Z field map (along-step-rzmap-msc) instead of the uniform field
+    bool has_rzmap;
+    RZMapData const* rzmap;  //!< In the same memory as the other tables
     LoopingRecord const* looping;  //!< [particle]
     //! XORWOW jump polynomials [2][32][5]: 4^i steps, then 4^i subsequences
     //! of 2^67 steps (XorwowRngParamsData, XorwowRngData.hh:46-47)

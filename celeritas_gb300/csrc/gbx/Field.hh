@@ -63,12 +63,48 @@ GBX_FORCEINLINE double fastpow(double a, double b)
     return std::exp(b * std::log(a));
 }
 
-//! Equation of motion in a uniform field: d(pos)/ds = p/|p|,
-//! d(mom)/ds = (q/|p|) p x B
+//! Field of an R-Z map at a position (RZMapField::operator(),
+//! src/celeritas/field/RZMapField.hh:70-108): bilinear in (r, z) on the
+//! uniform grids, zero outside the map, the radial component along (x, y)
+GBX_FUNCTION Real3 rzmap_field(RZMapData const& m, Real3 const& pos)
+{
+    Real3 value{0, 0, 0};
+    double const r = std::sqrt(ipow<2>(pos.x) + ipow<2>(pos.y));
+    if (!(pos.z >= m.z.front && pos.z <= m.z.back && r >= m.r.front && r <= m.r.back))
+        return value;
+    // find_interp on a uniform grid (UniformGrid::find, operator[]); a value
+    // on the last node takes the last interval
+    auto locate = [](FieldMapGrid const& g, double v, size_type* index) {
+        size_type i = static_cast<size_type>((v - g.front) / g.delta);
+        i = min_of(i, g.size - 2);
+        double const lower = g.front + g.delta * i;
+        double const upper = g.front + g.delta * (i + 1);
+        *index = i;
+        return (v - lower) / (upper - lower);
+    };
+    size_type ir, iz;
+    double const fr = locate(m.r, r, &ir);
+    double const fz = locate(m.z, pos.z, &iz);
+    size_type const nr = m.r.size;
+    double low = m.values[iz * nr + ir].value_z;
+    double high = m.values[(iz + 1) * nr + ir].value_z;
+    value.z = low + (high - low) * fz;
+    low = m.values[iz * nr + ir].value_r;
+    high = m.values[iz * nr + ir + 1].value_r;
+    double const tmp = (r != 0) ? (low + (high - low) * fr) / r : low;
+    value.x = tmp * pos.x;
+    value.y = tmp * pos.y;
+    return value;
+}
+
+//! Equation of motion in a magnetic field: d(pos)/ds = p/|p|,
+//! d(mom)/ds = (q/|p|) p x B(pos) (MagFieldEquation). The field is uniform,
+//! or an R-Z map evaluated at the state's position when 'map' is set.
 struct UniformFieldEquation
 {
     Real3 field;
     double coeffi;
+    RZMapData const* map{nullptr};
 
     GBX_FORCEINLINE OdeState operator()(OdeState const& y) const
     {
@@ -78,7 +114,7 @@ struct UniformFieldEquation
                       momentum_inv * y.mom.y,
                       momentum_inv * y.mom.z};
         double const scale = coeffi * momentum_inv;
-        Real3 c = cross_product(y.mom, field);
+        Real3 c = cross_product(y.mom, map ? rzmap_field(*map, y.pos) : field);
         result.mom = {scale * c.x, scale * c.y, scale * c.z};
         return result;
     }
@@ -326,9 +362,16 @@ GBX_FORCEINLINE FieldStepperResult dormand_prince_step(UniformFieldEquation cons
                                                        OdeState const& beg_state)
 {
     if constexpr (sizeof(real_type) == sizeof(double))
+    {
         return dormand_prince_step_fp64(rhs, step, beg_state);
+    }
     else
+    {
+        // The FP32 stages assume a field that does not depend on position
+        if (rhs.map)
+            return dormand_prince_step_fp64(rhs, step, beg_state);
         return dormand_prince_step_mixed(rhs, step, beg_state);
+    }
 }
 
 //---------------------------------------------------------------------------//
@@ -414,7 +457,7 @@ class FieldDriver
                                        double step,
                                        Real3 const& mom) const
     {
-        if constexpr (sizeof(real_type) == sizeof(double))
+        if (sizeof(real_type) == sizeof(double) || rhs_.map)
         {
             return rel_err_sq(result.err_state, step, mom)
                    / ipow<2>(opt_.epsilon_rel_max);
@@ -436,13 +479,12 @@ class FieldDriver
     }
 
     //! Distance of the stepper's midpoint from the chord
-    static GBX_FORCEINLINE double chord_distance(FieldStepperResult const& result,
-                                                 OdeState const& state)
+    GBX_FORCEINLINE double chord_distance(FieldStepperResult const& result,
+                                          OdeState const& state) const
     {
-        if constexpr (sizeof(real_type) == sizeof(double))
+        if (sizeof(real_type) == sizeof(double) || rhs_.map)
             return distance_chord(state.pos, result.mid_state.pos, result.end_state.pos);
-        else
-            return double(result.dchord);
+        return double(result.dchord);
     }
 
     static GBX_FORCEINLINE double distance_chord(Real3 const& beg_pos,
@@ -480,7 +522,7 @@ class FieldDriver
         do
         {
             result = dormand_prince_step(rhs_, step, state);
-            double dchord = chord_distance(result, state);
+            double dchord = this->chord_distance(result, state);
             if (dchord > opt_.delta_chord + FieldOptions::dchord_tol)
             {
                 double scale_step = max_of(std::sqrt(opt_.delta_chord / dchord),

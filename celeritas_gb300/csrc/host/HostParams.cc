@@ -18,6 +18,7 @@
 #include <tuple>
 #include <array>
 #include <cmath>
+#include <fstream>
 #include <map>
 #include <stdexcept>
 
@@ -204,6 +205,7 @@ class Builder
     void build_actions();
     void build_msc_field();
     void build_particles();
+    void read_rzmap(std::string const& path);
     void build_materials();
     void build_physics();
     void build_models();
@@ -724,6 +726,44 @@ void Builder::build_models()
     }
 }
 
+//! R-Z field map (RZMapFieldParams::RZMapFieldParams,
+//! src/celeritas/field/RZMapFieldParams.cc): header 'rzmap num_z num_r
+//! min_z max_z min_r max_r' [cm], then 'Bz Br' [tesla] per node, [z][r]
+void Builder::read_rzmap(std::string const& path)
+{
+    std::ifstream in(path);
+    if (!in)
+        throw std::runtime_error("cannot open field map " + path);
+    std::string tag;
+    unsigned int nz = 0, nr = 0;
+    double min_z, max_z, min_r, max_r;
+    in >> tag >> nz >> nr >> min_z >> max_z >> min_r >> max_r;
+    if (!in || tag != "rzmap")
+        throw std::runtime_error("bad field map header in " + path);
+    if (nz < 2 || nr < 2 || !(min_r >= 0) || !(max_r > min_r) || !(max_z > min_z))
+        throw std::runtime_error("invalid field map grid in " + path);
+    hp_.rzmap.resize(std::size_t(nz) * nr);
+    for (auto& el : hp_.rzmap)
+    {
+        double bz, br;
+        if (!(in >> bz >> br))
+            throw std::runtime_error("truncated field map " + path);
+        el.value_z = bz * constants::tesla;
+        el.value_r = br * constants::tesla;
+    }
+    auto grid = [](double lo, double hi, unsigned int n) {
+        FieldMapGrid g;
+        g.front = lo;
+        g.back = hi;
+        g.delta = (hi - lo) / (n - 1);
+        g.size = n;
+        return g;
+    };
+    hp_.rzmap_desc.z = grid(min_z, max_z, nz);
+    hp_.rzmap_desc.r = grid(min_r, max_r, nr);
+    hp_.rzmap_desc.values = hp_.rzmap.data();
+}
+
 void Builder::build_msc_field()
 {
     ParamsData& s = hp_.scalars;
@@ -737,6 +777,15 @@ void Builder::build_msc_field()
     }
     if (s.has_field)
         hp_.action_labels[s.action_along_step] = "along-step-uniform-msc";
+    s.has_rzmap = false;
+    if (!opts_.rz_field_file.empty())
+    {
+        if (s.has_field)
+            throw std::runtime_error("an R-Z field map excludes a uniform field");
+        this->read_rzmap(opts_.rz_field_file);
+        s.has_field = s.has_rzmap = true;
+        hp_.action_labels[s.action_along_step] = "along-step-rzmap-msc";
+    }
 
     // Looping thresholds (SimParams::from_import with 10 field substeps)
     {
@@ -1300,6 +1349,7 @@ ParamsData make_host_view(HostParams const& hp)
     p.msc.par_mat = hp.msc_par_mat.data();
     p.looping = hp.looping.data();
     p.rng_jump = hp.rng_jump.data();
+    p.rzmap = hp.rzmap.empty() ? nullptr : &hp.rzmap_desc;
     p.geo.surfaces = hp.surfaces.data();
     p.geo.volumes = hp.volumes.data();
     p.geo.neighbor_offset = hp.neighbor_offset.data();

@@ -74,6 +74,8 @@ struct ParamsOptions
     bool event_tallies{false};
     //! A reentrant boundary step keeps the looping-step count
     bool reentrant_looping{false};
+    //! R-Z field map file (empty: none); excludes a uniform field
+    std::string rz_field_file;
 };
 
 //! All parameter tables in host memory
@@ -96,6 +98,8 @@ struct HostParams
     std::vector<UrbanMscParMatRecord> msc_par_mat;
     std::vector<LoopingRecord> looping;
     std::vector<std::uint32_t> rng_jump;  //!< [2][32][5] jump polynomials
+    std::vector<FieldMapElement> rzmap;  //!< R-Z field map nodes
+    RZMapData rzmap_desc{};  //!< Grids, and the nodes in host memory
     // Geometry
     std::vector<SurfaceRecord> surfaces;
     std::vector<VolumeRecord> volumes;

@@ -99,6 +99,13 @@ typedef struct
      * global step limit (app/celer-sim/Transporter.cc:135-150). Zero keeps
      * the reference's behaviour. */
     int reentrant_looping;
+    /* Path of an R-Z magnetic field map (NULL or empty: none; excludes
+     * field_tesla): along-step-rzmap-msc with the map interpolated as
+     * RZMapField does (src/celeritas/field/RZMapField.hh), in place of
+     * along-step-uniform-msc. Text: 'rzmap num_z num_r min_z max_z min_r
+     * max_r' [cm], then 'Bz Br' [tesla] per node, z-major ([Z][R], the
+     * order of RZMapFieldInput, src/celeritas/field/RZMapFieldInput.hh). */
+    const char* rz_field_file;
 } gbx_params_options;
 
 /* Build problem parameters from a physics input file and a named geometry

@@ -345,6 +345,10 @@ ParamsOptions physics_options(int argc, char** argv)
         {
             opts.reentrant_looping = true;
         }
+        else if (a == "--rz-field" && i + 1 < argc)
+        {
+            opts.rz_field_file = argv[i + 1];
+        }
     }
     return opts;
 }

@@ -56,6 +56,8 @@
 #include "celeritas/global/Stepper.hh"
 #include "celeritas/global/alongstep/AlongStepGeneralLinearAction.hh"
 #include "celeritas/global/alongstep/AlongStepUniformMscAction.hh"
+#include "celeritas/global/alongstep/AlongStepRZMapFieldMscAction.hh"
+#include "celeritas/field/RZMapFieldInput.hh"
 #include "celeritas/io/ImportData.hh"
 #include "celeritas/mat/MaterialParams.hh"
 #include "celeritas/phys/CutoffParams.hh"
@@ -601,6 +603,32 @@ class HitPrinter final : public StepInterface
     unsigned int step_{0};
 };
 
+//! R-Z field map from the text form shared with the GB300 build: header
+//! 'rzmap num_z num_r min_z max_z min_r max_r' [cm], then 'Bz Br' [tesla]
+//! per node, [z][r]; converted to native units as the reference's inputs are
+RZMapFieldInput load_rzmap(std::string const& path)
+{
+    std::ifstream in(path);
+    CELER_VALIDATE(in, << "cannot open field map " << path);
+    std::string tag;
+    RZMapFieldInput inp;
+    in >> tag >> inp.num_grid_z >> inp.num_grid_r >> inp.min_z >> inp.max_z
+        >> inp.min_r >> inp.max_r;
+    CELER_VALIDATE(in && tag == "rzmap", << "bad field map header");
+    std::size_t const n = std::size_t(inp.num_grid_z) * inp.num_grid_r;
+    inp.field_z.resize(n);
+    inp.field_r.resize(n);
+    for (std::size_t i = 0; i < n; ++i)
+    {
+        double bz, br;
+        in >> bz >> br;
+        inp.field_z[i] = native_value_from(units::FieldTesla{bz});
+        inp.field_r[i] = native_value_from(units::FieldTesla{br});
+    }
+    CELER_VALIDATE(in, << "truncated field map");
+    return inp;
+}
+
 struct Problem
 {
     std::shared_ptr<CoreParams> core;
@@ -616,7 +644,8 @@ Problem build_problem(ImportData const& imported,
                       Real3 field,
                       bool msc,
                       TrackOrder track_order,
-                      bool print_hits)
+                      bool print_hits,
+                      std::string const& rz_field)
 {
     Problem prob;
     prob.geo = build_geometry(geo_name);
@@ -671,7 +700,18 @@ Problem build_problem(ImportData const& imported,
     auto urban = msc ? UrbanMscParams::from_import(
                            *params.particle, *params.material, imported)
                      : nullptr;
-    if (field[0] == 0 && field[1] == 0 && field[2] == 0)
+    if (!rz_field.empty())
+    {
+        auto along_step = AlongStepRZMapFieldMscAction::from_params(
+            params.action_reg->next_id(),
+            *params.material,
+            *params.particle,
+            load_rzmap(rz_field),
+            urban,
+            eloss);
+        params.action_reg->insert(along_step);
+    }
+    else if (field[0] == 0 && field[1] == 0 && field[2] == 0)
     {
         auto along_step = AlongStepGeneralLinearAction::from_params(
             params.action_reg->next_id(),
@@ -807,7 +847,8 @@ int run(int argc, char** argv)
     {
         std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
                      "<seed> [--field Bx By Bz] [--msc] [--steps N] "
-                     "[--track-order N] [--reseed EVENT] [--dump-rng N] [--hits]\n";
+                     "[--track-order N] [--reseed EVENT] [--dump-rng N] [--hits] "
+                     "[--rz-field FILE]\n";
         return 2;
     }
     std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
@@ -821,6 +862,7 @@ int run(int argc, char** argv)
     long long reseed = -1;
     size_type dump_rng = 0;
     bool print_hits = false;
+    std::string rz_field;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
@@ -845,12 +887,15 @@ int run(int argc, char** argv)
             dump_rng = std::stoul(argv[++i]);
         else if (a == "--hits")
             print_hits = true;
+        else if (a == "--rz-field")
+            rz_field = argv[++i];
     }
 
     KvFile kv(phys_path);
     ImportData imported = load_import(kv, msc);
     Problem prob
-        = build_problem(imported, geo_name, seed, field, msc, track_order, print_hits);
+        = build_problem(
+            imported, geo_name, seed, field, msc, track_order, print_hits, rz_field);
     auto primaries = load_primaries(prim_path, *prob.core->particle());
 
     StepperInput sinp;

@@ -27,7 +27,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 import oracle  # noqa: E402
-from celeritas_gb300 import physics_file  # noqa: E402
+from celeritas_gb300 import field_map_file, physics_file  # noqa: E402
 from celeritas_gb300.primaries import eta_beam, pencil_beam, write_primaries_text  # noqa: E402
 
 # name: primaries (pdg, energy [MeV], count), track slots, seed, msc, field [T]
@@ -65,6 +65,10 @@ CASES = {
                                          energy=5000.0, num=4, slots=16384, seed=9,
                                          beam_seed=3, msc=True, field=[0.0, 0.0, 3.8],
                                          track_order=7),
+    # R-Z field map (along-step-rzmap-msc) of the CMS-like detector
+    "cms_rzmap_mix_e2000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=2000.0,
+                                   num=4, slots=4096, seed=3, beam_seed=8, msc=True,
+                                   rz_field=True),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),
@@ -111,6 +115,8 @@ def case_options(c: dict) -> list[str]:
         opts += ["--track-order", str(int(c["track_order"]))]
     if c.get("reseed") is not None:
         opts += ["--reseed", str(int(c["reseed"]))]
+    if c.get("rz_field"):
+        opts += ["--rz-field", field_map_file(c.get("geometry", "cms"))]
     return opts
 
 
@@ -124,6 +130,8 @@ def make_case(name: str, hits: bool = False) -> dict:
             "track_order": int(c.get("track_order", 0))}
     if c.get("reseed") is not None:
         case["reseed"] = int(c["reseed"])
+    if c.get("rz_field"):
+        case["rz_field"] = True
     if c.get("beam", "pencil") == "eta":
         case.update(beam="eta", pdgs=list(c["pdgs"]), emax=c.get("emax"),
                     beam_seed=c["beam_seed"])

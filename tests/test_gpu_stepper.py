@@ -42,10 +42,11 @@ def params_for(gb, case):
     """Params with the case's field and MSC options (cached per options)."""
     geometry = case.get("geometry", "calo")
     key = (geometry, tuple(case.get("field", [0, 0, 0])), bool(case.get("msc")),
-           int(case.get("track_order", 0)))
+           int(case.get("track_order", 0)), bool(case.get("rz_field")))
     if key not in _PARAMS:
         _PARAMS[key] = gb.Params(gb.physics_file(geometry), geometry,
-                                 field_tesla=key[1], msc=key[2], track_order=key[3])
+                                 field_tesla=key[1], msc=key[2], track_order=key[3],
+                                 rz_field=gb.field_map_file(geometry) if key[4] else None)
     return _PARAMS[key]
 
 
@@ -211,3 +212,19 @@ def test_reentrant_looping_ends_grazing_orbit(gb, precision):
     res = [st.step(p)] + st.run(max_steps=199)
     assert res[-1].alive == 0 and res[-1].queued == 0
     assert len(res) < 200
+
+
+def test_rzmap_mixed_build(gb):
+    """The R-Z map in the mixed-precision build (FP64 integration where the
+    field depends on position): the golden transport's total deposition
+    within the CMS-like tolerance."""
+    golden = load_golden("cms_rzmap_mix_e2000_n4")
+    c = golden["case"]
+    params = gb.Params(gb.physics_file("cms"), "cms", msc=True, precision="mixed",
+                       rz_field=gb.field_map_file("cms"), reentrant_looping=True)
+    assert "along-step-rzmap-msc" in params.action_labels()
+    st = gb.Stepper(params, c["num_track_slots"], seed=c["seed"])
+    res = [st.step(case_primaries(c))] + st.run(max_steps=100000)
+    assert res[-1].alive == 0 and res[-1].queued == 0
+    ref = sum(golden["edep"].values())
+    np.testing.assert_allclose(st.energy_deposition().sum(), ref, rtol=LIBM_EDEP_RTOL)
