@@ -213,7 +213,8 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"],
                        track_order=track_order, precision=precision,
-                       reentrant_looping=wl.get("reentrant_looping", False))
+                       reentrant_looping=wl.get("reentrant_looping", False),
+                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
     labels = params.action_labels()
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     if tuning:
@@ -336,7 +337,8 @@ def measure_served(args, wl, rank, tuning=None):
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
                        precision="mixed", rng_per_track=True, event_tallies=True,
-                       reentrant_looping=wl.get("reentrant_looping", False))
+                       reentrant_looping=wl.get("reentrant_looping", False),
+                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     if tuning:
         stepper.set_tuning(**tuning)
@@ -372,7 +374,8 @@ def tune_workload(wl, precision, rank):
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"], track_order=7,
                        precision=precision, rng_per_track=True,
-                       reentrant_looping=wl.get("reentrant_looping", False))
+                       reentrant_looping=wl.get("reentrant_looping", False),
+                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
     # Calibration events drawn with another beam seed than the timed ones
     prim = make_primaries(wl, rank, num=wl["tune_primaries"], seed_offset=77)
     t0 = time.perf_counter()
@@ -401,7 +404,8 @@ def measure_step_output(args, wl, rank, batch=8):
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
                        precision="mixed",
-                       reentrant_looping=wl.get("reentrant_looping", False))
+                       reentrant_looping=wl.get("reentrant_looping", False),
+                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
     labels = params.action_labels()
     gather = labels.index("step-gather-post")
     st = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
@@ -806,7 +810,8 @@ def run_batching(args, wl):
     params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
                        field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
                        precision="mixed", rng_per_track=True,
-                       reentrant_looping=wl.get("reentrant_looping", False))
+                       reentrant_looping=wl.get("reentrant_looping", False),
+                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
 
     def make_stepper(slots):
         return gb.Stepper(params, slots, seed=wl["seed"] + rank)
@@ -933,7 +938,7 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]
-    if args.workload == "c3":
+    if args.workload in ("c3", "c3rz"):
         args.plain = True
         args.served_events = args.served_events or 195
     if args.workload == "c5":

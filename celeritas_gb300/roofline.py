@@ -33,6 +33,8 @@ ACTION_BYTES = {
     # multiple-scattering range, factor, minimum limit (r/w) and true path,
     # geometric path, slope (r/w)
     "along-step-uniform-msc": (243, 17, 5),
+    # the same state in an R-Z map field (the map itself is a read-only table)
+    "along-step-rzmap-msc": (243, 17, 5),
     # photons: no random numbers, no energy loss | reals: energy, MFP (r/w),
     # macro XS
     "along-step-neutral": (158, 4, 5),

@@ -58,6 +58,17 @@ WORKLOADS = {
                            "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
                            "one bench step = 65 of the 1300 events; launch "
                            "configuration autotuned on 16 other events"),
+    # c3 in the synthetic R-Z field map of the CMS-like detector (a 3.8 T
+    # solenoid with soft edges and a return flux) instead of the uniform field
+    "c3rz": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
+                 emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
+                 seed=0, events=1300, msc=True, field=(0.0, 0.0, 0.0), rz_field=True,
+                 bench_primaries=3250, tune_primaries=800, reentrant_looping=True,
+                 description="CMS-like detector in an R-Z field map (3.8 T solenoid, soft "
+                             "edges, return flux), Urban MSC; events of 50 e-/gamma, "
+                             "log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; one bench "
+                             "step = 65 events; launch configuration autotuned on 16 "
+                             "other events"),
     # Batching of uneven events: CMS-like detector, 4096 events with primaries
     # per event log-uniform in 1-1000 and energies log-uniform in
     # 0.1-100 GeV (e-/gamma alternating, |eta| < 1.5), all in flight
@@ -111,6 +122,10 @@ def physics_args(wl: dict) -> list[str]:
         args.append("--msc")
     if wl.get("reentrant_looping"):
         args.append("--reentrant-looping")
+    if wl.get("rz_field"):
+        from . import field_map_file
+
+        args += ["--rz-field", field_map_file(wl["geometry"])]
     if any(wl["field"]):
         args += ["--field"] + [repr(float(f)) for f in wl["field"]]
     return args
