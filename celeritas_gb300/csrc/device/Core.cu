@@ -308,6 +308,7 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_loop = pk.add(h.looping);
     std::size_t o_jump = pk.add(h.rng_jump);
     std::size_t o_rzmap = pk.add(h.rzmap);
+    std::size_t o_rzmap_f = pk.add(h.rzmap_f);
     std::size_t o_rzdesc = pk.add(std::vector<RZMapData>(1, h.rzmap_desc));
     std::size_t o_pl = pk.add(h.surfaces);
     std::size_t o_box = pk.add(h.volumes);
@@ -346,6 +347,7 @@ CoreParams::CoreParams(Input const& inp)
         // The map's description, pointing at its nodes on the device
         RZMapData desc = h.rzmap_desc;
         desc.values = reinterpret_cast<FieldMapElement const*>(base + o_rzmap);
+        desc.values_f = reinterpret_cast<FieldMapElementF const*>(base + o_rzmap_f);
         GBX_CUDA(cudaMemcpy(base + o_rzdesc, &desc, sizeof(desc), cudaMemcpyHostToDevice));
         device_.rzmap = reinterpret_cast<RZMapData const*>(base + o_rzdesc);
     }

@@ -318,12 +318,20 @@ struct FieldMapElement
     double value_r;
 };
 
+//! Field at a map node, rounded to FP32 (mixed-precision stages)
+struct FieldMapElementF
+{
+    float value_z;
+    float value_r;
+};
+
 //! R-Z map: nodes [z][r] with r fastest
 struct RZMapData
 {
     FieldMapGrid z;
     FieldMapGrid r;
     FieldMapElement const* values;
+    FieldMapElementF const* values_f;
 };
 
 //---------------------------------------------------------------------------//

@@ -97,6 +97,37 @@ GBX_FUNCTION Real3 rzmap_field(RZMapData const& m, Real3 const& pos)
     return value;
 }
 
+//! The R-Z map's field in FP32 (the mixed-precision stages): the same
+//! interpolation on the FP32 nodes at an FP32 position
+GBX_FUNCTION Vec3<float> rzmap_field_f(RZMapData const& m, Vec3<float> const& pos)
+{
+    Vec3<float> value{0, 0, 0};
+    float const r = std::sqrt(pos.x * pos.x + pos.y * pos.y);
+    if (!(pos.z >= float(m.z.front) && pos.z <= float(m.z.back) && r >= float(m.r.front)
+          && r <= float(m.r.back)))
+        return value;
+    auto locate = [](FieldMapGrid const& g, float v, size_type* index) {
+        float const u = (v - float(g.front)) / float(g.delta);
+        size_type const i = min_of(static_cast<size_type>(u), g.size - 2);
+        *index = i;
+        return u - float(i);
+    };
+    size_type ir, iz;
+    float const fr = locate(m.r, r, &ir);
+    float const fz = locate(m.z, pos.z, &iz);
+    size_type const nr = m.r.size;
+    FieldMapElementF const* v = m.values_f;
+    float low = v[iz * nr + ir].value_z;
+    float high = v[(iz + 1) * nr + ir].value_z;
+    value.z = low + (high - low) * fz;
+    low = v[iz * nr + ir].value_r;
+    high = v[iz * nr + ir + 1].value_r;
+    float const tmp = (r != 0) ? (low + (high - low) * fr) / r : low;
+    value.x = tmp * pos.x;
+    value.y = tmp * pos.y;
+    return value;
+}
+
 //! Equation of motion in a magnetic field: d(pos)/ds = p/|p|,
 //! d(mom)/ds = (q/|p|) p x B(pos) (MagFieldEquation). The field is uniform,
 //! or an R-Z map evaluated at the state's position when 'map' is set.
@@ -224,14 +255,14 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_fp64(UniformFieldEquation co
 }
 
 
-//! Mixed-precision Dormand-Prince 5(4) step for a uniform field. The field
-//! equation depends on the momentum only, so the stages carry FP32 momenta
-//! and FP32 derivatives; the end position is the FP64 start plus an FP32
-//! increment. The embedded error estimate (a weighted sum of the FP32 stage
-//! derivatives) and the chord distance (from the FP32 increments to the end
-//! and to Shampine's midpoint) are formed in FP32: their inputs carry FP32
-//! rounding, which FP64 arithmetic on them would not remove. The driver
-//! takes the error norms and the acceptance test in FP64.
+//! Mixed-precision Dormand-Prince 5(4) step. The stages carry FP32 momenta,
+//! FP32 derivatives and, for a field map, FP32 position increments from the
+//! start at which the map is read in FP32; the end position is the FP64
+//! start plus an FP32 increment. The embedded error estimate (a weighted sum
+//! of the FP32 stage derivatives) and the chord distance (from the FP32
+//! increments to the end and to Shampine's midpoint) are formed in FP32:
+//! their inputs carry FP32 rounding, which FP64 arithmetic on them would not
+//! remove. The driver takes the error norms and the acceptance test in FP64.
 GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation const& rhs,
                                                           double step,
                                                           OdeState const& beg_state)
@@ -256,10 +287,16 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation c
                 c5 = F(187940372067. / 1594534317056.),
                 c6 = F(-1776094331. / 19743644256.), c7 = F(11237099. / 235043384.);
 
-    F3 const field{F(rhs.field.x), F(rhs.field.y), F(rhs.field.z)};
+    F3 const uniform{F(rhs.field.x), F(rhs.field.y), F(rhs.field.z)};
     F const coeffi = F(rhs.coeffi);
-    // d(pos)/ds = p/|p|, d(mom)/ds = (q/|p|) p x B
-    auto eval = [&](F3 const& m, F3* kpos, F3* kmom) {
+    // Start position in FP32, for field-map lookups only
+    F3 const p0{F(beg_state.pos.x), F(beg_state.pos.y), F(beg_state.pos.z)};
+    // d(pos)/ds = p/|p|, d(mom)/ds = (q/|p|) p x B(pos), at the stage's
+    // position increment 'dp' from the start
+    auto eval = [&](F3 const& dp, F3 const& m, F3* kpos, F3* kmom) {
+        F3 const field
+            = rhs.map ? rzmap_field_f(*rhs.map, F3{p0.x + dp.x, p0.y + dp.y, p0.z + dp.z})
+                      : uniform;
         F const inv = F(1) / std::sqrt(m.x * m.x + m.y * m.y + m.z * m.z);
         *kpos = {m.x * inv, m.y * inv, m.z * inv};
         F const scale = coeffi * inv;
@@ -287,13 +324,18 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation c
 
     F const h = F(step);
     F3 const m0{F(beg_state.mom.x), F(beg_state.mom.y), F(beg_state.mom.z)};
+    F3 const zero{0, 0, 0};
     F3 kp[7], km[7];
-    eval(m0, &kp[0], &km[0]);
-    eval(stage(m0, h, A1, 1, km), &kp[1], &km[1]);
-    eval(stage(m0, h, A2, 2, km), &kp[2], &km[2]);
-    eval(stage(m0, h, A3, 3, km), &kp[3], &km[3]);
-    eval(stage(m0, h, A4, 4, km), &kp[4], &km[4]);
-    eval(stage(m0, h, A5, 5, km), &kp[5], &km[5]);
+    // Stage position increments matter only for a field map
+    auto dpos_at = [&](F const* a, int n) {
+        return rhs.map ? stage(zero, h, a, n, kp) : zero;
+    };
+    eval(zero, m0, &kp[0], &km[0]);
+    eval(dpos_at(A1, 1), stage(m0, h, A1, 1, km), &kp[1], &km[1]);
+    eval(dpos_at(A2, 2), stage(m0, h, A2, 2, km), &kp[2], &km[2]);
+    eval(dpos_at(A3, 3), stage(m0, h, A3, 3, km), &kp[3], &km[3]);
+    eval(dpos_at(A4, 4), stage(m0, h, A4, 4, km), &kp[4], &km[4]);
+    eval(dpos_at(A5, 5), stage(m0, h, A5, 5, km), &kp[5], &km[5]);
     // Fifth-order solution: FP32 increments added to the FP64 start
     F const bf[7] = {F(b1), 0, F(b3), F(b4), F(b5), F(b6), 0};
     F3 dpos{0, 0, 0}, m_end = m0;
@@ -307,10 +349,10 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation c
         m_end.y += h * bf[i] * km[i].y;
         m_end.z += h * bf[i] * km[i].z;
     }
-    eval(m_end, &kp[6], &km[6]);
+    F3 const end_inc{h * dpos.x, h * dpos.y, h * dpos.z};
+    eval(end_inc, m_end, &kp[6], &km[6]);
 
     FieldStepperResult result;
-    F3 const end_inc{h * dpos.x, h * dpos.y, h * dpos.z};
     result.end_state.pos = {beg_state.pos.x + double(end_inc.x),
                             beg_state.pos.y + double(end_inc.y),
                             beg_state.pos.z + double(end_inc.z)};
@@ -367,9 +409,6 @@ GBX_FORCEINLINE FieldStepperResult dormand_prince_step(UniformFieldEquation cons
     }
     else
     {
-        // The FP32 stages assume a field that does not depend on position
-        if (rhs.map)
-            return dormand_prince_step_fp64(rhs, step, beg_state);
         return dormand_prince_step_mixed(rhs, step, beg_state);
     }
 }
@@ -457,7 +496,7 @@ class FieldDriver
                                        double step,
                                        Real3 const& mom) const
     {
-        if (sizeof(real_type) == sizeof(double) || rhs_.map)
+        if constexpr (sizeof(real_type) == sizeof(double))
         {
             return rel_err_sq(result.err_state, step, mom)
                    / ipow<2>(opt_.epsilon_rel_max);
@@ -482,9 +521,10 @@ class FieldDriver
     GBX_FORCEINLINE double chord_distance(FieldStepperResult const& result,
                                           OdeState const& state) const
     {
-        if (sizeof(real_type) == sizeof(double) || rhs_.map)
+        if constexpr (sizeof(real_type) == sizeof(double))
             return distance_chord(state.pos, result.mid_state.pos, result.end_state.pos);
-        return double(result.dchord);
+        else
+            return double(result.dchord);
     }
 
     static GBX_FORCEINLINE double distance_chord(Real3 const& beg_pos,

@@ -762,6 +762,13 @@ void Builder::read_rzmap(std::string const& path)
     hp_.rzmap_desc.z = grid(min_z, max_z, nz);
     hp_.rzmap_desc.r = grid(min_r, max_r, nr);
     hp_.rzmap_desc.values = hp_.rzmap.data();
+    hp_.rzmap_f.resize(hp_.rzmap.size());
+    for (std::size_t i = 0; i < hp_.rzmap.size(); ++i)
+    {
+        hp_.rzmap_f[i] = {static_cast<float>(hp_.rzmap[i].value_z),
+                          static_cast<float>(hp_.rzmap[i].value_r)};
+    }
+    hp_.rzmap_desc.values_f = hp_.rzmap_f.data();
 }
 
 void Builder::build_msc_field()

@@ -99,6 +99,7 @@ struct HostParams
     std::vector<LoopingRecord> looping;
     std::vector<std::uint32_t> rng_jump;  //!< [2][32][5] jump polynomials
     std::vector<FieldMapElement> rzmap;  //!< R-Z field map nodes
+    std::vector<FieldMapElementF> rzmap_f;  //!< The nodes rounded to FP32
     RZMapData rzmap_desc{};  //!< Grids, and the nodes in host memory
     // Geometry
     std::vector<SurfaceRecord> surfaces;
