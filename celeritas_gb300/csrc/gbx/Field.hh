@@ -99,7 +99,7 @@ GBX_FUNCTION Real3 rzmap_field(RZMapData const& m, Real3 const& pos)
 
 //! The R-Z map's field in FP32 (the mixed-precision stages): the same
 //! interpolation on the FP32 nodes at an FP32 position
-GBX_FUNCTION Vec3<float> rzmap_field_f(RZMapData const& m, Vec3<float> const& pos)
+GBX_NOINLINE Vec3<float> rzmap_field_f(RZMapData const& m, Vec3<float> const& pos)
 {
     Vec3<float> value{0, 0, 0};
     float const r = std::sqrt(pos.x * pos.x + pos.y * pos.y);
@@ -163,8 +163,30 @@ struct FieldStepperResult
     float dchord;  //!< sagitta of the midpoint from the chord
 };
 
+//! The field equation with its field source fixed at compile time, so that
+//! each FP64 Runge-Kutta step branches once on the source, not per stage
+template<bool UseMap>
+struct FixedFieldEquation
+{
+    UniformFieldEquation const& eq;
+
+    GBX_FORCEINLINE OdeState operator()(OdeState const& y) const
+    {
+        double momentum_inv = 1.0 / std::sqrt(dot_product(y.mom, y.mom));
+        OdeState result;
+        result.pos = {momentum_inv * y.mom.x,
+                      momentum_inv * y.mom.y,
+                      momentum_inv * y.mom.z};
+        double const scale = eq.coeffi * momentum_inv;
+        Real3 c = cross_product(y.mom, UseMap ? rzmap_field(*eq.map, y.pos) : eq.field);
+        result.mom = {scale * c.x, scale * c.y, scale * c.z};
+        return result;
+    }
+};
+
 //! Dormand-Prince 5(4) step with Shampine's midpoint interpolation
-GBX_FUNCTION FieldStepperResult dormand_prince_step_fp64(UniformFieldEquation const& rhs,
+template<class Equation>
+GBX_FUNCTION FieldStepperResult dormand_prince_step_fp64(Equation const& rhs,
                                                          double step,
                                                          OdeState const& beg_state)
 {
@@ -405,7 +427,9 @@ GBX_FORCEINLINE FieldStepperResult dormand_prince_step(UniformFieldEquation cons
 {
     if constexpr (sizeof(real_type) == sizeof(double))
     {
-        return dormand_prince_step_fp64(rhs, step, beg_state);
+        if (rhs.map)
+            return dormand_prince_step_fp64(FixedFieldEquation<true>{rhs}, step, beg_state);
+        return dormand_prince_step_fp64(FixedFieldEquation<false>{rhs}, step, beg_state);
     }
     else
     {
