@@ -1,13 +1,24 @@
 """Benchmark: track-steps/s and events/s of the EM-shower stepping loop.
 
-One benchmark step transports one batch of synthetic primaries (the
-workload, default c2) to completion through the GB300 stepper. Prints one
-JSON line on rank 0. The headline is the mixed-precision build with
-action-sorted tracks; the plain FP64 build is timed the same way and
-reported under "fp64", with the per-layer energy-deposition difference
-between the two under "mixed_vs_fp64_edep".
+Default workload: c3, the CMS-like detector (1300 events of 50 e-/gamma
+primaries, 3.8 T, 2^21 track slots). Bench step k transports events
+[65k, 65k + 65) to completion, so the default 20 steps cover every event of
+the configuration once. Prints one JSON line on rank 0:
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1]
+* value / events_per_s: the batched, autotuned, action-sorted
+  mixed-precision path (the headline);
+* fp64_plain: the plain FP64 path (no action sort, default launches) on the
+  same events, and events_per_s_vs_fp64_plain;
+* served: the same events streamed through the continuous-batching server
+  as Poisson arrivals at each offered rate, with p50/p99 latency, and
+  served_events_per_s_vs_fp64_plain;
+* mixed_vs_fp64_edep: per-volume deposition of the two paths, paired by
+  batch; gpu_vs_cpu_edep: the CPU baseline's sample events transported on
+  the GPU (FP64 and mixed) against the CPU run, paired by event;
+* roofline, cpu_baseline (with the restatement's calibration against the
+  reference's own host stepper), clocks, e2e, and the c2 calorimeter line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c3]
                   [--precision mixed|double] [--track-order 0|5|6|7] [--no-fp64]
   python bench.py --impl reference ...   # CPU path of the reference loop
 
@@ -38,7 +49,8 @@ sys.path.insert(0, REPO)
 
 import numpy as np  # noqa: E402
 
-from celeritas_gb300.workloads import WORKLOADS, make_primaries, physics_args  # noqa: E402
+from celeritas_gb300.workloads import (  # noqa: E402
+    WORKLOADS, make_primaries, physics_args, step_batches)
 
 
 MAX_STEPS = 20000
@@ -110,45 +122,82 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(wl, threads, target_seconds=15.0, events=None):
-    """Time the oracle's CPU restatement on the host cores (bounded sample)."""
+def port_over_reference(name):
+    """Track-step rate of the CPU restatement over the reference's own host
+    stepper on the same events and cores, measured where the reference
+    sources exist (oracle/calibrate_port.py) and committed beside it."""
+    path = os.path.join(REPO, "oracle", "port_over_reference.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    ratio = d.get("port_over_reference", {}).get(name)
+    return None if ratio is None else {"ratio": ratio, "machine": d.get("machine"),
+                                       "command": d.get("command")}
+
+
+def cpu_baseline(wl, threads, target_seconds=15.0, events=None, tallies=False):
+    """Time the oracle's CPU restatement on the host cores (bounded sample).
+
+    The sample is the first 'events' events of the workload (sized to about
+    'target_seconds' from a short probe when not given). With 'tallies' the
+    per-event deposition of every detector is returned too (array
+    [events, detectors], rows in event order)."""
     import oracle
     from celeritas_gb300 import physics_file
     from celeritas_gb300.primaries import write_primaries_text
 
     exe = oracle.build_port()
-    # One primary per event, events distributed over threads (celer-sim with
-    # one stream per thread). A CPU stepper visits every slot each step, so
-    # each thread gets 4096 slots (enough for one shower of the workload):
-    # a CPU-favourable setting rather than the GPU's slot count per stream
+    # Events distributed over threads (celer-sim with one stream per
+    # thread). A CPU stepper visits every slot each step, so each thread gets
+    # 4096 slots (enough for one shower of the workload): a CPU-favourable
+    # setting rather than the GPU's slot count per stream
     slots = 4096
+    per_event = max(1, wl["num_primaries"] // wl["events"])
     if events is None:
         # Calibrate on a short sample, then size the sample to target_seconds
-        probe = cpu_baseline(wl, threads, events=2 * threads)
+        probe = cpu_baseline(wl, threads, events=threads)
         steps_per_event = probe["value"] / probe["events_per_s"]
         events = int(target_seconds * probe["value"] / max(steps_per_event, 1.0))
-        events = max(2 * threads, min(events, 20000))
-    prim = make_primaries(wl, num=events)
-    prim["event"] = np.arange(events)
+        events = max(threads, min(events, 20000))
+    prim = make_primaries(wl, num=events * per_event)
+    if per_event == 1:
+        prim["event"] = np.arange(events)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
+        ttxt = os.path.join(tmp, "t.txt")
         write_primaries_text(ptxt, prim)
+        extra = ["--event-tallies", ttxt] if tallies else []
         res = subprocess.run([exe, "bench", physics_file(wl["physics"]), wl["geometry"], ptxt,
                               str(slots), str(wl["seed"]), "--threads", str(threads)]
-                             + physics_args(wl),
+                             + extra + physics_args(wl),
                              capture_output=True, text=True, check=True)
+        table = np.loadtxt(ttxt, ndmin=2) if tallies else None
     tok = res.stdout.split()
     nev, steps, sec = int(tok[4]), int(tok[6]), float(tok[8])
-    return {
+    out = {
         "value": steps / sec,
         "unit": "track-steps/s",
         "events_per_s": nev / sec,
         "cores": threads,
         "kind": "port",
-        "sample": f"first {nev} events of the workload, 1 primary each ({steps} "
-                  f"track-steps) on {threads} threads, {slots} slots per thread "
+        "sample": f"first {nev} events of the workload ({per_event} primaries each, "
+                  f"{steps} track-steps) on {threads} threads, {slots} slots per thread "
                   f"stepper, {sec:.2f} s",
     }
+    name = next((k for k, v in WORKLOADS.items() if v is wl), None)
+    cal = port_over_reference(name) if name else None
+    if cal:
+        # The reference's own Stepper<host> ran 1/ratio as fast as the
+        # restatement on the same events and cores where it could be built
+        out["port_over_reference"] = cal["ratio"]
+        out["reference_estimate"] = out["value"] / cal["ratio"]
+        out["calibration"] = f"{cal['machine']}: {cal['command']}"
+    if tallies:
+        order = np.argsort(table[:, 0], kind="stable")
+        out["_events"] = prim
+        out["_tallies"] = table[order, 1:]
+    return out
 
 
 def run_reference(args, wl):
@@ -160,10 +209,10 @@ def run_reference(args, wl):
     vals, evs = [], []
     base = None
     # Size each step's sample to ~8 s of CPU work from a short probe
-    probe = cpu_baseline(wl, threads, events=2 * threads)
+    probe = cpu_baseline(wl, threads, events=threads)
     steps_per_event = probe["value"] / probe["events_per_s"]
     events = int(8.0 * probe["value"] / max(steps_per_event, 1.0))
-    events = max(2 * threads, min(events, 20000))
+    events = max(threads, min(events, 20000))
     for i in range(args.warmup + args.steps):
         r = cpu_baseline(wl, threads, events=events)
         if i >= args.warmup:
@@ -188,7 +237,8 @@ def run_reference(args, wl):
         "data": "synthetic",
         "config": {"workload": wl["description"], "name": args.workload},
         "cpu_baseline": {"value": value, "unit": "track-steps/s", "cores": threads,
-                         "kind": base["kind"], "sample": base["sample"]},
+                         "kind": base["kind"], "sample": base["sample"],
+                         "port_over_reference": base.get("port_over_reference")},
         "e2e": {"value": value, "unit": "track-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -198,30 +248,40 @@ def run_reference(args, wl):
 DTYPES = {"mixed": "f32 physics + f64 positions/geometry/field/tally", "double": "f64"}
 
 
+def make_params(wl, precision, track_order, **options):
+    """CoreParams of a workload through the public API."""
+    import celeritas_gb300 as gb
+
+    gb.load_library(precision=precision)
+    return gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
+                     field_tesla=wl["field"], msc=wl["msc"], track_order=track_order,
+                     precision=precision,
+                     reentrant_looping=wl.get("reentrant_looping", False),
+                     rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None,
+                     **options)
+
+
 def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
-            track_order=None, tuning=None):
+            track_order=None, tuning=None, steps=None, warmup=None, actions=True):
     """Time one precision's stepping loop: device and end-to-end throughput,
-    per-transport tallies, and per-action times for the roofline. 'tuning'
-    is a launch configuration (gbx_stepper_set_tuning settings)."""
+    per-step tallies, and per-action times for the roofline. Timed step k
+    transports the k-th batch of the workload (step_batches). 'tuning' is a
+    launch configuration (gbx_stepper_set_tuning settings)."""
     import torch
 
     import celeritas_gb300 as gb
     from celeritas_gb300 import roofline, sharding
 
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     track_order = args.track_order if track_order is None else track_order
-    gb.load_library(precision=precision)
-    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
-                       field_tesla=wl["field"], msc=wl["msc"],
-                       track_order=track_order, precision=precision,
-                       reentrant_looping=wl.get("reentrant_looping", False),
-                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
+    params = make_params(wl, precision, track_order)
     labels = params.action_labels()
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     if tuning:
         stepper.set_tuning(**tuning)
     stream = stream_cls(stepper.stream_handle())
-    prim = sharding.rank_primaries(wl, rank, num=wl.get("bench_primaries"))
-    events_per_step = len(np.unique(prim["event"]))
+    batches, warm = step_batches(wl, rank, steps)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     def finish(res):
@@ -232,12 +292,12 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
             raise RuntimeError(f"transport did not finish in {MAX_STEPS} steps")
         return res
 
-    for _ in range(args.warmup):
-        finish([stepper.step(prim)])
+    for _ in range(warmup):
+        finish([stepper.step(warm)])
     torch.cuda.synchronize()
 
-    dev_ms, e2e_s, track_steps, iterations, tallies = [], [], [], [], []
-    for _ in range(args.steps):
+    dev_ms, e2e_s, track_steps, iterations, tallies, events = [], [], [], [], [], 0
+    for prim in batches:
         flush.zero_()
         torch.cuda.synchronize()
         if dist:
@@ -259,65 +319,74 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
         track_steps.append(sum(r.active for r in res))
         iterations.append(len(res))
         tallies.append(edep)
+        events += len(np.unique(prim["event"]))
 
-    # Per-action device times over one more (untimed) transport, stepped
-    # eagerly so that each step's action ranges can be read back
-    stepper.set_action_times(True)
-    processed = {lab: 0 for lab in labels}
-    res = [stepper.step(prim)]
-    while True:
-        offs = stepper.get_state("action_offsets", np.uint32).astype(np.int64)
-        half = len(offs) // 2
-        along, post = np.diff(offs[:half]), np.diff(offs[half:])
-        active = res[-1].active
+    per_action, dom = {}, None
+    if actions:
+        # Per-action device times over one more (untimed) transport, stepped
+        # eagerly so that each step's action ranges can be read back
+        stepper.set_action_times(True)
+        processed = {lab: 0 for lab in labels}
+        res = [stepper.step(batches[0])]
+        while True:
+            offs = stepper.get_state("action_offsets", np.uint32).astype(np.int64)
+            half = len(offs) // 2
+            along, post = np.diff(offs[:half]), np.diff(offs[half:])
+            active = res[-1].active
+            for aid, lab in enumerate(labels):
+                if lab.startswith("along-step"):
+                    processed[lab] += int(along[aid])
+                elif lab in roofline.MODEL_ACTIONS or lab in ("geo-boundary", "tracking-cut"):
+                    processed[lab] += int(post[aid])
+                else:
+                    processed[lab] += active
+            if not (res[-1].alive or res[-1].queued) or len(res) >= MAX_STEPS:
+                break
+            res.append(stepper.step())
+        ms, launches = stepper.action_times()
+        stepper.set_action_times(False)
+
+        real_bytes = 4 if precision == "mixed" else 8
         for aid, lab in enumerate(labels):
-            if lab.startswith("along-step"):
-                processed[lab] += int(along[aid])
-            elif lab in roofline.MODEL_ACTIONS or lab in ("geo-boundary", "tracking-cut"):
-                processed[lab] += int(post[aid])
-            else:
-                processed[lab] += active
-        if not (res[-1].alive or res[-1].queued) or len(res) >= MAX_STEPS:
-            break
-        res.append(stepper.step())
-    ms, launches = stepper.action_times()
-    stepper.set_action_times(False)
-
-    real_bytes = 4 if precision == "mixed" else 8
-    per_action = {}
-    for aid, lab in enumerate(labels):
-        if launches[aid] == 0:
-            continue
-        nl = int(launches[aid])
-        proc = processed[lab]
-        idle = 0 if lab.startswith(("along-step", "sort-")) else wl["slots"] * nl - proc
-        b_proc, b_idle = roofline.bytes_per_slot(lab, real_bytes)
-        per_action[lab] = {"ms_per_launch": ms[aid] / nl,
-                           "bytes_per_launch": (proc * b_proc + max(idle, 0) * b_idle) / nl,
-                           "processed_per_launch": proc / nl}
-    dom = max(per_action, key=lambda lab: per_action[lab]["ms_per_launch"] * launches[labels.index(lab)])
+            if launches[aid] == 0:
+                continue
+            nl = int(launches[aid])
+            proc = processed[lab]
+            idle = 0 if lab.startswith(("along-step", "sort-")) else wl["slots"] * nl - proc
+            b_proc, b_idle = roofline.bytes_per_slot(lab, real_bytes)
+            per_action[lab] = {"ms_per_launch": ms[aid] / nl,
+                               "bytes_per_launch": (proc * b_proc + max(idle, 0) * b_idle) / nl,
+                               "processed_per_launch": proc / nl,
+                               "launches": nl}
+        dom = max(per_action,
+                  key=lambda lab: per_action[lab]["ms_per_launch"] * per_action[lab]["launches"])
     total_ms = float(np.sum(dev_ms))
     total_e2e = float(np.sum(e2e_s))
     total_steps = float(np.sum(track_steps))
-    # Slowest rank's times, all ranks' track-steps (no-op for one process)
-    red = sharding.reduce_run(dist, "cuda", total_ms, total_e2e, total_steps)
+    # Slowest rank's times, all ranks' track-steps and tallies (no-op for one
+    # process); the per-step tallies stay per rank for the comparisons
+    red = sharding.reduce_run(dist, "cuda", total_ms, total_e2e, total_steps,
+                              tallies=np.sum(tallies, axis=0))
     total_ms, total_e2e, total_steps = red["time_ms"], red["e2e_s"], red["track_steps"]
+    world = max(1, int(os.environ.get("WORLD_SIZE", "1")))
     out = {
         "precision": precision,
         "value": total_steps / (total_ms / 1e3),
         "e2e": total_steps / total_e2e,
-        "ms_per_step": total_ms / args.steps,
-        "events_per_s": events_per_step * max(1, int(os.environ.get("WORLD_SIZE", "1")))
-        * args.steps / (total_ms / 1e3),
+        "ms_per_step": total_ms / steps,
+        "events_per_s": events * world / (total_ms / 1e3),
+        "events_per_s_e2e": events * world / total_e2e,
+        "events": events * world,
         "track_order": track_order,
         "track_steps_per_step": int(np.mean(track_steps)),
         "iterations_per_step": int(np.mean(iterations)),
         "tallies": np.array(tallies),
+        "total_tallies": red["tallies"],
         "per_action": per_action,
         "dominant": dom,
         "kernels_per_step": stepper.step_kernels(),
         "iterations": iterations,
-        "h2d": int(len(prim)) * 80,
+        "h2d": int(np.mean([len(b) for b in batches])) * 80,
         "d2h": len(tallies[0]) * 8 + 16 * 64,
         "detectors": params.detector_labels(),
     }
@@ -325,41 +394,73 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
     return out
 
 
+def measure_vs_cpu(wl, rank, cpu, labels=None):
+    """Per-event, per-detector deposition of the CPU restatement's sample
+    events transported again on the GPU (FP64 and mixed, action-sorted,
+    per-event tallies), each compared with the CPU run event by event."""
+    import celeritas_gb300 as gb
+
+    prim, ref = cpu["_events"], cpu["_tallies"]
+    events = np.unique(prim["event"])
+    out = {"events": int(len(events)), "cpu": "the cpu_baseline sample (same primaries, "
+           "independent random streams)"}
+    for precision in ("double", "mixed"):
+        params = make_params(wl, precision, 7, event_tallies=True)
+        st = gb.Stepper(params, wl["slots"], seed=wl["seed"] + 17 + rank)
+        res = [st.step(prim)] + st.run(max_steps=MAX_STEPS, batch=64)
+        if res[-1].alive or res[-1].queued:
+            raise RuntimeError("transport did not finish")
+        gpu = st.event_detector_energy_deposition(0, int(events.max()) + 1)[events]
+        out["fp64" if precision == "double" else "mixed"] = compare_paired(gpu, ref, labels)
+        del st, params
+    return out
+
+
 def measure_served(args, wl, rank, tuning=None):
-    """Batched and served form: the workload's events streamed through the
+    """Served form: every event of the workload streamed through the
     continuous-batching server (mixed precision, action-sorted, per-track
-    streams), all arriving at once and admitted as queue space frees up, so
-    the tail of one event overlaps the start of the next."""
+    streams), arriving as a Poisson process at each offered rate in
+    'args.served_rates' (events/s). An event is admitted when it has arrived
+    and its footprint fits; its tracks join the running step loop, so the
+    events in flight overlap on the device. Latency = completion - arrival
+    on the host clock."""
     import celeritas_gb300 as gb
     from celeritas_gb300 import serving
 
-    gb.load_library(precision="mixed")
-    params = gb.Params(gb.physics_file(wl["physics"]), wl["geometry"],
-                       field_tesla=wl["field"], msc=wl["msc"], track_order=args.track_order,
-                       precision="mixed", rng_per_track=True, event_tallies=True,
-                       reentrant_looping=wl.get("reentrant_looping", False),
-                       rz_field=gb.field_map_file(wl["geometry"]) if wl.get("rz_field") else None)
+    params = make_params(wl, "mixed", args.track_order, rng_per_track=True,
+                         event_tallies=True)
     stepper = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
     if tuning:
         stepper.set_tuning(**tuning)
     per_event = wl["num_primaries"] // wl["events"]
+    num_events = wl["events"]
     server = serving.EventServer({wl["geometry"]: stepper},
                                  {wl["geometry"]: 16 * wl["slots"]}, 1 << 16)
+    allp = make_primaries(wl, rank)
 
-    def requests(num_events, first, seed):
-        prim = make_primaries(wl, rank, num=num_events * per_event, seed_offset=seed)
+    def requests(first, arrivals):
         out = []
-        for k in range(num_events):
-            p = prim[k * per_event:(k + 1) * per_event].copy()
+        for k, t in enumerate(arrivals):
+            p = allp[k * per_event:(k + 1) * per_event].copy()
             p["event"] = first + k
-            out.append(serving.Request(first + k, wl["geometry"], p, 0.0))
+            out.append(serving.Request(first + k, wl["geometry"], p, float(t)))
         return out
 
-    server.serve(requests(max(4, args.served_events // 8), 0, 99))  # warm-up
-    reqs = requests(args.served_events, 1 << 12, 0)
-    summary = server.serve(reqs)
-    summary["primaries_per_event"] = per_event
-    return summary
+    warm = 64
+    server.serve(requests(0, np.zeros(warm)))  # warm-up: graphs captured
+    runs = []
+    first = warm
+    for i, rate in enumerate(args.served_rates):
+        rng = np.random.default_rng(1000 + 7 * i + 7919 * rank)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, num_events))
+        summary = server.serve(requests(first, arrivals))
+        summary["offered_rate"] = rate
+        summary["arrivals"] = "Poisson"
+        runs.append(summary)
+        first += num_events
+    del server, stepper, params
+    return {"primaries_per_event": per_event, "rates": runs,
+            "events_per_s": max(r["events_per_s"] for r in runs)}
 
 
 def tune_workload(wl, precision, rank):
@@ -409,7 +510,7 @@ def measure_step_output(args, wl, rank, batch=8):
     labels = params.action_labels()
     gather = labels.index("step-gather-post")
     st = gb.Stepper(params, wl["slots"], seed=wl["seed"] + rank)
-    prim = sharding.rank_primaries(wl, rank, num=wl.get("bench_primaries"))
+    prim = step_batches(wl, rank, 1)[0][0]
     capacity = (batch + 1) * wl["slots"]  # every slot hitting in every step
 
     def transport(read):
@@ -544,6 +645,45 @@ def compare_tallies(mixed, fp64):
             "max_layer_rel_diff": float(rel.max()), "mean_layer_rel_diff": float(rel.mean())}
 
 
+def compare_paired(a, b, labels=None):
+    """Per-volume deposition of two runs over the same inputs (rows: the
+    same batch or event in both, random streams independent), as paired
+    differences: for each volume the mean difference over the rows and its
+    standard error from their scatter give a Student t, turned into the
+    normal deviate of the same tail probability; the sum of their squares is
+    the chi-square over the volumes. Also the relative difference of the
+    total with its standard error, and per-volume relative differences of
+    volumes above 1e-3 of the largest."""
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    n = len(a)
+    d = a - b
+    mean_d = d.mean(axis=0)
+    se = d.std(axis=0, ddof=1) / np.sqrt(n)
+    used = se > 0
+    from scipy import stats
+
+    t = mean_d[used] / se[used]
+    z = stats.norm.isf(stats.t.sf(np.abs(t), n - 1))
+    chi2 = float((z ** 2).sum())
+    dof = int(used.sum())
+    ref = b.mean(axis=0)
+    tot_d = d.sum(axis=1)
+    out = {"rows": int(n), "chi2": chi2, "dof": dof,
+           "p": float(stats.chi2.sf(chi2, dof)) if dof else None,
+           "total_rel_diff": float(tot_d.mean() / b.sum(axis=1).mean()),
+           "total_rel_sigma": float(tot_d.std(ddof=1) / np.sqrt(n) / b.sum(axis=1).mean())}
+    big = ref > 1e-3 * ref.max()
+    rel = mean_d[big] / ref[big]
+    out["mean_abs_volume_rel_diff"] = float(np.abs(rel).mean())
+    out["max_abs_volume_rel_diff"] = float(np.abs(rel).max())
+    if labels is not None:
+        worst = np.argsort(-np.where(used, np.abs(mean_d) / np.where(used, se, 1), 0))[:3]
+        out["largest_deviations"] = [
+            {"volume": labels[i], "rel_diff": float(mean_d[i] / ref[i]) if ref[i] else None,
+             "t": float(mean_d[i] / se[i]) if se[i] else None} for i in worst]
+    return out
+
+
 def run_gb300(args, wl):
     import torch
 
@@ -564,22 +704,36 @@ def run_gb300(args, wl):
     if dist:
         dist.barrier()
 
+    # Event batches (c3): the headline is the batched, autotuned mixed path
+    # beside the plain FP64 path (no action sort) on the same events; other
+    # workloads compare with the action-sorted FP64 path
+    batched = bool(wl.get("events_per_step"))
     precisions = [args.precision] + (["double"] if args.precision != "double"
-                                     and not args.no_fp64 else [])
+                                     and not args.no_fp64 and not batched else [])
     results = {}
     tuning, tuning_report = None, None
     if wl.get("tune_primaries") and not args.no_tune:
         tuning, tuning_report = tune_workload(wl, precisions[0], rank)
+    ES = torch.cuda.ExternalStream
     with ClockSampler(local_rank) as clocks:
         for prec in precisions:
-            results[prec] = measure(args, wl, prec, torch.cuda.ExternalStream, dist,
-                                    rank, local_rank, clocks,
+            results[prec] = measure(args, wl, prec, ES, dist, rank, local_rank, clocks,
                                     tuning=tuning if prec == precisions[0] else None)
-        if args.plain:
-            # The plain FP64 path: no action sort
-            results["plain"] = measure(args, wl, "double", torch.cuda.ExternalStream,
-                                       dist, rank, local_rank, clocks, track_order=0)
+        if args.plain or batched:
+            # The plain FP64 path: no action sort, default launch settings
+            results["plain"] = measure(args, wl, "double", ES, dist, rank, local_rank,
+                                       clocks, track_order=0, actions=False)
+        clocks_summary = clocks.summary()
     head = results[precisions[0]]
+    served = None
+    if batched and args.served_rates:
+        served = measure_served(args, wl, rank, tuning=tuning)
+    c2 = None
+    if batched and args.c2_steps and args.workload != "c2":
+        c2 = measure_c2(args, dist, rank, local_rank)
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline(wl, os.cpu_count() or 1, tallies=True)
 
     if rank != 0:
         if dist:
@@ -607,6 +761,7 @@ def run_gb300(args, wl):
         "config": {"workload": wl["description"], "name": args.workload,
                    "precision": head["precision"],
                    "track_order": args.track_order,
+                   "events_timed": head["events"],
                    "track_steps_per_step": head["track_steps_per_step"],
                    "iterations_per_step": head["iterations_per_step"],
                    "l2": "flushed (256 MiB write) between timed steps",
@@ -614,6 +769,7 @@ def run_gb300(args, wl):
                    "reentrant_looping": bool(wl.get("reentrant_looping", False)),
                    "tuning": tuning_report},
         "e2e": {"value": head["e2e"], "unit": "track-steps/s",
+                "events_per_s": head["events_per_s_e2e"],
                 "h2d_bytes_per_step": head["h2d"], "d2h_bytes_per_step": head["d2h"]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -624,8 +780,9 @@ def run_gb300(args, wl):
                                                    / max(v["ms_per_launch"], 1e-9) / 1e6, 2)}
                                  for k, v in head["per_action"].items()}},
         "gpu_launches": int(sum(it * head["kernels_per_step"] + 2 for it in head["iterations"])),
-        "clocks": clocks.summary(),
+        "clocks": clocks_summary,
     }
+    labels = head["detectors"]
     if "double" in results and head["precision"] != "double":
         fp = results["double"]
         line["fp64"] = {"value": fp["value"], "e2e": fp["e2e"], "ms_per_step": fp["ms_per_step"],
@@ -637,22 +794,56 @@ def run_gb300(args, wl):
         pl = results["plain"]
         line["fp64_plain"] = {"value": pl["value"], "e2e": pl["e2e"],
                               "events_per_s": pl["events_per_s"],
-                              "ms_per_step": pl["ms_per_step"], "track_order": 0}
+                              "events_per_s_e2e": pl["events_per_s_e2e"],
+                              "ms_per_step": pl["ms_per_step"], "track_order": 0,
+                              "events_timed": pl["events"]}
         line["events_per_s_vs_fp64_plain"] = head["events_per_s"] / pl["events_per_s"]
-        if args.served_events:
-            served = measure_served(args, wl, rank, tuning=tuning)
-            line["served"] = served
-            line["served_events_per_s_vs_fp64_plain"] = (served["events_per_s"]
-                                                         / pl["events_per_s"])
+        if batched:
+            # Same events in both: paired per-batch comparison
+            line["mixed_vs_fp64_edep"] = compare_paired(head["tallies"], pl["tallies"], labels)
+            line["mixed_vs_fp64_edep"]["compared"] = (
+                "mixed (sorted, tuned) against plain FP64, per timed batch of the same "
+                "events, independent random streams")
+    if served:
+        line["served"] = served
+        if "plain" in results:
+            line["served_events_per_s_vs_fp64_plain"] = (
+                served["events_per_s"] / results["plain"]["events_per_s"])
+    if c2:
+        line["c2"] = c2
     if args.step_output:
         line["step_output"] = measure_step_output(args, wl, rank)
     if args.primary_generation:
         line["primary_generation"] = measure_primary_generation(wl, rank)
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(wl, os.cpu_count() or 1)
+    if cpu is not None:
+        line["gpu_vs_cpu_edep"] = measure_vs_cpu(wl, rank, cpu, labels)
+        line["cpu_baseline"] = {k: v for k, v in cpu.items() if not k.startswith("_")}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def measure_c2(args, dist, rank, local_rank):
+    """The calorimeter workload (c2) as an extra line: the mixed and the
+    action-sorted FP64 paths, every step transporting all 10^4 primaries,
+    with their per-layer deposition difference."""
+    import torch
+
+    wl = WORKLOADS["c2"]
+    steps, warmup = args.c2_steps, 3
+    ES = torch.cuda.ExternalStream
+    out = {"workload": wl["description"], "steps": steps, "warmup": warmup}
+    with ClockSampler(local_rank) as clocks:
+        mixed = measure(args, wl, "mixed", ES, dist, rank, local_rank, clocks, track_order=7,
+                        steps=steps, warmup=warmup, actions=False)
+        fp64 = measure(args, wl, "double", ES, dist, rank, local_rank, clocks, track_order=7,
+                       steps=max(2, steps // 2), warmup=warmup, actions=False)
+        out["clocks"] = clocks.summary()
+    for name, r in (("mixed", mixed), ("fp64", fp64)):
+        out[name] = {"value": r["value"], "e2e": r["e2e"], "events_per_s": r["events_per_s"],
+                     "ms_per_step": r["ms_per_step"], "unit": "track-steps/s"}
+    out["mixed_vs_fp64_edep"] = compare_tallies(mixed["tallies"], fp64["tallies"])
+    return out
 
 
 def run_serving(args, wl):
@@ -915,15 +1106,18 @@ def main():
     parser.add_argument("--steps", type=int, default=10)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    parser.add_argument("--workload", default="c2", choices=list(WORKLOADS))
+    parser.add_argument("--workload", default="c3", choices=list(WORKLOADS))
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--precision", default="mixed", choices=["mixed", "double"])
     parser.add_argument("--track-order", type=int, default=7,
                         help="TrackOrder: 0 none, 5/6/7 action sorts")
     parser.add_argument("--no-fp64", action="store_true",
                         help="skip the FP64 comparison run")
-    parser.add_argument("--served-events", type=int, default=0,
-                        help="events streamed through the server (c3: 195)")
+    parser.add_argument("--served-rates", default="30,200",
+                        help="event batches (c3): offered Poisson rates [events/s] at "
+                             "which all events of the workload are served; empty: none")
+    parser.add_argument("--c2-steps", type=int, default=5,
+                        help="event batches (c3): timed steps of the extra c2 line; 0: none")
     parser.add_argument("--sequential-sample", type=int, default=40,
                         help="c5: requests timed alone on the plain FP64 path")
     parser.add_argument("--primary-generation", action="store_true",
@@ -933,14 +1127,13 @@ def main():
     parser.add_argument("--no-tune", action="store_true",
                         help="skip the autotuner where the workload uses it (c3)")
     parser.add_argument("--plain", action="store_true",
-                        help="also time the plain FP64 path (no action sort); on for c3")
+                        help="also time the plain FP64 path (no action sort); always on "
+                             "for event batches (c3)")
     args = parser.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    args.served_rates = [float(r) for r in args.served_rates.split(",") if r.strip()]
     wl = WORKLOADS[args.workload]
-    if args.workload in ("c3", "c3rz"):
-        args.plain = True
-        args.served_events = args.served_events or 195
     if args.workload == "c5":
         if args.impl == "reference":
             run_reference(args, WORKLOADS["c3"])

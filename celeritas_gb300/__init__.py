@@ -161,7 +161,28 @@ _PROTOTYPES = [
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint), ctypes.c_size_t]),
     ("gbx_stepper_event_energy_deposition", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int]),
+    ("gbx_stepper_event_detector_energy_deposition", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint, ctypes.c_size_t,
+      ctypes.c_int]),
+    ("gbx_libm_evaluate", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+      ctypes.c_size_t]),
 ]
+
+#: Elementary functions of the FP64 path (GBX_LIBM_* of the C header)
+LIBM_FUNCTIONS = ("exp", "log", "sin", "cos", "tanh", "log1p", "expm1", "cbrt")
+
+
+def libm_evaluate(function: str, x, precision: str = "double") -> np.ndarray:
+    """The stepping loop's FP64 elementary function 'function' evaluated on
+    the current device for every element of x."""
+    lib = load_library(precision=precision)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    ptr = ctypes.POINTER(ctypes.c_double)
+    _check(lib, lib.gbx_libm_evaluate(LIBM_FUNCTIONS.index(function), x.ctypes.data_as(ptr),
+                                      y.ctypes.data_as(ptr), x.size))
+    return y
 
 EXPORTED_SYMBOLS = [name for name, _, _ in _PROTOTYPES]
 
@@ -459,6 +480,18 @@ class Stepper:
         _check(self._lib, self._lib.gbx_stepper_event_energy_deposition(
             self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
             num_events, int(clear)))
+        return out
+
+    def event_detector_energy_deposition(self, first_event: int, num_events: int,
+                                         clear: bool = False) -> np.ndarray:
+        """Energy deposited in each detector per event [MeV], events
+        [first_event, first_event + num_events): array [events, detectors]
+        (event tallies)."""
+        ndet = len(self.params.detector_labels())
+        out = np.zeros((num_events, ndet), dtype=np.float64)
+        _check(self._lib, self._lib.gbx_stepper_event_detector_energy_deposition(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            first_event, num_events, int(clear)))
         return out
 
     def extend_from_secondaries_static(self):

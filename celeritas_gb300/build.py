@@ -51,6 +51,10 @@ def common_flags(precision: str = "double") -> list[str]:
         "-std=c++17",
         "-Xcompiler",
         "-fPIC",
+        # Host code (table set-up, the elementary functions' host copies)
+        # without contraction, as the CPU oracle programs are compiled
+        "-Xcompiler",
+        "-ffp-contract=off",
         "--expt-relaxed-constexpr",
         "-Xptxas",
         "-v" if os.environ.get("GBX_PTXAS_VERBOSE") else "-O3",

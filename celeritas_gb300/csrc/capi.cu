@@ -10,6 +10,7 @@
 #include <string>
 #include <type_traits>
 
+#include "gbx/Libm.hh"
 #include "host/Core.hh"
 
 struct gbx_params_s
@@ -25,6 +26,30 @@ struct gbx_stepper_s
 namespace
 {
 thread_local std::string g_last_error;
+
+//! y[i] = f(x[i]) with the stepping loop's FP64 elementary functions
+__global__ void libm_evaluate_kernel(int function, double const* x, double* y, size_t n)
+{
+    namespace L = gbx::libm;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+    {
+        double const v = x[i];
+        double r;
+        switch (function)
+        {
+            case GBX_LIBM_EXP: r = L::exp(v); break;
+            case GBX_LIBM_LOG: r = L::log(v); break;
+            case GBX_LIBM_SIN: r = L::sin(v); break;
+            case GBX_LIBM_COS: r = L::cos(v); break;
+            case GBX_LIBM_TANH: r = L::tanh(v); break;
+            case GBX_LIBM_LOG1P: r = L::log1p(v); break;
+            case GBX_LIBM_EXPM1: r = L::expm1(v); break;
+            default: r = L::cbrt(v); break;
+        }
+        y[i] = r;
+    }
+}
 
 template<class F>
 int guarded(F&& f)
@@ -375,6 +400,23 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
     });
 }
 
+int gbx_stepper_event_detector_energy_deposition(gbx_stepper* stepper,
+                                                 double* out,
+                                                 unsigned int first_event,
+                                                 size_t num_events,
+                                                 int clear)
+{
+    return guarded([&] {
+        if (!stepper || (num_events && !out))
+            throw std::runtime_error("null argument");
+        if (!stepper->stepper->params().host().scalars.event_tallies)
+            throw std::runtime_error("per-event tallies are not enabled");
+        auto v = stepper->stepper->state().event_detector_energy_deposition(
+            first_event, static_cast<gbx::size_type>(num_events), clear != 0);
+        std::copy(v.begin(), v.end(), out);
+    });
+}
+
 int gbx_stepper_generate_primaries(gbx_stepper* stepper,
                                    const gbx_primary_generator_options* options,
                                    unsigned int first_event)
@@ -523,6 +565,35 @@ int gbx_stepper_extend_from_secondaries_static(gbx_stepper* stepper)
         gbx::launch_extend_from_secondaries_static(state.context(), state.stream());
         if (cudaError_t err = cudaGetLastError(); err != cudaSuccess)
             throw std::runtime_error(cudaGetErrorString(err));
+    });
+}
+
+int gbx_libm_evaluate(int function, const double* x, double* y, size_t n)
+{
+    return guarded([&] {
+        if (function < GBX_LIBM_EXP || function > GBX_LIBM_CBRT)
+            throw std::runtime_error("unknown elementary function");
+        if (n == 0)
+            return;
+        if (!x || !y)
+            throw std::runtime_error("null argument");
+        double* buf = nullptr;
+        auto check = [&buf](cudaError_t err) {
+            if (err != cudaSuccess)
+            {
+                if (buf)
+                    cudaFree(buf);
+                throw std::runtime_error(cudaGetErrorString(err));
+            }
+        };
+        check(cudaMalloc(&buf, 2 * n * sizeof(double)));
+        check(cudaMemcpy(buf, x, n * sizeof(double), cudaMemcpyHostToDevice));
+        unsigned int const blocks
+            = static_cast<unsigned int>(std::min<size_t>((n + 255) / 256, 4096));
+        libm_evaluate_kernel<<<blocks, 256>>>(function, buf, buf + n, n);
+        check(cudaGetLastError());
+        check(cudaMemcpy(y, buf + n, n * sizeof(double), cudaMemcpyDeviceToHost));
+        check(cudaFree(buf));
     });
 }
 

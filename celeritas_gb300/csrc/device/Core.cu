@@ -386,6 +386,7 @@ CoreState::CoreState(CoreParams const& params,
     size_type const ndet = params.host().scalars.num_detectors;
     size_type const nblocks = (n + block_size - 1) / block_size;
     size_type const log_cap = 4096;
+    ndet_ = ndet;
 
     Layout L;
     auto arr = [&L, n](std::size_t elem) { return L.reserve(elem * n); };
@@ -418,6 +419,9 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_tcount = L.reserve(4 * std::size_t(max_events));
     std::size_t o_evedep = L.reserve(8 * std::size_t(max_events));
     std::size_t o_evlive = L.reserve(4 * std::size_t(max_events));
+    bool const event_tallies = params.host().scalars.event_tallies;
+    std::size_t o_evdet = L.reserve(
+        event_tallies ? 8 * std::size_t(max_events) * std::max<size_type>(ndet, 1) : 0);
     std::size_t o_secs = L.reserve(sizeof(Secondary) * std::size_t(sec_cap));
     std::size_t o_det = arr(4);
     std::size_t o_calo = L.reserve(8 * std::size_t(std::max<size_type>(ndet, 1)));
@@ -499,6 +503,7 @@ CoreState::CoreState(CoreParams const& params,
     s.track_counters = static_cast<size_type*>(at(o_tcount));
     s.event_edep = static_cast<double*>(at(o_evedep));
     s.event_live = static_cast<size_type*>(at(o_evlive));
+    s.event_det_edep = event_tallies ? static_cast<double*>(at(o_evdet)) : nullptr;
     s.max_events = max_events;
     s.secondaries = static_cast<Secondary*>(at(o_secs));
     s.secondary_capacity = sec_cap;
@@ -884,6 +889,28 @@ std::vector<double> CoreState::event_energy_deposition(size_type n, bool clear)
     if (clear)
     {
         GBX_CUDA(cudaMemsetAsync(ref_.event_edep, 0, sizeof(double) * n, stream_));
+    }
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    return out;
+}
+
+std::vector<double>
+CoreState::event_detector_energy_deposition(size_type first, size_type n, bool clear)
+{
+    if (!ref_.event_det_edep)
+        throw std::runtime_error("per-event tallies are not enabled");
+    if (std::size_t(first) + n > ref_.max_events)
+        throw std::runtime_error("more events requested than the stepper holds");
+    std::size_t const ndet = ndet_;
+    std::vector<double> out(std::size_t(n) * ndet);
+    if (out.empty())
+        return out;
+    double* src = ref_.event_det_edep + std::size_t(first) * ndet;
+    GBX_CUDA(cudaMemcpyAsync(
+        out.data(), src, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, stream_));
+    if (clear)
+    {
+        GBX_CUDA(cudaMemsetAsync(src, 0, sizeof(double) * out.size(), stream_));
     }
     GBX_CUDA(cudaStreamSynchronize(stream_));
     return out;

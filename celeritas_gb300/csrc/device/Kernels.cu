@@ -231,7 +231,12 @@ __global__ __launch_bounds__(block_size) void calo_kernel(ParamsData p, StateDat
     }
     warp_tally(s.calo_edep, det, edep);
     if (p.event_tallies)
+    {
         warp_tally(s.event_edep, event, edep);
+        warp_tally(s.event_det_edep,
+                   event == invalid_id ? invalid_id : event * p.num_detectors + det,
+                   edep);
+    }
 }
 
 //---------------------------------------------------------------------------//

@@ -662,6 +662,9 @@ struct StateData
     // ([max_events]; null without per-event tallies)
     double* event_edep;
     size_type* event_live;
+    // Per-event energy deposition of each detector ([max_events][detectors],
+    // event-major; null without per-event tallies)
+    double* event_det_edep;
 
     // Action-sorted thread -> slot indirection (CoreStateData::track_slots)
     // and the first thread of each action bin, one table per sort key:

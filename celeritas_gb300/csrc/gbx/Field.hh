@@ -60,7 +60,7 @@ GBX_FORCEINLINE Real3 cross_product(Real3 const& x, Real3 const& y)
 
 GBX_FORCEINLINE double fastpow(double a, double b)
 {
-    return std::exp(b * std::log(a));
+    return libm::exp(b * libm::log(a));
 }
 
 //! Field of an R-Z map at a position (RZMapField::operator(),
@@ -573,7 +573,7 @@ class FieldDriver
             // Heuristic step-size factor in FP32 (the acceptance test that
             // uses err_sq stays FP64); clamp the argument to FP32 range
             float const e = float(min_of(max_of(err_sq, 1e-30), 1e30));
-            return opt_.safety * double(std::exp(float(power) * std::log(e)));
+            return opt_.safety * double(libm::exp(float(power) * libm::log(e)));
         }
     }
 

@@ -104,7 +104,7 @@ GBX_FORCEINLINE real_type sample_tsai_urban(real_type energy,
     real_type u;
     do
     {
-        real_type uu = -std::log(generate_canonical<real_type>(rng)
+        real_type uu = -libm::log(generate_canonical<real_type>(rng)
                                  * generate_canonical<real_type>(rng));
         u = uu
             * (sample_bernoulli<real_type>(real_type(0.25), rng)
@@ -132,7 +132,7 @@ GBX_FUNCTION Interaction interact_klein_nishina(ParamsData const& p,
         = real_type(1 / p.particles[p.electron_id].mass);
     real_type const k = inc_energy * inv_electron_mass;
     real_type const epsilon_0 = 1 / (1 + 2 * k);
-    real_type const p_f1 = bernoulli_p(-std::log(epsilon_0),
+    real_type const p_f1 = bernoulli_p(-libm::log(epsilon_0),
                                        real_type(0.5) * (1 - ipow<2>(epsilon_0)));
     ReciprocalDistribution<real_type> sample_f1(1, epsilon_0);
     UniformRealDistribution<real_type> sample_f2_sq(ipow<2>(epsilon_0), 1);
@@ -283,13 +283,13 @@ GBX_FUNCTION Interaction interact_livermore_pe(ParamsData const& p,
 GBX_FORCEINLINE real_type bh_screening_f1(real_type delta)
 {
     using R = real_type;
-    return delta > R(1.4) ? R(42.038) - R(8.29) * std::log(delta + R(0.958))
+    return delta > R(1.4) ? R(42.038) - R(8.29) * libm::log(delta + R(0.958))
                           : R(42.184) - delta * (R(7.444) - R(1.623) * delta);
 }
 GBX_FORCEINLINE real_type bh_screening_f2(real_type delta)
 {
     using R = real_type;
-    return delta > R(1.4) ? R(42.038) - R(8.29) * std::log(delta + R(0.958))
+    return delta > R(1.4) ? R(42.038) - R(8.29) * libm::log(delta + R(0.958))
                           : R(41.326) - delta * (R(5.848) - R(0.902) * delta);
 }
 
@@ -323,7 +323,7 @@ GBX_FUNCTION Interaction interact_bethe_heitler(ParamsData const& p,
             f_z += 8 * real_type(element.coulomb_correction);
         }
         real_type const delta_max
-            = std::exp((real_type(42.038) - f_z) / real_type(8.29))
+            = libm::exp((real_type(42.038) - f_z) / real_type(8.29))
               - real_type(0.958);
         real_type const epsilon1
             = half - half * std::sqrt(1 - delta_min / delta_max);
@@ -342,7 +342,7 @@ GBX_FUNCTION Interaction interact_bethe_heitler(ParamsData const& p,
             {
                 epsilon = half
                           - (half - epsilon_min)
-                                * std::cbrt(generate_canonical<real_type>(rng));
+                                * libm::cbrt(generate_canonical<real_type>(rng));
                 real_type delta = impact_parameter(epsilon);
                 g = (bh_screening_f1(delta) - f_z) / f10;
             }
@@ -435,7 +435,7 @@ GBX_FUNCTION Interaction interact_seltzer_berger(ParamsData const& p,
     // Table position in log energy
     SBElementTable const& t = p.sb_tables[element_id];
     real_type const* xgrid = p.reals + t.x;
-    real_type const loge = std::log(inc_energy);
+    real_type const loge = libm::log(inc_energy);
     size_type ix = find_nonuniform(xgrid, t.nx, loge);
     real_type const xf = (loge - real_type(xgrid[ix]))
                          / (real_type(xgrid[ix + 1]) - real_type(xgrid[ix]));
@@ -476,7 +476,7 @@ GBX_FUNCTION Interaction interact_seltzer_berger(ParamsData const& p,
         else
         {
             real_type delta = cutoff_invbeta - calc_invbeta(gamma_energy);
-            xs = xs * std::exp(alpha_z * min_of(delta, real_type{0}));
+            xs = xs * libm::exp(alpha_z * min_of(delta, real_type{0}));
         }
     } while (reject_sample<real_type>(xs, max_xs, rng));
 
@@ -554,8 +554,8 @@ GBX_FUNCTION LPMFunctions calc_lpm(MaterialRecord const& mat,
     }
     else if (s_prime > sqrt_two * s1)
     {
-        real_type const log_s1 = std::log(sqrt_two * s1);
-        real_type const h = std::log(s_prime) / log_s1;
+        real_type const log_s1 = libm::log(sqrt_two * s1);
+        real_type const h = libm::log(s_prime) / log_s1;
         xi = 1 + h - real_type(0.08) * (1 - h) * h * (2 - h) / log_s1;
     }
     real_type s = s_prime / std::sqrt(xi);
@@ -572,7 +572,7 @@ GBX_FUNCTION LPMFunctions calc_lpm(MaterialRecord const& mat,
         }
         else if (s > s1)
         {
-            xi = 1 + std::log(s) / std::log(s1);
+            xi = 1 + libm::log(s) / libm::log(s1);
         }
     }
     real_type phi;
@@ -588,7 +588,7 @@ GBX_FUNCTION LPMFunctions calc_lpm(MaterialRecord const& mat,
         real_type const cb[3]
             = {real_type(-6), real_type(-6 * (3 - constants::pi)), 1 / a};
         real_type b = poly_eval<2>(cb, s);
-        phi = 1 - std::exp(s * b);
+        phi = 1 - libm::exp(s * b);
     }
     else
     {
@@ -614,7 +614,7 @@ GBX_FUNCTION LPMFunctions calc_lpm(MaterialRecord const& mat,
         real_type a = poly_eval<4>(ca, s);
         real_type const cb[2] = {real_type(-4), -8 / a};
         real_type b = poly_eval<1>(cb, s);
-        real_type psi = 1 - std::exp(s * b);
+        real_type psi = 1 - libm::exp(s * b);
         g = 3 * psi - 2 * phi;
     }
     else if (s < real_type(1.9156))
@@ -624,7 +624,7 @@ GBX_FUNCTION LPMFunctions calc_lpm(MaterialRecord const& mat,
                                 real_type(-1.798138),
                                 real_type(0.672827),
                                 real_type(-0.120772)};
-        g = std::tanh(poly_eval<4>(c, s));
+        g = libm::tanh(poly_eval<4>(c, s));
     }
     else
     {
@@ -677,13 +677,13 @@ GBX_FUNCTION Interaction interact_relativistic_brems(ParamsData const& p,
             real_type eps = term1 * R(ed.epsilon_factor);
             real_type gam2 = ipow<2>(gam);
             real_type eps2 = ipow<2>(eps);
-            real_type phi1 = R(16.863) - 2 * std::log(1 + R(0.311877) * gam2)
-                             + R(2.4) * std::exp(R(-0.9) * gam)
-                             + R(1.6) * std::exp(R(-1.5) * gam);
+            real_type phi1 = R(16.863) - 2 * libm::log(1 + R(0.311877) * gam2)
+                             + R(2.4) * libm::exp(R(-0.9) * gam)
+                             + R(1.6) * libm::exp(R(-1.5) * gam);
             real_type phi2 = 2 / (3 + R(19.5) * gam + 18 * gam2);
-            real_type psi1 = R(24.34) - 2 * std::log(1 + R(13.111641) * eps2)
-                             + R(2.8) * std::exp(R(-8) * eps)
-                             + R(1.2) * std::exp(R(-29.2) * eps);
+            real_type psi1 = R(24.34) - 2 * libm::log(1 + R(13.111641) * eps2)
+                             + R(2.8) * libm::exp(R(-8) * eps)
+                             + R(1.2) * libm::exp(R(-29.2) * eps);
             real_type psi2 = 2 / (3 + 120 * eps + 1200 * eps2);
             dxsec = term0
                         * ((R(0.25) * phi1 - R(ed.fz))

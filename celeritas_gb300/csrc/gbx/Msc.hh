@@ -127,7 +127,7 @@ GBX_FUNCTION GeoPath msc_true_to_geo(ParamsData const& p,
     }
     else if (tstep < range * msc::dtrl)
     {
-        result.step = -lambda * std::expm1(-tstep / lambda);
+        result.step = -lambda * libm::expm1(-tstep / lambda);
     }
     else
     {
@@ -147,7 +147,7 @@ GBX_FUNCTION GeoPath msc_true_to_geo(ParamsData const& p,
             mfp_slope = lambda1 / lambda;
         }
         real_type w = 1 + 1 / (result.alpha * lambda);
-        result.step = (1 - real_type(std::exp(w * std::log(mfp_slope))))
+        result.step = (1 - real_type(libm::exp(w * libm::log(mfp_slope))))
                       / (result.alpha * w);
     }
     result.step = min_of(result.step, tstep);
@@ -168,7 +168,7 @@ GBX_FUNCTION real_type msc_geo_to_true(real_type true_step,
     real_type tstep;
     if (alpha == msc::small_step_alpha)
     {
-        tstep = -lambda * std::log1p(-gstep / lambda);
+        tstep = -lambda * libm::log1p(-gstep / lambda);
         if (tstep < msc::min_step)
         {
             tstep = gstep;
@@ -179,7 +179,7 @@ GBX_FUNCTION real_type msc_geo_to_true(real_type true_step,
         real_type w = 1 + 1 / (alpha * lambda);
         real_type x = alpha * w * gstep;
         x = min_of(x, real_type(1));
-        real_type temp = 1 - std::exp((1 / w) * std::log(1 - x));
+        real_type temp = 1 - libm::exp((1 / w) * libm::log(1 - x));
         real_type result = temp / alpha;
         tstep = min_of(result, range);
     }
@@ -358,16 +358,16 @@ GBX_FORCEINLINE real_type urban_positron_correction(real_type zeff, real_type y)
     real_type corr;
     if (x < xl)
     {
-        corr = a * (1 - std::exp(-b * x));
+        corr = a * (1 - libm::exp(-b * x));
     }
     else if (x > xh)
     {
-        corr = c + d * std::exp(e * (x - 1));
+        corr = c + d * libm::exp(e * (x - 1));
     }
     else
     {
-        real_type yl = a * (1 - std::exp(-b * xl));
-        real_type yh = c + d * std::exp(e * (xh - 1));
+        real_type yl = a * (1 - libm::exp(-b * xl));
+        real_type yh = c + d * libm::exp(e * (xh - 1));
         real_type y0 = (yh - yl) / (xh - xl);
         real_type y1 = yl - y0 * xl;
         corr = y0 * x + y1;
@@ -458,12 +458,12 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
         if (std::fabs(lambda - lambda_end) < lambda * real_type(0.01))
             denom = helper.msc_mfp();
         else
-            denom = (lambda - lambda_end) / std::log(lambda / lambda_end);
+            denom = (lambda - lambda_end) / libm::log(lambda / lambda_end);
         tau = true_path / denom;
         if (tau < msc::tau_big)
         {
-            xmean = std::exp(-tau);
-            x2mean = (1 + 2 * std::exp(real_type(-2.5) * tau)) / 3;
+            xmean = libm::exp(-tau);
+            x2mean = (1 + 2 * libm::exp(real_type(-2.5) * tau)) / 3;
             if (limit_min == 0)
                 limit_min = msc::limit_min;
             limit_min = min_of(limit_min, real_type(p.msc.lambda_limit));
@@ -484,7 +484,7 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
             real_type th = c_highland * std::sqrt(y) * invbetacp;
             real_type const tc[2] = {real_type(md.theta_coeff[0]),
                                      real_type(md.theta_coeff[1])};
-            th *= poly_eval<1>(tc, std::log(y));
+            th *= poly_eval<1>(tc, libm::log(y));
             if (true_path < limit_min)
             {
                 th *= std::sqrt(true_path / limit_min);
@@ -511,7 +511,7 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
             real_type rdm = generate_canonical<real_type>(rng);
             result = 2
                          * (sample_bernoulli<real_type>(p_pow, rng)
-                                ? real_type(std::exp((1 / (a + 1)) * std::log(rdm)))
+                                ? real_type(libm::exp((1 / (a + 1)) * libm::log(rdm)))
                                 : rdm)
                      - 1;
         } while (std::fabs(result) > 1);
@@ -535,16 +535,16 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
     {
         // sample_cos_theta
         real_type maxtau = true_path < limit_min ? limit_min / helper.msc_mfp() : tau;
-        real_type u = std::exp((1 / real_type(6)) * std::log(maxtau));
+        real_type u = libm::exp((1 / real_type(6)) * libm::log(maxtau));
         real_type radlen_mfp = true_path / (tau * real_type(mat.rad_length));
         real_type const tq[3] = {real_type(md.tail_coeff[0]),
                                  real_type(md.tail_coeff[1]),
                                  real_type(md.tail_coeff[2])};
         real_type xsi = poly_eval<2>(tq, u)
-                        + real_type(md.tail_corr) * std::log(radlen_mfp);
+                        + real_type(md.tail_corr) * libm::log(radlen_mfp);
         xsi = max_of(xsi, real_type(1.9));
-        real_type ea = std::exp(-xsi);
-        real_type x = ipow<2>(2 * std::sin(real_type(0.5) * theta0));
+        real_type ea = libm::exp(-xsi);
+        real_type x = ipow<2>(2 * libm::sin(real_type(0.5) * theta0));
         real_type xmean_1 = 1 - x * (1 + (xsi * ea) / (1 - ea));
         if (xmean_1 <= real_type(0.999) * xmean)
         {
@@ -560,7 +560,7 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
             else
                 c = xsi;
             real_type b1 = 2 + (c - xsi) * x;
-            real_type d = std::exp((c - 1) * std::log(c * x / b1));
+            real_type d = libm::exp((c - 1) * libm::log(c * x / b1));
             real_type x0 = 1 - xsi * x;
             real_type xmean_2 = (x0 + d - (c * x - b1 * d) / (c - 2)) / (1 - d);
             real_type f2x0 = (c - 1) / (c * (1 - d));
@@ -573,7 +573,7 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
             else if (generate_canonical<real_type>(rng) < prob)
             {
                 UniformRealDistribution<real_type> sample_inner(ea, 1);
-                costheta = 1 + std::log(sample_inner(rng)) * x;
+                costheta = 1 + libm::log(sample_inner(rng)) * x;
             }
             else
             {
@@ -590,8 +590,8 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
                     costheta = x
                                    * (c - xsi
                                       - c
-                                            * real_type(std::exp(
-                                                (-1 / (c - 1)) * std::log(var + d))))
+                                            * real_type(libm::exp(
+                                                (-1 / (c - 1)) * libm::log(var + d))))
                                + 1;
                 }
             }
@@ -610,11 +610,11 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
             // sample_displacement_dir
             constexpr real_type cbeta = 2.160;
             constexpr real_type cbeta1 = 0.9988703417569197;
-            real_type psi = -std::log(1 - generate_canonical<real_type>(rng) * cbeta1)
+            real_type psi = -libm::log(1 - generate_canonical<real_type>(rng) * cbeta1)
                             / cbeta;
             real_type dphi = phi;
             dphi += sample_bernoulli<real_type>(real_type(0.5), rng) ? psi : -psi;
-            RVec3 dd{std::cos(dphi), std::sin(dphi), 0};
+            RVec3 dd{libm::cos(dphi), libm::sin(dphi), 0};
             dd = rotate(dd, inc_dir);
             displacement = {dd.x * length, dd.y * length, dd.z * length};
             displace = true;

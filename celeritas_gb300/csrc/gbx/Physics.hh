@@ -62,7 +62,7 @@ GBX_FORCEINLINE real_type calc_grid_xs(ParamsData const& p,
 {
     real_type const* values = p.reals + g.value;
     real_type const* energies = p.reals + g.energy;
-    real_type const loge = std::log(energy);
+    real_type const loge = libm::log(energy);
     auto extrapolated = [&](size_type idx) {
         real_type result = values[idx];
         if (idx >= g.prime_index)
@@ -93,11 +93,11 @@ GBX_FORCEINLINE real_type calc_range(ParamsData const& p,
 {
     real_type const* values = p.reals + g.value;
     real_type const* energies = p.reals + g.energy;
-    real_type const loge = std::log(energy);
+    real_type const loge = libm::log(energy);
     if (loge <= g.log_front)
     {
         real_type result = values[0];
-        result *= std::exp(real_type(.5) * (loge - g.log_front));
+        result *= libm::exp(real_type(.5) * (loge - g.log_front));
         return result;
     }
     if (loge >= g.log_back)
@@ -208,7 +208,7 @@ GBX_FORCEINLINE real_type eplusgg_macro_xs(ParamsData const& p,
     real_type result
         = real_type(constants::pi) * ipow<2>(real_type(constants::r_electron))
           * real_type(mat.electron_density)
-          * (poly_eval<2>(quad, gamma + 1) * std::log(gamma + 1 + sqrt_gg2)
+          * (poly_eval<2>(quad, gamma + 1) * libm::log(gamma + 1 + sqrt_gg2)
              - (gamma + 4) * sqrt_gg2)
           / (gamma * ipow<2>(gamma + 2));
     return result;
@@ -407,7 +407,7 @@ GBX_FUNCTION real_type sample_urban_eloss(UrbanFluctRecord const& params,
     real_type xs_exc[2] = {0, 0};
     if (max_energy > real_type(mat.mean_exc_energy))
     {
-        real_type const w = std::log(two_mebsgs) - beta_sq_val;
+        real_type const w = libm::log(two_mebsgs) - beta_sq_val;
         real_type const w_0 = mat.log_mean_exc_energy;
         if (w > w_0)
         {
@@ -438,7 +438,7 @@ GBX_FUNCTION real_type sample_urban_eloss(UrbanFluctRecord const& params,
         }
     }
     real_type xs_ion = mean_loss * (max_energy - e_0)
-                       / (max_energy * e_0 * std::log(max_energy / e_0));
+                       / (max_energy * e_0 * libm::log(max_energy / e_0));
     if (xs_exc[0] + xs_exc[1] > 0)
     {
         xs_ion *= rate;
@@ -483,7 +483,7 @@ GBX_FUNCTION real_type sample_urban_eloss(UrbanFluctRecord const& params,
         {
             alpha = (xs_ion + max_collisions) * energy_ratio
                     / (max_collisions * energy_ratio + xs_ion);
-            real_type const mean_loss_coll = alpha * std::log(alpha) / (alpha - 1);
+            real_type const mean_loss_coll = alpha * libm::log(alpha) / (alpha - 1);
             mean_num_coll = xs_ion * energy_ratio * (alpha - 1)
                             / ((energy_ratio - 1) * alpha);
             real_type const mean = mean_num_coll * mean_loss_coll * e_0;

@@ -244,7 +244,7 @@ template<class T = real_type, class G>
 GBX_FORCEINLINE T sample_exponential(G& rng)
 {
     T const neg_inv_lambda = T{-1} / T{1};
-    return std::log(generate_canonical<T>(rng)) * neg_inv_lambda;
+    return libm::log(generate_canonical<T>(rng)) * neg_inv_lambda;
 }
 
 //! Bernoulli trial: u < p
@@ -268,13 +268,13 @@ struct ReciprocalDistribution
     T a;
     T logratio;
     GBX_FORCEINLINE ReciprocalDistribution(T lo, T hi)
-        : a(lo), logratio(std::log((1 / lo) * hi))
+        : a(lo), logratio(libm::log((1 / lo) * hi))
     {
     }
     template<class G>
     GBX_FORCEINLINE T operator()(G& rng) const
     {
-        return a * std::exp(logratio * generate_canonical<T>(rng));
+        return a * libm::exp(logratio * generate_canonical<T>(rng));
     }
 };
 
@@ -304,10 +304,10 @@ class NormalDistribution
         }
         constexpr T twopi = static_cast<T>(2 * constants::pi);
         T theta = twopi * generate_canonical<T>(rng);
-        T r = std::sqrt(-2 * std::log(generate_canonical<T>(rng)));
-        spare_ = r * std::cos(theta);
+        T r = std::sqrt(-2 * libm::log(generate_canonical<T>(rng)));
+        spare_ = r * libm::cos(theta);
         has_spare_ = true;
-        return gbx_fma(r * std::sin(theta), stddev_, mean_);
+        return gbx_fma(r * libm::sin(theta), stddev_, mean_);
     }
 
   private:
@@ -324,7 +324,7 @@ GBX_FORCEINLINE unsigned int sample_poisson(T lambda, G& rng)
     if (lambda <= 16)
     {
         int k = 0;
-        T p = std::exp(lambda);
+        T p = libm::exp(lambda);
         do
         {
             ++k;

@@ -126,7 +126,7 @@ GBX_FUNCTION void generate_primary(PrimaryGeneratorData const& g,
         double const mu = 2 * generate_canonical<double>(rng) - 1;
         double const phi = 2 * constants::pi * generate_canonical<double>(rng);
         double const sintheta = std::sqrt(1 - mu * mu);
-        p.dir = {sintheta * std::cos(phi), sintheta * std::sin(phi), mu};
+        p.dir = {sintheta * libm::cos(phi), sintheta * libm::sin(phi), mu};
     }
     else
     {

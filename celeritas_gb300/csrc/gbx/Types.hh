@@ -10,17 +10,8 @@
 #include <cmath>
 #include <cstdint>
 
-#if defined(__CUDACC__)
-#    define GBX_FUNCTION __host__ __device__
-#    define GBX_FORCEINLINE __host__ __device__ __forceinline__
-//! Kept out of line: rarely taken code that would otherwise be inlined at
-//! every call site of a hot loop
-#    define GBX_NOINLINE __host__ __device__ __noinline__
-#else
-#    define GBX_FUNCTION
-#    define GBX_FORCEINLINE inline
-#    define GBX_NOINLINE inline
-#endif
+#include "Libm.hh"
+#include "Macros.hh"
 
 #ifndef GBX_PHYS_REAL
 #    define GBX_PHYS_REAL double
@@ -171,7 +162,7 @@ template<class T>
 GBX_FORCEINLINE Vec3<T> from_spherical(T costheta, T phi)
 {
     T const sintheta = std::sqrt(1 - costheta * costheta);
-    return {sintheta * std::cos(phi), sintheta * std::sin(phi), costheta};
+    return {sintheta * libm::cos(phi), sintheta * libm::sin(phi), costheta};
 }
 
 //! Rotate a direction given in the frame whose z axis is 'rot' into the lab

@@ -187,6 +187,10 @@ class CoreState
     std::vector<size_type> event_live(size_type n) const;
     //! Energy deposited in detectors per event [0, n); optionally cleared
     std::vector<double> event_energy_deposition(size_type n, bool clear);
+    //! Energy deposited in each detector per event, events [first, first +
+    //! n), event-major ([n][detectors]); optionally cleared
+    std::vector<double>
+    event_detector_energy_deposition(size_type first, size_type n, bool clear);
     //! Read the step log entries [first, first + n)
     std::vector<StepRecord> step_log(size_type first, size_type n) const;
     size_type log_capacity() const { return ctx_.log_capacity; }
@@ -216,6 +220,7 @@ class CoreState
     size_type pinned_capacity_{0};
     size_type pending_primaries_{0};
     unsigned int seed_{0};
+    size_type ndet_{0};
     //! Primaries inserted so far per event (seeds of per-track streams)
     std::unordered_map<size_type, size_type> primaries_per_event_;
     cudaStream_t stream_{nullptr};

@@ -88,8 +88,8 @@ double calc_mass_rad_coeff(ElementRecord const& el)
             lrad_prime = 5.924;
             break;
         default:
-            lrad = std::log(184.15 * std::pow(z_real, double(-1) / 3));
-            lrad_prime = std::log(1194.0 * std::pow(z_real, double(-2) / 3));
+            lrad = gbx::libm::log(184.15 * std::pow(z_real, double(-1) / 3));
+            lrad_prime = gbx::libm::log(1194.0 * std::pow(z_real, double(-2) / 3));
     }
     constexpr double inv_x0_factor = 4 * constants::alpha_fine_structure
                                      * ipow<2>(constants::r_electron);
@@ -219,8 +219,8 @@ size_type Builder::add_log_grid(std::vector<double> const& x,
     if (x.size() < 2 || x.size() != y.size() || !(x.front() > 0))
         throw std::runtime_error("invalid log grid");
     XsGrid g;
-    g.log_front = std::log(x.front());
-    g.log_back = std::log(x.back());
+    g.log_front = gbx::libm::log(x.front());
+    g.log_back = gbx::libm::log(x.back());
     g.size = static_cast<size_type>(x.size());
     g.log_delta = (g.log_back - g.log_front) / (g.size - 1);
     g.prime_index = invalid_id;
@@ -228,9 +228,9 @@ size_type Builder::add_log_grid(std::vector<double> const& x,
     std::vector<double> energies(g.size + 1);
     for (size_type i = 0; i < g.size; ++i)
     {
-        energies[i] = std::exp(g.log_front + g.log_delta * i);
+        energies[i] = gbx::libm::exp(g.log_front + g.log_delta * i);
     }
-    energies[g.size] = std::exp(g.log_back);
+    energies[g.size] = gbx::libm::exp(g.log_back);
     g.energy = this->add_reals(energies);
     size_type id = static_cast<size_type>(hp_.grids.size());
     hp_.grids.push_back(g);
@@ -364,9 +364,9 @@ void Builder::build_materials()
         el.z = static_cast<int>(kv_.i(p + ".z"));
         el.atomic_mass = kv_.d(p + ".a");
         double const z_real = el.z;
-        el.cbrt_z = std::cbrt(z_real);
-        el.cbrt_zzp = std::cbrt(z_real * (z_real + 1));
-        el.log_z = std::log(z_real);
+        el.cbrt_z = gbx::libm::cbrt(z_real);
+        el.cbrt_zzp = gbx::libm::cbrt(z_real * (z_real + 1));
+        el.log_z = gbx::libm::log(z_real);
         el.coulomb_correction = calc_coulomb_correction(el.z);
         el.mass_radiation_coeff = calc_mass_rad_coeff(el);
         hp_.elements.push_back(el);
@@ -416,7 +416,7 @@ void Builder::build_materials()
             avg_z += frac_z;
             rad_coeff += comps[j].second * el.mass_radiation_coeff;
             log_mean_exc_energy
-                += frac_z * std::log(mean_excitation_energy(el.z));
+                += frac_z * gbx::libm::log(mean_excitation_energy(el.z));
         }
         m.zeff = avg_z;
         m.density = m.number_density * avg_amu_mass * constants::atomic_mass;
@@ -425,7 +425,7 @@ void Builder::build_materials()
         log_mean_exc_energy = avg_z > 0 ? log_mean_exc_energy / avg_z
                                         : -INFINITY;
         m.log_mean_exc_energy = log_mean_exc_energy;
-        m.mean_exc_energy = std::exp(log_mean_exc_energy);
+        m.mean_exc_energy = gbx::libm::exp(log_mean_exc_energy);
         hp_.materials.push_back(m);
 
         // Urban fluctuation parameters
@@ -438,8 +438,8 @@ void Builder::build_materials()
             = std::pow(m.mean_exc_energy
                            / std::pow(f.binding_energy[1], f.oscillator_strength[1]),
                        1 / f.oscillator_strength[0]);
-        f.log_binding_energy[1] = std::log(f.binding_energy[1]);
-        f.log_binding_energy[0] = std::log(f.binding_energy[0]);
+        f.log_binding_energy[1] = gbx::libm::log(f.binding_energy[1]);
+        f.log_binding_energy[0] = gbx::libm::log(f.binding_energy[0]);
         hp_.fluct.push_back(f);
 
         // Production cutoffs per particle
@@ -672,8 +672,8 @@ void Builder::build_models()
             }
             else
             {
-                ff_el = double(std::log(184.15)) - el.log_z / 3;
-                ff_inel = double(std::log(1194.0)) - 2 * el.log_z / 3;
+                ff_el = double(gbx::libm::log(184.15)) - el.log_z / 3;
+                ff_inel = double(gbx::libm::log(1194.0)) - 2 * el.log_z / 3;
             }
             double const fc = el.coulomb_correction;
             double const invz = double(1) / z;
@@ -840,7 +840,7 @@ void Builder::build_msc_field()
         UrbanMscMaterialRecord md;
         md.stepmin_coeff[0] = 1e3 * 27.725 / (1 + 0.203 * zeff);
         md.stepmin_coeff[1] = 1e3 * 6.152 / (1 + 0.111 * zeff);
-        double const z16 = std::exp(1.0 / 6.0 * std::log(zeff));
+        double const z16 = gbx::libm::exp(1.0 / 6.0 * gbx::libm::log(zeff));
         double fz = poly2(0.990395, -0.168386, 0.093286, z16);
         md.theta_coeff[0] = fz * (1 - 8.7780e-2 / zeff);
         md.theta_coeff[1] = fz * (4.0780e-2 + 1.7315e-4 * zeff);
@@ -853,7 +853,7 @@ void Builder::build_msc_field()
         for (int pi = 0; pi < 2; ++pi)
         {
             UrbanMscParMatRecord pm;
-            pm.scaled_zeff = a_coeff[pi] * std::exp(b_coeff[pi] * std::log(zeff));
+            pm.scaled_zeff = a_coeff[pi] * gbx::libm::exp(b_coeff[pi] * gbx::libm::log(zeff));
             pm.d_over_r = 9.6280e-1 - 8.4848e-2 * std::sqrt(zeff) + 4.3769e-3 * zeff;
             hp_.msc_par_mat.push_back(pm);
             int pdg = (pi == 0) ? 11 : -11;

@@ -12,8 +12,9 @@ CUDA streams overlap on the device; ctypes releases the GIL during calls.
 
 Results are reproducible per event: with per-track random streams
 (rng_per_track) every track's random sequence depends only on its ancestry,
-so an event's energy deposition is the same alone and in any mix, up to the
-summation order of the device tally (atomics).
+so an event's energy deposition, in total and in each detector volume, is
+the same alone and in any mix, up to the summation order of the device
+tally (atomics).
 
 The latency of a request is its completion time minus its arrival time, on
 the host's monotonic clock.
@@ -40,6 +41,9 @@ class Request:
     admitted: float | None = None
     completed: float | None = None
     energy_deposition: float | None = None
+    #: Deposition of each detector volume [MeV], in the order of the
+    #: stepper's detector labels
+    detector_deposition: np.ndarray | None = None
 
     @property
     def latency(self) -> float | None:
@@ -135,10 +139,13 @@ class GeometryLane:
             done = [eid for eid in in_flight if live[eid] == 0]
             if done:
                 edep = self.stepper.event_energy_deposition(self.num_events)
+                lo, hi = min(done), max(done)
+                per_det = self.stepper.event_detector_energy_deposition(lo, hi - lo + 1)
                 for eid in done:
                     r = in_flight.pop(eid)
                     r.completed = now
                     r.energy_deposition = float(edep[eid])
+                    r.detector_deposition = per_det[eid - lo].copy()
 
 
 class EventServer:

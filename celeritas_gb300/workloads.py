@@ -43,32 +43,33 @@ WORKLOADS = {
                reentrant_looping=True,
                description="calorimeter 50x(2.3mm Pb+5.7mm lAr), Urban MSC, 1 T "
                            "uniform field along x, 10^4 e- log-uniform 0.1-10 GeV, "
-                           "sigma 1 cm, 2^20 track slots, FP64"),
+                           "sigma 1 cm, 2^20 track slots"),
     # CMS-like detector (concentric shells, 3.8 T along z): 1300 events of
     # 50 primaries, e-/gamma alternating, log-uniform 1-100 GeV, uniform in
     # |eta| < 1.5 from the origin, 2^21 slots
     "c3": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
                emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
                seed=0, events=1300, msc=True, field=(0.0, 0.0, 3.8),
-               bench_primaries=3250, tune_primaries=800,
+               events_per_step=65, tune_primaries=800,
                reentrant_looping=True,
                description="CMS-like: 10 Si shells (0.3 mm, r 4-110 cm), PbWO4 barrel "
                            "(r 129-152 cm), 17 x (5 cm brass + 0.4 cm scintillator) "
-                           "(r 180-295 cm), 3.8 T along z, Urban MSC; events of 50 "
+                           "(r 180-295 cm), 3.8 T along z, Urban MSC; 1300 events of 50 "
                            "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
-                           "one bench step = 65 of the 1300 events; launch "
-                           "configuration autotuned on 16 other events"),
+                           "bench step k transports events [65k, 65k + 65), so 20 "
+                           "steps cover all 1300 events; launch configuration "
+                           "autotuned on 16 other events"),
     # c3 in the synthetic R-Z field map of the CMS-like detector (a 3.8 T
     # solenoid with soft edges and a return flux) instead of the uniform field
     "c3rz": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
                  emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
                  seed=0, events=1300, msc=True, field=(0.0, 0.0, 0.0), rz_field=True,
-                 bench_primaries=3250, tune_primaries=800, reentrant_looping=True,
+                 events_per_step=65, tune_primaries=800, reentrant_looping=True,
                  description="CMS-like detector in an R-Z field map (3.8 T solenoid, soft "
-                             "edges, return flux), Urban MSC; events of 50 e-/gamma, "
-                             "log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; one bench "
-                             "step = 65 events; launch configuration autotuned on 16 "
-                             "other events"),
+                             "edges, return flux), Urban MSC; 1300 events of 50 e-/gamma, "
+                             "log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; bench step "
+                             "k transports events [65k, 65k + 65); launch configuration "
+                             "autotuned on 16 other events"),
     # Batching of uneven events: CMS-like detector, 4096 events with primaries
     # per event log-uniform in 1-1000 and energies log-uniform in
     # 0.1-100 GeV (e-/gamma alternating, |eta| < 1.5), all in flight
@@ -113,6 +114,28 @@ def make_primaries(wl: dict, rank: int = 0, num: int | None = None, seed_offset:
                         num_events=min(wl["events"], num))
     p["event"] += rank * wl["events"]
     return p
+
+
+def step_batches(wl: dict, rank: int, steps: int):
+    """Primaries of each timed bench step and of the warm-up steps.
+
+    A workload with 'events_per_step' splits its events into consecutive
+    batches: timed step k transports batch k (modulo the number of batches),
+    so that as many steps as batches cover every event of the workload once.
+    Warm-up steps transport one batch of other events (another beam seed).
+    Any other workload transports all its primaries in every step.
+    """
+    per_step = wl.get("events_per_step")
+    if not per_step:
+        p = make_primaries(wl, rank, num=wl.get("bench_primaries"))
+        return [p] * steps, p
+    per_event = wl["num_primaries"] // wl["events"]
+    allp = make_primaries(wl, rank)
+    size = per_step * per_event
+    nb = wl["events"] // per_step
+    batches = [allp[k * size:(k + 1) * size] for k in range(nb)]
+    warm = make_primaries(wl, rank, num=size, seed_offset=55)
+    return [batches[k % nb] for k in range(steps)], warm
 
 
 def physics_args(wl: dict) -> list[str]:

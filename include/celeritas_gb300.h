@@ -287,6 +287,19 @@ int gbx_stepper_event_energy_deposition(gbx_stepper* stepper,
                                         size_t num_events,
                                         int clear);
 
+/* Energy deposited in each detector per event [MeV], for events
+ * [first_event, first_event + num_events), with the event_tallies option:
+ * 'out' holds num_events x (number of detectors) values, event-major, in
+ * the detector order of gbx_params_detector_label; 'clear' resets those
+ * tallies after reading. The per-event form of the SimpleCalo tally
+ * (src/celeritas/user/SimpleCalo.hh:40-90 keeps one sum per detector for
+ * the whole run); no counterpart in the reference. */
+int gbx_stepper_event_detector_energy_deposition(gbx_stepper* stepper,
+                                                 double* out,
+                                                 unsigned int first_event,
+                                                 size_t num_events,
+                                                 int clear);
+
 /* Step data recorded for each hit (StepSelection's fields,
  * src/celeritas/user/StepData.hh:19-117, as DetectorStepOutput holds them,
  * src/celeritas/user/DetectorSteps.hh:49-80). The step index, detector and
@@ -405,6 +418,25 @@ int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* va
  * - Kernels are launched on the stepper's stream; the call does not wait
  *   for them. */
 int gbx_stepper_extend_from_secondaries_static(gbx_stepper* stepper);
+
+/* Elementary functions of the FP64 stepping loop (correctly rounded; see
+ * celeritas_gb300/csrc/gbx/Libm.hh), evaluated on the device: y[i] = f(x[i])
+ * for host arrays of n doubles, copied to and from the current device.
+ * No counterpart in the reference, whose host and device builds call their
+ * platforms' own libraries; this entry point lets a caller (or a test) check
+ * that the device results equal the host ones bit for bit. */
+enum
+{
+    GBX_LIBM_EXP = 0,
+    GBX_LIBM_LOG = 1,
+    GBX_LIBM_SIN = 2,
+    GBX_LIBM_COS = 3,
+    GBX_LIBM_TANH = 4,
+    GBX_LIBM_LOG1P = 5,
+    GBX_LIBM_EXPM1 = 6,
+    GBX_LIBM_CBRT = 7
+};
+int gbx_libm_evaluate(int function, const double* x, double* y, size_t n);
 
 #ifdef __cplusplus
 }

@@ -13,6 +13,14 @@ Two checkers live here:
   fixtures; it is the CPU baseline where the reference cannot be built and
   the per-action checker for the GPU kernels.
 
+Both come in two forms: with the host C library's elementary functions
+(exp, log, sin, cos, ...) and with correctly rounded ones ("pinned": the
+reference through ``ref/pinned_libm.cc``, the restatement through the GB300
+build's own ``gbx/Libm.hh``). The FP64 GPU path uses the correctly rounded
+functions, so its bit-for-bit parity is checked against the pinned fixtures
+(``tests/golden/pinned/``); the host C library's fixtures check the
+restatement against the unmodified reference.
+
 Only tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU baseline use
 this package. The shipped GB300 path never calls it.
 """
@@ -26,8 +34,21 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 PORT_DIR = os.path.join(HERE, "_port")
 PORT_BIN = os.path.join(PORT_DIR, "port_stepper")
+#: The restatement with the host C library's elementary functions instead of
+#: the GB300 build's correctly rounded ones (reproduces REF_BIN)
+PORT_SYSLIBM_BIN = os.path.join(PORT_DIR, "port_stepper_syslibm")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
-REFERENCE_DEFAULT = "/root/reference"
+#: The reference harness linked with correctly rounded elementary functions
+REF_PINNED_BIN = os.path.join(HERE, "_ref", "ref_harness_pinned")
+#: Which libm an oracle program uses: "pinned" (correctly rounded, as the
+#: GB300 FP64 build) or "system" (the host C library)
+LIBMS = ("pinned", "system")
+
+
+def reference_path() -> str:
+    """Root of the reference's source tree: $CELERITAS_REFERENCE if set,
+    else the default location of the sources."""
+    return os.environ.get("CELERITAS_REFERENCE", "/root/reference")
 
 
 def _port_sources():
@@ -39,24 +60,32 @@ def _port_sources():
     return srcs, deps
 
 
-def build_port(force: bool = False) -> str:
-    """Compile the CPU restatement with g++ (no FMA contraction)."""
+def build_port(force: bool = False, libm: str = "pinned") -> str:
+    """Compile the CPU restatement with g++ (no FMA contraction), with the
+    correctly rounded elementary functions of the GB300 build ("pinned") or
+    the host C library's ("system")."""
+    if libm not in LIBMS:
+        raise ValueError(f"libm must be one of {LIBMS}")
+    exe = PORT_BIN if libm == "pinned" else PORT_SYSLIBM_BIN
     os.makedirs(PORT_DIR, exist_ok=True)
     srcs, deps = _port_sources()
-    if (not force and os.path.exists(PORT_BIN)
-            and os.path.getmtime(PORT_BIN) >= max(os.path.getmtime(d) for d in deps)):
-        return PORT_BIN
+    if (not force and os.path.exists(exe)
+            and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps)):
+        return exe
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-pthread",
-           "-o", PORT_BIN + ".tmp"] + srcs
+           "-o", exe + ".tmp"] + srcs
+    if libm == "system":
+        cmd.insert(1, "-DGBX_SYSTEM_LIBM")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle port build failed:\n" + res.stderr[-4000:])
-    os.replace(PORT_BIN + ".tmp", PORT_BIN)
-    return PORT_BIN
+    os.replace(exe + ".tmp", exe)
+    return exe
 
 
-def build_reference(reference: str = REFERENCE_DEFAULT, jobs: int = 8) -> str | None:
+def build_reference(reference: str | None = None, jobs: int = 8) -> str | None:
     """Compile the reference harness if the reference sources are present."""
+    reference = reference or reference_path()
     if not os.path.isdir(os.path.join(reference, "src", "celeritas")):
         return None
     cmd = ["make", "-C", os.path.join(HERE, "ref"), f"-j{jobs}", f"REF={reference}"]
@@ -106,9 +135,9 @@ def parse_run_output(text: str) -> dict:
 
 
 def run_port(physics: str, primaries_txt: str, slots: int, seed: int = 0,
-             geometry: str = "calo", extra=()) -> dict:
+             geometry: str = "calo", extra=(), libm: str = "pinned") -> dict:
     """Run the CPU restatement and parse its output."""
-    exe = build_port()
+    exe = build_port(libm=libm)
     cmd = [exe, "run", physics, geometry, primaries_txt, str(slots), str(seed), *extra]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -117,10 +146,27 @@ def run_port(physics: str, primaries_txt: str, slots: int, seed: int = 0,
 
 
 def run_reference(physics: str, primaries_txt: str, slots: int, seed: int = 0,
-                  geometry: str = "calo", extra=()) -> dict:
-    """Run the reference harness (requires build_reference)."""
-    cmd = [REF_BIN, "run", physics, geometry, primaries_txt, str(slots), str(seed), *extra]
+                  geometry: str = "calo", extra=(), libm: str = "system") -> dict:
+    """Run the reference harness (requires build_reference), linked with the
+    host C library ("system") or with correctly rounded elementary functions
+    ("pinned")."""
+    exe = REF_BIN if libm == "system" else REF_PINNED_BIN
+    cmd = [exe, "run", physics, geometry, primaries_txt, str(slots), str(seed), *extra]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("reference harness failed: " + res.stderr[-2000:])
     return parse_run_output(res.stdout)
+
+
+def port_libm(function: str, x, libm: str = "pinned"):
+    """The restatement's FP64 elementary function 'function' (the GB300
+    build's correctly rounded one, or the host C library's) on the host, for
+    every element of x (numpy array of doubles)."""
+    import numpy as np
+
+    exe = build_port(libm=libm)
+    x = np.asarray(x, dtype=np.float64).ravel()
+    text = "".join(f"{float(v).hex()}\n" for v in x)
+    res = subprocess.run([exe, "libm", function], input=text, capture_output=True,
+                         text=True, check=True)
+    return np.array([float.fromhex(t) for t in res.stdout.split()], dtype=np.float64)

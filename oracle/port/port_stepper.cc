@@ -17,7 +17,10 @@
 //
 // Usage:
 //   port_stepper run <physics.txt> calo <primaries.txt> <slots> <seed>
-//                    [--steps N] [--quiet] [--threads T --events E] [--hits]
+//                    [--steps N] [--quiet] [--hits]
+//   port_stepper bench <physics.txt> <geometry> <primaries.txt> <slots> <seed>
+//                    [--threads T] [--event-tallies FILE] [physics options]
+//   port_stepper libm <exp|log|sin|cos|tanh|log1p|expm1|cbrt> < hex doubles
 #include <algorithm>
 #include <array>
 #include <chrono>
@@ -477,11 +480,14 @@ int bench(int argc, char** argv)
     size_type slots = std::stoul(argv[5]);
     unsigned int seed = std::stoul(argv[6]);
     unsigned int threads = 1;
+    std::string tally_path;
     for (int i = 7; i < argc; ++i)
     {
         std::string a = argv[i];
         if (a == "--threads")
             threads = std::stoul(argv[++i]);
+        else if (a == "--event-tallies")
+            tally_path = argv[++i];
     }
     HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
     auto primaries = load_primaries(prim);
@@ -490,12 +496,18 @@ int bench(int argc, char** argv)
     for (auto const& p : primaries)
         events[p.event_id].push_back(p);
     std::vector<std::vector<TrackInitializer>> ev_list;
+    std::vector<size_type> ev_ids;
     for (auto& kv : events)
     {
         for (auto& p : kv.second)
             p.event_id = 0;
+        ev_ids.push_back(kv.first);
         ev_list.push_back(std::move(kv.second));
     }
+    // Per-event deposition of every detector (the change of the stepper's
+    // tally over the event), written after the timed region
+    std::size_t const ndet = hp.detector_labels.size();
+    std::vector<double> ev_edep(tally_path.empty() ? 0 : ev_list.size() * ndet);
     std::vector<unsigned long long> steps(threads, 0);
     std::vector<size_type> done(threads, 0);
     auto t0 = std::chrono::steady_clock::now();
@@ -504,8 +516,11 @@ int bench(int argc, char** argv)
     {
         pool.emplace_back([&, t] {
             PortStepper step(hp, slots, seed + t, 1);
+            std::vector<double> before(ndet);
             for (std::size_t e = t; e < ev_list.size(); e += threads)
             {
+                if (!ev_edep.empty())
+                    before = step.edep();
                 StepCounts c = step(ev_list[e]);
                 steps[t] += c.active;
                 while (c)
@@ -514,6 +529,8 @@ int bench(int argc, char** argv)
                     steps[t] += c.active;
                 }
                 ++done[t];
+                for (std::size_t d = 0; d < ndet && !ev_edep.empty(); ++d)
+                    ev_edep[e * ndet + d] = step.edep()[d] - before[d];
             }
         });
     }
@@ -533,6 +550,20 @@ int bench(int argc, char** argv)
                 nev,
                 total,
                 sec);
+    if (!tally_path.empty())
+    {
+        std::FILE* f = std::fopen(tally_path.c_str(), "w");
+        if (!f)
+            throw std::runtime_error("cannot write " + tally_path);
+        for (std::size_t e = 0; e < ev_list.size(); ++e)
+        {
+            std::fprintf(f, "%u", ev_ids[e]);
+            for (std::size_t d = 0; d < ndet; ++d)
+                std::fprintf(f, " %.17g", ev_edep[e * ndet + d]);
+            std::fprintf(f, "\n");
+        }
+        std::fclose(f);
+    }
     return 0;
 }
 
@@ -552,6 +583,37 @@ int main(int argc, char** argv)
             return run(argc, argv);
         if (mode == "bench")
             return bench(argc, argv);
+        if (mode == "libm" && argc >= 3)
+        {
+            // The FP64 elementary functions of the build (gbx/Libm.hh): one
+            // hexadecimal double per input line, the result per output line
+            std::string fn = argv[2];
+            double x;
+            while (std::scanf("%la", &x) == 1)
+            {
+                double y;
+                if (fn == "exp")
+                    y = gbx::libm::exp(x);
+                else if (fn == "log")
+                    y = gbx::libm::log(x);
+                else if (fn == "sin")
+                    y = gbx::libm::sin(x);
+                else if (fn == "cos")
+                    y = gbx::libm::cos(x);
+                else if (fn == "tanh")
+                    y = gbx::libm::tanh(x);
+                else if (fn == "log1p")
+                    y = gbx::libm::log1p(x);
+                else if (fn == "expm1")
+                    y = gbx::libm::expm1(x);
+                else if (fn == "cbrt")
+                    y = gbx::libm::cbrt(x);
+                else
+                    return 2;
+                std::printf("%a\n", y);
+            }
+            return 0;
+        }
         if (mode == "geo" && argc >= 4)
         {
             // Geometry tables built by the GB300 path's host code

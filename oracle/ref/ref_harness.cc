@@ -13,7 +13,10 @@
 // Usage:
 //   ref_harness run <physics.txt> <geometry> <primaries.txt> <num_slots>
 //               <seed> [--field Bx By Bz] [--msc] [--steps N] [--track-order N] [--trace]
+//   ref_harness bench <physics.txt> <geometry> <primaries.txt> <num_slots>
+//               <seed> [--threads T] [--field Bx By Bz] [--msc] [--max-steps N]
 //   ref_harness geo <physics.txt> <geometry>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -23,6 +26,7 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "corecel/data/CollectionStateStore.hh"
@@ -645,7 +649,8 @@ Problem build_problem(ImportData const& imported,
                       bool msc,
                       TrackOrder track_order,
                       bool print_hits,
-                      std::string const& rz_field)
+                      std::string const& rz_field,
+                      size_type num_streams = 1)
 {
     Problem prob;
     prob.geo = build_geometry(geo_name);
@@ -741,7 +746,7 @@ Problem build_problem(ImportData const& imported,
     params.rng = std::make_shared<RngParams>(seed);
     params.sim = SimParams::from_import(
         imported, params.particle, FieldDriverOptions{}.max_substeps);
-    params.max_streams = 1;
+    params.max_streams = num_streams;
     {
         TrackInitParams::Input input;
         input.capacity = 1u << 22;
@@ -758,7 +763,7 @@ Problem build_problem(ImportData const& imported,
         for (auto const& l : prob.geo.vol_labels)
             labels.push_back(Label{l});
         prob.calo = std::make_shared<SimpleCalo>(
-            std::move(labels), *prob.core->geometry(), 1);
+            std::move(labels), *prob.core->geometry(), num_streams);
         StepCollector::VecInterface ifaces{prob.calo};
         if (print_hits)
         {
@@ -966,6 +971,126 @@ int run(int argc, char** argv)
     return 0;
 }
 
+//! Timed CPU run of the reference's host stepper: events distributed over
+//! threads, one Stepper<host> per thread on its own stream, each event
+//! transported to completion (celer-sim with CELERITAS_OPENMP=event,
+//! app/celer-sim/celer-sim.cc:126-138). A per-event step cap stands in for
+//! celer-sim's max_steps (an event that reaches it is counted as capped).
+int bench(int argc, char** argv)
+{
+    if (argc < 7)
+    {
+        std::cerr << "usage: bench <physics> <geometry> <primaries> <slots> "
+                     "<seed> [--threads T] [--field Bx By Bz] [--msc] "
+                     "[--rz-field FILE] [--max-steps N]\n";
+        return 2;
+    }
+    std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
+    size_type num_slots = std::stoul(argv[5]);
+    unsigned int seed = std::stoul(argv[6]);
+    Real3 field{0, 0, 0};
+    bool msc = false;
+    size_type threads = 1;
+    size_type max_steps = 100000;
+    std::string rz_field;
+    for (int i = 7; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--field")
+        {
+            field = {std::strtod(argv[i + 1], nullptr),
+                     std::strtod(argv[i + 2], nullptr),
+                     std::strtod(argv[i + 3], nullptr)};
+            i += 3;
+        }
+        else if (a == "--msc")
+            msc = true;
+        else if (a == "--threads")
+            threads = std::stoul(argv[++i]);
+        else if (a == "--max-steps")
+            max_steps = std::stoul(argv[++i]);
+        else if (a == "--rz-field")
+            rz_field = argv[++i];
+    }
+    KvFile kv(phys_path);
+    ImportData imported = load_import(kv, msc);
+    Problem prob = build_problem(imported,
+                                 geo_name,
+                                 seed,
+                                 field,
+                                 msc,
+                                 TrackOrder::none,
+                                 false,
+                                 rz_field,
+                                 threads);
+    auto primaries = load_primaries(prim_path, *prob.core->particle());
+    std::map<size_type, std::vector<Primary>> events;
+    for (auto const& p : primaries)
+        events[p.event_id.unchecked_get()].push_back(p);
+    std::vector<std::vector<Primary>> ev_list;
+    for (auto& kv_ev : events)
+    {
+        for (auto& p : kv_ev.second)
+            p.event_id = EventId{0};
+        ev_list.push_back(std::move(kv_ev.second));
+    }
+    std::vector<unsigned long long> steps(threads, 0);
+    std::vector<size_type> done(threads, 0), capped(threads, 0);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (size_type t = 0; t < threads; ++t)
+    {
+        pool.emplace_back([&, t] {
+            StepperInput sinp;
+            sinp.params = prob.core;
+            sinp.stream_id = StreamId{t};
+            sinp.num_track_slots = num_slots;
+            Stepper<MemSpace::host> step(std::move(sinp));
+            for (std::size_t e = t; e < ev_list.size(); e += threads)
+            {
+                StepperResult c = step(make_span(ev_list[e]));
+                steps[t] += c.active;
+                size_type iter = 1;
+                while (c && iter < max_steps)
+                {
+                    c = step();
+                    steps[t] += c.active;
+                    ++iter;
+                }
+                if (c)
+                {
+                    // celer-sim ends a run at its step limit by killing
+                    // the tracks still in flight
+                    step.kill_active();
+                    while (c)
+                        c = step();
+                    ++capped[t];
+                }
+                ++done[t];
+            }
+        });
+    }
+    for (auto& th : pool)
+        th.join();
+    auto t1 = std::chrono::steady_clock::now();
+    unsigned long long total = 0;
+    size_type nev = 0, ncap = 0;
+    for (size_type t = 0; t < threads; ++t)
+    {
+        total += steps[t];
+        nev += done[t];
+        ncap += capped[t];
+    }
+    double sec = std::chrono::duration<double>(t1 - t0).count();
+    std::printf("bench threads %u events %u track_steps %llu seconds %.6f capped %u\n",
+                static_cast<unsigned>(threads),
+                nev,
+                total,
+                sec,
+                ncap);
+    return 0;
+}
+
 int dump_geo(int argc, char** argv)
 {
     if (argc < 4)
@@ -1057,6 +1182,8 @@ int main(int argc, char** argv)
             return run(argc, argv);
         if (mode == "geo")
             return dump_geo(argc, argv);
+        if (mode == "bench")
+            return bench(argc, argv);
     }
     catch (std::exception const& e)
     {

@@ -18,8 +18,12 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 GPU (sm_103a)")
 
 
-def load_golden(name: str) -> dict:
-    with open(os.path.join(GOLDEN, f"{name}.json")) as f:
+def load_golden(name: str, libm: str = "system") -> dict:
+    """A golden fixture of the reference linked with the host C library
+    ("system", tests/golden/) or with correctly rounded elementary functions
+    ("pinned", tests/golden/pinned/)."""
+    folder = GOLDEN if libm == "system" else os.path.join(GOLDEN, "pinned")
+    with open(os.path.join(folder, f"{name}.json")) as f:
         return json.load(f)
 
 

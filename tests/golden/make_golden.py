@@ -11,6 +11,11 @@ geometry and reseeded XORWOW states.
 
 Usage (where the reference sources are present):
     python tests/golden/make_golden.py [--reference /path/to/reference]
+    python tests/golden/make_golden.py --libm pinned   # fixtures under pinned/
+
+With --libm pinned the reference runs with correctly rounded exp, log, sin,
+cos, tanh, log1p, expm1 and cbrt (oracle/ref/pinned_libm.cc), the elementary
+functions of the GB300 build's FP64 path.
 """
 
 from __future__ import annotations
@@ -120,7 +125,7 @@ def case_options(c: dict) -> list[str]:
     return opts
 
 
-def make_case(name: str, hits: bool = False) -> dict:
+def make_case(name: str, hits: bool = False, libm: str = "system") -> dict:
     c = (HIT_CASES if hits else CASES)[name]
     geometry = c.get("geometry", "calo")
     case = {"geometry": geometry, "energy": c["energy"],
@@ -143,7 +148,7 @@ def make_case(name: str, hits: bool = False) -> dict:
         write_primaries_text(ptxt, prim)
         out = oracle.run_reference(physics_file(geometry), ptxt, c["slots"], c["seed"],
                                    extra=case_options(c) + (["--hits"] if hits else []),
-                                   geometry=geometry)
+                                   geometry=geometry, libm=libm)
     if hits:
         per_step = {}
         for h in out["hits"]:
@@ -208,22 +213,30 @@ def geometry_dump() -> dict:
 
 def main():
     parser = argparse.ArgumentParser()
-    parser.add_argument("--reference", default=oracle.REFERENCE_DEFAULT)
+    parser.add_argument("--reference", default=oracle.reference_path())
     parser.add_argument("--cases", nargs="*", default=list(CASES))
     parser.add_argument("--hit-cases", nargs="*", default=list(HIT_CASES))
+    parser.add_argument("--libm", choices=oracle.LIBMS, default="system",
+                        help="the reference linked with the host C library's elementary "
+                             "functions (fixtures here) or with correctly rounded ones "
+                             "(fixtures under pinned/)")
     args = parser.parse_args()
     if oracle.build_reference(args.reference) is None:
         sys.exit("reference sources not found")
+    outdir = HERE if args.libm == "system" else os.path.join(HERE, "pinned")
+    os.makedirs(outdir, exist_ok=True)
     for name in args.cases:
-        data = make_case(name)
-        with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        data = make_case(name, libm=args.libm)
+        with open(os.path.join(outdir, f"{name}.json"), "w") as f:
             json.dump(data, f, indent=0)
         print(name, data["iterations"], data["total_steps"])
     for name in args.hit_cases:
-        data = make_case(name, hits=True)
-        with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        data = make_case(name, hits=True, libm=args.libm)
+        with open(os.path.join(outdir, f"{name}.json"), "w") as f:
             json.dump(data, f, indent=0)
         print(name, data["num_hits"], "hits")
+    if args.libm != "system":
+        return
     with open(os.path.join(HERE, "calo_geometry.json"), "w") as f:
         json.dump(geometry_dump(), f, indent=0)
     with open(os.path.join(HERE, "xorwow_reseed.json"), "w") as f:

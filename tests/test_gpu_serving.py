@@ -3,8 +3,9 @@
 Per-track random streams make every event's result independent of the
 events it shares the device with: each event is served alone, then all are
 served together as one stream of arrivals, and each event's energy
-deposition must agree to 1e-12 relative (the device tally sums with atomics,
-so only the summation order differs). Both precisions are checked.
+deposition, in total and in every detector volume, must agree to 1e-12
+relative (the device tally sums with atomics, so only the summation order
+differs). Both precisions are checked.
 """
 
 import numpy as np
@@ -65,7 +66,7 @@ def test_event_results_same_alone_and_in_mix(gb, precision):
     for r in copy.deepcopy(reqs):
         r.arrival = 0.0
         server.serve([r])
-        alone[r.event_id] = r.energy_deposition
+        alone[r.event_id] = (r.energy_deposition, r.detector_deposition)
     # Mixed: all requests on fresh steppers, arriving together
     server, _ = make_server(gb, precision)
     mixed = copy.deepcopy(reqs)
@@ -75,7 +76,12 @@ def test_event_results_same_alone_and_in_mix(gb, precision):
     assert summary["completed"] == len(reqs)
     for r in mixed:
         assert r.energy_deposition > 0
-        assert r.energy_deposition == pytest.approx(alone[r.event_id], rel=EDEP_RTOL)
+        total, per_volume = alone[r.event_id]
+        assert r.energy_deposition == pytest.approx(total, rel=EDEP_RTOL)
+        # Every detector volume's tally, not only the event's total
+        np.testing.assert_allclose(r.detector_deposition, per_volume, rtol=EDEP_RTOL,
+                                   atol=EDEP_RTOL * total)
+        assert r.detector_deposition.sum() == pytest.approx(total, rel=EDEP_RTOL)
 
 
 def test_served_stream_reports_latency(gb):

@@ -1,14 +1,17 @@
 """GPU stepping loop against the reference's golden fixtures (GB300).
 
 Every case is transported on the device through the C ABI and compared with
-the reference's own host stepping loop on the same inputs: per-step track
-counters (generated, queued, active, alive) and the number of iterations are
-bit-exact. The total deposited energy agrees to 1e-12 relative (the device
+the reference's own host stepping loop on the same inputs, for both sets of
+fixtures: the reference linked with correctly rounded elementary functions
+(the ones the FP64 device code uses, tests/golden/pinned/) and the
+unmodified reference with the host C library's (tests/golden/). Per-step
+track counters (generated, queued, active, alive), the number of iterations
+and the total track-steps are bit-exact in every case, calorimeter and
+CMS-like. The total deposited energy agrees to 1e-12 relative (the device
 tally adds per-slot deposits with atomics, so the summation order differs
-from the reference's slot-ordered sum). Per-volume depositions agree to 1e-9
-relative: the device's double-precision log/exp/sin/cos differ from the host
-C library's in the last bit on some inputs, and with multiple scattering a
-deposit of a few meV can land on the other side of a layer boundary.
+from the reference's slot-ordered sum); per-volume depositions agree to
+1e-11 with the pinned fixtures (summation order only) and to 1e-9 with the
+host library's (whose last-bit differences move them by up to 2.3e-12).
 """
 
 import numpy as np
@@ -59,19 +62,13 @@ def transport(gb, params, case, use_graph=True, batch=32):
     return st, res
 
 
-# CMS-like cases (3.8 T): the field driver scales its steps by exp/log, whose
-# device results differ from the host C library's in the last bit from the
-# first step on; the counters then agree exactly over the early shower and
-# the whole run agrees statistically (the CPU restatement, with the host's
-# exp/log, is bit-exact with the reference on these cases).
-LIBM_EXACT_STEPS = 50
-LIBM_STEPS_RTOL = 0.05
-LIBM_EDEP_RTOL = 0.02
+EDEP_RTOL_PINNED = 1e-11
 
 
+@pytest.mark.parametrize("libm", ["pinned", "system"])
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_matches_reference(gb, name):
-    golden = load_golden(name)
+def test_matches_reference(gb, name, libm):
+    golden = load_golden(name, libm)
     params = params_for(gb, golden["case"])
     st, res = transport(gb, params, golden["case"])
     steps = [[r.generated, r.queued, r.active, r.alive] for r in res]
@@ -79,17 +76,12 @@ def test_matches_reference(gb, name):
     labels = params.detector_labels()
     edep = st.energy_deposition()
     ref = np.array([golden["edep"][k] for k in labels])
-    if golden["case"].get("geometry") == "cms":
-        assert steps[:LIBM_EXACT_STEPS] == golden["steps"][:LIBM_EXACT_STEPS]
-        total = sum(r.active for r in res)
-        assert abs(total - golden["total_steps"]) <= LIBM_STEPS_RTOL * golden["total_steps"]
-        np.testing.assert_allclose(edep.sum(), ref.sum(), rtol=LIBM_EDEP_RTOL)
-        return
     assert steps == golden["steps"]
     assert len(res) == golden["iterations"]
     assert sum(r.active for r in res) == golden["total_steps"]
     np.testing.assert_allclose(edep.sum(), ref.sum(), rtol=TOTAL_RTOL)
-    np.testing.assert_allclose(edep, ref, rtol=EDEP_RTOL, atol=1e-9)
+    rtol = EDEP_RTOL_PINNED if libm == "pinned" else EDEP_RTOL
+    np.testing.assert_allclose(edep, ref, rtol=rtol, atol=1e-9)
 
 
 def test_action_labels(calo_params):
@@ -227,4 +219,5 @@ def test_rzmap_mixed_build(gb):
     res = [st.step(case_primaries(c))] + st.run(max_steps=100000)
     assert res[-1].alive == 0 and res[-1].queued == 0
     ref = sum(golden["edep"].values())
-    np.testing.assert_allclose(st.energy_deposition().sum(), ref, rtol=LIBM_EDEP_RTOL)
+    # Independent FP32 physics: the total within 2% on this small case
+    np.testing.assert_allclose(st.energy_deposition().sum(), ref, rtol=0.02)

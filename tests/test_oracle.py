@@ -1,8 +1,11 @@
 """The CPU oracle against the reference's golden fixtures (no GPU).
 
 The golden fixtures were produced by the reference's own host stepping loop
-(tests/golden/make_golden.py). The CPU restatement must reproduce them bit
-for bit: every per-step counter, the number of iterations, the total
+(tests/golden/make_golden.py), once linked with the host C library's
+elementary functions (tests/golden/) and once with correctly rounded ones
+(tests/golden/pinned/, the functions of the GB300 FP64 path). The CPU
+restatement built with the same functions must reproduce each set bit for
+bit: every per-step counter, the number of iterations, the total
 track-steps and every per-volume energy deposition.
 """
 
@@ -21,7 +24,7 @@ from celeritas_gb300 import physics_file
 from celeritas_gb300.primaries import write_primaries_text
 
 
-def run_case(golden):
+def run_case(golden, libm="pinned"):
     c = golden["case"]
     geometry = c.get("geometry", "calo")
     prim = case_primaries(c)
@@ -29,17 +32,31 @@ def run_case(golden):
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
         return oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
-                               geometry=geometry, extra=case_options(c))
+                               geometry=geometry, extra=case_options(c), libm=libm)
 
 
+@pytest.mark.parametrize("libm", oracle.LIBMS)
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_port_matches_reference(built_port, name):
-    golden = load_golden(name)
-    out = run_case(golden)
+def test_port_matches_reference(built_port, name, libm):
+    golden = load_golden(name, libm)
+    out = run_case(golden, libm)
     assert [list(s) for s in out["steps"]] == golden["steps"]
     assert out["total_steps"] == golden["total_steps"]
     assert out["iterations"] == golden["iterations"]
     assert out["edep"] == golden["edep"]  # bit-exact FP64
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES + ["hits_calo_msc_field_e300_n1",
+                                                 "hits_cms_mix_e2000_n2"])
+def test_reference_counters_independent_of_libm(name):
+    """The reference's own results with the host C library and with
+    correctly rounded elementary functions: identical per-step counters in
+    every case, depositions equal to within the functions' last-bit
+    differences (at most 2.3e-12 relative here)."""
+    system, pinned = load_golden(name, "system"), load_golden(name, "pinned")
+    assert system["steps"] == pinned["steps"]
+    for k, v in system["edep"].items():
+        assert pinned["edep"][k] == pytest.approx(v, rel=1e-11, abs=1e-12)
 
 
 FIELD_CASES = [n for n in GOLDEN_CASES if "field" in n or n.startswith("cms")]
@@ -50,7 +67,7 @@ def test_reentrant_looping_inert_in_normal_transport(built_port, name):
     """The reentrant_looping option only changes tracks that loop and then
     hit a surface they re-enter at once; in the golden transports (fields of
     1-3.8 T, calorimeter and CMS-like) the results stay the reference's."""
-    golden = load_golden(name)
+    golden = load_golden(name, "pinned")
     c = golden["case"]
     geometry = c.get("geometry", "calo")
     prim = case_primaries(c)
@@ -87,7 +104,7 @@ def test_reentrant_looping_ends_grazing_orbit(built_port):
         write_primaries_text(ptxt, p)
         for name, extra in (("reference", []), ("reentrant", ["--reentrant-looping"])):
             runs[name] = oracle.run_port(physics_file("cms"), ptxt, 256, 0, geometry="cms",
-                                         extra=base + extra)
+                                         extra=base + extra, libm="system")
         if os.path.exists(oracle.REF_BIN):
             runs["compiled"] = oracle.run_reference(physics_file("cms"), ptxt, 256, 0,
                                                     geometry="cms", extra=base)
@@ -169,12 +186,13 @@ def hit_summary(hits):
     return [per_step[k] for k in sorted(per_step)]
 
 
+@pytest.mark.parametrize("libm", oracle.LIBMS)
 @pytest.mark.parametrize("name", HIT_CASES)
-def test_port_hits_match_reference(built_port, name):
+def test_port_hits_match_reference(built_port, name, libm):
     """Step output: every step's detector hits (the reference's
     DetectorStepOutput via its own copy_steps) are reproduced bit for bit,
     in the same order, by the restatement's has_step_hit/write_step_hit."""
-    golden = load_golden(name)
+    golden = load_golden(name, libm)
     c = golden["case"]
     geometry = c.get("geometry", "calo")
     prim = case_primaries(c)
@@ -182,7 +200,8 @@ def test_port_hits_match_reference(built_port, name):
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
         out = oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
-                              geometry=geometry, extra=case_options(c) + ["--hits"])
+                              geometry=geometry, extra=case_options(c) + ["--hits"],
+                              libm=libm)
     assert [list(s) for s in out["steps"]] == golden["steps"]
     assert len(out["hits"]) == golden["num_hits"]
     assert out["hits"][:len(golden["records"])] == golden["records"]

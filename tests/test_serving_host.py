@@ -67,6 +67,10 @@ class FakeStepper:
     def event_energy_deposition(self, n, clear=False):
         return self.edep[:n].copy()
 
+    def event_detector_energy_deposition(self, first, n, clear=False):
+        # One detector volume holding the whole deposition
+        return self.edep[first:first + n, None].copy()
+
 
 def request(eid, geometry, energies, arrival):
     p = np.zeros(len(energies), dtype=PRIMARY_DTYPE)
