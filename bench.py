@@ -434,6 +434,7 @@ def measure_served(args, wl, rank, tuning=None):
         stepper.set_tuning(**tuning)
     per_event = wl["num_primaries"] // wl["events"]
     num_events = wl["events"]
+    # The stepper's initializer queue (16 x slots) bounds the tracks pending
     server = serving.EventServer({wl["geometry"]: stepper},
                                  {wl["geometry"]: 16 * wl["slots"]}, 1 << 16)
     allp = make_primaries(wl, rank)
@@ -725,15 +726,27 @@ def run_gb300(args, wl):
                                        clocks, track_order=0, actions=False)
         clocks_summary = clocks.summary()
     head = results[precisions[0]]
+    errors = {}
+
+    def optional(name, fn):
+        """A secondary measurement: its failure is reported in the line
+        instead of losing the headline"""
+        try:
+            return fn()
+        except Exception as e:  # noqa: BLE001
+            errors[name] = f"{type(e).__name__}: {e}"
+            return None
+
     served = None
     if batched and args.served_rates:
-        served = measure_served(args, wl, rank, tuning=tuning)
+        served = optional("served", lambda: measure_served(args, wl, rank, tuning=tuning))
     c2 = None
     if batched and args.c2_steps and args.workload != "c2":
-        c2 = measure_c2(args, dist, rank, local_rank)
+        c2 = optional("c2", lambda: measure_c2(args, dist, rank, local_rank))
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        cpu = cpu_baseline(wl, os.cpu_count() or 1, tallies=True)
+        cpu = optional("cpu_baseline",
+                       lambda: cpu_baseline(wl, os.cpu_count() or 1, tallies=True))
 
     if rank != 0:
         if dist:
@@ -816,8 +829,11 @@ def run_gb300(args, wl):
     if args.primary_generation:
         line["primary_generation"] = measure_primary_generation(wl, rank)
     if cpu is not None:
-        line["gpu_vs_cpu_edep"] = measure_vs_cpu(wl, rank, cpu, labels)
+        line["gpu_vs_cpu_edep"] = optional("gpu_vs_cpu_edep",
+                                           lambda: measure_vs_cpu(wl, rank, cpu, labels))
         line["cpu_baseline"] = {k: v for k, v in cpu.items() if not k.startswith("_")}
+    if errors:
+        line["errors"] = errors
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -45,7 +45,8 @@ class _ParamsOptions(ctypes.Structure):
     _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int),
                 ("track_order", ctypes.c_uint), ("rng_per_track", ctypes.c_int),
                 ("event_tallies", ctypes.c_int), ("reentrant_looping", ctypes.c_int),
-                ("rz_field_file", ctypes.c_char_p)]
+                ("rz_field_file", ctypes.c_char_p), ("brem_combined", ctypes.c_int),
+                ("secondary_stack_factor", ctypes.c_double)]
 
 
 #: Step data of a hit (GBX_STEP_* bits of the C header, the reference's
@@ -243,7 +244,8 @@ class Params:
                  field_tesla=(0.0, 0.0, 0.0), msc: bool = False,
                  track_order: int | str = "none", precision: str = "double",
                  rng_per_track: bool = False, event_tallies: bool = False,
-                 reentrant_looping: bool = False, rz_field: str | None = None):
+                 reentrant_looping: bool = False, rz_field: str | None = None,
+                 brem_combined: bool = False, secondary_stack_factor: float = 0.0):
         lib = load_library(precision=precision)
         self._lib = lib
         self.precision = precision
@@ -260,6 +262,8 @@ class Params:
         opts.reentrant_looping = int(reentrant_looping)
         self._rz_field = rz_field.encode() if rz_field else None
         opts.rz_field_file = self._rz_field
+        opts.brem_combined = int(brem_combined)
+        opts.secondary_stack_factor = float(secondary_stack_factor)
         _check(lib, lib.gbx_params_create(physics.encode(), geometry.encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle

@@ -228,6 +228,13 @@ int gbx_params_create(const char* physics_file,
             inp.options.reentrant_looping = options->reentrant_looping != 0;
             if (options->rz_field_file)
                 inp.options.rz_field_file = options->rz_field_file;
+            inp.options.brem_combined = options->brem_combined != 0;
+            if (options->secondary_stack_factor != 0)
+            {
+                if (!(options->secondary_stack_factor > 0))
+                    throw std::runtime_error("secondary_stack_factor must be positive");
+                inp.options.secondary_stack_factor = options->secondary_stack_factor;
+            }
             for (int i = 0; i < 3; ++i)
                 inp.options.field_tesla[i] = options->field_tesla[i];
         }

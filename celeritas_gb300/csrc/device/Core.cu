@@ -172,7 +172,8 @@ ActionId ActionRegistry::find_action(std::string_view label) const
 void register_core_actions(ActionRegistry* reg,
                            bool uniform_field,
                            bool rz_map,
-                           unsigned int track_order)
+                           unsigned int track_order,
+                           bool brem_combined)
 {
     using O = StepActionOrder;
     auto add = [reg](std::string label,
@@ -197,11 +198,21 @@ void register_core_actions(ActionRegistry* reg,
     implicit("physics-integral-rejected", "reject by integral cross section");
     // Models
     add("ioni-moller-bhabha", "interact by Moller+Bhabha", O::post, step_model);
-    add("brems-sb", "interact by Seltzer-Berger bremsstrahlung", O::post, step_model);
-    add("brems-rel",
-        "interact by relativistic bremsstrahlung",
-        O::post,
-        step_model);
+    if (brem_combined)
+    {
+        add("brems-combined",
+            "interact by bremsstrahlung (combined SB/relativistic, e+/-)",
+            O::post,
+            step_model);
+    }
+    else
+    {
+        add("brems-sb", "interact by Seltzer-Berger bremsstrahlung", O::post, step_model);
+        add("brems-rel",
+            "interact by relativistic bremsstrahlung",
+            O::post,
+            step_model);
+    }
     add("photoel-livermore",
         "interact by Livermore photoelectric effect",
         O::post,
@@ -280,7 +291,8 @@ CoreParams::CoreParams(Input const& inp)
     register_core_actions(actions_.get(),
                           host_.scalars.has_field && !host_.scalars.has_rzmap,
                           host_.scalars.has_rzmap,
-                          host_.scalars.track_order);
+                          host_.scalars.track_order,
+                          host_.scalars.action_combined_brems != invalid_id);
     for (size_type i = 0; i < host_.action_labels.size(); ++i)
     {
         if (actions_->id_to_label(i) != host_.action_labels[i])

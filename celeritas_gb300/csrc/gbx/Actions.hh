@@ -618,7 +618,7 @@ GBX_FUNCTION void interact(ParamsData const& p,
         MaterialRecord const& mat = p.materials[mid];
         size_type const elcomp = s.element[slot];
         if ((action == p.action_bethe_heitler || action == p.action_seltzer_berger
-             || action == p.action_rel_brems)
+             || action == p.action_rel_brems || action == p.action_combined_brems)
             && !(elcomp < mat.num_elements))
         {
             // Element-dependent model without a sampled element (possible
@@ -662,8 +662,13 @@ GBX_FUNCTION void interact(ParamsData const& p,
             result = interact_bethe_heitler(
                 p, p.elements[mat.element[elcomp]], energy, dir, allocate, rng);
         }
-        else if (action == p.action_seltzer_berger)
+        else if (action == p.action_seltzer_berger
+                 || (action == p.action_combined_brems
+                     && energy < seltzer_berger_upper_limit))
         {
+            // CombinedBremInteractor (CombinedBremInteractor.hh:129-160)
+            // samples with Seltzer-Berger below 1 GeV and the relativistic
+            // sampler above, the same final state after either
             result = interact_seltzer_berger(p,
                                              mat.element[elcomp],
                                              mat,
@@ -675,7 +680,7 @@ GBX_FUNCTION void interact(ParamsData const& p,
                                              allocate,
                                              rng);
         }
-        else if (action == p.action_rel_brems)
+        else if (action == p.action_rel_brems || action == p.action_combined_brems)
         {
             result = interact_relativistic_brems(p,
                                                  mat.element[elcomp],

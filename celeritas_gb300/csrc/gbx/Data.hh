@@ -416,6 +416,9 @@ struct ParamsData
     size_type action_moller_bhabha;
     size_type action_seltzer_berger;
     size_type action_rel_brems;
+    //! CombinedBremModel ("brems-combined"): Seltzer-Berger below 1 GeV,
+    //! relativistic above; invalid unless brem_combined
+    size_type action_combined_brems;
     size_type action_livermore_pe;
     size_type action_klein_nishina;
     size_type action_bethe_heitler;

@@ -379,6 +379,11 @@ GBX_FUNCTION Interaction interact_bethe_heitler(ParamsData const& p,
 }
 
 //---------------------------------------------------------------------------//
+//! Energy [MeV] above which the combined bremsstrahlung model samples with
+//! the relativistic model (seltzer_berger_upper_limit, 1 GeV,
+//! src/celeritas/em/interactor/detail/PhysicsConstants.hh)
+constexpr double seltzer_berger_upper_limit = 1000;
+
 // Seltzer-Berger bremsstrahlung
 //---------------------------------------------------------------------------//
 //! Bilinear lookup of the scaled DCS table at (log E, reduced energy)

@@ -354,6 +354,8 @@ class Stepper
 //! the list (CoreParams::build_actions, PhysicsParams actions, models)
 void register_core_actions(ActionRegistry* reg,
                            bool uniform_field,
-                           unsigned int track_order);
+                           bool rz_map,
+                           unsigned int track_order,
+                           bool brem_combined = false);
 
 }  // namespace gbx

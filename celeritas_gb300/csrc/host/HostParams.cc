@@ -176,6 +176,9 @@ class Builder
     GeometrySpec const& geo_;
     ParamsOptions const& opts_;
     HostParams hp_;
+    //! Registered model index of each model kind (the combined
+    //! bremsstrahlung model stands for both bremsstrahlung kinds)
+    size_type model_index_[model_size];
 
     size_type add_reals(std::vector<double> const& v)
     {
@@ -240,28 +243,42 @@ size_type Builder::add_log_grid(std::vector<double> const& x,
 //---------------------------------------------------------------------------//
 void Builder::build_actions()
 {
-    // Registration order of CoreParams/PhysicsParams/Runner (action IDs)
+    // Registration order of CoreParams/PhysicsParams/Runner (action IDs).
+    // The bremsstrahlung process builds either the Seltzer-Berger and the
+    // relativistic models or, with brem_combined, one combined model
+    // (BremsstrahlungProcess.cc:70-95), which shifts every later ID
+    bool const combined = opts_.brem_combined;
     hp_.action_labels = {"pre-step",
                          "msc-range",
                          "eloss-range",
                          "physics-discrete-select",
                          "physics-integral-rejected",
-                         "ioni-moller-bhabha",
-                         "brems-sb",
-                         "brems-rel",
-                         "photoel-livermore",
-                         "scat-klein-nishina",
-                         "conv-bethe-heitler",
-                         "annihil-2-gamma",
-                         "physics-failure",
-                         "along-step-general-linear",
-                         "extend-from-primaries",
-                         "initialize-tracks",
-                         "along-step-neutral",
-                         "geo-propagation-limit",
-                         "geo-boundary",
-                         "tracking-cut",
-                         "extend-from-secondaries"};
+                         "ioni-moller-bhabha"};
+    if (combined)
+    {
+        hp_.action_labels.push_back("brems-combined");
+    }
+    else
+    {
+        hp_.action_labels.push_back("brems-sb");
+        hp_.action_labels.push_back("brems-rel");
+    }
+    for (char const* label : {"photoel-livermore",
+                              "scat-klein-nishina",
+                              "conv-bethe-heitler",
+                              "annihil-2-gamma",
+                              "physics-failure",
+                              "along-step-general-linear",
+                              "extend-from-primaries",
+                              "initialize-tracks",
+                              "along-step-neutral",
+                              "geo-propagation-limit",
+                              "geo-boundary",
+                              "tracking-cut",
+                              "extend-from-secondaries"})
+    {
+        hp_.action_labels.push_back(label);
+    }
     ParamsData& s = hp_.scalars;
     // Optional track-sorting actions (CoreParams.cc:258-283): the step-limit
     // sort is registered before the along-step sort
@@ -292,26 +309,42 @@ void Builder::build_actions()
     hp_.action_labels.push_back("step-gather-pre");
     hp_.action_labels.push_back("step-gather-post");
     s.num_actions = hp_.action_labels.size();
-    s.action_pre_step = 0;
-    s.action_msc_range = 1;
-    s.action_range = 2;
-    s.action_discrete = 3;
-    s.action_integral_rejection = 4;
-    s.model_to_action = 5;
-    s.action_moller_bhabha = 5 + model_moller_bhabha;
-    s.action_seltzer_berger = 5 + model_seltzer_berger;
-    s.action_rel_brems = 5 + model_rel_brems;
-    s.action_livermore_pe = 5 + model_livermore_pe;
-    s.action_klein_nishina = 5 + model_klein_nishina;
-    s.action_bethe_heitler = 5 + model_bethe_heitler;
-    s.action_eplusgg = 5 + model_eplusgg;
-    s.num_models = model_size;
-    s.action_failure = 12;
-    s.action_along_step = 13;
-    s.action_along_step_neutral = 16;
-    s.action_propagation_limit = 17;
-    s.action_boundary = 18;
-    s.action_tracking_cut = 19;
+    auto id = [this](char const* label) {
+        auto const& v = hp_.action_labels;
+        return static_cast<size_type>(std::find(v.begin(), v.end(), label) - v.begin());
+    };
+    s.action_pre_step = id("pre-step");
+    s.action_msc_range = id("msc-range");
+    s.action_range = id("eloss-range");
+    s.action_discrete = id("physics-discrete-select");
+    s.action_integral_rejection = id("physics-integral-rejected");
+    // Registered models: IDs in registration order, the model actions
+    // following each other from model_to_action
+    s.model_to_action = id("ioni-moller-bhabha");
+    size_type next = 0;
+    model_index_[model_moller_bhabha] = next++;
+    model_index_[model_seltzer_berger] = next++;
+    model_index_[model_rel_brems] = combined ? model_index_[model_seltzer_berger] : next++;
+    for (ModelId m : {model_livermore_pe, model_klein_nishina, model_bethe_heitler,
+                      model_eplusgg})
+    {
+        model_index_[m] = next++;
+    }
+    s.num_models = next;
+    s.action_moller_bhabha = id("ioni-moller-bhabha");
+    s.action_seltzer_berger = combined ? invalid_id : id("brems-sb");
+    s.action_rel_brems = combined ? invalid_id : id("brems-rel");
+    s.action_combined_brems = combined ? id("brems-combined") : invalid_id;
+    s.action_livermore_pe = id("photoel-livermore");
+    s.action_klein_nishina = id("scat-klein-nishina");
+    s.action_bethe_heitler = id("conv-bethe-heitler");
+    s.action_eplusgg = id("annihil-2-gamma");
+    s.action_failure = id("physics-failure");
+    s.action_along_step = id("along-step-general-linear");
+    s.action_along_step_neutral = id("along-step-neutral");
+    s.action_propagation_limit = id("geo-propagation-limit");
+    s.action_boundary = id("geo-boundary");
+    s.action_tracking_cut = id("tracking-cut");
 }
 
 void Builder::build_particles()
@@ -469,8 +502,8 @@ void Builder::build_physics()
     s.photoelectric_process = proc_photoelectric;
     s.annihilation_process = proc_annihilation;
     s.photoelectric_table_thresh = 0.2;
-    s.livermore_model = model_livermore_pe;
-    s.eplusgg_model = model_eplusgg;
+    s.livermore_model = model_index_[model_livermore_pe];
+    s.eplusgg_model = model_index_[model_eplusgg];
 
     double const electron_mass = hp_.particles[s.electron_id].mass;
     double const max_e = INFINITY;
@@ -486,18 +519,39 @@ void Builder::build_physics()
     double const sb_upper = 1e3;  // seltzer_berger_upper_limit: 1 GeV
     double const high_limit = 1e8;  // 100 TeV
     std::vector<ModelDef> models = {
-        {model_moller_bhabha, proc_e_ioni, {{e, 0, 100e6}, {ep, 0, 100e6}}},
-        {model_seltzer_berger, proc_e_brems, {{e, 0, sb_upper}, {ep, 0, sb_upper}}},
-        {model_rel_brems,
-         proc_e_brems,
-         {{e, sb_upper, high_limit}, {ep, sb_upper, high_limit}}},
-        {model_livermore_pe, proc_photoelectric, {{g, 0, max_e}}},
-        {model_klein_nishina, proc_compton, {{g, 0, max_e}}},
-        {model_bethe_heitler, proc_conversion, {{g, 2 * electron_mass, 1e8}}},
-        {model_eplusgg, proc_annihilation, {{ep, 0, 1e8}}},
-    };
+        {model_moller_bhabha, proc_e_ioni, {{e, 0, 100e6}, {ep, 0, 100e6}}}};
+    if (opts_.brem_combined)
+    {
+        // CombinedBremModel::applicability (CombinedBremModel.cc:67-79): one
+        // model over the whole range, which picks Seltzer-Berger or the
+        // relativistic sampler per interaction. It has no per-element cross
+        // sections, so every material must hold a single element
+        // (PhysicsParams.cc:660-668)
+        for (auto const& m : hp_.materials)
+        {
+            if (m.num_elements > 1)
+                throw std::runtime_error(
+                    "model 'brems-combined' cannot be used with materials composed of "
+                    "more than one element");
+        }
+        models.push_back({model_seltzer_berger,
+                          proc_e_brems,
+                          {{e, 0, high_limit}, {ep, 0, high_limit}}});
+    }
+    else
+    {
+        models.push_back(
+            {model_seltzer_berger, proc_e_brems, {{e, 0, sb_upper}, {ep, 0, sb_upper}}});
+        models.push_back({model_rel_brems,
+                          proc_e_brems,
+                          {{e, sb_upper, high_limit}, {ep, sb_upper, high_limit}}});
+    }
+    models.push_back({model_livermore_pe, proc_photoelectric, {{g, 0, max_e}}});
+    models.push_back({model_klein_nishina, proc_compton, {{g, 0, max_e}}});
+    models.push_back({model_bethe_heitler, proc_conversion, {{g, 2 * electron_mass, 1e8}}});
+    models.push_back({model_eplusgg, proc_annihilation, {{ep, 0, 1e8}}});
 
-    // particle -> process -> [(lower, upper, model)]
+    // particle -> process -> [(lower, upper, registered model)]
     std::vector<std::map<size_type, std::vector<std::tuple<double, double, size_type>>>>
         particle_models(hp_.particles.size());
     for (auto const& md : models)
@@ -505,7 +559,7 @@ void Builder::build_physics()
         for (auto const& a : md.applic)
         {
             particle_models[a.particle][md.process].push_back(
-                {a.lower, a.upper, md.model});
+                {a.lower, a.upper, model_index_[md.model]});
         }
     }
 
@@ -1024,8 +1078,10 @@ void Builder::build_element_tables()
     // src/celeritas/phys/PhysicsParams.cc:638-768)
     size_type const nmat = static_cast<size_type>(hp_.materials.size());
     size_type const npar = static_cast<size_type>(hp_.particles.size());
-    std::vector<size_type> index(std::size_t(model_size) * npar * nmat, invalid_id);
-    auto build = [&](size_type model, size_type particle, std::string const& prefix) {
+    std::vector<size_type> index(std::size_t(hp_.scalars.num_models) * npar * nmat,
+                                 invalid_id);
+    auto build = [&](ModelId kind, size_type particle, std::string const& prefix) {
+        size_type const model = model_index_[kind];
         for (size_type mi = 0; mi < nmat; ++mi)
         {
             MaterialRecord const& m = hp_.materials[mi];
@@ -1074,6 +1130,8 @@ void Builder::build_element_tables()
     for (size_type pid : {s.electron_id, s.positron_id})
     {
         std::string pdg = pid == s.electron_id ? "11" : "-11";
+        if (hp_.scalars.action_combined_brems != invalid_id)
+            continue;  // single-element materials only: nothing to select
         build(model_seltzer_berger, pid, "model." + pdg + ".e_brems.e_brems_sb");
         build(model_rel_brems, pid, "model." + pdg + ".e_brems.e_brems_lpm");
     }

@@ -3,8 +3,9 @@
 Events (requests) arrive at given times, each with its own primaries and
 geometry. Every geometry has one stepper: a fixed pool of device track slots
 plus a queue of track initializers. A request is admitted as soon as it has
-arrived and its estimated footprint in the queue fits beside the tracks
-already in flight; its primaries join the running step loop (continuous
+arrived and its estimated footprint in the queue fits beside the capacity
+held by the events already in flight (their estimated peaks while their
+showers grow, their live tracks once past the peak); its primaries join the running step loop (continuous
 batching: in-flight events keep stepping while new ones enter), and it
 completes when it has no live track left (occupied slot or queued
 initializer). Each stepper is driven by its own host thread, so the steppers'
@@ -52,7 +53,11 @@ class Request:
         return self.completed - self.arrival
 
     def footprint(self, initializers_per_mev: float) -> float:
-        """Estimated peak queued initializers of this event."""
+        """Estimated peak queued initializers of this event: the pending-track
+        queue is the device memory that an event's shower fills (the
+        secondary stack, secondary_stack_factor x slots as in the
+        reference's PhysicsData.hh:250,501-502, takes at most two
+        secondaries per track and step and cannot overflow at factor 3)."""
         return float(self.primaries["energy"].sum()) * initializers_per_mev
 
 
@@ -60,8 +65,11 @@ class Request:
 class ServerOptions:
     #: Steps per graph-replayed batch between admissions and completion checks
     steps_per_batch: int = 16
-    #: Estimated queue footprint per MeV of primary energy (conservative)
-    initializers_per_mev: float = 0.3
+    #: Estimated peak queue footprint per MeV of primary energy (the c3
+    #: events peak at about 0.26 pending tracks per MeV)
+    initializers_per_mev: float = 0.35
+    #: Capacity held for an event past its peak, per live track
+    past_peak_margin: float = 1.25
     #: Fraction of the initializer queue that admitted events may fill
     queue_fill: float = 0.7
     #: Cap on primaries inserted in one step
@@ -94,26 +102,36 @@ class GeometryLane:
     def _run(self):
         pending = sorted(self.requests, key=lambda r: r.arrival)
         in_flight: dict[int, Request] = {}
+        # Queue capacity held for each event in flight: its estimated peak
+        # footprint while its live-track count grows, then (past the peak of
+        # its shower) its live tracks, which only shrink from there
+        reserved: dict[int, float] = {}
+        last_live: dict[int, int] = {}
         queued = 0
         deadline = self.opt.timeout
         while pending or in_flight:
             now = self.clock()
             if now > deadline:
                 raise TimeoutError("serving run exceeded its time limit")
-            # Admission: arrived requests whose footprint fits, in order
+            # Admission: arrived requests whose footprint fits beside the
+            # capacity held by the events in flight and beside the tracks
+            # actually queued, in arrival order
             batch = []
             nprim = 0
             limit = self.opt.queue_fill * self.capacity
+            held = sum(reserved.values())
             while pending and pending[0].arrival <= now:
                 r = pending[0]
                 need = r.footprint(self.opt.initializers_per_mev)
-                if in_flight and queued + need > limit:
+                if in_flight and max(held, queued) + need > limit:
                     break
                 if nprim + len(r.primaries) > self.opt.max_primaries_per_insert and batch:
                     break
                 pending.pop(0)
                 r.admitted = now
                 in_flight[r.event_id] = r
+                reserved[r.event_id] = need
+                held += need
                 queued += need
                 batch.append(r.primaries)
                 nprim += len(r.primaries)
@@ -136,7 +154,17 @@ class GeometryLane:
             # Completion: events with no live track
             live = self.stepper.event_live(self.num_events)
             now = self.clock()
+            for eid in in_flight:
+                n = int(live[eid])
+                if n < last_live.get(eid, 0):
+                    reserved[eid] = min(reserved[eid], self.opt.past_peak_margin * n)
+                else:
+                    reserved[eid] = max(reserved[eid], float(n))
+                last_live[eid] = n
             done = [eid for eid in in_flight if live[eid] == 0]
+            for eid in done:
+                reserved.pop(eid, None)
+                last_live.pop(eid, None)
             if done:
                 edep = self.stepper.event_energy_deposition(self.num_events)
                 lo, hi = min(done), max(done)

@@ -106,6 +106,17 @@ typedef struct
      * max_r' [cm], then 'Bz Br' [tesla] per node, z-major ([Z][R], the
      * order of RZMapFieldInput, src/celeritas/field/RZMapFieldInput.hh). */
     const char* rz_field_file;
+    /* RunnerInput::brem_combined (app/celer-sim/RunnerInput.hh:120):
+     * nonzero registers the combined bremsstrahlung model
+     * (CombinedBremModel, "brems-combined": Seltzer-Berger below 1 GeV,
+     * relativistic above) in place of "brems-sb" and "brems-rel"; every
+     * material must then hold a single element (otherwise an error, as
+     * PhysicsParams.cc:660-668 raises). */
+    int brem_combined;
+    /* RunnerInput::secondary_stack_factor: secondaries per track slot held
+     * by the per-step secondary stack (PhysicsParams.hh:250,501-502); zero
+     * takes the reference's default, 3. */
+    double secondary_stack_factor;
 } gbx_params_options;
 
 /* Build problem parameters from a physics input file and a named geometry

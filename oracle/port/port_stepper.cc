@@ -326,7 +326,8 @@ class PortStepper
 //! --track-order N (changes the registered actions only: the host loop's
 //! results do not depend on the thread order), --reentrant-looping (a
 //! reentrant boundary step keeps the looping-step count; off in the
-//! reference)
+//! reference), --rz-field FILE, --brem-combined (one combined
+//! bremsstrahlung model, RunnerInput::brem_combined)
 ParamsOptions physics_options(int argc, char** argv)
 {
     ParamsOptions opts;
@@ -351,6 +352,10 @@ ParamsOptions physics_options(int argc, char** argv)
         else if (a == "--rz-field" && i + 1 < argc)
         {
             opts.rz_field_file = argv[i + 1];
+        }
+        else if (a == "--brem-combined")
+        {
+            opts.brem_combined = true;
         }
     }
     return opts;

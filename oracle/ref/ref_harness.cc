@@ -13,6 +13,7 @@
 // Usage:
 //   ref_harness run <physics.txt> <geometry> <primaries.txt> <num_slots>
 //               <seed> [--field Bx By Bz] [--msc] [--steps N] [--track-order N] [--trace]
+//               [--brem-combined] [--rz-field FILE] [--hits] [--reseed N]
 //   ref_harness bench <physics.txt> <geometry> <primaries.txt> <num_slots>
 //               <seed> [--threads T] [--field Bx By Bz] [--msc] [--max-steps N]
 //   ref_harness geo <physics.txt> <geometry>
@@ -650,7 +651,8 @@ Problem build_problem(ImportData const& imported,
                       TrackOrder track_order,
                       bool print_hits,
                       std::string const& rz_field,
-                      size_type num_streams = 1)
+                      size_type num_streams = 1,
+                      bool brem_combined = false)
 {
     Problem prob;
     prob.geo = build_geometry(geo_name);
@@ -689,7 +691,8 @@ Problem build_problem(ImportData const& imported,
         input.options.lowest_electron_energy = PhysicsParamsOptions::Energy(
             imported.em_params.lowest_electron_energy);
         ProcessBuilder::Options opts;
-        opts.brem_combined = false;
+        // RunnerInput::brem_combined (app/celer-sim/RunnerInput.hh:120)
+        opts.brem_combined = brem_combined;
         opts.brems_selection = BremsModelSelection::all;
         ProcessBuilder build_process(
             imported, params.particle, params.material, opts);
@@ -853,7 +856,7 @@ int run(int argc, char** argv)
         std::cerr << "usage: run <physics> <geometry> <primaries> <slots> "
                      "<seed> [--field Bx By Bz] [--msc] [--steps N] "
                      "[--track-order N] [--reseed EVENT] [--dump-rng N] [--hits] "
-                     "[--rz-field FILE]\n";
+                     "[--rz-field FILE] [--brem-combined]\n";
         return 2;
     }
     std::string phys_path = argv[2], geo_name = argv[3], prim_path = argv[4];
@@ -867,6 +870,7 @@ int run(int argc, char** argv)
     long long reseed = -1;
     size_type dump_rng = 0;
     bool print_hits = false;
+    bool brem_combined = false;
     std::string rz_field;
     for (int i = 7; i < argc; ++i)
     {
@@ -894,13 +898,22 @@ int run(int argc, char** argv)
             print_hits = true;
         else if (a == "--rz-field")
             rz_field = argv[++i];
+        else if (a == "--brem-combined")
+            brem_combined = true;
     }
 
     KvFile kv(phys_path);
     ImportData imported = load_import(kv, msc);
-    Problem prob
-        = build_problem(
-            imported, geo_name, seed, field, msc, track_order, print_hits, rz_field);
+    Problem prob = build_problem(imported,
+                                 geo_name,
+                                 seed,
+                                 field,
+                                 msc,
+                                 track_order,
+                                 print_hits,
+                                 rz_field,
+                                 1,
+                                 brem_combined);
     auto primaries = load_primaries(prim_path, *prob.core->particle());
 
     StepperInput sinp;

