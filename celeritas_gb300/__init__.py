@@ -41,12 +41,26 @@ class _Primary(ctypes.Structure):
     ]
 
 
+#: FieldDriverOptions members in the order of gbx_field_driver_options
+FIELD_OPTION_NAMES = ("minimum_step", "delta_chord", "delta_intersection", "epsilon_step",
+                      "epsilon_rel_max", "errcon", "pgrow", "pshrink", "safety",
+                      "max_stepping_increase", "max_stepping_decrease", "max_nsteps",
+                      "max_substeps")
+
+
+class _FieldDriverOptions(ctypes.Structure):
+    _fields_ = ([(n, ctypes.c_double) for n in FIELD_OPTION_NAMES[:-2]]
+                + [("max_nsteps", ctypes.c_int), ("max_substeps", ctypes.c_int)])
+
+
 class _ParamsOptions(ctypes.Structure):
     _fields_ = [("field_tesla", ctypes.c_double * 3), ("msc", ctypes.c_int),
                 ("track_order", ctypes.c_uint), ("rng_per_track", ctypes.c_int),
                 ("event_tallies", ctypes.c_int), ("reentrant_looping", ctypes.c_int),
                 ("rz_field_file", ctypes.c_char_p), ("brem_combined", ctypes.c_int),
-                ("secondary_stack_factor", ctypes.c_double)]
+                ("secondary_stack_factor", ctypes.c_double),
+                ("field_options", ctypes.POINTER(_FieldDriverOptions)),
+                ("initializer_capacity", ctypes.c_uint)]
 
 
 #: Step data of a hit (GBX_STEP_* bits of the C header, the reference's
@@ -165,6 +179,9 @@ _PROTOTYPES = [
     ("gbx_stepper_event_detector_energy_deposition", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint, ctypes.c_size_t,
       ctypes.c_int]),
+    ("gbx_stepper_warm_up", ctypes.c_int, [ctypes.c_void_p]),
+    ("gbx_field_driver_options_default", None, [ctypes.POINTER(_FieldDriverOptions)]),
+    ("gbx_device_allocations", ctypes.c_int, [ctypes.POINTER(ctypes.c_ulonglong)]),
     ("gbx_libm_evaluate", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
       ctypes.c_size_t]),
@@ -232,6 +249,19 @@ def field_map_file(problem: str = "cms") -> str:
     return os.path.join(DATA_DIR, f"{problem}.rzmap.txt")
 
 
+def geometry_path(geometry: str) -> str:
+    """The geometry argument of Params and the oracle programs: a built-in
+    name ("calo", "cms") as is, a geometry file of the package's data
+    directory (name ending in .geo) as its path, any other path as is."""
+    if geometry in ("calo", "cms"):
+        return geometry
+    if geometry.endswith(".geo") and not os.path.isabs(geometry):
+        cand = os.path.join(DATA_DIR, geometry)
+        if os.path.exists(cand):
+            return cand
+    return geometry
+
+
 def physics_file(problem: str) -> str:
     """Path of a committed synthetic physics input ("calo" or "cms")."""
     return os.path.join(DATA_DIR, f"{problem}.physics.txt")
@@ -245,7 +275,8 @@ class Params:
                  track_order: int | str = "none", precision: str = "double",
                  rng_per_track: bool = False, event_tallies: bool = False,
                  reentrant_looping: bool = False, rz_field: str | None = None,
-                 brem_combined: bool = False, secondary_stack_factor: float = 0.0):
+                 brem_combined: bool = False, secondary_stack_factor: float = 0.0,
+                 field_options: dict | None = None, initializer_capacity: int = 0):
         lib = load_library(precision=precision)
         self._lib = lib
         self.precision = precision
@@ -264,7 +295,20 @@ class Params:
         opts.rz_field_file = self._rz_field
         opts.brem_combined = int(brem_combined)
         opts.secondary_stack_factor = float(secondary_stack_factor)
-        _check(lib, lib.gbx_params_create(physics.encode(), geometry.encode(),
+        opts.initializer_capacity = int(initializer_capacity)
+        if field_options:
+            # FieldDriverOptions: the reference's defaults, then the given
+            # members (lengths in cm)
+            fo = _FieldDriverOptions()
+            lib.gbx_field_driver_options_default(ctypes.byref(fo))
+            for name, value in field_options.items():
+                if name not in FIELD_OPTION_NAMES:
+                    raise GbxError(f"unknown field driver option '{name}'")
+                setattr(fo, name, int(value) if name.startswith("max_n") or
+                        name == "max_substeps" else float(value))
+            self._field_options = fo
+            opts.field_options = ctypes.pointer(fo)
+        _check(lib, lib.gbx_params_create(physics.encode(), geometry_path(geometry).encode(),
                                      ctypes.byref(opts), ctypes.byref(handle)))
         self._handle = handle
         self.geometry = geometry
@@ -373,6 +417,11 @@ class Stepper:
 
     def synchronize(self):
         _check(self._lib, self._lib.gbx_stepper_synchronize(self._handle))
+
+    def warm_up(self):
+        """Stepper::warm_up: one step over the empty state (kernels loaded,
+        step graphs captured); the state must hold no tracks."""
+        _check(self._lib, self._lib.gbx_stepper_warm_up(self._handle))
 
     def kill_active(self):
         _check(self._lib, self._lib.gbx_stepper_kill_active(self._handle))
@@ -560,3 +609,11 @@ class Stepper:
         data = np.ascontiguousarray(data)
         _check(self._lib, self._lib.gbx_stepper_copy_state(self._handle, field.encode(),
                                            data.ctypes.data_as(ctypes.c_void_p), data.nbytes, 1))
+
+
+def device_allocations(precision: str = "double") -> int:
+    """Device allocations (cudaMalloc calls) made so far by the library."""
+    lib = load_library(precision=precision)
+    n = ctypes.c_ulonglong()
+    _check(lib, lib.gbx_device_allocations(ctypes.byref(n)))
+    return int(n.value)

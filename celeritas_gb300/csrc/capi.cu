@@ -16,11 +16,13 @@
 struct gbx_params_s
 {
     std::shared_ptr<gbx::CoreParams const> params;
+    unsigned int initializer_capacity{0};  //!< Queue of each stepper (0: default)
 };
 
 struct gbx_stepper_s
 {
     std::unique_ptr<gbx::Stepper> stepper;
+    int device{-1};  //!< Device current when the stepper was created
 };
 
 namespace
@@ -208,6 +210,26 @@ const char* gbx_last_error(void)
     return g_last_error.c_str();
 }
 
+void gbx_field_driver_options_default(gbx_field_driver_options* options)
+{
+    if (!options)
+        return;
+    gbx::FieldOptions const o;
+    options->minimum_step = o.minimum_step;
+    options->delta_chord = o.delta_chord;
+    options->delta_intersection = o.delta_intersection;
+    options->epsilon_step = o.epsilon_step;
+    options->epsilon_rel_max = o.epsilon_rel_max;
+    options->errcon = o.errcon;
+    options->pgrow = o.pgrow;
+    options->pshrink = o.pshrink;
+    options->safety = o.safety;
+    options->max_stepping_increase = o.max_stepping_increase;
+    options->max_stepping_decrease = o.max_stepping_decrease;
+    options->max_nsteps = o.max_nsteps;
+    options->max_substeps = o.max_substeps;
+}
+
 int gbx_params_create(const char* physics_file,
                       const char* geometry,
                       const gbx_params_options* options,
@@ -229,6 +251,26 @@ int gbx_params_create(const char* physics_file,
             if (options->rz_field_file)
                 inp.options.rz_field_file = options->rz_field_file;
             inp.options.brem_combined = options->brem_combined != 0;
+            if (auto const* f = options->field_options)
+            {
+                gbx::FieldOptions& o = inp.options.field_options;
+                o.minimum_step = f->minimum_step;
+                o.delta_chord = f->delta_chord;
+                o.delta_intersection = f->delta_intersection;
+                o.epsilon_step = f->epsilon_step;
+                o.epsilon_rel_max = f->epsilon_rel_max;
+                o.errcon = f->errcon;
+                o.pgrow = f->pgrow;
+                o.pshrink = f->pshrink;
+                o.safety = f->safety;
+                o.max_stepping_increase = f->max_stepping_increase;
+                o.max_stepping_decrease = f->max_stepping_decrease;
+                if (f->max_nsteps <= 0 || f->max_nsteps > 32767 || f->max_substeps <= 0
+                    || f->max_substeps > 32767)
+                    throw std::runtime_error("invalid field driver options");
+                o.max_nsteps = static_cast<short>(f->max_nsteps);
+                o.max_substeps = static_cast<short>(f->max_substeps);
+            }
             if (options->secondary_stack_factor != 0)
             {
                 if (!(options->secondary_stack_factor > 0))
@@ -240,6 +282,8 @@ int gbx_params_create(const char* physics_file,
         }
         auto p = std::make_unique<gbx_params_s>();
         p->params = std::make_shared<gbx::CoreParams>(inp);
+        if (options)
+            p->initializer_capacity = options->initializer_capacity;
         *out = p.release();
     });
 }
@@ -299,8 +343,19 @@ int gbx_stepper_create(gbx_params* params,
         inp.num_track_slots = num_track_slots;
         inp.seed = seed;
         inp.use_graph = use_graph != 0;
+        inp.initializer_capacity = params->initializer_capacity;
         auto s = std::make_unique<gbx_stepper_s>();
         s->stepper = std::make_unique<gbx::Stepper>(inp);
+        if (cudaError_t err = cudaGetDevice(&s->device); err != cudaSuccess)
+            throw std::runtime_error(cudaGetErrorString(err));
+        if (num_track_slots <= GBX_STATIC_SCRATCH_MAX_SLOTS)
+        {
+            // Set up the static scratch of
+            // gbx_stepper_extend_from_secondaries_static now, so that its
+            // later calls do no lookup (that entry point still looks up
+            // lazily if this is skipped)
+            gbx::static_scratch_for_current_device();
+        }
         *out = s.release();
     });
 }
@@ -568,6 +623,18 @@ static_assert(GBX_STATIC_SCRATCH_MAX_SLOTS == gbx::static_scratch_max_slots,
 int gbx_stepper_extend_from_secondaries_static(gbx_stepper* stepper)
 {
     return guarded([&] {
+        if (!stepper)
+            throw std::runtime_error("null argument");
+        int device = -1;
+        if (cudaError_t err = cudaGetDevice(&device); err != cudaSuccess)
+            throw std::runtime_error(cudaGetErrorString(err));
+        if (device != stepper->device)
+        {
+            throw std::runtime_error(
+                "the stepper was created on device " + std::to_string(stepper->device)
+                + " but device " + std::to_string(device)
+                + " is current: make the stepper's device current first");
+        }
         auto& state = stepper->stepper->state();
         gbx::launch_extend_from_secondaries_static(state.context(), state.stream());
         if (cudaError_t err = cudaGetLastError(); err != cudaSuccess)
@@ -593,7 +660,7 @@ int gbx_libm_evaluate(int function, const double* x, double* y, size_t n)
                 throw std::runtime_error(cudaGetErrorString(err));
             }
         };
-        check(cudaMalloc(&buf, 2 * n * sizeof(double)));
+        check(gbx::device_malloc(reinterpret_cast<void**>(&buf), 2 * n * sizeof(double)));
         check(cudaMemcpy(buf, x, n * sizeof(double), cudaMemcpyHostToDevice));
         unsigned int const blocks
             = static_cast<unsigned int>(std::min<size_t>((n + 255) / 256, 4096));
@@ -601,6 +668,24 @@ int gbx_libm_evaluate(int function, const double* x, double* y, size_t n)
         check(cudaGetLastError());
         check(cudaMemcpy(y, buf + n, n * sizeof(double), cudaMemcpyDeviceToHost));
         check(cudaFree(buf));
+    });
+}
+
+int gbx_device_allocations(unsigned long long* count)
+{
+    return guarded([&] {
+        if (!count)
+            throw std::runtime_error("null argument");
+        *count = gbx::device_allocation_count();
+    });
+}
+
+int gbx_stepper_warm_up(gbx_stepper* stepper)
+{
+    return guarded([&] {
+        if (!stepper)
+            throw std::runtime_error("null argument");
+        stepper->stepper->warm_up();
     });
 }
 

@@ -4,6 +4,7 @@
 #include "../gbx/Random.hh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <stdexcept>
 
@@ -147,6 +148,25 @@ void step_sort_post(CoreParams const&, CoreState& state, ActionId)
 }
 
 }  // namespace
+
+//---------------------------------------------------------------------------//
+// Device allocations (counted)
+//---------------------------------------------------------------------------//
+namespace
+{
+std::atomic<unsigned long long> g_device_allocations{0};
+}  // namespace
+
+cudaError_t device_malloc(void** ptr, std::size_t bytes)
+{
+    ++g_device_allocations;
+    return cudaMalloc(ptr, bytes);
+}
+
+unsigned long long device_allocation_count()
+{
+    return g_device_allocations.load();
+}
 
 //---------------------------------------------------------------------------//
 // ActionRegistry and registration
@@ -330,7 +350,7 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_vd = pk.add(h.volume_detector);
 
     auto const& bytes = pk.bytes();
-    GBX_CUDA(cudaMalloc(&device_storage_, bytes.size()));
+    GBX_CUDA(device_malloc(&device_storage_, bytes.size()));
     GBX_CUDA(cudaMemcpy(
         device_storage_, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
     auto* base = static_cast<unsigned char*>(device_storage_);
@@ -454,7 +474,7 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_log = L.reserve(sizeof(StepRecord) * log_cap);
     std::size_t o_stepidx = L.reserve(sizeof(size_type));
 
-    GBX_CUDA(cudaMalloc(&storage_, L.size()));
+    GBX_CUDA(device_malloc(&storage_, L.size()));
     GBX_CUDA(cudaMemsetAsync(storage_, 0, L.size(), stream_));
     auto* b = static_cast<unsigned char*>(storage_);
     auto at = [b](std::size_t off) { return static_cast<void*>(b + off); };
@@ -665,7 +685,7 @@ void CoreState::set_step_output(unsigned int selection,
                       o_qdir = hit_array(step_post_dir, 24),
                       o_qen = hit_array(step_post_energy, 8);
     std::size_t const o_blocks = L.reserve(4 * std::size_t(nblocks));
-    GBX_CUDA(cudaMalloc(&hits_storage_, L.size()));
+    GBX_CUDA(device_malloc(&hits_storage_, L.size()));
     GBX_CUDA(cudaMemsetAsync(hits_storage_, 0, L.size(), stream_));
     auto* b = static_cast<unsigned char*>(hits_storage_);
     auto at = [b](std::size_t off) -> void* {
@@ -1257,6 +1277,39 @@ std::vector<StepperResult> Stepper::run_until_empty(size_type max_steps,
         taken += n;
     }
     return results;
+}
+
+void Stepper::warm_up()
+{
+    Counters c = state_->counters();
+    if (c.num_active != 0 || c.num_initializers != 0 || state_->pending_primaries() != 0)
+        throw std::runtime_error("cannot warm up when state has active tracks");
+    // Both sort states when the sort threshold switches between them
+    bool const sorted = state_->context().sort_enabled;
+    auto one_step = [this] {
+        if (use_graph_ && !actions_->action_times_enabled())
+        {
+            int const k = state_->context().sort_enabled ? 1 : 0;
+            if (!graph_exec_[k])
+                this->build_graph();
+            GBX_CUDA(cudaGraphLaunch(graph_exec_[k], stream_));
+        }
+        else
+        {
+            actions_->step(*params_, *state_);
+        }
+    };
+    one_step();
+    if (sort_threshold_ > 0 && params_->host().scalars.track_order != 0)
+    {
+        state_->set_tuning("sort", !sorted);
+        one_step();
+        state_->set_tuning("sort", sorted);
+    }
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    c = state_->counters();
+    if (c.num_active != 0 || c.num_initializers != 0)
+        throw std::runtime_error("warm-up step left tracks in the state");
 }
 
 void Stepper::reseed(unsigned long long event_id)

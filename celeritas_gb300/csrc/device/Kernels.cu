@@ -698,7 +698,7 @@ __global__ GBX_ALONG_BOUNDS(1) void along_charged_persistent_kernel(
     size_type const first = offsets ? offsets[bin] : 0;
     size_type const count = offsets ? offsets[bin + 1] - first : s.size;
     unsigned int const lane = threadIdx.x & 31u;
-    FieldOptions const opt;
+    FieldOptions const& opt = p.field_options;
     FieldPropagation fp(opt, UniformFieldEquation{});
     size_type slot = invalid_id;
     bool have = false;
@@ -1044,6 +1044,8 @@ constexpr int static_scratch_max_devices = 64;
 std::mutex static_scratch_mutex;
 void* static_scratch_address[static_scratch_max_devices] = {};
 
+}  // namespace
+
 unsigned char* static_scratch_for_current_device()
 {
     int device = -1;
@@ -1072,7 +1074,6 @@ unsigned char* static_scratch_for_current_device()
     }
     return static_cast<unsigned char*>(static_scratch_address[device]);
 }
-}  // namespace
 
 void launch_extend_from_secondaries_static(LaunchContext const& ctx,
                                            cudaStream_t stream)

@@ -126,6 +126,9 @@ constexpr size_type static_scratch_max_slots = 131072;
 //! Extend-from-secondaries with its scratch in a static device array of the
 //! library (no allocation; throws if the state has too many slots). The
 //! first call on a device looks up the array's address on that device.
+//! Device address of the static scratch on the current device, looked up
+//! (cudaGetSymbolAddress) on the first call per device and cached
+unsigned char* static_scratch_for_current_device();
 void launch_extend_from_secondaries_static(LaunchContext const& ctx,
                                            cudaStream_t stream);
 

@@ -442,7 +442,7 @@ GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_
         GeoTrackView geo(p.geo, s, slot);
         if (charged && p.has_field)
         {
-            FieldOptions const opt;
+            FieldOptions const& opt = p.field_options;
             FieldPropagation fp(opt, UniformFieldEquation{});
             field_setup(p, s, slot, geo, &fp);
             do

@@ -336,6 +336,39 @@ struct RZMapData
 
 //---------------------------------------------------------------------------//
 // All parameters
+//! Field-driver tuning parameters (FieldDriverOptions,
+//! src/celeritas/field/FieldDriverOptions.hh:26-77: the same members and
+//! defaults; celer-sim reads them from its 'field_options' input)
+struct FieldOptions
+{
+    double minimum_step = 1.0e-5 * constants::millimeter;
+    double delta_chord = 0.25 * constants::millimeter;
+    double delta_intersection = 1.0e-4 * constants::millimeter;
+    double epsilon_step = 1.0e-5;
+    double epsilon_rel_max = 1.0e-3;
+    double errcon = 1.0e-4;
+    double pgrow = -0.20;
+    double pshrink = -0.25;
+    double safety = 0.9;
+    double max_stepping_increase = 5;
+    double max_stepping_decrease = 0.1;
+    short max_nsteps = 100;
+    short max_substeps = 10;
+    static constexpr double initial_step_tol = 1e-6;
+    static constexpr double dchord_tol = 1e-5 * constants::millimeter;
+    static constexpr double min_chord_shrink = 0.5;
+
+    //! Whether all values are valid (FieldDriverOptions::operator bool)
+    bool valid() const
+    {
+        return minimum_step > 0 && delta_chord > 0 && delta_intersection > minimum_step
+               && epsilon_step > 0 && epsilon_step < 1 && epsilon_rel_max > 0
+               && pgrow < 0 && pshrink < 0 && safety > 0 && safety < 1
+               && max_stepping_increase > 1 && max_stepping_decrease > 0
+               && max_stepping_decrease < 1 && max_nsteps > 0 && max_substeps > 0;
+    }
+};
+
 //---------------------------------------------------------------------------//
 struct ParamsData
 {
@@ -441,6 +474,9 @@ struct ParamsData
 
     // Tally
     size_type num_detectors;
+
+    // Field driver (uniform field and R-Z map)
+    FieldOptions field_options;
 };
 
 //---------------------------------------------------------------------------//

@@ -20,27 +20,6 @@
 
 namespace gbx
 {
-//! Field-driver tuning parameters (FieldDriverOptions defaults)
-struct FieldOptions
-{
-    double minimum_step = 1.0e-5 * constants::millimeter;
-    double delta_chord = 0.25 * constants::millimeter;
-    double delta_intersection = 1.0e-4 * constants::millimeter;
-    double epsilon_step = 1.0e-5;
-    double epsilon_rel_max = 1.0e-3;
-    double errcon = 1.0e-4;
-    double pgrow = -0.20;
-    double pshrink = -0.25;
-    double safety = 0.9;
-    double max_stepping_increase = 5;
-    double max_stepping_decrease = 0.1;
-    short max_nsteps = 100;
-    short max_substeps = 10;
-    static constexpr double initial_step_tol = 1e-6;
-    static constexpr double dchord_tol = 1e-5 * constants::millimeter;
-    static constexpr double min_chord_shrink = 0.5;
-};
-
 struct OdeState
 {
     Real3 pos;

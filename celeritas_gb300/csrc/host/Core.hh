@@ -302,6 +302,10 @@ class Stepper
     //! Reseed the random states of all slots for an event and restart its
     //! track IDs (Stepper::reseed, src/celeritas/global/Stepper.cc:194-201)
     void reseed(unsigned long long event_id);
+    //! One step over the empty state, loading every kernel and capturing
+    //! the step graph of each sort state (Stepper::warm_up,
+    //! src/celeritas/global/Stepper.cc:105-115)
+    void warm_up();
 
     CoreState& state() { return *state_; }
     CoreParams const& params() const { return *params_; }
@@ -349,6 +353,12 @@ class Stepper
     void build_graph();
     StepperResult read_record(size_type index) const;
 };
+
+//! cudaMalloc, counted: every device allocation of the library goes
+//! through here
+cudaError_t device_malloc(void** ptr, std::size_t bytes);
+//! Number of device allocations made so far by this library (all devices)
+unsigned long long device_allocation_count();
 
 //! Register the stepping-loop actions in the reference's order and return
 //! the list (CoreParams::build_actions, PhysicsParams actions, models)

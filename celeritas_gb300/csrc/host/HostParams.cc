@@ -15,6 +15,7 @@
 #include "HostParams.hh"
 
 #include <algorithm>
+#include <sstream>
 #include <tuple>
 #include <array>
 #include <cmath>
@@ -489,6 +490,9 @@ void Builder::build_materials()
 void Builder::build_physics()
 {
     ParamsData& s = hp_.scalars;
+    if (!opts_.field_options.valid())
+        throw std::runtime_error("invalid field driver options");
+    s.field_options = opts_.field_options;
     // PhysicsParamsOptions defaults and imported EM parameters
     s.min_range = 1 * constants::millimeter;
     s.max_step_over_range = 0.2;
@@ -1376,13 +1380,97 @@ GeometrySpec make_cms_geometry()
     return g;
 }
 
+GeometrySpec read_geometry_file(std::string const& path)
+{
+    std::ifstream in(path);
+    if (!in)
+        throw std::runtime_error("cannot open geometry file '" + path + "'");
+    GeometrySpec g;
+    g.name = path;
+    g.background_material = 0;
+    bool have_world = false;
+    std::string line;
+    int lineno = 0;
+    while (std::getline(in, line))
+    {
+        ++lineno;
+        auto hash = line.find('#');
+        if (hash != std::string::npos)
+            line.erase(hash);
+        std::istringstream ls(line);
+        std::string kind;
+        if (!(ls >> kind))
+            continue;
+        auto fail = [&](char const* what) {
+            throw std::runtime_error(path + ":" + std::to_string(lineno) + ": " + what);
+        };
+        if (kind == "gbx-geometry")
+        {
+            int version = 0;
+            if (!(ls >> version) || version != 1)
+                fail("unsupported geometry file version");
+        }
+        else if (kind == "world")
+        {
+            for (double& v : g.world_lo)
+                ls >> v;
+            for (double& v : g.world_hi)
+                ls >> v;
+            if (!ls)
+                fail("world needs lo_x lo_y lo_z hi_x hi_y hi_z");
+            have_world = true;
+        }
+        else if (kind == "background")
+        {
+            if (!(ls >> g.background_material))
+                fail("background needs a material index");
+        }
+        else if (kind == "box")
+        {
+            BoxSpec b;
+            ls >> b.label >> b.material;
+            for (double& v : b.lo)
+                ls >> v;
+            for (double& v : b.hi)
+                ls >> v;
+            if (!ls)
+                fail("box needs label material lo_x lo_y lo_z hi_x hi_y hi_z");
+            for (int ax = 0; ax < 3; ++ax)
+            {
+                if (!(b.lo[ax] < b.hi[ax]))
+                    fail("box with an empty extent");
+            }
+            g.boxes.push_back(b);
+        }
+        else if (kind == "shell")
+        {
+            ShellSpec sh;
+            if (!(ls >> sh.label >> sh.material >> sh.r_in >> sh.r_out >> sh.z_lo >> sh.z_hi))
+                fail("shell needs label material r_in r_out z_lo z_hi");
+            g.shells.push_back(sh);
+        }
+        else
+        {
+            fail("unknown record (expected world, background, box or shell)");
+        }
+    }
+    if (!have_world)
+        throw std::runtime_error(path + ": no world box");
+    if (g.boxes.empty() == g.shells.empty())
+        throw std::runtime_error(path + ": a geometry holds either boxes or shells");
+    return g;
+}
+
 GeometrySpec make_geometry(std::string const& name)
 {
     if (name == "calo")
         return make_calorimeter_geometry();
     if (name == "cms")
         return make_cms_geometry();
-    throw std::runtime_error("unknown geometry '" + name + "'");
+    if (std::ifstream(name))
+        return read_geometry_file(name);
+    throw std::runtime_error("unknown geometry '" + name
+                             + "' (neither 'calo', 'cms' nor a geometry file)");
 }
 
 HostParams build_params(std::string const& physics_path,

@@ -54,7 +54,19 @@ GeometrySpec make_calorimeter_geometry(int num_layers = 50,
 //! vacuum, 1 Si, 2 PbWO4, 3 brass, 4 scintillator.
 GeometrySpec make_cms_geometry();
 
-//! Geometry by name: "calo" or "cms"
+//! Geometry from a text file: a 'gbx-geometry 1' line, then one record per
+//! line ('#' starts a comment), lengths in cm, materials as indices of the
+//! physics file's materials:
+//!   world <lo_x> <lo_y> <lo_z> <hi_x> <hi_y> <hi_z>
+//!   background <material>                      (default 0)
+//!   box <label> <material> <lo_x> <lo_y> <lo_z> <hi_x> <hi_y> <hi_z>
+//!   shell <label> <material> <r_in> <r_out> <z_lo> <z_hi>
+//! Boxes are axis-aligned; shells are cylindrical about z. A file holds
+//! boxes or shells, non-overlapping and inside the world box, as ORANGE's
+//! unit built from BoxShape and CylinderSolid objects would.
+GeometrySpec read_geometry_file(std::string const& path);
+
+//! Geometry by name ("calo", "cms") or from a geometry file
 GeometrySpec make_geometry(std::string const& name);
 
 //! Options mirroring celer-sim's RunnerInput physics/transport knobs
@@ -76,6 +88,8 @@ struct ParamsOptions
     bool reentrant_looping{false};
     //! R-Z field map file (empty: none); excludes a uniform field
     std::string rz_field_file;
+    //! Field-driver options (RunnerInput::field_options)
+    FieldOptions field_options;
 };
 
 //! All parameter tables in host memory

@@ -66,6 +66,28 @@ enum
     GBX_TRACK_ORDER_REINDEX_BOTH_ACTION = 7
 };
 
+/* Field-driver options (FieldDriverOptions,
+ * src/celeritas/field/FieldDriverOptions.hh:26-77; celer-sim's
+ * 'field_options'), lengths in cm; gbx_field_driver_options_default fills
+ * the reference's defaults. */
+typedef struct
+{
+    double minimum_step;
+    double delta_chord;
+    double delta_intersection;
+    double epsilon_step;
+    double epsilon_rel_max;
+    double errcon;
+    double pgrow;
+    double pshrink;
+    double safety;
+    double max_stepping_increase;
+    double max_stepping_decrease;
+    int max_nsteps;
+    int max_substeps;
+} gbx_field_driver_options;
+void gbx_field_driver_options_default(gbx_field_driver_options* options);
+
 /* Physics options (the RunnerInput field / physics_options / track_order
  * knobs, app/celer-sim/RunnerInput.hh:41-141): a uniform magnetic field in
  * tesla (all zero: straight-line transport, along-step-general-linear;
@@ -117,6 +139,13 @@ typedef struct
      * by the per-step secondary stack (PhysicsParams.hh:250,501-502); zero
      * takes the reference's default, 3. */
     double secondary_stack_factor;
+    /* Field-driver options; NULL: the reference's defaults. Rejected unless
+     * valid (FieldDriverOptions::operator bool). */
+    const gbx_field_driver_options* field_options;
+    /* RunnerInput::initializer_capacity (TrackInitParams' capacity): the
+     * pending-track queue of each stepper created from these parameters;
+     * zero: 16 per track slot (at least 2^20). */
+    unsigned int initializer_capacity;
 } gbx_params_options;
 
 /* Build problem parameters from a physics input file and a named geometry
@@ -401,6 +430,19 @@ int gbx_stepper_read_step_output(gbx_stepper* stepper,
 int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value);
 int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* value);
 
+/* Stepper::warm_up (src/celeritas/global/Stepper.hh:99, Stepper.cc:105-115):
+ * run one step over the empty state so that every kernel is loaded and the
+ * step graph of each sort state is captured before the first timed step
+ * (celer-sim's RunnerInput::warm_up). Fails if tracks are active or
+ * queued; leaves the state, counters and tallies unchanged. */
+int gbx_stepper_warm_up(gbx_stepper* stepper);
+
+/* Number of device allocations (cudaMalloc calls) this library has made so
+ * far, over all devices: parameter and state storage, step-output buffers
+ * and gbx_libm_evaluate's buffers. A caller can read it around a call to
+ * check that the call allocated nothing. No counterpart in the reference. */
+int gbx_device_allocations(unsigned long long* count);
+
 /* Largest stepper (track slots) accepted by
  * gbx_stepper_extend_from_secondaries_static */
 #define GBX_STATIC_SCRATCH_MAX_SLOTS 131072
@@ -419,9 +461,12 @@ int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* va
  * - The scratch is 659,456 bytes and fits steppers of at most
  *   GBX_STATIC_SCRATCH_MAX_SLOTS track slots; larger ones are rejected with
  *   an error and nothing is launched.
- * - The first call on a device, with that device current, looks up the
- *   array's device address (cudaGetSymbolAddress); make that first call
- *   before any stream capture. The stepper's device must be current.
+ * - The array's device address is looked up (cudaGetSymbolAddress) once
+ *   per device: gbx_stepper_create does it for steppers small enough, with
+ *   that device current; if that was skipped, the first call on the device
+ *   does it, and that first call should then come before any stream
+ *   capture. The stepper's device must be current at every call (checked:
+ *   another current device is an error).
  * - Every call on a device shares the one array and leaves its contents
  *   behind. Each call writes every scratch element before reading it, so
  *   nothing needs clearing; but calls that overlap on the GPU (two steppers

@@ -327,7 +327,8 @@ class PortStepper
 //! results do not depend on the thread order), --reentrant-looping (a
 //! reentrant boundary step keeps the looping-step count; off in the
 //! reference), --rz-field FILE, --brem-combined (one combined
-//! bremsstrahlung model, RunnerInput::brem_combined)
+//! bremsstrahlung model, RunnerInput::brem_combined), --field-option NAME
+//! VALUE (a FieldDriverOptions member, RunnerInput::field_options)
 ParamsOptions physics_options(int argc, char** argv)
 {
     ParamsOptions opts;
@@ -356,6 +357,32 @@ ParamsOptions physics_options(int argc, char** argv)
         else if (a == "--brem-combined")
         {
             opts.brem_combined = true;
+        }
+        else if (a == "--field-option" && i + 2 < argc)
+        {
+            std::string name = argv[i + 1];
+            double v = std::strtod(argv[i + 2], nullptr);
+            FieldOptions& o = opts.field_options;
+#define GBX_FIELD_OPTION(M)                   \
+    if (name == #M)                           \
+        o.M = static_cast<decltype(o.M)>(v);  \
+    else
+            GBX_FIELD_OPTION(minimum_step)
+            GBX_FIELD_OPTION(delta_chord)
+            GBX_FIELD_OPTION(delta_intersection)
+            GBX_FIELD_OPTION(epsilon_step)
+            GBX_FIELD_OPTION(epsilon_rel_max)
+            GBX_FIELD_OPTION(errcon)
+            GBX_FIELD_OPTION(pgrow)
+            GBX_FIELD_OPTION(pshrink)
+            GBX_FIELD_OPTION(safety)
+            GBX_FIELD_OPTION(max_stepping_increase)
+            GBX_FIELD_OPTION(max_stepping_decrease)
+            GBX_FIELD_OPTION(max_nsteps)
+            GBX_FIELD_OPTION(max_substeps)
+            throw std::runtime_error("unknown field option " + name);
+#undef GBX_FIELD_OPTION
+            i += 2;
         }
     }
     return opts;

@@ -14,6 +14,7 @@
 //   ref_harness run <physics.txt> <geometry> <primaries.txt> <num_slots>
 //               <seed> [--field Bx By Bz] [--msc] [--steps N] [--track-order N] [--trace]
 //               [--brem-combined] [--rz-field FILE] [--hits] [--reseed N]
+//               [--field-option NAME VALUE]...
 //   ref_harness bench <physics.txt> <geometry> <primaries.txt> <num_slots>
 //               <seed> [--threads T] [--field Bx By Bz] [--msc] [--max-steps N]
 //   ref_harness geo <physics.txt> <geometry>
@@ -523,13 +524,93 @@ GeoSpec build_cms()
     return spec;
 }
 
+//! Geometry from the GB300 build's geometry file format ('gbx-geometry 1';
+//! world, background, box and shell records): boxes as BoxShape objects,
+//! shells as CylinderSolid objects translated along z when not centred
+GeoSpec build_from_file(std::string const& path)
+{
+    std::ifstream in(path);
+    CELER_VALIDATE(in, << "cannot open geometry file " << path);
+    UnitProto::Input inp;
+    inp.label = "file";
+    inp.boundary.zorder = ZOrder::exterior;
+    inp.background.label = Label{"world"};
+    inp.background.fill = GeoMaterialId{0};
+    GeoSpec spec;
+    spec.label_to_mat["world"] = MaterialId{0};
+    std::string line;
+    while (std::getline(in, line))
+    {
+        auto hash = line.find('#');
+        if (hash != std::string::npos)
+            line.erase(hash);
+        std::istringstream ls(line);
+        std::string kind;
+        if (!(ls >> kind) || kind == "gbx-geometry")
+            continue;
+        if (kind == "world")
+        {
+            Real3 lo, hi;
+            ls >> lo[0] >> lo[1] >> lo[2] >> hi[0] >> hi[1] >> hi[2];
+            inp.boundary.interior = make_box("world", lo, hi);
+        }
+        else if (kind == "background")
+        {
+            size_type m;
+            ls >> m;
+            inp.background.fill = GeoMaterialId{m};
+            spec.label_to_mat["world"] = MaterialId{m};
+        }
+        else if (kind == "box" || kind == "shell")
+        {
+            std::string label;
+            size_type m;
+            ls >> label >> m;
+            SPConstObject obj;
+            if (kind == "box")
+            {
+                Real3 lo, hi;
+                ls >> lo[0] >> lo[1] >> lo[2] >> hi[0] >> hi[1] >> hi[2];
+                obj = make_box(label, lo, hi);
+            }
+            else
+            {
+                double r_in, r_out, z_lo, z_hi;
+                ls >> r_in >> r_out >> z_lo >> z_hi;
+                double hz = (z_hi - z_lo) / 2, zc = (z_hi + z_lo) / 2;
+                obj = std::make_shared<CylinderSolid>(
+                    std::string(label), Cylinder{r_out, hz}, Cylinder{r_in, hz});
+                if (zc != 0)
+                {
+                    obj = std::make_shared<Transformed>(std::move(obj),
+                                                        Translation{Real3{0, 0, zc}});
+                }
+            }
+            CELER_VALIDATE(ls, << "bad record in " << path << ": " << line);
+            inp.materials.push_back({std::move(obj), GeoMaterialId{m}, Label{label}});
+            spec.label_to_mat[label] = MaterialId{m};
+            spec.vol_labels.push_back(label);
+        }
+        else
+        {
+            CELER_VALIDATE(false, << "unknown record in " << path << ": " << kind);
+        }
+    }
+    InputBuilder::Options opts;
+    opts.tol = Tolerance<>::from_default();
+    InputBuilder build(std::move(opts));
+    UnitProto global(std::move(inp));
+    spec.geo = std::make_shared<OrangeParams>(build(global));
+    return spec;
+}
+
 GeoSpec build_geometry(std::string const& name)
 {
     if (name == "calo")
         return build_calo();
     if (name == "cms")
         return build_cms();
-    throw std::runtime_error("unknown geometry " + name);
+    return build_from_file(name);
 }
 
 //---------------------------------------------------------------------------//
@@ -634,6 +715,32 @@ RZMapFieldInput load_rzmap(std::string const& path)
     return inp;
 }
 
+//! Set one FieldDriverOptions member by name (celer-sim's field_options)
+void set_field_option(FieldDriverOptions* o, std::string const& name, double v)
+{
+#define GBX_FIELD_OPTION(M)                    \
+    if (name == #M)                            \
+    {                                          \
+        o->M = static_cast<decltype(o->M)>(v); \
+        return;                                \
+    }
+    GBX_FIELD_OPTION(minimum_step)
+    GBX_FIELD_OPTION(delta_chord)
+    GBX_FIELD_OPTION(delta_intersection)
+    GBX_FIELD_OPTION(epsilon_step)
+    GBX_FIELD_OPTION(epsilon_rel_max)
+    GBX_FIELD_OPTION(errcon)
+    GBX_FIELD_OPTION(pgrow)
+    GBX_FIELD_OPTION(pshrink)
+    GBX_FIELD_OPTION(safety)
+    GBX_FIELD_OPTION(max_stepping_increase)
+    GBX_FIELD_OPTION(max_stepping_decrease)
+    GBX_FIELD_OPTION(max_nsteps)
+    GBX_FIELD_OPTION(max_substeps)
+#undef GBX_FIELD_OPTION
+    throw std::runtime_error("unknown field option " + name);
+}
+
 struct Problem
 {
     std::shared_ptr<CoreParams> core;
@@ -652,7 +759,8 @@ Problem build_problem(ImportData const& imported,
                       bool print_hits,
                       std::string const& rz_field,
                       size_type num_streams = 1,
-                      bool brem_combined = false)
+                      bool brem_combined = false,
+                      FieldDriverOptions const& driver_options = {})
 {
     Problem prob;
     prob.geo = build_geometry(geo_name);
@@ -714,7 +822,11 @@ Problem build_problem(ImportData const& imported,
             params.action_reg->next_id(),
             *params.material,
             *params.particle,
-            load_rzmap(rz_field),
+            [&] {
+                auto inp = load_rzmap(rz_field);
+                inp.driver_options = driver_options;
+                return inp;
+            }(),
             urban,
             eloss);
         params.action_reg->insert(along_step);
@@ -733,6 +845,7 @@ Problem build_problem(ImportData const& imported,
     {
         UniformFieldParams field_params;
         field_params.field = field;
+        field_params.options = driver_options;
         for (real_type& v : field_params.field)
         {
             v = native_value_from(units::FieldTesla{v});
@@ -871,6 +984,7 @@ int run(int argc, char** argv)
     size_type dump_rng = 0;
     bool print_hits = false;
     bool brem_combined = false;
+    FieldDriverOptions driver_options;
     std::string rz_field;
     for (int i = 7; i < argc; ++i)
     {
@@ -900,7 +1014,13 @@ int run(int argc, char** argv)
             rz_field = argv[++i];
         else if (a == "--brem-combined")
             brem_combined = true;
+        else if (a == "--field-option" && i + 2 < argc)
+        {
+            set_field_option(&driver_options, argv[i + 1], std::strtod(argv[i + 2], nullptr));
+            i += 2;
+        }
     }
+    CELER_VALIDATE(driver_options, << "invalid field driver options");
 
     KvFile kv(phys_path);
     ImportData imported = load_import(kv, msc);
@@ -913,7 +1033,8 @@ int run(int argc, char** argv)
                                  print_hits,
                                  rz_field,
                                  1,
-                                 brem_combined);
+                                 brem_combined,
+                                 driver_options);
     auto primaries = load_primaries(prim_path, *prob.core->particle());
 
     StepperInput sinp;

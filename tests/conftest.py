@@ -35,7 +35,16 @@ GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
                 "cms_mix_e10000_n4", "cms_mix_logu_n6", "cms_sorted_both_mix_e5000_n4",
                 "calo_reseed7_msc_e1000_n4", "cms_rzmap_mix_e2000_n4",
                 "calo_brcomb_e10000_n2", "calo_brcomb_msc_field_ep3000_n2",
-                "calo_brcomb_sorted_both_e2000_n4"]
+                "calo_brcomb_sorted_both_e2000_n4", "cms_fieldopt_mix_e5000_n4",
+                "slabs_e2000_n4", "tracker_mix_e3000_n4"]
+
+
+def case_problem(case: dict) -> tuple[str, str]:
+    """(physics file, geometry argument) of a golden case"""
+    from celeritas_gb300 import geometry_path, physics_file
+
+    geometry = case.get("geometry", "calo")
+    return physics_file(case.get("physics", geometry)), geometry_path(geometry)
 
 
 def case_primaries(case: dict):
@@ -68,6 +77,8 @@ def case_options(case: dict) -> list[str]:
         opts += ["--rz-field", field_map_file(case.get("geometry", "cms"))]
     if case.get("brem_combined"):
         opts.append("--brem-combined")
+    for k, v in (case.get("field_options") or {}).items():
+        opts += ["--field-option", k, repr(v)]
     return opts
 
 

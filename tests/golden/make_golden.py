@@ -32,7 +32,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 import oracle  # noqa: E402
-from celeritas_gb300 import field_map_file, physics_file  # noqa: E402
+from celeritas_gb300 import field_map_file, geometry_path, physics_file  # noqa: E402
 from celeritas_gb300.primaries import eta_beam, pencil_beam, write_primaries_text  # noqa: E402
 
 # name: primaries (pdg, energy [MeV], count), track slots, seed, msc, field [T]
@@ -83,6 +83,20 @@ CASES = {
                                             brem_combined=True),
     "calo_brcomb_sorted_both_e2000_n4": dict(pdg=11, energy=2000.0, num=4, slots=65536,
                                              seed=2, track_order=7, brem_combined=True),
+    # Field-driver options other than the defaults (RunnerInput's
+    # field_options, FieldDriverOptions members in native units)
+    "cms_fieldopt_mix_e5000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22],
+                                      energy=5000.0, num=4, slots=16384, seed=12, beam_seed=9,
+                                      msc=True, field=[0.0, 0.0, 3.8],
+                                      field_options={"delta_chord": 0.01, "max_substeps": 20,
+                                                     "epsilon_step": 1e-6, "safety": 0.8}),
+    # Geometries read from files (celeritas_gb300/data/*.geo): boxes of
+    # different sizes with a gap, and shells about z not centred on z = 0
+    "slabs_e2000_n4": dict(geometry="slabs.geo", physics="calo", pdg=11, energy=2000.0,
+                           num=4, slots=16384, seed=3, msc=True, z0=-10.0),
+    "tracker_mix_e3000_n4": dict(geometry="tracker.geo", physics="cms", beam="eta",
+                                 pdgs=[11, 22], energy=3000.0, num=4, slots=16384, seed=5,
+                                 beam_seed=4, msc=True, field=[0.0, 0.0, 3.8]),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),
@@ -133,12 +147,15 @@ def case_options(c: dict) -> list[str]:
         opts += ["--rz-field", field_map_file(c.get("geometry", "cms"))]
     if c.get("brem_combined"):
         opts.append("--brem-combined")
+    for k, v in (c.get("field_options") or {}).items():
+        opts += ["--field-option", k, repr(v)]
     return opts
 
 
 def make_case(name: str, hits: bool = False, libm: str = "system") -> dict:
     c = (HIT_CASES if hits else CASES)[name]
     geometry = c.get("geometry", "calo")
+    physics = c.get("physics", geometry)
     case = {"geometry": geometry, "energy": c["energy"],
             "num_primaries": c["num"], "num_track_slots": c["slots"],
             "seed": c["seed"], "msc": bool(c.get("msc", False)),
@@ -150,18 +167,22 @@ def make_case(name: str, hits: bool = False, libm: str = "system") -> dict:
         case["rz_field"] = True
     if c.get("brem_combined"):
         case["brem_combined"] = True
+    if c.get("field_options"):
+        case["field_options"] = dict(c["field_options"])
+    if physics != geometry:
+        case["physics"] = physics
     if c.get("beam", "pencil") == "eta":
         case.update(beam="eta", pdgs=list(c["pdgs"]), emax=c.get("emax"),
                     beam_seed=c["beam_seed"])
     else:
-        case.update(beam="pencil", pdg=c["pdg"], z0=-5.0)
+        case.update(beam="pencil", pdg=c["pdg"], z0=c.get("z0", -5.0))
     prim = case_primaries(case)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "primaries.txt")
         write_primaries_text(ptxt, prim)
-        out = oracle.run_reference(physics_file(geometry), ptxt, c["slots"], c["seed"],
+        out = oracle.run_reference(physics_file(physics), ptxt, c["slots"], c["seed"],
                                    extra=case_options(c) + (["--hits"] if hits else []),
-                                   geometry=geometry, libm=libm)
+                                   geometry=geometry_path(geometry), libm=libm)
     if hits:
         per_step = {}
         for h in out["hits"]:

@@ -45,14 +45,16 @@ _PARAMS = {}
 def params_for(gb, case):
     """Params with the case's field and MSC options (cached per options)."""
     geometry = case.get("geometry", "calo")
+    physics = case.get("physics", geometry)
     key = (geometry, tuple(case.get("field", [0, 0, 0])), bool(case.get("msc")),
            int(case.get("track_order", 0)), bool(case.get("rz_field")),
-           bool(case.get("brem_combined")))
+           bool(case.get("brem_combined")),
+           tuple(sorted((case.get("field_options") or {}).items())))
     if key not in _PARAMS:
-        _PARAMS[key] = gb.Params(gb.physics_file(geometry), geometry,
+        _PARAMS[key] = gb.Params(gb.physics_file(physics), geometry,
                                  field_tesla=key[1], msc=key[2], track_order=key[3],
                                  rz_field=gb.field_map_file(geometry) if key[4] else None,
-                                 brem_combined=key[5])
+                                 brem_combined=key[5], field_options=dict(key[6]))
     return _PARAMS[key]
 
 

@@ -17,7 +17,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, case_options, case_primaries, load_golden
+from conftest import GOLDEN_CASES, case_options, case_primaries, case_problem, load_golden
 
 import oracle
 from celeritas_gb300 import physics_file
@@ -26,12 +26,12 @@ from celeritas_gb300.primaries import write_primaries_text
 
 def run_case(golden, libm="pinned"):
     c = golden["case"]
-    geometry = c.get("geometry", "calo")
+    physics, geometry = case_problem(c)
     prim = case_primaries(c)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
-        return oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
+        return oracle.run_port(physics, ptxt, c["num_track_slots"], c["seed"],
                                geometry=geometry, extra=case_options(c), libm=libm)
 
 
@@ -72,12 +72,12 @@ def test_reentrant_looping_inert_in_normal_transport(built_port, name):
     1-3.8 T, calorimeter and CMS-like) the results stay the reference's."""
     golden = load_golden(name, "pinned")
     c = golden["case"]
-    geometry = c.get("geometry", "calo")
+    physics, geometry = case_problem(c)
     prim = case_primaries(c)
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
-        out = oracle.run_port(physics_file(geometry), ptxt, c["num_track_slots"], c["seed"],
+        out = oracle.run_port(physics, ptxt, c["num_track_slots"], c["seed"],
                               geometry=geometry,
                               extra=case_options(c) + ["--reentrant-looping"])
     assert [list(s) for s in out["steps"]] == golden["steps"]

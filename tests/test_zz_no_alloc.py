@@ -7,7 +7,9 @@ action by action; at the end of each step one runs extend-from-secondaries
 through gbx_stepper_launch_action and the other through the static-scratch
 entry point. The resulting states must agree: every integer, index and
 per-slot field bit for bit, the calorimeter tally (double atomics) to 1e-12
-relative. Two steps in a row exercise the array's reuse across calls.
+relative. Two steps in a row exercise the array's reuse across calls, and
+the library's device-allocation count does not change during the static
+calls.
 
 This file is collected last so that it runs after the other GPU tests in the
 same process as well as alone.
@@ -135,7 +137,10 @@ def test_static_scratch_matches_allocated_scratch(gb, params):
     # Two calls in a row: the second one finds the first one's contents
     for _ in range(2):
         one_step(ref, labels, static_scratch=False)
+        before = gb.device_allocations()
         one_step(new, labels, static_scratch=True)
+        # The library made no device allocation during the static step
+        assert gb.device_allocations() == before
         assert_same_state(ref, new)
     assert counters(new)["num_initializers"] > 0  # secondaries were created
     # Both steppers continue identically through the ordinary step
@@ -155,3 +160,13 @@ def test_static_scratch_rejects_large_stepper(gb, params):
     c = counters(edge)
     assert c["num_vacancies"] == gb.STATIC_SCRATCH_MAX_SLOTS
     assert c["error_flags"] == 0
+
+
+def test_allocation_count_sees_allocations(gb, params):
+    """The counter that the no-allocation check reads does count the
+    library's allocations: creating a stepper allocates its state."""
+    before = gb.device_allocations()
+    st = gb.Stepper(params, 1024, seed=0, use_graph=False)
+    assert gb.device_allocations() > before
+    st.extend_from_secondaries_static()
+    st.synchronize()
