@@ -7,10 +7,11 @@ their transport times compare directly. The tuner runs a coordinate descent
 over
 
 * the number of track slots (one stepper per candidate),
-* threads per block of the charged along-step kernel (64, 128, 256; 512 is
-  reported as invalid: it exceeds the register file of that kernel) together
-  with its form, a persistent kernel or one thread per track (the best block
-  size differs between the two forms, so they are tuned as pairs),
+* threads per block of the charged along-step kernel (64, 128, 256 and 512,
+  the last from kernel instances whose registers are capped at 128 per
+  thread) together with its form, a persistent kernel or one thread per track
+  (the best block size differs between the two forms, so they are tuned as
+  pairs); a setting the stepper rejects is recorded and skipped,
 * the sort threshold: action sorts only in steps that start with at least
   this many live tracks (0: always),
 

@@ -841,11 +841,9 @@ void CoreState::set_tuning(std::string const& name, long long value)
 {
     if (name == "along_block_size")
     {
-        if (value != 64 && value != 128 && value != 256)
+        if (value != 64 && value != 128 && value != 256 && value != 512)
         {
-            throw std::runtime_error(
-                "along_block_size must be 64, 128 or 256 (512 threads exceed the "
-                "register file of the charged along-step kernel)");
+            throw std::runtime_error("along_block_size must be 64, 128, 256 or 512");
         }
         ctx_.along_block_size = static_cast<int>(value);
         if (ctx_.persistent_blocks > 0)

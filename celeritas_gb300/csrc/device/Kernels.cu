@@ -662,14 +662,19 @@ __device__ __forceinline__ bool sorted_slot(StateData const& s,
 #ifndef GBX_ALONG_MAXNREG
 #    define GBX_ALONG_MAXNREG 0
 #endif
+// The charged kernels come in two instances: blocks of up to 256 threads
+// (the kernel's natural register count), and blocks of 512, for which the
+// launch bound caps registers at 65536 / 512 = 128 per thread (the compiler
+// spills what does not fit)
 #if GBX_ALONG_MAXNREG > 0
-#    define GBX_ALONG_BOUNDS(MINB) __maxnreg__(GBX_ALONG_MAXNREG)
+#    define GBX_ALONG_BOUNDS(THREADS, MINB) __maxnreg__(GBX_ALONG_MAXNREG)
 #else
-#    define GBX_ALONG_BOUNDS(MINB) __launch_bounds__(block_size, MINB)
+#    define GBX_ALONG_BOUNDS(THREADS, MINB) __launch_bounds__(THREADS, MINB)
 #endif
+constexpr int along_block_large = 512;
 
-template<AlongKind K>
-__global__ GBX_ALONG_BOUNDS(K == AlongKind::charged ? GBX_ALONG_MIN_BLOCKS : 1) void
+template<AlongKind K, int Threads = block_size>
+__global__ GBX_ALONG_BOUNDS(Threads, K == AlongKind::charged ? GBX_ALONG_MIN_BLOCKS : 1) void
 along_step_sorted_kernel(ParamsData p,
                          StateData s,
                          size_type const* offsets,
@@ -688,7 +693,8 @@ along_step_sorted_kernel(ParamsData p,
 //! its own finishes. Lanes of a warp thus stay busy on different tracks
 //! instead of waiting for the one with the most substeps. Every track runs
 //! the same sequence of operations as along_step_impl.
-__global__ GBX_ALONG_BOUNDS(1) void along_charged_persistent_kernel(
+template<int Threads>
+__global__ GBX_ALONG_BOUNDS(Threads, 1) void along_charged_persistent_kernel(
     ParamsData p,
     StateData s,
     size_type const* offsets,
@@ -849,11 +855,24 @@ void launch_along_step(LaunchContext const& ctx,
         = key_offsets(ctx, SortKey::along_step, sorts_along_step(p.track_order));
     if (action == invalid_id || action == p.action_along_step)
     {
+        bool const large = abs > static_cast<unsigned int>(block_size);
         if (p.has_field && ctx.persistent_blocks > 0)
         {
             cudaMemsetAsync(ctx.work_counter, 0, sizeof(size_type), stream);
-            along_charged_persistent_kernel<<<ctx.persistent_blocks, abs, 0, stream>>>(
-                p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
+            if (large)
+                along_charged_persistent_kernel<along_block_large>
+                    <<<ctx.persistent_blocks, abs, 0, stream>>>(
+                        p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
+            else
+                along_charged_persistent_kernel<block_size>
+                    <<<ctx.persistent_blocks, abs, 0, stream>>>(
+                        p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
+        }
+        else if (large)
+        {
+            along_step_sorted_kernel<AlongKind::charged, along_block_large>
+                <<<anb, abs, 0, stream>>>(
+                    p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
         }
         else
         {
@@ -948,8 +967,17 @@ int persistent_along_blocks(int threads_per_block)
     if (cudaGetDevice(&device) != cudaSuccess
         || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)
                != cudaSuccess
-        || cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-               &per_sm, along_charged_persistent_kernel, threads_per_block, 0)
+        || (threads_per_block > block_size
+                ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                      &per_sm,
+                      along_charged_persistent_kernel<along_block_large>,
+                      threads_per_block,
+                      0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                      &per_sm,
+                      along_charged_persistent_kernel<block_size>,
+                      threads_per_block,
+                      0))
                != cudaSuccess)
     {
         return 0;
@@ -962,7 +990,20 @@ void launch_count_event_live(LaunchContext const& ctx,
                              cudaStream_t stream)
 {
     cudaMemsetAsync(ctx.state.event_live, 0, sizeof(size_type) * num_events, stream);
-    count_event_live_kernel<<<4 * 152, block_size, 0, stream>>>(ctx.state, num_events);
+    // A grid-stride pass: four blocks per SM of the current device
+    static thread_local int sms = 0;
+    if (sms == 0)
+    {
+        int device = 0;
+        if (cudaGetDevice(&device) != cudaSuccess
+            || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)
+                   != cudaSuccess
+            || sms <= 0)
+        {
+            sms = 1;
+        }
+    }
+    count_event_live_kernel<<<4 * sms, block_size, 0, stream>>>(ctx.state, num_events);
 }
 
 __global__ __launch_bounds__(block_size) void reseed_kernel(ParamsData p,

@@ -417,7 +417,8 @@ int gbx_stepper_read_step_output(gbx_stepper* stepper,
 
 /* Launch tuning of a stepper, for an autotuner (no counterpart in the
  * reference, whose block sizes and sort policy are build and run options):
- *   "along_block_size"  threads per block of the charged along-step (64, 128, 256)
+ *   "along_block_size"  threads per block of the charged along-step (64, 128,
+ *                       256, or 512 with registers capped at 128 per thread)
  *   "along_persistent"  1: charged along-step as a persistent kernel that
  *                       interleaves field substeps of different tracks
  *   "sort_threshold"    with an action-sorting track order, sort only in
