@@ -109,7 +109,7 @@ GBX_FUNCTION void pre_step(ParamsData const& p, StateData const& s, size_type sl
         if (eloss != invalid_id)
         {
             XsGrid const* g = phys.grid(vgt_range, eloss);
-            real_type range = calc_range(p, *g, energy);
+            real_type range = calc_range(p, *g, energy, phys.log_energy(energy));
             s.dedx_range[slot] = range;
             real_type eloss_step = phys.range_to_step(range);
             if (eloss_step <= step)
@@ -151,7 +151,7 @@ GBX_FORCEINLINE real_type calc_mean_eloss(ParamsData const& p,
 {
     size_type const ppid = phys.group().eloss_process;
     XsGrid const* dedx = phys.grid(vgt_energy_loss, ppid);
-    real_type eloss = step * calc_grid_xs(p, *dedx, pre_energy);
+    real_type eloss = step * calc_grid_xs(p, *dedx, pre_energy, phys.log_energy(pre_energy));
     if (eloss >= pre_energy * real_type(p.linear_loss_limit))
     {
         XsGrid const* rg = phys.grid(vgt_range, ppid);
@@ -531,7 +531,9 @@ GBX_FUNCTION void discrete_select(ParamsData const& p,
             size_type i = 0;
             for (; i + 1 < mat.num_elements; ++i)
             {
-                if (calc_grid_xs(p, p.grids[p.ints[table + i]], energy) > u)
+                if (calc_grid_xs(
+                        p, p.grids[p.ints[table + i]], energy, phys.log_energy(energy))
+                    > u)
                     break;
             }
             s.element[slot] = i;

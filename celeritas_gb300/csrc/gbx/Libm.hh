@@ -86,8 +86,9 @@ constexpr double pio2_0 = pio2_parts.v0, pio2_1 = pio2_parts.v1, pio2_2 = pio2_p
 constexpr double inv_ln2_n = GBX_LIBM_INV_LN2_N;
 constexpr double two_over_pi = GBX_LIBM_TWO_OVER_PI;
 
-//! Fast-path relative error bounds of exp and log, four times the largest
-//! errors measured against 250-bit evaluations (2^-65.5 and 2^-67.1)
+//! Fast-path relative error bounds of exp and log: at least eight times the
+//! largest errors measured against 250-bit evaluations (2^-65.5 and
+//! 2^-67.1)
 constexpr double exp_fast_err = 0x1p-62;
 constexpr double log_fast_err = 0x1p-63;
 
@@ -212,12 +213,12 @@ struct ExpReduced
 GBX_FORCEINLINE ExpReduced exp_reduce(double x)
 {
     double kd = std::rint(x * inv_ln2_n);
-    // kd * ln2_n0 is exact (35-bit part, |k| < 2^18) and so is the
-    // subtraction (Sterbenz); the second part's product error is kept
-    double r1 = x - kd * ln2_n0;
-    DD p2 = two_prod(kd, ln2_n1);
-    DD r = two_sum(r1, -p2.hi);
-    r.lo += -p2.lo - kd * ln2_n2;
+    // kd times either of the 35-bit parts is exact (|k| < 2^18), and so is
+    // the first subtraction (Sterbenz); the third part's product error is
+    // below 2^-120 of the result
+    double r1 = fma_(-kd, ln2_n0, x);
+    DD r = two_sum(r1, -kd * ln2_n1);
+    r.lo = fma_(-kd, ln2_n2, r.lo);
     return {static_cast<int>(kd), r};
 }
 
@@ -238,12 +239,13 @@ GBX_FORCEINLINE DD exp_core_fast(DD r, DD t)
     q = fma_(x, q, GBX_LIBM_LOAD(inv_fact, 8));
     q = fma_(x, q, GBX_LIBM_LOAD(inv_fact, 6));
     q = fma_(x, q, GBX_LIBM_LOAD(inv_fact, 4));
-    q = x * x * q + x * r.lo;
-    DD s = two_sum(x, r.lo + q);
-    // t * (1 + s)
-    DD m = two_prod(t.hi, s.hi);
+    // exp(r) - 1 = x + (r.lo + x r.lo + x^2 q), the parenthesis below
+    // 2^-16 of the result
+    double const tail = fma_(x * x, q, fma_(x, r.lo, r.lo));
+    // t (1 + x + tail): t.hi x exactly, the rest to double precision
+    DD m = two_prod(t.hi, x);
     DD out = fast_two_sum(t.hi, m.hi);
-    out.lo += m.lo + (t.hi * s.lo + (t.lo + t.lo * s.hi));
+    out.lo += m.lo + fma_(t.hi, tail, fma_(t.lo, x, t.lo));
     return out;
 }
 
@@ -283,6 +285,7 @@ GBX_FORCEINLINE double exp_scale(DD v, int m, double err, bool* ok)
         return 0.0;
     }
     double const scale = s >= -1022 ? pow2(s) : 0.0;
+    v = fast_two_sum(v.hi, v.lo);  // |lo| <= ulp(hi) / 2 for the test below
     double uh = v.hi * scale;
     double ul = v.lo * scale;
     double n = std::rint(uh);
@@ -361,14 +364,12 @@ GBX_FORCEINLINE DD log1p_small_fast(double zh, double zl)
     p = fma_(zh, p, GBX_LIBM_LOAD(inv_int, 10));
     p = fma_(zh, p, -GBX_LIBM_LOAD(inv_int, 8));
     p = fma_(zh, p, GBX_LIBM_LOAD(inv_int, 6));
-    double const z2 = zh * zh;
-    p = p * z2 * zh;
-    // -z^2/2 exactly, and the cross term -zh zl of the square
-    DD h = two_prod(zh, zh);
-    h.hi *= 0.5;
-    h.lo *= 0.5;
-    DD s = two_sum(zh, -h.hi);
-    s.lo += zl - h.lo - zh * zl + p;
+    p *= zh * zh * zh;
+    // -z^2/2 exactly (zh times the exact zh/2), then the first-order term
+    // of zl: log1p(zh + zl) = log1p(zh) + zl (1 - zh + zh^2) + O(zl zh^3)
+    DD h = two_prod(zh, 0.5 * zh);
+    DD s = fast_two_sum(zh, -h.hi);
+    s.lo += fma_(zl, fma_(zh, zh, -zh), zl) - h.lo + p;
     return s;
 }
 
@@ -419,9 +420,10 @@ GBX_FORCEINLINE LogReduced log_reduce(double x)
     red.j = static_cast<int>((u >> 45) & 127);
     double const m = from_bits((u & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
     double const inv_c = GBX_LIBM_LOAD(log_table, 3 * red.j);
-    // m inv_c - 1: the product exactly as p + pe, p - 1 exact (Sterbenz)
+    // m inv_c - 1: the product exactly as p + pe, p - 1 exact (Sterbenz);
+    // z = (p - 1) + pe is kept as that unnormalized pair (|pe| <= 2^-54)
     DD p = two_prod(m, inv_c);
-    red.z = two_sum(p.hi - 1.0, p.lo);
+    red.z = DD{p.hi - 1.0, p.lo};
     red.near_one = false;
     return red;
 }
@@ -431,14 +433,15 @@ GBX_FORCEINLINE DD log_fast(LogReduced const& red)
 {
     DD l = log1p_small_fast(red.z.hi, red.z.lo);
     if (red.near_one)
-        return fast_two_sum(l.hi, l.lo);
+        return l;
     double const ed = red.e;
     double const th = GBX_LIBM_LOAD(log_table, 3 * red.j + 1);
     double const tl = GBX_LIBM_LOAD(log_table, 3 * red.j + 2);
-    DD s = two_sum(ed * ln2_0, th);  // e ln2_0 is exact
+    // e ln2_0 is exact and at least ln 2 > th when e != 0 (th < 0.6913)
+    DD s = fast_two_sum(ed * ln2_0, th);
     DD t = two_sum(s.hi, l.hi);
-    double lo = s.lo + t.lo + l.lo + tl + ed * ln2_1 + ed * ln2_2;
-    return fast_two_sum(t.hi, lo);
+    double const lo = fma_(ed, ln2_2, fma_(ed, ln2_1, (s.lo + t.lo) + (l.lo + tl)));
+    return {t.hi, lo};
 }
 
 GBX_NOINLINE DD log_accurate(LogReduced const& red)

@@ -53,7 +53,8 @@ class MscHelper
 
     GBX_FORCEINLINE real_type calc_msc_mfp(real_type energy) const
     {
-        real_type xsec = calc_grid_xs(p_, *xs_, energy) / ipow<2>(energy);
+        real_type xsec
+            = calc_grid_xs(p_, *xs_, energy, phys_.log_energy(energy)) / ipow<2>(energy);
         if constexpr (sizeof(real_type) < sizeof(double))
         {
             // FP32: in a near-vacuum the cross section underflows to zero;
@@ -82,7 +83,7 @@ class MscHelper
         {
             XsGrid const* eg
                 = phys_.grid(vgt_energy_loss, phys_.group().eloss_process);
-            real_type dedx = calc_grid_xs(p_, *eg, energy_);
+            real_type dedx = calc_grid_xs(p_, *eg, energy_, phys_.log_energy(energy_));
             return energy_ - step * dedx;
         }
         return this->calc_inverse_range(range - step);

@@ -55,14 +55,15 @@ GBX_FORCEINLINE size_type find_nonuniform(T const* grid, size_type size, T v)
     return min_of(lo, size - 2);
 }
 
-//! Macroscopic cross section (or dE/dx) from a log-uniform grid
+//! Macroscopic cross section (or dE/dx) from a log-uniform grid, given
+//! log(energy)
 GBX_FORCEINLINE real_type calc_grid_xs(ParamsData const& p,
                                        XsGrid const& g,
-                                       real_type energy)
+                                       real_type energy,
+                                       real_type loge)
 {
     real_type const* values = p.reals + g.value;
     real_type const* energies = p.reals + g.energy;
-    real_type const loge = libm::log(energy);
     auto extrapolated = [&](size_type idx) {
         real_type result = values[idx];
         if (idx >= g.prime_index)
@@ -86,14 +87,23 @@ GBX_FORCEINLINE real_type calc_grid_xs(ParamsData const& p,
     return result;
 }
 
-//! Range from a log-uniform grid, with sqrt(E) scaling below the grid
+//! Macroscopic cross section (or dE/dx) from a log-uniform grid
+GBX_FORCEINLINE real_type calc_grid_xs(ParamsData const& p,
+                                       XsGrid const& g,
+                                       real_type energy)
+{
+    return calc_grid_xs(p, g, energy, libm::log(energy));
+}
+
+//! Range from a log-uniform grid, with sqrt(E) scaling below the grid,
+//! given log(energy)
 GBX_FORCEINLINE real_type calc_range(ParamsData const& p,
                                      XsGrid const& g,
-                                     real_type energy)
+                                     real_type energy,
+                                     real_type loge)
 {
     real_type const* values = p.reals + g.value;
     real_type const* energies = p.reals + g.energy;
-    real_type const loge = libm::log(energy);
     if (loge <= g.log_front)
     {
         real_type result = values[0];
@@ -106,6 +116,14 @@ GBX_FORCEINLINE real_type calc_range(ParamsData const& p,
     idx = min_of(idx, g.size - 2);
     return interp_linear<real_type>(
         energies[idx], values[idx], energies[idx + 1], values[idx + 1], energy);
+}
+
+//! Range from a log-uniform grid, with sqrt(E) scaling below the grid
+GBX_FORCEINLINE real_type calc_range(ParamsData const& p,
+                                     XsGrid const& g,
+                                     real_type energy)
+{
+    return calc_range(p, g, energy, libm::log(energy));
 }
 
 //! Energy from range (inverse of the range table)
@@ -234,6 +252,25 @@ class PhysicsTrack
     {
         return group_.num_processes;
     }
+
+    //! log(energy), remembered for the last two energies: the table lookups
+    //! of one step take the logarithm of the same few energies many times
+    //! (every process at E and at E * min_eprime_over_e, the range and the
+    //! stopping power at E), and the function returns the same double for
+    //! the same argument, so a remembered value changes no result
+    GBX_FORCEINLINE real_type log_energy(real_type energy) const
+    {
+        if (energy == memo_e_[0])
+            return memo_log_[0];
+        if (energy == memo_e_[1])
+            return memo_log_[1];
+        real_type const result = libm::log(energy);
+        memo_e_[1] = memo_e_[0];
+        memo_log_[1] = memo_log_[0];
+        memo_e_[0] = energy;
+        memo_log_[0] = result;
+        return result;
+    }
     GBX_FORCEINLINE ProcessGroup const& group() const { return group_; }
     GBX_FORCEINLINE MaterialRecord const& material() const
     {
@@ -309,7 +346,7 @@ class PhysicsTrack
         }
         else if (XsGrid const* g = this->grid(vgt_macro_xs, ppid))
         {
-            result = calc_grid_xs(p_, *g, energy);
+            result = calc_grid_xs(p_, *g, energy, this->log_energy(energy));
         }
         return result;
     }
@@ -343,6 +380,9 @@ class PhysicsTrack
     ProcessGroup const& group_;
     size_type particle_;
     size_type material_;
+    // log_energy's remembered arguments (NaN: none yet) and results
+    mutable real_type memo_e_[2]{real_type(NAN), real_type(NAN)};
+    mutable real_type memo_log_[2]{0, 0};
 };
 
 //---------------------------------------------------------------------------//

@@ -3,7 +3,7 @@
     python -m celeritas_gb300.profile_run --workload c2 [--primaries N]
         [--max-iterations K] [--steps-log FILE] [--graph]
         [--precision double|mixed] [--track-order N] [--slots S]
-        [--tuning name=value,...]
+        [--tuning name=value,...] [--initializer-capacity N]
 
 Inserts the workload's primaries, then steps (eagerly by default, so that
 every kernel is its own launch) until the state empties or K iterations have
@@ -36,6 +36,8 @@ def main(argv=None):
     ap.add_argument("--track-order", type=int, default=0)
     ap.add_argument("--slots", type=int, default=None,
                     help="track slots (default: the workload's)")
+    ap.add_argument("--initializer-capacity", type=int, default=0,
+                    help="pending-track queue per stepper (default: 16 per slot)")
     ap.add_argument("--tuning", default="",
                     help="launch settings, e.g. along_block_size=64,along_persistent=0")
     args = ap.parse_args(argv)
@@ -45,7 +47,8 @@ def main(argv=None):
     params = Params(physics_file(wl["physics"]), wl["geometry"],
                     field_tesla=wl["field"], msc=wl["msc"],
                     track_order=args.track_order, precision=args.precision,
-                    reentrant_looping=wl.get("reentrant_looping", False))
+                    reentrant_looping=wl.get("reentrant_looping", False),
+                    initializer_capacity=args.initializer_capacity)
     stepper = Stepper(params, args.slots or wl["slots"], seed=wl["seed"],
                       use_graph=args.graph)
     if args.tuning:

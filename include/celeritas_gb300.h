@@ -426,7 +426,10 @@ int gbx_stepper_read_step_output(gbx_stepper* stepper,
  *                       tracks (0: always)
  *   "sort"              0: action sorts off (each action kernel visits
  *                       every slot), 1: on; reset by the sort threshold
- * Results do not depend on these settings. Setting one drops the captured
+ * Results do not depend on these settings (in the mixed build, the
+ * 512-thread instances may round an FP32 deposit differently in its last
+ * bit, their compiled arithmetic being contracted separately). Setting one
+ * drops the captured
  * step graphs. */
 int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value);
 int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* value);

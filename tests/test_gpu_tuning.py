@@ -108,21 +108,26 @@ def test_autotuner_picks_a_measured_candidate(gb):
     assert all(t.track_steps > 0 for t in measured)
     # 512 threads run in both kernel forms (registers capped at 128)
     assert not [t for t in trials if not t.seconds]
-    assert {(t.config["along_block_size"], t.config["along_persistent"])
+    assert {(t.config.get("along_block_size"), t.config.get("along_persistent"))
             for t in measured} >= {(512, 0), (512, 1)}
     assert best["slots"] in (1 << 14, 1 << 15)
 
 
-def test_large_blocks_give_the_same_results(gb):
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_large_blocks_give_the_same_results(gb, precision):
     """512-thread blocks (the register-capped kernel instances) transport
-    each event exactly as 256-thread blocks do."""
+    each event as 256-thread blocks do: exactly in the FP64 build (no
+    contraction, the same operations in both instances); in the mixed
+    build, whose compiler contracts multiply-adds per instance, within FP32
+    rounding of a deposit."""
     prim = events()
     base = None
+    rtol = EDEP_RTOL if precision == "double" else 1e-6
     for persistent in (0, 1):
         for threads in (256, 512):
-            st = gb.Stepper(cms_params(gb, "mixed"), SLOTS, seed=5)
+            st = gb.Stepper(cms_params(gb, precision), SLOTS, seed=5)
             st.set_tuning(along_block_size=threads, along_persistent=persistent)
             edep = per_event_edep(st, prim)
             if base is None:
                 base = edep
-            np.testing.assert_allclose(edep, base, rtol=EDEP_RTOL)
+            np.testing.assert_allclose(edep, base, rtol=rtol)
