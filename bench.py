@@ -924,33 +924,43 @@ def run_serving(args, wl):
             reqs = stream(float(rate), wl["duration"], rate)
             summary = server.serve(reqs)
             summary["rate"] = rate
-            summary["arrivals"] = [r.arrival for r in reqs]
+            summary["requests"] = [serving.Request(r.event_id, r.geometry, r.primaries,
+                                                   r.arrival) for r in reqs]
             runs.append(summary)
         clocks.active = False
     del server, steppers
 
-    # Plain FP64 path, one request at a time: service times of a sample of
-    # requests (each inserted alone and stepped until empty)
+    # Plain FP64 path, one request at a time in arrival order on the host
+    # clock (a FIFO single server): the first 'sequential_sample' requests
+    # of each rate's stream, each transported alone from when it has
+    # arrived and the previous one has finished
     plain = make_steppers("double", 0, False)
-    sample = stream(200.0, 0.25, 424242)[:args.sequential_sample]
-    service = []
-    for r in sample:
-        st = plain[r.geometry]
-        t0 = time.perf_counter()
-        res = [st.step(r.primaries)] + st.run(max_steps=MAX_STEPS, batch=64)
-        service.append(time.perf_counter() - t0)
-        if res[-1].alive or res[-1].queued:
-            raise RuntimeError("plain FP64 transport did not finish")
-    service = np.array(service)
-    rng = np.random.default_rng(wl["seed"])
     for run in runs:
-        arr = np.array(run.pop("arrivals"))
-        svc = rng.choice(service, size=len(arr))
-        lat = serving.sequential_latencies(arr, svc)
-        span = max(float((arr + lat).max() - arr.min()), 1e-9)
-        run["sequential_fp64"] = {"p50_ms": float(np.percentile(lat, 50) * 1e3),
-                                  "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                                  "events_per_s": len(arr) / span}
+        reqs = run.pop("requests")[:args.sequential_sample]
+        first = reqs[0].arrival
+        t0 = time.perf_counter() - first
+        lat, service, last = [], [], first
+        for r in reqs:
+            now = time.perf_counter() - t0
+            if now < r.arrival:
+                time.sleep(r.arrival - now)
+            start = time.perf_counter() - t0
+            st = plain[r.geometry]
+            res = [st.step(r.primaries)] + st.run(max_steps=MAX_STEPS, batch=64)
+            if res[-1].alive or res[-1].queued:
+                raise RuntimeError("plain FP64 transport did not finish")
+            done = time.perf_counter() - t0
+            service.append(done - start)
+            lat.append(done - r.arrival)
+            last = done
+        lat = np.array(lat)
+        run["sequential_fp64"] = {
+            "requests": len(reqs), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "events_per_s": len(reqs) / max(last - first, 1e-9),
+            "service_ms_mean": float(np.mean(service) * 1e3),
+            "timing": "measured: the first requests of the same arrival stream served "
+                      "one at a time by the plain FP64 path, host clock"}
     served = runs[-1]["events_per_s"]
     if dist:
         t = torch.tensor([served], device="cuda", dtype=torch.float64)
@@ -979,10 +989,6 @@ def run_serving(args, wl):
         "e2e": {"value": served, "unit": "events/s",
                 "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
         "serving": runs,
-        "sequential_fp64": {"service_ms_mean": float(service.mean() * 1e3),
-                            "service_ms_p99": float(np.percentile(service, 99) * 1e3),
-                            "events_per_s": 1.0 / float(service.mean()),
-                            "sample": len(service)},
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -1050,6 +1056,24 @@ def run_batching(args, wl):
         default = make_stepper(wl["slots"])
         t_def, n_def = timed(default)
         del default
+        all_events = None
+        if args.c4_all:
+            # Every event of the workload in flight together: all primaries
+            # inserted at once into the tuned stepper (the pending-track
+            # queue takes the primaries waiting for slots and the
+            # secondaries of the showers under way), stepped to completion
+            allp = make_uneven_events(wl, wl["events"], seed=500 + rank)
+            st = make_stepper(best["slots"])
+            st.set_tuning(**{k: v for k, v in best.items() if k != "slots"})
+            autotune.transport(st, calib)  # warm-up: graph capture
+            secs, steps = autotune.transport(st, allp, max_steps=200000)
+            all_events = {"events": int(wl["events"]), "primaries": int(len(allp)),
+                          "energy_tev": float(allp["energy"].sum() / 1e6),
+                          "seconds": secs, "track_steps": int(steps),
+                          "track_steps_per_s": steps / secs,
+                          "events_per_s": wl["events"] / secs,
+                          "timing": "host clock around the one transport (synchronized)"}
+            del st
         clocks.active = False
     if dist:
         t = torch.tensor([t_tuned, t_def], device="cuda", dtype=torch.float64)
@@ -1090,6 +1114,7 @@ def run_batching(args, wl):
                                  "note": t.note} for t in trials]},
         "untuned": {"value": n_def / t_def, "events_per_s": world * nev * args.steps / t_def,
                     "slots": wl["slots"]},
+        "all_events_in_flight": all_events,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -1135,7 +1160,10 @@ def main():
     parser.add_argument("--c2-steps", type=int, default=5,
                         help="event batches (c3): timed steps of the extra c2 line; 0: none")
     parser.add_argument("--sequential-sample", type=int, default=40,
-                        help="c5: requests timed alone on the plain FP64 path")
+                        help="c5: requests of each stream served one at a time by the "
+                             "plain FP64 path")
+    parser.add_argument("--no-c4-all", dest="c4_all", action="store_false",
+                        help="c4: skip the transport of all events in flight together")
     parser.add_argument("--primary-generation", action="store_true",
                         help="also time device primary generation against host insertion")
     parser.add_argument("--step-output", action="store_true",

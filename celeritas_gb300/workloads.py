@@ -82,7 +82,8 @@ WORKLOADS = {
                description="batching: CMS-like, events with log-uniform 1-1000 "
                            "e-/gamma primaries of log-uniform 0.1-100 GeV, |eta| < 1.5, "
                            "3.8 T; one bench step = 64 of the 4096 events in flight "
-                           "together; launch configuration autotuned"),
+                           "together, then all 4096 in flight together in one "
+                           "transport; launch configuration autotuned"),
     # Serving: Poisson arrivals, Pareto(1.5) primaries per event capped at
     # 5000, CMS-like (as c3) or calorimeter (as c2) 50/50, one pool of 2^21
     # slots per geometry (2^22 in all) with queues of 16 x slots
