@@ -129,3 +129,56 @@ def test_cms_tracks_stay_in_their_volumes(built_lib, precision):
             f"{int(outside.sum())} tracks outside their silicon shell, e.g. r = "
             f"{r[outside][:3]} in layers {[det[i] for i in d[outside][:3]]}")
     assert checked > 100
+
+
+CMS_BATCHES = 12
+CMS_EVENTS_PER_BATCH = 10
+CMS_PRIMARIES_PER_EVENT = 20
+
+
+def cms_batches(gb, precision):
+    """Per-volume deposition of CMS-like batches (3.8 T, MSC; e-/gamma of
+    1-10 GeV, |eta| < 1.5), the same primaries for both builds"""
+    from celeritas_gb300.primaries import eta_beam
+
+    params = gb.Params(gb.physics_file("cms"), "cms", field_tesla=(0.0, 0.0, 3.8), msc=True,
+                       track_order="reindex_both_action", precision=precision,
+                       reentrant_looping=True)
+    out = []
+    n = CMS_EVENTS_PER_BATCH * CMS_PRIMARIES_PER_EVENT
+    for b in range(CMS_BATCHES):
+        st = gb.Stepper(params, 1 << 18, seed=300 + b)
+        prim = eta_beam(n, emin=1000.0, emax=10000.0, pdgs=(11, 22), seed=50 + b,
+                        num_events=CMS_EVENTS_PER_BATCH)
+        res = [st.step(prim)] + st.run(max_steps=20000, batch=64)
+        assert not (res[-1].alive or res[-1].queued), "transport did not finish"
+        out.append(st.energy_deposition())
+    return np.array(out)
+
+
+def test_cms_mixed_agrees_with_fp64(built_lib):
+    """CMS-like batches, paired by their primaries: per-volume chi-square
+    (each volume's mean difference over its standard error, as the tail
+    probability of a Student t turned into a normal deviate) with p > 0.01,
+    and the total within 0.5%."""
+    from scipy import stats
+
+    import celeritas_gb300 as gb
+    from celeritas_gb300.build import build
+
+    gb.load_library(built_lib)
+    gb.load_library(build(precision="mixed"), precision="mixed")
+    fp64 = cms_batches(gb, "double")
+    mixed = cms_batches(gb, "mixed")
+    d = mixed - fp64
+    n = len(d)
+    se = d.std(axis=0, ddof=1) / np.sqrt(n)
+    used = se > 0
+    t = d.mean(axis=0)[used] / se[used]
+    z = stats.norm.isf(stats.t.sf(np.abs(t), n - 1))
+    chi2 = float((z ** 2).sum())
+    dof = int(used.sum())
+    p = stats.chi2.sf(chi2, dof)
+    assert p > CHI2_PMIN, (chi2, dof, p)
+    rel = abs(mixed.sum() - fp64.sum()) / fp64.sum()
+    assert rel < TOTAL_RTOL, rel
