@@ -431,7 +431,8 @@ class Stepper:
         _check(self._lib, self._lib.gbx_stepper_reseed(self._handle, int(event_id)))
 
     def set_tuning(self, **settings):
-        """Launch tuning: along_block_size, along_persistent, sort_threshold."""
+        """Launch tuning: along_block_size, along_persistent, sort_threshold,
+        sort, partition_slots."""
         for name, value in settings.items():
             _check(self._lib, self._lib.gbx_stepper_set_tuning(
                 self._handle, name.encode(), int(value)))

@@ -346,6 +346,8 @@ CoreParams::CoreParams(Input const& inp)
     std::size_t o_box = pk.add(h.volumes);
     std::size_t o_no = pk.add(h.neighbor_offset);
     std::size_t o_nb = pk.add(h.neighbors);
+    std::size_t o_ss = pk.add(h.sorted_surfaces);
+    std::size_t o_sk = pk.add(h.sorted_key);
     std::size_t o_vm = pk.add(h.volume_material);
     std::size_t o_vd = pk.add(h.volume_detector);
 
@@ -387,6 +389,8 @@ CoreParams::CoreParams(Input const& inp)
     device_.geo.volumes = reinterpret_cast<VolumeRecord const*>(base + o_box);
     device_.geo.neighbor_offset = reinterpret_cast<size_type const*>(base + o_no);
     device_.geo.neighbors = reinterpret_cast<size_type const*>(base + o_nb);
+    device_.geo.sorted_surfaces = reinterpret_cast<size_type const*>(base + o_ss);
+    device_.geo.sorted_key = reinterpret_cast<float const*>(base + o_sk);
     device_.geo.volume_material = reinterpret_cast<size_type const*>(base + o_vm);
     device_.geo.volume_detector = reinterpret_cast<size_type const*>(base + o_vd);
 }
@@ -602,6 +606,7 @@ CoreState::CoreState(CoreParams const& params,
     // diverged FP64 multiple-scattering code makes it slower
     ctx_.along_block_size = block_size;
     ctx_.sort_enabled = true;
+    ctx_.partition_slots = false;
     ctx_.persistent_blocks = sizeof(real_type) < sizeof(double)
                                  ? persistent_along_blocks(ctx_.along_block_size)
                                  : 0;
@@ -860,6 +865,15 @@ void CoreState::set_tuning(std::string const& name, long long value)
     {
         ctx_.sort_enabled = value != 0;
     }
+    else if (name == "partition_slots")
+    {
+        if (value && !ctx_.params.rng_per_track)
+        {
+            throw std::runtime_error(
+                "partition_slots needs per-track random streams (rng_per_track)");
+        }
+        ctx_.partition_slots = value != 0;
+    }
     else
     {
         throw std::runtime_error("unknown tuning parameter '" + name + "'");
@@ -874,6 +888,8 @@ long long CoreState::tuning(std::string const& name) const
         return ctx_.persistent_blocks > 0;
     if (name == "sort")
         return ctx_.sort_enabled;
+    if (name == "partition_slots")
+        return ctx_.partition_slots;
     throw std::runtime_error("unknown tuning parameter '" + name + "'");
 }
 

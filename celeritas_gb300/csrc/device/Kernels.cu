@@ -142,6 +142,52 @@ __global__ __launch_bounds__(block_size) void initialize_tracks_kernel(
     }
 }
 
+//! Track initialization with partitioned slots: the same initializers as
+//! initialize_tracks_kernel, but a charged track takes the next vacancy from
+//! the front of the (ascending) list and a neutral one the next from the
+//! back. The front and back runs together cover num_new distinct vacancies;
+//! the vacancies left between them are not read again before the end of the
+//! step rebuilds the list. Which slot a track gets depends on the order in
+//! which warps claim them, which is why this needs per-track random streams.
+__global__ __launch_bounds__(block_size) void initialize_tracks_partitioned_kernel(
+    ParamsData p, StateData s)
+{
+    size_type tid = thread_slot();
+    Counters const c = *s.counters;
+    size_type num_new = min_of(c.num_vacancies, c.num_initializers);
+    if (blockIdx.x * blockDim.x >= num_new)
+        return;
+    bool const valid = tid < num_new;
+    bool charged = false;
+    if (valid)
+    {
+        TrackInitializer const& init = s.initializers[c.num_initializers - tid - 1];
+        charged = p.particles[init.particle_id].charge != 0;
+    }
+    // One atomic per warp and side: ranks within the warp by ballot
+    unsigned int const lane = threadIdx.x & 31u;
+    unsigned int const lt = (1u << lane) - 1u;
+    unsigned int const front = __ballot_sync(0xffffffffu, valid && charged);
+    unsigned int const back = __ballot_sync(0xffffffffu, valid && !charged);
+    size_type front_base = 0;
+    size_type back_base = 0;
+    if (lane == 0)
+    {
+        if (front)
+            front_base = atomicAdd(&s.counters->num_taken_front, __popc(front));
+        if (back)
+            back_base = atomicAdd(&s.counters->num_taken_back, __popc(back));
+    }
+    front_base = __shfl_sync(0xffffffffu, front_base, 0);
+    back_base = __shfl_sync(0xffffffffu, back_base, 0);
+    if (!valid)
+        return;
+    size_type const slot
+        = charged ? s.vacancies[front_base + __popc(front & lt)]
+                  : s.vacancies[c.num_vacancies - 1 - back_base - __popc(back & lt)];
+    init_track_at(p, s, c, tid, slot);
+}
+
 __global__ void finish_initialize_kernel(StateData s,
                                          StepRecord* log,
                                          size_type log_capacity,
@@ -151,6 +197,8 @@ __global__ void finish_initialize_kernel(StateData s,
     size_type num_new = min_of(c.num_vacancies, c.num_initializers);
     c.num_initializers -= num_new;
     c.num_vacancies -= num_new;
+    c.num_taken_front = 0;
+    c.num_taken_back = 0;
     c.num_active = s.size - c.num_vacancies;
     // pre-step clears the secondary stack
     c.secondary_stack_size = 0;
@@ -820,8 +868,18 @@ void launch_generate_primaries(LaunchContext const& ctx,
 
 void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream)
 {
-    initialize_tracks_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-        ctx.params, ctx.state);
+    if (ctx.partition_slots)
+    {
+        initialize_tracks_partitioned_kernel<<<num_blocks_for(ctx.state.size),
+                                               block_size,
+                                               0,
+                                               stream>>>(ctx.params, ctx.state);
+    }
+    else
+    {
+        initialize_tracks_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+            ctx.params, ctx.state);
+    }
     finish_initialize_kernel<<<1, 1, 0, stream>>>(
         ctx.state, ctx.log, ctx.log_capacity, ctx.step_index);
 }

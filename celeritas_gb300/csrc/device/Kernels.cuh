@@ -69,6 +69,10 @@ struct LaunchContext
     //! block_size) and whether the action sorts run this step
     int along_block_size;
     bool sort_enabled;
+    //! Tuning: new charged tracks take the lowest vacant slots and neutral
+    //! ones the highest (per-track random streams only), so that each
+    //! along-step kernel's sorted range covers mostly contiguous slots
+    bool partition_slots;
     StepRecord* log;  //!< Step log (ring buffer)
     size_type log_capacity;
     size_type* step_index;  //!< Device-resident step counter

@@ -296,6 +296,14 @@ struct GeoParams
     double tol_rel;
     size_type const* volume_material;  //!< [num_volumes], invalid if none
     size_type const* volume_detector;  //!< [num_volumes], invalid if none
+    //! Surfaces of each kind sorted by value, ties by ID: planes normal to
+    //! x, y and z, then z cylinders ([sorted_offset[k], sorted_offset[k+1])
+    //! for kind k = surface type). The background's searches walk them in
+    //! the order a ray meets them. sorted_key is each value rounded to FP32
+    //! (a cylinder's radius), used only for conservative index bounds.
+    size_type sorted_offset[5];
+    size_type const* sorted_surfaces;
+    float const* sorted_key;
 };
 
 //---------------------------------------------------------------------------//
@@ -517,7 +525,11 @@ struct Counters
     size_type num_pending_primaries;
     size_type error_flags;
     size_type num_hits;  //!< Step-output records held on the device
-    size_type pad[6];
+    //! Vacancies taken this step from the front (charged tracks) and the
+    //! back (neutral tracks) of the list when slots are partitioned
+    size_type num_taken_front;
+    size_type num_taken_back;
+    size_type pad[4];
 };
 
 //---------------------------------------------------------------------------//

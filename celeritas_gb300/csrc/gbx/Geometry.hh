@@ -40,6 +40,40 @@ struct Propagation
     bool looping;
 };
 
+//! First index in [lo, hi) whose sorted key is not below x (hi if none)
+GBX_FORCEINLINE size_type key_lower_bound(float const* key,
+                                          size_type lo,
+                                          size_type hi,
+                                          float x)
+{
+    while (lo < hi)
+    {
+        size_type const mid = lo + (hi - lo) / 2;
+        if (key[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+//! First index in [lo, hi) whose sorted key is above x (hi if none)
+GBX_FORCEINLINE size_type key_upper_bound(float const* key,
+                                          size_type lo,
+                                          size_type hi,
+                                          float x)
+{
+    while (lo < hi)
+    {
+        size_type const mid = lo + (hi - lo) / 2;
+        if (!(x < key[mid]))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
 class GeoTrackView
 {
   public:
@@ -247,6 +281,32 @@ class GeoTrackView
                 dist[0] = r0;
         }
     }
+
+    //! Accepted background crossing with the least (distance, surface ID)
+    struct Crossing
+    {
+        size_type surf;  //!< invalid_id while none is accepted
+        double dist;  //!< Its distance (the step limit while none)
+        std::int8_t sense;  //!< Sense of the crossed surface in the new volume
+    };
+    //! Largest distance at which a crossing can still replace the current
+    //! one (at equal distance the lower surface ID wins)
+    static GBX_FORCEINLINE double crossing_limit(Crossing const& hit)
+    {
+        return hit.dist;
+    }
+    GBX_FUNCTION void consider_crossing(size_type surf,
+                                        double d,
+                                        Real3 const& pos,
+                                        Real3 const& dir,
+                                        double bump,
+                                        double max_step,
+                                        Crossing* hit) const;
+    GBX_FUNCTION void background_crossing(Real3 const& pos,
+                                          Real3 const& dir,
+                                          size_type cur_surf,
+                                          double max_step,
+                                          Crossing* hit) const;
 
     //! Distance from a point to a surface (for the safety): the nearest
     //! intersection along the surface normal pointing toward the surface
@@ -470,76 +530,11 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
     }
     else
     {
-        // Implicit background: the reference visits crossings by increasing
-        // (distance, surface ID) and accepts the first whose bumped point lies
-        // inside a neighboring volume. Acceptance depends on that crossing
-        // alone, so the first accepted crossing is the (distance, surface)
-        // minimum over accepted crossings: one pass over the surfaces, testing
-        // only candidates that would improve the current best, gives the same
-        // hit with one intersection per surface instead of one scan per
-        // crossing.
-        double bump = p_.tol_abs;
-        for (int i = 0; i < 3; ++i)
-        {
-            bump = max_of(bump, p_.tol_rel * std::fabs(pos[i]));
-        }
-        for (size_type surf = 0; surf < p_.num_surfaces; ++surf)
-        {
-            double dd[2];
-            this->intersect(surf, pos, dir, surf == cur_surf, dd, max_step);
-            for (int k = 0; k < 2; ++k)
-            {
-                double const d = dd[k];
-                if (!(d <= max_step))
-                    continue;
-                if (hit_surf != invalid_id
-                    && !(d < hit_dist || (d == hit_dist && surf < hit_surf)))
-                {
-                    continue;
-                }
-                Real3 bumped = pos;
-                axpy(d + bump, dir, &bumped);
-                // Neighbors of this surface
-                size_type nbeg = p_.neighbor_offset[surf];
-                size_type nend = p_.neighbor_offset[surf + 1];
-                bool found = false;
-                bool found_outside = false;
-                if (nend - nbeg >= 3)
-                {
-                    // Many neighbors: locate by position (non-overlapping)
-                    size_type v = this->find_volume_at(
-                        bumped, invalid_id, invalid_id, nullptr);
-                    if (v != p_.background && v != p_.exterior)
-                    {
-                        found = true;
-                        // Sense of the crossed surface evaluated at the
-                        // bumped point inside the new volume, flipped
-                        found_outside
-                            = !sense_outside(this->surface_q(surf, bumped));
-                    }
-                }
-                else
-                {
-                    for (size_type n = nbeg; n < nend; ++n)
-                    {
-                        size_type v = p_.neighbors[n];
-                        if (this->volume_inside(v, bumped, invalid_id, false, nullptr))
-                        {
-                            found = true;
-                            found_outside
-                                = !sense_outside(this->surface_q(surf, bumped));
-                            break;
-                        }
-                    }
-                }
-                if (found)
-                {
-                    hit_surf = surf;
-                    hit_dist = d;
-                    hit_sense = found_outside ? 1 : -1;
-                }
-            }
-        }
+        Crossing hit{invalid_id, max_step, 0};
+        this->background_crossing(pos, dir, cur_surf, max_step, &hit);
+        hit_surf = hit.surf;
+        hit_dist = hit.dist;
+        hit_sense = hit.sense;
     }
 
     s_.next_step[slot_] = hit_dist;
@@ -548,6 +543,248 @@ GBX_FUNCTION Propagation GeoTrackView::find_next_step(double max_step)
     result.distance = hit_dist;
     result.boundary = (hit_surf != invalid_id);
     return result;
+}
+
+//! Test one background crossing: a candidate at distance d on surface surf
+//! that would improve the current crossing is accepted if the point bumped
+//! past it lies inside a volume neighboring the surface
+GBX_FUNCTION void GeoTrackView::consider_crossing(size_type surf,
+                                                  double d,
+                                                  Real3 const& pos,
+                                                  Real3 const& dir,
+                                                  double bump,
+                                                  double max_step,
+                                                  Crossing* hit) const
+{
+    if (!(d <= max_step))
+        return;
+    if (hit->surf != invalid_id
+        && !(d < hit->dist || (d == hit->dist && surf < hit->surf)))
+    {
+        return;
+    }
+    Real3 bumped = pos;
+    axpy(d + bump, dir, &bumped);
+    // Neighbors of this surface
+    size_type nbeg = p_.neighbor_offset[surf];
+    size_type nend = p_.neighbor_offset[surf + 1];
+    bool found = false;
+    bool found_outside = false;
+    if (nend - nbeg >= 3)
+    {
+        // Many neighbors: locate by position (non-overlapping)
+        size_type v = this->find_volume_at(bumped, invalid_id, invalid_id, nullptr);
+        if (v != p_.background && v != p_.exterior)
+        {
+            found = true;
+            // Sense of the crossed surface evaluated at the bumped point
+            // inside the new volume, flipped
+            found_outside = !sense_outside(this->surface_q(surf, bumped));
+        }
+    }
+    else
+    {
+        for (size_type n = nbeg; n < nend; ++n)
+        {
+            size_type v = p_.neighbors[n];
+            if (this->volume_inside(v, bumped, invalid_id, false, nullptr))
+            {
+                found = true;
+                found_outside = !sense_outside(this->surface_q(surf, bumped));
+                break;
+            }
+        }
+    }
+    if (found)
+    {
+        hit->surf = surf;
+        hit->dist = d;
+        hit->sense = found_outside ? 1 : -1;
+    }
+}
+
+//! Next boundary crossing of a track in the implicit background.
+//!
+//! The reference visits crossings by increasing (distance, surface ID) and
+//! accepts the first whose bumped point lies inside a neighboring volume
+//! (src/orange/univ/detail/Utils.hh, BackgroundImpl in SimpleUnitTracker).
+//! Acceptance depends on that crossing alone, so the result is the least
+//! (distance, surface ID) over accepted crossings, whatever order they are
+//! tested in; a crossing is tested only if it would improve the current one.
+//!
+//! Instead of solving every surface, the search walks the surfaces of each
+//! kind in the order the ray meets them and stops at the first whose
+//! distance exceeds the current crossing's. Each walk's distances are
+//! computed exactly as the per-surface solve computes them, and they are
+//! monotone along the walk in floating point, not only in exact arithmetic:
+//! - planes normal to axis k, moving toward +k: d = (v - x) / n grows with
+//!   the plane's value v (IEEE subtraction and division are monotone);
+//! - z cylinders of squared radius v: the solve forms c = (x^2 + y^2 - v)/a,
+//!   compares hba^2 with c and takes t = sqrt(hba^2 - c); c falls as v
+//!   grows, so whether the ray reaches the cylinder, the far root
+//!   -hba + t (growing with v) and the near root -hba - t (falling with v)
+//!   are all monotone. Far roots are walked upward from the radius of
+//!   closest approach, near roots downward from the track's radius.
+//! Index bounds from the FP32 keys only ever start a walk earlier than
+//! needed (rounding to FP32 is monotone too), and an FP32 radial bound |r -
+//! R| stops a cylinder walk only where every root is beyond the limit, with
+//! the same margin as the per-surface reachability test. The result is
+//! therefore the crossing a solve of every surface would give.
+GBX_FUNCTION void GeoTrackView::background_crossing(Real3 const& pos,
+                                                    Real3 const& dir,
+                                                    size_type cur_surf,
+                                                    double max_step,
+                                                    Crossing* hit) const
+{
+    double bump = p_.tol_abs;
+    for (int i = 0; i < 3; ++i)
+    {
+        bump = max_of(bump, p_.tol_rel * std::fabs(pos[i]));
+    }
+#ifdef GBX_GEO_SCAN_BACKGROUND
+    // Every surface in ID order (the CPU oracle's restatement, compiled
+    // only there to check the ordered walks below)
+    for (size_type surf = 0; surf < p_.num_surfaces; ++surf)
+    {
+        double dd[2];
+        this->intersect(surf, pos, dir, surf == cur_surf, dd, max_step);
+        for (int k = 0; k < 2; ++k)
+            this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
+    }
+    return;
+#endif
+    size_type const* sorted = p_.sorted_surfaces;
+    float const* key = p_.sorted_key;
+
+    // The surface the track is on: its crossing comes from the on-surface
+    // solve
+    if (cur_surf != invalid_id)
+    {
+        double dd[2];
+        this->intersect(cur_surf, pos, dir, true, dd);
+        for (int k = 0; k < 2; ++k)
+            this->consider_crossing(cur_surf, dd[k], pos, dir, bump, max_step, hit);
+    }
+
+    // Planes of each axis, in the order the ray meets them. A plane's
+    // distance |v - x| / |n| is at least |v - x| (1 - 2^-40) for a unit
+    // direction rounded to FP64, which ends the walk without a division.
+    for (int ax = 0; ax < 3; ++ax)
+    {
+        double const n = dir[ax];
+        if (n == 0)
+            continue;
+        size_type const beg = p_.sorted_offset[ax];
+        size_type const end = p_.sorted_offset[ax + 1];
+        double const x = pos[ax];
+        float const xf = static_cast<float>(x);
+        if (n > 0)
+        {
+            // Planes ahead (v > x) have keys at or above FP32(x)
+            for (size_type i = key_lower_bound(key, beg, end, xf); i < end; ++i)
+            {
+                size_type const surf = sorted[i];
+                double const gap = p_.surfaces[surf].value - x;
+                if (!(gap > 0) || surf == cur_surf)
+                    continue;
+                if (gap * (1 - 0x1p-40) > crossing_limit(*hit))
+                    break;
+                double const d = gap / n;
+                if (d > 0)
+                    this->consider_crossing(surf, d, pos, dir, bump, max_step, hit);
+            }
+        }
+        else
+        {
+            // Planes behind (v < x) have keys at or below FP32(x)
+            for (size_type i = key_upper_bound(key, beg, end, xf); i-- > beg;)
+            {
+                size_type const surf = sorted[i];
+                double const gap = p_.surfaces[surf].value - x;
+                if (!(gap < 0) || surf == cur_surf)
+                    continue;
+                if (-gap * (1 - 0x1p-40) > crossing_limit(*hit))
+                    break;
+                double const d = gap / n;
+                if (d > 0)
+                    this->consider_crossing(surf, d, pos, dir, bump, max_step, hit);
+            }
+        }
+    }
+
+    // Z cylinders. The per-surface solve finds none when traveling along the
+    // axis.
+    size_type const cbeg = p_.sorted_offset[surf_czc];
+    size_type const cend = p_.sorted_offset[surf_czc + 1];
+    constexpr double sqrt_quadratic = 1e-5;
+    if (cbeg == cend || 1 - ipow<2>(dir.z) < ipow<2>(sqrt_quadratic))
+        return;
+    float const xf = static_cast<float>(pos.x);
+    float const yf = static_cast<float>(pos.y);
+    float const rf = std::sqrt(xf * xf + yf * yf);
+    auto radial_margin = [](float radius, float limit) {
+        return 1e-5f * (radius + limit) + 1e-6f;
+    };
+
+    // Near roots (entering a smaller cylinder while moving inward), walked
+    // down from the track's radius r: they grow as the radius falls.
+    // Cylinders with keys above FP32(r) (1 + 1e-6) are outside r and have no
+    // near root.
+    for (size_type i = key_upper_bound(key, cbeg, cend, rf + (1e-6f * rf + 1e-20f));
+         i-- > cbeg;)
+    {
+        size_type const surf = sorted[i];
+        if (surf == cur_surf)
+            continue;
+        double const limit = crossing_limit(*hit);
+        float const limit_f = static_cast<float>(limit);
+        if (rf - key[i] - radial_margin(key[i], limit_f) > limit_f)
+            break;
+        double dd[2];
+        this->intersect(surf, pos, dir, false, dd);
+        if (dd[0] < INFINITY)
+        {
+            if (dd[0] > limit)
+                break;
+            for (int k = 0; k < 2; ++k)
+                this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
+        }
+        else if (!(dd[1] < INFINITY))
+        {
+            // Not reached, or moving outward: nor is any smaller cylinder
+            break;
+        }
+        // Else only a far root (a cylinder at r, or just below it with a
+        // near root that rounds to zero): the upward walk takes it
+    }
+
+    // Far roots, walked up from just below r: they grow with the radius.
+    // Below r - 1e-4 (r + 1) a reached cylinder has a near root of at least
+    // 5e-5 times its far one, so the downward walk above has taken
+    // both of its roots, or stopped where both lie beyond the limit.
+    float const delta = 1e-4f * (rf + 1);
+    for (size_type i = key_lower_bound(key, cbeg, cend, rf - delta); i < cend; ++i)
+    {
+        size_type const surf = sorted[i];
+        if (surf == cur_surf)
+            continue;
+        double const limit = crossing_limit(*hit);
+        float const limit_f = static_cast<float>(limit);
+        if (key[i] - rf - radial_margin(key[i], limit_f) > limit_f)
+            break;
+        double dd[2];
+        this->intersect(surf, pos, dir, false, dd);
+        double const far = (dd[1] < INFINITY) ? dd[1] : dd[0];
+        if (!(far < INFINITY))
+        {
+            // Behind the track or not reached: a larger cylinder may be
+            continue;
+        }
+        if (far > limit)
+            break;
+        for (int k = 0; k < 2; ++k)
+            this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
+    }
 }
 
 GBX_FUNCTION void GeoTrackView::move_to_boundary()
@@ -684,13 +921,65 @@ GBX_FUNCTION double GeoTrackView::find_safety() const
             visit(v.faces[f]);
         }
     }
+#ifdef GBX_GEO_SCAN_BACKGROUND
     else
     {
-        for (size_type s = 0; s < p_.num_surfaces; ++s)
+        for (size_type surf = 0; surf < p_.num_surfaces; ++surf)
+            visit(surf);
+    }
+#else
+    else
+    {
+        // Every surface bounds the background. Planes: the nearest on either
+        // side of the point along each axis (|x - v| grows away from x;
+        // keys below FP32(x) belong to planes below x)
+        size_type const* sorted = p_.sorted_surfaces;
+        float const* key = p_.sorted_key;
+        for (int ax = 0; ax < 3; ++ax)
         {
-            visit(s);
+            size_type const beg = p_.sorted_offset[ax];
+            size_type const end = p_.sorted_offset[ax + 1];
+            double const x = pos[ax];
+            size_type const mid = key_lower_bound(key, beg, end, static_cast<float>(x));
+            for (size_type i = mid; i < end; ++i)
+            {
+                double const v = p_.surfaces[sorted[i]].value;
+                if (v - x > result)
+                    break;
+                result = min_of(result, this->surface_safety(sorted[i], pos));
+            }
+            for (size_type i = mid; i-- > beg;)
+            {
+                double const v = p_.surfaces[sorted[i]].value;
+                if (x - v > result)
+                    break;
+                result = min_of(result, this->surface_safety(sorted[i], pos));
+            }
+        }
+        // Cylinders: outward and inward from the point's radius, until the
+        // FP32 bound above exceeds the minimum (it grows with |r - R|)
+        size_type const cbeg = p_.sorted_offset[surf_czc];
+        size_type const cend = p_.sorted_offset[surf_czc + 1];
+        size_type const mid = key_lower_bound(key, cbeg, cend, rf);
+        auto beyond = [&](size_type i) {
+            float const best = static_cast<float>(result);
+            float const margin = 1e-5f * (key[i] + rf + best) + 1e-6f;
+            return std::fabs(rf - key[i]) - margin > best;
+        };
+        for (size_type i = mid; i < cend; ++i)
+        {
+            if (beyond(i))
+                break;
+            result = min_of(result, this->surface_safety(sorted[i], pos));
+        }
+        for (size_type i = mid; i-- > cbeg;)
+        {
+            if (beyond(i))
+                break;
+            result = min_of(result, this->surface_safety(sorted[i], pos));
         }
     }
+#endif
     return result;
 }
 

@@ -148,15 +148,16 @@ GBX_FUNCTION void process_primary(StateData const& s,
     ti.parent_id = invalid_id;
 }
 
-//! Initialize a vacant slot from an initializer (InitTracksExecutor)
-GBX_FUNCTION void init_track(ParamsData const& p,
-                             StateData const& s,
-                             Counters const& counters,
-                             size_type tid)
+//! Initialize vacant slot 'slot' from initializer 'tid' counted from the
+//! back of the list (InitTracksExecutor)
+GBX_FUNCTION void init_track_at(ParamsData const& p,
+                                StateData const& s,
+                                Counters const& counters,
+                                size_type tid,
+                                size_type slot)
 {
     TrackInitializer const& init
         = s.initializers[counters.num_initializers - tid - 1];
-    size_type const slot = s.vacancies[counters.num_vacancies - tid - 1];
 
     // Sim state
     s.track_id[slot] = init.track_id;
@@ -205,6 +206,18 @@ GBX_FUNCTION void init_track(ParamsData const& p,
     {
         seed_xorwow(s.rng, slot, init.rng_key);
     }
+}
+
+//! Initialize a vacant slot from an initializer: new track 'tid' takes the
+//! tid-th initializer and vacancy from the back of their lists
+//! (InitTracksExecutor)
+GBX_FUNCTION void init_track(ParamsData const& p,
+                             StateData const& s,
+                             Counters const& counters,
+                             size_type tid)
+{
+    init_track_at(
+        p, s, counters, tid, s.vacancies[counters.num_vacancies - tid - 1]);
 }
 
 //! Flag the slot as vacant or occupied and count secondaries that need a

@@ -174,8 +174,10 @@ class CoreState
     Counters counters() const;
     //! Number of completed steps recorded on the device
     size_type step_index() const;
-    //! Launch tuning: "along_block_size" (64, 128, 256), "along_persistent"
-    //! (0/1), "sort" (0/1: whether the action sorts run)
+    //! Launch tuning: "along_block_size" (64, 128, 256, 512),
+    //! "along_persistent" (0/1), "sort" (0/1: whether the action sorts run),
+    //! "partition_slots" (0/1: charged tracks fill vacancies from the front
+    //! of the list, neutral ones from the back; per-track streams only)
     void set_tuning(std::string const& name, long long value);
     long long tuning(std::string const& name) const;
 

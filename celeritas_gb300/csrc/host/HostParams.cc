@@ -1056,6 +1056,37 @@ void Builder::build_geometry()
         hp_.neighbor_offset.push_back(static_cast<size_type>(hp_.neighbors.size()));
     }
 
+    // Surfaces by kind, sorted by value (ties by ID), for the ordered
+    // searches of the implicit background
+    {
+        std::vector<size_type> order(nsurf);
+        for (size_type i = 0; i < nsurf; ++i)
+            order[i] = i;
+        auto const& sf = hp_.surfaces;
+        std::sort(order.begin(), order.end(), [&sf](size_type a, size_type b) {
+            if (sf[a].type != sf[b].type)
+                return sf[a].type < sf[b].type;
+            if (sf[a].value != sf[b].value)
+                return sf[a].value < sf[b].value;
+            return a < b;
+        });
+        hp_.sorted_surfaces = order;
+        hp_.sorted_key.resize(nsurf);
+        for (int k = 0; k < 5; ++k)
+            g.sorted_offset[k] = 0;
+        for (size_type i = 0; i < nsurf; ++i)
+        {
+            SurfaceRecord const& sr = sf[order[i]];
+            if (sr.type < surf_px || sr.type > surf_czc)
+                throw std::runtime_error("unknown surface type");
+            hp_.sorted_key[i] = (sr.type == surf_czc) ? sr.radius
+                                                      : static_cast<float>(sr.value);
+            ++g.sorted_offset[sr.type + 1];
+        }
+        for (int k = 0; k < 4; ++k)
+            g.sorted_offset[k + 1] += g.sorted_offset[k];
+    }
+
     // Detectors: every volume, in order
     hp_.volume_detector.assign(nvol + 2, invalid_id);
     for (size_type b = 1; b <= nvol; ++b)
@@ -1507,6 +1538,8 @@ ParamsData make_host_view(HostParams const& hp)
     p.geo.volumes = hp.volumes.data();
     p.geo.neighbor_offset = hp.neighbor_offset.data();
     p.geo.neighbors = hp.neighbors.data();
+    p.geo.sorted_surfaces = hp.sorted_surfaces.data();
+    p.geo.sorted_key = hp.sorted_key.data();
     p.geo.volume_material = hp.volume_material.data();
     p.geo.volume_detector = hp.volume_detector.data();
     return p;

@@ -120,6 +120,8 @@ struct HostParams
     std::vector<VolumeRecord> volumes;
     std::vector<size_type> neighbor_offset;
     std::vector<size_type> neighbors;
+    std::vector<size_type> sorted_surfaces;  //!< By kind, then value
+    std::vector<float> sorted_key;
     std::vector<size_type> volume_material;
     std::vector<size_type> volume_detector;
     std::vector<std::string> volume_labels;

@@ -426,11 +426,15 @@ int gbx_stepper_read_step_output(gbx_stepper* stepper,
  *                       tracks (0: always)
  *   "sort"              0: action sorts off (each action kernel visits
  *                       every slot), 1: on; reset by the sort threshold
+ *   "partition_slots"   1: new charged tracks take the lowest vacant slots
+ *                       and neutral ones the highest, so the sorted ranges
+ *                       of the along-step kernels cover mostly contiguous
+ *                       slots (only with rng_per_track; error otherwise)
  * Results do not depend on these settings (in the mixed build, the
  * 512-thread instances may round an FP32 deposit differently in its last
- * bit, their compiled arithmetic being contracted separately). Setting one
- * drops the captured
- * step graphs. */
+ * bit, their compiled arithmetic being contracted separately; with
+ * partitioned slots the per-event tallies sum in another order). Setting
+ * one drops the captured step graphs. */
 int gbx_stepper_set_tuning(gbx_stepper* stepper, const char* name, long long value);
 int gbx_stepper_get_tuning(gbx_stepper* stepper, const char* name, long long* value);
 

@@ -37,6 +37,10 @@ PORT_BIN = os.path.join(PORT_DIR, "port_stepper")
 #: The restatement with the host C library's elementary functions instead of
 #: the GB300 build's correctly rounded ones (reproduces REF_BIN)
 PORT_SYSLIBM_BIN = os.path.join(PORT_DIR, "port_stepper_syslibm")
+#: The restatement with the implicit background navigated by solving every
+#: surface (the reference's search), instead of the GB300 path's ordered
+#: walks; only its 'geo-rays' mode is used, to check those walks
+PORT_GEOSCAN_BIN = os.path.join(PORT_DIR, "port_stepper_geoscan")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 #: The reference harness linked with correctly rounded elementary functions
 REF_PINNED_BIN = os.path.join(HERE, "_ref", "ref_harness_pinned")
@@ -60,13 +64,16 @@ def _port_sources():
     return srcs, deps
 
 
-def build_port(force: bool = False, libm: str = "pinned") -> str:
+def build_port(force: bool = False, libm: str = "pinned", geo_scan: bool = False) -> str:
     """Compile the CPU restatement with g++ (no FMA contraction), with the
     correctly rounded elementary functions of the GB300 build ("pinned") or
-    the host C library's ("system")."""
+    the host C library's ("system"); with geo_scan, the background is
+    navigated by solving every surface."""
     if libm not in LIBMS:
         raise ValueError(f"libm must be one of {LIBMS}")
     exe = PORT_BIN if libm == "pinned" else PORT_SYSLIBM_BIN
+    if geo_scan:
+        exe = PORT_GEOSCAN_BIN
     os.makedirs(PORT_DIR, exist_ok=True)
     srcs, deps = _port_sources()
     if (not force and os.path.exists(exe)
@@ -76,6 +83,8 @@ def build_port(force: bool = False, libm: str = "pinned") -> str:
            "-o", exe + ".tmp"] + srcs
     if libm == "system":
         cmd.insert(1, "-DGBX_SYSTEM_LIBM")
+    if geo_scan:
+        cmd.insert(1, "-DGBX_GEO_SCAN_BACKGROUND")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle port build failed:\n" + res.stderr[-4000:])

@@ -29,6 +29,7 @@
 #include <fstream>
 #include <iostream>
 #include <map>
+#include <random>
 #include <string>
 #include <thread>
 #include <vector>
@@ -599,6 +600,135 @@ int bench(int argc, char** argv)
     return 0;
 }
 
+//! Random straight walks through a geometry: every query's next step and
+//! safety as hexadecimal doubles, for comparing two builds of the
+//! navigation (the ordered background search against a solve of every
+//! surface). Usage: geo-rays <physics> <geometry> <num_walks> <seed>
+int geo_rays(int argc, char** argv)
+{
+    if (argc < 6)
+        return 2;
+    HostParams hp = build_params(argv[2], make_geometry(argv[3]), ParamsOptions{});
+    ParamsData const p = make_host_view(hp);
+    size_type const num_walks = std::stoul(argv[4]);
+    std::mt19937_64 gen(std::stoull(argv[5]));
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    HostState st(1, 16, 1, 16, hp.scalars.num_detectors, 0);
+    StateData s = st.view();
+    GeoTrackView geo(p.geo, s, 0);
+
+    // Extent of the world box and of the cylinders
+    double lo[3], hi[3];
+    for (int ax = 0; ax < 3; ++ax)
+    {
+        lo[ax] = hp.surfaces[p.geo.world_faces[2 * ax]].value;
+        hi[ax] = hp.surfaces[p.geo.world_faces[2 * ax + 1]].value;
+    }
+    std::vector<double> radii;
+    for (auto const& sr : hp.surfaces)
+    {
+        if (sr.type == surf_czc)
+            radii.push_back(std::sqrt(sr.value));
+    }
+    auto isotropic = [&] {
+        double const mu = 2 * u(gen) - 1;
+        double const phi = 2 * constants::pi * u(gen);
+        double const st = std::sqrt(1 - mu * mu);
+        return Real3{st * std::cos(phi), st * std::sin(phi), mu};
+    };
+    auto direction = [&] {
+        double const k = u(gen);
+        if (k < 0.05)
+        {
+            // Along an axis, or within 1e-6 of the z axis
+            Real3 d{0, 0, 0};
+            d[static_cast<int>(3 * u(gen)) % 3] = (u(gen) < 0.5) ? -1 : 1;
+            if (u(gen) < 0.5)
+                d = make_unit_vector(Real3{1e-6 * (u(gen) - 0.5), 1e-6 * (u(gen) - 0.5),
+                                           (u(gen) < 0.5) ? -1.0 : 1.0});
+            return d;
+        }
+        if (k < 0.15)
+        {
+            // Nearly tangent to a cylinder through the point: radial
+            // component near zero
+            Real3 d = isotropic();
+            Real3 const r = make_unit_vector(Real3{geo.pos().x, geo.pos().y, 0});
+            if (!std::isnan(r.x))
+            {
+                double const dr = d.x * r.x + d.y * r.y;
+                d = make_unit_vector(Real3{d.x - dr * r.x * (1 - 1e-9 * u(gen)),
+                                           d.y - dr * r.y * (1 - 1e-9 * u(gen)), d.z});
+            }
+            return d;
+        }
+        return isotropic();
+    };
+    auto max_step = [&] {
+        double const k = u(gen);
+        if (k < 0.3)
+            return static_cast<double>(INFINITY);
+        if (k < 0.35)
+            return 1e10;
+        return std::pow(10.0, -6 + 10 * u(gen));
+    };
+
+    size_type background = 0;
+    for (size_type w = 0; w < num_walks; ++w)
+    {
+        Real3 pos;
+        if (!radii.empty() && u(gen) < 0.7)
+        {
+            // Near a cylinder: a radius within 1 cm of one, or exactly on it
+            double r = radii[static_cast<std::size_t>(u(gen) * radii.size()) % radii.size()];
+            if (u(gen) < 0.8)
+                r += 2 * u(gen) - 1;
+            double const phi = 2 * constants::pi * u(gen);
+            pos = {r * std::cos(phi), r * std::sin(phi),
+                   lo[2] + (hi[2] - lo[2]) * u(gen)};
+        }
+        else
+        {
+            for (int ax = 0; ax < 3; ++ax)
+                pos[ax] = lo[ax] + (hi[ax] - lo[ax]) * u(gen);
+        }
+        geo.initialize(pos, Real3{0, 0, 1});
+        if (geo.failed() || geo.is_outside())
+            continue;
+        geo.set_dir(direction());
+        for (int k = 0; k < 40; ++k)
+        {
+            double const step = max_step();
+            Propagation const prop = geo.find_next_step(step);
+            double const safety = geo.is_on_boundary() ? 0.0 : geo.find_safety();
+            background += (geo.volume() == p.geo.background);
+            std::printf("%u %d %u %a %d %u %a\n",
+                        w,
+                        k,
+                        geo.volume(),
+                        prop.distance,
+                        prop.boundary ? 1 : 0,
+                        s.next_surface[0],
+                        safety);
+            if (prop.boundary)
+            {
+                geo.move_to_boundary();
+                geo.cross_boundary();
+                if (geo.is_outside() || geo.failed())
+                    break;
+            }
+            else if (std::isfinite(prop.distance))
+            {
+                geo.move_internal(prop.distance * u(gen));
+            }
+            if (u(gen) < 0.3)
+                geo.set_dir(direction());
+        }
+    }
+    std::fprintf(stderr, "background queries %u\n", background);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv)
@@ -615,6 +745,8 @@ int main(int argc, char** argv)
             return run(argc, argv);
         if (mode == "bench")
             return bench(argc, argv);
+        if (mode == "geo-rays")
+            return geo_rays(argc, argv);
         if (mode == "libm" && argc >= 3)
         {
             // The FP64 elementary functions of the build (gbx/Libm.hh): one

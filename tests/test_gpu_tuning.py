@@ -3,7 +3,8 @@
 With per-track random streams the launch configuration of a stepper changes
 its speed, not its results: every event's energy deposition must be the same
 under each tuning (threads per block of the charged along-step, persistent
-charged kernel, action sorts on or off) and each track order to 1e-12
+charged kernel, action sorts on or off, charged and neutral tracks in
+partitioned slot ranges) and each track order to 1e-12
 relative (the device tally sums with atomics, so only the summation order
 differs). This holds in the mixed-precision build too, whose compiler may
 contract multiply-adds, because sorted and unsorted orders run the same
@@ -59,6 +60,8 @@ TUNINGS = [
     {"sort": 0},
     {"sort_threshold": 1 << 30},
     {"along_persistent": 1, "along_block_size": 128},
+    {"partition_slots": 1},
+    {"partition_slots": 1, "along_persistent": 0, "sort_threshold": 1 << 12},
 ]
 
 
@@ -93,6 +96,14 @@ def test_invalid_tuning_rejected(gb):
     assert st.get_tuning("along_block_size") == before
     # The stepper still transports after the rejected settings
     assert per_event_edep(st, events()).sum() > 0
+    # Partitioned slots need per-track streams: with per-slot streams the
+    # slot a track lands in would change its random sequence
+    shared = gb.Params(gb.physics_file("cms"), "cms", field_tesla=(0.0, 0.0, 3.8), msc=True,
+                       track_order="reindex_both_action", precision="mixed")
+    st = gb.Stepper(shared, SLOTS, seed=5)
+    with pytest.raises(gb.GbxError):
+        st.set_tuning(partition_slots=1)
+    assert st.get_tuning("partition_slots") == 0
 
 
 def test_autotuner_picks_a_measured_candidate(gb):
