@@ -688,6 +688,7 @@ class FieldPropagation
         Real3 const dir0 = geo.dir();
         state_.mom = {momentum * dir0.x, momentum * dir0.y, momentum * dir0.z};
         result_ = {0, geo.is_on_boundary(), false};
+        safe_radius_ = 0;
         step_ = step;
         remaining_ = step;
         remaining_substeps_ = driver_.max_substeps();
@@ -730,7 +731,10 @@ class FieldPropagation
         {
             geo.set_dir(cdir);
         }
-        Propagation linear_step = geo.find_next_step(clen + delta_intersection);
+        double const max_dist = clen + delta_intersection;
+        Propagation linear_step = this->inside_safe_ball(geo, max_dist)
+                                      ? geo.no_crossing(max_dist)
+                                      : geo.find_next_step(max_dist);
         double const update_length = substep.step * linear_step.distance / clen;
         auto is_intercept_close = [&]() {
             double delta_sq = 0;
@@ -813,9 +817,51 @@ class FieldPropagation
     }
 
   private:
+    //! Whether the chord query from the current position reaches no
+    //! surface within max_dist, because the segment lies inside a ball that
+    //! holds no surface of the current volume: then find_next_step would
+    //! return max_dist without a crossing, and no_crossing() leaves the
+    //! same result and state without solving the surfaces. The ball is
+    //! centred where the track stands after its first substep of the step
+    //! (a step of one substep never pays for it), with the safety distance
+    //! there as radius, shrunk by 1e-6 relative and 1e-6 cm so that FP64
+    //! rounding of the safety and of the distances cannot admit a crossing
+    //! the full query would find. Any point of a plane or z cylinder is at
+    //! least the safety distance (|x - v|, |r - R|) from the centre.
+    GBX_FUNCTION bool inside_safe_ball(GeoTrackView& geo, double max_dist)
+    {
+        if (result_.distance == 0 || safe_radius_ < 0 || !geo.is_clear_of_boundary())
+            return false;
+        if (safe_radius_ == 0)
+        {
+            double const radius = geo.find_safety() * (1 - 1e-6) - 1e-6;
+            if (!(radius > 0))
+            {
+                safe_radius_ = -1;
+                return false;
+            }
+            safe_radius_ = radius;
+            center_ = state_.pos;
+        }
+        double const room = safe_radius_ - max_dist;
+        if (!(room > 0))
+            return false;
+        double dsq = 0;
+        for (int i = 0; i < 3; ++i)
+            dsq += ipow<2>(state_.pos[i] - center_[i]);
+        return dsq < room * room;
+    }
+
+  public:
+
+  private:
     FieldDriver driver_;
     OdeState state_;
     Propagation result_;
+    //! Ball free of surfaces: its center and radius (0: not yet measured,
+    //! negative: too small to use)
+    Real3 center_;
+    double safe_radius_;
     double step_;
     double remaining_;
     short remaining_substeps_;

@@ -162,6 +162,22 @@ class GeoTrackView
         s_.next_surface[slot_] = invalid_id;
     }
     GBX_FUNCTION void cross_boundary();
+    //! Whether find_next_step would solve the surfaces: the track is
+    //! neither on a boundary nor flagged to re-enter its volume
+    GBX_FORCEINLINE bool is_clear_of_boundary() const
+    {
+        return s_.surface[slot_] == invalid_id
+               && s_.boundary[slot_] != boundary_reentrant;
+    }
+    //! find_next_step's result and state for a segment of length max_step
+    //! that reaches no surface (the caller has a surface-free ball around it)
+    GBX_FORCEINLINE Propagation no_crossing(double max_step)
+    {
+        s_.next_step[slot_] = max_step;
+        s_.next_surface[slot_] = invalid_id;
+        s_.next_sense[slot_] = 0;
+        return {max_step, false, false};
+    }
     GBX_FUNCTION void set_dir(Real3 const& newdir);
     GBX_FUNCTION double find_safety() const;
 
