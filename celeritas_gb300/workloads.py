@@ -50,7 +50,7 @@ WORKLOADS = {
     "c3": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
                emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
                seed=0, events=1300, msc=True, field=(0.0, 0.0, 3.8),
-               events_per_step=65, tune_primaries=800,
+               events_per_step=65, tune_primaries=3250,
                reentrant_looping=True,
                description="CMS-like: 10 Si shells (0.3 mm, r 4-110 cm), PbWO4 barrel "
                            "(r 129-152 cm), 17 x (5 cm brass + 0.4 cm scintillator) "
@@ -58,18 +58,18 @@ WORKLOADS = {
                            "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
                            "bench step k transports events [65k, 65k + 65), so 20 "
                            "steps cover all 1300 events; launch configuration "
-                           "autotuned on 16 other events"),
+                           "autotuned on 65 other events (one batch)"),
     # c3 in the synthetic R-Z field map of the CMS-like detector (a 3.8 T
     # solenoid with soft edges and a return flux) instead of the uniform field
     "c3rz": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
                  emax=1e5, sigma=None, pdg=None, pdgs=(11, 22), eta_max=1.5, slots=1 << 21,
                  seed=0, events=1300, msc=True, field=(0.0, 0.0, 0.0), rz_field=True,
-                 events_per_step=65, tune_primaries=800, reentrant_looping=True,
+                 events_per_step=65, tune_primaries=3250, reentrant_looping=True,
                  description="CMS-like detector in an R-Z field map (3.8 T solenoid, soft "
                              "edges, return flux), Urban MSC; 1300 events of 50 e-/gamma, "
                              "log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; bench step "
                              "k transports events [65k, 65k + 65); launch configuration "
-                             "autotuned on 16 other events"),
+                             "autotuned on 65 other events (one batch)"),
     # Batching of uneven events: CMS-like detector, 4096 events with primaries
     # per event log-uniform in 1-1000 and energies log-uniform in
     # 0.1-100 GeV (e-/gamma alternating, |eta| < 1.5), all in flight
