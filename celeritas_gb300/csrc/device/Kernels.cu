@@ -773,7 +773,8 @@ __global__ GBX_ALONG_BOUNDS(Threads, 1) void along_charged_persistent_kernel(
                 break;
             slot = offsets ? s.track_slots[first + idx] : idx;
             bool charged;
-            if (!along_prologue<AlongKind::charged>(p, s, slot, &charged))
+            double start_safety;
+            if (!along_prologue<AlongKind::charged>(p, s, slot, &charged, &start_safety))
                 continue;
             if (s.step_length[slot] == 0)
             {
@@ -781,7 +782,7 @@ __global__ GBX_ALONG_BOUNDS(Threads, 1) void along_charged_persistent_kernel(
                 continue;
             }
             GeoTrackView geo(p.geo, s, slot);
-            field_setup(p, s, slot, geo, &fp);
+            field_setup(p, s, slot, geo, &fp, start_safety);
             have = true;
         }
         GeoTrackView geo(p.geo, s, slot);

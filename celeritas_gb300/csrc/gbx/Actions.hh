@@ -243,7 +243,8 @@ template<AlongKind K>
 GBX_FUNCTION bool along_prologue(ParamsData const& p,
                                  StateData const& s,
                                  size_type slot,
-                                 bool* charged)
+                                 bool* charged,
+                                 double* start_safety = nullptr)
 {
     size_type const along = s.along_step_action[slot];
     if (!is_track_valid(s.status[slot]))
@@ -262,11 +263,14 @@ GBX_FUNCTION bool along_prologue(ParamsData const& p,
                || (K == AlongKind::any && along == p.action_along_step);
 
     // MscStepLimitApplier
+    double safety = 0;
     if (*charged && p.msc.enabled)
     {
         XorwowEngine rng(s.rng, slot);
-        msc_limit_step(p, s, slot, rng);
+        safety = msc_limit_step(p, s, slot, rng);
     }
+    if (start_safety)
+        *start_safety = safety;
     return true;
 }
 
@@ -275,7 +279,8 @@ GBX_FUNCTION void field_setup(ParamsData const& p,
                               StateData const& s,
                               size_type slot,
                               GeoTrackView& geo,
-                              FieldPropagation* fp)
+                              FieldPropagation* fp,
+                              double start_safety)
 {
     size_type const pid = s.particle_id[slot];
     real_type const mass = p.particles[pid].mass;
@@ -287,7 +292,7 @@ GBX_FUNCTION void field_setup(ParamsData const& p,
     rhs.coeffi = (p.particles[pid].charge * detail::e_electron)
                  / (1 * (detail::mev_value / constants::c_light));
     fp->set_rhs(rhs);
-    fp->init(geo, momentum, s.step_length[slot]);
+    fp->init(geo, momentum, s.step_length[slot], start_safety);
 }
 
 //! Step limit and looping bookkeeping after a field propagation
@@ -433,7 +438,8 @@ template<AlongKind K>
 GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_type slot)
 {
     bool charged;
-    if (!along_prologue<K>(p, s, slot, &charged))
+    double start_safety;
+    if (!along_prologue<K>(p, s, slot, &charged, &start_safety))
         return;
     // PropagationApplier: straight line, or the uniform-field integrator for
     // charged tracks (which can loop)
@@ -444,7 +450,7 @@ GBX_FUNCTION void along_step_impl(ParamsData const& p, StateData const& s, size_
         {
             FieldOptions const& opt = p.field_options;
             FieldPropagation fp(opt, UniformFieldEquation{});
-            field_setup(p, s, slot, geo, &fp);
+            field_setup(p, s, slot, geo, &fp, start_safety);
             do
             {
                 fp.substep(geo);

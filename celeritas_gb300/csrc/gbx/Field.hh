@@ -666,6 +666,13 @@ class FieldDriver
 //---------------------------------------------------------------------------//
 // Field propagator
 //---------------------------------------------------------------------------//
+#ifdef GBX_CHECK_SAFE_BALL
+//! Chord queries the surface-free ball answered, and those the full query
+//! contradicted (CPU oracle check build only, single-threaded runs)
+inline unsigned long long safe_ball_uses = 0;
+inline unsigned long long safe_ball_mismatches = 0;
+#endif
+
 //! Propagation of a charged track up to 'step' along its curved trajectory,
 //! stopping at the first boundary crossing (FieldPropagator::operator()),
 //! split into its set-up, one substep of its loop and its completion so that
@@ -681,7 +688,10 @@ class FieldPropagation
     {
     }
 
-    GBX_FORCEINLINE void init(GeoTrackView& geo, double momentum, double step)
+    //! Start a propagation; 'start_safety' is a safety distance already
+    //! known at the track's position (0 if none)
+    GBX_FORCEINLINE void
+    init(GeoTrackView& geo, double momentum, double step, double start_safety = 0)
     {
         driver_.reset();
         state_.pos = geo.pos();
@@ -689,6 +699,15 @@ class FieldPropagation
         state_.mom = {momentum * dir0.x, momentum * dir0.y, momentum * dir0.z};
         result_ = {0, geo.is_on_boundary(), false};
         safe_radius_ = 0;
+        if (start_safety > 0 && off_axis(state_.pos))
+        {
+            double const radius = start_safety * (1 - 1e-6) - 1e-6;
+            if (radius > 0)
+            {
+                safe_radius_ = radius;
+                center_ = state_.pos;
+            }
+        }
         step_ = step;
         remaining_ = step;
         remaining_substeps_ = driver_.max_substeps();
@@ -732,9 +751,23 @@ class FieldPropagation
             geo.set_dir(cdir);
         }
         double const max_dist = clen + delta_intersection;
+#ifdef GBX_CHECK_SAFE_BALL
+        // CPU oracle check build: always run the full query, and count the
+        // queries the ball would have answered and any it would have got
+        // wrong
+        bool const ball = this->inside_safe_ball(geo, max_dist);
+        Propagation linear_step = geo.find_next_step(max_dist);
+        if (ball)
+        {
+            ++safe_ball_uses;
+            if (linear_step.boundary || linear_step.distance != max_dist)
+                ++safe_ball_mismatches;
+        }
+#else
         Propagation linear_step = this->inside_safe_ball(geo, max_dist)
                                       ? geo.no_crossing(max_dist)
                                       : geo.find_next_step(max_dist);
+#endif
         double const update_length = substep.step * linear_step.distance / clen;
         auto is_intercept_close = [&]() {
             double delta_sq = 0;
@@ -817,23 +850,37 @@ class FieldPropagation
     }
 
   private:
+    //! Whether the safety distance at a point bounds the distance to every
+    //! surface: on (or within 1e-150 of) the z axis a z cylinder's safety is
+    //! taken as infinite (its normal is undefined there, as in the
+    //! reference's CalcSafetyDistance), so no ball is centred there
+    static GBX_FORCEINLINE bool off_axis(Real3 const& pos)
+    {
+        return ipow<2>(pos.x) + ipow<2>(pos.y) > 1e-300;
+    }
+
     //! Whether the chord query from the current position reaches no
     //! surface within max_dist, because the segment lies inside a ball that
     //! holds no surface of the current volume: then find_next_step would
     //! return max_dist without a crossing, and no_crossing() leaves the
-    //! same result and state without solving the surfaces. The ball is
-    //! centred where the track stands after its first substep of the step
-    //! (a step of one substep never pays for it), with the safety distance
+    //! same result and state without solving the surfaces. Without a known
+    //! safety the ball is centred where the track stands after its first
+    //! substep of the step (a step of one substep never pays for it), with
+    //! the safety distance
     //! there as radius, shrunk by 1e-6 relative and 1e-6 cm so that FP64
     //! rounding of the safety and of the distances cannot admit a crossing
     //! the full query would find. Any point of a plane or z cylinder is at
-    //! least the safety distance (|x - v|, |r - R|) from the centre.
+    //! least the safety distance (|x - v|, |r - R|) from the centre. A
+    //! safety the multiple-scattering step limit measured at the start
+    //! gives the ball from the first substep on.
     GBX_FUNCTION bool inside_safe_ball(GeoTrackView& geo, double max_dist)
     {
-        if (result_.distance == 0 || safe_radius_ < 0 || !geo.is_clear_of_boundary())
+        if (safe_radius_ < 0 || !geo.is_clear_of_boundary())
             return false;
         if (safe_radius_ == 0)
         {
+            if (result_.distance == 0 || !off_axis(state_.pos))
+                return false;
             double const radius = geo.find_safety() * (1 - 1e-6) - 1e-6;
             if (!(radius > 0))
             {

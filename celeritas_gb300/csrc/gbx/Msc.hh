@@ -215,18 +215,22 @@ GBX_FORCEINLINE bool msc_is_applicable(ParamsData const& p,
            && e < real_type(p.msc.high_energy_limit);
 }
 
-//! Limit the step due to multiple scattering (MscStepLimitApplier)
+//! Limit the step due to multiple scattering (MscStepLimitApplier). Returns
+//! the FP64 safety distance at the track's position if the limit computed
+//! it (0 otherwise), which the field propagation reuses.
 template<class G>
-GBX_FUNCTION void msc_limit_step(ParamsData const& p,
-                                 StateData const& s,
-                                 size_type slot,
-                                 G& rng)
+GBX_FUNCTION double msc_limit_step(ParamsData const& p,
+                                   StateData const& s,
+                                   size_type slot,
+                                   G& rng)
 {
     if (!msc_is_applicable(p, s, slot, s.step_length[slot]))
     {
         s.msc_geom_path[slot] = 0;
-        return;
+        return 0;
     }
+    // FP64 safety distance at the step's start when the limit needs it
+    double start_safety = 0;
     size_type const pid = s.particle_id[slot];
     size_type const mid = s.material[slot];
     real_type const energy = s.energy[slot];
@@ -249,7 +253,8 @@ GBX_FUNCTION void msc_limit_step(ParamsData const& p,
         if (!on_boundary)
         {
             real_type const max_step = helper.max_step();
-            safety = geo.find_safety();
+            start_safety = geo.find_safety();
+            safety = start_safety;
             if (safety >= max_step)
             {
                 true_path = phys_step;
@@ -337,6 +342,7 @@ GBX_FUNCTION void msc_limit_step(ParamsData const& p,
     {
         s.post_step_action[slot] = p.action_msc_range;
     }
+    return start_safety;
 }
 
 //! Urban positron correction to the scattering angle width

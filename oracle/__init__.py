@@ -41,6 +41,10 @@ PORT_SYSLIBM_BIN = os.path.join(PORT_DIR, "port_stepper_syslibm")
 #: surface (the reference's search), instead of the GB300 path's ordered
 #: walks; only its 'geo-rays' mode is used, to check those walks
 PORT_GEOSCAN_BIN = os.path.join(PORT_DIR, "port_stepper_geoscan")
+#: The restatement that runs every field chord query in full and counts the
+#: queries the surface-free ball of the GB300 path would have answered, and
+#: any it would have answered wrongly
+PORT_BALLCHECK_BIN = os.path.join(PORT_DIR, "port_stepper_ballcheck")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 #: The reference harness linked with correctly rounded elementary functions
 REF_PINNED_BIN = os.path.join(HERE, "_ref", "ref_harness_pinned")
@@ -64,16 +68,20 @@ def _port_sources():
     return srcs, deps
 
 
-def build_port(force: bool = False, libm: str = "pinned", geo_scan: bool = False) -> str:
+def build_port(force: bool = False, libm: str = "pinned", geo_scan: bool = False,
+               check_ball: bool = False) -> str:
     """Compile the CPU restatement with g++ (no FMA contraction), with the
     correctly rounded elementary functions of the GB300 build ("pinned") or
     the host C library's ("system"); with geo_scan, the background is
-    navigated by solving every surface."""
+    navigated by solving every surface; with check_ball, every field chord
+    query runs in full and the surface-free ball's answers are counted."""
     if libm not in LIBMS:
         raise ValueError(f"libm must be one of {LIBMS}")
     exe = PORT_BIN if libm == "pinned" else PORT_SYSLIBM_BIN
     if geo_scan:
         exe = PORT_GEOSCAN_BIN
+    if check_ball:
+        exe = PORT_BALLCHECK_BIN
     os.makedirs(PORT_DIR, exist_ok=True)
     srcs, deps = _port_sources()
     if (not force and os.path.exists(exe)
@@ -85,6 +93,8 @@ def build_port(force: bool = False, libm: str = "pinned", geo_scan: bool = False
         cmd.insert(1, "-DGBX_SYSTEM_LIBM")
     if geo_scan:
         cmd.insert(1, "-DGBX_GEO_SCAN_BACKGROUND")
+    if check_ball:
+        cmd.insert(1, "-DGBX_CHECK_SAFE_BALL")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle port build failed:\n" + res.stderr[-4000:])

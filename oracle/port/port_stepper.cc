@@ -499,6 +499,10 @@ int run(int argc, char** argv)
     auto const& edep = step.edep();
     for (std::size_t i = 0; i < edep.size(); ++i)
         std::printf("edep %s %.17g\n", hp.detector_labels[i].c_str(), edep[i]);
+    #ifdef GBX_CHECK_SAFE_BALL
+    std::fprintf(stderr, "safe_ball uses %llu mismatches %llu\n",
+                 safe_ball_uses, safe_ball_mismatches);
+#endif
     return 0;
 }
 

@@ -41,3 +41,38 @@ def test_ordered_walks_match_full_solve(ports, geometry, walks):
     assert len(lines_o) == len(lines_s)
     bad = [(a, b) for a, b in zip(lines_o, lines_s) if a != b]
     assert not bad, bad[:5]
+
+
+FIELD_CASES = ["calo_msc_field_e5000_n2", "calo_msc_field_ep2000_n2", "cms_mix_e10000_n4",
+               "cms_mix_logu_n6", "cms_rzmap_mix_e2000_n4", "cms_fieldopt_mix_e5000_n4",
+               "tracker_mix_e3000_n4"]
+
+
+@pytest.mark.parametrize("name", FIELD_CASES)
+def test_safe_ball_never_contradicts_full_query(name):
+    """The field propagation answers a chord query without the geometry when
+    the chord lies in a ball free of surfaces (``inside_safe_ball``,
+    ``gbx/Field.hh``). The check build of the CPU restatement runs every
+    query in full along the golden transports and counts the queries the
+    ball answered and any whose full answer differs: there must be none, and
+    the ball must have been used."""
+    import os
+    import tempfile
+
+    from celeritas_gb300.primaries import write_primaries_text
+    from conftest import case_options, case_primaries, case_problem, load_golden
+
+    exe = oracle.build_port(check_ball=True)
+    case = load_golden(name, "pinned")["case"]
+    physics, geometry = case_problem(case)
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "p.txt")
+        write_primaries_text(ptxt, case_primaries(case))
+        res = subprocess.run([exe, "run", physics, geometry, ptxt,
+                              str(case["num_track_slots"]), str(case["seed"]),
+                              *case_options(case)],
+                             capture_output=True, text=True, check=True)
+    line = [ln for ln in res.stderr.splitlines() if ln.startswith("safe_ball")][-1]
+    uses, mismatches = int(line.split()[2]), int(line.split()[4])
+    assert mismatches == 0, line
+    assert uses > 0, line
