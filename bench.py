@@ -1063,12 +1063,29 @@ def run_batching(args, wl):
             # queue takes the primaries waiting for slots and the
             # secondaries of the showers under way), stepped to completion
             allp = make_uneven_events(wl, wl["events"], seed=500 + rank)
-            st = make_stepper(best["slots"])
+            # All primaries wait in the initializer queue at first, beside the
+            # secondaries of the showers under way: a queue of 2^26 (about
+            # 6 GB of initializers) instead of the default 4 x slots
+            params_all = gb.Params(
+                gb.physics_file(wl["physics"]), wl["geometry"], field_tesla=wl["field"],
+                msc=wl["msc"], track_order=args.track_order, precision="mixed",
+                rng_per_track=True, reentrant_looping=wl.get("reentrant_looping", False),
+                initializer_capacity=max(1 << 26, 16 * len(allp)))
+            st = gb.Stepper(params_all, best["slots"], seed=wl["seed"] + rank)
             st.set_tuning(**{k: v for k, v in best.items() if k != "slots"})
             autotune.transport(st, calib)  # warm-up: graph capture
-            secs, steps = autotune.transport(st, allp, max_steps=200000)
+            st.synchronize()
+            t_all = time.perf_counter()
+            res = [st.step(allp)] + st.run(max_steps=200000, batch=64)
+            st.synchronize()
+            secs = time.perf_counter() - t_all
+            if res[-1].alive or res[-1].queued:
+                raise RuntimeError("the 4096-event transport did not finish")
+            steps = sum(r.active for r in res)
             all_events = {"events": int(wl["events"]), "primaries": int(len(allp)),
                           "energy_tev": float(allp["energy"].sum() / 1e6),
+                          "peak_queued_initializers": int(max(r.queued for r in res)),
+                          "step_iterations": len(res),
                           "seconds": secs, "track_steps": int(steps),
                           "track_steps_per_s": steps / secs,
                           "events_per_s": wl["events"] / secs,
