@@ -329,9 +329,7 @@ def measure(args, wl, precision, stream_cls, dist, rank, local_rank, clocks,
         processed = {lab: 0 for lab in labels}
         res = [stepper.step(batches[0])]
         while True:
-            offs = stepper.get_state("action_offsets", np.uint32).astype(np.int64)
-            half = len(offs) // 2
-            along, post = np.diff(offs[:half]), np.diff(offs[half:])
+            along, post = stepper.sorted_action_sizes()
             active = res[-1].active
             for aid, lab in enumerate(labels):
                 if lab.startswith("along-step"):
@@ -756,7 +754,8 @@ def run_gb300(args, wl):
     act = head["per_action"][dom]
     peak, peak_kind = load_peaks()
     achieved = act["bytes_per_launch"] / (act["ms_per_launch"] / 1e3) / 1e9
-    traffic = read_traffic(dom, act["processed_per_launch"], head["precision"])
+    traffic = read_traffic(dom, act["processed_per_launch"], head["precision"],
+                           args.workload)
     line = {
         "metric": "track-steps/s",
         "value": head["value"],
@@ -1139,23 +1138,29 @@ def run_batching(args, wl):
         dist.destroy_process_group()
 
 
-def read_traffic(kernel_label, processed, precision):
+def read_traffic(kernel_label, processed, precision, workload=None):
     """DRAM bytes per launch of a kernel, from the committed ncu capture.
 
     The capture holds one launch's DRAM bytes and the track slots that
     launch processed; the figure is scaled to this run's mean processed
     slots per launch (an action's traffic grows with the tracks it
-    processes). Only captures of the same precision are used.
+    processes). Only captures of the same precision are used, of the same
+    workload where one exists (fifth column).
     """
     path = os.path.join(REPO, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
+    fallback = None
     with open(path) as f:
         for line in f:
             tok = line.split()
             if len(tok) >= 4 and tok[0] == kernel_label and tok[1] == precision:
-                return float(tok[2]) * processed / float(tok[3])
-    return None
+                value = float(tok[2]) * processed / float(tok[3])
+                if len(tok) >= 5 and tok[4] == workload:
+                    return value
+                if fallback is None and len(tok) == 4:
+                    fallback = value
+    return fallback
 
 
 def main():

@@ -174,6 +174,8 @@ _PROTOTYPES = [
      [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]),
     ("gbx_stepper_event_live", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint), ctypes.c_size_t]),
+    ("gbx_stepper_sorted_action_sizes", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint), ctypes.c_size_t]),
     ("gbx_stepper_event_energy_deposition", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int]),
     ("gbx_stepper_event_detector_energy_deposition", ctypes.c_int,
@@ -432,7 +434,7 @@ class Stepper:
 
     def set_tuning(self, **settings):
         """Launch tuning: along_block_size, along_persistent, sort_threshold,
-        sort, partition_slots."""
+        sort, sort_material, partition_slots."""
         for name, value in settings.items():
             _check(self._lib, self._lib.gbx_stepper_set_tuning(
                 self._handle, name.encode(), int(value)))
@@ -520,6 +522,18 @@ class Stepper:
         _check(self._lib, self._lib.gbx_stepper_get_tuning(
             self._handle, name.encode(), ctypes.byref(v)))
         return v.value
+
+    def sorted_action_sizes(self) -> tuple[np.ndarray, np.ndarray]:
+        """Tracks per action (by action ID) in the last along-step and
+        step-limit action sorts."""
+        n = len(self.params.action_labels())
+        out = []
+        for key in (0, 1):
+            v = np.zeros(n, dtype=np.uint32)
+            _check(self._lib, self._lib.gbx_stepper_sorted_action_sizes(
+                self._handle, key, v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), n))
+            out.append(v.astype(np.int64))
+        return out[0], out[1]
 
     def event_live(self, num_events: int) -> np.ndarray:
         """Live tracks (slots + queued initializers) of events [0, n)."""

@@ -433,6 +433,21 @@ int gbx_stepper_insert_primaries(gbx_stepper* stepper,
     });
 }
 
+int gbx_stepper_sorted_action_sizes(gbx_stepper* stepper,
+                                    int key,
+                                    unsigned int* sizes,
+                                    size_t num_actions)
+{
+    return guarded([&] {
+        if (!sizes || (key != 0 && key != 1))
+            throw std::runtime_error("invalid argument");
+        auto v = stepper->stepper->state().sorted_action_sizes(key);
+        if (num_actions != v.size())
+            throw std::runtime_error("expected one size per action");
+        std::copy(v.begin(), v.end(), sizes);
+    });
+}
+
 int gbx_stepper_event_live(gbx_stepper* stepper,
                            unsigned int* counts,
                            size_t num_events)

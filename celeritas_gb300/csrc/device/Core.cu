@@ -469,7 +469,9 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_svac = arr(1);
     std::size_t o_scnt = arr(4);
     // Action sort: thread -> slot indirection, bin offsets, block counts
-    size_type const num_bins = params.host().scalars.num_actions + 1;
+    size_type const num_actions = params.host().scalars.num_actions;
+    size_type const num_materials = max_of<size_type>(1, params.host().scalars.num_materials);
+    size_type const num_bins = num_actions + num_materials + 1;
     size_type const sort_blocks = (n + sort_block_size - 1) / sort_block_size;
     std::size_t o_tslots = arr(4);
     std::size_t o_aoff = L.reserve(4 * 2 * std::size_t(num_bins + 1));
@@ -600,6 +602,9 @@ CoreState::CoreState(CoreParams const& params,
     ctx_.sort.block_hist = static_cast<size_type*>(at(o_shist));
     ctx_.sort.num_bins = num_bins;
     ctx_.sort.num_blocks = sort_blocks;
+    ctx_.sort.num_actions = num_actions;
+    ctx_.sort.num_materials = num_materials;
+    ctx_.sort.material_action = invalid_id;
     ctx_.work_counter = static_cast<size_type*>(at(o_work));
     // Persistent charged along-step: on by default in the mixed-precision
     // build, where it outruns the one-thread-per-track kernel; in FP64 the
@@ -865,6 +870,10 @@ void CoreState::set_tuning(std::string const& name, long long value)
     {
         ctx_.sort_enabled = value != 0;
     }
+    else if (name == "sort_material")
+    {
+        ctx_.sort.material_action = value ? ctx_.params.action_along_step : invalid_id;
+    }
     else if (name == "partition_slots")
     {
         if (value && !ctx_.params.rng_per_track)
@@ -890,6 +899,8 @@ long long CoreState::tuning(std::string const& name) const
         return ctx_.sort_enabled;
     if (name == "partition_slots")
         return ctx_.partition_slots;
+    if (name == "sort_material")
+        return ctx_.sort.material_action != invalid_id;
     throw std::runtime_error("unknown tuning parameter '" + name + "'");
 }
 
@@ -900,6 +911,29 @@ void CoreState::reseed(unsigned long long event_id)
     // TrackInitParams::reset_track_ids: every per-event counter restarts
     GBX_CUDA(cudaMemsetAsync(
         ref_.track_counters, 0, sizeof(size_type) * ref_.max_events, stream_));
+}
+
+std::vector<size_type> CoreState::sorted_action_sizes(int key) const
+{
+    SortScratch const& srt = ctx_.sort;
+    std::size_t const table = std::size_t(srt.num_bins) + 1;
+    std::vector<size_type> off(table);
+    GBX_CUDA(cudaMemcpyAsync(off.data(),
+                             ref_.action_offsets + (key ? table : 0),
+                             sizeof(size_type) * table,
+                             cudaMemcpyDeviceToHost,
+                             stream_));
+    GBX_CUDA(cudaStreamSynchronize(stream_));
+    std::vector<size_type> out(srt.num_actions);
+    for (size_type a = 0; a < srt.num_actions; ++a)
+    {
+        size_type first = a;
+        size_type end = a + 1;
+        if (key == 0)
+            along_bins(srt, a, &first, &end);
+        out[a] = off[end] - off[first];
+    }
+    return out;
 }
 
 std::vector<size_type> CoreState::event_live(size_type n) const

@@ -557,13 +557,25 @@ __global__ void kill_active_kernel(ParamsData p, StateData s)
 // slots of one action stay in increasing order.
 //---------------------------------------------------------------------------//
 __device__ __forceinline__ size_type sort_key(StateData const& s,
+                                              SortScratch const& srt,
                                               SortKey key,
-                                              size_type slot,
-                                              size_type invalid_bin)
+                                              size_type slot)
 {
+    size_type const invalid_bin = srt.num_bins - 1;
     size_type a = (key == SortKey::along_step) ? s.along_step_action[slot]
                                                : s.post_step_action[slot];
-    return a < invalid_bin ? a : invalid_bin;
+    if (!(a < srt.num_actions))
+        return invalid_bin;
+    if (key == SortKey::along_step && srt.material_action != invalid_id)
+    {
+        // Tracks of the material-sorted action by material; later actions
+        // after its bins
+        if (a == srt.material_action)
+            a += min_of(s.material[slot], srt.num_materials - 1);
+        else if (a > srt.material_action)
+            a += srt.num_materials - 1;
+    }
+    return a;
 }
 
 __global__ __launch_bounds__(sort_block_size) void sort_count_kernel(
@@ -575,8 +587,7 @@ __global__ __launch_bounds__(sort_block_size) void sort_count_kernel(
     __syncthreads();
     size_type const slot = blockIdx.x * sort_block_size + threadIdx.x;
     bool const valid = slot < s.size;
-    size_type const k = valid ? sort_key(s, key, slot, srt.num_bins - 1)
-                              : srt.num_bins;
+    size_type const k = valid ? sort_key(s, srt, key, slot) : srt.num_bins;
     unsigned int const peers = __match_any_sync(0xffffffffu, k);
     unsigned int const lane = threadIdx.x & 31u;
     if (valid && (peers & ((1u << lane) - 1u)) == 0)
@@ -649,7 +660,7 @@ __global__ __launch_bounds__(sort_block_size) void sort_scatter_kernel(
     __syncthreads();
     size_type const slot = blockIdx.x * sort_block_size + threadIdx.x;
     bool const valid = slot < s.size;
-    size_type const k = valid ? sort_key(s, key, slot, nb - 1) : nb;
+    size_type const k = valid ? sort_key(s, srt, key, slot) : nb;
     unsigned int const peers = __match_any_sync(0xffffffffu, k);
     unsigned int const lane = threadIdx.x & 31u;
     unsigned int const warp = threadIdx.x >> 5;
@@ -746,11 +757,12 @@ __global__ GBX_ALONG_BOUNDS(Threads, 1) void along_charged_persistent_kernel(
     ParamsData p,
     StateData s,
     size_type const* offsets,
-    size_type bin,
+    size_type first_bin,
+    size_type end_bin,
     size_type* work_counter)
 {
-    size_type const first = offsets ? offsets[bin] : 0;
-    size_type const count = offsets ? offsets[bin + 1] - first : s.size;
+    size_type const first = offsets ? offsets[first_bin] : 0;
+    size_type const count = offsets ? offsets[end_bin] - first : s.size;
     unsigned int const lane = threadIdx.x & 31u;
     FieldOptions const& opt = p.field_options;
     FieldPropagation fp(opt, UniformFieldEquation{});
@@ -912,6 +924,9 @@ void launch_along_step(LaunchContext const& ctx,
     unsigned int const anb = (ctx.state.size + abs - 1) / abs;
     size_type const* offsets
         = key_offsets(ctx, SortKey::along_step, sorts_along_step(p.track_order));
+    size_type cfirst, cend, nfirst, nend;
+    along_bins(ctx.sort, p.action_along_step, &cfirst, &cend);
+    along_bins(ctx.sort, p.action_along_step_neutral, &nfirst, &nend);
     if (action == invalid_id || action == p.action_along_step)
     {
         bool const large = abs > static_cast<unsigned int>(block_size);
@@ -921,32 +936,27 @@ void launch_along_step(LaunchContext const& ctx,
             if (large)
                 along_charged_persistent_kernel<along_block_large>
                     <<<ctx.persistent_blocks, abs, 0, stream>>>(
-                        p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
+                        p, ctx.state, offsets, cfirst, cend, ctx.work_counter);
             else
                 along_charged_persistent_kernel<block_size>
                     <<<ctx.persistent_blocks, abs, 0, stream>>>(
-                        p, ctx.state, offsets, p.action_along_step, ctx.work_counter);
+                        p, ctx.state, offsets, cfirst, cend, ctx.work_counter);
         }
         else if (large)
         {
             along_step_sorted_kernel<AlongKind::charged, along_block_large>
-                <<<anb, abs, 0, stream>>>(
-                    p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
+                <<<anb, abs, 0, stream>>>(p, ctx.state, offsets, cfirst, cend);
         }
         else
         {
             along_step_sorted_kernel<AlongKind::charged><<<anb, abs, 0, stream>>>(
-                p, ctx.state, offsets, p.action_along_step, p.action_along_step + 1);
+                p, ctx.state, offsets, cfirst, cend);
         }
     }
     if (action == invalid_id || action == p.action_along_step_neutral)
     {
         along_step_sorted_kernel<AlongKind::neutral><<<nb, block_size, 0, stream>>>(
-            p,
-            ctx.state,
-            offsets,
-            p.action_along_step_neutral,
-            p.action_along_step_neutral + 1);
+            p, ctx.state, offsets, nfirst, nend);
     }
 }
 

@@ -31,9 +31,32 @@ struct ScanScratch
 struct SortScratch
 {
     size_type* block_hist;  //!< [num_bins * num_blocks]
-    size_type num_bins;  //!< num_actions + 1 (last: invalid action)
+    //! num_actions + num_materials + 1 (last: invalid action)
+    size_type num_bins;
     size_type num_blocks;
+    size_type num_actions;
+    size_type num_materials;
+    //! Along-step sort by material within one action: that action's tracks
+    //! take bins [action, action + num_materials) by their material, and the
+    //! bins of later actions shift by num_materials - 1 (invalid_id: off)
+    size_type material_action;
 };
+
+//! Bins [first, end) of an action in the along-step sort
+inline void along_bins(SortScratch const& srt, size_type action, size_type* first, size_type* end)
+{
+    size_type b = action;
+    size_type n = 1;
+    if (srt.material_action != invalid_id)
+    {
+        if (action == srt.material_action)
+            n = srt.num_materials;
+        else if (action > srt.material_action)
+            b += srt.num_materials - 1;
+    }
+    *first = b;
+    *end = b + n;
+}
 
 //! Which action a sort orders tracks by
 enum class SortKey

@@ -187,6 +187,9 @@ class CoreState
 
     //! Live tracks (slots and queued initializers) per event [0, n)
     std::vector<size_type> event_live(size_type n) const;
+    //! Tracks in each action's range of the last action sort by 'key' (0:
+    //! along-step action, 1: step-limit action), indexed by action ID
+    std::vector<size_type> sorted_action_sizes(int key) const;
     //! Energy deposited in detectors per event [0, n); optionally cleared
     std::vector<double> event_energy_deposition(size_type n, bool clear);
     //! Energy deposited in each detector per event, events [first, first +

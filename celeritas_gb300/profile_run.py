@@ -3,7 +3,7 @@
     python -m celeritas_gb300.profile_run --workload c2 [--primaries N]
         [--max-iterations K] [--steps-log FILE] [--graph]
         [--precision double|mixed] [--track-order N] [--slots S]
-        [--tuning name=value,...] [--initializer-capacity N]
+        [--tuning name=value,...] [--initializer-capacity N] [--rng-per-track]
 
 Inserts the workload's primaries, then steps (eagerly by default, so that
 every kernel is its own launch) until the state empties or K iterations have
@@ -38,6 +38,8 @@ def main(argv=None):
                     help="track slots (default: the workload's)")
     ap.add_argument("--initializer-capacity", type=int, default=0,
                     help="pending-track queue per stepper (default: 16 per slot)")
+    ap.add_argument("--rng-per-track", action="store_true",
+                    help="per-track random streams (needed by partition_slots)")
     ap.add_argument("--tuning", default="",
                     help="launch settings, e.g. along_block_size=64,along_persistent=0")
     args = ap.parse_args(argv)
@@ -48,7 +50,8 @@ def main(argv=None):
                     field_tesla=wl["field"], msc=wl["msc"],
                     track_order=args.track_order, precision=args.precision,
                     reentrant_looping=wl.get("reentrant_looping", False),
-                    initializer_capacity=args.initializer_capacity)
+                    initializer_capacity=args.initializer_capacity,
+                    rng_per_track=args.rng_per_track)
     stepper = Stepper(params, args.slots or wl["slots"], seed=wl["seed"],
                       use_graph=args.graph)
     if args.tuning:
@@ -62,9 +65,7 @@ def main(argv=None):
         # Slots per action in this step's sorted ranges (along-step sort,
         # step-limit sort); empty without an action sort
         if args.track_order:
-            offs = stepper.get_state("action_offsets", np.uint32).astype(np.int64)
-            half = len(offs) // 2
-            along, post = np.diff(offs[:half]), np.diff(offs[half:])
+            along, post = stepper.sorted_action_sizes()
             counts.append({lab: int(along[i] if lab.startswith("along-step") else post[i])
                            for i, lab in enumerate(labels) if along[i] or post[i]})
 

@@ -311,6 +311,18 @@ int gbx_stepper_state_info(gbx_stepper* stepper,
                            size_t* elem_bytes,
                            size_t* count);
 
+/* Tracks in each action's range of the stepper's last action sort, indexed
+ * by action ID: key 0 the sort by along-step action (before the along-step
+ * kernels), 1 the sort by step-limit action (before the interactions);
+ * num_actions must equal gbx_params_num_actions. Synchronizes the stepper's
+ * stream. A profiler's view of what SortTracksAction partitioned
+ * (src/celeritas/track/SortTracksAction.cc); no counterpart in the
+ * reference's API. */
+int gbx_stepper_sorted_action_sizes(gbx_stepper* stepper,
+                                    int key,
+                                    unsigned int* sizes,
+                                    size_t num_actions);
+
 /* Live tracks per event, for events [0, num_events): occupied track slots
  * plus queued track initializers; synchronizes the stepper's stream. A
  * serving loop reads it to detect completed events. No counterpart in the
@@ -426,6 +438,9 @@ int gbx_stepper_read_step_output(gbx_stepper* stepper,
  *                       tracks (0: always)
  *   "sort"              0: action sorts off (each action kernel visits
  *                       every slot), 1: on; reset by the sort threshold
+ *   "sort_material"     1: the along-step sort orders the charged tracks by
+ *                       material too, so that warps of the charged kernel
+ *                       hold tracks of one material
  *   "partition_slots"   1: new charged tracks take the lowest vacant slots
  *                       and neutral ones the highest, so the sorted ranges
  *                       of the along-step kernels cover mostly contiguous

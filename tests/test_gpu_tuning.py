@@ -3,8 +3,9 @@
 With per-track random streams the launch configuration of a stepper changes
 its speed, not its results: every event's energy deposition must be the same
 under each tuning (threads per block of the charged along-step, persistent
-charged kernel, action sorts on or off, charged and neutral tracks in
-partitioned slot ranges) and each track order to 1e-12
+charged kernel, action sorts on or off, charged tracks sorted by material
+too, charged and neutral tracks in partitioned slot ranges) and each track
+order to 1e-12
 relative (the device tally sums with atomics, so only the summation order
 differs). This holds in the mixed-precision build too, whose compiler may
 contract multiply-adds, because sorted and unsorted orders run the same
@@ -60,6 +61,8 @@ TUNINGS = [
     {"sort": 0},
     {"sort_threshold": 1 << 30},
     {"along_persistent": 1, "along_block_size": 128},
+    {"sort_material": 1},
+    {"sort_material": 1, "along_persistent": 1, "along_block_size": 128},
     {"partition_slots": 1},
     {"partition_slots": 1, "along_persistent": 0, "sort_threshold": 1 << 12},
 ]
@@ -142,3 +145,27 @@ def test_large_blocks_give_the_same_results(gb, precision):
             if base is None:
                 base = edep
             np.testing.assert_allclose(edep, base, rtol=rtol)
+
+
+def test_material_sort_keeps_action_ranges(gb):
+    """With the charged tracks also sorted by material, each action's range
+    holds the same tracks: the per-action sizes of both sorts agree with the
+    plain action sort step by step (per-track streams: the same histories)."""
+    prim = events()
+    sizes = []
+    for material in (0, 1):
+        st = gb.Stepper(cms_params(gb, "mixed"), SLOTS, seed=5, use_graph=False)
+        st.set_tuning(sort_material=material)
+        assert st.get_tuning("sort_material") == material
+        res = [st.step(prim)]
+        steps = []
+        for _ in range(12):
+            along, post = st.sorted_action_sizes()
+            steps.append((along.copy(), post.copy(), res[-1].active))
+            res.append(st.step())
+        sizes.append(steps)
+    for (a0, p0, n0), (a1, p1, n1) in zip(*sizes):
+        assert n0 == n1
+        np.testing.assert_array_equal(a0, a1)
+        np.testing.assert_array_equal(p0, p1)
+    assert sum(a.sum() for a, _, _ in sizes[0]) > 0
