@@ -14,6 +14,7 @@ over
   pairs); a setting the stepper rejects is recorded and skipped,
 * the sort threshold: action sorts only in steps that start with at least
   this many live tracks (0: always),
+* the along-step sort by material within the charged tracks (off, on),
 
 keeping the best value of each parameter before tuning the next. Every
 candidate first transports the calibration events once untimed (a new
@@ -61,7 +62,8 @@ def autotune(make_stepper: Callable[[int], object], primaries: np.ndarray,
              slot_counts: Sequence[int] = SLOT_COUNTS,
              block_sizes: Sequence[int] = BLOCK_SIZES,
              thresholds: Sequence[int] = THRESHOLDS,
-             start: dict | None = None) -> tuple[dict, list[Trial]]:
+             start: dict | None = None,
+             materials: Sequence[int] = (0, 1)) -> tuple[dict, list[Trial]]:
     """Tune on 'primaries'; return the best configuration and every trial."""
     trials: list[Trial] = []
     best = dict(start or {})
@@ -97,6 +99,7 @@ def autotune(make_stepper: Callable[[int], object], primaries: np.ndarray,
     stages = (
         [{"along_block_size": b, "along_persistent": f} for f in (1, 0) for b in block_sizes],
         [{"sort_threshold": v} for v in thresholds],
+        [{"sort_material": v} for v in materials],
     )
     for candidates in stages:
         winner = None

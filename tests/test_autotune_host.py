@@ -21,7 +21,8 @@ class FakeStepper:
     def __init__(self, slots, cost):
         self.slots = slots
         self.cost = cost
-        self.cfg = {"along_block_size": 256, "along_persistent": 1, "sort_threshold": 0}
+        self.cfg = {"along_block_size": 256, "along_persistent": 1, "sort_threshold": 0,
+                    "sort_material": 0}
         self.calls = []
 
     def set_tuning(self, **settings):
@@ -63,7 +64,7 @@ def test_block_size_and_kernel_form_tuned_together(monkeypatch):
 
     best, trials = autotune.autotune(lambda n: FakeStepper(n, cost), np.zeros(4))
     assert best == {"slots": 1 << 21, "along_block_size": 128, "along_persistent": 0,
-                    "sort_threshold": 1 << 17}
+                    "sort_threshold": 1 << 17, "sort_material": 0}
     rejected = [t for t in trials if t.seconds is None]
     assert [t.config["along_block_size"] for t in rejected] == [512, 512]
     # Every measured candidate was timed after an untimed warm-up transport
@@ -83,4 +84,19 @@ def test_start_configuration_kept_when_nothing_is_faster(monkeypatch):
                                 slot_counts=(1 << 20,), block_sizes=(256, 512),
                                 thresholds=(0, 1 << 14))
     assert best == {"slots": 1 << 20, "along_block_size": 256, "along_persistent": 1,
-                    "sort_threshold": 0}
+                    "sort_threshold": 0, "sort_material": 0}
+
+
+def test_material_sort_taken_when_faster(monkeypatch):
+    _patch_clock(monkeypatch)
+
+    def cost(slots, c):
+        if c["along_block_size"] == 512:
+            return None
+        return 1.0 - 0.05 * c["sort_material"]
+
+    best, trials = autotune.autotune(lambda n: FakeStepper(n, cost), np.zeros(1),
+                                     slot_counts=(1 << 20,), block_sizes=(256,),
+                                     thresholds=(0,))
+    assert best["sort_material"] == 1
+    assert [t.config.get("sort_material") for t in trials][-2:] == [0, 1]
