@@ -379,6 +379,10 @@ class GeoTrackView
                 }
             }
             inside = inside && (vol.inside_sense[f] > 0 ? s : !s);
+            // Without an on-surface report the remaining faces cannot
+            // change the answer
+            if (!inside && !on_surface)
+                return false;
         }
         return inside;
     }
@@ -430,10 +434,12 @@ GBX_FUNCTION size_type GeoTrackView::find_volume_at(Real3 const& pos,
                                                     bool forced_outside) const
 {
     // Exterior first: outside the world box
+    // Faces are evaluated to the last only when the caller wants to know
+    // whether the point lies on one
     if (exclude != p_.exterior)
     {
         bool on = false;
-        if (this->exterior_inside(pos, forced, forced_outside, &on))
+        if (this->exterior_inside(pos, forced, forced_outside, on_surface ? &on : nullptr))
         {
             if (on_surface)
                 *on_surface = on;
@@ -447,7 +453,11 @@ GBX_FUNCTION size_type GeoTrackView::find_volume_at(Real3 const& pos,
             if (cand == exclude)
                 continue;
             bool on = false;
-            if (this->volume_logic(p_.volumes[cand], pos, forced, forced_outside, &on))
+            if (this->volume_logic(p_.volumes[cand],
+                                   pos,
+                                   forced,
+                                   forced_outside,
+                                   on_surface ? &on : nullptr))
             {
                 if (on_surface)
                     *on_surface = on;
@@ -480,7 +490,8 @@ GBX_FUNCTION size_type GeoTrackView::find_volume_at(Real3 const& pos,
         if (cand == exclude)
             continue;
         bool on = false;
-        if (this->volume_logic(p_.volumes[cand], pos, forced, forced_outside, &on))
+        if (this->volume_logic(
+                p_.volumes[cand], pos, forced, forced_outside, on_surface ? &on : nullptr))
         {
             if (on_surface)
                 *on_surface = on;
@@ -682,6 +693,84 @@ GBX_FUNCTION void GeoTrackView::background_crossing(Real3 const& pos,
             this->consider_crossing(cur_surf, dd[k], pos, dir, bump, max_step, hit);
     }
 
+    // Z cylinders first: in a barrel of shells they usually hold the nearest
+    // crossing, which then bounds the plane walks below, so that fewer
+    // plane candidates need the acceptance test (a plane shared by many
+    // shells locates the bumped point among all volumes). The per-surface
+    // solve finds no cylinder crossing when traveling along the axis.
+    size_type const cbeg = p_.sorted_offset[surf_czc];
+    size_type const cend = p_.sorted_offset[surf_czc + 1];
+    constexpr double sqrt_quadratic = 1e-5;
+    if (cbeg < cend && !(1 - ipow<2>(dir.z) < ipow<2>(sqrt_quadratic)))
+    {
+        float const xf = static_cast<float>(pos.x);
+        float const yf = static_cast<float>(pos.y);
+        float const rf = std::sqrt(xf * xf + yf * yf);
+        auto radial_margin = [](float radius, float limit) {
+            return 1e-5f * (radius + limit) + 1e-6f;
+        };
+
+        // Near roots (entering a smaller cylinder while moving inward), walked
+        // down from the track's radius r: they grow as the radius falls.
+        // Cylinders with keys above FP32(r) (1 + 1e-6) are outside r and have no
+        // near root.
+        for (size_type i = key_upper_bound(key, cbeg, cend, rf + (1e-6f * rf + 1e-20f));
+             i-- > cbeg;)
+        {
+            size_type const surf = sorted[i];
+            if (surf == cur_surf)
+                continue;
+            double const limit = crossing_limit(*hit);
+            float const limit_f = static_cast<float>(limit);
+            if (rf - key[i] - radial_margin(key[i], limit_f) > limit_f)
+                break;
+            double dd[2];
+            this->intersect(surf, pos, dir, false, dd);
+            if (dd[0] < INFINITY)
+            {
+                if (dd[0] > limit)
+                    break;
+                for (int k = 0; k < 2; ++k)
+                    this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
+            }
+            else if (!(dd[1] < INFINITY))
+            {
+                // Not reached, or moving outward: nor is any smaller cylinder
+                break;
+            }
+            // Else only a far root (a cylinder at r, or just below it with a
+            // near root that rounds to zero): the upward walk takes it
+        }
+
+        // Far roots, walked up from just below r: they grow with the radius.
+        // Below r - 1e-4 (r + 1) a reached cylinder has a near root of at least
+        // 5e-5 times its far one, so the downward walk above has taken
+        // both of its roots, or stopped where both lie beyond the limit.
+        float const delta = 1e-4f * (rf + 1);
+        for (size_type i = key_lower_bound(key, cbeg, cend, rf - delta); i < cend; ++i)
+        {
+            size_type const surf = sorted[i];
+            if (surf == cur_surf)
+                continue;
+            double const limit = crossing_limit(*hit);
+            float const limit_f = static_cast<float>(limit);
+            if (key[i] - rf - radial_margin(key[i], limit_f) > limit_f)
+                break;
+            double dd[2];
+            this->intersect(surf, pos, dir, false, dd);
+            double const far = (dd[1] < INFINITY) ? dd[1] : dd[0];
+            if (!(far < INFINITY))
+            {
+                // Behind the track or not reached: a larger cylinder may be
+                continue;
+            }
+            if (far > limit)
+                break;
+            for (int k = 0; k < 2; ++k)
+                this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
+        }
+    }
+
     // Planes of each axis, in the order the ray meets them. A plane's
     // distance |v - x| / |n| is at least |v - x| (1 - 2^-40) for a unit
     // direction rounded to FP64, which ends the walk without a division.
@@ -726,80 +815,6 @@ GBX_FUNCTION void GeoTrackView::background_crossing(Real3 const& pos,
                     this->consider_crossing(surf, d, pos, dir, bump, max_step, hit);
             }
         }
-    }
-
-    // Z cylinders. The per-surface solve finds none when traveling along the
-    // axis.
-    size_type const cbeg = p_.sorted_offset[surf_czc];
-    size_type const cend = p_.sorted_offset[surf_czc + 1];
-    constexpr double sqrt_quadratic = 1e-5;
-    if (cbeg == cend || 1 - ipow<2>(dir.z) < ipow<2>(sqrt_quadratic))
-        return;
-    float const xf = static_cast<float>(pos.x);
-    float const yf = static_cast<float>(pos.y);
-    float const rf = std::sqrt(xf * xf + yf * yf);
-    auto radial_margin = [](float radius, float limit) {
-        return 1e-5f * (radius + limit) + 1e-6f;
-    };
-
-    // Near roots (entering a smaller cylinder while moving inward), walked
-    // down from the track's radius r: they grow as the radius falls.
-    // Cylinders with keys above FP32(r) (1 + 1e-6) are outside r and have no
-    // near root.
-    for (size_type i = key_upper_bound(key, cbeg, cend, rf + (1e-6f * rf + 1e-20f));
-         i-- > cbeg;)
-    {
-        size_type const surf = sorted[i];
-        if (surf == cur_surf)
-            continue;
-        double const limit = crossing_limit(*hit);
-        float const limit_f = static_cast<float>(limit);
-        if (rf - key[i] - radial_margin(key[i], limit_f) > limit_f)
-            break;
-        double dd[2];
-        this->intersect(surf, pos, dir, false, dd);
-        if (dd[0] < INFINITY)
-        {
-            if (dd[0] > limit)
-                break;
-            for (int k = 0; k < 2; ++k)
-                this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
-        }
-        else if (!(dd[1] < INFINITY))
-        {
-            // Not reached, or moving outward: nor is any smaller cylinder
-            break;
-        }
-        // Else only a far root (a cylinder at r, or just below it with a
-        // near root that rounds to zero): the upward walk takes it
-    }
-
-    // Far roots, walked up from just below r: they grow with the radius.
-    // Below r - 1e-4 (r + 1) a reached cylinder has a near root of at least
-    // 5e-5 times its far one, so the downward walk above has taken
-    // both of its roots, or stopped where both lie beyond the limit.
-    float const delta = 1e-4f * (rf + 1);
-    for (size_type i = key_lower_bound(key, cbeg, cend, rf - delta); i < cend; ++i)
-    {
-        size_type const surf = sorted[i];
-        if (surf == cur_surf)
-            continue;
-        double const limit = crossing_limit(*hit);
-        float const limit_f = static_cast<float>(limit);
-        if (key[i] - rf - radial_margin(key[i], limit_f) > limit_f)
-            break;
-        double dd[2];
-        this->intersect(surf, pos, dir, false, dd);
-        double const far = (dd[1] < INFINITY) ? dd[1] : dd[0];
-        if (!(far < INFINITY))
-        {
-            // Behind the track or not reached: a larger cylinder may be
-            continue;
-        }
-        if (far > limit)
-            break;
-        for (int k = 0; k < 2; ++k)
-            this->consider_crossing(surf, dd[k], pos, dir, bump, max_step, hit);
     }
 }
 
