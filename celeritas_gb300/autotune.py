@@ -14,7 +14,8 @@ over
   pairs); a setting the stepper rejects is recorded and skipped,
 * the sort threshold: action sorts only in steps that start with at least
   this many live tracks (0: always),
-* the along-step sort by material within the charged tracks (off, on),
+* the along-step sort by material within the charged tracks, and within the
+  neutral ones too (off, charged, both),
 
 keeping the best value of each parameter before tuning the next. Every
 candidate first transports the calibration events once untimed (a new
@@ -63,7 +64,7 @@ def autotune(make_stepper: Callable[[int], object], primaries: np.ndarray,
              block_sizes: Sequence[int] = BLOCK_SIZES,
              thresholds: Sequence[int] = THRESHOLDS,
              start: dict | None = None,
-             materials: Sequence[int] = (0, 1)) -> tuple[dict, list[Trial]]:
+             materials: Sequence[int] = (0, 1, 3)) -> tuple[dict, list[Trial]]:
     """Tune on 'primaries'; return the best configuration and every trial."""
     trials: list[Trial] = []
     best = dict(start or {})

@@ -471,7 +471,9 @@ CoreState::CoreState(CoreParams const& params,
     // Action sort: thread -> slot indirection, bin offsets, block counts
     size_type const num_actions = params.host().scalars.num_actions;
     size_type const num_materials = max_of<size_type>(1, params.host().scalars.num_materials);
-    size_type const num_bins = num_actions + num_materials + 1;
+    // Up to two along-step actions sorted by material take num_materials
+    // bins each
+    size_type const num_bins = num_actions + 2 * num_materials + 1;
     size_type const sort_blocks = (n + sort_block_size - 1) / sort_block_size;
     std::size_t o_tslots = arr(4);
     std::size_t o_aoff = L.reserve(4 * 2 * std::size_t(num_bins + 1));
@@ -604,7 +606,8 @@ CoreState::CoreState(CoreParams const& params,
     ctx_.sort.num_blocks = sort_blocks;
     ctx_.sort.num_actions = num_actions;
     ctx_.sort.num_materials = num_materials;
-    ctx_.sort.material_action = invalid_id;
+    ctx_.sort.material_actions[0] = invalid_id;
+    ctx_.sort.material_actions[1] = invalid_id;
     ctx_.work_counter = static_cast<size_type*>(at(o_work));
     // Persistent charged along-step: on by default in the mixed-precision
     // build, where it outruns the one-thread-per-track kernel; in FP64 the
@@ -872,7 +875,22 @@ void CoreState::set_tuning(std::string const& name, long long value)
     }
     else if (name == "sort_material")
     {
-        ctx_.sort.material_action = value ? ctx_.params.action_along_step : invalid_id;
+        // Bit 0: the charged along-step action, bit 1: the neutral one
+        if (value < 0 || value > 3)
+            throw std::runtime_error("sort_material must be 0-3");
+        size_type ids[2];
+        int n = 0;
+        size_type const charged = ctx_.params.action_along_step;
+        size_type const neutral = ctx_.params.action_along_step_neutral;
+        if ((value & 1) && charged != invalid_id)
+            ids[n++] = charged;
+        if ((value & 2) && neutral != invalid_id)
+            ids[n++] = neutral;
+        if (n == 2 && ids[1] < ids[0])
+            std::swap(ids[0], ids[1]);
+        ctx_.sort.material_actions[0] = n > 0 ? ids[0] : invalid_id;
+        ctx_.sort.material_actions[1] = n > 1 ? ids[1] : invalid_id;
+        sort_material_ = static_cast<int>(value);
     }
     else if (name == "partition_slots")
     {
@@ -900,7 +918,7 @@ long long CoreState::tuning(std::string const& name) const
     if (name == "partition_slots")
         return ctx_.partition_slots;
     if (name == "sort_material")
-        return ctx_.sort.material_action != invalid_id;
+        return sort_material_;
     throw std::runtime_error("unknown tuning parameter '" + name + "'");
 }
 

@@ -566,14 +566,14 @@ __device__ __forceinline__ size_type sort_key(StateData const& s,
                                                : s.post_step_action[slot];
     if (!(a < srt.num_actions))
         return invalid_bin;
-    if (key == SortKey::along_step && srt.material_action != invalid_id)
+    if (key == SortKey::along_step && srt.material_actions[0] != invalid_id)
     {
-        // Tracks of the material-sorted action by material; later actions
+        // Tracks of a material-sorted action by material; later actions
         // after its bins
-        if (a == srt.material_action)
-            a += min_of(s.material[slot], srt.num_materials - 1);
-        else if (a > srt.material_action)
-            a += srt.num_materials - 1;
+        size_type const mat = (a == srt.material_actions[0] || a == srt.material_actions[1])
+                                  ? min_of(s.material[slot], srt.num_materials - 1)
+                                  : 0;
+        a = along_bin(srt, a, mat);
     }
     return a;
 }

@@ -36,26 +36,39 @@ struct SortScratch
     size_type num_blocks;
     size_type num_actions;
     size_type num_materials;
-    //! Along-step sort by material within one action: that action's tracks
-    //! take bins [action, action + num_materials) by their material, and the
-    //! bins of later actions shift by num_materials - 1 (invalid_id: off)
-    size_type material_action;
+    //! Along-step sort by material within up to two actions (ascending IDs,
+    //! invalid_id where unused): such an action's tracks take num_materials
+    //! bins by their material, and the bins of later actions shift by
+    //! num_materials - 1
+    size_type material_actions[2];
 };
+
+//! Bin of a track of along-step action 'a' (a valid action ID) and material
+//! 'mat' in the along-step sort; mat = 0 gives the action's first bin
+__host__ __device__ inline size_type
+along_bin(SortScratch const& srt, size_type a, size_type mat)
+{
+    size_type shift = 0;
+    for (int i = 0; i < 2; ++i)
+    {
+        size_type const m = srt.material_actions[i];
+        if (m == invalid_id)
+            break;
+        if (a == m)
+            return a + shift + mat;
+        if (a > m)
+            shift += srt.num_materials - 1;
+    }
+    return a + shift;
+}
 
 //! Bins [first, end) of an action in the along-step sort
 inline void along_bins(SortScratch const& srt, size_type action, size_type* first, size_type* end)
 {
-    size_type b = action;
-    size_type n = 1;
-    if (srt.material_action != invalid_id)
-    {
-        if (action == srt.material_action)
-            n = srt.num_materials;
-        else if (action > srt.material_action)
-            b += srt.num_materials - 1;
-    }
-    *first = b;
-    *end = b + n;
+    bool const by_material = action == srt.material_actions[0]
+                             || action == srt.material_actions[1];
+    *first = along_bin(srt, action, 0);
+    *end = *first + (by_material ? srt.num_materials : 1);
 }
 
 //! Which action a sort orders tracks by

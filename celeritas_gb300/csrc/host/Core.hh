@@ -177,7 +177,9 @@ class CoreState
     //! Launch tuning: "along_block_size" (64, 128, 256, 512),
     //! "along_persistent" (0/1), "sort" (0/1: whether the action sorts run),
     //! "partition_slots" (0/1: charged tracks fill vacancies from the front
-    //! of the list, neutral ones from the back; per-track streams only)
+    //! of the list, neutral ones from the back; per-track streams only),
+    //! "sort_material" (bit 0: the along-step sort orders the charged
+    //! tracks by material too, bit 1: the neutral ones)
     void set_tuning(std::string const& name, long long value);
     long long tuning(std::string const& name) const;
 
@@ -219,6 +221,7 @@ class CoreState
   private:
     StateData ref_{};
     LaunchContext ctx_{};
+    int sort_material_ = 0;  //!< Tuning value of "sort_material"
     void* storage_{nullptr};
     void* hits_storage_{nullptr};
     TrackInitializer* pinned_primaries_{nullptr};

@@ -438,9 +438,10 @@ int gbx_stepper_read_step_output(gbx_stepper* stepper,
  *                       tracks (0: always)
  *   "sort"              0: action sorts off (each action kernel visits
  *                       every slot), 1: on; reset by the sort threshold
- *   "sort_material"     1: the along-step sort orders the charged tracks by
- *                       material too, so that warps of the charged kernel
- *                       hold tracks of one material
+ *   "sort_material"     bit 0: the along-step sort orders the charged
+ *                       tracks by material too, so that warps of the charged
+ *                       kernel hold tracks of one material; bit 1: the
+ *                       neutral tracks (0-3)
  *   "partition_slots"   1: new charged tracks take the lowest vacant slots
  *                       and neutral ones the highest, so the sorted ranges
  *                       of the along-step kernels cover mostly contiguous

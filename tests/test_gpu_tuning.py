@@ -62,6 +62,8 @@ TUNINGS = [
     {"sort_threshold": 1 << 30},
     {"along_persistent": 1, "along_block_size": 128},
     {"sort_material": 1},
+    {"sort_material": 3, "along_persistent": 0},
+    {"sort_material": 2},
     {"sort_material": 1, "along_persistent": 1, "along_block_size": 128},
     {"partition_slots": 1},
     {"partition_slots": 1, "along_persistent": 0, "sort_threshold": 1 << 12},
@@ -153,7 +155,7 @@ def test_material_sort_keeps_action_ranges(gb):
     plain action sort step by step (per-track streams: the same histories)."""
     prim = events()
     sizes = []
-    for material in (0, 1):
+    for material in (0, 1, 3):
         st = gb.Stepper(cms_params(gb, "mixed"), SLOTS, seed=5, use_graph=False)
         st.set_tuning(sort_material=material)
         assert st.get_tuning("sort_material") == material
@@ -164,8 +166,9 @@ def test_material_sort_keeps_action_ranges(gb):
             steps.append((along.copy(), post.copy(), res[-1].active))
             res.append(st.step())
         sizes.append(steps)
-    for (a0, p0, n0), (a1, p1, n1) in zip(*sizes):
-        assert n0 == n1
-        np.testing.assert_array_equal(a0, a1)
-        np.testing.assert_array_equal(p0, p1)
+    for other in sizes[1:]:
+        for (a0, p0, n0), (a1, p1, n1) in zip(sizes[0], other):
+            assert n0 == n1
+            np.testing.assert_array_equal(a0, a1)
+            np.testing.assert_array_equal(p0, p1)
     assert sum(a.sum() for a, _, _ in sizes[0]) > 0
