@@ -850,7 +850,7 @@ def measure_c2(args, dist, rank, local_rank):
     out = {"workload": wl["description"], "steps": steps, "warmup": warmup}
     with ClockSampler(local_rank) as clocks:
         mixed = measure(args, wl, "mixed", ES, dist, rank, local_rank, clocks, track_order=7,
-                        steps=steps, warmup=warmup, actions=False)
+                        steps=steps, warmup=warmup, actions=True)
         fp64 = measure(args, wl, "double", ES, dist, rank, local_rank, clocks, track_order=7,
                        steps=max(2, steps // 2), warmup=warmup, actions=False)
         out["clocks"] = clocks.summary()
@@ -858,6 +858,20 @@ def measure_c2(args, dist, rank, local_rank):
         out[name] = {"value": r["value"], "e2e": r["e2e"], "events_per_s": r["events_per_s"],
                      "ms_per_step": r["ms_per_step"], "unit": "track-steps/s"}
     out["mixed_vs_fp64_edep"] = compare_tallies(mixed["tallies"], fp64["tallies"])
+    dom = mixed.get("dominant")
+    if dom:
+        # The dominant kernel of the mixed path on this workload: its mean
+        # launch time (CUDA events over an eager transport) and its DRAM
+        # traffic against the algorithmic bytes
+        act = mixed["per_action"][dom]
+        traffic = read_traffic(dom, act["processed_per_launch"], "mixed", "c2")
+        out["dominant_kernel"] = {
+            "kernel": dom, "launch_ms": act["ms_per_launch"],
+            "processed_per_launch": act["processed_per_launch"],
+            "algorithmic_bytes_per_launch": act["bytes_per_launch"],
+            "traffic": traffic,
+            "traffic_over_algorithmic": (traffic / act["bytes_per_launch"]
+                                         if traffic else None)}
     return out
 
 

@@ -259,6 +259,9 @@ struct SurfaceRecord
     //! for conservative reachability bounds, never for a distance
     float radius;
     double value;
+    //! sqrt(value) for a z cylinder (0 for a plane), for the mixed build's
+    //! safety distance
+    double radius_d;
 };
 
 //! Volume: conjunction of face senses; inside_sense +1 means the inside is

@@ -944,7 +944,8 @@ void Builder::build_geometry()
         }
         float const radius
             = (type == surf_czc) ? static_cast<float>(std::sqrt(value)) : 0.0f;
-        hp_.surfaces.push_back({type, radius, value});
+        double const radius_d = (type == surf_czc) ? std::sqrt(value) : 0.0;
+        hp_.surfaces.push_back({type, radius, value, radius_d});
         return static_cast<size_type>(hp_.surfaces.size() - 1);
     };
     auto box_faces = [&](double const* lo, double const* hi, size_type* faces) {
