@@ -615,6 +615,13 @@ CoreState::CoreState(CoreParams const& params,
     ctx_.along_block_size = block_size;
     ctx_.sort_enabled = true;
     ctx_.partition_slots = false;
+    {
+        int device = 0, sms = 0;
+        GBX_CUDA(cudaGetDevice(&device));
+        GBX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        ctx_.range_blocks = std::min<unsigned int>(
+            (n + block_size - 1) / block_size, 8u * static_cast<unsigned int>(sms));
+    }
     ctx_.persistent_blocks = sizeof(real_type) < sizeof(double)
                                  ? persistent_along_blocks(ctx_.along_block_size)
                                  : 0;

@@ -709,6 +709,30 @@ __device__ __forceinline__ bool sorted_slot(StateData const& s,
     return true;
 }
 
+//! Call f(slot) for every slot of the sorted bins [first_bin, end_bin) (or,
+//! without offsets, every slot) with a grid-stride loop: a grid of a few
+//! blocks per SM covers a range of any length, where a grid sized for the
+//! whole state would launch mostly blocks that find no track of the action
+//! (the range lives on the device, so the host cannot size the grid to it)
+template<class F>
+__device__ __forceinline__ void for_each_sorted_slot(StateData const& s,
+                                                     size_type const* offsets,
+                                                     size_type first_bin,
+                                                     size_type end_bin,
+                                                     F&& f)
+{
+    size_type begin = 0;
+    size_type end = s.size;
+    if (offsets)
+    {
+        begin = offsets[first_bin];
+        end = offsets[end_bin];
+    }
+    size_type const stride = gridDim.x * blockDim.x;
+    for (size_type t = begin + blockIdx.x * blockDim.x + threadIdx.x; t < end; t += stride)
+        f(offsets ? s.track_slots[t] : t);
+}
+
 // Minimum resident blocks per SM requested for the charged along-step kernel
 // (1: the compiler may use up to 255 registers per thread)
 #ifndef GBX_ALONG_MIN_BLOCKS
@@ -740,9 +764,18 @@ along_step_sorted_kernel(ParamsData p,
                          size_type first_bin,
                          size_type end_bin)
 {
-    size_type slot;
-    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
-        along_step_impl<K>(p, s, slot);
+    if constexpr (K == AlongKind::neutral)
+    {
+        for_each_sorted_slot(s, offsets, first_bin, end_bin, [&](size_type slot) {
+            along_step_impl<K>(p, s, slot);
+        });
+    }
+    else
+    {
+        size_type slot;
+        if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
+            along_step_impl<K>(p, s, slot);
+    }
 }
 
 //! Charged along-step in a uniform field over the sorted charged range, as
@@ -815,13 +848,11 @@ __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
     size_type first_bin,
     size_type end_bin)
 {
-    size_type slot;
-    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
-    {
+    for_each_sorted_slot(s, offsets, first_bin, end_bin, [&](size_type slot) {
         size_type a = s.post_step_action[slot];
         if (a >= first_bin && a < end_bin)
             interact(p, s, slot, a);
-    }
+    });
 }
 
 __global__ __launch_bounds__(block_size) void boundary_sorted_kernel(
@@ -831,9 +862,8 @@ __global__ __launch_bounds__(block_size) void boundary_sorted_kernel(
     size_type first_bin,
     size_type end_bin)
 {
-    size_type slot;
-    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
-        boundary_cross(p, s, slot);
+    for_each_sorted_slot(
+        s, offsets, first_bin, end_bin, [&](size_type slot) { boundary_cross(p, s, slot); });
 }
 
 __global__ __launch_bounds__(block_size) void tracking_cut_sorted_kernel(
@@ -843,9 +873,8 @@ __global__ __launch_bounds__(block_size) void tracking_cut_sorted_kernel(
     size_type first_bin,
     size_type end_bin)
 {
-    size_type slot;
-    if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
-        tracking_cut(p, s, slot);
+    for_each_sorted_slot(
+        s, offsets, first_bin, end_bin, [&](size_type slot) { tracking_cut(p, s, slot); });
 }
 
 //! Bin offsets written by the sort for a key
@@ -955,7 +984,7 @@ void launch_along_step(LaunchContext const& ctx,
     }
     if (action == invalid_id || action == p.action_along_step_neutral)
     {
-        along_step_sorted_kernel<AlongKind::neutral><<<nb, block_size, 0, stream>>>(
+        along_step_sorted_kernel<AlongKind::neutral><<<ctx.range_blocks, block_size, 0, stream>>>(
             p, ctx.state, offsets, nfirst, nend);
     }
 }
@@ -976,7 +1005,7 @@ void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t st
         first = p.model_to_action;
         end = p.model_to_action + p.num_models;
     }
-    interact_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+    interact_sorted_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
         p,
         ctx.state,
         key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
@@ -987,7 +1016,7 @@ void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t st
 void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
-    boundary_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+    boundary_sorted_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
         p,
         ctx.state,
         key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
@@ -998,7 +1027,7 @@ void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
 void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
-    tracking_cut_sorted_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
+    tracking_cut_sorted_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
         p,
         ctx.state,
         key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),

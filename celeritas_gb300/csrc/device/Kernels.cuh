@@ -104,6 +104,9 @@ struct LaunchContext
     //! Tuning: threads per block of the charged along-step kernels (at most
     //! block_size) and whether the action sorts run this step
     int along_block_size;
+    //! Grid of the short sorted-range kernels (grid-stride loops): a few
+    //! blocks per SM, at most one block per block_size slots
+    unsigned int range_blocks;
     bool sort_enabled;
     //! Tuning: new charged tracks take the lowest vacant slots and neutral
     //! ones the highest (per-track random streams only), so that each
