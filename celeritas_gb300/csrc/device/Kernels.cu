@@ -133,10 +133,11 @@ __global__ __launch_bounds__(block_size) void generate_primaries_kernel(
 __global__ __launch_bounds__(block_size) void initialize_tracks_kernel(
     ParamsData p, StateData s)
 {
-    size_type tid = thread_slot();
+    // Grid-stride over the new tracks, whose number is on the device
     Counters const c = *s.counters;
-    size_type num_new = min_of(c.num_vacancies, c.num_initializers);
-    if (tid < num_new)
+    size_type const num_new = min_of(c.num_vacancies, c.num_initializers);
+    size_type const stride = gridDim.x * blockDim.x;
+    for (size_type tid = thread_slot(); tid < num_new; tid += stride)
     {
         init_track(p, s, c, tid);
     }
@@ -919,8 +920,8 @@ void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream)
     }
     else
     {
-        initialize_tracks_kernel<<<num_blocks_for(ctx.state.size), block_size, 0, stream>>>(
-            ctx.params, ctx.state);
+        initialize_tracks_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(ctx.params,
+                                                                            ctx.state);
     }
     finish_initialize_kernel<<<1, 1, 0, stream>>>(
         ctx.state, ctx.log, ctx.log_capacity, ctx.step_index);
