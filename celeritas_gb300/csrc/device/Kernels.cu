@@ -688,28 +688,6 @@ __global__ __launch_bounds__(sort_block_size) void sort_scatter_kernel(
     }
 }
 
-//! Slot of this thread within the sorted bins [first_bin, end_bin), or,
-//! without offsets (sorting off), the thread's own slot: the action
-//! functions then skip slots whose action is not theirs, as the sort would
-__device__ __forceinline__ bool sorted_slot(StateData const& s,
-                                            size_type const* offsets,
-                                            size_type first_bin,
-                                            size_type end_bin,
-                                            size_type* slot)
-{
-    size_type const i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!offsets)
-    {
-        *slot = i;
-        return i < s.size;
-    }
-    size_type const t = offsets[first_bin] + i;
-    if (t >= offsets[end_bin])
-        return false;
-    *slot = s.track_slots[t];
-    return true;
-}
-
 //! Call f(slot) for every slot of the sorted bins [first_bin, end_bin) (or,
 //! without offsets, every slot) with a grid-stride loop: a grid of a few
 //! blocks per SM covers a range of any length, where a grid sized for the
@@ -765,18 +743,9 @@ along_step_sorted_kernel(ParamsData p,
                          size_type first_bin,
                          size_type end_bin)
 {
-    if constexpr (K == AlongKind::neutral)
-    {
-        for_each_sorted_slot(s, offsets, first_bin, end_bin, [&](size_type slot) {
-            along_step_impl<K>(p, s, slot);
-        });
-    }
-    else
-    {
-        size_type slot;
-        if (sorted_slot(s, offsets, first_bin, end_bin, &slot))
-            along_step_impl<K>(p, s, slot);
-    }
+    for_each_sorted_slot(s, offsets, first_bin, end_bin, [&](size_type slot) {
+        along_step_impl<K>(p, s, slot);
+    });
 }
 
 //! Charged along-step in a uniform field over the sorted charged range, as
@@ -952,6 +921,10 @@ void launch_along_step(LaunchContext const& ctx,
     unsigned int const nb = num_blocks_for(ctx.state.size);
     unsigned int const abs = static_cast<unsigned int>(ctx.along_block_size);
     unsigned int const anb = (ctx.state.size + abs - 1) / abs;
+    // Charged along-step grid: up to 2^19 threads (grid-stride beyond), so
+    // that a charged range well below the state size does not launch
+    // thousands of blocks that find no track
+    unsigned int const cnb = min_of(anb, max_of(1u, (1u << 19) / abs));
     size_type const* offsets
         = key_offsets(ctx, SortKey::along_step, sorts_along_step(p.track_order));
     size_type cfirst, cend, nfirst, nend;
@@ -975,11 +948,11 @@ void launch_along_step(LaunchContext const& ctx,
         else if (large)
         {
             along_step_sorted_kernel<AlongKind::charged, along_block_large>
-                <<<anb, abs, 0, stream>>>(p, ctx.state, offsets, cfirst, cend);
+                <<<cnb, abs, 0, stream>>>(p, ctx.state, offsets, cfirst, cend);
         }
         else
         {
-            along_step_sorted_kernel<AlongKind::charged><<<anb, abs, 0, stream>>>(
+            along_step_sorted_kernel<AlongKind::charged><<<cnb, abs, 0, stream>>>(
                 p, ctx.state, offsets, cfirst, cend);
         }
     }
