@@ -1,9 +1,10 @@
 """Benchmark: track-steps/s and events/s of the EM-shower stepping loop.
 
 Default workload: c3, the CMS-like detector (1300 events of 50 e-/gamma
-primaries, 3.8 T, 2^21 track slots). Bench step k transports events
-[65k, 65k + 65) to completion, so the default 20 steps cover every event of
-the configuration once. Prints one JSON line on rank 0:
+primaries, 3.8 T, 2^21 track slots). The timed steps transport every event
+of the configuration once: step k transports the k-th batch of
+max(65, ceil(1300 / steps)) consecutive events to completion. Prints one
+JSON line on rank 0:
 
 * value / events_per_s: the batched, autotuned, action-sorted
   mixed-precision path (the headline);

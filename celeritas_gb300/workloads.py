@@ -56,9 +56,9 @@ WORKLOADS = {
                            "(r 129-152 cm), 17 x (5 cm brass + 0.4 cm scintillator) "
                            "(r 180-295 cm), 3.8 T along z, Urban MSC; 1300 events of 50 "
                            "e-/gamma, log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; "
-                           "bench step k transports events [65k, 65k + 65), so 20 "
-                           "steps cover all 1300 events; launch configuration "
-                           "autotuned on 65 other events (one batch)"),
+                           "the timed steps transport all 1300 events in consecutive "
+                           "batches of max(65, ceil(1300 / steps)) events; launch "
+                           "configuration autotuned on 65 other events"),
     # c3 in the synthetic R-Z field map of the CMS-like detector (a 3.8 T
     # solenoid with soft edges and a return flux) instead of the uniform field
     "c3rz": dict(geometry="cms", physics="cms", num_primaries=65000, energy=1000.0,
@@ -67,9 +67,10 @@ WORKLOADS = {
                  events_per_step=65, tune_primaries=3250, reentrant_looping=True,
                  description="CMS-like detector in an R-Z field map (3.8 T solenoid, soft "
                              "edges, return flux), Urban MSC; 1300 events of 50 e-/gamma, "
-                             "log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; bench step "
-                             "k transports events [65k, 65k + 65); launch configuration "
-                             "autotuned on 65 other events (one batch)"),
+                             "log-uniform 1-100 GeV, |eta| < 1.5; 2^21 slots; the timed "
+                             "steps transport all 1300 events in batches of max(65, "
+                             "ceil(1300 / steps)); launch configuration autotuned on 65 "
+                             "other events"),
     # Batching of uneven events: CMS-like detector, 4096 events with primaries
     # per event log-uniform in 1-1000 and energies log-uniform in
     # 0.1-100 GeV (e-/gamma alternating, |eta| < 1.5), all in flight
@@ -121,19 +122,22 @@ def step_batches(wl: dict, rank: int, steps: int):
     """Primaries of each timed bench step and of the warm-up steps.
 
     A workload with 'events_per_step' splits its events into consecutive
-    batches: timed step k transports batch k (modulo the number of batches),
-    so that as many steps as batches cover every event of the workload once.
-    Warm-up steps transport one batch of other events (another beam seed).
-    Any other workload transports all its primaries in every step.
+    batches of that many events, or of ceil(events / steps) where fewer
+    steps would leave events out: timed step k transports batch k (modulo the
+    number of batches), so that the timed steps cover every event of the
+    workload once. Warm-up steps transport one batch of other events
+    (another beam seed). Any other workload transports all its primaries in
+    every step.
     """
     per_step = wl.get("events_per_step")
     if not per_step:
         p = make_primaries(wl, rank, num=wl.get("bench_primaries"))
         return [p] * steps, p
+    per_step = max(per_step, -(-wl["events"] // max(1, steps)))
     per_event = wl["num_primaries"] // wl["events"]
     allp = make_primaries(wl, rank)
     size = per_step * per_event
-    nb = wl["events"] // per_step
+    nb = -(-wl["events"] // per_step)
     batches = [allp[k * size:(k + 1) * size] for k in range(nb)]
     warm = make_primaries(wl, rank, num=size, seed_offset=55)
     return [batches[k % nb] for k in range(steps)], warm
