@@ -89,3 +89,25 @@ def test_single_process_reduction_is_identity():
     red = sharding.reduce_run(None, "cpu", 5.0, 0.5, 123.0, np.ones(3))
     assert (red["time_ms"], red["e2e_s"], red["track_steps"]) == (5.0, 0.5, 123.0)
     np.testing.assert_array_equal(red["tallies"], np.ones(3))
+
+
+@pytest.mark.parametrize("steps", [1, 3, 10, 20, 25])
+def test_bench_batches_cover_every_event(steps):
+    """The timed bench steps of a batched workload transport every event of
+    the configuration: batches of max(65, ceil(1300 / steps)) consecutive
+    events, the warm-up batch of other events."""
+    import numpy as np
+
+    from celeritas_gb300.workloads import WORKLOADS, step_batches
+
+    wl = WORKLOADS["c3"]
+    batches, warm = step_batches(wl, 0, steps)
+    assert len(batches) == steps
+    per_event = wl["num_primaries"] // wl["events"]
+    size = max(wl["events_per_step"], -(-wl["events"] // steps))
+    first = min(steps, -(-wl["events"] // size))
+    events = np.concatenate([b["event"] for b in batches[:first]])
+    assert len(np.unique(events)) == wl["events"]
+    assert all(len(b) <= size * per_event for b in batches)
+    assert len(warm) == size * per_event
+    assert not np.array_equal(warm["energy"], batches[0]["energy"])
