@@ -648,7 +648,8 @@ GBX_FUNCTION void GeoTrackView::consider_crossing(size_type surf,
 //!
 //! The reference visits crossings by increasing (distance, surface ID) and
 //! accepts the first whose bumped point lies inside a neighboring volume
-//! (src/orange/univ/detail/Utils.hh, BackgroundImpl in SimpleUnitTracker).
+//! (SimpleUnitTracker::background_intersect,
+//! src/orange/univ/SimpleUnitTracker.hh:572-645).
 //! Acceptance depends on that crossing alone, so the result is the least
 //! (distance, surface ID) over accepted crossings, whatever order they are
 //! tested in; a crossing is tested only if it would improve the current one.
@@ -664,8 +665,9 @@ GBX_FUNCTION void GeoTrackView::consider_crossing(size_type surf,
 //!   compares hba^2 with c and takes t = sqrt(hba^2 - c); c falls as v
 //!   grows, so whether the ray reaches the cylinder, the far root
 //!   -hba + t (growing with v) and the near root -hba - t (falling with v)
-//!   are all monotone. Far roots are walked upward from the radius of
-//!   closest approach, near roots downward from the track's radius.
+//!   are all monotone. Near roots are walked downward from the track's
+//!   radius, far roots upward from just below it (a reached cylinder well
+//!   inside the track's radius has both roots taken by the downward walk).
 //! Index bounds from the FP32 keys only ever start a walk earlier than
 //! needed (rounding to FP32 is monotone too), and an FP32 radial bound |r -
 //! R| stops a cylinder walk only where every root is beyond the limit, with
