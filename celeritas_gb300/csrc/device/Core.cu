@@ -448,7 +448,8 @@ CoreState::CoreState(CoreParams const& params,
     std::size_t o_mdisp = arr(1), o_mtrue = arr(sizeof(real_type)),
                 o_mgeom = arr(sizeof(real_type)), o_malpha = arr(sizeof(real_type)),
                 o_mrinit = arr(sizeof(real_type)), o_mrfac = arr(sizeof(real_type)),
-                o_mlmin = arr(sizeof(real_type)), o_nloop = arr(4);
+                o_mlmin = arr(sizeof(real_type)), o_nloop = arr(4),
+                o_lekey = arr(sizeof(real_type)), o_leval = arr(sizeof(real_type));
     std::size_t o_rng = L.reserve(std::size_t(6) * 4 * n);
     std::size_t o_vac = arr(4), o_cnts = arr(4), o_parents = arr(4);
     std::size_t o_inits = L.reserve(sizeof(TrackInitializer) * std::size_t(init_cap));
@@ -526,6 +527,8 @@ CoreState::CoreState(CoreParams const& params,
     s.msc_displaced = static_cast<std::uint8_t*>(at(o_mdisp));
     s.msc_true_path = static_cast<real_type*>(at(o_mtrue));
     s.msc_geom_path = static_cast<real_type*>(at(o_mgeom));
+    s.log_energy_key = static_cast<real_type*>(at(o_lekey));
+    s.log_energy_value = static_cast<real_type*>(at(o_leval));
     s.msc_alpha = static_cast<real_type*>(at(o_malpha));
     s.msc_range_init = static_cast<real_type*>(at(o_mrinit));
     s.msc_range_factor = static_cast<real_type*>(at(o_mrfac));
@@ -555,7 +558,10 @@ CoreState::CoreState(CoreParams const& params,
     s.track_slots = static_cast<size_type*>(at(o_tslots));
     s.action_offsets = static_cast<size_type*>(at(o_aoff));
 
-    // Initial values that are not zero: fill from host staging
+    // Initial values that are not zero: fill from host staging. All-ones
+    // bytes make the log(energy) keys NaN (they match no energy).
+    GBX_CUDA(cudaMemsetAsync(
+        s.log_energy_key, 0xFF, sizeof(real_type) * std::size_t(n), stream_));
     {
         std::vector<std::uint32_t> words;
         initialize_xorwow(seed, n, &words);

@@ -80,7 +80,7 @@ GBX_FUNCTION void pre_step(ParamsData const& p, StateData const& s, size_type sl
     size_type const pid = s.particle_id[slot];
     size_type const mid = s.material[slot];
     real_type const energy = s.energy[slot];
-    PhysicsTrack phys(p, pid, mid);
+    PhysicsTrack phys(p, pid, mid, s, slot);
 
     // calc_physics_step_limit
     real_type total_macro_xs = 0;
@@ -390,7 +390,7 @@ GBX_FUNCTION void along_epilogue(ParamsData const& p,
     }
 
     // ElossApplier
-    PhysicsTrack phys(p, pid, s.material[slot]);
+    PhysicsTrack phys(p, pid, s.material[slot], s, slot);
     if (charged && phys.group().eloss_process != invalid_id && s.energy[slot] != 0)
     {
         real_type const step = s.step_length[slot];
@@ -483,7 +483,7 @@ GBX_FUNCTION void discrete_select(ParamsData const& p,
     size_type const pid = s.particle_id[slot];
     size_type const mid = s.material[slot];
     real_type const energy = s.energy[slot];
-    PhysicsTrack phys(p, pid, mid);
+    PhysicsTrack phys(p, pid, mid, s, slot);
     XorwowEngine rng(s.rng, slot);
 
     // Select the process (Selector with total = macro xs)

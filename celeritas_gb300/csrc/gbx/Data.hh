@@ -673,6 +673,10 @@ struct StateData
     std::uint8_t* msc_displaced;
     real_type* msc_true_path;
     real_type* msc_geom_path;
+    //! log(energy) of the slot's energy 'key' (FP64 build), kept across the
+    //! step's actions; a NaN key matches no energy
+    real_type* log_energy_key;
+    real_type* log_energy_value;
     real_type* msc_alpha;
     real_type* msc_range_init;
     real_type* msc_range_factor;

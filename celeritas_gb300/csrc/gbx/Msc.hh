@@ -234,7 +234,7 @@ GBX_FUNCTION double msc_limit_step(ParamsData const& p,
     size_type const pid = s.particle_id[slot];
     size_type const mid = s.material[slot];
     real_type const energy = s.energy[slot];
-    PhysicsTrack phys(p, pid, mid);
+    PhysicsTrack phys(p, pid, mid, s, slot);
     MscHelper helper(p, s, phys, slot, pid, mid);
     GeoTrackView geo(p.geo, s, slot);
     bool displaced = false;
@@ -395,7 +395,7 @@ GBX_FUNCTION void msc_apply_step(ParamsData const& p,
         return;
     size_type const pid = s.particle_id[slot];
     size_type const mid = s.material[slot];
-    PhysicsTrack phys(p, pid, mid);
+    PhysicsTrack phys(p, pid, mid, s, slot);
     MscHelper helper(p, s, phys, slot, pid, mid);
     GeoTrackView geo(p.geo, s, slot);
     MaterialRecord const& mat = p.materials[mid];

@@ -248,6 +248,26 @@ class PhysicsTrack
     {
     }
 
+    //! Physics of the track in 'slot', whose log(energy) the FP64 build
+    //! keeps per slot between the step's actions (a correctly rounded FP64
+    //! logarithm costs tens of FP64 instructions, of which GB300 issues two
+    //! per SM and clock; the mixed build's FP32 logarithm costs less than
+    //! the memory traffic would)
+    GBX_FORCEINLINE PhysicsTrack(ParamsData const& p,
+                                 size_type particle,
+                                 size_type material,
+                                 StateData const& s,
+                                 size_type slot)
+        : PhysicsTrack(p, particle, material)
+    {
+        if constexpr (sizeof(real_type) == sizeof(double))
+        {
+            cache_key_ = s.log_energy_key + slot;
+            cache_val_ = s.log_energy_value + slot;
+            slot_energy_ = s.energy[slot];
+        }
+    }
+
     GBX_FORCEINLINE size_type num_processes() const
     {
         return group_.num_processes;
@@ -257,14 +277,29 @@ class PhysicsTrack
     //! of one step take the logarithm of the same few energies many times
     //! (every process at E and at E * min_eprime_over_e, the range and the
     //! stopping power at E), and the function returns the same double for
-    //! the same argument, so a remembered value changes no result
+    //! the same argument, so a remembered value changes no result. With a
+    //! slot cache, the log of the slot's energy is also kept across the
+    //! step's actions, keyed by the exact energy.
     GBX_FORCEINLINE real_type log_energy(real_type energy) const
     {
         if (energy == memo_e_[0])
             return memo_log_[0];
         if (energy == memo_e_[1])
             return memo_log_[1];
-        real_type const result = libm::log(energy);
+        real_type result;
+        if (cache_key_ && energy == *cache_key_)
+        {
+            result = *cache_val_;
+        }
+        else
+        {
+            result = libm::log(energy);
+            if (cache_key_ && energy == slot_energy_)
+            {
+                *cache_key_ = energy;
+                *cache_val_ = result;
+            }
+        }
         memo_e_[1] = memo_e_[0];
         memo_log_[1] = memo_log_[0];
         memo_e_[0] = energy;
@@ -383,6 +418,10 @@ class PhysicsTrack
     // log_energy's remembered arguments (NaN: none yet) and results
     mutable real_type memo_e_[2]{real_type(NAN), real_type(NAN)};
     mutable real_type memo_log_[2]{0, 0};
+    //! Per-slot cache of log(energy) (FP64 build; null otherwise)
+    real_type* cache_key_{nullptr};
+    real_type* cache_val_{nullptr};
+    real_type slot_energy_{0};
 };
 
 //---------------------------------------------------------------------------//
