@@ -746,6 +746,8 @@ class FieldPropagation
             cdir.y *= inv_clen;
             cdir.z *= inv_clen;
         }
+        // The geometry's direction is always the last chord's (a query of a
+        // later substep with a chord shorter than the minimum uses it)
         if (clen >= minimum_substep)
         {
             geo.set_dir(cdir);
@@ -768,6 +770,17 @@ class FieldPropagation
                                       ? geo.no_crossing(max_dist)
                                       : geo.find_next_step(max_dist);
 #endif
+        if (!linear_step.boundary)
+        {
+            state_ = substep.state;
+            result_.boundary = false;
+            result_.distance += substep.step;
+            remaining_ = step_ - result_.distance;
+            geo.move_internal_to(state_.pos);
+            --remaining_substeps_;
+            return;
+        }
+        // Scaled length of the chord up to the crossing (only with one)
         double const update_length = substep.step * linear_step.distance / clen;
         auto is_intercept_close = [&]() {
             double delta_sq = 0;
@@ -778,16 +791,7 @@ class FieldPropagation
             }
             return delta_sq <= ipow<2>(delta_intersection);
         };
-        if (!linear_step.boundary)
-        {
-            state_ = substep.state;
-            result_.boundary = false;
-            result_.distance += substep.step;
-            remaining_ = step_ - result_.distance;
-            geo.move_internal_to(state_.pos);
-            --remaining_substeps_;
-        }
-        else if (result_.boundary && (linear_step.distance) < bump_distance)
+        if (result_.boundary && (linear_step.distance) < bump_distance)
         {
             remaining_ = substep.step / 2;
         }
