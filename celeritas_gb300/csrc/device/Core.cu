@@ -449,7 +449,8 @@ CoreState::CoreState(CoreParams const& params,
                 o_mgeom = arr(sizeof(real_type)), o_malpha = arr(sizeof(real_type)),
                 o_mrinit = arr(sizeof(real_type)), o_mrfac = arr(sizeof(real_type)),
                 o_mlmin = arr(sizeof(real_type)), o_nloop = arr(4),
-                o_lekey = arr(sizeof(real_type)), o_leval = arr(sizeof(real_type));
+                o_lekey = arr(sizeof(real_type)), o_leval = arr(sizeof(real_type)),
+                o_iidx = arr(4);
     std::size_t o_rng = L.reserve(std::size_t(6) * 4 * n);
     std::size_t o_vac = arr(4), o_cnts = arr(4), o_parents = arr(4);
     std::size_t o_inits = L.reserve(sizeof(TrackInitializer) * std::size_t(init_cap));
@@ -529,6 +530,7 @@ CoreState::CoreState(CoreParams const& params,
     s.msc_geom_path = static_cast<real_type*>(at(o_mgeom));
     s.log_energy_key = static_cast<real_type*>(at(o_lekey));
     s.log_energy_value = static_cast<real_type*>(at(o_leval));
+    s.init_indices = static_cast<size_type*>(at(o_iidx));
     s.msc_alpha = static_cast<real_type*>(at(o_malpha));
     s.msc_range_init = static_cast<real_type*>(at(o_mrinit));
     s.msc_range_factor = static_cast<real_type*>(at(o_mrfac));

@@ -189,6 +189,110 @@ __global__ __launch_bounds__(block_size) void initialize_tracks_partitioned_kern
     init_track_at(p, s, c, tid, slot);
 }
 
+//---------------------------------------------------------------------------//
+// Charge partition of new tracks (TrackOrder init_charge): a stable
+// partition of the last num_new initializers, neutral ones first
+// (partition_initializers, src/celeritas/track/detail/
+// TrackInitAlgorithms.cc:75-95), as a per-block count, a scan of the block
+// counts and a scatter that ranks each initializer within its group. The
+// end-of-step scan scratch is free at the start of the step: block_vacant
+// holds the neutral count of each block, count[0] the total.
+//---------------------------------------------------------------------------//
+__device__ __forceinline__ bool new_track_is_neutral(ParamsData const& p,
+                                                     StateData const& s,
+                                                     Counters const& c,
+                                                     size_type num_new,
+                                                     size_type i)
+{
+    return i < num_new
+           && is_neutral(p, s.initializers[c.num_initializers - num_new + i]);
+}
+
+__global__ __launch_bounds__(block_size) void charge_partition_count_kernel(
+    ParamsData p, StateData s, ScanScratch scr)
+{
+    Counters const c = *s.counters;
+    size_type const num_new = min_of(c.num_vacancies, c.num_initializers);
+    bool const neutral = new_track_is_neutral(p, s, c, num_new, thread_slot());
+    int const n = __syncthreads_count(neutral);
+    if (threadIdx.x == 0)
+        scr.block_vacant[blockIdx.x] = static_cast<size_type>(n);
+}
+
+__global__ __launch_bounds__(1024) void charge_partition_scan_kernel(ScanScratch scr)
+{
+    // Exclusive scan of the per-block neutral counts by one block
+    __shared__ size_type sh[1024];
+    __shared__ size_type carry;
+    if (threadIdx.x == 0)
+        carry = 0;
+    __syncthreads();
+    for (size_type base = 0; base < scr.num_blocks; base += 1024)
+    {
+        size_type const i = base + threadIdx.x;
+        size_type const v = i < scr.num_blocks ? scr.block_vacant[i] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1)
+        {
+            size_type const a = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += a;
+            __syncthreads();
+        }
+        if (i < scr.num_blocks)
+            scr.block_vacant[i] = carry + sh[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023)
+            carry += sh[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        scr.count[0] = carry;
+}
+
+__global__ __launch_bounds__(block_size) void charge_partition_scatter_kernel(
+    ParamsData p, StateData s, ScanScratch scr)
+{
+    __shared__ size_type warp_neutral[block_size / 32];
+    Counters const c = *s.counters;
+    size_type const num_new = min_of(c.num_vacancies, c.num_initializers);
+    size_type const i = thread_slot();
+    bool const neutral = new_track_is_neutral(p, s, c, num_new, i);
+    unsigned int const lane = threadIdx.x & 31u;
+    unsigned int const warp = threadIdx.x >> 5;
+    unsigned int const ballot = __ballot_sync(0xffffffffu, neutral);
+    if (lane == 0)
+        warp_neutral[warp] = __popc(ballot);
+    __syncthreads();
+    size_type before = scr.block_vacant[blockIdx.x] + __popc(ballot & ((1u << lane) - 1u));
+    for (unsigned int w = 0; w < warp; ++w)
+        before += warp_neutral[w];
+    if (i < num_new)
+    {
+        size_type const pos = neutral ? before : scr.count[0] + (i - before);
+        s.init_indices[pos] = i;
+    }
+}
+
+__global__ __launch_bounds__(block_size) void initialize_tracks_charge_kernel(
+    ParamsData p, StateData s)
+{
+    Counters const c = *s.counters;
+    size_type const num_new = min_of(c.num_vacancies, c.num_initializers);
+    size_type const stride = gridDim.x * blockDim.x;
+    for (size_type tid = thread_slot(); tid < num_new; tid += stride)
+        init_track_charge_partitioned(p, s, c, num_new, tid);
+}
+
+//! Clear stale parent slots after the charge-partitioned initialization
+__global__ __launch_bounds__(block_size) void clear_parents_kernel(StateData s)
+{
+    size_type const stride = gridDim.x * blockDim.x;
+    for (size_type i = thread_slot(); i < s.size; i += stride)
+        s.parents[i] = invalid_id;
+}
+
 __global__ void finish_initialize_kernel(StateData s,
                                          StepRecord* log,
                                          size_type log_capacity,
@@ -395,7 +499,8 @@ __global__ void count_event_live_kernel(StateData s, size_type num_events)
 // End of step: vacancies and secondaries
 //---------------------------------------------------------------------------//
 __global__ __launch_bounds__(block_size) void locate_alive_kernel(StateData s,
-                                                                  ScanScratch scr)
+                                                                  ScanScratch scr,
+                                                                  bool in_place)
 {
     __shared__ BlockScanStorage tmp;
     size_type slot = thread_slot();
@@ -403,7 +508,7 @@ __global__ __launch_bounds__(block_size) void locate_alive_kernel(StateData s,
     size_type count = 0;
     if (slot < s.size)
     {
-        locate_alive(s, slot, &vacant, &count);
+        locate_alive(s, slot, &vacant, &count, in_place);
         scr.vacant[slot] = vacant;
         scr.count[slot] = count;
     }
@@ -880,6 +985,23 @@ void launch_generate_primaries(LaunchContext const& ctx,
 
 void launch_initialize_tracks(LaunchContext const& ctx, cudaStream_t stream)
 {
+    if (partitions_by_charge(ctx.params.track_order))
+    {
+        // InitializeTracksAction with TrackOrder init_charge
+        // (InitializeTracksAction.cc:55-95)
+        unsigned int const nb = num_blocks_for(ctx.state.size);
+        charge_partition_count_kernel<<<nb, block_size, 0, stream>>>(
+            ctx.params, ctx.state, ctx.scratch);
+        charge_partition_scan_kernel<<<1, 1024, 0, stream>>>(ctx.scratch);
+        charge_partition_scatter_kernel<<<nb, block_size, 0, stream>>>(
+            ctx.params, ctx.state, ctx.scratch);
+        initialize_tracks_charge_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
+            ctx.params, ctx.state);
+        finish_initialize_kernel<<<1, 1, 0, stream>>>(
+            ctx.state, ctx.log, ctx.log_capacity, ctx.step_index);
+        clear_parents_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(ctx.state);
+        return;
+    }
     if (ctx.partition_slots)
     {
         initialize_tracks_partitioned_kernel<<<num_blocks_for(ctx.state.size),
@@ -1027,7 +1149,8 @@ void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream)
 void launch_extend_from_secondaries(LaunchContext const& ctx, cudaStream_t stream)
 {
     unsigned int nb = num_blocks_for(ctx.state.size);
-    locate_alive_kernel<<<nb, block_size, 0, stream>>>(ctx.state, ctx.scratch);
+    locate_alive_kernel<<<nb, block_size, 0, stream>>>(
+        ctx.state, ctx.scratch, !partitions_by_charge(ctx.params.track_order));
     scan_blocks_kernel<<<1, 1024, 0, stream>>>(
         ctx.state, ctx.scratch, ctx.log, ctx.log_capacity, ctx.step_index);
     scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, ctx.scratch);
@@ -1215,7 +1338,8 @@ void launch_extend_from_secondaries_static(LaunchContext const& ctx,
     scr.vacant = base + 2 * block_part + count_part;
     scr.num_blocks = nb;
 
-    locate_alive_kernel<<<nb, block_size, 0, stream>>>(ctx.state, scr);
+    locate_alive_kernel<<<nb, block_size, 0, stream>>>(
+        ctx.state, scr, !partitions_by_charge(ctx.params.track_order));
     scan_blocks_kernel<<<1, 1024, 0, stream>>>(
         ctx.state, scr, ctx.log, ctx.log_capacity, ctx.step_index);
     scatter_kernel<<<nb, block_size, 0, stream>>>(ctx.params, ctx.state, scr);

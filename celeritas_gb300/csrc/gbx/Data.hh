@@ -33,11 +33,12 @@ GBX_FORCEINLINE bool is_track_valid(std::uint8_t s)
 }
 
 //! Track ordering policies (src/celeritas/Types.hh:151-171); the values
-//! are the reference's enumerators. Only 'none' and the action sorts are
-//! built.
+//! are the reference's enumerators. Built: 'none', the charge partition of
+//! new tracks' slots and the action sorts.
 enum TrackOrder : unsigned int
 {
     track_order_none = 0,
+    track_order_init_charge = 1,
     track_order_reindex_along_step_action = 5,
     track_order_reindex_step_limit_action = 6,
     track_order_reindex_both_action = 7,
@@ -53,6 +54,12 @@ GBX_FORCEINLINE bool sorts_step_limit(unsigned int order)
 {
     return order == track_order_reindex_step_limit_action
            || order == track_order_reindex_both_action;
+}
+
+//! Whether new tracks' slots are partitioned by charge (init_charge)
+GBX_FORCEINLINE bool partitions_by_charge(unsigned int order)
+{
+    return order == track_order_init_charge;
 }
 
 //! Value grid types (src/celeritas/phys/PhysicsData.hh ValueGridType)
@@ -677,6 +684,9 @@ struct StateData
     //! step's actions; a NaN key matches no energy
     real_type* log_energy_key;
     real_type* log_energy_value;
+    //! init_charge: the new tracks' initializers (offsets into the last
+    //! num_new of the list), neutral ones first, each group in list order
+    size_type* init_indices;
     real_type* msc_alpha;
     real_type* msc_range_init;
     real_type* msc_range_factor;

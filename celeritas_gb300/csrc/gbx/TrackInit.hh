@@ -148,17 +148,14 @@ GBX_FUNCTION void process_primary(StateData const& s,
     ti.parent_id = invalid_id;
 }
 
-//! Initialize vacant slot 'slot' from initializer 'tid' counted from the
-//! back of the list (InitTracksExecutor)
-GBX_FUNCTION void init_track_at(ParamsData const& p,
-                                StateData const& s,
-                                Counters const& counters,
-                                size_type tid,
-                                size_type slot)
+//! Initialize vacant slot 'slot' from an initializer, copying the geometry
+//! state of slot 'parent' if valid (InitTracksExecutor)
+GBX_FUNCTION void init_track_from(ParamsData const& p,
+                                  StateData const& s,
+                                  TrackInitializer const& init,
+                                  size_type slot,
+                                  size_type parent)
 {
-    TrackInitializer const& init
-        = s.initializers[counters.num_initializers - tid - 1];
-
     // Sim state
     s.track_id[slot] = init.track_id;
     s.parent_id[slot] = init.parent_id;
@@ -175,11 +172,6 @@ GBX_FUNCTION void init_track_at(ParamsData const& p,
 
     // Geometry: copy the parent's state or locate from scratch
     GeoTrackView geo(p.geo, s, slot);
-    size_type parent = invalid_id;
-    if (tid < counters.num_secondaries)
-    {
-        parent = s.parents[s.size - tid - 1];
-    }
     if (parent != invalid_id)
     {
         geo.copy_from(parent, init.dir);
@@ -208,6 +200,24 @@ GBX_FUNCTION void init_track_at(ParamsData const& p,
     }
 }
 
+//! Initialize vacant slot 'slot' from initializer 'tid' counted from the
+//! back of the list; the first num_secondaries new tracks may have a parent
+//! slot to copy the geometry from
+GBX_FUNCTION void init_track_at(ParamsData const& p,
+                                StateData const& s,
+                                Counters const& counters,
+                                size_type tid,
+                                size_type slot)
+{
+    size_type parent = invalid_id;
+    if (tid < counters.num_secondaries)
+    {
+        parent = s.parents[s.size - tid - 1];
+    }
+    init_track_from(
+        p, s, s.initializers[counters.num_initializers - tid - 1], slot, parent);
+}
+
 //! Initialize a vacant slot from an initializer: new track 'tid' takes the
 //! tid-th initializer and vacancy from the back of their lists
 //! (InitTracksExecutor)
@@ -220,12 +230,49 @@ GBX_FUNCTION void init_track(ParamsData const& p,
         p, s, counters, tid, s.vacancies[counters.num_vacancies - tid - 1]);
 }
 
+//! Whether an initializer is neutral (IsNeutral, src/celeritas/track/
+//! detail/Utils.hh:34-46)
+GBX_FORCEINLINE bool is_neutral(ParamsData const& p, TrackInitializer const& init)
+{
+    return p.particles[init.particle_id].charge == 0;
+}
+
+//! Initialize new track 'tid' with the charge partition (TrackOrder
+//! init_charge; InitTracksExecutor.hh:71-108): s.init_indices lists the
+//! last num_new initializers neutral ones first, and thread 'tid' takes
+//! entry num_new - tid - 1 of it. A neutral track takes the vacancy at the
+//! same position from the front of the list's first num_new entries, a
+//! charged one the tid-th from the back of the whole list, so that charged
+//! and neutral tracks fill the two ends of the vacant slots. The parent
+//! slot, for the first num_secondaries threads, is at the same partitioned
+//! position of the parent list.
+GBX_FUNCTION void init_track_charge_partitioned(ParamsData const& p,
+                                                StateData const& s,
+                                                Counters const& counters,
+                                                size_type num_new,
+                                                size_type tid)
+{
+    size_type const j = s.init_indices[num_new - tid - 1];
+    TrackInitializer const& init
+        = s.initializers[j + counters.num_initializers - num_new];
+    size_type const slot = is_neutral(p, init)
+                               ? s.vacancies[num_new - tid - 1]
+                               : s.vacancies[counters.num_vacancies - tid - 1];
+    size_type parent = invalid_id;
+    if (tid < counters.num_secondaries)
+    {
+        parent = s.parents[j + s.size - num_new];
+    }
+    init_track_from(p, s, init, slot, parent);
+}
+
 //! Flag the slot as vacant or occupied and count secondaries that need a
 //! new slot (LocateAliveExecutor); returns {is_vacant, num_new_secondaries}
 GBX_FUNCTION void locate_alive(StateData const& s,
                                size_type slot,
                                bool* vacant,
-                               size_type* count)
+                               size_type* count,
+                               bool in_place = true)
 {
     size_type num_secondaries = 0;
     std::uint8_t const status = s.status[slot];
@@ -243,8 +290,11 @@ GBX_FUNCTION void locate_alive(StateData const& s,
     {
         *vacant = false;
     }
-    else if (num_secondaries > 0)
+    else if (num_secondaries > 0 && in_place)
     {
+        // The first secondary will take the dead track's slot (not with
+        // the charge partition, which initializes every secondary from the
+        // queue)
         --num_secondaries;
         *vacant = false;
     }
@@ -296,7 +346,8 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
         ti.dir = to_geo_dir(secondary.direction);
         ti.particle_id = secondary.particle_id;
         ti.energy = secondary.energy;
-        if (!initialized && status != status_alive)
+        if (!initialized && status != status_alive
+            && !partitions_by_charge(p.track_order))
         {
             // Reuse this slot for the first secondary
             s.track_id[slot] = ti.track_id;
@@ -320,7 +371,10 @@ GBX_FUNCTION void process_secondaries(ParamsData const& p,
         else
         {
             s.initializers[counters.num_initializers - offset] = ti;
-            if (offset <= s.size)
+            // With the charge partition a secondary copies the geometry of
+            // a parent that is still alive only (its slot is not reused)
+            if (offset <= s.size
+                && (!partitions_by_charge(p.track_order) || status == status_alive))
             {
                 s.parents[s.size - offset] = slot;
             }

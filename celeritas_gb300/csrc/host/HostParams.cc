@@ -288,6 +288,9 @@ void Builder::build_actions()
     switch (opts_.track_order)
     {
         case track_order_none:
+        case track_order_init_charge:
+            // No sort action: the charge partition is part of the track
+            // initialization (CoreParams.cc:264-269)
             break;
         case track_order_reindex_along_step_action:
             s.action_sort_along = hp_.action_labels.size();
@@ -305,7 +308,7 @@ void Builder::build_actions()
             break;
         default:
             throw std::runtime_error("track order " + std::to_string(opts_.track_order)
-                                     + " is not supported (0, 5, 6 or 7)");
+                                     + " is not supported (0, 1, 5, 6 or 7)");
     }
     hp_.action_labels.push_back("step-gather-pre");
     hp_.action_labels.push_back("step-gather-post");

@@ -58,6 +58,7 @@ struct HostState
     std::vector<std::uint8_t> msc_displaced;
     std::vector<real_type> msc_true_path, msc_geom_path, msc_alpha;
     std::vector<real_type> log_energy_key, log_energy_value;
+    std::vector<size_type> init_indices;
     std::vector<real_type> msc_range_init, msc_range_factor, msc_limit_min;
     std::vector<size_type> num_looping_steps;
     std::vector<std::uint32_t> rng_words;
@@ -118,6 +119,7 @@ struct HostState
         msc_displaced.assign(n, 0);
         msc_true_path.assign(n, 0);
         log_energy_key.assign(n, real_type(NAN));
+        init_indices.assign(n, 0);
         log_energy_value.assign(n, 0);
         msc_geom_path.assign(n, 0);
         msc_alpha.assign(n, 0);
@@ -181,6 +183,7 @@ struct HostState
         s.msc_displaced = msc_displaced.data();
         s.msc_true_path = msc_true_path.data();
         s.log_energy_key = log_energy_key.data();
+        s.init_indices = init_indices.data();
         s.log_energy_value = log_energy_value.data();
         s.msc_geom_path = msc_geom_path.data();
         s.msc_alpha = msc_alpha.data();

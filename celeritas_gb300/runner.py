@@ -44,11 +44,12 @@ import time
 import numpy as np
 
 #: TrackOrder names (src/celeritas/Types.cc:51-63) and the orders this build
-#: runs: none and the three action sorts
-TRACK_ORDER_NAMES = {"none": 0, "reindex_shuffle": 1, "reindex_status": 2,
-                     "reindex_particle_type": 3, "reindex_along_step_action": 5,
-                     "reindex_step_limit_action": 6, "reindex_both_action": 7}
-SUPPORTED_TRACK_ORDERS = (0, 5, 6, 7)
+#: runs: none, the charge partition and the three action sorts
+TRACK_ORDER_NAMES = {"none": 0, "init_charge": 1, "reindex_shuffle": 2,
+                     "reindex_status": 3, "reindex_particle_type": 4,
+                     "reindex_along_step_action": 5, "reindex_step_limit_action": 6,
+                     "reindex_both_action": 7}
+SUPPORTED_TRACK_ORDERS = (0, 1, 5, 6, 7)
 
 #: Keys renamed in the reference (old -> new, RunnerInputIO.json.cc:51-109)
 DEPRECATED_KEYS = {"hepmc3_filename": "event_file", "event_filename": "event_file",

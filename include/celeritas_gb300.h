@@ -92,10 +92,13 @@ void gbx_field_driver_options_default(gbx_field_driver_options* options);
  * knobs, app/celer-sim/RunnerInput.hh:41-141): a uniform magnetic field in
  * tesla (all zero: straight-line transport, along-step-general-linear;
  * otherwise along-step-uniform-msc), Urban multiple scattering for e-/e+,
- * and the track order. An action-sorting order registers the reference's
- * sort-tracks-post-step and/or sort-tracks-along-step actions (after
- * extend-from-secondaries, CoreParams.cc:258-283) and launches the sorted
- * actions over their ranges of action-sorted track slots. */
+ * and the track order (the reference's TrackOrder values: 0 none, 1
+ * init_charge, 5-7 the action sorts). An action-sorting order registers the
+ * reference's sort-tracks-post-step and/or sort-tracks-along-step actions
+ * (after extend-from-secondaries, CoreParams.cc:258-283) and launches the
+ * sorted actions over their ranges of action-sorted track slots;
+ * init_charge registers none and lets neutral and charged new tracks fill
+ * the two ends of the vacant slots (InitTracksExecutor.hh:71-108). */
 typedef struct
 {
     double field_tesla[3];

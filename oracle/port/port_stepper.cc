@@ -229,11 +229,33 @@ class PortStepper
         // initialize-tracks (start)
         {
             size_type num_new = std::min(c.num_vacancies, c.num_initializers);
-            for (size_type i = 0; i < num_new; ++i)
-                init_track(p, s, c, i);
+            if (partitions_by_charge(p.track_order))
+            {
+                // InitializeTracksAction with TrackOrder init_charge: the
+                // last num_new initializers' offsets, neutral ones first in
+                // a stable partition, then the initialization, then the
+                // parent slots cleared
+                size_type* idx = s.init_indices;
+                for (size_type i = 0; i < num_new; ++i)
+                    idx[i] = i;
+                TrackInitializer const* stencil
+                    = s.initializers + c.num_initializers - num_new;
+                std::stable_partition(idx, idx + num_new, [&](size_type i) {
+                    return is_neutral(p, stencil[i]);
+                });
+                for (size_type i = 0; i < num_new; ++i)
+                    init_track_charge_partitioned(p, s, c, num_new, i);
+            }
+            else
+            {
+                for (size_type i = 0; i < num_new; ++i)
+                    init_track(p, s, c, i);
+            }
             c.num_initializers -= num_new;
             c.num_vacancies -= num_new;
             c.num_active = n - c.num_vacancies;
+            if (partitions_by_charge(p.track_order))
+                std::fill(state_.parents.begin(), state_.parents.end(), invalid_id);
         }
         size_type const active = c.num_active;
         // pre-step (pre): thread 0 clears the secondary stack
@@ -288,7 +310,7 @@ class PortStepper
             {
                 bool v;
                 size_type cnt;
-                locate_alive(s, i, &v, &cnt);
+                locate_alive(s, i, &v, &cnt, !partitions_by_charge(p.track_order));
                 vacant[i] = v;
                 s.secondary_counts[i] = cnt;
             }

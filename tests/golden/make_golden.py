@@ -97,6 +97,18 @@ CASES = {
     "tracker_mix_e3000_n4": dict(geometry="tracker.geo", physics="cms", beam="eta",
                                  pdgs=[11, 22], energy=3000.0, num=4, slots=16384, seed=5,
                                  beam_seed=4, msc=True, field=[0.0, 0.0, 3.8]),
+    # Charge partition of new tracks' slots (TrackOrder init_charge = 1):
+    # neutral and charged tracks fill the two ends of the vacancies, and no
+    # secondary takes its dead parent's slot
+    "calo_initcharge_msc_field_e2000_n4": dict(pdg=11, energy=2000.0, num=4, slots=4096,
+                                               seed=3, msc=True, field=[1.0, 0.0, 0.0],
+                                               track_order=1),
+    "calo_initcharge_g100_n16": dict(pdg=22, energy=100.0, num=16, slots=1024, seed=7,
+                                     track_order=1),
+    "cms_initcharge_mix_e5000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22],
+                                        energy=5000.0, num=4, slots=16384, seed=2,
+                                        beam_seed=6, msc=True, field=[0.0, 0.0, 3.8],
+                                        track_order=1),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),
