@@ -207,7 +207,8 @@ def libm_evaluate(function: str, x, precision: str = "double") -> np.ndarray:
 EXPORTED_SYMBOLS = [name for name, _, _ in _PROTOTYPES]
 
 #: Supported TrackOrder policies (the reference's enumerator values)
-TRACK_ORDERS = {"none": 0, "init_charge": 1, "reindex_along_step_action": 5,
+TRACK_ORDERS = {"none": 0, "init_charge": 1, "reindex_shuffle": 2, "reindex_status": 3,
+                "reindex_particle_type": 4, "reindex_along_step_action": 5,
                 "reindex_step_limit_action": 6, "reindex_both_action": 7}
 
 #: GBX_STATIC_SCRATCH_MAX_SLOTS of the C header

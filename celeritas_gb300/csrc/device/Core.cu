@@ -4,6 +4,7 @@
 #include "../gbx/Random.hh"
 
 #include <algorithm>
+#include <random>
 #include <atomic>
 #include <cstring>
 #include <stdexcept>
@@ -140,6 +141,11 @@ void step_sort_along(CoreParams const&, CoreState& state, ActionId)
 {
     if (state.context().sort_enabled)
         launch_sort_tracks(state.context(), SortKey::along_step, state.stream());
+}
+void step_sort_start(CoreParams const&, CoreState& state, ActionId)
+{
+    if (state.context().sort_enabled)
+        launch_sort_tracks(state.context(), SortKey::start, state.stream());
 }
 void step_sort_post(CoreParams const&, CoreState& state, ActionId)
 {
@@ -294,6 +300,14 @@ void register_core_actions(ActionRegistry* reg,
             "sort tracks states",
             O::sort_pre,
             step_sort_along);
+    }
+    if (track_order == track_order_reindex_status)
+    {
+        add("sort-tracks-status", "sort tracks states", O::sort_start, step_sort_start);
+    }
+    if (track_order == track_order_reindex_particle_type)
+    {
+        add("sort-tracks-start", "sort tracks states", O::sort_start, step_sort_start);
     }
     // Step gathering: the pre-step detector lookup is fused into the
     // pre-step kernel; the post-step gather applies the calorimeter tally
@@ -599,6 +613,33 @@ CoreState::CoreState(CoreParams const& params,
         c.num_vacancies = n;
         GBX_CUDA(cudaMemcpyAsync(
             s.counters, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+        // reindex_shuffle: one random thread -> slot permutation for the
+        // whole run (CoreTrackData.cc:47-56), the reference's own: a
+        // Mersenne twister seeded with the number of slots shuffling the
+        // identity (TrackSlotUtils.cc:21-31), visited through the first
+        // offsets table's full range [offsets[0], offsets[num_bins])
+        std::vector<size_type> perm;
+        std::vector<size_type> offs;
+        if (params.host().scalars.track_order == track_order_reindex_shuffle)
+        {
+            perm.resize(n);
+            for (size_type i = 0; i < n; ++i)
+                perm[i] = i;
+            std::mt19937 gen{static_cast<unsigned int>(n)};
+            std::shuffle(perm.begin(), perm.end(), gen);
+            offs.assign(std::size_t(num_bins) + 1, n);
+            offs[0] = 0;
+            GBX_CUDA(cudaMemcpyAsync(s.track_slots,
+                                     perm.data(),
+                                     4 * std::size_t(n),
+                                     cudaMemcpyHostToDevice,
+                                     stream_));
+            GBX_CUDA(cudaMemcpyAsync(s.action_offsets,
+                                     offs.data(),
+                                     4 * offs.size(),
+                                     cudaMemcpyHostToDevice,
+                                     stream_));
+        }
         GBX_CUDA(cudaStreamSynchronize(stream_));
     }
 
@@ -616,6 +657,7 @@ CoreState::CoreState(CoreParams const& params,
     ctx_.sort.num_materials = num_materials;
     ctx_.sort.material_actions[0] = invalid_id;
     ctx_.sort.material_actions[1] = invalid_id;
+    ctx_.sort.track_order = params.host().scalars.track_order;
     ctx_.work_counter = static_cast<size_type*>(at(o_work));
     // Persistent charged along-step: on by default in the mixed-precision
     // build, where it outruns the one-thread-per-track kernel; in FP64 the
@@ -958,6 +1000,9 @@ std::vector<size_type> CoreState::sorted_action_sizes(int key) const
                              stream_));
     GBX_CUDA(cudaStreamSynchronize(stream_));
     std::vector<size_type> out(srt.num_actions);
+    unsigned int const order = ctx_.params.track_order;
+    if (!(key == 0 ? sorts_along_step(order) : sorts_step_limit(order)))
+        return std::vector<size_type>(srt.num_actions, 0);
     for (size_type a = 0; a < srt.num_actions; ++a)
     {
         size_type first = a;

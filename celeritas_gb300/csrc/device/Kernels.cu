@@ -668,6 +668,15 @@ __device__ __forceinline__ size_type sort_key(StateData const& s,
                                               size_type slot)
 {
     size_type const invalid_bin = srt.num_bins - 1;
+    if (key == SortKey::start)
+    {
+        // reindex_status: tracks that are not inactive first (IsNotInactive,
+        // TrackSortUtils.cc:71-79); reindex_particle_type: by particle ID
+        if (srt.track_order == track_order_reindex_status)
+            return s.status[slot] != status_inactive ? 0 : 1;
+        size_type const pid = s.particle_id[slot];
+        return pid < invalid_bin ? pid : invalid_bin;
+    }
     size_type a = (key == SortKey::along_step) ? s.along_step_action[slot]
                                                : s.post_step_action[slot];
     if (!(a < srt.num_actions))
@@ -921,11 +930,13 @@ __global__ __launch_bounds__(block_size) void interact_sorted_kernel(
     StateData s,
     size_type const* offsets,
     size_type first_bin,
-    size_type end_bin)
+    size_type end_bin,
+    size_type first_action,
+    size_type end_action)
 {
     for_each_sorted_slot(s, offsets, first_bin, end_bin, [&](size_type slot) {
         size_type a = s.post_step_action[slot];
-        if (a >= first_bin && a < end_bin)
+        if (a >= first_action && a < end_action)
             interact(p, s, slot, a);
     });
 }
@@ -957,6 +968,32 @@ inline size_type* sort_offsets(LaunchContext const& ctx, SortKey key)
 {
     std::size_t const table = std::size_t(ctx.sort.num_bins) + 1;
     return ctx.state.action_offsets + (key == SortKey::step_limit ? table : 0);
+}
+
+//! Offsets and bins through which a sorted-range kernel visits its tracks:
+//! the action's range of the key's sort; or, for the reindexing orders
+//! (shuffle, status, particle type), every slot through the thread -> slot
+//! permutation (the shuffle's is fixed when the state is made, the others'
+//! are this step's start sort, when it runs)
+struct SlotRange
+{
+    size_type const* offsets;
+    size_type first_bin;
+    size_type end_bin;
+};
+
+inline SlotRange
+slot_range(LaunchContext const& ctx, SortKey key, size_type first_bin, size_type end_bin)
+{
+    unsigned int const order = ctx.params.track_order;
+    if (reindexes_all(order))
+    {
+        bool const permuted = order == track_order_reindex_shuffle || ctx.sort_enabled;
+        return {permuted ? sort_offsets(ctx, SortKey::start) : nullptr, 0, ctx.sort.num_bins};
+    }
+    bool const sorts = key == SortKey::along_step ? sorts_along_step(order)
+                                                  : sorts_step_limit(order);
+    return {sorts && ctx.sort_enabled ? sort_offsets(ctx, key) : nullptr, first_bin, end_bin};
 }
 
 }  // namespace
@@ -1024,12 +1061,6 @@ void launch_pre_step(LaunchContext const& ctx, cudaStream_t stream)
         ctx.params, ctx.state);
 }
 
-//! Bin offsets of a sort key, or none (slots in their own order) when the
-//! track order does not sort by that key or sorting is switched off
-inline size_type const* key_offsets(LaunchContext const& ctx, SortKey key, bool sorts)
-{
-    return sorts && ctx.sort_enabled ? sort_offsets(ctx, key) : nullptr;
-}
 
 void launch_along_step(LaunchContext const& ctx,
                        size_type action,
@@ -1047,11 +1078,16 @@ void launch_along_step(LaunchContext const& ctx,
     // that a charged range well below the state size does not launch
     // thousands of blocks that find no track
     unsigned int const cnb = min_of(anb, max_of(1u, (1u << 19) / abs));
-    size_type const* offsets
-        = key_offsets(ctx, SortKey::along_step, sorts_along_step(p.track_order));
     size_type cfirst, cend, nfirst, nend;
     along_bins(ctx.sort, p.action_along_step, &cfirst, &cend);
     along_bins(ctx.sort, p.action_along_step_neutral, &nfirst, &nend);
+    SlotRange const cr = slot_range(ctx, SortKey::along_step, cfirst, cend);
+    SlotRange const nr = slot_range(ctx, SortKey::along_step, nfirst, nend);
+    size_type const* offsets = cr.offsets;
+    cfirst = cr.first_bin;
+    cend = cr.end_bin;
+    nfirst = nr.first_bin;
+    nend = nr.end_bin;
     if (action == invalid_id || action == p.action_along_step)
     {
         bool const large = abs > static_cast<unsigned int>(block_size);
@@ -1101,34 +1137,27 @@ void launch_interact(LaunchContext const& ctx, size_type action, cudaStream_t st
         first = p.model_to_action;
         end = p.model_to_action + p.num_models;
     }
+    SlotRange const r = slot_range(ctx, SortKey::step_limit, first, end);
     interact_sorted_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
-        p,
-        ctx.state,
-        key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
-        first,
-        end);
+        p, ctx.state, r.offsets, r.first_bin, r.end_bin, first, end);
 }
 
 void launch_boundary(LaunchContext const& ctx, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
+    SlotRange const r
+        = slot_range(ctx, SortKey::step_limit, p.action_boundary, p.action_boundary + 1);
     boundary_sorted_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
-        p,
-        ctx.state,
-        key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
-        p.action_boundary,
-        p.action_boundary + 1);
+        p, ctx.state, r.offsets, r.first_bin, r.end_bin);
 }
 
 void launch_tracking_cut(LaunchContext const& ctx, cudaStream_t stream)
 {
     ParamsData const& p = ctx.params;
+    SlotRange const r = slot_range(
+        ctx, SortKey::step_limit, p.action_tracking_cut, p.action_tracking_cut + 1);
     tracking_cut_sorted_kernel<<<ctx.range_blocks, block_size, 0, stream>>>(
-        p,
-        ctx.state,
-        key_offsets(ctx, SortKey::step_limit, sorts_step_limit(p.track_order)),
-        p.action_tracking_cut,
-        p.action_tracking_cut + 1);
+        p, ctx.state, r.offsets, r.first_bin, r.end_bin);
 }
 
 void launch_calo_tally(LaunchContext const& ctx, cudaStream_t stream)

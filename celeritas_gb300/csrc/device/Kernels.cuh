@@ -36,6 +36,9 @@ struct SortScratch
     size_type num_blocks;
     size_type num_actions;
     size_type num_materials;
+    //! TrackOrder of the parameters (the start sort's key: status or
+    //! particle type)
+    unsigned int track_order;
     //! Along-step sort by material within up to two actions (ascending IDs,
     //! invalid_id where unused): such an action's tracks take num_materials
     //! bins by their material, and the bins of later actions shift by
@@ -76,6 +79,7 @@ enum class SortKey
 {
     along_step,  //!< along_step_action (reindex_along_step_action)
     step_limit,  //!< post_step_action (reindex_step_limit_action)
+    start,  //!< status or particle type (reindex_status, _particle_type)
 };
 
 //! Error flags written by device code

@@ -33,12 +33,16 @@ GBX_FORCEINLINE bool is_track_valid(std::uint8_t s)
 }
 
 //! Track ordering policies (src/celeritas/Types.hh:151-171); the values
-//! are the reference's enumerators. Built: 'none', the charge partition of
-//! new tracks' slots and the action sorts.
+//! are the reference's enumerators, all built: 'none', the charge partition
+//! of new tracks' slots, the thread -> slot reindexings (shuffle, status,
+//! particle type) and the action sorts.
 enum TrackOrder : unsigned int
 {
     track_order_none = 0,
     track_order_init_charge = 1,
+    track_order_reindex_shuffle = 2,
+    track_order_reindex_status = 3,
+    track_order_reindex_particle_type = 4,
     track_order_reindex_along_step_action = 5,
     track_order_reindex_step_limit_action = 6,
     track_order_reindex_both_action = 7,
@@ -54,6 +58,14 @@ GBX_FORCEINLINE bool sorts_step_limit(unsigned int order)
 {
     return order == track_order_reindex_step_limit_action
            || order == track_order_reindex_both_action;
+}
+
+//! Whether the kernels visit every slot through a thread -> slot
+//! permutation without action ranges (shuffle, status, particle type)
+GBX_FORCEINLINE bool reindexes_all(unsigned int order)
+{
+    return order == track_order_reindex_shuffle || order == track_order_reindex_status
+           || order == track_order_reindex_particle_type;
 }
 
 //! Whether new tracks' slots are partitioned by charge (init_charge)
@@ -486,6 +498,7 @@ struct ParamsData
     unsigned int track_order;
     size_type action_sort_along;
     size_type action_sort_post;
+    size_type action_sort_start;  //!< sort-tracks-status or -start
     size_type num_actions;
 
     GeoParams geo;

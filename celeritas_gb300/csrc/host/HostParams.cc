@@ -284,13 +284,23 @@ void Builder::build_actions()
     // Optional track-sorting actions (CoreParams.cc:258-283): the step-limit
     // sort is registered before the along-step sort
     s.track_order = opts_.track_order;
-    s.action_sort_along = s.action_sort_post = invalid_id;
+    s.action_sort_along = s.action_sort_post = s.action_sort_start = invalid_id;
     switch (opts_.track_order)
     {
         case track_order_none:
         case track_order_init_charge:
+        case track_order_reindex_shuffle:
             // No sort action: the charge partition is part of the track
-            // initialization (CoreParams.cc:264-269)
+            // initialization, the shuffle is done once with the state
+            // (CoreParams.cc:264-269, CoreTrackData.cc:47-56)
+            break;
+        case track_order_reindex_status:
+            s.action_sort_start = hp_.action_labels.size();
+            hp_.action_labels.push_back("sort-tracks-status");
+            break;
+        case track_order_reindex_particle_type:
+            s.action_sort_start = hp_.action_labels.size();
+            hp_.action_labels.push_back("sort-tracks-start");
             break;
         case track_order_reindex_along_step_action:
             s.action_sort_along = hp_.action_labels.size();
@@ -308,7 +318,7 @@ void Builder::build_actions()
             break;
         default:
             throw std::runtime_error("track order " + std::to_string(opts_.track_order)
-                                     + " is not supported (0, 1, 5, 6 or 7)");
+                                     + " is not a TrackOrder (0-7)");
     }
     hp_.action_labels.push_back("step-gather-pre");
     hp_.action_labels.push_back("step-gather-post");

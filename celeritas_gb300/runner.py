@@ -43,13 +43,12 @@ import time
 
 import numpy as np
 
-#: TrackOrder names (src/celeritas/Types.cc:51-63) and the orders this build
-#: runs: none, the charge partition and the three action sorts
+#: TrackOrder names (src/celeritas/Types.cc:51-63); this build runs them all
 TRACK_ORDER_NAMES = {"none": 0, "init_charge": 1, "reindex_shuffle": 2,
                      "reindex_status": 3, "reindex_particle_type": 4,
                      "reindex_along_step_action": 5, "reindex_step_limit_action": 6,
                      "reindex_both_action": 7}
-SUPPORTED_TRACK_ORDERS = (0, 1, 5, 6, 7)
+SUPPORTED_TRACK_ORDERS = tuple(range(8))
 
 #: Keys renamed in the reference (old -> new, RunnerInputIO.json.cc:51-109)
 DEPRECATED_KEYS = {"hepmc3_filename": "event_file", "event_filename": "event_file",
@@ -169,11 +168,8 @@ class RunnerInput:
             raise RunnerInputError("'step_limiter' is not supported by the GB300 "
                                    "stepping loop")
         order = TRACK_ORDER_NAMES.get(self.track_order)
-        if order is None:
-            raise RunnerInputError(f"unknown track order '{self.track_order}'")
-        if order not in SUPPORTED_TRACK_ORDERS:
-            raise RunnerInputError(f"track order '{self.track_order}' is not supported "
-                                   "(none or an action sort)")
+        if order is None or order not in SUPPORTED_TRACK_ORDERS:
+            raise RunnerInputError(f"unknown track order '{self.track_order}' (track_order)")
         if self.precision not in ("double", "mixed"):
             raise RunnerInputError("precision must be 'double' or 'mixed'")
         if self.rz_field_file and any(self.field):

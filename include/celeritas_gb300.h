@@ -93,7 +93,10 @@ void gbx_field_driver_options_default(gbx_field_driver_options* options);
  * tesla (all zero: straight-line transport, along-step-general-linear;
  * otherwise along-step-uniform-msc), Urban multiple scattering for e-/e+,
  * and the track order (the reference's TrackOrder values: 0 none, 1
- * init_charge, 5-7 the action sorts). An action-sorting order registers the
+ * init_charge, 2 reindex_shuffle, 3 reindex_status, 4
+ * reindex_particle_type, 5-7 the action sorts). The reindexing orders 2-4
+ * change which thread visits which slot, not the results; 3 and 4 register
+ * sort-tracks-status and sort-tracks-start. An action-sorting order registers the
  * reference's sort-tracks-post-step and/or sort-tracks-along-step actions
  * (after extend-from-secondaries, CoreParams.cc:258-283) and launches the
  * sorted actions over their ranges of action-sorted track slots;

@@ -109,6 +109,17 @@ CASES = {
                                         energy=5000.0, num=4, slots=16384, seed=2,
                                         beam_seed=6, msc=True, field=[0.0, 0.0, 3.8],
                                         track_order=1),
+    # Thread -> slot reindexing orders (reindex_shuffle = 2, reindex_status = 3,
+    # reindex_particle_type = 4): the visiting order changes, the physics
+    # does not (the same counters as the unsorted runs of the same problems)
+    "calo_shuffle_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=65536, seed=0,
+                                      msc=True, track_order=2),
+    "calo_status_g100_n16": dict(pdg=22, energy=100.0, num=16, slots=4096, seed=7,
+                                 track_order=3),
+    "cms_particle_mix_e10000_n4": dict(geometry="cms", beam="eta", pdgs=[11, 22],
+                                       energy=10000.0, num=4, slots=65536, seed=0,
+                                       beam_seed=1, msc=True, field=[0.0, 0.0, 3.8],
+                                       track_order=4),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),

@@ -60,7 +60,7 @@ def test_required_keys(key):
     ({"primary_options": {"pdg": 11}}, "but not both"),
     ({"field_options": {"delta_chord": 0.1}}, "without providing 'field'"),
     ({"num_track_slots": 0}, "must be positive"),
-    ({"track_order": "reindex_shuffle"}, "not supported"),
+    ({"track_order": "reindex_randomly"}, "track_order"),
     ({"track_order": "sideways"}, "unknown track order"),
     ({"step_limiter": 1.0}, "step_limiter"),
     ({"physics_options": {}}, "not supported"),
