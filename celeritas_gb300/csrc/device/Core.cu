@@ -257,7 +257,7 @@ void register_core_actions(ActionRegistry* reg,
         step_model);
     implicit("physics-failure",
              "mark a track that failed to sample an interaction");
-    // Along-step action registered by the driver
+    // The along-step action of this problem: field map, uniform field or none
     add(rz_map          ? "along-step-rzmap-msc"
         : uniform_field ? "along-step-uniform-msc"
                         : "along-step-general-linear",

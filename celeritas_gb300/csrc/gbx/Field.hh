@@ -263,7 +263,7 @@ GBX_FUNCTION FieldStepperResult dormand_prince_step_fp64(Equation const& rhs,
 //! of the FP32 stage derivatives) and the chord distance (from the FP32
 //! increments to the end and to Shampine's midpoint) are formed in FP32:
 //! their inputs carry FP32 rounding, which FP64 arithmetic on them would not
-//! remove. The driver takes the error norms and the acceptance test in FP64.
+//! remove. The field driver takes the error norms and the acceptance test in FP64.
 GBX_FUNCTION FieldStepperResult dormand_prince_step_mixed(UniformFieldEquation const& rhs,
                                                           double step,
                                                           OdeState const& beg_state)
