@@ -20,7 +20,7 @@ JSON line on rank 0:
   reference's own host stepper), clocks, e2e, and the c2 calorimeter line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c3]
-                  [--precision mixed|double] [--track-order 0|5|6|7] [--no-fp64]
+                  [--precision mixed|double] [--track-order 0-7] [--no-fp64]
   python bench.py --impl reference ...   # CPU path of the reference loop
 
 Timing: W untimed warm-up steps, then K timed steps; each timed step is
@@ -1188,7 +1188,8 @@ def main():
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--precision", default="mixed", choices=["mixed", "double"])
     parser.add_argument("--track-order", type=int, default=7,
-                        help="TrackOrder: 0 none, 5/6/7 action sorts")
+                        help="TrackOrder (0-7): 0 none, 1 init_charge, 2-4 reindex "
+                             "shuffle/status/particle type, 5-7 action sorts")
     parser.add_argument("--no-fp64", action="store_true",
                         help="skip the FP64 comparison run")
     parser.add_argument("--served-rates", default="30,200",
