@@ -36,6 +36,14 @@ def test_python_bindings_cover_header():
     assert sorted(gb.EXPORTED_SYMBOLS) == declared_functions()
 
 
+def test_integration_guide_maps_every_entry_point():
+    """The integration guide names, for every declared entry point, the
+    reference call it replaces."""
+    guide = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    missing = [n for n in declared_functions() if n not in guide]
+    assert not missing, missing
+
+
 def test_errors_are_reported_without_gpu(built_lib):
     """Without a device, creation fails loudly with a message (no CPU fallback)."""
     gb.load_library(built_lib)
