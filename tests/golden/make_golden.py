@@ -120,6 +120,16 @@ CASES = {
                                        energy=10000.0, num=4, slots=65536, seed=0,
                                        beam_seed=1, msc=True, field=[0.0, 0.0, 3.8],
                                        track_order=4),
+    # Edge cases at the bottom of the energy range: electrons below the
+    # 1 keV tracking cut (killed in their first along-step), positrons that
+    # stop and annihilate at rest, photons just above the pair threshold,
+    # and a log-uniform 1 keV-10 MeV e-/gamma mixture in the CMS-like field
+    "calo_e0.0005_n64": dict(pdg=11, energy=0.0005, num=64, slots=256, seed=1),
+    "calo_ep0.01_n64": dict(pdg=-11, energy=0.01, num=64, slots=256, seed=2, msc=True),
+    "calo_g1.1_n64": dict(pdg=22, energy=1.1, num=64, slots=1024, seed=3),
+    "cms_lowe_mix_n64": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=0.001,
+                             emax=10.0, num=64, slots=1024, seed=4, beam_seed=11,
+                             msc=True, field=[0.0, 0.0, 3.8]),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),
