@@ -177,6 +177,69 @@ def run_reference(physics: str, primaries_txt: str, slots: int, seed: int = 0,
     return parse_run_output(res.stdout)
 
 
+#: Fields of an 'int' line of the 'interact' mode, after the input index
+#: and the model label
+INTERACT_FIELDS = ("st", "act", "mat", "E", "dir", "edep", "nsec", "rng")
+
+
+def write_interaction_inputs(path: str, inputs) -> None:
+    """Write interaction inputs, one per line: model label, PDG, energy
+    [MeV], position (3) [cm], direction (3), element component."""
+    with open(path, "w") as f:
+        for model, pdg, e, pos, d, elcomp in inputs:
+            f.write(f"{model} {int(pdg)} {float(e)!r} "
+                    + " ".join(repr(float(v)) for v in (*pos, *d))
+                    + f" {int(elcomp)}\n")
+
+
+def parse_interact_output(text: str) -> list[dict]:
+    """Parse the 'int' and 'sec' lines of the 'interact' mode: per input, the
+    track after its interaction (status, step-limit action, material,
+    energy, direction, deposition, random state) and its secondaries (PDG,
+    energy, direction; PDG 0 for one killed by a cutoff)."""
+    out: list[dict] = []
+
+    def vec(t):
+        return [float(v) for v in t.strip("()").split(",")]
+
+    for line in text.splitlines():
+        tok = line.split()
+        if not tok:
+            continue
+        if tok[0] == "int":
+            kv = dict(t.split("=", 1) for t in tok[3:])
+            assert int(tok[1]) == len(out)
+            out.append({"model": tok[2], "status": int(kv["st"]),
+                        "action": int(kv["act"]), "material": int(kv["mat"]),
+                        "energy": float(kv["E"]), "direction": vec(kv["dir"]),
+                        "edep": float(kv["edep"]), "num_secondaries": int(kv["nsec"]),
+                        "rng": [int(w) for w in kv["rng"].split(",")],
+                        "secondaries": []})
+        elif tok[0] == "sec":
+            kv = dict(t.split("=", 1) for t in tok[3:])
+            out[int(tok[1])]["secondaries"].append(
+                {"pdg": int(kv["pdg"]), "energy": float(kv["E"]),
+                 "direction": vec(kv["dir"])})
+    return out
+
+
+def run_interactions(program: str, physics: str, geometry: str, inputs_txt: str,
+                     seed: int = 0, extra=(), libm: str = "pinned") -> list[dict]:
+    """One interaction per input through the reference's model actions
+    (program "reference", requires build_reference) or the restatement's
+    (program "port"), with the host C library's or correctly rounded
+    elementary functions."""
+    if program == "reference":
+        exe = REF_BIN if libm == "system" else REF_PINNED_BIN
+    else:
+        exe = build_port(libm=libm)
+    cmd = [exe, "interact", physics, geometry, inputs_txt, str(seed), *extra]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"{program} interact failed: " + res.stderr[-2000:])
+    return parse_interact_output(res.stdout)
+
+
 def port_libm(function: str, x, libm: str = "pinned"):
     """The restatement's FP64 elementary function 'function' (the GB300
     build's correctly rounded one, or the host C library's) on the host, for

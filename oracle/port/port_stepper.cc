@@ -20,6 +20,8 @@
 //                    [--steps N] [--quiet] [--hits]
 //   port_stepper bench <physics.txt> <geometry> <primaries.txt> <slots> <seed>
 //                    [--threads T] [--event-tallies FILE] [physics options]
+//   port_stepper interact <physics.txt> <geometry> <inputs.txt> <seed>
+//                    [physics options]
 //   port_stepper libm <exp|log|sin|cos|tanh|log1p|expm1|cbrt> < hex doubles
 #include <algorithm>
 #include <array>
@@ -98,6 +100,17 @@ class PortStepper
         return this->step(true);
     }
     StepCounts operator()() { return this->step(false); }
+
+    //! Insert primaries and run the first actions of a step (through
+    //! pre-step), leaving every track ready for its step-limit action
+    void prepare(std::vector<TrackInitializer> const& primaries)
+    {
+        state_.primaries = primaries;
+        this->begin_step(true);
+    }
+    StateData view() { return state_.view(); }
+    ParamsData const& params() const { return params_; }
+    std::vector<std::string> const& action_labels() const { return action_labels_; }
 
     std::vector<double> const& edep() const { return state_.calo_edep; }
 
@@ -206,7 +219,10 @@ class PortStepper
         }
     }
 
-    StepCounts step(bool with_primaries)
+    //! The actions of a step up to and including pre-step:
+    //! extend-from-primaries, initialize-tracks, pre-step. Returns the
+    //! number of active tracks.
+    size_type begin_step(bool with_primaries)
     {
         ParamsData const& p = params_;
         StateData s = state_.view();
@@ -257,11 +273,20 @@ class PortStepper
             if (partitions_by_charge(p.track_order))
                 std::fill(state_.parents.begin(), state_.parents.end(), invalid_id);
         }
-        size_type const active = c.num_active;
         // pre-step (pre): thread 0 clears the secondary stack
         c.secondary_stack_size = 0;
         for (size_type i = 0; i < n; ++i)
             pre_step(p, s, i);
+        return c.num_active;
+    }
+
+    StepCounts step(bool with_primaries)
+    {
+        ParamsData const& p = params_;
+        StateData s = state_.view();
+        Counters& c = state_.counters;
+        size_type const n = s.size;
+        size_type const active = this->begin_step(with_primaries);
         // step-gather-pre (user_pre)
         for (size_type i = 0; i < n; ++i)
             gather_pre(p, s, i);
@@ -432,6 +457,115 @@ std::vector<TrackInitializer> load_primaries(std::string const& path)
         result.push_back(ti);
     }
     return result;
+}
+
+//! One interaction per input, the GB300 path's model code on tracks that its
+//! own first actions prepared, as the reference harness's 'interact' mode
+//! does with the reference's model actions: each input line (model label,
+//! PDG, energy [MeV], position [cm], direction, element component) becomes a
+//! primary of its own event; extend-from-primaries, initialize-tracks and
+//! pre-step run; each track's step-limit action and element component are
+//! set as physics-discrete-select would (PhysicsStepUtils.hh:253-308); the
+//! named models run in action-ID order over the slots.
+int interact_inputs(int argc, char** argv)
+{
+    if (argc < 6)
+    {
+        std::cerr << "usage: interact <physics> <geometry> <inputs> <seed> "
+                     "[physics options]\n";
+        return 2;
+    }
+    std::string phys = argv[2], geo = argv[3], in_path = argv[4];
+    unsigned int seed = std::stoul(argv[5]);
+    HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
+
+    std::ifstream in(in_path);
+    if (!in)
+        throw std::runtime_error("cannot open " + in_path);
+    std::vector<TrackInitializer> primaries;
+    std::vector<std::string> models;
+    std::vector<size_type> elcomps;
+    std::string model;
+    int pdg;
+    double e, x, y, z, dx, dy, dz;
+    size_type elcomp;
+    while (in >> model >> pdg >> e >> x >> y >> z >> dx >> dy >> dz >> elcomp)
+    {
+        TrackInitializer ti{};
+        ti.particle_id = pdg == 11 ? 0 : (pdg == -11 ? 1 : 2);
+        ti.energy = e;
+        ti.pos = {x, y, z};
+        ti.dir = {dx, dy, dz};
+        ti.time = 0;
+        ti.event_id = static_cast<size_type>(primaries.size());
+        primaries.push_back(ti);
+        models.push_back(model);
+        elcomps.push_back(elcomp);
+    }
+    if (primaries.empty())
+        throw std::runtime_error("no inputs in " + in_path);
+
+    size_type const n = static_cast<size_type>(primaries.size());
+    PortStepper stepper(hp, n, seed, n);
+    stepper.prepare(primaries);
+    ParamsData const& p = stepper.params();
+    StateData s = stepper.view();
+    auto const& labels = stepper.action_labels();
+    std::vector<size_type> to_run;
+    std::vector<size_type> slot_of(n);
+    for (size_type i = 0; i < n; ++i)
+    {
+        if (s.status[i] != status_alive)
+            throw std::runtime_error("track slot " + std::to_string(i)
+                                     + " is not alive after pre-step");
+        size_type const idx = s.event_id[i];
+        auto found = std::find(labels.begin(), labels.end(), models[idx]);
+        if (found == labels.end())
+            throw std::runtime_error("no action '" + models[idx] + "'");
+        size_type const aid = static_cast<size_type>(found - labels.begin());
+        s.post_step_action[i] = aid;
+        s.element[i] = elcomps[idx];
+        slot_of[idx] = i;
+        if (std::find(to_run.begin(), to_run.end(), aid) == to_run.end())
+            to_run.push_back(aid);
+    }
+    std::sort(to_run.begin(), to_run.end());
+    for (size_type aid : to_run)
+    {
+        for (size_type i = 0; i < n; ++i)
+            interact(p, s, i, aid);
+    }
+    for (size_type idx = 0; idx < n; ++idx)
+    {
+        size_type const i = slot_of[idx];
+        size_type const nsec = s.secondaries_count[i];
+        std::printf("int %u %s st=%d act=%u mat=%u E=%.17g dir=(%.17g,%.17g,%.17g) "
+                    "edep=%.17g nsec=%u rng=%u,%u,%u,%u,%u,%u\n",
+                    idx,
+                    models[idx].c_str(),
+                    int(s.status[i]),
+                    s.post_step_action[i],
+                    s.material[i],
+                    double(s.energy[i]),
+                    s.dir[0][i], s.dir[1][i], s.dir[2][i],
+                    double(s.energy_deposition[i]),
+                    nsec,
+                    s.rng.s[0][i], s.rng.s[1][i], s.rng.s[2][i],
+                    s.rng.s[3][i], s.rng.s[4][i], s.rng.weyl[i]);
+        for (size_type k = 0; k < nsec; ++k)
+        {
+            Secondary const& sec = s.secondaries[s.secondaries_offset[i] + k];
+            std::printf("sec %u %u pdg=%d E=%.17g dir=(%.17g,%.17g,%.17g)\n",
+                        idx,
+                        k,
+                        sec.particle_id == invalid_id ? 0 : p.particles[sec.particle_id].pdg,
+                        double(sec.energy),
+                        double(sec.direction[0]),
+                        double(sec.direction[1]),
+                        double(sec.direction[2]));
+        }
+    }
+    return 0;
 }
 
 int run(int argc, char** argv)
@@ -771,6 +905,8 @@ int main(int argc, char** argv)
             return run(argc, argv);
         if (mode == "bench")
             return bench(argc, argv);
+        if (mode == "interact")
+            return interact_inputs(argc, argv);
         if (mode == "geo-rays")
             return geo_rays(argc, argv);
         if (mode == "libm" && argc >= 3)

@@ -18,6 +18,7 @@
 //   ref_harness bench <physics.txt> <geometry> <primaries.txt> <num_slots>
 //               <seed> [--threads T] [--field Bx By Bz] [--msc] [--max-steps N]
 //   ref_harness geo <physics.txt> <geometry>
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -72,6 +73,7 @@
 #include "celeritas/phys/Primary.hh"
 #include "celeritas/phys/ProcessBuilder.hh"
 #include "celeritas/random/RngParams.hh"
+#include "celeritas/track/ExtendFromPrimariesAction.hh"
 #include "celeritas/track/SimParams.hh"
 #include "celeritas/track/TrackInitParams.hh"
 #include "celeritas/user/DetectorSteps.hh"
@@ -1105,6 +1107,163 @@ int run(int argc, char** argv)
     return 0;
 }
 
+//! One interaction per input, through the reference's own model actions.
+//! Each input line (model label, PDG, energy [MeV], position [cm],
+//! direction, element component) becomes a primary of its own event. The
+//! step actions up to and including pre-step (extend-from-primaries,
+//! initialize-tracks, pre-step: ActionSequence.cc:77-138) prepare the tracks
+//! as in a step; then each track's step-limit action and element component
+//! are set as physics-discrete-select would (PhysicsStepUtils.hh:253-308)
+//! and only the named models run (their InteractionApplier executors).
+//! Prints per input the track after the interaction, its random state and
+//! its secondaries.
+int interact(int argc, char** argv)
+{
+    if (argc < 6)
+    {
+        std::cerr << "usage: interact <physics> <geometry> <inputs> <seed> "
+                     "[--msc] [--brem-combined]\n";
+        return 2;
+    }
+    std::string phys_path = argv[2], geo_name = argv[3], in_path = argv[4];
+    unsigned int seed = std::stoul(argv[5]);
+    bool msc = false;
+    bool brem_combined = false;
+    for (int i = 6; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--msc")
+            msc = true;
+        else if (a == "--brem-combined")
+            brem_combined = true;
+    }
+    KvFile kv(phys_path);
+    ImportData imported = load_import(kv, msc);
+    Problem prob = build_problem(imported,
+                                 geo_name,
+                                 seed,
+                                 Real3{0, 0, 0},
+                                 msc,
+                                 TrackOrder::none,
+                                 false,
+                                 "",
+                                 1,
+                                 brem_combined);
+    CoreParams const& core = *prob.core;
+    ParticleParams const& particles = *core.particle();
+
+    std::ifstream in(in_path);
+    CELER_VALIDATE(in, << "cannot open " << in_path);
+    std::vector<Primary> primaries;
+    std::vector<std::string> models;
+    std::vector<unsigned int> elcomps;
+    std::string model;
+    int pdg;
+    double e, x, y, z, dx, dy, dz;
+    unsigned int elcomp;
+    while (in >> model >> pdg >> e >> x >> y >> z >> dx >> dy >> dz >> elcomp)
+    {
+        Primary p;
+        p.particle_id = particles.find(PDGNumber{pdg});
+        CELER_VALIDATE(p.particle_id, << "unknown PDG " << pdg);
+        p.energy = units::MevEnergy{e};
+        p.position = {x, y, z};
+        p.direction = {dx, dy, dz};
+        p.time = 0;
+        p.event_id = EventId{static_cast<size_type>(primaries.size())};
+        primaries.push_back(p);
+        models.push_back(model);
+        elcomps.push_back(elcomp);
+    }
+    CELER_VALIDATE(!primaries.empty(), << "no inputs in " << in_path);
+
+    StepperInput sinp;
+    sinp.params = prob.core;
+    sinp.stream_id = StreamId{0};
+    sinp.num_track_slots = static_cast<size_type>(primaries.size());
+    Stepper<MemSpace::host> step(std::move(sinp));
+    auto& state = dynamic_cast<CoreState<MemSpace::host>&>(*step.sp_state());
+    ExtendFromPrimariesAction::find_action(core)->insert(
+        core, state, make_span(primaries));
+    state.counters().num_generated = 0;
+    for (auto const& action : step.actions().actions().step())
+    {
+        if (action->order() > StepActionOrder::pre)
+            break;
+        action->step(core, state);
+    }
+
+    auto const& reg = *core.action_reg();
+    auto const& pref = core.ref<MemSpace::host>();
+    auto const& sref = state.ref();
+    std::vector<ActionId> to_run;
+    for (size_type i = 0; i < state.size(); ++i)
+    {
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        auto sim = track.make_sim_view();
+        CELER_VALIDATE(sim.status() == TrackStatus::alive,
+                       << "track slot " << i << " is not alive after pre-step");
+        size_type const idx = sim.event_id().unchecked_get();
+        ActionId aid = reg.find_action(models[idx]);
+        CELER_VALIDATE(aid, << "no action '" << models[idx] << "'");
+        sim.post_step_action(aid);
+        track.make_physics_step_view().element(ElementComponentId{elcomps[idx]});
+        if (std::find(to_run.begin(), to_run.end(), aid) == to_run.end())
+            to_run.push_back(aid);
+    }
+    std::sort(to_run.begin(), to_run.end());
+    for (ActionId aid : to_run)
+    {
+        auto const* action
+            = dynamic_cast<CoreStepActionInterface const*>(reg.action(aid).get());
+        CELER_VALIDATE(action, << "action " << aid.unchecked_get() << " does not step");
+        action->step(core, state);
+    }
+
+    std::vector<size_type> slot_of(primaries.size());
+    for (size_type i = 0; i < state.size(); ++i)
+    {
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        slot_of[track.make_sim_view().event_id().unchecked_get()] = i;
+    }
+    for (size_type idx = 0; idx < slot_of.size(); ++idx)
+    {
+        size_type const i = slot_of[idx];
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        auto sim = track.make_sim_view();
+        auto par = track.make_particle_view();
+        auto geo = track.make_geo_view();
+        auto pstep = track.make_physics_step_view();
+        auto const& dir = geo.dir();
+        auto const& r = sref.rng.state[TrackSlotId{i}];
+        auto secondaries = pstep.secondaries();
+        std::printf("int %u %s st=%d act=%u mat=%u E=%.17g dir=(%.17g,%.17g,%.17g) "
+                    "edep=%.17g nsec=%u rng=%u,%u,%u,%u,%u,%u\n",
+                    idx,
+                    models[idx].c_str(),
+                    static_cast<int>(sim.status()),
+                    sim.post_step_action().unchecked_get(),
+                    track.make_material_view().material_id().unchecked_get(),
+                    par.energy().value(),
+                    dir[0], dir[1], dir[2],
+                    pstep.energy_deposition().value(),
+                    static_cast<unsigned>(secondaries.size()),
+                    r.xorstate[0], r.xorstate[1], r.xorstate[2],
+                    r.xorstate[3], r.xorstate[4], r.weylstate);
+        for (size_type k = 0; k < secondaries.size(); ++k)
+        {
+            Secondary const& sec = secondaries[k];
+            std::printf("sec %u %u pdg=%d E=%.17g dir=(%.17g,%.17g,%.17g)\n",
+                        idx,
+                        k,
+                        sec ? particles.id_to_pdg(sec.particle_id).get() : 0,
+                        sec.energy.value(),
+                        sec.direction[0], sec.direction[1], sec.direction[2]);
+        }
+    }
+    return 0;
+}
+
 //! Timed CPU run of the reference's host stepper: events distributed over
 //! threads, one Stepper<host> per thread on its own stream, each event
 //! transported to completion (celer-sim with CELERITAS_OPENMP=event,
@@ -1318,6 +1477,8 @@ int main(int argc, char** argv)
             return dump_geo(argc, argv);
         if (mode == "bench")
             return bench(argc, argv);
+        if (mode == "interact")
+            return interact(argc, argv);
     }
     catch (std::exception const& e)
     {

@@ -9,9 +9,13 @@ DetectorStepOutput of every step (the first records in full, per-step counts
 and column sums). Also records the ORANGE surface data of the calorimeter
 geometry and reseeded XORWOW states.
 
+Also records, per interaction case, one interaction per input through the
+reference's own model actions (the harness's 'interact' mode).
+
 Usage (where the reference sources are present):
     python tests/golden/make_golden.py [--reference /path/to/reference]
     python tests/golden/make_golden.py --libm pinned   # fixtures under pinned/
+    python tests/golden/make_golden.py --cases --hit-cases --interactions interact_cms
 
 With --libm pinned the reference runs with correctly rounded exp, log, sin,
 cos, tanh, log1p, expm1 and cbrt (oracle/ref/pinned_libm.cc), the elementary
@@ -146,6 +150,81 @@ HIT_CASES = {
                                   field=[0.0, 0.0, 3.8]),
 }
 HIT_RECORDS = 150
+
+# Interactor parity: one interaction per input, through the reference's own
+# model actions (the 'interact' mode of the harness), on tracks that its
+# extend-from-primaries, initialize-tracks and pre-step prepared; inputs span
+# each model's energy range, every element component of each material and
+# isotropic directions. Per case: geometry, physics, seed, combined brems,
+# and the material points (position, number of element components)
+INTERACTION_CASES = {
+    "interact_calo": dict(geometry="calo", seed=0,
+                          points=[((0.0, 0.0, 0.1), 1), ((0.0, 0.0, 0.5), 1)]),
+    "interact_cms": dict(geometry="cms", seed=1,
+                         points=[((4.01, 0.0, 0.0), 1), ((140.0, 0.0, 0.0), 3),
+                                 ((182.0, 0.0, 0.0), 2), ((185.2, 0.0, 0.0), 2)]),
+    "interact_calo_brcomb": dict(geometry="calo", seed=2, brem_combined=True,
+                                 points=[((0.0, 0.0, 0.1), 1), ((0.0, 0.0, 0.5), 1)]),
+}
+# Energies [MeV] per model and particle, inside each model's range (the
+# electron production cut is at most 1.02 MeV here, so Moller scattering
+# needs more than 2.04 MeV)
+INTERACTION_ENERGIES = {
+    ("scat-klein-nishina", 22): [0.005, 0.05, 0.5, 5.0, 50.0, 5e3, 5e5],
+    ("photoel-livermore", 22): [0.002, 0.02, 0.087, 0.089, 0.3, 3.0],
+    ("conv-bethe-heitler", 22): [1.1, 2.0, 10.0, 100.0, 1e4, 8e4],
+    ("brems-sb", 11): [0.1, 1.0, 10.0, 100.0, 999.0],
+    ("brems-sb", -11): [0.1, 1.0, 10.0, 100.0, 999.0],
+    ("brems-rel", 11): [1001.0, 1e4, 1e5, 1e6],
+    ("brems-rel", -11): [1001.0, 1e4, 1e5, 1e6],
+    ("ioni-moller-bhabha", 11): [5.0, 50.0, 500.0, 5e4],
+    ("ioni-moller-bhabha", -11): [5.0, 50.0, 500.0, 5e4],
+    ("annihil-2-gamma", -11): [0.01, 1.0, 100.0, 1e4],
+}
+COMBINED_ENERGIES = [0.1, 10.0, 500.0, 999.0, 1001.0, 5e3, 1e5, 1e6]
+#: Models whose interactor reads the element component
+ELEMENT_MODELS = ("photoel-livermore", "conv-bethe-heitler", "brems-sb", "brems-rel",
+                  "brems-combined")
+
+
+def interaction_inputs(name: str) -> list:
+    """Inputs of an interaction case: (model, PDG, energy, position,
+    direction, element component), directions isotropic from a seeded
+    generator."""
+    import numpy as np
+
+    c = INTERACTION_CASES[name]
+    rng = np.random.default_rng(1000 + c["seed"])
+    if c.get("brem_combined"):
+        energies = {("brems-combined", pdg): COMBINED_ENERGIES for pdg in (11, -11)}
+    else:
+        energies = INTERACTION_ENERGIES
+    out = []
+    for pos, ncomp in c["points"]:
+        for (model, pdg), es in energies.items():
+            comps = range(ncomp) if model in ELEMENT_MODELS else [0]
+            for elcomp in comps:
+                for e in es:
+                    v = rng.normal(size=3)
+                    d = v / np.linalg.norm(v)
+                    out.append([model, pdg, e, list(pos), [float(x) for x in d], elcomp])
+    return out
+
+
+def make_interaction_case(name: str, libm: str = "system") -> dict:
+    c = INTERACTION_CASES[name]
+    inputs = interaction_inputs(name)
+    extra = ["--brem-combined"] if c.get("brem_combined") else []
+    with tempfile.TemporaryDirectory() as tmp:
+        txt = os.path.join(tmp, "inputs.txt")
+        oracle.write_interaction_inputs(txt, inputs)
+        results = oracle.run_interactions("reference", physics_file(c["geometry"]),
+                                          geometry_path(c["geometry"]), txt, c["seed"],
+                                          extra=extra, libm=libm)
+    case = {"geometry": c["geometry"], "seed": c["seed"],
+            "brem_combined": bool(c.get("brem_combined", False))}
+    return {"case": case, "inputs": inputs, "results": results}
+
 
 # Reseeded XORWOW states: seed, track slots, events, and the slots recorded
 RNG_SEED = 5
@@ -283,6 +362,7 @@ def main():
     parser.add_argument("--reference", default=oracle.reference_path())
     parser.add_argument("--cases", nargs="*", default=list(CASES))
     parser.add_argument("--hit-cases", nargs="*", default=list(HIT_CASES))
+    parser.add_argument("--interactions", nargs="*", default=list(INTERACTION_CASES))
     parser.add_argument("--libm", choices=oracle.LIBMS, default="system",
                         help="the reference linked with the host C library's elementary "
                              "functions (fixtures here) or with correctly rounded ones "
@@ -302,6 +382,11 @@ def main():
         with open(os.path.join(outdir, f"{name}.json"), "w") as f:
             json.dump(data, f, indent=0)
         print(name, data["num_hits"], "hits")
+    for name in args.interactions:
+        data = make_interaction_case(name, libm=args.libm)
+        with open(os.path.join(outdir, f"{name}.json"), "w") as f:
+            json.dump(data, f, indent=0)
+        print(name, len(data["results"]), "interactions")
     if args.libm != "system":
         return
     with open(os.path.join(HERE, "calo_geometry.json"), "w") as f:
