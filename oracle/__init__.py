@@ -193,11 +193,14 @@ def write_interaction_inputs(path: str, inputs) -> None:
 
 
 def parse_interact_output(text: str) -> list[dict]:
-    """Parse the 'int' and 'sec' lines of the 'interact' mode: per input, the
-    track after its interaction (status, step-limit action, material,
-    energy, direction, deposition, random state) and its secondaries (PDG,
-    energy, direction; PDG 0 for one killed by a cutoff)."""
+    """Parse the 'pre', 'int' and 'sec' lines of the 'interact' mode: per
+    input, the pre-step's results (step limit and its action, sampled MFP,
+    macroscopic and per-process cross sections, range), the track after its
+    interaction (status, step-limit action, material, energy, direction,
+    deposition, random state) and its secondaries (PDG, energy, direction;
+    PDG 0 for one killed by a cutoff)."""
     out: list[dict] = []
+    pre: dict[int, dict] = {}
 
     def vec(t):
         return [float(v) for v in t.strip("()").split(",")]
@@ -206,10 +209,17 @@ def parse_interact_output(text: str) -> list[dict]:
         tok = line.split()
         if not tok:
             continue
-        if tok[0] == "int":
+        if tok[0] == "pre":
+            kv = dict(t.split("=", 1) for t in tok[2:])
+            pre[int(tok[1])] = {"action": int(kv["act"]), "step": float(kv["len"]),
+                                "mfp": float(kv["mfp"]), "macro_xs": float(kv["macro"]),
+                                "range": float(kv["range"]),
+                                "xs": [float(v) for v in kv["xs"].split(",")]}
+        elif tok[0] == "int":
             kv = dict(t.split("=", 1) for t in tok[3:])
             assert int(tok[1]) == len(out)
-            out.append({"model": tok[2], "status": int(kv["st"]),
+            out.append({"model": tok[2], "pre_step": pre[int(tok[1])],
+                        "status": int(kv["st"]),
                         "action": int(kv["act"]), "material": int(kv["mat"]),
                         "energy": float(kv["E"]), "direction": vec(kv["dir"]),
                         "edep": float(kv["edep"]), "num_secondaries": int(kv["nsec"]),

@@ -511,6 +511,22 @@ int interact_inputs(int argc, char** argv)
     ParamsData const& p = stepper.params();
     StateData s = stepper.view();
     auto const& labels = stepper.action_labels();
+    // The pre-step's results per input: step limit and its action, sampled
+    // interaction MFP, macroscopic and per-process cross sections, range
+    for (size_type i = 0; i < n; ++i)
+    {
+        std::printf("pre %u act=%u len=%.17g mfp=%.17g macro=%.17g range=%.17g xs=",
+                    s.event_id[i],
+                    s.post_step_action[i],
+                    s.step_length[i],
+                    double(s.interaction_mfp[i]),
+                    double(s.macro_xs[i]),
+                    double(s.dedx_range[i]));
+        size_type const np = p.process_groups[s.particle_id[i]].num_processes;
+        for (size_type k = 0; k < np; ++k)
+            std::printf("%s%.17g", k ? "," : "", double(s.per_process_xs[k][i]));
+        std::printf("\n");
+    }
     std::vector<size_type> to_run;
     std::vector<size_type> slot_of(n);
     for (size_type i = 0; i < n; ++i)

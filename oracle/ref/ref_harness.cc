@@ -1196,6 +1196,27 @@ int interact(int argc, char** argv)
     auto const& reg = *core.action_reg();
     auto const& pref = core.ref<MemSpace::host>();
     auto const& sref = state.ref();
+    // The pre-step's results per input: step limit and its action, sampled
+    // interaction MFP, macroscopic and per-process cross sections, range
+    for (size_type i = 0; i < state.size(); ++i)
+    {
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        auto sim = track.make_sim_view();
+        auto phys = track.make_physics_view();
+        auto pstep = track.make_physics_step_view();
+        std::printf("pre %u act=%u len=%.17g mfp=%.17g macro=%.17g range=%.17g xs=",
+                    sim.event_id().unchecked_get(),
+                    sim.post_step_action().unchecked_get(),
+                    sim.step_length(),
+                    phys.interaction_mfp(),
+                    pstep.macro_xs(),
+                    phys.dedx_range());
+        for (auto ppid : range(ParticleProcessId{phys.num_particle_processes()}))
+        {
+            std::printf("%s%.17g", ppid.get() ? "," : "", pstep.per_process_xs(ppid));
+        }
+        std::printf("\n");
+    }
     std::vector<ActionId> to_run;
     for (size_type i = 0; i < state.size(); ++i)
     {

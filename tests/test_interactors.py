@@ -17,9 +17,11 @@ The CPU restatement runs the GB300 path's interactor code (the same source
 the device kernels compile) on the same inputs and the same random states.
 The bar for interactor outputs fed the same random state is 1e-12 relative;
 the FP64 code meets it bit for bit, which is what is asserted after the
-tolerance check: status, step-limit action, material, outgoing energy and
-direction, local deposition, every secondary (PDG, energy, direction) and
-the random state after the interaction.
+tolerance check: the pre-step's results (step limit and its action, sampled
+interaction MFP, macroscopic and per-process cross sections, range), then
+status, step-limit action, material, outgoing energy and direction, local
+deposition, every secondary (PDG, energy, direction) and the random state
+after the interaction.
 """
 
 import os
@@ -48,7 +50,9 @@ def run(golden, libm, tmp_path):
 
 def floats(r):
     """Every floating-point output of one interaction, flattened."""
-    out = [r["energy"], r["edep"], *r["direction"]]
+    pre = r["pre_step"]
+    out = [pre["step"], pre["mfp"], pre["macro_xs"], pre["range"], *pre["xs"]]
+    out += [r["energy"], r["edep"], *r["direction"]]
     for sec in r["secondaries"]:
         out += [sec["energy"], *sec["direction"]]
     return out
