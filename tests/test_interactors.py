@@ -106,3 +106,13 @@ def test_reference_conserves_energy():
             elif model == "annihil-2-gamma":
                 total -= 2 * electron_mass
             assert total == pytest.approx(e0, rel=1e-9, abs=1e-9), inp
+
+
+def test_check_detects_another_random_state(built_port, tmp_path):
+    """The comparison is sensitive: the same inputs with the random states of
+    another seed give other results for every sampled interaction."""
+    golden = load_golden("interact_calo", "pinned")
+    golden = dict(golden, case=dict(golden["case"], seed=golden["case"]["seed"] + 1))
+    got = run(golden, "pinned", tmp_path)
+    differ = [g != r for g, r in zip(got, golden["results"])]
+    assert all(differ)
