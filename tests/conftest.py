@@ -40,7 +40,8 @@ GOLDEN_CASES = ["calo_e1000_n4", "calo_e1000_n4_slots512", "calo_g100_n16",
                 "calo_initcharge_msc_field_e2000_n4", "calo_initcharge_g100_n16",
                 "cms_initcharge_mix_e5000_n4", "calo_shuffle_msc_e1000_n4",
                 "calo_status_g100_n16", "cms_particle_mix_e10000_n4",
-                "calo_e0.0005_n64", "calo_ep0.01_n64", "calo_g1.1_n64", "cms_lowe_mix_n64"]
+                "calo_e0.0005_n64", "calo_ep0.01_n64", "calo_g1.1_n64", "cms_lowe_mix_n64",
+                "cms_mix_e100000_n2"]
 
 
 def case_problem(case: dict) -> tuple[str, str]:

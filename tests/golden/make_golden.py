@@ -134,6 +134,10 @@ CASES = {
     "cms_lowe_mix_n64": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=0.001,
                              emax=10.0, num=64, slots=1024, seed=4, beam_seed=11,
                              msc=True, field=[0.0, 0.0, 3.8]),
+    # The top of the CMS-like beam's energy range (100 GeV)
+    "cms_mix_e100000_n2": dict(geometry="cms", beam="eta", pdgs=[11, 22], energy=1e5,
+                               num=2, slots=65536, seed=5, beam_seed=12, msc=True,
+                               field=[0.0, 0.0, 3.8]),
     # Stepper::reseed(event 7) before the first step
     "calo_reseed7_msc_e1000_n4": dict(pdg=11, energy=1000.0, num=4, slots=4096, seed=2,
                                       msc=True, reseed=7),
