@@ -233,21 +233,45 @@ def parse_interact_output(text: str) -> list[dict]:
     return out
 
 
+def parse_along_output(text: str) -> list[dict]:
+    """Parse the 'along' lines of the 'along' mode: per input, the track after
+    its along-step (status, step limit's action, step length, position,
+    direction, energy, local deposition, random state)."""
+    out: list[dict] = []
+
+    def vec(t):
+        return [float(v) for v in t.strip("()").split(",")]
+
+    for line in text.splitlines():
+        tok = line.split()
+        if tok and tok[0] == "along":
+            kv = dict(t.split("=", 1) for t in tok[2:])
+            assert int(tok[1]) == len(out)
+            out.append({"status": int(kv["st"]), "action": int(kv["act"]),
+                        "step": float(kv["len"]), "position": vec(kv["pos"]),
+                        "direction": vec(kv["dir"]), "energy": float(kv["E"]),
+                        "edep": float(kv["edep"]),
+                        "rng": [int(w) for w in kv["rng"].split(",")]})
+    return out
+
+
 def run_interactions(program: str, physics: str, geometry: str, inputs_txt: str,
-                     seed: int = 0, extra=(), libm: str = "pinned") -> list[dict]:
-    """One interaction per input through the reference's model actions
-    (program "reference", requires build_reference) or the restatement's
-    (program "port"), with the host C library's or correctly rounded
-    elementary functions."""
+                     seed: int = 0, extra=(), libm: str = "pinned",
+                     mode: str = "interact") -> list[dict]:
+    """One interaction ('interact') or one along-step ('along') per input,
+    through the reference's own actions (program "reference", requires
+    build_reference) or the restatement's (program "port"), with the host C
+    library's or correctly rounded elementary functions."""
     if program == "reference":
         exe = REF_BIN if libm == "system" else REF_PINNED_BIN
     else:
         exe = build_port(libm=libm)
-    cmd = [exe, "interact", physics, geometry, inputs_txt, str(seed), *extra]
+    cmd = [exe, mode, physics, geometry, inputs_txt, str(seed), *extra]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f"{program} interact failed: " + res.stderr[-2000:])
-    return parse_interact_output(res.stdout)
+        raise RuntimeError(f"{program} {mode} failed: " + res.stderr[-2000:])
+    parse = parse_interact_output if mode == "interact" else parse_along_output
+    return parse(res.stdout)
 
 
 def port_libm(function: str, x, libm: str = "pinned"):

@@ -20,7 +20,7 @@
 //                    [--steps N] [--quiet] [--hits]
 //   port_stepper bench <physics.txt> <geometry> <primaries.txt> <slots> <seed>
 //                    [--threads T] [--event-tallies FILE] [physics options]
-//   port_stepper interact <physics.txt> <geometry> <inputs.txt> <seed>
+//   port_stepper interact|along <physics.txt> <geometry> <inputs.txt> <seed>
 //                    [physics options]
 //   port_stepper libm <exp|log|sin|cos|tanh|log1p|expm1|cbrt> < hex doubles
 #include <algorithm>
@@ -584,6 +584,76 @@ int interact_inputs(int argc, char** argv)
     return 0;
 }
 
+//! One along-step per input, as the reference harness's 'along' mode: each
+//! input line (as for 'interact'; the label is not used) becomes a primary of
+//! its own event; extend-from-primaries, initialize-tracks, pre-step,
+//! step-gather-pre and the along-step actions run.
+int along_inputs(int argc, char** argv)
+{
+    if (argc < 6)
+    {
+        std::cerr << "usage: along <physics> <geometry> <inputs> <seed> "
+                     "[physics options]\n";
+        return 2;
+    }
+    std::string phys = argv[2], geo = argv[3], in_path = argv[4];
+    unsigned int seed = std::stoul(argv[5]);
+    HostParams hp = build_params(phys, make_geometry(geo), physics_options(argc, argv));
+
+    std::ifstream in(in_path);
+    if (!in)
+        throw std::runtime_error("cannot open " + in_path);
+    std::vector<TrackInitializer> primaries;
+    std::string label;
+    int pdg;
+    double e, x, y, z, dx, dy, dz;
+    size_type elcomp;
+    while (in >> label >> pdg >> e >> x >> y >> z >> dx >> dy >> dz >> elcomp)
+    {
+        TrackInitializer ti{};
+        ti.particle_id = pdg == 11 ? 0 : (pdg == -11 ? 1 : 2);
+        ti.energy = e;
+        ti.pos = {x, y, z};
+        ti.dir = {dx, dy, dz};
+        ti.time = 0;
+        ti.event_id = static_cast<size_type>(primaries.size());
+        primaries.push_back(ti);
+    }
+    if (primaries.empty())
+        throw std::runtime_error("no inputs in " + in_path);
+
+    size_type const n = static_cast<size_type>(primaries.size());
+    PortStepper stepper(hp, n, seed, n);
+    stepper.prepare(primaries);
+    ParamsData const& p = stepper.params();
+    StateData s = stepper.view();
+    for (size_type i = 0; i < n; ++i)
+        gather_pre(p, s, i);
+    for (size_type i = 0; i < n; ++i)
+        along_step(p, s, i);
+    std::vector<size_type> slot_of(n);
+    for (size_type i = 0; i < n; ++i)
+        slot_of[s.event_id[i]] = i;
+    for (size_type idx = 0; idx < n; ++idx)
+    {
+        size_type const i = slot_of[idx];
+        std::printf("along %u st=%d act=%u len=%.17g pos=(%.17g,%.17g,%.17g) "
+                    "dir=(%.17g,%.17g,%.17g) E=%.17g edep=%.17g "
+                    "rng=%u,%u,%u,%u,%u,%u\n",
+                    idx,
+                    int(s.status[i]),
+                    s.post_step_action[i],
+                    s.step_length[i],
+                    s.pos[0][i], s.pos[1][i], s.pos[2][i],
+                    s.dir[0][i], s.dir[1][i], s.dir[2][i],
+                    double(s.energy[i]),
+                    double(s.energy_deposition[i]),
+                    s.rng.s[0][i], s.rng.s[1][i], s.rng.s[2][i],
+                    s.rng.s[3][i], s.rng.s[4][i], s.rng.weyl[i]);
+    }
+    return 0;
+}
+
 int run(int argc, char** argv)
 {
     if (argc < 7)
@@ -923,6 +993,8 @@ int main(int argc, char** argv)
             return bench(argc, argv);
         if (mode == "interact")
             return interact_inputs(argc, argv);
+        if (mode == "along")
+            return along_inputs(argc, argv);
         if (mode == "geo-rays")
             return geo_rays(argc, argv);
         if (mode == "libm" && argc >= 3)

@@ -1285,6 +1285,116 @@ int interact(int argc, char** argv)
     return 0;
 }
 
+//! One along-step per input, through the reference's own actions: each input
+//! line (as for 'interact'; the label is not used) becomes a primary of its
+//! own event, and the step actions up to and including the along-step ones
+//! run (ActionSequence.cc:77-138). Prints per input the step limit's action,
+//! the step length, position, direction, energy, local deposition, status
+//! and random state after the along-step.
+int along(int argc, char** argv)
+{
+    if (argc < 6)
+    {
+        std::cerr << "usage: along <physics> <geometry> <inputs> <seed> "
+                     "[--field Bx By Bz] [--msc]\n";
+        return 2;
+    }
+    std::string phys_path = argv[2], geo_name = argv[3], in_path = argv[4];
+    unsigned int seed = std::stoul(argv[5]);
+    Real3 field{0, 0, 0};
+    bool msc = false;
+    for (int i = 6; i < argc; ++i)
+    {
+        std::string a = argv[i];
+        if (a == "--msc")
+            msc = true;
+        else if (a == "--field" && i + 3 < argc)
+        {
+            field = {std::strtod(argv[i + 1], nullptr),
+                     std::strtod(argv[i + 2], nullptr),
+                     std::strtod(argv[i + 3], nullptr)};
+            i += 3;
+        }
+    }
+    KvFile kv(phys_path);
+    ImportData imported = load_import(kv, msc);
+    Problem prob = build_problem(
+        imported, geo_name, seed, field, msc, TrackOrder::none, false, "", 1);
+    CoreParams const& core = *prob.core;
+    ParticleParams const& particles = *core.particle();
+
+    std::ifstream in(in_path);
+    CELER_VALIDATE(in, << "cannot open " << in_path);
+    std::vector<Primary> primaries;
+    std::string label;
+    int pdg;
+    double e, x, y, z, dx, dy, dz;
+    unsigned int elcomp;
+    while (in >> label >> pdg >> e >> x >> y >> z >> dx >> dy >> dz >> elcomp)
+    {
+        Primary p;
+        p.particle_id = particles.find(PDGNumber{pdg});
+        CELER_VALIDATE(p.particle_id, << "unknown PDG " << pdg);
+        p.energy = units::MevEnergy{e};
+        p.position = {x, y, z};
+        p.direction = {dx, dy, dz};
+        p.time = 0;
+        p.event_id = EventId{static_cast<size_type>(primaries.size())};
+        primaries.push_back(p);
+    }
+    CELER_VALIDATE(!primaries.empty(), << "no inputs in " << in_path);
+
+    StepperInput sinp;
+    sinp.params = prob.core;
+    sinp.stream_id = StreamId{0};
+    sinp.num_track_slots = static_cast<size_type>(primaries.size());
+    Stepper<MemSpace::host> step(std::move(sinp));
+    auto& state = dynamic_cast<CoreState<MemSpace::host>&>(*step.sp_state());
+    ExtendFromPrimariesAction::find_action(core)->insert(
+        core, state, make_span(primaries));
+    state.counters().num_generated = 0;
+    for (auto const& action : step.actions().actions().step())
+    {
+        if (action->order() > StepActionOrder::along)
+            break;
+        action->step(core, state);
+    }
+
+    auto const& pref = core.ref<MemSpace::host>();
+    auto const& sref = state.ref();
+    std::vector<size_type> slot_of(primaries.size());
+    for (size_type i = 0; i < state.size(); ++i)
+    {
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        slot_of[track.make_sim_view().event_id().unchecked_get()] = i;
+    }
+    for (size_type idx = 0; idx < slot_of.size(); ++idx)
+    {
+        size_type const i = slot_of[idx];
+        CoreTrackView track(pref, sref, TrackSlotId{i});
+        auto sim = track.make_sim_view();
+        auto par = track.make_particle_view();
+        auto geo = track.make_geo_view();
+        auto pstep = track.make_physics_step_view();
+        auto const& pos = geo.pos();
+        auto const& dir = geo.dir();
+        auto const& r = sref.rng.state[TrackSlotId{i}];
+        std::printf("along %u st=%d act=%u len=%.17g pos=(%.17g,%.17g,%.17g) "
+                    "dir=(%.17g,%.17g,%.17g) E=%.17g edep=%.17g "
+                    "rng=%u,%u,%u,%u,%u,%u\n",
+                    idx,
+                    static_cast<int>(sim.status()),
+                    sim.post_step_action().unchecked_get(),
+                    sim.step_length(),
+                    pos[0], pos[1], pos[2], dir[0], dir[1], dir[2],
+                    par.energy().value(),
+                    pstep.energy_deposition().value(),
+                    r.xorstate[0], r.xorstate[1], r.xorstate[2],
+                    r.xorstate[3], r.xorstate[4], r.weylstate);
+    }
+    return 0;
+}
+
 //! Timed CPU run of the reference's host stepper: events distributed over
 //! threads, one Stepper<host> per thread on its own stream, each event
 //! transported to completion (celer-sim with CELERITAS_OPENMP=event,
@@ -1500,6 +1610,8 @@ int main(int argc, char** argv)
             return bench(argc, argv);
         if (mode == "interact")
             return interact(argc, argv);
+        if (mode == "along")
+            return along(argc, argv);
     }
     catch (std::exception const& e)
     {

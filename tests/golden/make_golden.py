@@ -10,12 +10,14 @@ and column sums). Also records the ORANGE surface data of the calorimeter
 geometry and reseeded XORWOW states.
 
 Also records, per interaction case, one interaction per input through the
-reference's own model actions (the harness's 'interact' mode).
+reference's own model actions (the harness's 'interact' mode), and per
+along-step case one along-step per input (its 'along' mode).
 
 Usage (where the reference sources are present):
     python tests/golden/make_golden.py [--reference /path/to/reference]
     python tests/golden/make_golden.py --libm pinned   # fixtures under pinned/
     python tests/golden/make_golden.py --cases --hit-cases --interactions interact_cms
+    python tests/golden/make_golden.py --cases --hit-cases --interactions --along
 
 With --libm pinned the reference runs with correctly rounded exp, log, sin,
 cos, tanh, log1p, expm1 and cbrt (oracle/ref/pinned_libm.cc), the elementary
@@ -230,6 +232,62 @@ def make_interaction_case(name: str, libm: str = "system") -> dict:
     return {"case": case, "inputs": inputs, "results": results}
 
 
+# Along-step parity: one along-step per input through the reference's own
+# actions (the harness's 'along' mode) on tracks that its first actions
+# prepared: material points and points just inside boundaries, e-/e+ from 10
+# keV to 100 GeV and photons, isotropic directions
+ALONG_CASES = {
+    "along_cms_msc_field": dict(geometry="cms", seed=3, msc=True, field=[0.0, 0.0, 3.8],
+                                points=[(4.01, 0.0, 0.0), (50.0, 0.0, 0.0),
+                                        (129.0001, 0.0, 0.0), (140.0, 0.0, 0.0),
+                                        (151.9999, 0.0, 0.0), (182.0, 0.0, 0.0),
+                                        (185.2, 0.0, 0.0)]),
+    "along_calo_msc": dict(geometry="calo", seed=4, msc=True, field=[0.0, 0.0, 0.0],
+                           points=[(0.0, 0.0, 0.1), (0.0, 0.0, 0.2299), (0.0, 0.0, 0.5)]),
+    "along_calo_msc_field": dict(geometry="calo", seed=5, msc=True, field=[1.0, 0.0, 0.0],
+                                 points=[(0.0, 0.0, 0.1), (0.0, 0.0, 0.2299),
+                                         (0.0, 0.0, 0.5)]),
+}
+ALONG_ENERGIES = {11: [0.01, 0.1, 1.0, 10.0, 100.0, 1e3, 1e4, 1e5],
+                  -11: [0.01, 0.1, 1.0, 10.0, 100.0, 1e3, 1e4, 1e5],
+                  22: [0.1, 10.0, 1e4]}
+ALONG_DIRECTIONS = 2
+
+
+def along_inputs(name: str) -> list:
+    """Inputs of an along-step case (the interaction inputs' format, with
+    '-' for the model), directions isotropic from a seeded generator."""
+    import numpy as np
+
+    c = ALONG_CASES[name]
+    rng = np.random.default_rng(2000 + c["seed"])
+    out = []
+    for pos in c["points"]:
+        for pdg, es in ALONG_ENERGIES.items():
+            for e in es:
+                for _ in range(ALONG_DIRECTIONS):
+                    v = rng.normal(size=3)
+                    d = v / np.linalg.norm(v)
+                    out.append(["-", pdg, e, list(pos), [float(x) for x in d], 0])
+    return out
+
+
+def make_along_case(name: str, libm: str = "system") -> dict:
+    c = ALONG_CASES[name]
+    inputs = along_inputs(name)
+    extra = (["--msc"] if c["msc"] else []) + (
+        ["--field"] + [repr(float(f)) for f in c["field"]] if any(c["field"]) else [])
+    with tempfile.TemporaryDirectory() as tmp:
+        txt = os.path.join(tmp, "inputs.txt")
+        oracle.write_interaction_inputs(txt, inputs)
+        results = oracle.run_interactions("reference", physics_file(c["geometry"]),
+                                          geometry_path(c["geometry"]), txt, c["seed"],
+                                          extra=extra, libm=libm, mode="along")
+    case = {"geometry": c["geometry"], "seed": c["seed"], "msc": c["msc"],
+            "field": list(c["field"])}
+    return {"case": case, "inputs": inputs, "results": results}
+
+
 # Reseeded XORWOW states: seed, track slots, events, and the slots recorded
 RNG_SEED = 5
 RNG_SLOTS = 4096
@@ -367,6 +425,7 @@ def main():
     parser.add_argument("--cases", nargs="*", default=list(CASES))
     parser.add_argument("--hit-cases", nargs="*", default=list(HIT_CASES))
     parser.add_argument("--interactions", nargs="*", default=list(INTERACTION_CASES))
+    parser.add_argument("--along", nargs="*", default=list(ALONG_CASES))
     parser.add_argument("--libm", choices=oracle.LIBMS, default="system",
                         help="the reference linked with the host C library's elementary "
                              "functions (fixtures here) or with correctly rounded ones "
@@ -391,6 +450,11 @@ def main():
         with open(os.path.join(outdir, f"{name}.json"), "w") as f:
             json.dump(data, f, indent=0)
         print(name, len(data["results"]), "interactions")
+    for name in args.along:
+        data = make_along_case(name, libm=args.libm)
+        with open(os.path.join(outdir, f"{name}.json"), "w") as f:
+            json.dump(data, f, indent=0)
+        print(name, len(data["results"]), "along-steps")
     if args.libm != "system":
         return
     with open(os.path.join(HERE, "calo_geometry.json"), "w") as f:

@@ -1,0 +1,64 @@
+"""Along-step parity against the reference (CPU, no GPU).
+
+The fixtures hold, per input, the track after one along-step computed by the
+reference's own actions (the harness's 'along' mode,
+tests/golden/make_golden.py): each input (particle, energy, position,
+direction) is a primary of its own event, and the reference runs
+extend-from-primaries, initialize-tracks, pre-step, step-gather-pre and the
+along-step action (Urban multiple scattering, uniform-field Runge-Kutta
+propagation with boundary search, energy loss with fluctuations). The inputs
+place e-/e+ of 10 keV to 100 GeV and photons in every material of the
+calorimeter and of the CMS-like detector (3.8 T), at points just inside
+boundaries too, with isotropic directions; the steps end on every kind of
+limit (range, multiple scattering, boundary, discrete interaction,
+propagation limit in the field).
+
+The CPU restatement runs the GB300 path's along-step code (the source the
+device kernels compile) on the same inputs and must give, bit for bit, the
+step limit's action, step length, position, direction, energy, local
+deposition, status and random state.
+"""
+
+import os
+
+import pytest
+
+from conftest import load_golden
+
+import oracle
+from celeritas_gb300 import geometry_path, physics_file
+
+CASES = ["along_cms_msc_field", "along_calo_msc", "along_calo_msc_field"]
+
+
+def run(golden, libm, tmp_path):
+    c = golden["case"]
+    txt = os.path.join(tmp_path, "inputs.txt")
+    oracle.write_interaction_inputs(txt, golden["inputs"])
+    extra = (["--msc"] if c["msc"] else []) + (
+        ["--field"] + [repr(float(f)) for f in c["field"]] if any(c["field"]) else [])
+    return oracle.run_interactions("port", physics_file(c["geometry"]),
+                                   geometry_path(c["geometry"]), txt, c["seed"],
+                                   extra=extra, libm=libm, mode="along")
+
+
+@pytest.mark.parametrize("libm", oracle.LIBMS)
+@pytest.mark.parametrize("name", CASES)
+def test_along_step_matches_reference(built_port, name, libm, tmp_path):
+    golden = load_golden(name, libm)
+    got = run(golden, libm, tmp_path)
+    assert len(got) == len(golden["results"])
+    for inp, g, r in zip(golden["inputs"], got, golden["results"]):
+        assert g == r, f"pdg {inp[1]} E {inp[2]} MeV at {inp[3]} along {inp[4]}"
+
+
+def test_steps_end_on_every_kind_of_limit():
+    """The inputs exercise every step limit of the along-step."""
+    actions = set()
+    for name in CASES:
+        golden = load_golden(name, "pinned")
+        ref_actions = load_golden("cms_mix_e10000_n4" if "cms" in name
+                                  else "calo_msc_field_e5000_n2", "pinned")["actions"]
+        actions |= {ref_actions[r["action"]] for r in golden["results"]}
+    assert {"eloss-range", "msc-range", "geo-boundary", "physics-discrete-select",
+            "geo-propagation-limit"} <= actions
