@@ -235,8 +235,9 @@ def parse_interact_output(text: str) -> list[dict]:
 
 def parse_along_output(text: str) -> list[dict]:
     """Parse the 'along' lines of the 'along' mode: per input, the track after
-    its along-step (status, step limit's action, step length, position,
-    direction, energy, local deposition, random state)."""
+    its along-step and discrete selection (status, step limit's action, the
+    action after selection and the element component it chose or -1, step
+    length, position, direction, energy, local deposition, random state)."""
     out: list[dict] = []
 
     def vec(t):
@@ -248,6 +249,7 @@ def parse_along_output(text: str) -> list[dict]:
             kv = dict(t.split("=", 1) for t in tok[2:])
             assert int(tok[1]) == len(out)
             out.append({"status": int(kv["st"]), "action": int(kv["act"]),
+                        "selected": int(kv["sel"]), "element": int(kv["el"]),
                         "step": float(kv["len"]), "position": vec(kv["pos"]),
                         "direction": vec(kv["dir"]), "energy": float(kv["E"]),
                         "edep": float(kv["edep"]),

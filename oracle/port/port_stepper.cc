@@ -587,7 +587,7 @@ int interact_inputs(int argc, char** argv)
 //! One along-step per input, as the reference harness's 'along' mode: each
 //! input line (as for 'interact'; the label is not used) becomes a primary of
 //! its own event; extend-from-primaries, initialize-tracks, pre-step,
-//! step-gather-pre and the along-step actions run.
+//! step-gather-pre, the along-step actions and physics-discrete-select run.
 int along_inputs(int argc, char** argv)
 {
     if (argc < 6)
@@ -631,18 +631,32 @@ int along_inputs(int argc, char** argv)
         gather_pre(p, s, i);
     for (size_type i = 0; i < n; ++i)
         along_step(p, s, i);
+    std::vector<size_type> along_action(s.post_step_action, s.post_step_action + n);
+    for (size_type i = 0; i < n; ++i)
+        discrete_select(p, s, i);
+    auto const& labels = stepper.action_labels();
+    size_type const rejected = static_cast<size_type>(
+        std::find(labels.begin(), labels.end(), "physics-integral-rejected")
+        - labels.begin());
     std::vector<size_type> slot_of(n);
     for (size_type i = 0; i < n; ++i)
         slot_of[s.event_id[i]] = i;
     for (size_type idx = 0; idx < n; ++idx)
     {
         size_type const i = slot_of[idx];
-        std::printf("along %u st=%d act=%u len=%.17g pos=(%.17g,%.17g,%.17g) "
+        size_type const sel = s.post_step_action[i];
+        int const el = (sel != along_action[i] && sel != rejected)
+                           ? static_cast<int>(s.element[i])
+                           : -1;
+        std::printf("along %u st=%d act=%u sel=%u el=%d len=%.17g "
+                    "pos=(%.17g,%.17g,%.17g) "
                     "dir=(%.17g,%.17g,%.17g) E=%.17g edep=%.17g "
                     "rng=%u,%u,%u,%u,%u,%u\n",
                     idx,
                     int(s.status[i]),
-                    s.post_step_action[i],
+                    along_action[i],
+                    sel,
+                    el,
                     s.step_length[i],
                     s.pos[0][i], s.pos[1][i], s.pos[2][i],
                     s.dir[0][i], s.dir[1][i], s.dir[2][i],

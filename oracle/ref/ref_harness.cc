@@ -1288,9 +1288,10 @@ int interact(int argc, char** argv)
 //! One along-step per input, through the reference's own actions: each input
 //! line (as for 'interact'; the label is not used) becomes a primary of its
 //! own event, and the step actions up to and including the along-step ones
-//! run (ActionSequence.cc:77-138). Prints per input the step limit's action,
-//! the step length, position, direction, energy, local deposition, status
-//! and random state after the along-step.
+//! run (ActionSequence.cc:77-138), then physics-discrete-select. Prints per
+//! input the step limit's action, the action after discrete selection and
+//! the element component it chose, the step length, position, direction,
+//! energy, local deposition, status and random state.
 int along(int argc, char** argv)
 {
     if (argc < 6)
@@ -1353,15 +1354,29 @@ int along(int argc, char** argv)
     ExtendFromPrimariesAction::find_action(core)->insert(
         core, state, make_span(primaries));
     state.counters().num_generated = 0;
-    for (auto const& action : step.actions().actions().step())
-    {
-        if (action->order() > StepActionOrder::along)
-            break;
-        action->step(core, state);
-    }
-
     auto const& pref = core.ref<MemSpace::host>();
     auto const& sref = state.ref();
+    std::vector<ActionId> along_action(state.size());
+    bool selected = false;
+    for (auto const& action : step.actions().actions().step())
+    {
+        if (action->order() > StepActionOrder::pre_post)
+            break;
+        if (action->order() > StepActionOrder::along && !selected)
+        {
+            // Step limits of the along-step, before discrete selection
+            for (size_type i = 0; i < state.size(); ++i)
+            {
+                CoreTrackView track(pref, sref, TrackSlotId{i});
+                along_action[i] = track.make_sim_view().post_step_action();
+            }
+            selected = true;
+        }
+        action->step(core, state);
+    }
+    ActionId const rejected
+        = core.action_reg()->find_action("physics-integral-rejected");
+
     std::vector<size_type> slot_of(primaries.size());
     for (size_type i = 0; i < state.size(); ++i)
     {
@@ -1379,12 +1394,20 @@ int along(int argc, char** argv)
         auto const& pos = geo.pos();
         auto const& dir = geo.dir();
         auto const& r = sref.rng.state[TrackSlotId{i}];
-        std::printf("along %u st=%d act=%u len=%.17g pos=(%.17g,%.17g,%.17g) "
+        // A discrete interaction was selected: its element component
+        ActionId const sel = sim.post_step_action();
+        int const el = (sel != along_action[i] && sel != rejected)
+                           ? static_cast<int>(pstep.element().unchecked_get())
+                           : -1;
+        std::printf("along %u st=%d act=%u sel=%u el=%d len=%.17g "
+                    "pos=(%.17g,%.17g,%.17g) "
                     "dir=(%.17g,%.17g,%.17g) E=%.17g edep=%.17g "
                     "rng=%u,%u,%u,%u,%u,%u\n",
                     idx,
                     static_cast<int>(sim.status()),
-                    sim.post_step_action().unchecked_get(),
+                    along_action[i].unchecked_get(),
+                    sel.unchecked_get(),
+                    el,
                     sim.step_length(),
                     pos[0], pos[1], pos[2], dir[0], dir[1], dir[2],
                     par.energy().value(),

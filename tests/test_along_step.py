@@ -13,10 +13,15 @@ boundaries too, with isotropic directions; the steps end on every kind of
 limit (range, multiple scattering, boundary, discrete interaction,
 propagation limit in the field).
 
-The CPU restatement runs the GB300 path's along-step code (the source the
-device kernels compile) on the same inputs and must give, bit for bit, the
-step limit's action, step length, position, direction, energy, local
-deposition, status and random state.
+After the along-step the reference runs physics-discrete-select, which for
+steps ended by the discrete-interaction limit samples the process, applies
+the integral-approach rejection and selects the model and element component.
+
+The CPU restatement runs the GB300 path's along-step and selection code (the
+source the device kernels compile) on the same inputs and must give, bit
+for bit, the step limit's action, the selected action and element, step
+length, position, direction, energy, local deposition, status and random
+state.
 """
 
 import os
