@@ -58,12 +58,19 @@ def test_along_step_matches_reference(built_port, name, libm, tmp_path):
 
 
 def test_steps_end_on_every_kind_of_limit():
-    """The inputs exercise every step limit of the along-step."""
+    """The inputs exercise every step limit of the along-step, and discrete
+    selection picks every model and the integral-approach rejection."""
     actions = set()
+    selected = set()
     for name in CASES:
         golden = load_golden(name, "pinned")
         ref_actions = load_golden("cms_mix_e10000_n4" if "cms" in name
                                   else "calo_msc_field_e5000_n2", "pinned")["actions"]
         actions |= {ref_actions[r["action"]] for r in golden["results"]}
+        selected |= {ref_actions[r["selected"]] for r in golden["results"]
+                     if ref_actions[r["action"]] == "physics-discrete-select"}
     assert {"eloss-range", "msc-range", "geo-boundary", "physics-discrete-select",
             "geo-propagation-limit"} <= actions
+    assert selected == {"physics-integral-rejected", "ioni-moller-bhabha", "brems-sb",
+                        "brems-rel", "photoel-livermore", "scat-klein-nishina",
+                        "conv-bethe-heitler", "annihil-2-gamma"}
