@@ -76,21 +76,3 @@ def launch_bytes(label: str, processed: int, slots: int, real_bytes: int = 8) ->
     """Algorithmic bytes for one launch of an action over 'slots' slots."""
     b_proc, b_idle = bytes_per_slot(label, real_bytes)
     return processed * b_proc + (slots - processed) * b_idle
-
-
-# Persistent per-slot state of this build's layout (bytes), for the
-# per-track-step figure: read once + written once per step
-def state_bytes_per_slot(real_bytes: int = 8) -> int:
-    fixed = (1 + 4 * 4 + 8 * 2 + 4 * 2      # sim: status, ids, steps, time, step, actions
-             + 4                          # particle ID
-             + 8 * 6 + 4 * 2 + 1 * 3 + 8 + 4 + 1  # geometry
-             + 4                          # material
-             + 4 * 3                      # secondary span, element
-             + 1 + 4                      # MSC displaced flag, looping counter
-             + 24                         # rng
-             + 4 * 5 + 1)                 # vacancy, counts, parents, detector, slot index, scratch
-    reals = 1 + 3 + 4 + 1 + 6             # energy; MFP, range, macro XS; 4 XS; deposition; MSC
-    return fixed + reals * real_bytes
-
-
-B_STEP = 2 * state_bytes_per_slot(8)
