@@ -74,3 +74,35 @@ def test_steps_end_on_every_kind_of_limit():
     assert selected == {"physics-integral-rejected", "ioni-moller-bhabha", "brems-sb",
                         "brems-rel", "photoel-livermore", "scat-klein-nishina",
                         "conv-bethe-heitler", "annihil-2-gamma"}
+
+
+@pytest.mark.skipif(not (os.path.exists(oracle.REF_BIN) and os.path.exists(oracle.REF_PINNED_BIN)),
+                    reason="the compiled reference is not present")
+@pytest.mark.parametrize("libm", oracle.LIBMS)
+def test_random_inputs_against_live_reference(built_port, libm, tmp_path):
+    """Fresh inputs beyond the fixtures: 500 along-steps (and discrete
+    selections) of e-, e+ and photons, log-uniform 1 keV-100 GeV, at random
+    points of the CMS-like detector (radius 0-300 cm, |z| < 320 cm) in 3.8 T
+    with MSC, through the compiled reference and the restatement."""
+    import numpy as np
+
+    rng = np.random.default_rng(13579)
+    inputs = []
+    for _ in range(500):
+        pdg = int(rng.choice([11, -11, 22]))
+        e = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e5))))
+        r = float(rng.uniform(0.0, 300.0))
+        phi = float(rng.uniform(0.0, 2 * np.pi))
+        pos = [r * float(np.cos(phi)), r * float(np.sin(phi)), float(rng.uniform(-320, 320))]
+        v = rng.normal(size=3)
+        d = [float(x) for x in v / np.linalg.norm(v)]
+        inputs.append(["-", pdg, e, pos, d, 0])
+    txt = os.path.join(tmp_path, "inputs.txt")
+    oracle.write_interaction_inputs(txt, inputs)
+    args = (physics_file("cms"), geometry_path("cms"), txt, 88)
+    extra = ["--msc", "--field", "0.0", "0.0", "3.8"]
+    ref = oracle.run_interactions("reference", *args, extra=extra, libm=libm, mode="along")
+    got = oracle.run_interactions("port", *args, extra=extra, libm=libm, mode="along")
+    assert len(got) == len(ref) == len(inputs)
+    for inp, g, r in zip(inputs, got, ref):
+        assert g == r, inp

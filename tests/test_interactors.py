@@ -116,3 +116,41 @@ def test_check_detects_another_random_state(built_port, tmp_path):
     got = run(golden, "pinned", tmp_path)
     differ = [g != r for g, r in zip(got, golden["results"])]
     assert all(differ)
+
+
+@pytest.mark.skipif(not (os.path.exists(oracle.REF_BIN) and os.path.exists(oracle.REF_PINNED_BIN)),
+                    reason="the compiled reference is not present")
+@pytest.mark.parametrize("libm", oracle.LIBMS)
+def test_random_inputs_against_live_reference(built_port, libm, tmp_path):
+    """Fresh inputs beyond the fixtures: 600 interactions drawn at random
+    (model, log-uniform energy inside the model's range, CMS-like material
+    point, element component, direction), through the compiled reference
+    and the restatement."""
+    rng = np.random.default_rng(24680)
+    points = [((4.01, 0.0, 0.0), 1), ((140.0, 0.0, 0.0), 3), ((182.0, 0.0, 0.0), 2),
+              ((185.2, 0.0, 0.0), 2)]
+    models = [("scat-klein-nishina", 22, 1e-3, 1e6, False),
+              ("photoel-livermore", 22, 1e-3, 10.0, False),
+              ("conv-bethe-heitler", 22, 1.05, 1e5, True),
+              ("brems-sb", 11, 0.1, 1000.0, True), ("brems-sb", -11, 0.1, 1000.0, True),
+              ("brems-rel", 11, 1000.0, 1e6, True), ("brems-rel", -11, 1000.0, 1e6, True),
+              ("ioni-moller-bhabha", 11, 3.0, 1e5, False),
+              ("ioni-moller-bhabha", -11, 3.0, 1e5, False),
+              ("annihil-2-gamma", -11, 1e-3, 1e5, False)]
+    inputs = []
+    for _ in range(600):
+        model, pdg, lo, hi, by_element = models[rng.integers(len(models))]
+        pos, ncomp = points[rng.integers(len(points))]
+        e = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        v = rng.normal(size=3)
+        d = [float(x) for x in v / np.linalg.norm(v)]
+        elcomp = int(rng.integers(ncomp)) if by_element else 0
+        inputs.append([model, pdg, e, list(pos), d, elcomp])
+    txt = os.path.join(tmp_path, "inputs.txt")
+    oracle.write_interaction_inputs(txt, inputs)
+    args = (physics_file("cms"), geometry_path("cms"), txt, 77)
+    ref = oracle.run_interactions("reference", *args, libm=libm)
+    got = oracle.run_interactions("port", *args, libm=libm)
+    assert len(got) == len(ref) == len(inputs)
+    for inp, g, r in zip(inputs, got, ref):
+        assert g == r, inp
