@@ -227,3 +227,43 @@ def test_combined_brems_rejects_compound_materials(built_port):
                              capture_output=True, text=True)
     assert res.returncode != 0
     assert "more than one element" in res.stderr
+
+
+@pytest.mark.skipif(not (os.path.exists(oracle.REF_BIN) and os.path.exists(oracle.REF_PINNED_BIN)),
+                    reason="the compiled reference is not present")
+@pytest.mark.parametrize("draw", range(4))
+def test_random_transports_against_live_reference(built_port, draw):
+    """Fresh problems beyond the fixtures, drawn at random: geometry, track
+    order, seed, slots, and the beam (CMS-like e-/e+/gamma mixtures in 3.8 T
+    with MSC, or a calorimeter pencil beam with MSC and a 1 T field or
+    none), transported by the compiled reference and the restatement, per
+    step and per volume, with both libm variants."""
+    from celeritas_gb300.primaries import eta_beam, pencil_beam
+
+    rng = np.random.default_rng(97531 + draw)
+    order = int(rng.integers(8))
+    seed = int(rng.integers(1 << 20))
+    slots = int(rng.choice([256, 1024, 4096]))
+    energy = float(np.exp(rng.uniform(np.log(1.0), np.log(3000.0))))
+    if draw % 2 == 0:
+        geometry = "cms"
+        pdgs = tuple(int(p) for p in rng.permutation([11, -11, 22]))
+        prim = eta_beam(3, emin=energy, emax=2 * energy, pdgs=pdgs,
+                        seed=int(rng.integers(1000)))
+        extra = ["--msc", "--field", "0.0", "0.0", "3.8"]
+    else:
+        geometry = "calo"
+        prim = pencil_beam(3, energy=energy, pdg=int(rng.choice([11, -11, 22])))
+        extra = ["--msc"] + (["--field", "1.0", "0.0", "0.0"] if draw % 4 == 1 else [])
+    extra += ["--track-order", str(order)]
+    with tempfile.TemporaryDirectory() as tmp:
+        ptxt = os.path.join(tmp, "p.txt")
+        write_primaries_text(ptxt, prim)
+        for libm in oracle.LIBMS:
+            ref = oracle.run_reference(physics_file(geometry), ptxt, slots, seed,
+                                       geometry=geometry, extra=extra, libm=libm)
+            got = oracle.run_port(physics_file(geometry), ptxt, slots, seed,
+                                  geometry=geometry, extra=extra, libm=libm)
+            assert got["steps"] == ref["steps"], (libm, order, seed, energy)
+            assert got["total_steps"] == ref["total_steps"]
+            assert got["edep"] == ref["edep"]
