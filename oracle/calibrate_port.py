@@ -6,7 +6,9 @@ repository's per-slot action code compiled for the host) on the same event
 subsets of the c2 and c3 workloads, one stepper per thread over all the
 machine's cores, and writes the ratio of their track-step rates to
 ``oracle/port_over_reference.json``. Both run the reference's algorithm
-(no reentrant-looping option), FP64, with 4096 slots per thread stepper.
+(no reentrant-looping option), FP64, with 4096 slots per thread stepper,
+and the host C library's elementary functions (the restatement built as
+``bench.py`` times it).
 
 The reference sources exist only where this is run (not on the GPU host),
 so the ratio is measured here and committed; ``bench.py`` reports it beside
@@ -57,7 +59,8 @@ def time_both(name: str, num_events: int, threads: int, slots: int = 4096) -> di
     with tempfile.TemporaryDirectory() as tmp:
         ptxt = os.path.join(tmp, "p.txt")
         write_primaries_text(ptxt, prim)
-        for kind, exe in (("reference", oracle.REF_BIN), ("port", oracle.build_port())):
+        for kind, exe in (("reference", oracle.REF_BIN),
+                          ("port", oracle.build_port(libm="system"))):
             cmd = [exe, "bench", physics_file(wl["physics"]), wl["geometry"], ptxt,
                    str(slots), str(wl["seed"]), "--threads", str(threads)] + args
             res = subprocess.run(cmd, capture_output=True, text=True, check=True)
