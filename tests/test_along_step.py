@@ -106,3 +106,33 @@ def test_random_inputs_against_live_reference(built_port, libm, tmp_path):
     assert len(got) == len(ref) == len(inputs)
     for inp, g, r in zip(inputs, got, ref):
         assert g == r, inp
+
+
+@pytest.mark.skipif(not (os.path.exists(oracle.REF_BIN) and os.path.exists(oracle.REF_PINNED_BIN)),
+                    reason="the compiled reference is not present")
+@pytest.mark.parametrize("libm", oracle.LIBMS)
+def test_random_calorimeter_inputs_against_live_reference(built_port, libm, tmp_path):
+    """Fresh inputs in the calorimeter (1 T along x, MSC): 400 along-steps of
+    e-, e+ and photons, log-uniform 1 keV-10 GeV, at random depths in the
+    first 20 layers and random transverse points, random directions."""
+    import numpy as np
+
+    rng = np.random.default_rng(86420)
+    inputs = []
+    for _ in range(400):
+        pdg = int(rng.choice([11, -11, 22]))
+        e = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e4))))
+        pos = [float(rng.uniform(-19, 19)), float(rng.uniform(-19, 19)),
+               float(rng.uniform(0.0, 16.0))]
+        v = rng.normal(size=3)
+        d = [float(x) for x in v / np.linalg.norm(v)]
+        inputs.append(["-", pdg, e, pos, d, 0])
+    txt = os.path.join(tmp_path, "inputs.txt")
+    oracle.write_interaction_inputs(txt, inputs)
+    args = (physics_file("calo"), geometry_path("calo"), txt, 99)
+    extra = ["--msc", "--field", "1.0", "0.0", "0.0"]
+    ref = oracle.run_interactions("reference", *args, extra=extra, libm=libm, mode="along")
+    got = oracle.run_interactions("port", *args, extra=extra, libm=libm, mode="along")
+    assert len(got) == len(ref) == len(inputs)
+    for inp, g, r in zip(inputs, got, ref):
+        assert g == r, inp

@@ -154,3 +154,29 @@ def test_random_inputs_against_live_reference(built_port, libm, tmp_path):
     assert len(got) == len(ref) == len(inputs)
     for inp, g, r in zip(inputs, got, ref):
         assert g == r, inp
+
+
+@pytest.mark.skipif(not (os.path.exists(oracle.REF_BIN) and os.path.exists(oracle.REF_PINNED_BIN)),
+                    reason="the compiled reference is not present")
+@pytest.mark.parametrize("libm", oracle.LIBMS)
+def test_random_combined_brems_against_live_reference(built_port, libm, tmp_path):
+    """Fresh inputs for the combined bremsstrahlung model: 300 e-/e+ of
+    log-uniform 50 keV-1 TeV (both sides of its 1 GeV switch) in Pb and lAr,
+    random directions."""
+    rng = np.random.default_rng(11235)
+    inputs = []
+    for _ in range(300):
+        pdg = int(rng.choice([11, -11]))
+        e = float(np.exp(rng.uniform(np.log(0.05), np.log(1e6))))
+        pos = [(0.0, 0.0, 0.1), (0.0, 0.0, 0.5)][int(rng.integers(2))]
+        v = rng.normal(size=3)
+        d = [float(x) for x in v / np.linalg.norm(v)]
+        inputs.append(["brems-combined", pdg, e, list(pos), d, 0])
+    txt = os.path.join(tmp_path, "inputs.txt")
+    oracle.write_interaction_inputs(txt, inputs)
+    args = (physics_file("calo"), geometry_path("calo"), txt, 55)
+    ref = oracle.run_interactions("reference", *args, extra=["--brem-combined"], libm=libm)
+    got = oracle.run_interactions("port", *args, extra=["--brem-combined"], libm=libm)
+    assert len(got) == len(ref) == len(inputs)
+    for inp, g, r in zip(inputs, got, ref):
+        assert g == r, inp
